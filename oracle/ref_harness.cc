@@ -1,0 +1,213 @@
+// ref_harness.cc -- C entry points over the reference's own classes.
+//
+// TEST INFRASTRUCTURE ONLY.  Compiled (by oracle/Makefile) together with the
+// reference's unmodified sources read in place from the reference checkout;
+// the output goes to oracle/_ref/ and is never committed.  It drives the
+// reference exactly the way its unit tests do (cc_code/src/hmm/hmm/
+// peptide-hmm.test.cc:154-188) and the way its CLI does
+// (cc_code/src/main/run-classify-hmm.cc:38-98, run-fit.cc:37-137), so that
+// the CPU oracle (wp_oracle.c) and the CUDA path can be compared with the
+// reference itself on the same inputs.
+#include <omp.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "classifiers/hmm-classifier.h"
+#include "common/dye-seq.h"
+#include "common/radiometry.h"
+#include "common/scored-classification.h"
+#include "common/sourced-data.h"
+#include "fitters/hmm-fitter.h"
+#include "hmm/hmm/peptide-hmm.h"
+#include "hmm/precomputations/dye-seq-precomputations.h"
+#include "hmm/precomputations/radiometry-precomputations.h"
+#include "hmm/precomputations/universal-precomputations.h"
+#include "parameterization/fit/sequencing-model-fitter.h"
+#include "parameterization/model/sequencing-model.h"
+#include "parameterization/settings/fit-settings.h"
+#include "parameterization/settings/sequencing-settings.h"
+#include "wp_oracle.h"
+
+using namespace whatprot;
+
+namespace {
+
+void to_reference(const wpo_model* m, SequencingModel* sm) {
+    sm->p_edman_failure = m->p_edman_failure;
+    sm->p_detach.base = m->p_detach;
+    sm->p_detach.initial = m->p_initial_detach;
+    sm->p_detach.initial_decay = m->p_initial_detach_decay;
+    sm->p_initial_block = m->p_initial_block;
+    sm->p_cyclic_block = m->p_cyclic_block;
+    int C = m->num_channels;
+    for (int c = 0; c < C; c++) {
+        ChannelModel* cm = new ChannelModel(c, C);
+        cm->p_bleach = m->p_bleach[c];
+        cm->p_dud = m->p_dud[c];
+        cm->bg_sig = m->bg_sig[c];
+        cm->mu = m->mu[c];
+        cm->sig = m->sig[c];
+        for (int o = 0; o < C; o++) {
+            cm->interactions[o] = m->interactions[c][o];
+            cm->flat_interactions[o] = m->flat_interactions[c][o];
+        }
+        sm->channel_models.push_back(cm);
+    }
+}
+
+void from_reference(const SequencingModel& sm, int C, wpo_model* m) {
+    m->num_channels = C;
+    m->p_edman_failure = sm.p_edman_failure;
+    m->p_detach = sm.p_detach.base;
+    m->p_initial_detach = sm.p_detach.initial;
+    m->p_initial_detach_decay = sm.p_detach.initial_decay;
+    m->p_initial_block = sm.p_initial_block;
+    m->p_cyclic_block = sm.p_cyclic_block;
+    for (int c = 0; c < C; c++) {
+        m->p_bleach[c] = sm.channel_models[c]->p_bleach;
+        m->p_dud[c] = sm.channel_models[c]->p_dud;
+        m->bg_sig[c] = sm.channel_models[c]->bg_sig;
+        m->mu[c] = sm.channel_models[c]->mu;
+        m->sig[c] = sm.channel_models[c]->sig;
+    }
+}
+
+Radiometry make_radiometry(int T, int C, const double* rad) {
+    Radiometry r(T, C);
+    for (int t = 0; t < T; t++)
+        for (int c = 0; c < C; c++) r(t, c) = rad[t * C + c];
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+// PeptideHMM(...).probability() for one pair, built as in
+// peptide-hmm.test.cc:154-188.
+double ref_peptide_probability(const wpo_model* m, int T, const char* dye_seq,
+                               const double* rad, unsigned max_num_dyes,
+                               double dist_cutoff) {
+    int C = m->num_channels;
+    SequencingModel sm;
+    to_reference(m, &sm);
+    SequencingSettings ss;
+    ss.dist_cutoff = dist_cutoff;
+    UniversalPrecomputations up(sm, T, C);
+    up.set_max_num_dyes(max_num_dyes);
+    DyeSeq ds(C, std::string(dye_seq));
+    DyeSeqPrecomputations dsp(ds, sm, T, C);
+    Radiometry r = make_radiometry(T, C, rad);
+    RadiometryPrecomputations rp(r, sm, ss, max_num_dyes);
+    PeptideHMM hmm(T, C, dsp, rp, up);
+    return hmm.probability();
+}
+
+// HMMClassifier::classify(vector<Radiometry>) (hmm-classifier.cc:84-93),
+// OpenMP-parallel over reads exactly as the CLI runs it.  *seconds receives
+// the wall time of the classify call alone (run-classify-hmm.cc:85-88).
+void ref_classify(const wpo_model* m, int T, int P, const char* const* seqs,
+                  const int* ids, const int* counts, int R, const double* rads,
+                  double dist_cutoff, int threads, int* out_id,
+                  double* out_score, double* out_total, double* seconds) {
+    int C = m->num_channels;
+    SequencingModel sm;
+    to_reference(m, &sm);
+    SequencingSettings ss;
+    ss.dist_cutoff = dist_cutoff;
+    std::vector<SourcedData<DyeSeq, SourceCount<int>>> dye_seqs;
+    dye_seqs.reserve(P);
+    for (int i = 0; i < P; i++)
+        dye_seqs.push_back(SourcedData<DyeSeq, SourceCount<int>>(
+                DyeSeq(C, std::string(seqs[i])), SourceCount<int>(ids[i], counts[i])));
+    std::vector<Radiometry> radiometries;
+    radiometries.reserve(R);
+    for (int r = 0; r < R; r++)
+        radiometries.push_back(make_radiometry(T, C, rads + (long)r * T * C));
+    if (threads > 0) omp_set_num_threads(threads);
+    HMMClassifier classifier(T, C, sm, ss, dye_seqs);
+    double t0 = omp_get_wtime();
+    std::vector<ScoredClassification> results = classifier.classify(radiometries);
+    double t1 = omp_get_wtime();
+    if (seconds) *seconds = t1 - t0;
+    for (int r = 0; r < R; r++) {
+        out_id[r] = results[r].id;
+        out_score[r] = results[r].score;
+        out_total[r] = results[r].total;
+    }
+}
+
+// GenericHMM::improve_fit for one read (generic-hmm.h:60-109) into a fresh
+// SequencingModelFitter; returns P and the expected counts.
+double ref_improve_fit(const wpo_model* m, int T, const char* dye_seq,
+                       const double* rad, unsigned max_num_dyes,
+                       double dist_cutoff, wpo_fit_sums* sums) {
+    int C = m->num_channels;
+    SequencingModel sm;
+    to_reference(m, &sm);
+    SequencingSettings ss;
+    ss.dist_cutoff = dist_cutoff;
+    UniversalPrecomputations up(sm, T, C);
+    up.set_max_num_dyes(max_num_dyes);
+    DyeSeq ds(C, std::string(dye_seq));
+    DyeSeqPrecomputations dsp(ds, sm, T, C);
+    Radiometry r = make_radiometry(T, C, rad);
+    RadiometryPrecomputations rp(r, sm, ss, max_num_dyes);
+    PeptideHMM hmm(T, C, dsp, rp, up);
+    FitSettings fs(C);
+    SequencingModelFitter smf(T, C, sm, fs);
+    double p = hmm.improve_fit(&smf);
+    sums->edman_num = smf.p_edman_failure_fit.numerator;
+    sums->edman_den = smf.p_edman_failure_fit.denominator;
+    for (int t = 0; t < T - 1; t++) {
+        sums->detach_x[t] = smf.p_detach_fit.xvec[t];
+        sums->detach_n[t] = smf.p_detach_fit.nvec[t];
+    }
+    sums->init_block_num = smf.p_initial_block_fit.numerator;
+    sums->init_block_den = smf.p_initial_block_fit.denominator;
+    sums->cyc_block_num = smf.p_cyclic_block_fit.numerator;
+    sums->cyc_block_den = smf.p_cyclic_block_fit.denominator;
+    for (int c = 0; c < C; c++) {
+        sums->bleach_num[c] = smf.channel_fits[c]->p_bleach_fit.numerator;
+        sums->bleach_den[c] = smf.channel_fits[c]->p_bleach_fit.denominator;
+        sums->dud_num[c] = smf.channel_fits[c]->p_dud_fit.numerator;
+        sums->dud_den[c] = smf.channel_fits[c]->p_dud_fit.denominator;
+    }
+    return p;
+}
+
+// HMMFitter::fit (hmm-fitter.h:49-116) with no holds and no pruning, as the
+// `fit` CLI runs it (run-fit.cc:55-95).  Returns log(L) of the fitted model.
+double ref_fit(const wpo_model* start, int T, const char* dye_seq, int R,
+               const double* rads, double stopping_threshold,
+               double max_runtime, wpo_model* out, double* step_size,
+               double* seconds) {
+    int C = start->num_channels;
+    SequencingModel sm;
+    to_reference(start, &sm);
+    SequencingSettings ss;
+    ss.dist_cutoff = std::numeric_limits<double>::max();
+    FitSettings fs(C);
+    DyeSeq ds(C, std::string(dye_seq));
+    std::vector<Radiometry> radiometries;
+    radiometries.reserve(R);
+    for (int r = 0; r < R; r++)
+        radiometries.push_back(make_radiometry(T, C, rads + (long)r * T * C));
+    HMMFitter fitter(T, C, stopping_threshold, max_runtime, sm, ss, fs, ds);
+    SequencingModel fitted;
+    double t0 = omp_get_wtime();
+    double log_l = fitter.fit(radiometries, &fitted, step_size);
+    double t1 = omp_get_wtime();
+    if (seconds) *seconds = t1 - t0;
+    from_reference(fitted, C, out);
+    for (int c = 0; c < C; c++)
+        for (int o = 0; o < C; o++) {
+            out->interactions[c][o] = start->interactions[c][o];
+            out->flat_interactions[c][o] = start->flat_interactions[c][o];
+        }
+    return log_l;
+}
+
+}  // extern "C"

@@ -1,0 +1,1193 @@
+/*
+ * wp_oracle.c -- CPU FP64 restatement of whatprot's peptide HMM.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker).  See wp_oracle.h for the contract.
+ * Every routine below restates one reference routine; the reference
+ * file:line it follows is cited at each definition.  Paths are relative to
+ * the reference project's cc_code/src/.
+ *
+ * Representation: a state vector is two dense FP64 tensors (normal and
+ * broken-N) over an axis-aligned box of (Edman count, dye count per
+ * channel), a detached-state scalar and an allow-detached flag, exactly as
+ * hmm/state-vector/peptide-state-vector.{h,cc}.  Tensors are row-major over
+ * their own box (tensor/tensor.cc:45-54).
+ */
+#include "wp_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORD_MAX (1 + WPO_MAX_CHANNELS)
+
+/* ---------------------------------------------------------------- KDRange */
+/* util/kd-range.cc:18-48 */
+typedef struct {
+    int n;
+    unsigned min[ORD_MAX];
+    unsigned max[ORD_MAX];
+} krange;
+
+static krange kr_intersect(const krange* a, const krange* b) {
+    krange r;
+    r.n = a->n;
+    for (int i = 0; i < a->n; i++) {
+        r.min[i] = a->min[i] > b->min[i] ? a->min[i] : b->min[i];
+        r.max[i] = a->max[i] < b->max[i] ? a->max[i] : b->max[i];
+    }
+    return r;
+}
+
+static int kr_empty(const krange* r) {
+    for (int i = 0; i < r->n; i++)
+        if (r->min[i] >= r->max[i]) return 1;
+    return 0;
+}
+
+static int kr_includes_zero(const krange* r) {
+    for (int i = 0; i < r->n; i++) {
+        if (r->min[i] > 0) return 0;
+        if (r->max[i] <= 0) return 0;
+    }
+    return 1;
+}
+
+/* Row-major odometer over a box (tensor/base-tensor-iterator.h:68-90). */
+typedef struct {
+    krange r;
+    unsigned loc[ORD_MAX];
+    int done;
+} kiter;
+
+static void kit_begin(kiter* it, const krange* r) {
+    it->r = *r;
+    it->done = kr_empty(r);
+    for (int i = 0; i < r->n; i++) it->loc[i] = r->min[i];
+}
+
+static void kit_next(kiter* it) {
+    for (int o = it->r.n - 1; o >= 0; o--) {
+        it->loc[o]++;
+        if (it->loc[o] < it->r.max[o]) return;
+        it->loc[o] = it->r.min[o];
+    }
+    it->done = 1;
+}
+
+/* ----------------------------------------------------------------- Tensor */
+/* tensor/tensor.cc:45-54 (strides from the box extents, zero-filled). */
+typedef struct {
+    krange range;
+    long strides[ORD_MAX];
+    long size;
+    double* v;
+} tensor;
+
+static void tensor_init(tensor* t, const krange* r) {
+    t->range = *r;
+    long size = 1;
+    for (int i = r->n - 1; i >= 0; i--) {
+        t->strides[i] = size;
+        size *= (long)(r->max[i] - r->min[i]);
+    }
+    t->size = size;
+    t->v = (double*)calloc(size > 0 ? size : 1, sizeof(double));
+}
+
+static void tensor_free(tensor* t) {
+    free(t->v);
+    t->v = NULL;
+}
+
+static long tensor_index(const tensor* t, const unsigned* loc) {
+    long idx = 0;
+    for (int i = 0; i < t->range.n; i++)
+        idx += t->strides[i] * (long)(loc[i] - t->range.min[i]);
+    return idx;
+}
+
+/* tensor/tensor.cc:111-121 */
+static double tensor_sum(const tensor* t, const krange* r) {
+    double total = 0.0;
+    kiter it;
+    for (kit_begin(&it, r); !it.done; kit_next(&it))
+        total += t->v[tensor_index(t, it.loc)];
+    return total;
+}
+
+/* ------------------------------------------------------------ StateVector */
+/* hmm/state-vector/peptide-state-vector.cc:32-58 */
+typedef struct {
+    tensor a;  /* tensor */
+    tensor b;  /* broken_n_tensor */
+    krange range;
+    double pd; /* p_detached */
+    int allow; /* allow_detached */
+} psv;
+
+static psv* psv_new(const krange* r) {
+    psv* s = (psv*)calloc(1, sizeof(psv));
+    tensor_init(&s->a, r);
+    tensor_init(&s->b, r);
+    s->range.n = 0;
+    s->pd = 0.0;
+    s->allow = 1;
+    return s;
+}
+
+static void psv_free(psv* s) {
+    if (!s) return;
+    tensor_free(&s->a);
+    tensor_free(&s->b);
+    free(s);
+}
+
+static double psv_sum(const psv* s) {
+    return tensor_sum(&s->a, &s->range) + tensor_sum(&s->b, &s->range) + s->pd;
+}
+
+/* Multiply every stored value by 2^-k (exact; used for rescaling). */
+static void psv_scale_pow2(psv* s, int k) {
+    for (long i = 0; i < s->a.size; i++) s->a.v[i] = ldexp(s->a.v[i], -k);
+    for (long i = 0; i < s->b.size; i++) s->b.v[i] = ldexp(s->b.v[i], -k);
+    s->pd = ldexp(s->pd, -k);
+}
+
+/* ----------------------------------------------------------- Model pieces */
+/* parameterization/model/channel-model.h:35-54 (adjusted_mu). */
+double wpo_adjusted_mu(const wpo_model* m, int channel, const unsigned* counts) {
+    double amu = m->mu[channel];
+    amu *= (double)counts[channel];
+    for (int c = 0; c < m->num_channels; c++) {
+        if (c == channel) {
+            if (counts[c] > 1) {
+                amu *= m->flat_interactions[channel][c];
+                amu *= pow(m->interactions[channel][c], counts[c] - 1);
+            }
+        } else {
+            if (counts[c] > 0) {
+                amu *= m->flat_interactions[channel][c];
+                amu *= pow(m->interactions[channel][c], counts[c]);
+            }
+        }
+    }
+    return amu;
+}
+
+/* parameterization/model/channel-model.cc:35-37 */
+double wpo_sigma(const wpo_model* m, int channel, double amu) {
+    return sqrt(m->bg_sig[channel] * m->bg_sig[channel]
+                + amu * m->sig[channel] * m->sig[channel]);
+}
+
+/* parameterization/model/channel-model.h:61-70 (pdf_helper). */
+double wpo_pdf(const wpo_model* m, int channel, double observed,
+               const unsigned* counts) {
+    static const double pi = 3.141592653589793238;
+    double amu = wpo_adjusted_mu(m, channel, counts);
+    double offset = observed - amu;
+    double s = wpo_sigma(m, channel, amu);
+    return (1.0 / (s * sqrt(2.0 * pi))) * exp(-offset * offset / (2.0 * s * s));
+}
+
+/* parameterization/model/decaying-rate-model.cc:47-50 */
+double wpo_p_detach_at(const wpo_model* m, unsigned t) {
+    return m->p_detach + m->p_initial_detach
+                                 * exp(-(double)t * m->p_initial_detach_decay);
+}
+
+/* common/dye-track.cc:26-43 */
+void wpo_dye_track(int T, int C, const int16_t* seq, int length, int16_t* out) {
+    int16_t cs[WPO_MAX_CHANNELS];
+    memset(cs, 0, sizeof(cs));
+    memset(out, 0, sizeof(int16_t) * T * C);
+    for (int t = length - 1; t >= 0; t--) {
+        int16_t dye = seq[t];
+        if (dye != -1) cs[dye]++;
+        if (t < T) memcpy(&out[t * C], cs, sizeof(int16_t) * C);
+    }
+}
+
+/* common/dye-seq.cc:52-58: out-of-range positions read as -1. */
+static int dye_at(const int16_t* seq, int length, unsigned i) {
+    return (int)i < length ? seq[i] : -1;
+}
+
+/* hmm/step/peptide-emission.cc:50-163 */
+void wpo_emission_range(const wpo_model* m, const double* rad, int t,
+                        unsigned max_num_dyes, double dist_cutoff,
+                        unsigned* out_min, unsigned* out_max) {
+    int C = m->num_channels;
+    if (dist_cutoff == DBL_MAX) {
+        for (int c = 0; c < C; c++) {
+            out_min[c] = 0;
+            out_max[c] = max_num_dyes + 1;
+        }
+        return;
+    }
+    unsigned counts_lo[WPO_MAX_CHANNELS] = {0};
+    unsigned counts_hi[WPO_MAX_CHANNELS] = {0};
+    int did_change = 1;
+    while (did_change) {
+        did_change = 0;
+        for (int c = 0; c < C; c++) {
+            double old_counts_hi_c = counts_hi[c];
+            counts_hi[c] = 1;
+            double mu1 = wpo_adjusted_mu(m, c, counts_hi);
+            counts_hi[c] = (unsigned)old_counts_hi_c;
+            double mu = wpo_adjusted_mu(m, c, counts_hi);
+            double s = dist_cutoff * wpo_sigma(m, c, mu);
+            unsigned new_cts = (unsigned)lround((rad[t * C + c] + s) / mu1);
+            if (new_cts > max_num_dyes + 1) new_cts = max_num_dyes + 1;
+            if (new_cts != counts_hi[c]) {
+                did_change = 1;
+                counts_hi[c] = new_cts;
+            }
+        }
+    }
+    for (int c = 0; c < C; c++) {
+        unsigned cmin = max_num_dyes + 1;
+        double old_lo = counts_lo[c];
+        for (unsigned d = 0; d < max_num_dyes + 1; d++) {
+            counts_lo[c] = d;
+            double mu = wpo_adjusted_mu(m, c, counts_lo);
+            double s = dist_cutoff * wpo_sigma(m, c, mu);
+            if (mu + s > rad[t * C + c]) {
+                cmin = d;
+                break;
+            }
+        }
+        out_min[c] = cmin;
+        counts_lo[c] = (unsigned)old_lo;
+        unsigned cmax = max_num_dyes + 1;
+        double old_hi = counts_hi[c];
+        for (unsigned d = cmin; d < max_num_dyes + 1; d++) {
+            counts_hi[c] = d;
+            double mu = wpo_adjusted_mu(m, c, counts_hi);
+            double s = dist_cutoff * wpo_sigma(m, c, mu);
+            if (mu - s > rad[t * C + c]) {
+                cmax = d;
+                break;
+            }
+        }
+        out_max[c] = cmax;
+        counts_hi[c] = (unsigned)old_hi;
+    }
+}
+
+/* hmm/step/binomial-transition.cc:51-67 (reserve) and :69-75 (prob). */
+static void binomial_table(double q, unsigned max_n, double* tab) {
+    double p = (double)1 - q;
+    tab[0] = 1.0;
+    for (unsigned i = 1; i <= max_n; i++) {
+        tab[i * (i + 1) / 2 + 0] = tab[(i - 1) * i / 2 + 0] * q;
+        for (unsigned j = 1; j < i; j++)
+            tab[i * (i + 1) / 2 + j] = tab[(i - 1) * i / 2 + j] * q
+                                       + tab[(i - 1) * i / 2 + j - 1] * p;
+        tab[i * (i + 1) / 2 + i] = tab[(i - 1) * i / 2 + i - 1] * p;
+    }
+}
+#define BPROB(tab, from, to) ((tab)[(from) * ((from) + 1) / 2 + (to)])
+
+/* ------------------------------------------------------------------ Steps */
+enum { S_INIT_BLOCK, S_DUD, S_EMIT, S_CYC_BLOCK, S_DETACH, S_BLEACH, S_EDMAN };
+
+typedef struct {
+    int kind;
+    int channel; /* binomial steps */
+    int t;       /* emission timestep or detach timestep index */
+    double p;    /* block p / detach p / edman p_fail / binomial q */
+    const double* tab; /* binomial table */
+    const tensor* ptsr; /* emission table (over the emission's own box) */
+    /* block, detach, emission: r1 = pruned_range.
+     * binomial: r1 = forward_range, r2 = backward_range.
+     * edman: r1 = true_forward, r2 = safe_forward, r3 = true_backward,
+     *        r4 = safe_backward. */
+    krange r1, r2, r3, r4;
+    int allow;   /* emission allow_detached */
+    int det_fwd; /* detach detached_forward */
+    int det_bwd; /* detach detached_backward */
+} step;
+
+typedef struct {
+    int T, C;
+    const wpo_model* m;
+    const int16_t* seq;
+    int length;
+    int16_t track[WPO_MAX_TIMESTEPS * WPO_MAX_CHANNELS];
+    int nsteps;
+    step* steps;
+    krange forward_range, backward_range;
+    int empty;
+    /* emission tables (RadiometryPrecomputations) and binomial tables */
+    tensor ptsr[WPO_MAX_TIMESTEPS];
+    krange emit_range[WPO_MAX_TIMESTEPS];
+    double* dud_tab[WPO_MAX_CHANNELS];
+    double* bleach_tab[WPO_MAX_CHANNELS];
+    double p_detach[WPO_MAX_TIMESTEPS];
+} hmm;
+
+/* Edman ranges (hmm/step/edman-transition.cc:28-60). */
+static void edman_set_true_forward(step* s, const krange* r) {
+    s->r1 = *r;
+    s->r4 = *r;
+    s->r4.max[0]++;
+    for (int c = 0; c < s->r4.n - 1; c++)
+        if (s->r4.min[1 + c] != 0) s->r4.min[1 + c]--;
+}
+
+static void edman_set_true_backward(step* s, const krange* r) {
+    s->r3 = *r;
+    s->r2 = *r;
+    if (s->r2.min[0] != 0) s->r2.min[0]--;
+    for (int c = 0; c < s->r2.n - 1; c++) s->r2.max[1 + c]++;
+}
+
+static void prune_forward(step* s, krange* range, int* allow_detached) {
+    switch (s->kind) {
+    case S_INIT_BLOCK:
+    case S_CYC_BLOCK: /* hmm/step/block-transition.cc:24-26 */
+        s->r1 = *range;
+        break;
+    case S_DUD:
+    case S_BLEACH: /* hmm/step/binomial-transition.cc:77-81 */
+        s->r1 = *range;
+        range->min[1 + s->channel] = 0;
+        s->r2 = *range;
+        break;
+    case S_EMIT: /* hmm/step/peptide-emission.cc:198-203 */
+        s->r1 = kr_intersect(&s->r1, range);
+        *range = s->r1;
+        s->allow = kr_includes_zero(&s->r1);
+        *allow_detached = s->allow;
+        break;
+    case S_DETACH: /* hmm/step/detach-transition.cc:24-28 */
+        s->r1 = *range;
+        s->det_fwd = *allow_detached;
+        *allow_detached = 1;
+        break;
+    case S_EDMAN: /* hmm/step/edman-transition.cc:50-53 */
+        edman_set_true_forward(s, range);
+        *range = s->r4;
+        break;
+    }
+}
+
+static void prune_backward(step* s, krange* range, int* allow_detached) {
+    switch (s->kind) {
+    case S_INIT_BLOCK:
+    case S_CYC_BLOCK: /* hmm/step/block-transition.cc:28-31 */
+        s->r1 = kr_intersect(&s->r1, range);
+        *range = s->r1;
+        break;
+    case S_DUD:
+    case S_BLEACH: /* hmm/step/binomial-transition.cc:83-89 */
+        s->r2 = kr_intersect(&s->r2, range);
+        *range = s->r2;
+        range->max[1 + s->channel] = UINT32_MAX;
+        s->r1 = kr_intersect(&s->r1, range);
+        *range = s->r1;
+        break;
+    case S_EMIT: /* hmm/step/peptide-emission.cc:205-210 */
+        s->r1 = kr_intersect(&s->r1, range);
+        *range = s->r1;
+        s->allow = kr_includes_zero(&s->r1);
+        *allow_detached = s->allow;
+        break;
+    case S_DETACH: /* hmm/step/detach-transition.cc:30-34: the reference
+                      assigns the (non-null) pointer, so this is true. */
+        s->r1 = kr_intersect(&s->r1, range);
+        *range = s->r1;
+        s->det_bwd = 1;
+        break;
+    case S_EDMAN: /* hmm/step/edman-transition.cc:55-60 */
+        *range = kr_intersect(&s->r4, range);
+        edman_set_true_backward(s, range);
+        *range = kr_intersect(&s->r2, &s->r1);
+        edman_set_true_forward(s, range);
+        break;
+    }
+}
+
+/* RadiometryPrecomputations / PeptideEmission ctor
+ * (hmm/precomputations/radiometry-precomputations.cc:20-29,
+ *  hmm/step/peptide-emission.cc:39-181). */
+static void build_emissions(hmm* h, const double* rad, unsigned max_num_dyes,
+                            double dist_cutoff) {
+    int C = h->C;
+    for (int t = 0; t < h->T; t++) {
+        unsigned lo[WPO_MAX_CHANNELS], hi[WPO_MAX_CHANNELS];
+        wpo_emission_range(h->m, rad, t, max_num_dyes, dist_cutoff, lo, hi);
+        krange pr;
+        pr.n = 1 + C;
+        pr.min[0] = 0;
+        pr.max[0] = (unsigned)t + 1;
+        for (int c = 0; c < C; c++) {
+            pr.min[1 + c] = lo[c];
+            pr.max[1 + c] = hi[c];
+        }
+        h->emit_range[t] = pr;
+        krange tr;
+        tr.n = C;
+        for (int c = 0; c < C; c++) {
+            tr.min[c] = lo[c];
+            tr.max[c] = hi[c];
+        }
+        tensor_init(&h->ptsr[t], &tr);
+        kiter it;
+        for (kit_begin(&it, &tr); !it.done; kit_next(&it)) {
+            double v = 1.0;
+            for (int c = 0; c < C; c++)
+                v *= wpo_pdf(h->m, c, rad[t * C + c], it.loc);
+            h->ptsr[t].v[tensor_index(&h->ptsr[t], it.loc)] = v;
+        }
+    }
+}
+
+/* PeptideHMM ctor (hmm/hmm/peptide-hmm.cc:33-84), with
+ * DyeSeqPrecomputations (hmm/precomputations/dye-seq-precomputations.cc:20-39)
+ * and UniversalPrecomputations (universal-precomputations.cc:23-59). */
+static void hmm_build(hmm* h, const wpo_model* m, int T, const int16_t* seq,
+                      int length, const double* rad, unsigned max_num_dyes,
+                      double dist_cutoff) {
+    memset(h, 0, sizeof(*h));
+    int C = m->num_channels;
+    h->T = T;
+    h->C = C;
+    h->m = m;
+    h->seq = seq;
+    h->length = length;
+    wpo_dye_track(T, C, seq, length, h->track);
+    for (int c = 0; c < C; c++) {
+        h->dud_tab[c] = (double*)calloc((max_num_dyes + 1) * (max_num_dyes + 2) / 2,
+                                        sizeof(double));
+        h->bleach_tab[c] = (double*)calloc((max_num_dyes + 1) * (max_num_dyes + 2) / 2,
+                                           sizeof(double));
+        binomial_table(m->p_dud[c], max_num_dyes, h->dud_tab[c]);
+        binomial_table(m->p_bleach[c], max_num_dyes, h->bleach_tab[c]);
+    }
+    for (int t = 0; t < T; t++) h->p_detach[t] = wpo_p_detach_at(m, (unsigned)t);
+    build_emissions(h, rad, max_num_dyes, dist_cutoff);
+
+    h->nsteps = 1 + C + 1 + (T - 1) * (3 + C + 1);
+    h->steps = (step*)calloc(h->nsteps, sizeof(step));
+    int k = 0;
+    step* s;
+    s = &h->steps[k++];
+    s->kind = S_INIT_BLOCK;
+    s->p = m->p_initial_block;
+    for (int c = 0; c < C; c++) {
+        s = &h->steps[k++];
+        s->kind = S_DUD;
+        s->channel = c;
+        s->p = m->p_dud[c];
+        s->tab = h->dud_tab[c];
+    }
+    s = &h->steps[k++];
+    s->kind = S_EMIT;
+    s->t = 0;
+    s->r1 = h->emit_range[0];
+    s->ptsr = &h->ptsr[0];
+    for (int t = 1; t < T; t++) {
+        s = &h->steps[k++];
+        s->kind = S_CYC_BLOCK;
+        s->p = m->p_cyclic_block;
+        s = &h->steps[k++];
+        s->kind = S_DETACH;
+        s->t = t - 1;
+        s->p = h->p_detach[t - 1];
+        for (int c = 0; c < C; c++) {
+            s = &h->steps[k++];
+            s->kind = S_BLEACH;
+            s->channel = c;
+            s->p = m->p_bleach[c];
+            s->tab = h->bleach_tab[c];
+        }
+        s = &h->steps[k++];
+        s->kind = S_EDMAN;
+        s->p = m->p_edman_failure;
+        s = &h->steps[k++];
+        s->kind = S_EMIT;
+        s->t = t;
+        s->r1 = h->emit_range[t];
+        s->ptsr = &h->ptsr[t];
+    }
+
+    krange range;
+    range.n = 1 + C;
+    range.min[0] = 0;
+    range.max[0] = (unsigned)T;
+    for (int c = 0; c < C; c++) {
+        range.min[1 + c] = 0;
+        range.max[1 + c] = 1 + (unsigned)h->track[c]; /* dye_track(0, c) */
+    }
+    int allow_detached = 0;
+    for (int i = 0; i < h->nsteps; i++) {
+        prune_forward(&h->steps[i], &range, &allow_detached);
+        if (kr_empty(&range)) {
+            h->empty = 1;
+            return;
+        }
+    }
+    h->backward_range = range;
+    for (int i = h->nsteps - 1; i >= 0; i--) {
+        prune_backward(&h->steps[i], &range, &allow_detached);
+        if (kr_empty(&range)) {
+            h->empty = 1;
+            return;
+        }
+    }
+    h->forward_range = range;
+}
+
+static void hmm_free(hmm* h) {
+    for (int c = 0; c < h->C; c++) {
+        free(h->dud_tab[c]);
+        free(h->bleach_tab[c]);
+    }
+    for (int t = 0; t < h->T; t++) tensor_free(&h->ptsr[t]);
+    free(h->steps);
+}
+
+/* Fiber transform along one channel axis (binomial-transition.cc:104-136). */
+static void binomial_fwd_tensor(const step* s, const tensor* in, tensor* out,
+                                double* flops) {
+    int dim = 1 + s->channel;
+    krange fibers = s->r2; /* iterate other coordinates over backward_range */
+    fibers.min[dim] = 0;
+    fibers.max[dim] = 1;
+    unsigned to_min = s->r2.min[dim], to_max = s->r2.max[dim];
+    unsigned fr_min = s->r1.min[dim], fr_max = s->r1.max[dim];
+    kiter it;
+    for (kit_begin(&it, &fibers); !it.done; kit_next(&it)) {
+        unsigned loc[ORD_MAX];
+        memcpy(loc, it.loc, sizeof(loc));
+        for (unsigned to = to_min; to < to_max; to++) {
+            double v_to = 0.0;
+            unsigned from_min = to > fr_min ? to : fr_min;
+            for (unsigned from = from_min; from < fr_max; from++) {
+                loc[dim] = from;
+                v_to += BPROB(s->tab, from, to) * in->v[tensor_index(in, loc)];
+                if (flops) *flops += 2.0;
+            }
+            loc[dim] = to;
+            out->v[tensor_index(out, loc)] = v_to;
+        }
+    }
+}
+
+static int g_count_broken = 0; /* visited-flops count only the normal tensor */
+
+static psv* step_forward(const hmm* h, const step* s, const psv* in,
+                         double* flops) {
+    psv* out = NULL;
+    kiter it;
+    switch (s->kind) {
+    case S_INIT_BLOCK:
+    case S_CYC_BLOCK: { /* hmm/step/block-transition.cc:33-62 */
+        out = psv_new(&s->r1);
+        for (kit_begin(&it, &s->r1); !it.done; kit_next(&it)) {
+            double ta = in->a.v[tensor_index(&in->a, it.loc)];
+            double tb = in->b.v[tensor_index(&in->b, it.loc)];
+            out->a.v[tensor_index(&out->a, it.loc)] = (1 - s->p) * ta;
+            out->b.v[tensor_index(&out->b, it.loc)] = tb + s->p * ta;
+            if (flops && s->p != 0.0) *flops += 3.0;
+        }
+        out->range = s->r1;
+        out->allow = in->allow;
+        if (out->allow) out->pd = in->pd;
+        break;
+    }
+    case S_DUD:
+    case S_BLEACH: { /* hmm/step/binomial-transition.cc:91-102 */
+        out = psv_new(&s->r2);
+        binomial_fwd_tensor(s, &in->a, &out->a, flops);
+        binomial_fwd_tensor(s, &in->b, &out->b, g_count_broken ? flops : NULL);
+        out->range = s->r2;
+        out->allow = in->allow;
+        if (out->allow) out->pd = in->pd;
+        break;
+    }
+    case S_EMIT: { /* hmm/step/peptide-emission.cc:212-243 */
+        out = psv_new(&s->r1);
+        for (kit_begin(&it, &s->r1); !it.done; kit_next(&it)) {
+            double prob = s->ptsr->v[tensor_index(s->ptsr, &it.loc[1])];
+            out->a.v[tensor_index(&out->a, it.loc)] =
+                    in->a.v[tensor_index(&in->a, it.loc)] * prob;
+            if (flops) *flops += 1.0;
+        }
+        for (kit_begin(&it, &s->r1); !it.done; kit_next(&it)) {
+            double prob = s->ptsr->v[tensor_index(s->ptsr, &it.loc[1])];
+            out->b.v[tensor_index(&out->b, it.loc)] =
+                    in->b.v[tensor_index(&in->b, it.loc)] * prob;
+        }
+        if (s->allow) {
+            unsigned zeros[ORD_MAX] = {0};
+            double prob = s->ptsr->v[tensor_index(s->ptsr, zeros)];
+            out->pd = in->pd * prob;
+        }
+        out->range = s->r1;
+        out->allow = s->allow;
+        break;
+    }
+    case S_DETACH: { /* hmm/step/detach-transition.cc:36-68 */
+        out = psv_new(&s->r1);
+        double sum = 0.0;
+        for (kit_begin(&it, &s->r1); !it.done; kit_next(&it)) {
+            double value = in->a.v[tensor_index(&in->a, it.loc)];
+            out->a.v[tensor_index(&out->a, it.loc)] = value * (1 - s->p);
+            sum += value;
+            if (flops) *flops += 2.0;
+        }
+        double sum_b = 0.0;
+        for (kit_begin(&it, &s->r1); !it.done; kit_next(&it)) {
+            double value = in->b.v[tensor_index(&in->b, it.loc)];
+            out->b.v[tensor_index(&out->b, it.loc)] = value * (1 - s->p);
+            sum_b += value;
+        }
+        sum += sum_b;
+        if (s->det_bwd) {
+            if (s->det_fwd)
+                out->pd = in->pd + s->p * sum;
+            else
+                out->pd = s->p * sum;
+        }
+        out->range = s->r1;
+        out->allow = s->det_bwd;
+        break;
+    }
+    case S_EDMAN: { /* hmm/step/edman-transition.cc:62-162 */
+        const krange* tf = &s->r1;
+        out = psv_new(&s->r4);
+        long t_stride = out->a.strides[0];
+        double pf = s->p;
+        for (kit_begin(&it, tf); !it.done; kit_next(&it)) {
+            double f_val = in->a.v[tensor_index(&in->a, it.loc)];
+            long i = tensor_index(&out->a, it.loc);
+            unsigned t = it.loc[0];
+            int c = dye_at(h->seq, h->length, t);
+            out->a.v[i] += pf * f_val;
+            if (c == -1) {
+                out->a.v[i + t_stride] += (1 - pf) * f_val;
+            } else {
+                unsigned c_idx = it.loc[1 + c];
+                unsigned c_total = (unsigned)h->track[t * h->C + c];
+                double ratio = (double)c_idx / (double)c_total;
+                long c_stride = out->a.strides[1 + c];
+                if (c_idx < c_total)
+                    out->a.v[i + t_stride] += (1 - pf) * (1 - ratio) * f_val;
+                if (c_idx > 0)
+                    out->a.v[i + t_stride - c_stride] += (1 - pf) * ratio * f_val;
+            }
+            if (flops) *flops += 6.0;
+        }
+        for (kit_begin(&it, tf); !it.done; kit_next(&it))
+            out->b.v[tensor_index(&out->b, it.loc)] =
+                    in->b.v[tensor_index(&in->b, it.loc)];
+        out->range = s->r3;
+        out->allow = in->allow;
+        if (out->allow) out->pd = in->pd;
+        break;
+    }
+    }
+    return out;
+}
+
+/* Exact power-of-two rescale so the state sums to [0.5, 1). */
+static void rescale(psv* s, long* expo, double* flops) {
+    double total = psv_sum(s);
+    if (total > 0.0 && isfinite(total)) {
+        int e;
+        frexp(total, &e);
+        psv_scale_pow2(s, e);
+        *expo += e;
+    }
+    if (flops) {
+        double states = 1.0;
+        for (int i = 0; i < s->range.n; i++)
+            states *= (double)(s->range.max[i] - s->range.min[i]);
+        *flops += 2.0 * states;
+    }
+}
+
+/* GenericHMM::probability (hmm/hmm/generic-hmm.h:41-55) with
+ * PeptideHMM::probability (hmm/hmm/peptide-hmm.cc:94-100). */
+static double hmm_probability(const hmm* h, double* log_p, double* flops) {
+    if (h->empty) {
+        if (log_p) *log_p = -INFINITY;
+        return 0.0;
+    }
+    psv* in = psv_new(&h->forward_range);
+    in->a.v[in->a.strides[0] - 1] = 1.0; /* initialize_from_start */
+    long expo = 0;
+    for (int i = 0; i < h->nsteps; i++) {
+        psv* out = step_forward(h, &h->steps[i], in, flops);
+        psv_free(in);
+        in = out;
+        if (h->steps[i].kind == S_EMIT) rescale(in, &expo, flops);
+    }
+    double s = psv_sum(in);
+    psv_free(in);
+    if (log_p) *log_p = (s > 0.0) ? log(s) + (double)expo * M_LN2 : -INFINITY;
+    return ldexp(s, (int)expo);
+}
+
+double wpo_peptide_probability(const wpo_model* m, int num_timesteps,
+                               const int16_t* seq, int length,
+                               const double* rad, unsigned max_num_dyes,
+                               double dist_cutoff, double* log_p,
+                               double* visited_flops) {
+    hmm h;
+    hmm_build(&h, m, num_timesteps, seq, length, rad, max_num_dyes, dist_cutoff);
+    if (visited_flops) *visited_flops = 0.0;
+    double p = hmm_probability(&h, log_p, visited_flops);
+    hmm_free(&h);
+    return p;
+}
+
+int wpo_pruned_emission_boxes(const wpo_model* m, int num_timesteps,
+                              const int16_t* seq, int length,
+                              const double* rad, unsigned max_num_dyes,
+                              double dist_cutoff, unsigned* lo, unsigned* hi) {
+    hmm h;
+    hmm_build(&h, m, num_timesteps, seq, length, rad, max_num_dyes, dist_cutoff);
+    int empty = h.empty;
+    if (!empty) {
+        for (int i = 0; i < h.nsteps; i++) {
+            const step* s = &h.steps[i];
+            if (s->kind != S_EMIT) continue;
+            for (int c = 0; c < h.C; c++) {
+                lo[s->t * h.C + c] = s->r1.min[1 + c];
+                hi[s->t * h.C + c] = s->r1.max[1 + c];
+            }
+        }
+    }
+    hmm_free(&h);
+    return empty;
+}
+
+/* ------------------------------------------------------ Backward / EM */
+/* binomial-transition.cc:151-183 */
+static void binomial_bwd_tensor(const step* s, const tensor* in, tensor* out) {
+    int dim = 1 + s->channel;
+    krange fibers = s->r1; /* iterate other coordinates over forward_range */
+    fibers.min[dim] = 0;
+    fibers.max[dim] = 1;
+    int from_min = (int)s->r1.min[dim], from_max = (int)s->r1.max[dim];
+    int to_min = (int)s->r2.min[dim];
+    int to_cap = (int)s->r2.max[dim] - 1;
+    kiter it;
+    for (kit_begin(&it, &fibers); !it.done; kit_next(&it)) {
+        unsigned loc[ORD_MAX];
+        memcpy(loc, it.loc, sizeof(loc));
+        for (int from = from_max - 1; from >= from_min; from--) {
+            double v_from = 0.0;
+            int to_max = from < to_cap ? from : to_cap;
+            for (int to = to_min; to <= to_max; to++) {
+                loc[dim] = (unsigned)to;
+                v_from += BPROB(s->tab, from, to) * in->v[tensor_index(in, loc)];
+            }
+            loc[dim] = (unsigned)from;
+            out->v[tensor_index(out, loc)] = v_from;
+        }
+    }
+}
+
+static psv* step_backward(const hmm* h, const step* s, const psv* in) {
+    psv* out = NULL;
+    kiter it;
+    switch (s->kind) {
+    case S_INIT_BLOCK:
+    case S_CYC_BLOCK: { /* hmm/step/block-transition.cc:64-93 */
+        out = psv_new(&s->r1);
+        for (kit_begin(&it, &s->r1); !it.done; kit_next(&it)) {
+            double ta = in->a.v[tensor_index(&in->a, it.loc)];
+            double tb = in->b.v[tensor_index(&in->b, it.loc)];
+            out->a.v[tensor_index(&out->a, it.loc)] = s->p * tb + (1 - s->p) * ta;
+            out->b.v[tensor_index(&out->b, it.loc)] = tb;
+        }
+        out->range = s->r1;
+        out->allow = in->allow;
+        if (out->allow) out->pd = in->pd;
+        break;
+    }
+    case S_DUD:
+    case S_BLEACH: { /* hmm/step/binomial-transition.cc:138-149 */
+        out = psv_new(&s->r1);
+        binomial_bwd_tensor(s, &in->a, &out->a);
+        binomial_bwd_tensor(s, &in->b, &out->b);
+        out->range = s->r1;
+        out->allow = in->allow;
+        if (out->allow) out->pd = in->pd;
+        break;
+    }
+    case S_EMIT: /* emission is its own transpose (peptide-emission.cc:250-253) */
+        out = step_forward(h, s, in, NULL);
+        break;
+    case S_DETACH: { /* hmm/step/detach-transition.cc:70-103 */
+        out = psv_new(&s->r1);
+        for (kit_begin(&it, &s->r1); !it.done; kit_next(&it)) {
+            long o = tensor_index(&out->a, it.loc);
+            out->a.v[o] = (1 - s->p) * in->a.v[tensor_index(&in->a, it.loc)];
+            if (s->det_bwd) out->a.v[o] += s->p * in->pd;
+        }
+        for (kit_begin(&it, &s->r1); !it.done; kit_next(&it)) {
+            long o = tensor_index(&out->b, it.loc);
+            out->b.v[o] = (1 - s->p) * in->b.v[tensor_index(&in->b, it.loc)];
+            if (s->det_bwd) out->b.v[o] += s->p * in->pd;
+        }
+        if (s->det_fwd) out->pd = s->det_bwd ? in->pd : 0.0;
+        out->range = s->r1;
+        out->allow = s->det_fwd;
+        break;
+    }
+    case S_EDMAN: { /* hmm/step/edman-transition.cc:164-277 */
+        const krange* tb = &s->r3;
+        out = psv_new(&s->r2);
+        long t_stride = out->a.strides[0];
+        double pf = s->p;
+        for (kit_begin(&it, tb); !it.done; kit_next(&it)) {
+            double f_val = in->a.v[tensor_index(&in->a, it.loc)];
+            long i = tensor_index(&out->a, it.loc);
+            unsigned t = it.loc[0];
+            out->a.v[i] += pf * f_val;
+            if (t > 0) {
+                int c = dye_at(h->seq, h->length, t - 1);
+                if (c == -1) {
+                    out->a.v[i - t_stride] += (1 - pf) * f_val;
+                } else {
+                    unsigned c_total = (unsigned)h->track[(t - 1) * h->C + c];
+                    long c_stride = out->a.strides[1 + c];
+                    unsigned c_idx = it.loc[1 + c];
+                    if (c_idx < c_total) {
+                        double ratio = (double)c_idx / (double)c_total;
+                        out->a.v[i - t_stride] += (1 - pf) * (1 - ratio) * f_val;
+                    }
+                    c_idx = it.loc[1 + c] + 1;
+                    if (c_idx > 0) {
+                        double ratio = (double)c_idx / (double)c_total;
+                        out->a.v[i - t_stride + c_stride] += (1 - pf) * ratio * f_val;
+                    }
+                }
+            }
+        }
+        for (kit_begin(&it, tb); !it.done; kit_next(&it))
+            out->b.v[tensor_index(&out->b, it.loc)] =
+                    in->b.v[tensor_index(&in->b, it.loc)];
+        out->range = s->r1;
+        out->allow = in->allow;
+        if (out->allow) out->pd = in->pd;
+        break;
+    }
+    }
+    return out;
+}
+
+/* binomial-transition.cc:185-256 */
+static void binomial_fit_tensor(const step* s, const tensor* f, const tensor* b,
+                                const tensor* nb, double P, double* num,
+                                double* den) {
+    int dim = 1 + s->channel;
+    krange fibers = s->r1;
+    fibers.min[dim] = 0;
+    fibers.max[dim] = 1;
+    int from_min = (int)s->r1.min[dim], from_max = (int)s->r1.max[dim];
+    int to_min = (int)s->r2.min[dim], to_max = (int)s->r2.max[dim];
+    kiter it;
+    for (kit_begin(&it, &fibers); !it.done; kit_next(&it)) {
+        unsigned loc[ORD_MAX];
+        memcpy(loc, it.loc, sizeof(loc));
+        int lo = from_min > 1 ? from_min : 1;
+        for (int from = from_max - 1; from >= lo; from--) {
+            loc[dim] = (unsigned)from;
+            double fv = f->v[tensor_index(f, loc)];
+            double p_state = fv * b->v[tensor_index(b, loc)] / P;
+            *den += p_state * (double)from;
+            int hi = to_max < from ? to_max : from;
+            for (int to = to_min; to < hi; to++) {
+                loc[dim] = (unsigned)to;
+                double p_tr = fv * BPROB(s->tab, from, to)
+                              * nb->v[tensor_index(nb, loc)] / P;
+                *num += p_tr * (double)(from - to);
+            }
+        }
+    }
+}
+
+/* detach-transition.cc:121-166 (one tensor). */
+static void detach_fit_tensor(const step* s, const tensor* f, const tensor* b,
+                              double nb_pd, double P, wpo_fit_sums* sums) {
+    double forward_sum = 0.0, fb_sum = 0.0;
+    int skip_zero = kr_includes_zero(&s->r1);
+    unsigned old_t = UINT32_MAX;
+    kiter it;
+    for (kit_begin(&it, &s->r1); !it.done; kit_next(&it)) {
+        if (skip_zero && it.loc[0] != old_t) {
+            old_t = it.loc[0];
+            continue;
+        }
+        double fv = f->v[tensor_index(f, it.loc)];
+        double bv = b->v[tensor_index(b, it.loc)];
+        forward_sum += fv;
+        fb_sum += fv * bv;
+    }
+    sums->detach_x[s->t] += forward_sum * s->p * nb_pd / P;
+    sums->detach_n[s->t] += fb_sum / P;
+}
+
+static void step_improve_fit(const hmm* h, const step* s, const psv* fw,
+                             const psv* bw, const psv* nbw, double P,
+                             wpo_fit_sums* sums) {
+    kiter it;
+    switch (s->kind) {
+    case S_INIT_BLOCK:
+    case S_CYC_BLOCK: { /* block-transition.cc:95-116 */
+        double* num = s->kind == S_INIT_BLOCK ? &sums->init_block_num : &sums->cyc_block_num;
+        double* den = s->kind == S_INIT_BLOCK ? &sums->init_block_den : &sums->cyc_block_den;
+        for (kit_begin(&it, &s->r1); !it.done; kit_next(&it)) {
+            double fv = fw->a.v[tensor_index(&fw->a, it.loc)];
+            *num += fv * s->p * nbw->b.v[tensor_index(&nbw->b, it.loc)] / P;
+            *den += fv * bw->a.v[tensor_index(&bw->a, it.loc)] / P;
+        }
+        break;
+    }
+    case S_DUD:
+    case S_BLEACH: { /* dud-transition.cc:25-37, bleach-transition.cc:25-38 */
+        int c = s->channel;
+        double* num = s->kind == S_DUD ? &sums->dud_num[c] : &sums->bleach_num[c];
+        double* den = s->kind == S_DUD ? &sums->dud_den[c] : &sums->bleach_den[c];
+        binomial_fit_tensor(s, &fw->a, &bw->a, &nbw->a, P, num, den);
+        binomial_fit_tensor(s, &fw->b, &bw->b, &nbw->b, P, num, den);
+        break;
+    }
+    case S_EMIT: /* peptide-emission.cc:255-260: no-op */
+        break;
+    case S_DETACH:
+        detach_fit_tensor(s, &fw->a, &bw->a, nbw->pd, P, sums);
+        detach_fit_tensor(s, &fw->b, &bw->b, nbw->pd, P, sums);
+        break;
+    case S_EDMAN: { /* edman-transition.cc:279-325 */
+        const krange* tf = &s->r1;
+        int skip_zero = kr_includes_zero(tf);
+        unsigned old_t = UINT32_MAX;
+        for (kit_begin(&it, tf); !it.done; kit_next(&it)) {
+            if (skip_zero && it.loc[0] != old_t) {
+                old_t = it.loc[0];
+                continue;
+            }
+            double fv = fw->a.v[tensor_index(&fw->a, it.loc)];
+            double bv = bw->a.v[tensor_index(&bw->a, it.loc)];
+            double nbv = nbw->a.v[tensor_index(&nbw->a, it.loc)];
+            sums->edman_num += fv * s->p * nbv / P;
+            sums->edman_den += fv * bv / P;
+        }
+        break;
+    }
+    }
+}
+
+/* GenericHMM::improve_fit (hmm/hmm/generic-hmm.h:60-109). */
+double wpo_improve_fit(const wpo_model* m, int T, const int16_t* seq, int length,
+                       const double* rad, unsigned max_num_dyes,
+                       double dist_cutoff, wpo_fit_sums* sums, double* log_p) {
+    hmm h;
+    hmm_build(&h, m, T, seq, length, rad, max_num_dyes, dist_cutoff);
+    if (log_p) hmm_probability(&h, log_p, NULL);
+    if (h.empty) {
+        hmm_free(&h);
+        return 0.0;
+    }
+    psv** bsv = (psv**)calloc(h.nsteps + 1, sizeof(psv*));
+    psv* fin = psv_new(&h.backward_range); /* initialize_from_finish */
+    for (long i = 0; i < fin->a.size; i++) fin->a.v[i] = 1.0;
+    for (long i = 0; i < fin->b.size; i++) fin->b.v[i] = 1.0;
+    fin->pd = 1.0;
+    bsv[h.nsteps] = fin; /* bsv[i] = backward state at the input of step i */
+    for (int i = h.nsteps - 1; i >= 0; i--)
+        bsv[i] = step_backward(&h, &h.steps[i], bsv[i + 1]);
+    double P = bsv[0]->a.v[bsv[0]->a.strides[0] - 1]; /* source() */
+    if (P != 0.0) {
+        psv* fw = psv_new(&h.forward_range);
+        fw->a.v[fw->a.strides[0] - 1] = 1.0;
+        for (int i = 0; i < h.nsteps; i++) {
+            step_improve_fit(&h, &h.steps[i], fw, bsv[i], bsv[i + 1], P, sums);
+            psv* nx = step_forward(&h, &h.steps[i], fw, NULL);
+            psv_free(fw);
+            fw = nx;
+        }
+        psv_free(fw);
+    }
+    for (int i = 0; i <= h.nsteps; i++) psv_free(bsv[i]);
+    free(bsv);
+    hmm_free(&h);
+    return P;
+}
+
+/* ------------------------------------------------------------- Classifier */
+static unsigned max_num_dyes_of(int C, const int16_t* seqs, const int32_t* offsets,
+                                int P, int T) {
+    /* hmm/classifiers/hmm-classifier.cc:47-66: Dmax over all dye-seqs. */
+    unsigned dmax = 0;
+    int16_t track[WPO_MAX_TIMESTEPS * WPO_MAX_CHANNELS];
+    for (int i = 0; i < P; i++) {
+        wpo_dye_track(T, C, seqs + offsets[i], offsets[i + 1] - offsets[i], track);
+        for (int c = 0; c < C; c++)
+            if ((unsigned)track[c] > dmax) dmax = (unsigned)track[c];
+    }
+    return dmax;
+}
+
+static void classify_with_dmax(const wpo_model* m, int T, const int16_t* seqs,
+                               const int32_t* offsets, const int32_t* ids,
+                               const int32_t* counts, int P, const int32_t* cand,
+                               int num_cand, const double* rad,
+                               double dist_cutoff, unsigned dmax,
+                               int32_t* out_id, double* out_score,
+                               double* out_total) {
+    /* classifiers/hmm-classifier.h:45-78 */
+    int best_i = -1;
+    double best_score = -1.0;
+    double total_score = 0.0;
+    int n = cand ? num_cand : P;
+    for (int k = 0; k < n; k++) {
+        int i = cand ? cand[k] : k;
+        double score = wpo_peptide_probability(
+                m, T, seqs + offsets[i], offsets[i + 1] - offsets[i], rad, dmax,
+                dist_cutoff, NULL, NULL);
+        total_score += score * counts[i];
+        if (score > best_score) {
+            best_score = score;
+            best_i = i;
+        }
+    }
+    double score = best_score, total = total_score;
+    if (isnan(score / total)) {
+        score = 0.0;
+        total = 1.0;
+    }
+    *out_id = best_i >= 0 ? ids[best_i] : -1;
+    *out_score = score;
+    *out_total = total;
+}
+
+void wpo_classify_one(const wpo_model* m, int T, const int16_t* seqs,
+                      const int32_t* offsets, const int32_t* ids,
+                      const int32_t* counts, int P, const int32_t* cand,
+                      int num_cand, const double* rad, double dist_cutoff,
+                      int32_t* out_id, double* out_score, double* out_total) {
+    unsigned dmax = max_num_dyes_of(m->num_channels, seqs, offsets, P, T);
+    classify_with_dmax(m, T, seqs, offsets, ids, counts, P, cand, num_cand, rad,
+                       dist_cutoff, dmax, out_id, out_score, out_total);
+}
+
+typedef struct {
+    const wpo_model* m;
+    int T;
+    const int16_t* seqs;
+    const int32_t* offsets;
+    const int32_t* ids;
+    const int32_t* counts;
+    int P;
+    const double* rads;
+    int R;
+    const int32_t* cand;
+    const int32_t* cand_off;
+    double dist_cutoff;
+    unsigned dmax;
+    int32_t* out_id;
+    double* out_score;
+    double* out_total;
+    double* out_logp; /* loglik_all mode when non-NULL */
+    int next;
+    pthread_mutex_t lock;
+} batch_job;
+
+static void* batch_worker(void* arg) {
+    batch_job* j = (batch_job*)arg;
+    int C = j->m->num_channels;
+    for (;;) {
+        pthread_mutex_lock(&j->lock);
+        int r = j->next++;
+        pthread_mutex_unlock(&j->lock);
+        if (r >= j->R) break;
+        const double* rad = j->rads + (long)r * j->T * C;
+        if (j->out_logp) {
+            for (int i = 0; i < j->P; i++) {
+                double lp;
+                wpo_peptide_probability(j->m, j->T, j->seqs + j->offsets[i],
+                                        j->offsets[i + 1] - j->offsets[i], rad,
+                                        j->dmax, j->dist_cutoff, &lp, NULL);
+                j->out_logp[(long)r * j->P + i] = lp;
+            }
+        } else {
+            const int32_t* cand = NULL;
+            int nc = 0;
+            if (j->cand) {
+                cand = j->cand + j->cand_off[r];
+                nc = j->cand_off[r + 1] - j->cand_off[r];
+            }
+            classify_with_dmax(j->m, j->T, j->seqs, j->offsets, j->ids, j->counts,
+                               j->P, cand, nc, rad, j->dist_cutoff, j->dmax,
+                               &j->out_id[r], &j->out_score[r], &j->out_total[r]);
+        }
+    }
+    return NULL;
+}
+
+static void run_batch(batch_job* j, int threads) {
+    if (threads < 1) threads = 1;
+    pthread_mutex_init(&j->lock, NULL);
+    j->next = 0;
+    pthread_t* th = (pthread_t*)calloc(threads, sizeof(pthread_t));
+    for (int i = 0; i < threads; i++) pthread_create(&th[i], NULL, batch_worker, j);
+    for (int i = 0; i < threads; i++) pthread_join(th[i], NULL);
+    free(th);
+    pthread_mutex_destroy(&j->lock);
+}
+
+void wpo_classify_batch(const wpo_model* m, int T, const int16_t* seqs,
+                        const int32_t* offsets, const int32_t* ids,
+                        const int32_t* counts, int P, const double* rads, int R,
+                        const int32_t* cand, const int32_t* cand_off,
+                        double dist_cutoff, int threads, int32_t* out_id,
+                        double* out_score, double* out_total) {
+    batch_job j;
+    memset(&j, 0, sizeof(j));
+    j.m = m;
+    j.T = T;
+    j.seqs = seqs;
+    j.offsets = offsets;
+    j.ids = ids;
+    j.counts = counts;
+    j.P = P;
+    j.rads = rads;
+    j.R = R;
+    j.cand = cand;
+    j.cand_off = cand_off;
+    j.dist_cutoff = dist_cutoff;
+    j.dmax = max_num_dyes_of(m->num_channels, seqs, offsets, P, T);
+    j.out_id = out_id;
+    j.out_score = out_score;
+    j.out_total = out_total;
+    run_batch(&j, threads);
+}
+
+void wpo_loglik_all(const wpo_model* m, int T, const int16_t* seqs,
+                    const int32_t* offsets, int P, const double* rads, int R,
+                    double dist_cutoff, int threads, double* out_logp) {
+    batch_job j;
+    memset(&j, 0, sizeof(j));
+    j.m = m;
+    j.T = T;
+    j.seqs = seqs;
+    j.offsets = offsets;
+    j.P = P;
+    j.rads = rads;
+    j.R = R;
+    j.dist_cutoff = dist_cutoff;
+    j.dmax = max_num_dyes_of(m->num_channels, seqs, offsets, P, T);
+    j.out_logp = out_logp;
+    run_batch(&j, threads);
+}

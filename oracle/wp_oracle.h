@@ -1,0 +1,144 @@
+/*
+ * wp_oracle.h -- CPU FP64 restatement of whatprot's peptide HMM.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker that the CUDA path
+ * is compared against.  Only tests/, __graft_entry__.smoke() and the CPU
+ * baseline leg of bench.py may load it; the product never links or calls it.
+ *
+ * It restates, in plain C and double precision, the algorithm of the
+ * reference's cc_code/src/hmm/ tree (step chain, KDRange pruning, forward,
+ * backward and Baum-Welch expected counts), cc_code/src/parameterization/model
+ * (channel model, decaying detach rate) and cc_code/src/classifiers/
+ * hmm-classifier.h (argmax + count-weighted total).  Each function cites the
+ * reference file:line it follows.  The range pruning is restated literally
+ * (prune_forward / prune_backward per step), not in closed form, so that the
+ * closed-form boxes used by the CUDA kernels can be checked against it.
+ *
+ * Parity pin: the five "no change" probabilities of the reference's
+ * cc_code/src/hmm/hmm/peptide-hmm.test.cc:188,227,266,305,344 and outputs of
+ * the reference itself compiled from source into oracle/_ref (see Makefile).
+ */
+#ifndef WP_ORACLE_H
+#define WP_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WPO_MAX_CHANNELS 8
+#define WPO_MAX_TIMESTEPS 64
+
+typedef struct {
+    int num_channels;
+    double p_edman_failure;
+    double p_detach;               /* DecayingRateModel.base */
+    double p_initial_detach;       /* DecayingRateModel.initial */
+    double p_initial_detach_decay; /* DecayingRateModel.initial_decay */
+    double p_initial_block;
+    double p_cyclic_block;
+    double p_bleach[WPO_MAX_CHANNELS];
+    double p_dud[WPO_MAX_CHANNELS];
+    double bg_sig[WPO_MAX_CHANNELS];
+    double mu[WPO_MAX_CHANNELS];
+    double sig[WPO_MAX_CHANNELS];
+    /* interactions[c][o]: multiplicative factor on channel c's mu per dye on
+     * channel o (1.0 = no interaction); flat_interactions likewise, applied
+     * once when channel o has any dye (self: when >1 dye). */
+    double interactions[WPO_MAX_CHANNELS][WPO_MAX_CHANNELS];
+    double flat_interactions[WPO_MAX_CHANNELS][WPO_MAX_CHANNELS];
+} wpo_model;
+
+/* Expected counts, one per fitted parameter (SequencingModelFitter). */
+typedef struct {
+    double edman_num, edman_den;
+    double detach_x[WPO_MAX_TIMESTEPS], detach_n[WPO_MAX_TIMESTEPS];
+    double init_block_num, init_block_den;
+    double cyc_block_num, cyc_block_den;
+    double bleach_num[WPO_MAX_CHANNELS], bleach_den[WPO_MAX_CHANNELS];
+    double dud_num[WPO_MAX_CHANNELS], dud_den[WPO_MAX_CHANNELS];
+} wpo_fit_sums;
+
+/* Channel model (channel-model.h:35-70, channel-model.cc:35-49). */
+double wpo_adjusted_mu(const wpo_model* m, int channel, const unsigned* counts);
+double wpo_sigma(const wpo_model* m, int channel, double amu);
+double wpo_pdf(const wpo_model* m, int channel, double observed,
+               const unsigned* counts);
+/* DecayingRateModel::operator[] (decaying-rate-model.cc:47-50). */
+double wpo_p_detach_at(const wpo_model* m, unsigned t);
+
+/* DyeTrack(T, C, dye_seq) (dye-track.cc:26-43).  out[t*C + c]. */
+void wpo_dye_track(int num_timesteps, int num_channels, const int16_t* seq,
+                   int length, int16_t* out);
+
+/* PeptideEmission pruned range for one timestep (peptide-emission.cc:50-163).
+ * rad is [T][C] (already divided by mu).  Writes [min, max) per channel.
+ * dist_cutoff >= DBL_MAX means "no pruning". */
+void wpo_emission_range(const wpo_model* m, const double* rad, int t,
+                        unsigned max_num_dyes, double dist_cutoff,
+                        unsigned* cmin, unsigned* cmax);
+
+/* PeptideHMM(...).probability() for one (radiometry, dye-seq) pair.
+ * Returns the reference's FP64 probability.  *log_p receives log(P) computed
+ * with exact power-of-two rescaling after every emission (no underflow);
+ * *visited_flops receives the visited-state operation count of the pruned
+ * schedule (emission 1, detach 2, binomial 2 per MAC, Edman 6, block 3 when
+ * p != 0, rescale 2 per state per timestep).  Either pointer may be NULL.
+ * max_num_dyes is the classifier-wide Dmax (hmm-classifier.cc:47-66). */
+double wpo_peptide_probability(const wpo_model* m, int num_timesteps,
+                               const int16_t* seq, int length,
+                               const double* rad, unsigned max_num_dyes,
+                               double dist_cutoff, double* log_p,
+                               double* visited_flops);
+
+/* The pruned ranges of one (radiometry, dye-seq) pair after both prune
+ * passes, flattened: for each emission t (0..T-1) the [min,max) per channel
+ * of its final pruned_range.  Returns 1 if the pruning emptied the range
+ * (probability 0), else 0.  lo/hi are [T][C]. */
+int wpo_pruned_emission_boxes(const wpo_model* m, int num_timesteps,
+                              const int16_t* seq, int length,
+                              const double* rad, unsigned max_num_dyes,
+                              double dist_cutoff, unsigned* lo, unsigned* hi);
+
+/* HMMClassifier::classify_helper (hmm-classifier.h:45-78) over a candidate
+ * list (all peptides when cand == NULL).  Peptides are given as a ragged
+ * array: seqs[offsets[i] .. offsets[i+1]).  Writes the id of the best
+ * peptide, its probability and the count-weighted total, with the reference's
+ * NaN patch. */
+void wpo_classify_one(const wpo_model* m, int num_timesteps,
+                      const int16_t* seqs, const int32_t* offsets,
+                      const int32_t* ids, const int32_t* counts,
+                      int num_peptides, const int32_t* cand, int num_cand,
+                      const double* rad, double dist_cutoff, int32_t* out_id,
+                      double* out_score, double* out_total);
+
+/* Batch over reads with `threads` worker threads (OpenMP-free, pthreads);
+ * rads is [R][T][C].  cand/cand_off may be NULL. */
+void wpo_classify_batch(const wpo_model* m, int num_timesteps,
+                        const int16_t* seqs, const int32_t* offsets,
+                        const int32_t* ids, const int32_t* counts,
+                        int num_peptides, const double* rads, int num_reads,
+                        const int32_t* cand, const int32_t* cand_off,
+                        double dist_cutoff, int threads, int32_t* out_id,
+                        double* out_score, double* out_total);
+
+/* log P for every (read, peptide) pair: out[r*P + p]. */
+void wpo_loglik_all(const wpo_model* m, int num_timesteps, const int16_t* seqs,
+                    const int32_t* offsets, int num_peptides,
+                    const double* rads, int num_reads, double dist_cutoff,
+                    int threads, double* out_logp);
+
+/* GenericHMM::improve_fit (generic-hmm.h:60-109) for one read: adds this
+ * read's expected counts into *sums (when P > 0) and returns P (reference
+ * FP64 value); *log_p receives log(P) from the rescaled computation. */
+double wpo_improve_fit(const wpo_model* m, int num_timesteps,
+                       const int16_t* seq, int length, const double* rad,
+                       unsigned max_num_dyes, double dist_cutoff,
+                       wpo_fit_sums* sums, double* log_p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WP_ORACLE_H */

@@ -1,0 +1,259 @@
+"""ctypes bindings to the checkers: oracle/liboracle.so (the C restatement)
+and, when it was built in this container, oracle/_ref/libwpref.so (the
+reference's own sources).  Test infrastructure only."""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+from typing import Optional
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(REPO, "oracle")
+ORACLE_SO = os.path.join(ORACLE_DIR, "liboracle.so")
+REF_SO = os.path.join(ORACLE_DIR, "_ref", "libwpref.so")
+DBL_MAX = sys.float_info.max
+
+MAXC = 8
+MAXT = 64
+
+
+class WpoModel(ctypes.Structure):
+    _fields_ = [("num_channels", ctypes.c_int),
+                ("p_edman_failure", ctypes.c_double),
+                ("p_detach", ctypes.c_double),
+                ("p_initial_detach", ctypes.c_double),
+                ("p_initial_detach_decay", ctypes.c_double),
+                ("p_initial_block", ctypes.c_double),
+                ("p_cyclic_block", ctypes.c_double),
+                ("p_bleach", ctypes.c_double * MAXC),
+                ("p_dud", ctypes.c_double * MAXC),
+                ("bg_sig", ctypes.c_double * MAXC),
+                ("mu", ctypes.c_double * MAXC),
+                ("sig", ctypes.c_double * MAXC),
+                ("interactions", (ctypes.c_double * MAXC) * MAXC),
+                ("flat_interactions", (ctypes.c_double * MAXC) * MAXC)]
+
+
+class WpoFitSums(ctypes.Structure):
+    _fields_ = [("edman_num", ctypes.c_double), ("edman_den", ctypes.c_double),
+                ("detach_x", ctypes.c_double * MAXT), ("detach_n", ctypes.c_double * MAXT),
+                ("init_block_num", ctypes.c_double), ("init_block_den", ctypes.c_double),
+                ("cyc_block_num", ctypes.c_double), ("cyc_block_den", ctypes.c_double),
+                ("bleach_num", ctypes.c_double * MAXC), ("bleach_den", ctypes.c_double * MAXC),
+                ("dud_num", ctypes.c_double * MAXC), ("dud_den", ctypes.c_double * MAXC)]
+
+    def as_dict(self, T, C):
+        return {
+            "edman": (self.edman_num, self.edman_den),
+            "detach_x": np.array(self.detach_x[: T - 1]),
+            "detach_n": np.array(self.detach_n[: T - 1]),
+            "init_block": (self.init_block_num, self.init_block_den),
+            "cyc_block": (self.cyc_block_num, self.cyc_block_den),
+            "bleach": (np.array(self.bleach_num[:C]), np.array(self.bleach_den[:C])),
+            "dud": (np.array(self.dud_num[:C]), np.array(self.dud_den[:C])),
+        }
+
+
+def to_wpo(sm) -> WpoModel:
+    m = WpoModel()
+    C = sm.num_channels
+    m.num_channels = C
+    m.p_edman_failure = sm.p_edman_failure
+    m.p_detach = sm.p_detach
+    m.p_initial_detach = sm.p_initial_detach
+    m.p_initial_detach_decay = sm.p_initial_detach_decay
+    m.p_initial_block = sm.p_initial_block
+    m.p_cyclic_block = sm.p_cyclic_block
+    for c, cm in enumerate(sm.channel_models):
+        m.p_bleach[c] = cm.p_bleach
+        m.p_dud[c] = cm.p_dud
+        m.bg_sig[c] = cm.bg_sig
+        m.mu[c] = cm.mu
+        m.sig[c] = cm.sig
+        for o in range(MAXC):
+            m.interactions[c][o] = cm.interactions[o] if o < C else 1.0
+            m.flat_interactions[c][o] = cm.flat_interactions[o] if o < C else 1.0
+    return m
+
+
+def build_oracle() -> None:
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR, "all"], check=True)
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+class Oracle:
+    def __init__(self):
+        if not os.path.exists(ORACLE_SO):
+            build_oracle()
+        self.lib = ctypes.CDLL(ORACLE_SO)
+        L = self.lib
+        L.wpo_peptide_probability.restype = ctypes.c_double
+        L.wpo_peptide_probability.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p,
+                                              ctypes.c_int, ctypes.c_void_p, ctypes.c_uint, ctypes.c_double,
+                                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        L.wpo_pruned_emission_boxes.restype = ctypes.c_int
+        L.wpo_pruned_emission_boxes.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p,
+                                                ctypes.c_int, ctypes.c_void_p, ctypes.c_uint,
+                                                ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
+        L.wpo_emission_range.restype = None
+        L.wpo_emission_range.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.c_uint, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
+        L.wpo_classify_batch.restype = None
+        L.wpo_classify_batch.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p]
+        L.wpo_loglik_all.restype = None
+        L.wpo_loglik_all.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                     ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
+        L.wpo_improve_fit.restype = ctypes.c_double
+        L.wpo_improve_fit.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p,
+                                      ctypes.c_int, ctypes.c_void_p, ctypes.c_uint, ctypes.c_double,
+                                      ctypes.POINTER(WpoFitSums), ctypes.POINTER(ctypes.c_double)]
+
+    def probability(self, sm, T, seq, rad, max_num_dyes, cutoff=DBL_MAX):
+        m = to_wpo(sm)
+        seq = np.ascontiguousarray(seq, dtype=np.int16)
+        rad = np.ascontiguousarray(rad, dtype=np.float64)
+        lp = ctypes.c_double()
+        fl = ctypes.c_double()
+        p = self.lib.wpo_peptide_probability(ctypes.byref(m), T, _p(seq) if len(seq) else None, len(seq),
+                                             _p(rad), max_num_dyes, cutoff, ctypes.byref(lp), ctypes.byref(fl))
+        return p, lp.value, fl.value
+
+    def pruned_boxes(self, sm, T, seq, rad, max_num_dyes, cutoff):
+        m = to_wpo(sm)
+        C = sm.num_channels
+        seq = np.ascontiguousarray(seq, dtype=np.int16)
+        rad = np.ascontiguousarray(rad, dtype=np.float64)
+        lo = np.zeros((T, C), np.uint32)
+        hi = np.zeros((T, C), np.uint32)
+        empty = self.lib.wpo_pruned_emission_boxes(ctypes.byref(m), T, _p(seq) if len(seq) else None,
+                                                   len(seq), _p(rad), max_num_dyes, cutoff, _p(lo), _p(hi))
+        return bool(empty), lo, hi
+
+    def emission_range(self, sm, rad, t, max_num_dyes, cutoff):
+        m = to_wpo(sm)
+        C = sm.num_channels
+        rad = np.ascontiguousarray(rad, dtype=np.float64)
+        lo = np.zeros(C, np.uint32)
+        hi = np.zeros(C, np.uint32)
+        self.lib.wpo_emission_range(ctypes.byref(m), _p(rad), t, max_num_dyes, cutoff, _p(lo), _p(hi))
+        return lo, hi
+
+    def classify(self, sm, T, dye_seqs, rads, cutoff=DBL_MAX, threads=8, cand=None, cand_off=None):
+        m = to_wpo(sm)
+        flat, off = dye_seqs.ragged()
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        R = rads.shape[0]
+        oid = np.zeros(R, np.int32)
+        osc = np.zeros(R, np.float64)
+        otot = np.zeros(R, np.float64)
+        ids = np.ascontiguousarray(dye_seqs.ids, np.int32)
+        cnt = np.ascontiguousarray(dye_seqs.counts, np.int32)
+        if cand is not None:
+            cand = np.ascontiguousarray(cand, np.int32)
+            cand_off = np.ascontiguousarray(cand_off, np.int32)
+        self.lib.wpo_classify_batch(ctypes.byref(m), T, _p(flat), _p(off), _p(ids), _p(cnt), len(dye_seqs),
+                                    _p(rads), R, _p(cand), _p(cand_off), cutoff, threads,
+                                    _p(oid), _p(osc), _p(otot))
+        return oid, osc, otot
+
+    def loglik_all(self, sm, T, dye_seqs, rads, cutoff=DBL_MAX, threads=8):
+        m = to_wpo(sm)
+        flat, off = dye_seqs.ragged()
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        R = rads.shape[0]
+        out = np.zeros((R, len(dye_seqs)), np.float64)
+        self.lib.wpo_loglik_all(ctypes.byref(m), T, _p(flat), _p(off), len(dye_seqs), _p(rads), R,
+                                cutoff, threads, _p(out))
+        return out
+
+    def improve_fit(self, sm, T, seq, rad, max_num_dyes, cutoff=DBL_MAX, sums=None):
+        m = to_wpo(sm)
+        seq = np.ascontiguousarray(seq, dtype=np.int16)
+        rad = np.ascontiguousarray(rad, dtype=np.float64)
+        if sums is None:
+            sums = WpoFitSums()
+        lp = ctypes.c_double()
+        p = self.lib.wpo_improve_fit(ctypes.byref(m), T, _p(seq) if len(seq) else None, len(seq), _p(rad),
+                                     max_num_dyes, cutoff, ctypes.byref(sums), ctypes.byref(lp))
+        return p, lp.value, sums
+
+
+class Reference:
+    """The reference's own classes, compiled from its sources (oracle/_ref)."""
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.exists(REF_SO)
+
+    def __init__(self):
+        self.lib = ctypes.CDLL(REF_SO)
+        L = self.lib
+        L.ref_peptide_probability.restype = ctypes.c_double
+        L.ref_peptide_probability.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_char_p,
+                                              ctypes.c_void_p, ctypes.c_uint, ctypes.c_double]
+        L.ref_classify.restype = None
+        L.ref_classify.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(ctypes.c_char_p), ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_int, ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.POINTER(ctypes.c_double)]
+        L.ref_improve_fit.restype = ctypes.c_double
+        L.ref_improve_fit.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_char_p,
+                                      ctypes.c_void_p, ctypes.c_uint, ctypes.c_double,
+                                      ctypes.POINTER(WpoFitSums)]
+        L.ref_fit.restype = ctypes.c_double
+        L.ref_fit.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
+                              ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.POINTER(WpoModel),
+                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+
+    def probability(self, sm, T, seq_str, rad, max_num_dyes, cutoff=DBL_MAX):
+        m = to_wpo(sm)
+        rad = np.ascontiguousarray(rad, dtype=np.float64)
+        return self.lib.ref_peptide_probability(ctypes.byref(m), T, seq_str.encode(), _p(rad),
+                                                max_num_dyes, cutoff)
+
+    def classify(self, sm, T, dye_seqs, rads, cutoff=DBL_MAX, threads=8):
+        m = to_wpo(sm)
+        strs = [s.encode() for s in dye_seqs.strings()]
+        arr = (ctypes.c_char_p * len(strs))(*strs)
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        R = rads.shape[0]
+        oid = np.zeros(R, np.int32)
+        osc = np.zeros(R, np.float64)
+        otot = np.zeros(R, np.float64)
+        secs = ctypes.c_double()
+        ids = np.ascontiguousarray(dye_seqs.ids, np.int32)
+        cnt = np.ascontiguousarray(dye_seqs.counts, np.int32)
+        self.lib.ref_classify(ctypes.byref(m), T, len(strs), arr, _p(ids), _p(cnt), R, _p(rads), cutoff,
+                              threads, _p(oid), _p(osc), _p(otot), ctypes.byref(secs))
+        return oid, osc, otot, secs.value
+
+    def improve_fit(self, sm, T, seq_str, rad, max_num_dyes, cutoff=DBL_MAX):
+        m = to_wpo(sm)
+        rad = np.ascontiguousarray(rad, dtype=np.float64)
+        sums = WpoFitSums()
+        p = self.lib.ref_improve_fit(ctypes.byref(m), T, seq_str.encode(), _p(rad), max_num_dyes,
+                                     cutoff, ctypes.byref(sums))
+        return p, sums
+
+    def fit(self, sm, T, seq_str, rads, threshold, max_runtime=1e9):
+        m = to_wpo(sm)
+        out = WpoModel()
+        step = ctypes.c_double()
+        secs = ctypes.c_double()
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        ll = self.lib.ref_fit(ctypes.byref(m), T, seq_str.encode(), rads.shape[0], _p(rads), threshold,
+                              max_runtime, ctypes.byref(out), ctypes.byref(step), ctypes.byref(secs))
+        return out, ll, step.value, secs.value
