@@ -1,0 +1,309 @@
+#!/usr/bin/env python
+"""Benchmark: HMM read x peptide forwards per second on one GB300.
+
+Workload (the batched persistent-HMM configuration): 3 channels, 16
+timesteps (1 mock + 15 Edman cycles), 1,000 dye-seqs of length 8-30 with at
+most 5 dyes per channel and at least one dye, 100,000 simulated reads, HMM
+pruning cutoff 5 sigma; error model p_edman_failure 0.06, p_detach 0.05,
+p_bleach 0.05, p_dud 0.07, intensity ~ N(n, sqrt(0.00667^2 + n 0.16^2)).
+Inputs come from the package's seeded simulator (synthetic data).
+
+A step is one `classify hmm` pass over the batch: 100,000 x 1,000 =
+1e8 (read, peptide) forwards, argmax and count-weighted totals per read.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` is measured with the reads already in
+device memory (CUDA events on the library's stream, L2 flushed between
+steps); `e2e` is the same metric through the public C ABI call with host
+buffers (pinned), host->device copy and result read-back inside the timed
+region; `roofline` reports the forward kernel's algorithmic FP32 work (the
+reference's pruned visited-state op count) per unit time against the
+device's measured FP32 FMA throughput; `cpu_baseline` times the CPU oracle
+(a restatement of the reference's algorithm) on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "HMM read x peptide forwards/s (classify hmm, -p 5)"
+UNIT = "fwd/s"
+T, C, P, READS, CUTOFF = 16, 3, 1000, 100_000, 5.0
+WORKLOAD = ("classify hmm: 3 channels x 16 timesteps, 1000 dye-seqs (8-30 positions, <=5 dyes "
+            "per channel, >=1 dye), 100000 reads float64 [100000,16,3], pruning 5 sigma")
+
+
+def make_data(seed: int, reads: int):
+    from whatprot_gb300.simulate import paper_model, random_dye_seqs, simulate_radiometries
+    sm = paper_model(C)
+    ds = random_dye_seqs(P, C, 8, 30, max_per_channel=5, min_total=1, seed=1234)
+    rads, ids = simulate_radiometries(sm, ds, T, int(reads * 1.15) + 64, seed=seed)
+    return sm, ds, rads[:reads].copy(), ids[:reads].copy()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def cpu_baseline(sm, ds, rads, seconds_target=15.0):
+    """Time the CPU oracle (a restatement of the reference's algorithm,
+    pthreads over reads) on a bounded sample of the same workload."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from oracle_lib import Oracle
+    threads = os.cpu_count() or 1
+    o = Oracle()
+    n = max(threads, 16)
+    t0 = time.perf_counter()
+    o.classify(sm, T, ds, rads[:n], CUTOFF, threads=threads)
+    dt = time.perf_counter() - t0
+    # grow the sample to about seconds_target of work
+    n2 = int(min(len(rads), max(n, n * seconds_target / max(dt, 1e-3))))
+    t0 = time.perf_counter()
+    o.classify(sm, T, ds, rads[:n2], CUTOFF, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n2 * len(ds) / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n2} reads x {len(ds)} dye-seqs of the same workload, "
+                      f"{dt:.1f} s, oracle/wp_oracle.c with {threads} threads"}
+
+
+def run_reference(args):
+    """The reference's CPU implementation of the path, timed on the host:
+    oracle/_ref (the reference's own sources) when it was built for this
+    machine, else the oracle port; all host threads; each step classifies a
+    bounded sample of the workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib
+    sm, ds, rads, _ = make_data(seed=99, reads=4096)
+    threads = os.cpu_count() or 1
+    kind = "port"
+    runner = None
+    if oracle_lib.Reference.available():
+        try:
+            ref = oracle_lib.Reference()
+            kind = "reference"
+
+            def runner(x):
+                ref.classify(sm, T, ds, x, CUTOFF, threads=threads)
+        except OSError:
+            runner = None
+    if runner is None:
+        o = oracle_lib.Oracle()
+
+        def runner(x):
+            o.classify(sm, T, ds, x, CUTOFF, threads=threads)
+    # size a step to about 8 s of CPU work
+    n = max(threads * 2, 32)
+    t0 = time.perf_counter()
+    runner(rads[:n])
+    dt = time.perf_counter() - t0
+    n = int(min(len(rads), max(n, n * 8.0 / max(dt, 1e-3))))
+    for _ in range(args.warmup):
+        runner(rads[:n])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        runner(rads[:n])
+    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    value = n * len(ds) / dt
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded simulator)",
+            "config": {"workload": WORKLOAD, "sample_reads_per_step": n, "peptides": len(ds)},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": f"{n} reads x {len(ds)} dye-seqs per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--reads", type=int, default=READS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    from whatprot_gb300 import capi
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sm, ds, rads, _ = make_data(seed=2024 + rank, reads=args.reads)
+    R = rads.shape[0]
+    ctx = capi.Context(local)
+    ctx.upload_model(sm, T)
+    ctx.upload_peptides(ds)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=torch.device("cuda", local))
+    d_rads = torch.from_numpy(rads).to(f"cuda:{local}")
+    d_id = torch.empty(R, dtype=torch.int32, device=f"cuda:{local}")
+    d_sc = torch.empty(R, dtype=torch.float64, device=f"cuda:{local}")
+    d_tot = torch.empty(R, dtype=torch.float64, device=f"cuda:{local}")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    def step_device():
+        ctx.classify_device(d_rads.data_ptr(), R, CUTOFF, d_id.data_ptr(), d_sc.data_ptr(),
+                            d_tot.data_ptr(), async_=True)
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    stream.synchronize()
+
+    algo_flops = ctx.count_flops(rads, CUTOFF)  # per step, outside the timed region
+    ctx.timing_enable(True)
+    launches0 = ctx.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)  # evict L2 (129 MB) between steps, outside the events
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        step_device()
+        ev1.record(stream)
+        ev1.synchronize()
+        total_ms += ev0.elapsed_time(ev1)
+    barrier()
+    clk = clocks.stop()
+    launches = ctx.launch_count() - launches0
+    fwd_ms, fwd_n = ctx.timing_read(ctx.KIND_FORWARD)
+    prep_ms, _ = ctx.timing_read(ctx.KIND_PREP)
+    ctx.timing_enable(False)
+    t_step = total_ms / args.steps
+    if dist:
+        t = torch.tensor([t_step], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+    pairs = float(R) * len(ds)
+    value = pairs * world / (t_step * 1e-3)
+
+    # End to end through the public API with host (pinned) buffers.
+    h_rads = torch.from_numpy(rads).pin_memory()
+    h_np = h_rads.numpy()
+    for _ in range(1):
+        ctx.classify(h_np, CUTOFF)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.classify(h_np, CUTOFF)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": pairs * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(rads.nbytes),
+           "d2h_bytes_per_step": int(R * (4 + 8 + 8 + 8))}
+
+    peak = ctx.fp32_peak_tflops()
+    fwd_avg_ms = fwd_ms / max(fwd_n, 1)
+    flops_per_launch = algo_flops * args.steps / max(fwd_n, 1)
+    achieved = flops_per_launch / (fwd_avg_ms * 1e-3) / 1e12 if fwd_n else None
+    roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if (achieved and peak) else None, "traffic": None,
+                "kernel": "wp_forward_kernel",
+                "peak_source": "FP32 FMA loop measured live (wp_probe_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
+                "algorithmic_flops_per_step": algo_flops,
+                "forward_ms_per_step": fwd_ms / args.steps, "prep_ms_per_step": prep_ms / args.steps,
+                "forward_launches_per_step": fwd_n / args.steps}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded simulator)",
+            "config": {"workload": WORKLOAD, "reads": R, "peptides": len(ds), "timesteps": T,
+                       "channels": C, "dist_cutoff": CUTOFF, "pairs_per_step": pairs,
+                       "l2": "flushed between steps (512 MB write)"},
+            "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(sm, ds, rads)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

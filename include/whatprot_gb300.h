@@ -1,0 +1,167 @@
+/*
+ * whatprot_gb300.h -- C ABI of the GB300 (sm_103a) peptide-HMM engine.
+ *
+ * This is the drop-in boundary for whatprot's classification and fitting hot
+ * path.  Plain C types only: callers own every buffer they pass; nothing here
+ * throws; every call returns a wp_status.  One wp_ctx per host thread (calls
+ * on one context are serialised by an internal mutex).
+ *
+ * Each entry point names the reference interface it replaces (paths are
+ * relative to the reference project's cc_code/src/).
+ */
+#ifndef WHATPROT_GB300_H
+#define WHATPROT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int wp_status;
+enum {
+    WP_OK = 0,
+    WP_ERR_INVALID = 1,     /* bad argument (null pointer, size out of range) */
+    WP_ERR_OOM = 2,         /* device or host allocation failed */
+    WP_ERR_CUDA = 3,        /* a CUDA call failed; see wp_last_error */
+    WP_ERR_TIMEOUT = 4,     /* a bounded device wait expired */
+    WP_ERR_UNSUPPORTED = 5, /* shape beyond this build's limits */
+    WP_ERR_STATE = 6        /* model or peptides not uploaded yet */
+};
+
+/* Limits of this build (checked; WP_ERR_UNSUPPORTED beyond them). */
+#define WP_MAX_CHANNELS 4
+#define WP_MAX_TIMESTEPS 64
+#define WP_MAX_DYES_PER_CHANNEL 15
+
+typedef struct wp_ctx wp_ctx;
+
+/* Sequencing model, already divided by mu (SequencingModel::with_mu_as_one,
+ * parameterization/model/sequencing-model.cc:140-151).  Per-channel arrays
+ * have num_channels entries; interactions / flat_interactions are
+ * [num_channels][num_channels] row-major: row c is channel c's model, entry o
+ * the multiplicative factor for dyes on channel o (1.0 = none), as
+ * ChannelModel::interactions / flat_interactions (channel-model.h:35-54).
+ * Either interaction pointer may be NULL (all 1.0). */
+typedef struct {
+    int num_channels;
+    double p_edman_failure;
+    double p_detach;               /* DecayingRateModel base    */
+    double p_initial_detach;       /* DecayingRateModel initial */
+    double p_initial_detach_decay; /* DecayingRateModel initial_decay */
+    double p_initial_block;
+    double p_cyclic_block;
+    const double* p_bleach;
+    const double* p_dud;
+    const double* bg_sig;
+    const double* mu;
+    const double* sig;
+    const double* interactions;
+    const double* flat_interactions;
+} wp_seq_model;
+
+/* Baum-Welch expected counts of one E-step, the fields of
+ * SequencingModelFitter (parameterization/fit/sequencing-model-fitter.h):
+ * numerator/denominator per fitted parameter, detach per timestep. */
+typedef struct {
+    double p_edman_failure_num, p_edman_failure_den;
+    double p_detach_x[WP_MAX_TIMESTEPS], p_detach_n[WP_MAX_TIMESTEPS];
+    double p_initial_block_num, p_initial_block_den;
+    double p_cyclic_block_num, p_cyclic_block_den;
+    double p_bleach_num[WP_MAX_CHANNELS], p_bleach_den[WP_MAX_CHANNELS];
+    double p_dud_num[WP_MAX_CHANNELS], p_dud_den[WP_MAX_CHANNELS];
+} wp_fit_sums;
+
+/* Context on one CUDA device.  Replaces nothing in the reference (which has
+ * no device); it owns the stream, the uploaded model and peptide tables. */
+wp_status wp_ctx_create(wp_ctx** out, int device);
+void wp_ctx_destroy(wp_ctx* ctx);
+/* Message of the last failed call on this context ("" if none). */
+const char* wp_last_error(const wp_ctx* ctx);
+
+/* Upload the model for num_timesteps.  Replaces the model part of
+ * UniversalPrecomputations (hmm/precomputations/universal-precomputations.cc:
+ * 23-59: binomial dud/bleach tables, per-timestep detach rates) and the
+ * SequencingModel the classifier holds (classifiers/hmm-classifier.h:32-37). */
+wp_status wp_model_upload(wp_ctx* ctx, const wp_seq_model* model,
+                          int num_timesteps);
+
+/* Upload the peptide (dye-seq) set.  Replaces DyeSeqPrecomputations per
+ * dye-seq (hmm/precomputations/dye-seq-precomputations.cc:20-39) and the
+ * HMMClassifier's dye_seqs / max_num_dyes (classifiers/hmm-classifier.cc:
+ * 35-67).  dye_seqs is ragged: peptide i is dye_seqs[offsets[i] ..
+ * offsets[i+1]), entries -1 (unlabeled) or a channel index, trailing -1
+ * already trimmed or not (trimming does not change results).  ids[i] is the
+ * peptide id written to predictions, counts[i] its multiplicity. */
+wp_status wp_peptides_upload(wp_ctx* ctx, const int16_t* dye_seqs,
+                             const int32_t* offsets, const int32_t* ids,
+                             const int32_t* counts, int num_peptides);
+
+/* Classify reads.  Replaces HMMClassifier::classify(vector<Radiometry>)
+ * (classifiers/hmm-classifier.cc:84-93) and, with candidates,
+ * HMMClassifier::classify(radiometry, candidate_indices) (:79-82).
+ * rads: [num_reads][T][C] host doubles, already divided by mu
+ * (io/radiometries-io.cc:50-51).  dist_cutoff is SequencingSettings::
+ * dist_cutoff (DBL_MAX: no pruning).  cand / cand_off: optional ragged
+ * candidate peptide indices per read (cand_off has num_reads+1 entries);
+ * NULL means all peptides.  Outputs per read: id of the best peptide (first
+ * in candidate order on ties), its probability and the count-weighted total,
+ * with the reference's NaN patch (classifiers/hmm-classifier.h:73-76).  When
+ * the best probability is below the double range, score and total are both
+ * scaled by the same power of two so that score/total stays exact.
+ * out_log_score (nullable) receives log(P_best). */
+wp_status wp_hmm_classify(wp_ctx* ctx, const double* rads, int num_reads,
+                          double dist_cutoff, const int32_t* cand,
+                          const int32_t* cand_off, int32_t* out_id,
+                          double* out_score, double* out_total,
+                          double* out_log_score);
+
+/* Same as wp_hmm_classify with inputs and outputs already in device memory
+ * (d_rads: [num_reads][T][C] doubles; d_cand/d_cand_off as above or NULL;
+ * outputs device arrays).  Runs on the context's stream; returns after the
+ * launches are queued when `async` is nonzero, else after completion. */
+wp_status wp_hmm_classify_device(wp_ctx* ctx, const double* d_rads,
+                                 int num_reads, double dist_cutoff,
+                                 int32_t* d_out_id, double* d_out_score,
+                                 double* d_out_total, int async);
+
+/* log P for every (read, peptide) pair: out_logp[r * P + p] (host), -inf
+ * where P == 0.  PeptideHMM::probability (hmm/hmm/peptide-hmm.cc:94-100),
+ * per pair, computed in FP32 with exact power-of-two rescaling. */
+wp_status wp_hmm_loglik_all(wp_ctx* ctx, const double* rads, int num_reads,
+                            double dist_cutoff, double* out_logp);
+
+/* Algorithmic work of the pruned schedule: the number of visited-state
+ * operations the reference's pruned step chain performs for every (read,
+ * peptide) pair of this batch (emission 1, detach 2, binomial 2 per
+ * multiply-add, Edman 6, block 3 when its rate is nonzero, rescale 2 per
+ * state per timestep), summed.  Device-computed from the closed-form boxes. */
+wp_status wp_hmm_count_flops(wp_ctx* ctx, const double* rads, int num_reads,
+                             double dist_cutoff, double* out_flops);
+
+/* Kernel launches issued by this context since creation (all kinds). */
+long long wp_launch_count(const wp_ctx* ctx);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or events against it.  No reference counterpart. */
+void* wp_ctx_stream(const wp_ctx* ctx);
+
+/* Per-kernel timing with CUDA events recorded on the context's stream around
+ * every launch while enabled.  kind: 0 forward, 1 prep, 2 combine, 3 flop
+ * count.  wp_timing_read synchronises and returns the summed duration in ms
+ * and the number of launches since the last enable.  No reference
+ * counterpart (the reference only prints phase wall times,
+ * main/cmd-line-out.cc). */
+wp_status wp_timing_enable(wp_ctx* ctx, int enable);
+wp_status wp_timing_read(wp_ctx* ctx, int kind, double* total_ms, long long* launches);
+
+/* Measured FP32 fused-multiply-add throughput of the context's device in
+ * TFLOP/s (2 flops per FMA), from a timed loop of independent FMA chains on
+ * every SM.  The denominator of the forward kernel's roofline. */
+wp_status wp_probe_fp32_peak(wp_ctx* ctx, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WHATPROT_GB300_H */

@@ -229,9 +229,17 @@ void wpo_emission_range(const wpo_model* m, const double* rad, int t,
     }
     unsigned counts_lo[WPO_MAX_CHANNELS] = {0};
     unsigned counts_hi[WPO_MAX_CHANNELS] = {0};
+    /* The reference iterates to a fixed point without a bound; for
+     * intensities below about -0.5 mu the iteration cycles forever (e.g.
+     * counts 0 -> max+1 -> 1 -> 0 ...).  Both this restatement and the CUDA
+     * prep kernel stop after 1000 rounds, so they agree on
+     * such inputs; on every input where the reference terminates they
+     * perform the same iterations. */
     int did_change = 1;
-    while (did_change) {
+    int rounds = 0;
+    while (did_change && rounds < 1000) {
         did_change = 0;
+        rounds++;
         for (int c = 0; c < C; c++) {
             double old_counts_hi_c = counts_hi[c];
             counts_hi[c] = 1;

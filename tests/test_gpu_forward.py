@@ -1,0 +1,196 @@
+"""Parity of the CUDA forward pass (through the C ABI) with the oracle and
+with fixtures recorded from the reference.
+
+Tolerance: the kernels compute in FP32 with exact power-of-two rescaling; a
+probability P is accepted when |log P_gpu - log P_oracle| <= 1e-5 (relative
+error 1e-5 on P), and exact zeros (pruned-empty pairs) must be exact zeros.
+Top-1 ids must be identical except where the reference's own best and
+second-best scores tie within 1e-5."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import load_fixture
+from oracle_lib import DBL_MAX
+from whatprot_gb300 import capi
+from whatprot_gb300.model import DyeSeqSet, SequencingModel, parse_dye_seq
+from whatprot_gb300.simulate import paper_model, random_dye_seqs, simulate_radiometries
+
+pytestmark = pytest.mark.gpu
+LOG_TOL = 1e-5
+
+
+def assert_logp_close(gpu, ora, what=""):
+    fin = np.isfinite(ora)
+    assert np.array_equal(np.isfinite(gpu), fin), f"{what}: zero pattern differs " \
+        f"({np.sum(np.isfinite(gpu) != fin)} pairs)"
+    if np.any(fin):
+        err = np.max(np.abs(gpu[fin] - ora[fin]))
+        assert err <= LOG_TOL, f"{what}: max |dlogP| {err}"
+
+
+def test_goldens_on_gpu(gpu_ctx, goldens):
+    sm = SequencingModel.from_json(goldens["model"])
+    T = goldens["num_timesteps"]
+    ds = DyeSeqSet(2, [parse_dye_seq(goldens["dye_seq"])], np.array([0], np.int32),
+                   np.array([1], np.int32))
+    gpu_ctx.upload_model(sm, T)
+    gpu_ctx.upload_peptides(ds)
+    for case in goldens["cases"]:
+        cut = DBL_MAX if case["dist_cutoff"] is None else case["dist_cutoff"]
+        lp = gpu_ctx.loglik_all(np.array([case["rad"]]), cut)[0, 0]
+        exp = case["expected"]
+        if exp == 0.0:
+            assert lp == -np.inf, case["name"]
+        else:
+            assert abs(lp - math.log(exp)) <= LOG_TOL, (case["name"], lp, math.log(exp))
+
+
+def _model(C, block=False, inter=False, detach_decay=False):
+    sm = paper_model(C)
+    if block:
+        sm.p_initial_block, sm.p_cyclic_block = 0.07, 0.025
+    if detach_decay:
+        sm.p_initial_detach, sm.p_initial_detach_decay = 0.03, 0.04
+    if inter and C > 1:
+        sm.channel_models[0].interactions[1] = 0.9
+        sm.channel_models[1].flat_interactions[0] = 0.95
+        sm.channel_models[C - 1].interactions[C - 1] = 0.93
+    return sm
+
+
+CASES = [
+    # C, T, P, lmin, lmax, maxc, reads, cutoff, block, inter, decay
+    (2, 8, 40, 6, 12, None, 40, 5.0, False, False, False),
+    (2, 8, 40, 6, 12, None, 30, DBL_MAX, False, False, False),
+    (3, 16, 40, 8, 30, 5, 30, 5.0, False, False, False),
+    (3, 12, 25, 8, 20, 4, 20, DBL_MAX, True, False, True),
+    (3, 10, 25, 6, 18, 4, 20, 5.0, True, True, True),
+    (2, 9, 20, 6, 14, 4, 20, 3.0, False, True, False),
+    (1, 6, 15, 3, 12, 6, 20, 5.0, False, False, True),
+    (4, 6, 20, 6, 16, 3, 15, 5.0, False, False, False),
+    (2, 1, 10, 2, 8, None, 10, 5.0, True, False, False),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[f"C{c[0]}T{c[1]}cut{c[7] if c[7] != DBL_MAX else 'inf'}"
+                                             f"{'B' if c[8] else ''}{'I' if c[9] else ''}" for c in CASES])
+def test_loglik_all_vs_oracle(gpu_ctx, oracle, case):
+    C, T, P, lmin, lmax, maxc, nreads, cut, block, inter, decay = case
+    sm = _model(C, block, inter, decay)
+    ds = random_dye_seqs(P, C, lmin, lmax, max_per_channel=maxc, seed=C * 31 + T)
+    rads, _ = simulate_radiometries(sm, ds, T, nreads, seed=C * 17 + T)
+    gpu_ctx.upload_model(sm, T)
+    gpu_ctx.upload_peptides(ds)
+    g = gpu_ctx.loglik_all(rads, cut)
+    o = oracle.loglik_all(sm, T, ds, rads, cut, threads=8)
+    assert_logp_close(g, o, str(case))
+
+
+def test_wide_extents_and_big_states(gpu_ctx, oracle):
+    # Up to 11 dyes on one channel (binomial path for W > 8) and states of
+    # several hundred per Edman slice (larger shape buckets).
+    sm = _model(2)
+    seqs = [parse_dye_seq("0" * 11 + ".1.1"), parse_dye_seq("..0.0.1.1.1.0"),
+            parse_dye_seq("1" * 9 + "0" * 9), parse_dye_seq("."), parse_dye_seq("0")]
+    ds = DyeSeqSet(2, seqs, np.arange(5, dtype=np.int32), np.ones(5, np.int32))
+    rads, _ = simulate_radiometries(sm, ds, 7, 12, seed=3)
+    gpu_ctx.upload_model(sm, 7)
+    gpu_ctx.upload_peptides(ds)
+    for cut in (5.0, DBL_MAX):
+        g = gpu_ctx.loglik_all(rads, cut)
+        o = oracle.loglik_all(sm, 7, ds, rads, cut, threads=8)
+        assert_logp_close(g, o, f"wide cut={cut}")
+
+
+def _tie_ok(ref_scores_all, i):
+    s = np.sort(ref_scores_all[i])[::-1]
+    return len(s) > 1 and s[0] > 0 and abs(s[0] - s[1]) <= 1e-5 * s[0]
+
+
+@pytest.mark.parametrize("name", ["classify_c2_t8.npz", "classify_c3_t16.npz",
+                                  "classify_c2_t6_block_nocut.npz"])
+def test_classify_vs_reference_fixture(gpu_ctx, oracle, name):
+    z, ds = load_fixture(name)
+    C, T = int(z["C"]), int(z["T"])
+    sm = _model(C, block=bool(z["block"]), detach_decay=bool(z["block"]))
+    cut = DBL_MAX if np.isnan(z["cutoff"]) else float(z["cutoff"])
+    gpu_ctx.upload_model(sm, T)
+    gpu_ctx.upload_peptides(ds)
+    ids, sc, tot, _ = gpu_ctx.classify(z["rads"], cut)
+    ref_adj = z["ref_score"] / z["ref_total"]
+    adj = sc / tot
+    mism = np.nonzero(ids != z["ref_id"])[0]
+    if len(mism):
+        allp = np.exp(oracle.loglik_all(sm, T, ds, z["rads"][mism], cut, threads=8))
+        for k, i in enumerate(mism):
+            assert _tie_ok(allp, k), f"read {i}: gpu {ids[i]} ref {z['ref_id'][i]}"
+    np.testing.assert_allclose(adj, ref_adj, rtol=1e-5, atol=1e-300)
+
+
+def test_classify_candidates_vs_oracle(gpu_ctx, oracle):
+    sm = _model(3)
+    ds = random_dye_seqs(60, 3, 8, 24, max_per_channel=5, min_total=1, seed=5)
+    rads, _ = simulate_radiometries(sm, ds, 12, 30, seed=6)
+    rng = np.random.default_rng(7)
+    cands = [rng.permutation(60)[: rng.integers(1, 25)] for _ in range(rads.shape[0])]
+    cands[3] = np.array([5, 5, 5], np.int32)  # duplicates: first position wins
+    cand_off = np.zeros(len(cands) + 1, np.int32)
+    for i, c in enumerate(cands):
+        cand_off[i + 1] = cand_off[i] + len(c)
+    cand = np.concatenate(cands).astype(np.int32)
+    gpu_ctx.upload_model(sm, 12)
+    gpu_ctx.upload_peptides(ds)
+    ids, sc, tot, _ = gpu_ctx.classify(rads, 5.0, cand, cand_off)
+    oid, osc, otot = oracle.classify(sm, 12, ds, rads, 5.0, threads=8, cand=cand, cand_off=cand_off)
+    assert np.array_equal(ids, oid)
+    np.testing.assert_allclose(sc / tot, osc / otot, rtol=1e-5)
+
+
+def test_flop_count_matches_oracle(gpu_ctx, oracle):
+    for C, T, block in ((2, 8, False), (3, 10, True)):
+        sm = _model(C, block=block)
+        ds = random_dye_seqs(20, C, 6, 16, max_per_channel=4, seed=C + T)
+        rads, _ = simulate_radiometries(sm, ds, T, 12, seed=C * T)
+        gpu_ctx.upload_model(sm, T)
+        gpu_ctx.upload_peptides(ds)
+        dmax = ds.max_num_dyes(T)
+        for cut in (5.0, DBL_MAX):
+            want = 0.0
+            for i in range(rads.shape[0]):
+                for j in range(len(ds)):
+                    _, _, fl = oracle.probability(sm, T, ds.seqs[j], rads[i], dmax, cut)
+                    want += fl
+            got = gpu_ctx.count_flops(rads, cut)
+            assert got == want, (C, T, cut, got, want)
+
+
+def test_empty_inputs_and_errors(gpu_ctx):
+    sm = _model(2)
+    ds = random_dye_seqs(5, 2, 4, 8, seed=1)
+    gpu_ctx.upload_model(sm, 5)
+    gpu_ctx.upload_peptides(ds)
+    ids, sc, tot, _ = gpu_ctx.classify(np.zeros((0, 5, 2)), 5.0)
+    assert len(ids) == 0
+    # A read far from every peptide: all probabilities zero -> NaN patch.
+    far = np.full((1, 5, 2), 40.0)
+    ids, sc, tot, _ = gpu_ctx.classify(far, 5.0)
+    assert sc[0] == 0.0 and tot[0] == 1.0 and ids[0] == ds.ids[0]
+    # Channel index beyond the model's channels is rejected.
+    bad = DyeSeqSet(2, [np.array([0, 2], np.int16)], np.array([0], np.int32), np.array([1], np.int32))
+    gpu_ctx.upload_peptides(bad)
+    with pytest.raises(capi.WpError):
+        gpu_ctx.classify(np.zeros((1, 5, 2)), 5.0)
+
+
+def test_determinism(gpu_ctx):
+    sm = _model(3)
+    ds = random_dye_seqs(80, 3, 8, 24, max_per_channel=5, min_total=1, seed=8)
+    rads, _ = simulate_radiometries(sm, ds, 16, 50, seed=9)
+    gpu_ctx.upload_model(sm, 16)
+    gpu_ctx.upload_peptides(ds)
+    a = gpu_ctx.classify(rads, 5.0)
+    b = gpu_ctx.classify(rads, 5.0)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)

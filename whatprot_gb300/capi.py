@@ -1,0 +1,271 @@
+"""ctypes binding of the C ABI (include/whatprot_gb300.h).
+
+Loading fails loudly when the CUDA library has not been built: there is no
+CPU fallback.  Build it with ``python -c "import __graft_entry__ as g;
+g.build()"`` or ``python whatprot_gb300/build.py``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+from typing import Optional, Tuple
+
+import numpy as np
+
+from .model import DyeSeqSet, SequencingModel
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libwhatprot_gb300.so")
+DBL_MAX = sys.float_info.max
+
+WP_MAX_CHANNELS = 4
+WP_MAX_TIMESTEPS = 64
+
+STATUS = {0: "WP_OK", 1: "WP_ERR_INVALID", 2: "WP_ERR_OOM", 3: "WP_ERR_CUDA",
+          4: "WP_ERR_TIMEOUT", 5: "WP_ERR_UNSUPPORTED", 6: "WP_ERR_STATE"}
+
+EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload",
+           "wp_peptides_upload", "wp_hmm_classify", "wp_hmm_classify_device",
+           "wp_hmm_loglik_all", "wp_hmm_count_flops", "wp_launch_count", "wp_ctx_stream",
+           "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak"]
+
+
+class WpSeqModel(ctypes.Structure):
+    _fields_ = [("num_channels", ctypes.c_int),
+                ("p_edman_failure", ctypes.c_double),
+                ("p_detach", ctypes.c_double),
+                ("p_initial_detach", ctypes.c_double),
+                ("p_initial_detach_decay", ctypes.c_double),
+                ("p_initial_block", ctypes.c_double),
+                ("p_cyclic_block", ctypes.c_double),
+                ("p_bleach", ctypes.c_void_p),
+                ("p_dud", ctypes.c_void_p),
+                ("bg_sig", ctypes.c_void_p),
+                ("mu", ctypes.c_void_p),
+                ("sig", ctypes.c_void_p),
+                ("interactions", ctypes.c_void_p),
+                ("flat_interactions", ctypes.c_void_p)]
+
+
+class WpError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def load_library(path: Optional[str] = None):
+    """Load the CUDA library (no fallback: raises if it is missing)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"{p} not built; run whatprot_gb300/build.py (there is no CPU fallback)")
+    lib = ctypes.CDLL(p)
+    V, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    lib.wp_ctx_create.argtypes = [ctypes.POINTER(V), I]
+    lib.wp_ctx_create.restype = I
+    lib.wp_ctx_destroy.argtypes = [V]
+    lib.wp_ctx_destroy.restype = None
+    lib.wp_last_error.argtypes = [V]
+    lib.wp_last_error.restype = ctypes.c_char_p
+    lib.wp_model_upload.argtypes = [V, ctypes.POINTER(WpSeqModel), I]
+    lib.wp_model_upload.restype = I
+    lib.wp_peptides_upload.argtypes = [V, V, V, V, V, I]
+    lib.wp_peptides_upload.restype = I
+    lib.wp_hmm_classify.argtypes = [V, V, I, D, V, V, V, V, V, V]
+    lib.wp_hmm_classify.restype = I
+    lib.wp_hmm_classify_device.argtypes = [V, V, I, D, V, V, V, I]
+    lib.wp_hmm_classify_device.restype = I
+    lib.wp_hmm_loglik_all.argtypes = [V, V, I, D, V]
+    lib.wp_hmm_loglik_all.restype = I
+    lib.wp_hmm_count_flops.argtypes = [V, V, I, D, ctypes.POINTER(D)]
+    lib.wp_hmm_count_flops.restype = I
+    lib.wp_launch_count.argtypes = [V]
+    lib.wp_launch_count.restype = ctypes.c_longlong
+    lib.wp_ctx_stream.argtypes = [V]
+    lib.wp_ctx_stream.restype = V
+    lib.wp_timing_enable.argtypes = [V, I]
+    lib.wp_timing_enable.restype = I
+    lib.wp_timing_read.argtypes = [V, I, ctypes.POINTER(D), ctypes.POINTER(ctypes.c_longlong)]
+    lib.wp_timing_read.restype = I
+    lib.wp_probe_fp32_peak.argtypes = [V, ctypes.POINTER(D)]
+    lib.wp_probe_fp32_peak.restype = I
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """One wp_ctx on one CUDA device (the C ABI's handle)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        st = self.lib.wp_ctx_create(ctypes.byref(h), device)
+        if st != 0:
+            raise WpError(st, "wp_ctx_create failed (no CUDA device?)")
+        self.h = h
+        self.num_timesteps = None
+        self.num_channels = None
+        self._keep = []
+
+    def close(self):
+        if self.h:
+            self.lib.wp_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int):
+        if st != 0:
+            raise WpError(st, self.lib.wp_last_error(self.h).decode())
+
+    def upload_model(self, sm: SequencingModel, num_timesteps: int) -> None:
+        C = sm.num_channels
+        arr = lambda xs: np.ascontiguousarray(np.asarray(xs, dtype=np.float64))
+        cms = sm.channel_models
+        keep = [arr([c.p_bleach for c in cms]), arr([c.p_dud for c in cms]),
+                arr([c.bg_sig for c in cms]), arr([c.mu for c in cms]), arr([c.sig for c in cms]),
+                arr([[c.interactions[o] for o in range(C)] for c in cms]).reshape(-1),
+                arr([[c.flat_interactions[o] for o in range(C)] for c in cms]).reshape(-1)]
+        m = WpSeqModel(C, sm.p_edman_failure, sm.p_detach, sm.p_initial_detach,
+                       sm.p_initial_detach_decay, sm.p_initial_block, sm.p_cyclic_block,
+                       *[k.ctypes.data for k in keep])
+        self._check(self.lib.wp_model_upload(self.h, ctypes.byref(m), num_timesteps))
+        self.num_timesteps = num_timesteps
+        self.num_channels = C
+
+    def upload_peptides(self, ds: DyeSeqSet) -> None:
+        flat, off = ds.ragged()
+        ids = np.ascontiguousarray(ds.ids, dtype=np.int32)
+        counts = np.ascontiguousarray(ds.counts, dtype=np.int32)
+        self._check(self.lib.wp_peptides_upload(self.h, _ptr(flat), _ptr(off), _ptr(ids),
+                                                _ptr(counts), len(ds)))
+        self.num_peptides = len(ds)
+
+    def classify(self, rads: np.ndarray, dist_cutoff: float = DBL_MAX,
+                 cand: Optional[np.ndarray] = None, cand_off: Optional[np.ndarray] = None):
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        R = rads.shape[0]
+        oid = np.zeros(R, np.int32)
+        osc = np.zeros(R, np.float64)
+        otot = np.zeros(R, np.float64)
+        olog = np.zeros(R, np.float64)
+        if cand is not None:
+            cand = np.ascontiguousarray(cand, np.int32)
+            cand_off = np.ascontiguousarray(cand_off, np.int32)
+        self._check(self.lib.wp_hmm_classify(self.h, _ptr(rads), R, dist_cutoff, _ptr(cand),
+                                             _ptr(cand_off), _ptr(oid), _ptr(osc), _ptr(otot),
+                                             _ptr(olog)))
+        return oid, osc, otot, olog
+
+    def classify_device(self, d_rads_ptr: int, R: int, dist_cutoff: float, d_id: int,
+                        d_score: int, d_total: int, async_: bool = True) -> None:
+        self._check(self.lib.wp_hmm_classify_device(self.h, ctypes.c_void_p(d_rads_ptr), R,
+                                                    dist_cutoff, ctypes.c_void_p(d_id),
+                                                    ctypes.c_void_p(d_score),
+                                                    ctypes.c_void_p(d_total), 1 if async_ else 0))
+
+    def loglik_all(self, rads: np.ndarray, dist_cutoff: float = DBL_MAX) -> np.ndarray:
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        R = rads.shape[0]
+        out = np.zeros((R, self.num_peptides), np.float64)
+        self._check(self.lib.wp_hmm_loglik_all(self.h, _ptr(rads), R, dist_cutoff, _ptr(out)))
+        return out
+
+    def count_flops(self, rads: np.ndarray, dist_cutoff: float = DBL_MAX) -> float:
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        out = ctypes.c_double()
+        self._check(self.lib.wp_hmm_count_flops(self.h, _ptr(rads), rads.shape[0], dist_cutoff,
+                                                ctypes.byref(out)))
+        return out.value
+
+    def launch_count(self) -> int:
+        return int(self.lib.wp_launch_count(self.h))
+
+    def stream_handle(self) -> int:
+        return int(self.lib.wp_ctx_stream(self.h) or 0)
+
+    def timing_enable(self, on: bool = True) -> None:
+        self._check(self.lib.wp_timing_enable(self.h, 1 if on else 0))
+
+    KIND_FORWARD, KIND_PREP, KIND_COMBINE, KIND_FLOPS = 0, 1, 2, 3
+
+    def timing_read(self, kind: int) -> Tuple[float, int]:
+        ms = ctypes.c_double()
+        n = ctypes.c_longlong()
+        self._check(self.lib.wp_timing_read(self.h, kind, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def fp32_peak_tflops(self) -> float:
+        out = ctypes.c_double()
+        self._check(self.lib.wp_probe_fp32_peak(self.h, ctypes.byref(out)))
+        return out.value
+
+
+class ScoredClassification:
+    """common/scored-classification.{h,cc}: id, score, total; adjusted_score =
+    score / total."""
+    __slots__ = ("id", "score", "total")
+
+    def __init__(self, id: int, score: float, total: float):
+        self.id = id
+        self.score = score
+        self.total = total
+
+    def adjusted_score(self) -> float:
+        return self.score / self.total
+
+
+class HMMClassifier:
+    """Mirror of the reference's HMMClassifier (classifiers/hmm-classifier.h:
+    32-43): construct with (num_timesteps, num_channels, seq_model,
+    seq_settings dist_cutoff, dye_seqs) and classify one or many radiometries,
+    optionally restricted to candidate peptide indices.  Runs on the GPU
+    through the C ABI."""
+
+    def __init__(self, num_timesteps: int, num_channels: int, seq_model: SequencingModel,
+                 dist_cutoff: float, dye_seqs: DyeSeqSet, device: int = 0,
+                 context: Optional[Context] = None):
+        if seq_model.num_channels != num_channels or dye_seqs.num_channels != num_channels:
+            raise ValueError("num_channels mismatch")
+        self.ctx = context or Context(device)
+        self.ctx.upload_model(seq_model, num_timesteps)
+        self.ctx.upload_peptides(dye_seqs)
+        self.num_timesteps = num_timesteps
+        self.num_channels = num_channels
+        self.dist_cutoff = dist_cutoff
+        self.dye_seqs = dye_seqs
+
+    def classify(self, radiometries: np.ndarray, candidate_indices=None):
+        """radiometries: [T, C] (one read) or [R, T, C].  candidate_indices:
+        one list (single read) or a list of lists (one per read)."""
+        rads = np.asarray(radiometries, dtype=np.float64)
+        single = rads.ndim == 2
+        if single:
+            rads = rads[None]
+            if candidate_indices is not None:
+                candidate_indices = [candidate_indices]
+        cand = cand_off = None
+        if candidate_indices is not None:
+            cand_off = np.zeros(len(candidate_indices) + 1, np.int32)
+            for i, c in enumerate(candidate_indices):
+                cand_off[i + 1] = cand_off[i] + len(c)
+            cand = (np.concatenate([np.asarray(c, np.int32) for c in candidate_indices])
+                    if cand_off[-1] else np.zeros(1, np.int32))
+        ids, sc, tot, _ = self.ctx.classify(rads, self.dist_cutoff, cand, cand_off)
+        res = [ScoredClassification(int(i), float(s), float(t)) for i, s, t in zip(ids, sc, tot)]
+        return res[0] if single else res
