@@ -544,7 +544,9 @@ __device__ void pair_forward(const SmemHead& H, const EmitEntry* __restrict__ rt
                 if (j >= S) j -= S;
             }
         }
-        float sum_ab = warp_sum(part);
+        // The butterfly leaves lane-dependent rounding; take lane 0's value so
+        // that every lane applies the same rescale.
+        float sum_ab = __shfl_sync(0xffffffffu, warp_sum(part), 0);
         pd = H.allow[t] ? pd * em0 : 0.0f;
         expo += kmax;
         float tot = sum_ab + pd;
