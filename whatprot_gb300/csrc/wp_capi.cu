@@ -1,14 +1,20 @@
 // wp_capi.cu -- host side of the C ABI declared in include/whatprot_gb300.h.
 //
 // The context owns one CUDA stream and the device copies of the model
-// (DevModel) and peptide set (PeptideRec[]).  A classify call:
-//   1. copies the reads to the device (or takes device pointers),
-//   2. runs the prep kernel (per-read emission boxes and factors),
-//   3. runs the forward kernel once per shape bucket -- peptides are bucketed
-//      by the size of their Edman slice S = prod_c (D_c + 1) so that each
-//      launch sizes its per-warp shared-memory buffers to its bucket --
-//      with one CTA per (read, chunk of the bucket's peptides),
-//   4. combines the per-chunk partials per read and copies the results back.
+// (DevModel) and the peptide set (PeptideRec[]).  One batch of reads runs
+// as a fixed sequence of launches on that stream, with no host round trip
+// in between:
+//   prep      per (read, t): emission pruning boxes and factors
+//   summary   per read: closed-form pruning boxes, allow flags, emptiness
+//   compact   per read: empty pairs -> probability 0; others -> work list
+//   engine    thread-per-pair pruned forward pass, pass 1 (small per-thread
+//             shared-memory slabs, many resident warps) and pass 2 (large
+//             slabs) on what did not fit
+//   dense     warp-per-pair forward pass on what did not fit pass 2
+//   reduce    per read: best peptide and weighted total (classify), or
+//   logp      log P per pair (all-pairs mode)
+// The engine and dense kernels are persistent grids that pull work from
+// device-side counters, so the list sizes never travel to the host.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -22,18 +28,23 @@
 
 #include "wp_common.cuh"
 
-// Kernels (wp_kernels.cu).
+// Kernels.
 __global__ void wp_prep_reads_kernel(const DevModel*, const double*, int, unsigned, double,
                                      uint8_t*, uint8_t*, EmitEntry*, int);
-__global__ void wp_combine_kernel(int, const int*, const int*, const int*, const float*,
-                                  const int*, const double*, const int*, int32_t*, double*,
-                                  double*, double*);
-__global__ void wp_count_flops_kernel(const DevModel*, const PeptideRec*, int, const uint8_t*,
-                                      const uint8_t*, int, double*);
-size_t wp_forward_smem_bytes(int T, int S_cap, int C, bool has_block, int warps);
+__global__ void wp_read_summary_kernel(BatchArgs);
+__global__ void wp_compact_kernel(BatchArgs);
+__global__ void wp_reduce_kernel(BatchArgs, int32_t*, double*, double*, double*, const int*);
+__global__ void wp_logp_kernel(const float*, const int*, long, double*);
+__global__ void wp_count_flops_kernel(BatchArgs, double*);
+cudaError_t wp_launch_engine(int C, bool has_block, int threads, size_t smem, cudaStream_t s,
+                             const BatchArgs& a, const int2* in, const int* in_count, int* in_head,
+                             int2* out, int* out_count, int slab_half, int scr_floats,
+                             int spill_error, int* grid_out);
+size_t wp_engine_smem_bytes(int slab_half, int scr_floats, bool has_block, int threads);
+cudaError_t wp_launch_dense(bool has_block, int threads, size_t smem, cudaStream_t stream,
+                            const BatchArgs& a);
+size_t wp_dense_smem_bytes(int T, int S_cap, int C, bool has_block, int warps);
 cudaError_t wp_launch_fma_probe(int blocks, int threads, int iters, cudaStream_t stream, float* sink);
-cudaError_t wp_launch_forward(bool has_block, int grid, int threads, size_t smem,
-                              cudaStream_t stream, const TileArgs& args);
 
 namespace {
 
@@ -59,10 +70,9 @@ struct DevBuf {
     }
 };
 
-struct Bucket {
-    int S_cap;
-    std::vector<int> peps;  // ascending peptide indices
-};
+// Engine pass shapes (threads per CTA).
+constexpr int kPass1Threads = 256;
+constexpr int kPass2Threads = 128;
 
 }  // namespace
 
@@ -85,11 +95,10 @@ struct wp_ctx {
     // Derived at plan time (need C and T).
     int plan_C = -1, plan_T = -1;
     int dmax = 0;
+    int S_max = 1;       // max over peptides of prod_c (D_c + 1)
+    int scr_floats = 1;  // max over peptides of sum_c (D_c + 1)
     std::vector<PeptideRec> recs;
-    std::vector<Bucket> buckets;
-    DevBuf d_peps, d_ids, d_counts, d_list, d_chunk_b, d_chunk_e;
-    std::vector<int> list;  // concatenated bucket lists
-    std::vector<int> list_off;  // per bucket start in list
+    DevBuf d_peps, d_ids, d_counts;
 
     // Kernel timing.
     bool timing = false;
@@ -100,11 +109,12 @@ struct wp_ctx {
     std::vector<Timed> timed;
     double t_ms[4] = {0, 0, 0, 0};
     long long t_n[4] = {0, 0, 0, 0};
+    int last_engine_grid = 0;
 
-    // Per-call scratch.
-    DevBuf d_rads, d_lo, d_hi, d_table, d_part_key, d_part_pep, d_part_mant, d_part_expo,
-            d_part_total, d_read_tile_off, d_out_id, d_out_score, d_out_total, d_out_log,
-            d_logp, d_flops, d_err, d_tiles, d_cand_list, d_cand_key;
+    // Per-batch scratch.
+    DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_allow, d_flags, d_table, d_res_mant, d_res_expo,
+            d_work, d_ovf1, d_ovf2, d_counters, d_cand, d_slot_off, d_out_id, d_out_score,
+            d_out_total, d_out_log, d_logp, d_flops, d_err;
 };
 
 namespace {
@@ -119,9 +129,9 @@ wp_status cuda_fail(wp_ctx* ctx, cudaError_t e, const char* what) {
     return e == cudaErrorMemoryAllocation ? WP_ERR_OOM : WP_ERR_CUDA;
 }
 
-#define WP_CUDA(call, what)                                   \
-    do {                                                      \
-        cudaError_t _e = (call);                              \
+#define WP_CUDA(call, what)                                     \
+    do {                                                        \
+        cudaError_t _e = (call);                                \
         if (_e != cudaSuccess) return cuda_fail(ctx, _e, what); \
     } while (0)
 
@@ -173,14 +183,16 @@ void binomial_table(double q, int max_n, float* out) {
     for (size_t k = 0; k < tab.size(); k++) out[k] = (float)tab[k];
 }
 
-// Build per-peptide records and shape buckets for (C, T).
+// Per-peptide records (DyeSeqPrecomputations, dye-seq-precomputations.cc:
+// 20-39) for the current (C, T).
 wp_status plan_peptides(wp_ctx* ctx) {
     const int C = ctx->hm.C, T = ctx->hm.T;
     if (ctx->plan_C == C && ctx->plan_T == T) return WP_OK;
     const int P = ctx->P;
     ctx->recs.assign(P, PeptideRec());
     ctx->dmax = 0;
-    std::vector<int> S(P);
+    ctx->S_max = 1;
+    ctx->scr_floats = 1;
     for (int i = 0; i < P; i++) {
         PeptideRec& rec = ctx->recs[i];
         memset(&rec, 0, sizeof(rec));
@@ -194,7 +206,7 @@ wp_status plan_peptides(wp_ctx* ctx) {
                                                          std::to_string(d) + " >= num_channels");
             if (d >= 0) cnt[d]++;
         }
-        int prod = 1;
+        int prod = 1, sum = 0;
         for (int c = 0; c < C; c++) {
             if (cnt[c] > WP_MAX_DYES_PER_CHANNEL)
                 return fail(ctx, WP_ERR_UNSUPPORTED, "dye-seq " + std::to_string(i) +
@@ -202,8 +214,10 @@ wp_status plan_peptides(wp_ctx* ctx) {
             rec.D[c] = (uint8_t)cnt[c];
             ctx->dmax = std::max(ctx->dmax, cnt[c]);
             prod *= cnt[c] + 1;
+            sum += cnt[c] + 1;
         }
-        S[i] = prod;
+        ctx->S_max = std::max(ctx->S_max, prod);
+        ctx->scr_floats = std::max(ctx->scr_floats, sum);
         // DyeTrack(e, c) for c = dye_seq[e] (common/dye-track.cc:26-43).
         int rem[WP_MAX_CHANNELS];
         memcpy(rem, cnt, sizeof(rem));
@@ -214,32 +228,9 @@ wp_status plan_peptides(wp_ctx* ctx) {
             if (d >= 0) rem[d]--;
         }
     }
-    // Buckets by S (powers of two from 16).
-    ctx->buckets.clear();
-    int max_S = 1;
-    for (int i = 0; i < P; i++) max_S = std::max(max_S, S[i]);
-    for (int cap = 16;; cap *= 2) {
-        Bucket b;
-        b.S_cap = cap;
-        int lo = cap == 16 ? 0 : cap / 2;
-        for (int i = 0; i < P; i++)
-            if (S[i] > lo && S[i] <= cap) b.peps.push_back(i);
-        if (!b.peps.empty()) ctx->buckets.push_back(b);
-        if (cap >= max_S) break;
-    }
-    ctx->list.clear();
-    ctx->list_off.clear();
-    for (auto& b : ctx->buckets) {
-        ctx->list_off.push_back((int)ctx->list.size());
-        ctx->list.insert(ctx->list.end(), b.peps.begin(), b.peps.end());
-    }
-    ctx->list_off.push_back((int)ctx->list.size());
     WP_CUDA(ctx->d_peps.ensure(sizeof(PeptideRec) * std::max(P, 1)), "alloc peptides");
     WP_CUDA(cudaMemcpyAsync(ctx->d_peps.p, ctx->recs.data(), sizeof(PeptideRec) * P,
                             cudaMemcpyHostToDevice, ctx->stream), "copy peptides");
-    WP_CUDA(ctx->d_list.ensure(sizeof(int) * std::max<size_t>(ctx->list.size(), 1)), "alloc list");
-    WP_CUDA(cudaMemcpyAsync(ctx->d_list.p, ctx->list.data(), sizeof(int) * ctx->list.size(),
-                            cudaMemcpyHostToDevice, ctx->stream), "copy list");
     WP_CUDA(ctx->d_ids.ensure(sizeof(int) * std::max(P, 1)), "alloc ids");
     WP_CUDA(cudaMemcpyAsync(ctx->d_ids.p, ctx->ids.data(), sizeof(int) * P, cudaMemcpyHostToDevice,
                             ctx->stream), "copy ids");
@@ -252,200 +243,166 @@ wp_status plan_peptides(wp_ctx* ctx) {
     return WP_OK;
 }
 
-int warps_for(wp_ctx* ctx, int S_cap) {
-    const int T = ctx->hm.T, C = ctx->hm.C;
-    bool hb = ctx->hm.has_block != 0;
-    for (int w = 16; w >= 1; w--)
-        if (wp_forward_smem_bytes(T, S_cap, C, hb, w) <= (size_t)ctx->smem_optin) return w;
-    return 0;
+// Largest slab half (state elements) that lets `per_sm` CTAs of `threads`
+// share one SM's shared memory.
+int slab_half_for(wp_ctx* ctx, int threads, int per_sm, bool hb) {
+    size_t budget = (size_t)ctx->smem_optin;
+    if (per_sm > 1) budget = std::min(budget, (size_t)(228 * 1024) / per_sm - 1024);
+    size_t elem = hb ? 8 : 4;
+    size_t fixed = wp_engine_smem_bytes(0, ctx->scr_floats, hb, threads);
+    if (budget <= fixed) return 0;
+    return (int)((budget - fixed) / (2 * elem * threads));
 }
 
-constexpr int kChunk = 256;  // peptides per CTA in the all-peptides mode
+enum Mode { MODE_CLASSIFY, MODE_LOGP, MODE_FLOPS };
 
-
-
-// Run prep + forward (+ combine when outputs given) on device-resident reads.
+// Everything between "reads are on the device" and "per-read outputs are
+// on the device".  Slots: all peptides (cand == null) or a ragged candidate
+// list per read (host arrays, copied here).
 wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff,
-                    const int32_t* h_cand, const int32_t* h_cand_off, double* d_logp,
-                    int32_t* d_out_id, double* d_out_score, double* d_out_total, double* d_out_log) {
+                    const int32_t* h_cand, const int32_t* h_cand_off, Mode mode, double* d_logp,
+                    int32_t* d_out_id, double* d_out_score, double* d_out_total, double* d_out_log,
+                    double* d_flops) {
     const int C = ctx->hm.C, T = ctx->hm.T;
     wp_status st = plan_peptides(ctx);
     if (st != WP_OK) return st;
+    const bool hb = ctx->hm.has_block != 0;
     const int W = ctx->dmax + 1;
     const int entries = wp_read_table_entries(T, C, W, ctx->hm.interacting);
-    WP_CUDA(ctx->d_lo.ensure((size_t)R * T * C), "alloc boxes");
-    WP_CUDA(ctx->d_hi.ensure((size_t)R * T * C), "alloc boxes");
+    long n_slots = h_cand ? (long)h_cand_off[R] : (long)R * ctx->P;
+    if (n_slots > INT32_MAX) return fail(ctx, WP_ERR_UNSUPPORTED, "too many (read, peptide) pairs in one batch");
+    const size_t rtc = (size_t)R * T * C;
+    WP_CUDA(ctx->d_lo.ensure(rtc), "alloc");
+    WP_CUDA(ctx->d_hi.ensure(rtc), "alloc");
+    WP_CUDA(ctx->d_Ls.ensure(rtc), "alloc");
+    WP_CUDA(ctx->d_Up.ensure(rtc), "alloc");
+    WP_CUDA(ctx->d_allow.ensure((size_t)R * T), "alloc");
+    WP_CUDA(ctx->d_flags.ensure((size_t)R), "alloc");
     WP_CUDA(ctx->d_table.ensure(sizeof(EmitEntry) * (size_t)R * entries), "alloc emission table");
-    WP_CUDA(ctx->d_err.ensure(sizeof(int)), "alloc err");
+    WP_CUDA(ctx->d_err.ensure(sizeof(int)), "alloc");
     WP_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(int), ctx->stream), "clear err");
-    {
-        long n = (long)R * T;
-        int threads = 128;
-        int blocks = (int)((n + threads - 1) / threads);
-        if (blocks > 0) {
-            TimedLaunch tl(ctx, 1);
-            wp_prep_reads_kernel<<<blocks, threads, 0, ctx->stream>>>(
-                    ctx->d_model.as<DevModel>(), d_rads, R, (unsigned)ctx->dmax, dist_cutoff,
-                    ctx->d_lo.as<uint8_t>(), ctx->d_hi.as<uint8_t>(), ctx->d_table.as<EmitEntry>(),
-                    entries);
-            ctx->launches++;
-            WP_CUDA(cudaGetLastError(), "prep launch");
-        }
-    }
-    const bool classify = d_out_id != nullptr;
-    TileArgs a;
+
+    BatchArgs a;
     memset(&a, 0, sizeof(a));
     a.model = ctx->d_model.as<DevModel>();
     a.peps = ctx->d_peps.as<PeptideRec>();
-    a.box_lo = ctx->d_lo.as<uint8_t>();
-    a.box_hi = ctx->d_hi.as<uint8_t>();
-    a.table = ctx->d_table.as<EmitEntry>();
-    a.entries = entries;
-    a.W = W;
-    a.num_peptides = ctx->P;
     a.counts = ctx->d_counts.as<int>();
-    a.out_logp = d_logp;
+    a.R = R;
+    a.P = ctx->P;
+    a.W = W;
+    a.entries = entries;
+    a.lo = ctx->d_lo.as<uint8_t>();
+    a.hi = ctx->d_hi.as<uint8_t>();
+    a.Lsuf = ctx->d_Ls.as<uint8_t>();
+    a.Upre = ctx->d_Up.as<uint8_t>();
+    a.allow = ctx->d_allow.as<uint8_t>();
+    a.flags = ctx->d_flags.as<uint8_t>();
+    a.tab = ctx->d_table.as<EmitEntry>();
     a.err = ctx->d_err.as<int>();
-    const bool hb = ctx->hm.has_block != 0;
 
-    // Tiles: (read, bucket, chunk).  In candidate mode each read's candidates
-    // are bucketed on the host.
-    std::vector<int> tile_read, tile_begin, tile_end, tile_bucket, read_tile_off(R + 1, 0);
-    std::vector<int> cand_list, cand_key;
+    {
+        long n = (long)R * T;
+        TimedLaunch tl(ctx, 1);
+        wp_prep_reads_kernel<<<(int)((n + 127) / 128), 128, 0, ctx->stream>>>(
+                a.model, d_rads, R, (unsigned)ctx->dmax, dist_cutoff, ctx->d_lo.as<uint8_t>(),
+                ctx->d_hi.as<uint8_t>(), ctx->d_table.as<EmitEntry>(), entries);
+        ctx->launches++;
+        WP_CUDA(cudaGetLastError(), "prep launch");
+        wp_read_summary_kernel<<<(R + 127) / 128, 128, 0, ctx->stream>>>(a);
+        ctx->launches++;
+        WP_CUDA(cudaGetLastError(), "summary launch");
+    }
+    if (mode == MODE_FLOPS) {
+        long np = (long)R * ctx->P;
+        TimedLaunch tl(ctx, 3);
+        wp_count_flops_kernel<<<(int)((np + 127) / 128), 128, 0, ctx->stream>>>(a, d_flops);
+        ctx->launches++;
+        WP_CUDA(cudaGetLastError(), "flops launch");
+        return WP_OK;
+    }
     if (h_cand) {
-        std::vector<int> bucket_of(ctx->P, -1);
-        for (size_t b = 0; b < ctx->buckets.size(); b++)
-            for (int p : ctx->buckets[b].peps) bucket_of[p] = (int)b;
-        std::vector<std::vector<std::pair<int, int>>> per(ctx->buckets.size());
-        for (int r = 0; r < R; r++) {
-            for (auto& v : per) v.clear();
-            for (int k = h_cand_off[r]; k < h_cand_off[r + 1]; k++) {
-                int p = h_cand[k];
-                if (p < 0 || p >= ctx->P) return fail(ctx, WP_ERR_INVALID, "candidate index out of range");
-                per[bucket_of[p]].push_back({p, k - h_cand_off[r]});
-            }
-            for (size_t b = 0; b < per.size(); b++) {
-                for (size_t s0 = 0; s0 < per[b].size(); s0 += kChunk) {
-                    size_t s1 = std::min(per[b].size(), s0 + kChunk);
-                    tile_read.push_back(r);
-                    tile_begin.push_back((int)cand_list.size());
-                    for (size_t q = s0; q < s1; q++) {
-                        cand_list.push_back(per[b][q].first);
-                        cand_key.push_back(per[b][q].second);
-                    }
-                    tile_end.push_back((int)cand_list.size());
-                    tile_bucket.push_back((int)b);
-                }
-            }
-            read_tile_off[r + 1] = (int)tile_read.size();
-        }
-    } else {
-        int per_read = 0;
-        std::vector<int> cb, ce, cbk;
-        for (size_t b = 0; b < ctx->buckets.size(); b++) {
-            int s = ctx->list_off[b], e = ctx->list_off[b + 1];
-            for (int s0 = s; s0 < e; s0 += kChunk) {
-                cb.push_back(s0);
-                ce.push_back(std::min(e, s0 + kChunk));
-                cbk.push_back((int)b);
-                per_read++;
-            }
-        }
-        tile_read.reserve((size_t)R * per_read);
-        for (int r = 0; r < R; r++) {
-            for (int k = 0; k < per_read; k++) {
-                tile_read.push_back(r);
-                tile_begin.push_back(cb[k]);
-                tile_end.push_back(ce[k]);
-                tile_bucket.push_back(cbk[k]);
-            }
-            read_tile_off[r + 1] = (int)tile_read.size();
-        }
+        WP_CUDA(ctx->d_cand.ensure(sizeof(int) * std::max<long>(n_slots, 1)), "alloc cand");
+        WP_CUDA(ctx->d_slot_off.ensure(sizeof(int) * (R + 1)), "alloc cand");
+        for (long k = 0; k < n_slots; k++)
+            if (h_cand[k] < 0 || h_cand[k] >= ctx->P) return fail(ctx, WP_ERR_INVALID, "candidate index out of range");
+        if (n_slots > 0)
+            WP_CUDA(cudaMemcpyAsync(ctx->d_cand.p, h_cand, sizeof(int) * n_slots, cudaMemcpyHostToDevice, ctx->stream), "copy cand");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_slot_off.p, h_cand_off, sizeof(int) * (R + 1), cudaMemcpyHostToDevice, ctx->stream), "copy cand");
+        a.cand = ctx->d_cand.as<int>();
+        a.slot_off = ctx->d_slot_off.as<int>();
     }
-    const int ntiles = (int)tile_read.size();
-    // Order tiles by bucket so that each launch gets a contiguous range.
-    std::vector<int> order(ntiles);
-    for (int i = 0; i < ntiles; i++) order[i] = i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int x, int y) { return tile_bucket[x] < tile_bucket[y]; });
-    // Tile arrays in launch order; partial outputs are written at the tile's
-    // original index (read-major) so that read_tile_off indexes them.
-    std::vector<int> t_read(ntiles), t_begin(ntiles), t_end(ntiles), t_out(ntiles);
-    for (int i = 0; i < ntiles; i++) {
-        t_read[i] = tile_read[order[i]];
-        t_begin[i] = tile_begin[order[i]];
-        t_end[i] = tile_end[order[i]];
-        t_out[i] = order[i];
-    }
-    WP_CUDA(ctx->d_tiles.ensure(sizeof(int) * 4 * std::max(ntiles, 1)), "alloc tiles");
-    int* d_t = ctx->d_tiles.as<int>();
-    WP_CUDA(cudaMemcpyAsync(d_t, t_read.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, ctx->stream), "tiles");
-    WP_CUDA(cudaMemcpyAsync(d_t + ntiles, t_begin.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, ctx->stream), "tiles");
-    WP_CUDA(cudaMemcpyAsync(d_t + 2 * ntiles, t_end.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, ctx->stream), "tiles");
-    WP_CUDA(cudaMemcpyAsync(d_t + 3 * ntiles, t_out.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice, ctx->stream), "tiles");
-    if (h_cand) {
-        WP_CUDA(ctx->d_cand_list.ensure(sizeof(int) * std::max<size_t>(cand_list.size(), 1)), "alloc cand");
-        WP_CUDA(ctx->d_cand_key.ensure(sizeof(int) * std::max<size_t>(cand_key.size(), 1)), "alloc cand");
-        WP_CUDA(cudaMemcpyAsync(ctx->d_cand_list.p, cand_list.data(), sizeof(int) * cand_list.size(),
-                                cudaMemcpyHostToDevice, ctx->stream), "cand");
-        WP_CUDA(cudaMemcpyAsync(ctx->d_cand_key.p, cand_key.data(), sizeof(int) * cand_key.size(),
-                                cudaMemcpyHostToDevice, ctx->stream), "cand");
-        a.list = ctx->d_cand_list.as<int>();
-        a.key = ctx->d_cand_key.as<int>();
-    } else {
-        a.list = ctx->d_list.as<int>();
-        a.key = ctx->d_list.as<int>();  // key = peptide index
-    }
-    WP_CUDA(ctx->d_part_key.ensure(sizeof(int) * std::max(ntiles, 1)), "alloc partials");
-    WP_CUDA(ctx->d_part_pep.ensure(sizeof(int) * std::max(ntiles, 1)), "alloc partials");
-    WP_CUDA(ctx->d_part_mant.ensure(sizeof(float) * std::max(ntiles, 1)), "alloc partials");
-    WP_CUDA(ctx->d_part_expo.ensure(sizeof(int) * std::max(ntiles, 1)), "alloc partials");
-    WP_CUDA(ctx->d_part_total.ensure(sizeof(double) * std::max(ntiles, 1)), "alloc partials");
-    a.part_key = ctx->d_part_key.as<int>();
-    a.part_pep = ctx->d_part_pep.as<int>();
-    a.part_mant = ctx->d_part_mant.as<float>();
-    a.part_expo = ctx->d_part_expo.as<int>();
-    a.part_total = ctx->d_part_total.as<double>();
-    // One launch per bucket.
-    int i0 = 0;
-    while (i0 < ntiles) {
-        int b = tile_bucket[order[i0]];
-        int i1 = i0;
-        while (i1 < ntiles && tile_bucket[order[i1]] == b) i1++;
-        int S_cap = ctx->buckets[b].S_cap;
-        int warps = warps_for(ctx, S_cap);
-        if (warps < 1)
-            return fail(ctx, WP_ERR_UNSUPPORTED, "peptide state (" + std::to_string(S_cap) + " x " +
-                                                         std::to_string(T) + ") exceeds shared memory");
-        size_t smem = wp_forward_smem_bytes(T, S_cap, C, hb, warps);
-        TileArgs la = a;
-        la.S_cap = S_cap;
-        la.tile_read = d_t + i0;
-        la.tile_begin = d_t + ntiles + i0;
-        la.tile_end = d_t + 2 * ntiles + i0;
-        la.tile_out = d_t + 3 * ntiles + i0;
+    const size_t ns = (size_t)std::max<long>(n_slots, 1);
+    WP_CUDA(ctx->d_res_mant.ensure(sizeof(float) * ns), "alloc results");
+    WP_CUDA(ctx->d_res_expo.ensure(sizeof(int) * ns), "alloc results");
+    WP_CUDA(ctx->d_work.ensure(sizeof(int2) * ns), "alloc work list");
+    WP_CUDA(ctx->d_ovf1.ensure(sizeof(int2) * ns), "alloc work list");
+    WP_CUDA(ctx->d_ovf2.ensure(sizeof(int2) * ns), "alloc work list");
+    WP_CUDA(ctx->d_counters.ensure(sizeof(int) * 8), "alloc counters");
+    WP_CUDA(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(int) * 8, ctx->stream), "clear counters");
+    int* cnt = ctx->d_counters.as<int>();
+    a.res_mant = ctx->d_res_mant.as<float>();
+    a.res_expo = ctx->d_res_expo.as<int>();
+    a.work = ctx->d_work.as<int2>();
+    a.work_count = cnt + 0;
+    a.work_head = cnt + 1;
+    a.ovf = ctx->d_ovf2.as<int2>();
+    a.ovf_count = cnt + 4;
+    a.ovf_head = cnt + 5;
+    a.dense_S_cap = ((ctx->S_max + 31) / 32) * 32;
+    if (n_slots > 0) {
+        {
+            TimedLaunch tl(ctx, 1);
+            wp_compact_kernel<<<R, 256, 0, ctx->stream>>>(a);
+            ctx->launches++;
+            WP_CUDA(cudaGetLastError(), "compact launch");
+        }
+        // Dense fallback shape: as many warps as fit (0: unavailable).
+        int dense_warps = 0;
+        for (int w = 16; w >= 1; w--)
+            if (wp_dense_smem_bytes(T, a.dense_S_cap, C, hb, w) <= (size_t)ctx->smem_optin) {
+                dense_warps = w;
+                break;
+            }
+        // Pass 1: two CTAs of 256 threads per SM; pass 2: one CTA of 128.
+        int half1 = slab_half_for(ctx, kPass1Threads, 2, hb);
+        int half2 = slab_half_for(ctx, kPass2Threads, 1, hb);
+        if (half1 < 4 || half2 < 4)
+            return fail(ctx, WP_ERR_UNSUPPORTED, "shared memory too small for the pair engine");
         {
             TimedLaunch tl(ctx, 0);
-            WP_CUDA(wp_launch_forward(hb, i1 - i0, warps * 32, smem, ctx->stream, la), "forward launch");
-        }
-        ctx->launches++;
-        i0 = i1;
-    }
-    if (classify) {
-        WP_CUDA(ctx->d_read_tile_off.ensure(sizeof(int) * (R + 1)), "alloc offsets");
-        WP_CUDA(cudaMemcpyAsync(ctx->d_read_tile_off.p, read_tile_off.data(), sizeof(int) * (R + 1),
-                                cudaMemcpyHostToDevice, ctx->stream), "offsets");
-        int threads = 128;
-        int blocks = (R + threads - 1) / threads;
-        if (blocks > 0) {
-            TimedLaunch tl(ctx, 2);
-            wp_combine_kernel<<<blocks, threads, 0, ctx->stream>>>(
-                    R, ctx->d_read_tile_off.as<int>(), a.part_key, a.part_pep, a.part_mant,
-                    a.part_expo, a.part_total, ctx->d_ids.as<int>(), d_out_id, d_out_score,
-                    d_out_total, d_out_log);
+            size_t smem = wp_engine_smem_bytes(half1, ctx->scr_floats, hb, kPass1Threads);
+            WP_CUDA(wp_launch_engine(C, hb, kPass1Threads, smem, ctx->stream, a, a.work, cnt + 0, cnt + 1,
+                                     ctx->d_ovf1.as<int2>(), cnt + 2, half1, ctx->scr_floats, 0,
+                                     &ctx->last_engine_grid), "engine pass 1");
             ctx->launches++;
-            WP_CUDA(cudaGetLastError(), "combine launch");
         }
+        {
+            TimedLaunch tl(ctx, 0);
+            size_t smem = wp_engine_smem_bytes(half2, ctx->scr_floats, hb, kPass2Threads);
+            WP_CUDA(wp_launch_engine(C, hb, kPass2Threads, smem, ctx->stream, a, ctx->d_ovf1.as<int2>(),
+                                     cnt + 2, cnt + 3, ctx->d_ovf2.as<int2>(), cnt + 4, half2,
+                                     ctx->scr_floats, dense_warps == 0 ? 1 : 0, nullptr), "engine pass 2");
+            ctx->launches++;
+        }
+        if (dense_warps > 0) {
+            TimedLaunch tl(ctx, 0);
+            size_t smem = wp_dense_smem_bytes(T, a.dense_S_cap, C, hb, dense_warps);
+            WP_CUDA(wp_launch_dense(hb, dense_warps * 32, smem, ctx->stream, a), "dense launch");
+            ctx->launches++;
+        }
+    }
+    if (mode == MODE_CLASSIFY) {
+        TimedLaunch tl(ctx, 2);
+        wp_reduce_kernel<<<(R + 3) / 4, 128, 0, ctx->stream>>>(a, d_out_id, d_out_score, d_out_total,
+                                                              d_out_log, ctx->d_ids.as<int>());
+        ctx->launches++;
+        WP_CUDA(cudaGetLastError(), "reduce launch");
+    } else if (mode == MODE_LOGP && n_slots > 0) {
+        TimedLaunch tl(ctx, 2);
+        wp_logp_kernel<<<(int)((n_slots + 255) / 256), 256, 0, ctx->stream>>>(a.res_mant, a.res_expo,
+                                                                              n_slots, d_logp);
+        ctx->launches++;
+        WP_CUDA(cudaGetLastError(), "logp launch");
     }
     return WP_OK;
 }
@@ -460,7 +417,15 @@ wp_status finish(wp_ctx* ctx) {
     WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
     int err = 0;
     WP_CUDA(cudaMemcpy(&err, ctx->d_err.p, sizeof(int), cudaMemcpyDeviceToHost), "read err");
-    if (err) return fail(ctx, WP_ERR_CUDA, "internal: peptide state exceeded its bucket");
+    if (err == 2) return fail(ctx, WP_ERR_UNSUPPORTED, "a pair's state exceeds every shared-memory shape");
+    if (err) return fail(ctx, WP_ERR_CUDA, "internal: peptide state exceeded its shape");
+    return WP_OK;
+}
+
+wp_status upload_reads(wp_ctx* ctx, const double* rads, int R) {
+    const size_t bytes = sizeof(double) * (size_t)R * ctx->hm.T * ctx->hm.C;
+    WP_CUDA(ctx->d_rads.ensure(bytes), "alloc reads");
+    WP_CUDA(cudaMemcpyAsync(ctx->d_rads.p, rads, bytes, cudaMemcpyHostToDevice, ctx->stream), "copy reads");
     return WP_OK;
 }
 
@@ -472,12 +437,12 @@ wp_status wp_ctx_create(wp_ctx** out, int device) {
     if (!out) return WP_ERR_INVALID;
     *out = nullptr;
     int n = 0;
-    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || device < 0 || device >= n)
-        return WP_ERR_CUDA;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || device < 0 || device >= n) return WP_ERR_CUDA;
     wp_ctx* ctx = new (std::nothrow) wp_ctx();
     if (!ctx) return WP_ERR_OOM;
     ctx->device = device;
-    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete ctx;
         return WP_ERR_CUDA;
     }
@@ -495,21 +460,16 @@ void wp_ctx_destroy(wp_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    collect_timing(ctx);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
 
-const char* wp_last_error(const wp_ctx* ctx) {
-    return ctx ? ctx->err.c_str() : "null context";
-}
+const char* wp_last_error(const wp_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
-long long wp_launch_count(const wp_ctx* ctx) {
-    return ctx ? ctx->launches : 0;
-}
+long long wp_launch_count(const wp_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
-void* wp_ctx_stream(const wp_ctx* ctx) {
-    return ctx ? (void*)ctx->stream : nullptr;
-}
+void* wp_ctx_stream(const wp_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
 wp_status wp_timing_enable(wp_ctx* ctx, int enable) {
     if (!ctx) return WP_ERR_INVALID;
@@ -607,10 +567,10 @@ wp_status wp_peptides_upload(wp_ctx* ctx, const int16_t* dye_seqs, const int32_t
                              const int32_t* ids, const int32_t* counts, int P) {
     if (!ctx || P < 0 || (P > 0 && (!offsets || !ids || !counts))) return WP_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
-    if (offsets[0] != 0) return fail(ctx, WP_ERR_INVALID, "offsets[0] must be 0");
+    if (P > 0 && offsets[0] != 0) return fail(ctx, WP_ERR_INVALID, "offsets[0] must be 0");
     for (int i = 0; i < P; i++)
         if (offsets[i + 1] < offsets[i]) return fail(ctx, WP_ERR_INVALID, "offsets not ascending");
-    int n = offsets[P];
+    int n = P > 0 ? offsets[P] : 0;
     if (n > 0 && !dye_seqs) return WP_ERR_INVALID;
     ctx->seqs.assign(dye_seqs, dye_seqs + n);
     ctx->offsets.assign(offsets, offsets + P + 1);
@@ -633,17 +593,20 @@ wp_status wp_hmm_classify(wp_ctx* ctx, const double* rads, int R, double dist_cu
     if (st != WP_OK) return st;
     if (R == 0) return WP_OK;
     if (ctx->P == 0) return fail(ctx, WP_ERR_INVALID, "no peptides");
-    const int T = ctx->hm.T, C = ctx->hm.C;
-    size_t rbytes = sizeof(double) * (size_t)R * T * C;
-    WP_CUDA(ctx->d_rads.ensure(rbytes), "alloc reads");
-    WP_CUDA(cudaMemcpyAsync(ctx->d_rads.p, rads, rbytes, cudaMemcpyHostToDevice, ctx->stream), "copy reads");
+    if (cand) {
+        if (cand_off[0] != 0) return fail(ctx, WP_ERR_INVALID, "cand_off[0] must be 0");
+        for (int r = 0; r < R; r++)
+            if (cand_off[r + 1] < cand_off[r]) return fail(ctx, WP_ERR_INVALID, "cand_off not ascending");
+    }
+    st = upload_reads(ctx, rads, R);
+    if (st != WP_OK) return st;
     WP_CUDA(ctx->d_out_id.ensure(sizeof(int32_t) * R), "alloc out");
     WP_CUDA(ctx->d_out_score.ensure(sizeof(double) * R), "alloc out");
     WP_CUDA(ctx->d_out_total.ensure(sizeof(double) * R), "alloc out");
     WP_CUDA(ctx->d_out_log.ensure(sizeof(double) * R), "alloc out");
-    st = run_batch(ctx, ctx->d_rads.as<double>(), R, dist_cutoff, cand, cand_off, nullptr,
+    st = run_batch(ctx, ctx->d_rads.as<double>(), R, dist_cutoff, cand, cand_off, MODE_CLASSIFY, nullptr,
                    ctx->d_out_id.as<int32_t>(), ctx->d_out_score.as<double>(),
-                   ctx->d_out_total.as<double>(), ctx->d_out_log.as<double>());
+                   ctx->d_out_total.as<double>(), ctx->d_out_log.as<double>(), nullptr);
     if (st != WP_OK) return st;
     WP_CUDA(cudaMemcpyAsync(out_id, ctx->d_out_id.p, sizeof(int32_t) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy out");
     WP_CUDA(cudaMemcpyAsync(out_score, ctx->d_out_score.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy out");
@@ -654,17 +617,16 @@ wp_status wp_hmm_classify(wp_ctx* ctx, const double* rads, int R, double dist_cu
 }
 
 wp_status wp_hmm_classify_device(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff,
-                                 int32_t* d_out_id, double* d_out_score, double* d_out_total,
-                                 int async) {
+                                 int32_t* d_out_id, double* d_out_score, double* d_out_total, int async) {
     if (!ctx || R < 0 || (R > 0 && (!d_rads || !d_out_id || !d_out_score || !d_out_total))) return WP_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
     wp_status st = check_ready(ctx);
     if (st != WP_OK) return st;
     if (R == 0) return WP_OK;
-    WP_CUDA(ctx->d_out_log.ensure(sizeof(double) * R), "alloc out");
-    st = run_batch(ctx, d_rads, R, dist_cutoff, nullptr, nullptr, nullptr, d_out_id, d_out_score,
-                   d_out_total, ctx->d_out_log.as<double>());
+    if (ctx->P == 0) return fail(ctx, WP_ERR_INVALID, "no peptides");
+    st = run_batch(ctx, d_rads, R, dist_cutoff, nullptr, nullptr, MODE_CLASSIFY, nullptr, d_out_id,
+                   d_out_score, d_out_total, nullptr, nullptr);
     if (st != WP_OK) return st;
     if (async) return WP_OK;
     return finish(ctx);
@@ -677,14 +639,12 @@ wp_status wp_hmm_loglik_all(wp_ctx* ctx, const double* rads, int R, double dist_
     wp_status st = check_ready(ctx);
     if (st != WP_OK) return st;
     if (R == 0 || ctx->P == 0) return WP_OK;
-    const int T = ctx->hm.T, C = ctx->hm.C;
-    size_t rbytes = sizeof(double) * (size_t)R * T * C;
-    WP_CUDA(ctx->d_rads.ensure(rbytes), "alloc reads");
-    WP_CUDA(cudaMemcpyAsync(ctx->d_rads.p, rads, rbytes, cudaMemcpyHostToDevice, ctx->stream), "copy reads");
+    st = upload_reads(ctx, rads, R);
+    if (st != WP_OK) return st;
     size_t lbytes = sizeof(double) * (size_t)R * ctx->P;
     WP_CUDA(ctx->d_logp.ensure(lbytes), "alloc logp");
-    st = run_batch(ctx, ctx->d_rads.as<double>(), R, dist_cutoff, nullptr, nullptr,
-                   ctx->d_logp.as<double>(), nullptr, nullptr, nullptr, nullptr);
+    st = run_batch(ctx, ctx->d_rads.as<double>(), R, dist_cutoff, nullptr, nullptr, MODE_LOGP,
+                   ctx->d_logp.as<double>(), nullptr, nullptr, nullptr, nullptr, nullptr);
     if (st != WP_OK) return st;
     WP_CUDA(cudaMemcpyAsync(out_logp, ctx->d_logp.p, lbytes, cudaMemcpyDeviceToHost, ctx->stream), "copy logp");
     return finish(ctx);
@@ -698,31 +658,13 @@ wp_status wp_hmm_count_flops(wp_ctx* ctx, const double* rads, int R, double dist
     if (st != WP_OK) return st;
     *out_flops = 0.0;
     if (R == 0 || ctx->P == 0) return WP_OK;
-    st = plan_peptides(ctx);
+    st = upload_reads(ctx, rads, R);
     if (st != WP_OK) return st;
-    const int T = ctx->hm.T, C = ctx->hm.C;
-    const int W = ctx->dmax + 1;
-    const int entries = wp_read_table_entries(T, C, W, ctx->hm.interacting);
-    size_t rbytes = sizeof(double) * (size_t)R * T * C;
-    WP_CUDA(ctx->d_rads.ensure(rbytes), "alloc reads");
-    WP_CUDA(cudaMemcpyAsync(ctx->d_rads.p, rads, rbytes, cudaMemcpyHostToDevice, ctx->stream), "copy reads");
-    WP_CUDA(ctx->d_lo.ensure((size_t)R * T * C), "alloc boxes");
-    WP_CUDA(ctx->d_hi.ensure((size_t)R * T * C), "alloc boxes");
-    WP_CUDA(ctx->d_table.ensure(sizeof(EmitEntry) * (size_t)R * entries), "alloc emission table");
-    long n = (long)R * T;
-    wp_prep_reads_kernel<<<(int)((n + 127) / 128), 128, 0, ctx->stream>>>(
-            ctx->d_model.as<DevModel>(), ctx->d_rads.as<double>(), R, (unsigned)ctx->dmax, dist_cutoff,
-            ctx->d_lo.as<uint8_t>(), ctx->d_hi.as<uint8_t>(), ctx->d_table.as<EmitEntry>(), entries);
-    ctx->launches++;
     WP_CUDA(ctx->d_flops.ensure(sizeof(double) * R), "alloc flops");
     WP_CUDA(cudaMemsetAsync(ctx->d_flops.p, 0, sizeof(double) * R, ctx->stream), "clear flops");
-    long np = (long)R * ctx->P;
-    TimedLaunch tl(ctx, 3);
-    wp_count_flops_kernel<<<(int)((np + 127) / 128), 128, 0, ctx->stream>>>(
-            ctx->d_model.as<DevModel>(), ctx->d_peps.as<PeptideRec>(), ctx->P, ctx->d_lo.as<uint8_t>(),
-            ctx->d_hi.as<uint8_t>(), R, ctx->d_flops.as<double>());
-    ctx->launches++;
-    WP_CUDA(cudaGetLastError(), "flops launch");
+    st = run_batch(ctx, ctx->d_rads.as<double>(), R, dist_cutoff, nullptr, nullptr, MODE_FLOPS, nullptr,
+                   nullptr, nullptr, nullptr, nullptr, ctx->d_flops.as<double>());
+    if (st != WP_OK) return st;
     std::vector<double> per(R);
     WP_CUDA(cudaMemcpyAsync(per.data(), ctx->d_flops.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy flops");
     WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");

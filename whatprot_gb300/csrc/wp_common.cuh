@@ -68,31 +68,67 @@ __host__ __device__ inline int wp_read_table_entries(int T, int C, int W, int in
     return interacting ? T * wp_ipow(W, C) : T * C * W;
 }
 
-// Arguments of one forward launch (one shape bucket).
-struct TileArgs {
+// Model tables a CTA keeps in shared memory.
+struct SmemModel {
+    float dud[WP_MAX_CHANNELS][WP_TRI];
+    float bleach[WP_MAX_CHANNELS][WP_TRI];
+    float p_det[WP_MAX_TIMESTEPS];
+};
+
+// Everything one batch of reads needs on the device.  Per-read arrays are
+// indexed [r][t][c] (uint8) or [r][t]; per-slot arrays by the slot g: the
+// slots of read r are [slot_off[r], slot_off[r+1]) (all-peptides mode:
+// slot_off == null, slots r*P .. r*P+P-1 and slot g holds peptide g - r*P).
+struct BatchArgs {
     const DevModel* model;
     const PeptideRec* peps;
-    const uint8_t* box_lo;   // [R][T][C]
-    const uint8_t* box_hi;
-    const EmitEntry* table;  // [R][entries]
-    int entries;             // per read
-    int W;                   // Dmax + 1 (table extent per channel)
-    const int* list;         // peptide index per list entry
-    const int* key;          // tie-break key (candidate position) per entry
-    const int* tile_read;    // per CTA
-    const int* tile_begin;
-    const int* tile_end;
-    const int* tile_out;     // partial index per CTA
-    int S_cap;               // max states per Edman slice in this launch
-    int num_peptides;
-    const int* counts;       // peptide multiplicities
-    // outputs
-    double* out_logp;        // [R][P] or null
-    // per tile partials (classify mode) or null
-    int* part_key;
-    int* part_pep;
-    float* part_mant;
-    int* part_expo;
-    double* part_total;      // total relative to 2^part_expo
-    int* err;                // set nonzero on an internal error
+    const int* counts;         // peptide multiplicities
+    int R;
+    int P;
+    int W;                     // Dmax + 1
+    int entries;               // emission entries per read
+    const uint8_t* lo;         // cmin per (r, t, c)
+    const uint8_t* hi;         // cmax
+    uint8_t* Lsuf;             // max_{t' >= t} cmin
+    uint8_t* Upre;             // min_{t' <= t} cmax
+    uint8_t* allow;            // per (r, t): the emission box includes zero
+    uint8_t* flags;            // per r: bit 0 = the read prunes every pair
+    const EmitEntry* tab;      // per read: emission factors
+    const int* cand;           // per slot: peptide index (null: all peptides)
+    const int* slot_off;       // [R + 1] or null
+    float* res_mant;           // per slot: P = res_mant * 2^res_expo
+    int* res_expo;
+    int2* work;                // non-empty (r, g) pairs
+    int* work_count;
+    int* work_head;
+    int2* ovf;                 // pairs whose state exceeds the thread slab
+    int* ovf_count;
+    int* ovf_head;
+    int* err;
+    int slab_half;             // per-thread slab half, in state elements
+    int dense_S_cap;           // overflow kernel: max states per Edman slice
 };
+
+__host__ __device__ inline int slot_begin(const BatchArgs& a, int r) {
+    return a.slot_off ? a.slot_off[r] : r * a.P;
+}
+__host__ __device__ inline int slot_pep(const BatchArgs& a, int r, int g) {
+    return a.cand ? a.cand[g] : g - r * a.P;
+}
+
+// 2^x as a float for x <= 127 (0 below the subnormal range).
+__device__ __forceinline__ float exp2i(int x) {
+    if (x > 127) x = 127;
+    if (x >= -126) return __int_as_float((x + 127) << 23);
+    if (x >= -149) return ldexpf(1.0f, x);
+    return 0.0f;
+}
+
+__device__ __forceinline__ void load_smem_model(SmemModel& S, const DevModel& m) {
+    for (int i = threadIdx.x; i < m.C * WP_TRI; i += blockDim.x) {
+        int c = i / WP_TRI, k = i % WP_TRI;
+        S.dud[c][k] = m.dud[c][k];
+        S.bleach[c][k] = m.bleach[c][k];
+    }
+    for (int t = threadIdx.x; t < m.T; t += blockDim.x) S.p_det[t] = m.p_det[t];
+}

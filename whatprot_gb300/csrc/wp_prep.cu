@@ -1,0 +1,269 @@
+// wp_prep.cu -- per-read preparation and pair compaction.
+//
+//   wp_prep_reads_kernel    one thread per (read, timestep): the emission
+//                           pruning box [cmin, cmax) of the reference's
+//                           PeptideEmission (hmm/step/peptide-emission.cc:
+//                           50-163) and the emission factors, computed in FP64
+//                           as the reference does and stored as (FP32
+//                           mantissa, int exponent).
+//   wp_read_summary_kernel  one thread per read: the closed-form pruning boxes
+//                           every pair of the read shares, L_t = max_{t'>=t}
+//                           cmin_{t'} and min_{t'<=t} cmax_{t'}, the
+//                           allow-detached flag of each emission and whether
+//                           the read prunes every pair.
+//   wp_compact_kernel       one CTA per read: pairs whose pruned range is
+//                           empty get probability 0 (PeptideHMM::probability,
+//                           hmm/hmm/peptide-hmm.cc:94-100); the others are
+//                           appended to the work list of the pair engine.
+//
+// Pruning.  After the reference's forward and backward prune passes
+// (hmm/hmm/peptide-hmm.cc:63-83) the box of emission t of a pair is
+// [L_t, U_t) per channel with L_t = max_{t'>=t} cmin_{t'} and
+// U_t = min(D + 1, min_{t'<=t} cmax_{t'}) (D = the pair's dyes on that
+// channel); the binomial and Edman steps in between use the boxes derived
+// from these two; the pair is empty iff some L_t >= U_t, i.e. iff the read is
+// empty on its own or L_0 > D on some channel.  tests/test_oracle.py checks
+// this closed form against the literal prune passes of the oracle.
+#include <cuda_runtime.h>
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "wp_common.cuh"
+
+
+// ChannelModel::adjusted_mu (parameterization/model/channel-model.h:35-54).
+__device__ double dev_adjusted_mu(const DevModel& m, int channel, const unsigned* counts) {
+    double amu = m.mu[channel];
+    amu *= (double)counts[channel];
+    for (int c = 0; c < m.C; c++) {
+        if (c == channel) {
+            if (counts[c] > 1) {
+                amu *= m.flat[channel][c];
+                amu *= pow(m.inter[channel][c], (double)(counts[c] - 1));
+            }
+        } else if (counts[c] > 0) {
+            amu *= m.flat[channel][c];
+            amu *= pow(m.inter[channel][c], (double)counts[c]);
+        }
+    }
+    return amu;
+}
+
+__device__ double dev_sigma(const DevModel& m, int c, double amu) {
+    return sqrt(m.bg_sig[c] * m.bg_sig[c] + amu * m.sig[c] * m.sig[c]);
+}
+
+// ChannelModel::pdf_helper (channel-model.h:61-70).
+__device__ double dev_pdf(const DevModel& m, int c, double observed, const unsigned* counts) {
+    const double pi = 3.141592653589793238;
+    double amu = dev_adjusted_mu(m, c, counts);
+    double offset = observed - amu;
+    double s = dev_sigma(m, c, amu);
+    return (1.0 / (s * sqrt(2.0 * pi))) * exp(-offset * offset / (2.0 * s * s));
+}
+
+__device__ EmitEntry make_entry(double v) {
+    EmitEntry e;
+    if (v > 0.0 && isfinite(v)) {
+        int ex;
+        double mant = frexp(v, &ex);
+        e.mant = (float)mant;
+        e.expo = ex;
+        if (e.mant >= 1.0f) {  // rounding up to 1.0
+            e.mant = 0.5f;
+            e.expo += 1;
+        }
+    } else {
+        e.mant = 0.0f;
+        e.expo = WP_EXPO_ZERO;
+    }
+    return e;
+}
+
+// One thread per (read, t).  Writes box_lo/box_hi[r][t][c] and the
+// emission entries of timestep t.
+__global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
+                                     const double* __restrict__ rads, int R,
+                                     unsigned max_num_dyes, double dist_cutoff,
+                                     uint8_t* __restrict__ box_lo,
+                                     uint8_t* __restrict__ box_hi,
+                                     EmitEntry* __restrict__ table, int entries_per_read) {
+    const DevModel& m = *model;
+    const int T = m.T, C = m.C;
+    long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long)R * T) return;
+    int r = (int)(gid / T), t = (int)(gid % T);
+    const double* rad = rads + (long)r * T * C;
+    unsigned lo[WP_MAX_CHANNELS], hi[WP_MAX_CHANNELS];
+    // PeptideEmission ctor pruned_range (peptide-emission.cc:50-163).
+    if (dist_cutoff == DBL_MAX) {
+        for (int c = 0; c < C; c++) {
+            lo[c] = 0;
+            hi[c] = max_num_dyes + 1;
+        }
+    } else {
+        unsigned counts_lo[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+        unsigned counts_hi[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+        bool did_change = true;
+        int guard = 0;
+        // The reference loops to a fixed point without a bound and cycles
+        // forever for intensities below about -0.5 mu; stop after 1000
+        // rounds (the oracle uses the same bound).
+        while (did_change && guard < 1000) {
+            did_change = false;
+            guard++;
+            for (int c = 0; c < C; c++) {
+                unsigned old = counts_hi[c];
+                counts_hi[c] = 1;
+                double mu1 = dev_adjusted_mu(m, c, counts_hi);
+                counts_hi[c] = old;
+                double mu = dev_adjusted_mu(m, c, counts_hi);
+                double s = dist_cutoff * dev_sigma(m, c, mu);
+                unsigned new_cts = (unsigned)lround((rad[t * C + c] + s) / mu1);
+                if (new_cts > max_num_dyes + 1) new_cts = max_num_dyes + 1;
+                if (new_cts != counts_hi[c]) {
+                    did_change = true;
+                    counts_hi[c] = new_cts;
+                }
+            }
+        }
+        for (int c = 0; c < C; c++) {
+            unsigned cmin = max_num_dyes + 1;
+            for (unsigned d = 0; d < max_num_dyes + 1; d++) {
+                counts_lo[c] = d;
+                double mu = dev_adjusted_mu(m, c, counts_lo);
+                double s = dist_cutoff * dev_sigma(m, c, mu);
+                if (mu + s > rad[t * C + c]) {
+                    cmin = d;
+                    break;
+                }
+            }
+            counts_lo[c] = 0;
+            unsigned cmax = max_num_dyes + 1;
+            unsigned old = counts_hi[c];
+            for (unsigned d = cmin; d < max_num_dyes + 1; d++) {
+                counts_hi[c] = d;
+                double mu = dev_adjusted_mu(m, c, counts_hi);
+                double s = dist_cutoff * dev_sigma(m, c, mu);
+                if (mu - s > rad[t * C + c]) {
+                    cmax = d;
+                    break;
+                }
+            }
+            counts_hi[c] = old;
+            lo[c] = cmin;
+            hi[c] = cmax;
+        }
+    }
+    for (int c = 0; c < C; c++) {
+        box_lo[((long)r * T + t) * C + c] = (uint8_t)lo[c];
+        box_hi[((long)r * T + t) * C + c] = (uint8_t)hi[c];
+    }
+    // Emission factors (peptide-emission.cc:167-180): the product over
+    // channels of the Gaussian pdf, zero outside the box.
+    const int W = (int)max_num_dyes + 1;
+    EmitEntry* out = table + (long)r * entries_per_read;
+    if (!m.interacting) {
+        // pdf of channel c depends on n_c only: store per (t, c, n).
+        for (int c = 0; c < C; c++) {
+            for (int n = 0; n < W; n++) {
+                double v = 0.0;
+                if ((unsigned)n >= lo[c] && (unsigned)n < hi[c]) {
+                    unsigned counts[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+                    counts[c] = (unsigned)n;
+                    v = dev_pdf(m, c, rad[t * C + c], counts);
+                }
+                out[(t * C + c) * W + n] = make_entry(v);
+            }
+        }
+    } else {
+        int G = wp_ipow(W, C);
+        for (int g = 0; g < G; g++) {
+            unsigned counts[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+            int rem = g;
+            bool in_box = true;
+            for (int c = C - 1; c >= 0; c--) {
+                counts[c] = (unsigned)(rem % W);
+                rem /= W;
+                if (counts[c] < lo[c] || counts[c] >= hi[c]) in_box = false;
+            }
+            double v = 0.0;
+            if (in_box) {
+                v = 1.0;
+                for (int c = 0; c < C; c++) v *= dev_pdf(m, c, rad[t * C + c], counts);
+            }
+            out[t * G + g] = make_entry(v);
+        }
+    }
+}
+
+
+// One thread per read.
+__global__ void wp_read_summary_kernel(BatchArgs a) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.R) return;
+    const DevModel& m = *a.model;
+    const int T = m.T, C = m.C;
+    const uint8_t* lo = a.lo + (long)r * T * C;
+    const uint8_t* hi = a.hi + (long)r * T * C;
+    uint8_t* Ls = a.Lsuf + (long)r * T * C;
+    uint8_t* Up = a.Upre + (long)r * T * C;
+    int L[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+    for (int t = T - 1; t >= 0; t--)
+        for (int c = 0; c < C; c++) {
+            L[c] = max(L[c], (int)lo[t * C + c]);
+            Ls[t * C + c] = (uint8_t)L[c];
+        }
+    int U[WP_MAX_CHANNELS] = {255, 255, 255, 255};
+    int empty = 0;
+    for (int t = 0; t < T; t++) {
+        int allow = 1;
+        for (int c = 0; c < C; c++) {
+            U[c] = min(U[c], (int)hi[t * C + c]);
+            Up[t * C + c] = (uint8_t)U[c];
+            int l = Ls[t * C + c];
+            if (l >= U[c]) empty = 1;
+            // PeptideEmission::prune_* sets allow_detached =
+            // pruned_range.includes_zero() (peptide-emission.cc:198-210).
+            if (l != 0 || U[c] == 0) allow = 0;
+        }
+        a.allow[(long)r * T + t] = (uint8_t)allow;
+    }
+    a.flags[r] = (uint8_t)empty;
+}
+
+// One CTA per read.  Warp-aggregated appends keep each warp's pairs
+// contiguous in the work list (they share the read's data in L1).
+__global__ void wp_compact_kernel(BatchArgs a) {
+    const int r = blockIdx.x;
+    const DevModel& m = *a.model;
+    const int C = m.C;
+    const int g0 = slot_begin(a, r);
+    const int g1 = a.slot_off ? a.slot_off[r + 1] : g0 + a.P;
+    const bool read_empty = a.flags[r] != 0;
+    int minD[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+    for (int c = 0; c < C; c++) minD[c] = a.Lsuf[(long)r * m.T * C + c];  // L_0
+    const int lane = threadIdx.x & 31;
+    for (int base = g0; base < g1; base += blockDim.x) {
+        int g = base + threadIdx.x;
+        bool live = false;
+        if (g < g1) {
+            int p = slot_pep(a, r, g);
+            const PeptideRec& pep = a.peps[p];
+            live = !read_empty;
+            for (int c = 0; c < C; c++)
+                if (pep.D[c] < minD[c]) live = false;
+            if (!live) {
+                a.res_mant[g] = 0.0f;
+                a.res_expo[g] = 0;
+            }
+        }
+        unsigned mask = __ballot_sync(0xffffffffu, live);
+        int n = __popc(mask);
+        int pos = 0;
+        if (lane == 0 && n) pos = atomicAdd(a.work_count, n);
+        pos = __shfl_sync(0xffffffffu, pos, 0);
+        if (live) a.work[pos + __popc(mask & ((1u << lane) - 1))] = make_int2(r, g);
+    }
+}

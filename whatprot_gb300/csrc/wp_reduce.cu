@@ -1,0 +1,208 @@
+// wp_reduce.cu -- per-read reductions over the per-pair probabilities, the
+// visited-work counter and the FP32 throughput probe.
+//
+//   wp_reduce_kernel        one warp per read: HMMClassifier::classify_helper
+//                           (classifiers/hmm-classifier.h:45-78) -- the best
+//                           peptide (strict '>', so the first candidate wins
+//                           ties), its probability, the total weighted by
+//                           peptide multiplicity, and the NaN patch
+//                           (:73-76).  Deterministic: fixed lane assignment
+//                           and a fixed butterfly.
+//   wp_logp_kernel          log P per slot.
+//   wp_count_flops_kernel   the pruned schedule's visited-state op count.
+//   wp_fma_probe_kernel     FP32 FMA throughput.
+#include <cuda_runtime.h>
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "wp_common.cuh"
+
+// A probability mant * 2^expo (mant in [0.5, 1) or 0) with its tie key.
+struct Cand {
+    float mant;
+    int expo;
+    int key;
+    int idx;  // < 0: no candidate
+};
+
+// True if a beats b: larger probability, then smaller key (the reference's
+// strict '>' over candidates in order, classifiers/hmm-classifier.h:62).
+__device__ __forceinline__ bool cand_better(const Cand& a, const Cand& b) {
+    if (a.idx < 0) return false;
+    if (b.idx < 0) return true;
+    bool az = a.mant == 0.0f, bz = b.mant == 0.0f;
+    if (az && bz) return a.key < b.key;
+    if (az) return false;
+    if (bz) return true;
+    if (a.expo != b.expo) return a.expo > b.expo;
+    if (a.mant != b.mant) return a.mant > b.mant;
+    return a.key < b.key;
+}
+
+
+// One warp per read (blockDim.x == 128: four reads per CTA).
+__global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
+                                 double* __restrict__ out_score, double* __restrict__ out_total,
+                                 double* __restrict__ out_log, const int* __restrict__ pep_ids) {
+    const int r = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x % 32;
+    if (r >= a.R) return;
+    const int g0 = slot_begin(a, r);
+    const int g1 = a.slot_off ? a.slot_off[r + 1] : g0 + a.P;
+    Cand best = {0.0f, 0, INT_MAX, -1};
+    for (int g = g0 + lane; g < g1; g += 32) {
+        Cand c = {a.res_mant[g], a.res_expo[g], g - g0, g};
+        if (cand_better(c, best)) best = c;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        Cand c;
+        c.mant = __shfl_xor_sync(0xffffffffu, best.mant, o);
+        c.expo = __shfl_xor_sync(0xffffffffu, best.expo, o);
+        c.key = __shfl_xor_sync(0xffffffffu, best.key, o);
+        c.idx = __shfl_xor_sync(0xffffffffu, best.idx, o);
+        if (cand_better(c, best)) best = c;
+    }
+    const int E = best.mant > 0.0f ? best.expo : 0;
+    double tot = 0.0;
+    for (int g = g0 + lane; g < g1; g += 32) {
+        float mm = a.res_mant[g];
+        if (mm > 0.0f) tot += (double)a.counts[slot_pep(a, r, g)] * ldexp((double)mm, a.res_expo[g] - E);
+    }
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    if (lane != 0) return;
+    if (best.idx < 0) {  // no candidates
+        out_id[r] = -1;
+        out_score[r] = 0.0;
+        out_total[r] = 1.0;
+        if (out_log) out_log[r] = -INFINITY;
+        return;
+    }
+    out_id[r] = pep_ids[slot_pep(a, r, best.idx)];
+    const double sc = (double)best.mant;
+    if (!(tot > 0.0) || isnan(sc / tot)) {
+        out_score[r] = 0.0;
+        out_total[r] = 1.0;
+        if (out_log) out_log[r] = -INFINITY;
+        return;
+    }
+    const double s_abs = ldexp(sc, E), t_abs = ldexp(tot, E);
+    if (s_abs >= DBL_MIN && isfinite(s_abs) && isfinite(t_abs)) {
+        out_score[r] = s_abs;
+        out_total[r] = t_abs;
+    } else {  // outside the double range: same power of two on both
+        out_score[r] = sc;
+        out_total[r] = tot;
+    }
+    if (out_log) out_log[r] = log(sc) + (double)E * 0.69314718055994530942;
+}
+
+// log P per slot (-inf where P == 0).
+__global__ void wp_logp_kernel(const float* __restrict__ mant, const int* __restrict__ expo, long n,
+                               double* __restrict__ out) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float mm = mant[i];
+    out[i] = mm > 0.0f ? log((double)mm) + (double)expo[i] * 0.69314718055994530942 : -INFINITY;
+}
+
+// ---------------------------------------------------------------- flops --
+
+// Visited-state operation count of the reference's pruned schedule for one
+// pair, from the closed-form boxes (see the header comment).  One thread per
+// (read, peptide).  Sums per read into out[r] (exact: integers < 2^53).
+__global__ void wp_count_flops_kernel(BatchArgs a, double* __restrict__ out) {
+    const DevModel& m = *a.model;
+    const int T = m.T, C = m.C;
+    long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long)a.R * a.P) return;
+    int r = (int)(gid / a.P), p = (int)(gid % a.P);
+    const uint8_t* lo = a.lo + (long)r * T * C;
+    const uint8_t* hi = a.hi + (long)r * T * C;
+    const PeptideRec& pep = a.peps[p];
+    int L[WP_MAX_TIMESTEPS][WP_MAX_CHANNELS], U[WP_MAX_TIMESTEPS][WP_MAX_CHANNELS];
+    for (int c = 0; c < C; c++) {
+        int l = 0;
+        for (int t = T - 1; t >= 0; t--) {
+            l = max(l, (int)lo[t * C + c]);
+            L[t][c] = l;
+        }
+        int u = pep.D[c] + 1;
+        for (int t = 0; t < T; t++) {
+            u = min(u, (int)hi[t * C + c]);
+            U[t][c] = u;
+        }
+    }
+    for (int t = 0; t < T; t++)
+        for (int c = 0; c < C; c++)
+            if (L[t][c] >= U[t][c]) return;  // empty: no work
+    double fl = 0.0;
+    // t = 0
+    {
+        double vol_init = 1.0, vol_emit = 1.0;
+        for (int c = 0; c < C; c++) {
+            vol_init *= (double)(pep.D[c] + 1 - L[0][c]);
+            vol_emit *= (double)(U[0][c] - L[0][c]);
+        }
+        if (m.p_ib != 0.0f) fl += 3.0 * vol_init;
+        for (int c = 0; c < C; c++) {
+            double fibers = 1.0;
+            for (int c2 = 0; c2 < C; c2++) {
+                if (c2 == c) continue;
+                fibers *= (c2 < c) ? (double)(U[0][c2] - L[0][c2]) : (double)(pep.D[c2] + 1 - L[0][c2]);
+            }
+            double macs = 0.0;
+            for (int to = L[0][c]; to < U[0][c]; to++) macs += (double)(pep.D[c] + 1 - to);
+            fl += 2.0 * fibers * macs;
+        }
+        fl += 1.0 * vol_emit + 2.0 * vol_emit;
+    }
+    for (int t = 1; t < T; t++) {
+        double vol_prev = 1.0, vol_bt = 1.0, vol_next = 1.0;
+        int Bt[WP_MAX_CHANNELS];
+        for (int c = 0; c < C; c++) {
+            Bt[c] = min(U[t][c] + 1, U[t - 1][c]);
+            vol_prev *= (double)(U[t - 1][c] - L[t - 1][c]);
+            vol_bt *= (double)(Bt[c] - L[t][c]);
+            vol_next *= (double)(U[t][c] - L[t][c]);
+        }
+        if (m.p_cb != 0.0f) fl += 3.0 * t * vol_prev;
+        fl += 2.0 * t * vol_prev;  // detach
+        for (int c = 0; c < C; c++) {
+            double fibers = (double)t;
+            for (int c2 = 0; c2 < C; c2++) {
+                if (c2 == c) continue;
+                fibers *= (c2 < c) ? (double)(Bt[c2] - L[t][c2]) : (double)(U[t - 1][c2] - L[t - 1][c2]);
+            }
+            double macs = 0.0;
+            for (int to = L[t][c]; to < Bt[c]; to++) {
+                int from_min = max(to, L[t - 1][c]);
+                if (U[t - 1][c] > from_min) macs += (double)(U[t - 1][c] - from_min);
+            }
+            fl += 2.0 * fibers * macs;
+        }
+        fl += 6.0 * t * vol_bt;             // Edman
+        fl += 3.0 * (t + 1) * vol_next;     // emission + rescale
+    }
+    atomicAdd(&out[r], fl);
+}
+
+// ------------------------------------------------------------ FP32 peak --
+
+// Eight independent FMA chains per thread; the result is stored so that the
+// chains are not removed.  2 flops per FMA.
+__global__ void wp_fma_probe_kernel(int iters, float* sink) {
+    float a0 = threadIdx.x * 1e-3f, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3;
+    float a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+    const float b = 0.999f, c = 1e-3f;
+    for (int i = 0; i < iters; i++) {
+        a0 = fmaf(a0, b, c); a1 = fmaf(a1, b, c); a2 = fmaf(a2, b, c); a3 = fmaf(a3, b, c);
+        a4 = fmaf(a4, b, c); a5 = fmaf(a5, b, c); a6 = fmaf(a6, b, c); a7 = fmaf(a7, b, c);
+    }
+    sink[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+cudaError_t wp_launch_fma_probe(int blocks, int threads, int iters, cudaStream_t stream, float* sink) {
+    wp_fma_probe_kernel<<<blocks, threads, 0, stream>>>(iters, sink);
+    return cudaGetLastError();
+}
