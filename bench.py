@@ -250,6 +250,7 @@ def main():
     barrier()
     clk = clocks.stop()
     launches = ctx.launch_count() - launches0
+    work = ctx.last_batch_stats()
     fwd_ms, fwd_n = ctx.timing_read(ctx.KIND_FORWARD)
     prep_ms, _ = ctx.timing_read(ctx.KIND_PREP)
     ctx.timing_enable(False)
@@ -288,7 +289,7 @@ def main():
                 "peak_source": "FP32 FMA loop measured live (wp_probe_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                 "algorithmic_flops_per_step": algo_flops,
                 "forward_ms_per_step": fwd_ms / args.steps, "prep_ms_per_step": prep_ms / args.steps,
-                "forward_launches_per_step": fwd_n / args.steps}
+                "forward_launches_per_step": fwd_n / args.steps, "work": work}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded simulator)",

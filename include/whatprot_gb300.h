@@ -142,6 +142,12 @@ wp_status wp_hmm_count_flops(wp_ctx* ctx, const double* rads, int num_reads,
 /* Kernel launches issued by this context since creation (all kinds). */
 long long wp_launch_count(const wp_ctx* ctx);
 
+/* Work statistics of the last batch run on this context (synchronises):
+ * stats[0] (read, peptide) slots, [1] slots the pruning left non-empty,
+ * [2] pairs spilled past the first engine pass, [3] pairs spilled past the
+ * second to the dense fallback.  No reference counterpart. */
+wp_status wp_last_batch_stats(wp_ctx* ctx, long long* stats4);
+
 /* The context's CUDA stream (a cudaStream_t), for callers that order their
  * own work or events against it.  No reference counterpart. */
 void* wp_ctx_stream(const wp_ctx* ctx);

@@ -28,7 +28,7 @@ STATUS = {0: "WP_OK", 1: "WP_ERR_INVALID", 2: "WP_ERR_OOM", 3: "WP_ERR_CUDA",
 EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload",
            "wp_peptides_upload", "wp_hmm_classify", "wp_hmm_classify_device",
            "wp_hmm_loglik_all", "wp_hmm_count_flops", "wp_launch_count", "wp_ctx_stream",
-           "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak"]
+           "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak", "wp_last_batch_stats"]
 
 
 class WpSeqModel(ctypes.Structure):
@@ -95,6 +95,8 @@ def load_library(path: Optional[str] = None):
     lib.wp_timing_read.restype = I
     lib.wp_probe_fp32_peak.argtypes = [V, ctypes.POINTER(D)]
     lib.wp_probe_fp32_peak.restype = I
+    lib.wp_last_batch_stats.argtypes = [V, V]
+    lib.wp_last_batch_stats.restype = I
     if path is None:
         _lib = lib
     return lib
@@ -209,6 +211,12 @@ class Context:
         n = ctypes.c_longlong()
         self._check(self.lib.wp_timing_read(self.h, kind, ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
+
+    def last_batch_stats(self) -> dict:
+        out = np.zeros(4, np.int64)
+        self._check(self.lib.wp_last_batch_stats(self.h, _ptr(out)))
+        return {"slots": int(out[0]), "nonempty": int(out[1]), "spilled_pass2": int(out[2]),
+                "spilled_dense": int(out[3])}
 
     def fp32_peak_tflops(self) -> float:
         out = ctypes.c_double()

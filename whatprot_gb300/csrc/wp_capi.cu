@@ -110,6 +110,7 @@ struct wp_ctx {
     double t_ms[4] = {0, 0, 0, 0};
     long long t_n[4] = {0, 0, 0, 0};
     int last_engine_grid = 0;
+    long long last_slots = 0;
 
     // Per-batch scratch.
     DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_allow, d_flags, d_table, d_res_mant, d_res_expo,
@@ -331,6 +332,7 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         a.cand = ctx->d_cand.as<int>();
         a.slot_off = ctx->d_slot_off.as<int>();
     }
+    ctx->last_slots = n_slots;
     const size_t ns = (size_t)std::max<long>(n_slots, 1);
     WP_CUDA(ctx->d_res_mant.ensure(sizeof(float) * ns), "alloc results");
     WP_CUDA(ctx->d_res_expo.ensure(sizeof(int) * ns), "alloc results");
@@ -470,6 +472,22 @@ const char* wp_last_error(const wp_ctx* ctx) { return ctx ? ctx->err.c_str() : "
 long long wp_launch_count(const wp_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 void* wp_ctx_stream(const wp_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+wp_status wp_last_batch_stats(wp_ctx* ctx, long long* stats) {
+    if (!ctx || !stats) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    int c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (ctx->d_counters.p) {
+        WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        WP_CUDA(cudaMemcpy(c, ctx->d_counters.p, sizeof(c), cudaMemcpyDeviceToHost), "read counters");
+    }
+    stats[0] = ctx->last_slots;
+    stats[1] = c[0];
+    stats[2] = c[2];
+    stats[3] = c[4];
+    return WP_OK;
+}
 
 wp_status wp_timing_enable(wp_ctx* ctx, int enable) {
     if (!ctx) return WP_ERR_INVALID;
