@@ -166,6 +166,29 @@ wp_status wp_timing_read(wp_ctx* ctx, int kind, double* total_ms, long long* lau
  * every SM.  The denominator of the forward kernel's roofline. */
 wp_status wp_probe_fp32_peak(wp_ctx* ctx, double* tflops);
 
+/* Classify without allocating any memory.  No counterpart in the reference:
+ * it exists for callers that cannot call cudaMalloc, such as an
+ * acquisition loop that may not stall the device with an allocation or a
+ * host that runs this library under a memory budget it does not own.  Same
+ * kernels and results as wp_hmm_classify (all peptides as candidates), but
+ * every input copy and intermediate buffer lives in one device array of
+ * 64 MiB that is part of the library (every GPU that loads the library holds
+ * it until the process exits); no context, stream or event is created.  All
+ * pointers are host pointers; the call runs on the legacy default stream of
+ * `device` and returns when the outputs are written.  The first call on a
+ * device looks up the array's device address (set-up) and must come before
+ * any stream capture.  Inputs whose buffers do not fit the array (32 bytes
+ * per (read, peptide) pair plus under 1 KB per read and per peptide: about
+ * two million pairs) are rejected with WP_ERR_UNSUPPORTED.  Calls share the array: calls that overlap on the GPU
+ * race; calls through this entry point in one process are serialised. */
+wp_status wp_hmm_classify_noalloc(int device, const wp_seq_model* model,
+                                  int num_timesteps, const int16_t* dye_seqs,
+                                  const int32_t* offsets, const int32_t* ids,
+                                  const int32_t* counts, int num_peptides,
+                                  const double* rads, int num_reads,
+                                  double dist_cutoff, int32_t* out_id,
+                                  double* out_score, double* out_total);
+
 #ifdef __cplusplus
 }
 #endif
