@@ -72,7 +72,7 @@ struct DevBuf {
 
 // Engine pass shapes (threads per CTA).
 constexpr int kPass1Threads = 256;
-constexpr int kPass2Threads = 128;
+constexpr int kPass2Threads = 256;
 
 }  // namespace
 
@@ -98,7 +98,7 @@ struct wp_ctx {
     int S_max = 1;       // max over peptides of prod_c (D_c + 1)
     int scr_floats = 1;  // max over peptides of sum_c (D_c + 1)
     std::vector<PeptideRec> recs;
-    DevBuf d_peps, d_ids, d_counts;
+    DevBuf d_peps, d_ids, d_counts, d_perm;
 
     // Kernel timing.
     bool timing = false;
@@ -113,7 +113,7 @@ struct wp_ctx {
     long long last_slots = 0;
 
     // Per-batch scratch.
-    DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_allow, d_flags, d_table, d_res_mant, d_res_expo,
+    DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_Lpk, d_Upk, d_allow, d_flags, d_table, d_res_mant, d_res_expo,
             d_work, d_ovf1, d_ovf2, d_counters, d_cand, d_slot_off, d_out_id, d_out_score,
             d_out_total, d_out_log, d_logp, d_flops, d_err;
 };
@@ -229,6 +229,19 @@ wp_status plan_peptides(wp_ctx* ctx) {
             if (d >= 0) rem[d]--;
         }
     }
+    // Shape order (Edman-slice size, then dye counts) for the compaction.
+    std::vector<int> perm(P);
+    for (int i = 0; i < P; i++) perm[i] = i;
+    auto key = [&](int i) {
+        long k = 1;
+        for (int c = 0; c < C; c++) k *= ctx->recs[i].D[c] + 1;
+        for (int c = 0; c < C; c++) k = k * 16 + ctx->recs[i].D[c];
+        return k;
+    };
+    std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return key(x) < key(y); });
+    WP_CUDA(ctx->d_perm.ensure(sizeof(int) * std::max(P, 1)), "alloc perm");
+    WP_CUDA(cudaMemcpyAsync(ctx->d_perm.p, perm.data(), sizeof(int) * P, cudaMemcpyHostToDevice, ctx->stream),
+            "copy perm");
     WP_CUDA(ctx->d_peps.ensure(sizeof(PeptideRec) * std::max(P, 1)), "alloc peptides");
     WP_CUDA(cudaMemcpyAsync(ctx->d_peps.p, ctx->recs.data(), sizeof(PeptideRec) * P,
                             cudaMemcpyHostToDevice, ctx->stream), "copy peptides");
@@ -250,7 +263,7 @@ int slab_half_for(wp_ctx* ctx, int threads, int per_sm, bool hb) {
     size_t budget = (size_t)ctx->smem_optin;
     if (per_sm > 1) budget = std::min(budget, (size_t)(228 * 1024) / per_sm - 1024);
     size_t elem = hb ? 8 : 4;
-    size_t fixed = wp_engine_smem_bytes(0, ctx->scr_floats, hb, threads);
+    size_t fixed = wp_engine_smem_bytes(0, 0, hb, threads);
     if (budget <= fixed) return 0;
     return (int)((budget - fixed) / (2 * elem * threads));
 }
@@ -278,6 +291,8 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
     WP_CUDA(ctx->d_Ls.ensure(rtc), "alloc");
     WP_CUDA(ctx->d_Up.ensure(rtc), "alloc");
     WP_CUDA(ctx->d_allow.ensure((size_t)R * T), "alloc");
+    WP_CUDA(ctx->d_Lpk.ensure(sizeof(uint32_t) * (size_t)R * T), "alloc");
+    WP_CUDA(ctx->d_Upk.ensure(sizeof(uint32_t) * (size_t)R * T), "alloc");
     WP_CUDA(ctx->d_flags.ensure((size_t)R), "alloc");
     WP_CUDA(ctx->d_table.ensure(sizeof(EmitEntry) * (size_t)R * entries), "alloc emission table");
     WP_CUDA(ctx->d_err.ensure(sizeof(int)), "alloc");
@@ -297,6 +312,8 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
     a.Lsuf = ctx->d_Ls.as<uint8_t>();
     a.Upre = ctx->d_Up.as<uint8_t>();
     a.allow = ctx->d_allow.as<uint8_t>();
+    a.Lpk = ctx->d_Lpk.as<uint32_t>();
+    a.Upk = ctx->d_Upk.as<uint32_t>();
     a.flags = ctx->d_flags.as<uint8_t>();
     a.tab = ctx->d_table.as<EmitEntry>();
     a.err = ctx->d_err.as<int>();
@@ -331,6 +348,8 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         WP_CUDA(cudaMemcpyAsync(ctx->d_slot_off.p, h_cand_off, sizeof(int) * (R + 1), cudaMemcpyHostToDevice, ctx->stream), "copy cand");
         a.cand = ctx->d_cand.as<int>();
         a.slot_off = ctx->d_slot_off.as<int>();
+    } else {
+        a.perm = ctx->d_perm.as<int>();
     }
     ctx->last_slots = n_slots;
     const size_t ns = (size_t)std::max<long>(n_slots, 1);
@@ -365,25 +384,25 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
                 dense_warps = w;
                 break;
             }
-        // Pass 1: two CTAs of 256 threads per SM; pass 2: one CTA of 128.
+        // Pass 1: two CTAs of 256 threads per SM; pass 2: one CTA of 256
+        // with twice the slab; the dense kernel takes what is left.
         int half1 = slab_half_for(ctx, kPass1Threads, 2, hb);
         int half2 = slab_half_for(ctx, kPass2Threads, 1, hb);
         if (half1 < 4 || half2 < 4)
             return fail(ctx, WP_ERR_UNSUPPORTED, "shared memory too small for the pair engine");
         {
             TimedLaunch tl(ctx, 0);
-            size_t smem = wp_engine_smem_bytes(half1, ctx->scr_floats, hb, kPass1Threads);
+            size_t smem = wp_engine_smem_bytes(half1, 0, hb, kPass1Threads);
             WP_CUDA(wp_launch_engine(C, hb, kPass1Threads, smem, ctx->stream, a, a.work, cnt + 0, cnt + 1,
-                                     ctx->d_ovf1.as<int2>(), cnt + 2, half1, ctx->scr_floats, 0,
+                                     ctx->d_ovf1.as<int2>(), cnt + 2, half1, 0, 0,
                                      &ctx->last_engine_grid), "engine pass 1");
             ctx->launches++;
         }
         {
             TimedLaunch tl(ctx, 0);
-            size_t smem = wp_engine_smem_bytes(half2, ctx->scr_floats, hb, kPass2Threads);
+            size_t smem = wp_engine_smem_bytes(half2, 0, hb, kPass2Threads);
             WP_CUDA(wp_launch_engine(C, hb, kPass2Threads, smem, ctx->stream, a, ctx->d_ovf1.as<int2>(),
-                                     cnt + 2, cnt + 3, ctx->d_ovf2.as<int2>(), cnt + 4, half2,
-                                     ctx->scr_floats, dense_warps == 0 ? 1 : 0, nullptr), "engine pass 2");
+                                     cnt + 2, cnt + 3, ctx->d_ovf2.as<int2>(), cnt + 4, half2, 0, dense_warps == 0 ? 1 : 0, nullptr), "engine pass 2");
             ctx->launches++;
         }
         if (dense_warps > 0) {

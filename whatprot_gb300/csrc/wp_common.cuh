@@ -92,9 +92,12 @@ struct BatchArgs {
     uint8_t* Lsuf;             // max_{t' >= t} cmin
     uint8_t* Upre;             // min_{t' <= t} cmax
     uint8_t* allow;            // per (r, t): the emission box includes zero
+    uint32_t* Lpk;             // per (r, t): L per channel in bits 8c..8c+6, bit 31 = allow
+    uint32_t* Upk;             // per (r, t): U byte per channel
     uint8_t* flags;            // per r: bit 0 = the read prunes every pair
     const EmitEntry* tab;      // per read: emission factors
     const int* cand;           // per slot: peptide index (null: all peptides)
+    const int* perm;           // all-peptides mode: peptides in shape order (or null)
     const int* slot_off;       // [R + 1] or null
     float* res_mant;           // per slot: P = res_mant * 2^res_expo
     int* res_expo;

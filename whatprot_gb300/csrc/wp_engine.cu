@@ -12,11 +12,17 @@
 // State storage.  A pair's state is one dense box per step (row-major over
 // Edman count e and the dye count of each channel, anchored at the box's
 // lower corner).  Each thread owns a slab of shared memory holding two such
-// boxes (ping-pong) plus its per-channel emission factors; slabs are
-// interleaved across the CTA's threads (element k of thread i at
-// k * blockDim.x + i) so every access of a warp hits 32 distinct banks
-// whatever the index.  A pair whose largest box does not fit its slab is
-// handed to the overflow list (wp_dense.cu).
+// boxes (ping-pong); slabs are interleaved across the CTA's threads (element
+// k of thread i at k * blockDim.x + i) so every access of a warp hits 32
+// distinct banks whatever the index.  A pair whose largest box does not fit
+// its slab is handed to the next pass's list (wp_capi.cu).
+//
+// Boxes are kept packed, one byte per channel in a 32-bit word (lower
+// corner) and another (width), so that the per-channel loops need no
+// unrolling; the binomial step is one out-of-line routine shared by the dud
+// and bleach steps, and the rarely taken paths (wide boxes, interacting
+// channels) are out of line too.  This keeps the timestep loop small enough
+// for the instruction cache.
 //
 // With blocking (p_initial_block or p_cyclic_block nonzero) each state holds
 // the normal and the broken-N value as a float2.
@@ -49,51 +55,77 @@ __device__ __forceinline__ float2 vmul(float k, float2 v) { return make_float2(k
 __device__ __forceinline__ float vtotal(float v) { return v; }
 __device__ __forceinline__ float vtotal(float2 v) { return v.x + v.y; }
 
-// Box of one step: per-channel [lo, lo + w).
-template <int C>
-struct Box {
-    int lo[C];
-    int w[C];
-    __device__ __forceinline__ int vol() const {
-        int v = 1;
-#pragma unroll
-        for (int c = 0; c < C; c++) v *= w[c];
-        return v;
-    }
+// Packed box: byte c of lo / w is channel c's lower corner / width.
+struct PBox {
+    uint32_t lo;
+    uint32_t w;
 };
+__device__ __forceinline__ int bget(uint32_t v, int c) { return (int)((v >> (8 * c)) & 0xffu); }
+__device__ __forceinline__ uint32_t bset(uint32_t v, int c, int x) {
+    return (v & ~(0xffu << (8 * c))) | ((uint32_t)x << (8 * c));
+}
+template <int C>
+__device__ __forceinline__ int bvol(uint32_t w) {
+    int v = 1;
+#pragma unroll
+    for (int c = 0; c < C; c++) v *= bget(w, c);
+    return v;
+}
 
-// Binomial transition along channel c (BinomialTransition::forward,
-// hmm/step/binomial-transition.cc:104-136) from box `in` to box `out`, which
-// differ only on channel c, over E Edman slices:
+// Binomial transition along channel ch (BinomialTransition::forward,
+// hmm/step/binomial-transition.cc:104-136) from box `in` to the box with
+// channel ch moved to [to0, to0 + wout), over E Edman slices:
 //   out[to] = sum_{from >= to, from in box} prob(from, to) * in[from].
 template <int C, class V>
-__device__ __forceinline__ void binomial_boxes(const V* __restrict__ src, V* __restrict__ dst,
-                                               int stride, int E, const Box<C>& in,
-                                               const Box<C>& out, int ch,
-                                               const float* __restrict__ tab) {
-    int outer = E, inner = 1, win = 1, wout = 1, from0 = 0, to0 = 0;
+__device__ __noinline__ void binomial_step(const V* __restrict__ src, V* __restrict__ dst, int stride,
+                                           int E, PBox in, int ch, int to0, int wout,
+                                           const float* __restrict__ tab) {
+    int outer = E, inner = 1;
 #pragma unroll
     for (int c = 0; c < C; c++) {
-        if (c < ch) outer *= in.w[c];
-        if (c > ch) inner *= in.w[c];
-        if (c == ch) {
-            win = in.w[c];
-            wout = out.w[c];
-            from0 = in.lo[c];
-            to0 = out.lo[c];
+        const int w = bget(in.w, c);
+        if (c < ch) outer *= w;
+        if (c > ch) inner *= w;
+    }
+    const int win = bget(in.w, ch), from0 = bget(in.lo, ch);
+    const int sk = inner * stride;
+    if (win <= 4) {
+        // Coefficients depend on (to, from) only: load them once per output
+        // row, then one predicated dot product per column.
+        for (int k2 = 0; k2 < wout; k2++) {
+            const int to = to0 + k2;
+            float cf[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int from = from0 + k;
+                cf[k] = (k < win && from >= to) ? tab[from * (from + 1) / 2 + to] : 0.0f;
+            }
+            for (int o = 0; o < outer; o++) {
+                const V* s = src + o * win * sk;
+                V* d = dst + (o * wout + k2) * sk;
+                for (int i = 0; i < inner; i++) {
+                    const V* si = s + i * stride;
+                    V acc = vmul(cf[0], si[0]);
+                    if (win > 1) acc = vfma(cf[1], si[sk], acc);
+                    if (win > 2) acc = vfma(cf[2], si[2 * sk], acc);
+                    if (win > 3) acc = vfma(cf[3], si[3 * sk], acc);
+                    d[i * stride] = acc;
+                }
+            }
         }
+        return;
     }
     for (int o = 0; o < outer; o++) {
         for (int k2 = 0; k2 < wout; k2++) {
             const int to = to0 + k2;
             const int kmin = max(0, to - from0);
-            const V* s = src + (o * win) * inner * stride;
-            V* d = dst + ((o * wout + k2) * inner) * stride;
+            const V* s = src + o * win * sk;
+            V* d = dst + (o * wout + k2) * sk;
             for (int i = 0; i < inner; i++) {
                 V acc = vzero(V());
                 for (int k = kmin; k < win; k++) {
                     const int from = from0 + k;
-                    acc = vfma(tab[from * (from + 1) / 2 + to], s[(k * inner + i) * stride], acc);
+                    acc = vfma(tab[from * (from + 1) / 2 + to], s[k * sk + i * stride], acc);
                 }
                 d[i * stride] = acc;
             }
@@ -101,74 +133,187 @@ __device__ __forceinline__ void binomial_boxes(const V* __restrict__ src, V* __r
     }
 }
 
+// Emission multiply for boxes with a channel wider than 4, or interacting
+// channels: the factor of each state read from the table.  Returns the sum
+// of the multiplied states; *kmax_out receives the normalising exponent
+// (WP_EXPO_ZERO: every factor is zero), *em0 the factor of the all-zero
+// state (unscaled by the pending rescale).
+template <int C, class V>
+__device__ __noinline__ float emission_table(V* cur, int stride, int t, PBox nx, int W,
+                                             const EmitEntry* __restrict__ tab, bool interacting,
+                                             float fac_prev, int k_prev, int* kmax_out, float* em0) {
+    const int vn = bvol<C>(nx.w);
+    const int G = interacting ? wp_ipow(W, C) : 0;
+    int jc[C];
+    // pass 1: normalising exponent over the box
+    int kmax = 0;
+    if (!interacting) {
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+            const EmitEntry* row = tab + (t * C + c) * W + bget(nx.lo, c);
+            int km = WP_EXPO_ZERO;
+            for (int k = 0; k < bget(nx.w, c); k++)
+                if (row[k].mant != 0.0f) km = max(km, row[k].expo);
+            if (km == WP_EXPO_ZERO) {
+                *kmax_out = WP_EXPO_ZERO;
+                return 0.0f;
+            }
+            kmax += km;
+        }
+    } else {
+        int km = WP_EXPO_ZERO;
+#pragma unroll
+        for (int c = 0; c < C; c++) jc[c] = 0;
+        for (int j = 0; j < vn; j++) {
+            int gi = 0;
+#pragma unroll
+            for (int c = 0; c < C; c++) gi = gi * W + bget(nx.lo, c) + jc[c];
+            EmitEntry en = tab[t * G + gi];
+            if (en.mant != 0.0f) km = max(km, en.expo);
+#pragma unroll
+            for (int c = C - 1; c >= 0; c--) {
+                if (++jc[c] < bget(nx.w, c)) break;
+                jc[c] = 0;
+            }
+        }
+        if (km == WP_EXPO_ZERO) {
+            *kmax_out = WP_EXPO_ZERO;
+            return 0.0f;
+        }
+        kmax = km;
+    }
+    *kmax_out = kmax;
+    // factor of the all-zero state (only used when the box starts at zero)
+    {
+        float mm = 1.0f;
+        int ks = 0;
+        if (!interacting) {
+#pragma unroll
+            for (int c = 0; c < C; c++) {
+                EmitEntry en = tab[(t * C + c) * W];
+                mm *= en.mant;
+                ks += en.expo;
+            }
+        } else {
+            EmitEntry en = tab[t * G];
+            mm = en.mant;
+            ks = en.expo;
+        }
+        *em0 = mm != 0.0f ? mm * exp2i(max(ks - kmax, -200)) : 0.0f;
+    }
+    // pass 2: multiply
+    float part = 0.0f;
+#pragma unroll
+    for (int c = 0; c < C; c++) jc[c] = 0;
+    for (int j = 0; j < vn; j++) {
+        float mm = fac_prev;
+        int ks = 0;
+        if (!interacting) {
+#pragma unroll
+            for (int c = 0; c < C; c++) {
+                EmitEntry en = tab[(t * C + c) * W + bget(nx.lo, c) + jc[c]];
+                mm *= en.mant;
+                ks += en.expo;
+            }
+        } else {
+            int gi = 0;
+#pragma unroll
+            for (int c = 0; c < C; c++) gi = gi * W + bget(nx.lo, c) + jc[c];
+            EmitEntry en = tab[t * G + gi];
+            mm *= en.mant;
+            ks = en.expo;
+        }
+        const float w = mm != 0.0f ? mm * exp2i(max(ks - kmax - k_prev, -200)) : 0.0f;
+        for (int e = 0; e <= t; e++) {
+            V s = vmul(w, cur[(e * vn + j) * stride]);
+            cur[(e * vn + j) * stride] = s;
+            part += vtotal(s);
+        }
+#pragma unroll
+        for (int c = C - 1; c >= 0; c--) {
+            if (++jc[c] < bget(nx.w, c)) break;
+            jc[c] = 0;
+        }
+    }
+    return part;
+}
+
 // Runs one pair.  Returns 1 when its boxes exceed the slab (nothing
 // written), else 0 with P = *mant * 2^*expo (mant == 0: P == 0).
 template <int C, bool HB>
 __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
-                           const PeptideRec& pep, typename StateOf<HB>::V* slab,
-                           float* scr, int stride, int half, float* out_mant, int* out_expo) {
+                           const PeptideRec& pep, typename StateOf<HB>::V* slab, int stride,
+                           int half, float* out_mant, int* out_expo) {
     using V = typename StateOf<HB>::V;
     const DevModel& m = *a.model;
     const int T = m.T;
-    const uint8_t* Ls = a.Lsuf + (long)r * T * C;
-    const uint8_t* Up = a.Upre + (long)r * T * C;
-    const uint8_t* allow = a.allow + (long)r * T;
     const EmitEntry* tab = a.tab + (long)r * a.entries;
-    int D1[C];
+    const uint32_t* Lpk = a.Lpk + (long)r * T;
+    const uint32_t* Upk = a.Upk + (long)r * T;
+    uint32_t D1 = 0;  // D_c + 1 per channel, packed
 #pragma unroll
-    for (int c = 0; c < C; c++) D1[c] = pep.D[c] + 1;
+    for (int c = 0; c < C; c++) D1 = bset(D1, c, pep.D[c] + 1);
+    // Emission box of timestep t: [L_t, min(U_t, D + 1)), packed.
+    auto emission_box = [&](int t) {
+        const uint32_t lw = Lpk[t], uw = Upk[t];
+        PBox b;
+        b.lo = lw & 0x7f7f7f7fu;  // bit 31 of the word is the allow flag
+        b.w = 0;
+#pragma unroll
+        for (int c = 0; c < C; c++) b.w = bset(b.w, c, min(bget(uw, c), bget(D1, c)) - bget(b.lo, c));
+        return b;
+    };
 
-    // Boxes per timestep: Nx_t = [L_t, U_t) (emission), Bt_t = [L_t,
-    // min(U_t + 1, U_{t-1})) (bleach output / Edman input).  First pass:
-    // the largest box any step of this pair uses.
-    int need;
+    // First pass: the largest box any step of this pair uses (emission box
+    // Nx_t, bleach output / Edman input box [L_t, min(U_t + 1, U_{t-1}))
+    // and the mixed boxes in between).
     {
-        int v0 = 1, vmax = 0;
+        PBox p = emission_box(0);
+        int vmax = 1;
 #pragma unroll
-        for (int c = 0; c < C; c++) v0 *= D1[c] - Ls[c];
-        vmax = v0;
+        for (int c = 0; c < C; c++) vmax *= bget(D1, c) - bget(p.lo, c);
         for (int t = 1; t < T; t++) {
-            int vp = t, vb = t, vn = t + 1;
-            int mix[C];
+            const PBox n = emission_box(t);
+            int vp = t, vb = t, vn = t + 1, vm = t;
 #pragma unroll
             for (int c = 0; c < C; c++) {
-                int lp = Ls[(t - 1) * C + c], up = min((int)Up[(t - 1) * C + c], D1[c]);
-                int ln = Ls[t * C + c], un = min((int)Up[t * C + c], D1[c]);
-                int bu = min(un + 1, up);
-                vp *= up - lp;
-                vb *= bu - ln;
-                vn *= un - ln;
-                mix[c] = (bu - ln) > (up - lp) ? (bu - ln) : (up - lp);
+                const int wp = bget(p.w, c), ln = bget(n.lo, c), wn = bget(n.w, c);
+                const int wb = min(ln + wn + 1, bget(p.lo, c) + wp) - ln;
+                vp *= wp;
+                vb *= wb;
+                vn *= wn;
+                vm *= max(wb, wp);
             }
-            int vm = t;
-#pragma unroll
-            for (int c = 0; c < C; c++) vm *= mix[c];
             vmax = max(vmax, max(max(vp, vb), max(vn, vm)));
+            p = n;
         }
-        need = vmax;
+        if (vmax > half) return 1;
     }
-    if (need > half) return 1;
+    // Dye channel and remaining dyes of that channel per Edman position,
+    // packed 4 bits each (positions < 16) so the Edman loop reads registers.
+    const bool pk = T <= 17;
+    uint64_t dye_pk = 0, tot_pk = 0;
+    if (pk) {
+        for (int e = 0; e + 1 < T; e++) {
+            dye_pk |= (uint64_t)((pep.dye[e] + 1) & 15) << (4 * e);
+            tot_pk |= (uint64_t)(pep.tot[e] & 15) << (4 * e);
+        }
+    }
 
     V* cur = slab;
     V* nxt = slab + half * stride;
-    auto swap_bufs = [&]() {
-        V* tmp = cur;
-        cur = nxt;
-        nxt = tmp;
-    };
 
     // ---- t = 0: start state (0, D) (peptide-state-vector.cc:38-40) in the
     // box [L_0, D + 1), initial block, duds.
-    Box<C> bx;
+    PBox bx;
+    bx.lo = Lpk[0] & 0x7f7f7f7fu;
+    bx.w = 0;
 #pragma unroll
-    for (int c = 0; c < C; c++) {
-        bx.lo[c] = Ls[c];
-        bx.w[c] = D1[c] - Ls[c];
-    }
+    for (int c = 0; c < C; c++) bx.w = bset(bx.w, c, bget(D1, c) - bget(bx.lo, c));
     {
-        int v = bx.vol();
+        const int v = bvol<C>(bx.w);
         for (int i = 0; i < v - 1; i++) cur[i * stride] = vzero(V());
-        V start = vzero(V());
+        V start;
         if constexpr (HB) {
             start = make_float2(1.0f - m.p_ib, m.p_ib);  // block-transition.cc:33-62
         } else {
@@ -176,14 +321,17 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         }
         cur[(v - 1) * stride] = start;
     }
-#pragma unroll
-    for (int c = 0; c < C; c++) {
-        Box<C> ob = bx;
-        int u0 = min((int)Up[c], D1[c]);
-        ob.w[c] = u0 - bx.lo[c];
-        binomial_boxes<C, V>(cur, nxt, stride, 1, bx, ob, c, M.dud[c]);
-        swap_bufs();
-        bx = ob;
+    {
+        const PBox n0 = emission_box(0);
+#pragma unroll 1
+        for (int c = 0; c < C; c++) {
+            const int wout = bget(n0.w, c);
+            binomial_step<C, V>(cur, nxt, stride, 1, bx, c, bget(bx.lo, c), wout, M.dud[c]);
+            V* tmp = cur;
+            cur = nxt;
+            nxt = tmp;
+            bx.w = bset(bx.w, c, wout);
+        }
     }
 
     int expo = 0;           // the true state is the stored state times 2^expo
@@ -191,18 +339,14 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
     int k_prev = 0;         // exponent removed at the last rescale
     float fac_prev = 1.0f;  // (1 - p_detach) pending from the last timestep
     for (int t = 0; t < T; t++) {
-        Box<C> nx;  // emission box [L_t, U_t)
-#pragma unroll
-        for (int c = 0; c < C; c++) {
-            nx.lo[c] = Ls[t * C + c];
-            nx.w[c] = min((int)Up[t * C + c], D1[c]) - nx.lo[c];
-        }
+        const PBox nx = emission_box(t);
+        const bool allow_t = (Lpk[t] >> 31) != 0;
         if (t > 0) {
             // Cyclic block (block-transition.cc:33-62) over e < t and the
             // previous emission box.
             if constexpr (HB) {
                 if (m.p_cb != 0.0f) {
-                    int n = t * bx.vol();
+                    const int n = t * bvol<C>(bx.w);
                     for (int i = 0; i < n; i++) {
                         float2 s = cur[i * stride];
                         cur[i * stride] = make_float2((1.0f - m.p_cb) * s.x, s.y + m.p_cb * s.x);
@@ -213,49 +357,62 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             // rescale: pd already holds it, fac_prev carries (1 - p).
             // Bleach per channel: channel c moves from the previous box to
             // [L_t, min(U_t + 1, U_{t-1})).
-#pragma unroll
+#pragma unroll 1
             for (int c = 0; c < C; c++) {
-                Box<C> ob = bx;
-                int bu = min(nx.lo[c] + nx.w[c] + 1, bx.lo[c] + bx.w[c]);
-                ob.lo[c] = nx.lo[c];
-                ob.w[c] = bu - nx.lo[c];
-                binomial_boxes<C, V>(cur, nxt, stride, t, bx, ob, c, M.bleach[c]);
-                swap_bufs();
-                bx = ob;
+                const int ln = bget(nx.lo, c);
+                const int bu = min(ln + bget(nx.w, c) + 1, bget(bx.lo, c) + bget(bx.w, c));
+                binomial_step<C, V>(cur, nxt, stride, t, bx, c, ln, bu - ln, M.bleach[c]);
+                V* tmp = cur;
+                cur = nxt;
+                nxt = tmp;
+                bx.lo = bset(bx.lo, c, ln);
+                bx.w = bset(bx.w, c, bu - ln);
             }
-            // Edman (edman-transition.cc:62-162) as a gather from slices
-            // e-1 (success) and e (failure) into the emission box.
+            // Edman (edman-transition.cc:62-162) as a gather from slices e-1
+            // (success) and e (failure) of the bleached box into the
+            // emission box; both boxes share the lower corner L_t.
             {
                 const float pf = m.pf, qf = 1.0f - m.pf;
-                int stb[C], stn[C];
-                int vb = 1, vn = 1;
+                int stb[C];
+                int vb = 1;
 #pragma unroll
                 for (int c = C - 1; c >= 0; c--) {
                     stb[c] = vb;
-                    stn[c] = vn;
-                    vb *= bx.w[c];
-                    vn *= nx.w[c];
+                    vb *= bget(bx.w, c);
                 }
+                const int vn = bvol<C>(nx.w);
                 for (int e = 0; e <= t; e++) {
-                    int dc = e >= 1 ? pep.dye[e - 1] : -1;
-                    float tot = e >= 1 ? (float)pep.tot[e - 1] : 1.0f;
-                    // Select the removal channel's box terms once per slice.
+                    int dc = -1, tot_i = 1;
+                    if (e >= 1) {
+                        if (pk) {
+                            dc = (int)((dye_pk >> (4 * (e - 1))) & 15) - 1;
+                            tot_i = (int)((tot_pk >> (4 * (e - 1))) & 15);
+                        } else {
+                            dc = pep.dye[e - 1];
+                            tot_i = pep.tot[e - 1];
+                        }
+                    }
+                    // (1 - p_fail) / DyeTrack(e - 1, dc): one reciprocal per slice.
+                    const float c1 = dc >= 0 ? qf * __frcp_rn((float)tot_i) : 0.0f;
                     int d_lo = 0, d_wb = 0, d_st = 0;
 #pragma unroll
                     for (int c = 0; c < C; c++)
                         if (c == dc) {
-                            d_lo = nx.lo[c];
-                            d_wb = bx.w[c];
+                            d_lo = bget(nx.lo, c);
+                            d_wb = bget(bx.w, c);
                             d_st = stb[c];
                         }
                     int jc[C];
 #pragma unroll
                     for (int c = 0; c < C; c++) jc[c] = 0;
                     int ib = 0;
+                    const V* fail_row = cur + e * vb * stride;
+                    const V* succ_row = cur + (e - 1) * vb * stride;
+                    V* out_row = nxt + e * vn * stride;
                     for (int j = 0; j < vn; j++) {
                         V v = vzero(V());
                         if (e < t) {
-                            V f = cur[(e * vb + ib) * stride];
+                            const V f = fail_row[ib * stride];
                             if constexpr (HB) {
                                 v = make_float2(pf * f.x, f.y);  // broken-N copied unchanged
                             } else {
@@ -265,9 +422,9 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
                         if (e >= 1) {
                             float xin;
                             if constexpr (HB) {
-                                xin = cur[((e - 1) * vb + ib) * stride].x;
+                                xin = succ_row[ib * stride].x;
                             } else {
-                                xin = cur[((e - 1) * vb + ib) * stride];
+                                xin = succ_row[ib * stride];
                             }
                             float add;
                             if (dc < 0) {
@@ -278,16 +435,15 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
                                 for (int c = 0; c < C; c++)
                                     if (c == dc) jd = jc[c];
                                 const int nc = d_lo + jd;
-                                add = 0.0f;
-                                if ((float)nc < tot) add = qf * (1.0f - (float)nc / tot) * xin;
+                                add = nc < tot_i ? fmaf(-(float)nc, c1, qf) * xin : 0.0f;
                                 if (jd + 1 < d_wb) {
                                     float xr;
                                     if constexpr (HB) {
-                                        xr = cur[((e - 1) * vb + ib + d_st) * stride].x;
+                                        xr = succ_row[(ib + d_st) * stride].x;
                                     } else {
-                                        xr = cur[((e - 1) * vb + ib + d_st) * stride];
+                                        xr = succ_row[(ib + d_st) * stride];
                                     }
-                                    add = fmaf(qf * ((float)(nc + 1) / tot), xr, add);
+                                    add = fmaf((float)(nc + 1) * c1, xr, add);
                                 }
                             }
                             if constexpr (HB) {
@@ -296,139 +452,106 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
                                 v += add;
                             }
                         }
-                        nxt[(e * vn + j) * stride] = v;
+                        out_row[j * stride] = v;
                         // advance the multi-index over the emission box
 #pragma unroll
                         for (int c = C - 1; c >= 0; c--) {
                             jc[c]++;
                             ib += stb[c];
-                            if (jc[c] < nx.w[c]) break;
-                            ib -= stb[c] * nx.w[c];
+                            if (jc[c] < bget(nx.w, c)) break;
+                            ib -= stb[c] * bget(nx.w, c);
                             jc[c] = 0;
                         }
                     }
                 }
-                swap_bufs();
+                V* tmp = cur;
+                cur = nxt;
+                nxt = tmp;
                 bx = nx;
             }
         }
-        // ---- Emission t (peptide-emission.cc:212-243).  Per-channel factors
-        // normalised by their largest exponent over the pair's box, stored
-        // in the scratch; the pending rescale is folded into the multiplier.
+        // ---- Emission t (peptide-emission.cc:212-243).  Factors normalised
+        // by the largest exponent over the pair's box (a power of two, carried
+        // in expo); the pending rescale is folded into the multiplier.
         int kmax = 0;
-        bool dead = false;
-        int goff[C];
-        {
-            int off = 0;
-#pragma unroll
-            for (int c = 0; c < C; c++) {
-                goff[c] = off;
-                off += nx.w[c];
-            }
-        }
-        if (!m.interacting) {
-#pragma unroll
-            for (int c = 0; c < C; c++) {
-                const EmitEntry* row = tab + (t * C + c) * a.W + nx.lo[c];
-                int km = WP_EXPO_ZERO;
-                for (int k = 0; k < nx.w[c]; k++)
-                    if (row[k].mant != 0.0f) km = max(km, row[k].expo);
-                if (km == WP_EXPO_ZERO) dead = true;
-                kmax += km;
-                for (int k = 0; k < nx.w[c]; k++) {
-                    EmitEntry en = row[k];
-                    scr[(goff[c] + k) * stride] =
-                            en.mant != 0.0f ? en.mant * exp2i(max(en.expo - km, -200)) : 0.0f;
-                }
-            }
-        }
-        if (dead) {
-            *out_mant = 0.0f;
-            *out_expo = 0;
-            return 0;
-        }
-        const float sfac = fac_prev * exp2i(-k_prev);
         float part = 0.0f;
         float em0 = 0.0f;
-        const int vn = nx.vol();
-        if (!m.interacting) {
-            // emission factor of state n is prod_c g_c[n_c - L_t]
-            if (allow[t]) {
-                em0 = 1.0f;
+        bool narrow = !m.interacting;
 #pragma unroll
-                for (int c = 0; c < C; c++) em0 *= scr[goff[c] * stride];
-            }
-            int jc[C];
+        for (int c = 0; c < C; c++) narrow = narrow && bget(nx.w, c) <= 4;
+        if (narrow) {
+            // Per channel: the box's entries normalised by their largest
+            // exponent, in registers; the factor of state n is
+            // prod_c g[c][n_c - L_t] * 2^kmax.
+            float g[C][4];
+            bool dead = false;
 #pragma unroll
-            for (int c = 0; c < C; c++) jc[c] = 0;
-            for (int j = 0; j < vn; j++) {
-                float w = sfac;
+            for (int c = 0; c < C; c++) {
+                const EmitEntry* row = tab + (t * C + c) * a.W + bget(nx.lo, c);
+                const int wc = bget(nx.w, c);
+                EmitEntry en[4];
+                int km = WP_EXPO_ZERO;
 #pragma unroll
-                for (int c = 0; c < C; c++) w *= scr[(goff[c] + jc[c]) * stride];
-                for (int e = 0; e <= t; e++) {
-                    V s = vmul(w, cur[(e * vn + j) * stride]);
-                    cur[(e * vn + j) * stride] = s;
-                    part += vtotal(s);
+                for (int k = 0; k < 4; k++) {
+                    en[k].mant = 0.0f;
+                    en[k].expo = WP_EXPO_ZERO;
+                    if (k < wc) en[k] = row[k];
+                    if (en[k].mant != 0.0f) km = max(km, en[k].expo);
                 }
 #pragma unroll
-                for (int c = C - 1; c >= 0; c--) {
-                    jc[c]++;
-                    if (jc[c] < nx.w[c]) break;
-                    jc[c] = 0;
-                }
+                for (int k = 0; k < 4; k++)
+                    g[c][k] = en[k].mant != 0.0f ? en[k].mant * exp2i(max(en[k].expo - km, -200)) : 0.0f;
+                if (km == WP_EXPO_ZERO) dead = true;
+                kmax += km;
             }
-        } else {
-            // Interacting channels: one factor per dye-count vector.
-            const int G = wp_ipow(a.W, C);
-            int km = WP_EXPO_ZERO;
-            int jc[C];
-#pragma unroll
-            for (int c = 0; c < C; c++) jc[c] = 0;
-            for (int j = 0; j < vn; j++) {
-                int gi = 0;
-#pragma unroll
-                for (int c = 0; c < C; c++) gi = gi * a.W + nx.lo[c] + jc[c];
-                EmitEntry en = tab[t * G + gi];
-                if (en.mant != 0.0f) km = max(km, en.expo);
-#pragma unroll
-                for (int c = C - 1; c >= 0; c--) {
-                    jc[c]++;
-                    if (jc[c] < nx.w[c]) break;
-                    jc[c] = 0;
-                }
-            }
-            if (km == WP_EXPO_ZERO) {
+            if (dead) {
                 *out_mant = 0.0f;
                 *out_expo = 0;
                 return 0;
             }
-            kmax = km;
-            if (allow[t]) {
-                EmitEntry en = tab[t * G];
-                em0 = en.mant != 0.0f ? en.mant * exp2i(max(en.expo - km, -200)) : 0.0f;
-            }
-            for (int j = 0; j < vn; j++) {
-                int gi = 0;
+            if (allow_t) {
+                em0 = 1.0f;
 #pragma unroll
-                for (int c = 0; c < C; c++) gi = gi * a.W + nx.lo[c] + jc[c];
-                EmitEntry en = tab[t * G + gi];
-                float w = en.mant != 0.0f ? sfac * (en.mant * exp2i(max(en.expo - km, -200))) : 0.0f;
+                for (int c = 0; c < C; c++) em0 *= g[c][0];
+            }
+            // the pending rescale 2^-k_prev (1 - p) of the last timestep
+            const float sf = fac_prev * exp2i(min(-k_prev, 127));
+            const int vn = bvol<C>(nx.w);
+            int jc[C];
+#pragma unroll
+            for (int c = 0; c < C; c++) jc[c] = 0;
+            for (int j = 0; j < vn; j++) {
+                float w = sf;
+#pragma unroll
+                for (int c = 0; c < C; c++) {
+                    const int k = jc[c];
+                    w *= k == 0 ? g[c][0] : k == 1 ? g[c][1] : k == 2 ? g[c][2] : g[c][3];
+                }
+                V* col = cur + j * stride;
                 for (int e = 0; e <= t; e++) {
-                    V s = vmul(w, cur[(e * vn + j) * stride]);
-                    cur[(e * vn + j) * stride] = s;
+                    V s = vmul(w, col[e * vn * stride]);
+                    col[e * vn * stride] = s;
                     part += vtotal(s);
                 }
 #pragma unroll
                 for (int c = C - 1; c >= 0; c--) {
-                    jc[c]++;
-                    if (jc[c] < nx.w[c]) break;
+                    if (++jc[c] < bget(nx.w, c)) break;
                     jc[c] = 0;
                 }
             }
+        } else {
+            part = emission_table<C, V>(cur, stride, t, nx, a.W, tab, m.interacting != 0, fac_prev, k_prev,
+                                        &kmax, &em0);
+            if (kmax == WP_EXPO_ZERO) {
+                *out_mant = 0.0f;
+                *out_expo = 0;
+                return 0;
+            }
+            if (!allow_t) em0 = 0.0f;
         }
         // Detached state: kept only while the box includes zero
         // (peptide-emission.cc:218-223).
-        pd = allow[t] ? pd * em0 : 0.0f;
+        pd = allow_t ? pd * em0 : 0.0f;
         expo += kmax;
         const float tot = part + pd;
         if (!(tot > 0.0f) || !isfinite(tot)) {
@@ -456,7 +579,6 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
     return 0;
 }
 
-// Persistent: each warp takes 32 consecutive work items at a time.
 // Lists one engine pass reads and spills to.
 struct EngineLists {
     const int2* in;
@@ -465,10 +587,11 @@ struct EngineLists {
     int2* out;
     int* out_count;
     int slab_half;
-    int scr_floats;
+    int scr_floats;   // reserved per-thread scratch (floats), 0 when unused
     int spill_error;  // nonzero: nothing downstream takes spills; flag err
 };
 
+// Persistent: each warp takes 32 consecutive work items at a time.
 template <int C, bool HB>
 __global__ void __launch_bounds__(WP_ENGINE_THREADS) wp_engine_kernel(BatchArgs a, EngineLists L) {
     using V = typename StateOf<HB>::V;
@@ -478,9 +601,7 @@ __global__ void __launch_bounds__(WP_ENGINE_THREADS) wp_engine_kernel(BatchArgs 
     __syncthreads();
     const int nt = blockDim.x;
     V* slab_region = reinterpret_cast<V*>(smem_raw + ((sizeof(SmemModel) + 15) & ~(size_t)15));
-    float* scr_region = reinterpret_cast<float*>(slab_region + (size_t)2 * L.slab_half * nt);
     V* slab = slab_region + threadIdx.x;
-    float* scr = scr_region + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const int count = *L.in_count;
     for (;;) {
@@ -494,7 +615,7 @@ __global__ void __launch_bounds__(WP_ENGINE_THREADS) wp_engine_kernel(BatchArgs 
             const int p = slot_pep(a, rg.x, rg.y);
             float mant;
             int ex;
-            int ov = engine_pair<C, HB>(a, M, rg.x, a.peps[p], slab, scr, nt, L.slab_half, &mant, &ex);
+            int ov = engine_pair<C, HB>(a, M, rg.x, a.peps[p], slab, nt, L.slab_half, &mant, &ex);
             if (ov) {
                 if (L.spill_error) {
                     atomicExch(a.err, 2);

@@ -170,6 +170,7 @@ extern "C" wp_status wp_hmm_classify_noalloc(int device, const wp_seq_model* m, 
     const size_t o_rads = take(sizeof(double) * rtc);
     const size_t o_lo = take(rtc), o_hi = take(rtc), o_Ls = take(rtc), o_Up = take(rtc);
     const size_t o_allow = take((size_t)R * T), o_flags = take((size_t)R);
+    const size_t o_Lpk = take(sizeof(uint32_t) * (size_t)R * T), o_Upk = take(sizeof(uint32_t) * (size_t)R * T);
     const size_t o_table = take(sizeof(EmitEntry) * (size_t)R * entries);
     const size_t o_mant = take(sizeof(float) * n_slots), o_expo = take(sizeof(int) * n_slots);
     const size_t o_work = take(sizeof(int2) * n_slots), o_ovf1 = take(sizeof(int2) * n_slots),
@@ -227,6 +228,8 @@ extern "C" wp_status wp_hmm_classify_noalloc(int device, const wp_seq_model* m, 
     a.Lsuf = base + o_Ls;
     a.Upre = base + o_Up;
     a.allow = base + o_allow;
+    a.Lpk = reinterpret_cast<uint32_t*>(base + o_Lpk);
+    a.Upk = reinterpret_cast<uint32_t*>(base + o_Upk);
     a.flags = base + o_flags;
     a.tab = reinterpret_cast<const EmitEntry*>(base + o_table);
     a.res_mant = reinterpret_cast<float*>(base + o_mant);

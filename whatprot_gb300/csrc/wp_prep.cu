@@ -37,14 +37,17 @@ __device__ double dev_adjusted_mu(const DevModel& m, int channel, const unsigned
     double amu = m.mu[channel];
     amu *= (double)counts[channel];
     for (int c = 0; c < m.C; c++) {
+        // A factor of exactly 1 leaves amu unchanged (pow(1, n) == 1 and
+        // x * 1 == x), so the common no-interaction case skips the pow.
+        const double fi = m.flat[channel][c], ii = m.inter[channel][c];
         if (c == channel) {
             if (counts[c] > 1) {
-                amu *= m.flat[channel][c];
-                amu *= pow(m.inter[channel][c], (double)(counts[c] - 1));
+                if (fi != 1.0) amu *= fi;
+                if (ii != 1.0) amu *= pow(ii, (double)(counts[c] - 1));
             }
         } else if (counts[c] > 0) {
-            amu *= m.flat[channel][c];
-            amu *= pow(m.inter[channel][c], (double)counts[c]);
+            if (fi != 1.0) amu *= fi;
+            if (ii != 1.0) amu *= pow(ii, (double)counts[c]);
         }
     }
     return amu;
@@ -219,6 +222,7 @@ __global__ void wp_read_summary_kernel(BatchArgs a) {
     int empty = 0;
     for (int t = 0; t < T; t++) {
         int allow = 1;
+        uint32_t lpk = 0, upk = 0;
         for (int c = 0; c < C; c++) {
             U[c] = min(U[c], (int)hi[t * C + c]);
             Up[t * C + c] = (uint8_t)U[c];
@@ -227,8 +231,13 @@ __global__ void wp_read_summary_kernel(BatchArgs a) {
             // PeptideEmission::prune_* sets allow_detached =
             // pruned_range.includes_zero() (peptide-emission.cc:198-210).
             if (l != 0 || U[c] == 0) allow = 0;
+            lpk |= (uint32_t)l << (8 * c);
+            upk |= (uint32_t)U[c] << (8 * c);
         }
         a.allow[(long)r * T + t] = (uint8_t)allow;
+        // One word per (read, t) and bound: byte c is channel c.
+        a.Lpk[(long)r * T + t] = lpk | ((uint32_t)allow << 31);
+        a.Upk[(long)r * T + t] = upk;
     }
     a.flags[r] = (uint8_t)empty;
 }
@@ -246,9 +255,13 @@ __global__ void wp_compact_kernel(BatchArgs a) {
     for (int c = 0; c < C; c++) minD[c] = a.Lsuf[(long)r * m.T * C + c];  // L_0
     const int lane = threadIdx.x & 31;
     for (int base = g0; base < g1; base += blockDim.x) {
+        // In all-peptides mode walk the peptides in shape order, so that the
+        // engine's warps get pairs of similar size; results still go to
+        // their own slots, so the candidate order (ties) is unchanged.
         int g = base + threadIdx.x;
+        if (g < g1 && a.perm) g = g0 + a.perm[g - g0];
         bool live = false;
-        if (g < g1) {
+        if (base + threadIdx.x < g1) {
             int p = slot_pep(a, r, g);
             const PeptideRec& pep = a.peps[p];
             live = !read_empty;
