@@ -139,6 +139,80 @@ wp_status wp_hmm_loglik_all(wp_ctx* ctx, const double* rads, int num_reads,
 wp_status wp_hmm_count_flops(wp_ctx* ctx, const double* rads, int num_reads,
                              double dist_cutoff, double* out_flops);
 
+/* Stage a Baum-Welch fit: the dye-seq being fitted (-1 unlabeled, channel
+ * index otherwise) and the reads, [num_reads][T][C] host doubles divided by
+ * mu.  Replaces the data HMMFitter holds (fitters/hmm-fitter.h:35-48, 118-144:
+ * dye_seq, radiometries).  The reads stay on the device until the next
+ * wp_fit_begin or the context's destruction. */
+wp_status wp_fit_begin(wp_ctx* ctx, const int16_t* dye_seq, int length,
+                       const double* rads, int num_reads);
+
+/* One E-step with the context's current model (wp_model_upload): the
+ * expected counts of GenericHMM::improve_fit (hmm/hmm/generic-hmm.h:60-109)
+ * summed over every staged read, as HMMFitter::fit accumulates them
+ * (fitters/hmm-fitter.h:63-78), without pruning (main/run-fit.cc:59).
+ * Reads with P == 0 add nothing (generic-hmm.h:85-87) and are counted in
+ * *num_zero.  *sum_logp receives the sum of log P over the other reads
+ * (HMMFitter::log_likelihood, fitters/hmm-fitter.h:119-142).  Any output
+ * pointer but `out` may be NULL.  The dye-seq must have at most 15 dyes per
+ * channel and the model no channel interactions (WP_ERR_UNSUPPORTED). */
+wp_status wp_fit_estep(wp_ctx* ctx, wp_fit_sums* out, double* sum_logp,
+                       int* num_zero);
+
+/* Which parameters a fit holds at their starting values: FitSettings and
+ * ChannelFitSettings (parameterization/settings/fit-settings.h,
+ * channel-fit-settings.h).  Non-zero = hold. */
+typedef struct {
+    int hold_p_edman_failure;
+    int hold_p_detach;
+    int hold_p_initial_detach;
+    int hold_p_initial_detach_decay;
+    int hold_p_initial_block;
+    int hold_p_cyclic_block;
+    int hold_p_bleach[WP_MAX_CHANNELS];
+    int hold_p_dud[WP_MAX_CHANNELS];
+} wp_fit_settings;
+
+/* The fitted parameters of a SequencingModel (bg_sig, mu, sig and the
+ * interactions are never fitted: fitters/hmm-fitter.cc:94-95). */
+typedef struct {
+    double p_edman_failure;
+    double p_detach;
+    double p_initial_detach;
+    double p_initial_detach_decay;
+    double p_initial_block;
+    double p_cyclic_block;
+    double p_bleach[WP_MAX_CHANNELS];
+    double p_dud[WP_MAX_CHANNELS];
+} wp_fit_params;
+
+/* HMMFitter::fit (fitters/hmm-fitter.h:49-117) with its log_likelihood
+ * (:119-142): Baum-Welch from `start` on one dye-seq and R reads
+ * ([R][T][C] host doubles divided by mu), GPU E-steps (wp_fit_estep), the
+ * dud hidden-count correction and the M-step on the host; stops when the
+ * largest parameter change is below stopping_threshold or after max_runtime
+ * seconds of wall time.  settings may be NULL (fit everything).  Writes the
+ * fitted parameters, the last step size, the final log-likelihood (-inf if
+ * some read has P == 0 under the fitted model, as log(0) in the reference)
+ * and the number of E-steps (iterations may be NULL).  Stages the reads with
+ * wp_fit_begin and leaves the fitted model uploaded on the context. */
+wp_status wp_hmm_fit(wp_ctx* ctx, const wp_seq_model* start, int num_timesteps,
+                     const int16_t* dye_seq, int length, const double* rads,
+                     int num_reads, const wp_fit_settings* settings,
+                     double stopping_threshold, double max_runtime,
+                     wp_fit_params* out, double* step_size, double* log_l,
+                     int* iterations);
+
+/* Box-constrained weighted least-squares fit of base + initial *
+ * exp(-decay * i), i = 0..n-1, to y with weights w, parameters in [0, 1] and
+ * held ones fixed (held[k] != 0), at most 10 Levenberg-Marquardt iterations
+ * from params[3] (updated in place).  The detach M-step of
+ * DecayingParameterFitter::get (parameterization/fit/decaying-parameter-
+ * fitter.cc:42-66) through least_squares_fit_of_offset_exponential
+ * (util/levmar-helper.cc:44-85).  Host only. */
+wp_status wp_fit_offset_exponential(const double* y, const double* w, int n,
+                                    const int* held, double* params);
+
 /* Kernel launches issued by this context since creation (all kinds). */
 long long wp_launch_count(const wp_ctx* ctx);
 

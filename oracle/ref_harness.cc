@@ -28,6 +28,7 @@
 #include "parameterization/model/sequencing-model.h"
 #include "parameterization/settings/fit-settings.h"
 #include "parameterization/settings/sequencing-settings.h"
+#include "util/levmar-helper.h"
 #include "wp_oracle.h"
 
 using namespace whatprot;
@@ -208,6 +209,17 @@ double ref_fit(const wpo_model* start, int T, const char* dye_seq, int R,
             out->flat_interactions[c][o] = start->flat_interactions[c][o];
         }
     return log_l;
+}
+
+/* least_squares_fit_of_offset_exponential (util/levmar-helper.cc:44-85)
+ * on y, w (n points) from params[3], holds as non-zero held[k]. */
+void ref_offset_exponential(const double* y, const double* w, int n,
+                            const int* held, double* params) {
+    std::vector<double> yv(y, y + n), wv(w, w + n), p(params, params + 3);
+    std::vector<bool> hold(3);
+    for (int k = 0; k < 3; k++) hold[k] = held[k] != 0;
+    least_squares_fit_of_offset_exponential(yv, wv, hold, &p);
+    for (int k = 0; k < 3; k++) params[k] = p[k];
 }
 
 }  // extern "C"

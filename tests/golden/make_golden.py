@@ -65,10 +65,54 @@ def pair_fixture(name, C, T, P, nreads, seed):
     print(name, probs.shape, "nonzero pruned", int(np.sum(probs[0] > 0)))
 
 
+def fit_fixture(name, C, T, seq_str, nreads, threshold, seed, block=False):
+    """HMMFitter::fit of the reference on simulated reads of one dye-seq,
+    from a seeded perturbation (x0.5..x1.5) of the generating model."""
+    import copy
+    from whatprot_gb300.model import DyeSeqSet, parse_dye_seq
+    true = paper_model(C)
+    if block:
+        true.p_initial_block, true.p_cyclic_block = 0.07, 0.025
+        true.p_initial_detach, true.p_initial_detach_decay = 0.03, 0.04
+    seq = parse_dye_seq(seq_str)
+    ds = DyeSeqSet(num_channels=C, seqs=[seq], counts=np.array([1], np.int32), ids=np.array([0], np.int32))
+    rads, _ = simulate_radiometries(true, ds, T, nreads, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    start = copy.deepcopy(true)
+    f = lambda: rng.uniform(0.5, 1.5)
+    start.p_edman_failure *= f()
+    start.p_detach *= f()
+    start.p_initial_detach *= f()
+    start.p_initial_detach_decay *= f()
+    start.p_initial_block *= f()
+    start.p_cyclic_block *= f()
+    for cm in start.channel_models:
+        cm.p_bleach *= f()
+        cm.p_dud *= f()
+    out, ll, step, secs = Reference().fit(start, T, seq_str, rads, threshold)
+    def params(m):
+        get = (lambda c, k: getattr(m.channel_models[c], k)) if hasattr(m, "channel_models") else (
+            lambda c, k: getattr(m, k)[c])
+        return np.array([m.p_edman_failure, m.p_detach, m.p_initial_detach, m.p_initial_detach_decay,
+                         m.p_initial_block, m.p_cyclic_block]
+                        + [get(c, "p_bleach") for c in range(C)] + [get(c, "p_dud") for c in range(C)])
+    np.savez_compressed(os.path.join(HERE, name), C=C, T=T, seq=seq, seq_str=seq_str, rads=rads,
+                        threshold=threshold, start=params(start), bg_sig=[cm.bg_sig for cm in true.channel_models],
+                        sig=[cm.sig for cm in true.channel_models], ref_params=params(out), ref_log_l=ll,
+                        ref_step=step)
+    print(name, rads.shape, "ref fit", params(out), ll, step, f"{secs:.1f}s")
+
+
 if __name__ == "__main__":
     if not Reference.available():
         sys.exit("oracle/_ref/libwpref.so missing: run `make -C oracle ref` where the reference is present")
-    classify_fixture("classify_c2_t8.npz", 2, 8, 100, 6, 12, 300, 5.0, seed=101)
-    classify_fixture("classify_c3_t16.npz", 3, 16, 60, 8, 30, 60, 5.0, seed=202, maxc=5, mint=1)
-    classify_fixture("classify_c2_t6_block_nocut.npz", 2, 6, 30, 4, 10, 40, None, seed=303, block=True)
-    pair_fixture("pairs_c3_t6_block.npz", 3, 6, 12, 10, seed=404)
+    which = sys.argv[1:] or ["classify", "pairs", "fit"]
+    if "classify" in which:
+        classify_fixture("classify_c2_t8.npz", 2, 8, 100, 6, 12, 300, 5.0, seed=101)
+        classify_fixture("classify_c3_t16.npz", 3, 16, 60, 8, 30, 60, 5.0, seed=202, maxc=5, mint=1)
+        classify_fixture("classify_c2_t6_block_nocut.npz", 2, 6, 30, 4, 10, 40, None, seed=303, block=True)
+    if "pairs" in which:
+        pair_fixture("pairs_c3_t6_block.npz", 3, 6, 12, 10, seed=404)
+    if "fit" in which:
+        fit_fixture("fit_c2_t8.npz", 2, 8, "..0.1.0..1", 400, 1e-6, seed=505)
+        fit_fixture("fit_c2_t6_block.npz", 2, 6, "0.1.01", 300, 1e-6, seed=606, block=True)

@@ -213,6 +213,9 @@ class Reference:
         L.ref_improve_fit.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_char_p,
                                       ctypes.c_void_p, ctypes.c_uint, ctypes.c_double,
                                       ctypes.POINTER(WpoFitSums)]
+        L.ref_offset_exponential.restype = None
+        L.ref_offset_exponential.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                             ctypes.c_void_p, ctypes.c_void_p]
         L.ref_fit.restype = ctypes.c_double
         L.ref_fit.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                               ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.POINTER(WpoModel),
@@ -247,6 +250,14 @@ class Reference:
         p = self.lib.ref_improve_fit(ctypes.byref(m), T, seq_str.encode(), _p(rad), max_num_dyes,
                                      cutoff, ctypes.byref(sums))
         return p, sums
+
+    def offset_exponential(self, y, w, params, held=(0, 0, 0)):
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        p = np.ascontiguousarray(params, dtype=np.float64).copy()
+        h = np.ascontiguousarray(held, dtype=np.int32)
+        self.lib.ref_offset_exponential(_p(y), _p(w), len(y), _p(h), _p(p))
+        return p
 
     def fit(self, sm, T, seq_str, rads, threshold, max_runtime=1e9):
         m = to_wpo(sm)

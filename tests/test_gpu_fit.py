@@ -1,0 +1,181 @@
+"""Parity of the GPU Baum-Welch fit (wp_fit_estep, wp_hmm_fit) with the
+oracle's improve_fit and with fits recorded from the reference.
+
+Tolerances.  E-step: each expected count is a sum over reads of FP32
+state-vector products with exact power-of-two frames, accumulated in FP64;
+it must match the oracle's FP64 sum to a relative 1e-5 of the sum of the
+magnitudes involved (the denominator of the same parameter).  Sum of log P:
+|delta| <= 1e-5 per read.  Full fit: the reference stops when the largest
+parameter change falls below 1e-6, so fitted parameters are compared to
+1e-4 absolute, and the detach rate curve base + initial * exp(-decay * t)
+(identifiable even where base and initial trade off at decay = 0) to 1e-4.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from whatprot_gb300 import capi
+from whatprot_gb300.model import DyeSeqSet, parse_dye_seq
+from whatprot_gb300.simulate import paper_model, simulate_radiometries
+
+from conftest import GOLDEN  # noqa: F401
+
+pytestmark = pytest.mark.gpu
+
+
+def _model(C, block=False):
+    sm = paper_model(C)
+    if block:
+        sm.p_initial_block, sm.p_cyclic_block = 0.07, 0.025
+        sm.p_initial_detach, sm.p_initial_detach_decay = 0.03, 0.04
+    return sm
+
+
+def _reads(sm, seq, T, n, seed):
+    ds = DyeSeqSet(sm.num_channels, [seq], np.array([0], np.int32), np.array([1], np.int32))
+    rads, _ = simulate_radiometries(sm, ds, T, n, seed=seed)
+    return rads
+
+
+def _oracle_sums(oracle, sm, T, seq, rads):
+    from oracle_lib import WpoFitSums
+    dmax = max(int(np.sum(seq == c)) for c in range(sm.num_channels))
+    s = WpoFitSums()
+    lps = []
+    for r in rads:
+        _, lp, _ = oracle.improve_fit(sm, T, seq, r, dmax, sums=s)
+        lps.append(lp)
+    return s.as_dict(T, sm.num_channels), np.array(lps)
+
+
+def _close(g, o, scale, what):
+    g, o = np.asarray(g, float), np.asarray(o, float)
+    if g.size == 0:
+        assert o.size == 0, what
+        return
+    err = np.max(np.abs(g - o))
+    assert err <= 1e-5 * max(float(np.max(np.abs(scale))), 1e-300), (what, g, o)
+
+
+ESTEP_CASES = [
+    # C, T, dye-seq, reads, block
+    (2, 8, "..0.1.0..1", 64, False),
+    (2, 6, "0.1.01", 48, True),
+    (3, 10, "0.1.2.0.1.2", 40, False),
+    (1, 5, "..000", 30, True),
+    (3, 16, "0.1.2.0..1.2.0..1.2.0", 24, False),   # 4/3/3 dyes, T=16
+    (4, 6, "0123.0", 20, False),
+    (2, 1, "01", 16, True),
+]
+
+
+@pytest.mark.parametrize("case", ESTEP_CASES, ids=[f"C{c[0]}T{c[1]}{'B' if c[4] else ''}" for c in ESTEP_CASES])
+def test_estep_vs_oracle(gpu_ctx, oracle, case):
+    C, T, seq_str, n, block = case
+    sm = _model(C, block)
+    seq = parse_dye_seq(seq_str)
+    rads = _reads(sm, seq, T, n, seed=7 * len(seq_str) + C)
+    # start the E-step away from the generating model
+    sm.p_edman_failure *= 1.3
+    for cm in sm.channel_models:
+        cm.p_bleach *= 0.8
+    gpu_ctx.upload_model(sm, T)
+    gpu_ctx.fit_begin(seq, rads)
+    s, sl, nz = gpu_ctx.fit_estep()
+    g = s.as_dict(T, C)
+    o, lps = _oracle_sums(oracle, sm, T, seq, rads)
+    assert nz == int(np.sum(~np.isfinite(lps)))
+    assert abs(sl - float(np.sum(lps[np.isfinite(lps)]))) <= 1e-5 * len(rads)
+    _close(g["edman_num"], o["edman"][0], o["edman"][1], "edman num")
+    _close(g["edman_den"], o["edman"][1], o["edman"][1], "edman den")
+    _close(g["detach_x"], o["detach_x"], o["detach_n"], "detach x")
+    _close(g["detach_n"], o["detach_n"], o["detach_n"], "detach n")
+    _close(g["init_block_num"], o["init_block"][0], o["init_block"][1], "initial block num")
+    _close(g["init_block_den"], o["init_block"][1], o["init_block"][1], "initial block den")
+    _close(g["cyc_block_num"], o["cyc_block"][0], o["cyc_block"][1], "cyclic block num")
+    _close(g["cyc_block_den"], o["cyc_block"][1], o["cyc_block"][1], "cyclic block den")
+    for c in range(C):
+        _close(g["bleach_num"][c], o["bleach"][0][c], o["bleach"][1][c], f"bleach num {c}")
+        _close(g["bleach_den"][c], o["bleach"][1][c], o["bleach"][1][c], f"bleach den {c}")
+        _close(g["dud_num"][c], o["dud"][0][c], o["dud"][1][c], f"dud num {c}")
+        _close(g["dud_den"][c], o["dud"][1][c], o["dud"][1][c], f"dud den {c}")
+
+
+def test_estep_zero_probability_read(gpu_ctx, oracle):
+    """A read no state can emit (P == 0 in FP64) adds nothing and is counted."""
+    C, T = 2, 6
+    sm = _model(C)
+    seq = parse_dye_seq("0.1.01")
+    rads = _reads(sm, seq, T, 10, seed=9)
+    rads[3, 0, 0] = 1e4
+    gpu_ctx.upload_model(sm, T)
+    gpu_ctx.fit_begin(seq, rads)
+    s, sl, nz = gpu_ctx.fit_estep()
+    o, lps = _oracle_sums(oracle, sm, T, seq, rads)
+    assert not np.isfinite(lps[3])
+    assert nz == 1
+    _close(s.as_dict(T, C)["edman_den"], o["edman"][1], o["edman"][1], "edman den")
+
+
+def test_estep_errors(gpu_ctx):
+    C, T = 2, 6
+    sm = _model(C)
+    gpu_ctx.upload_model(sm, T)
+    with pytest.raises(capi.WpError):
+        gpu_ctx.fit_begin(np.array([0, 2], np.int16), np.zeros((1, T, C)))  # channel 2 of 2
+    with pytest.raises(capi.WpError):
+        gpu_ctx.fit_begin(np.zeros(16, np.int16), np.zeros((1, T, C)))  # 16 dyes on a channel
+    inter = _model(C)
+    inter.channel_models[0].interactions[1] = 0.9
+    gpu_ctx.fit_begin(parse_dye_seq("01"), np.zeros((2, T, C)))
+    gpu_ctx.upload_model(inter, T)
+    with pytest.raises(capi.WpError) as e:
+        gpu_ctx.fit_estep()
+    assert e.value.status == 5
+    gpu_ctx.upload_model(sm, T + 1)
+    with pytest.raises(capi.WpError) as e:
+        gpu_ctx.fit_estep()  # model timesteps differ from the staged reads
+    assert e.value.status == 6
+    gpu_ctx.upload_model(sm, T)
+    gpu_ctx.fit_begin(parse_dye_seq("01"), np.zeros((0, T, C)))
+    s, sl, nz = gpu_ctx.fit_estep()
+    assert s.p_edman_failure_den == 0.0 and sl == 0.0 and nz == 0
+
+
+def _params(m):
+    return np.array([m.p_edman_failure, m.p_detach, m.p_initial_detach, m.p_initial_detach_decay,
+                     m.p_initial_block, m.p_cyclic_block]
+                    + [c.p_bleach for c in m.channel_models] + [c.p_dud for c in m.channel_models])
+
+
+def _detach_curve(p, T):
+    t = np.arange(T - 1)
+    return p[1] + p[2] * np.exp(-p[3] * t)
+
+
+@pytest.mark.parametrize("name", ["fit_c2_t8.npz", "fit_c2_t6_block.npz"])
+def test_fit_vs_reference(name):
+    import os
+    from conftest import GOLDEN
+    z = np.load(os.path.join(GOLDEN, name))
+    C, T = int(z["C"]), int(z["T"])
+    st = z["start"]
+    sm = paper_model(C)
+    (sm.p_edman_failure, sm.p_detach, sm.p_initial_detach, sm.p_initial_detach_decay,
+     sm.p_initial_block, sm.p_cyclic_block) = st[:6]
+    for c in range(C):
+        sm.channel_models[c].p_bleach = st[6 + c]
+        sm.channel_models[c].p_dud = st[6 + C + c]
+    fitter = capi.HMMFitter(T, C, float(z["threshold"]), 1e9, sm, None, z["seq"])
+    fitted, log_l = fitter.fit(z["rads"])
+    got, ref = _params(fitted), z["ref_params"]
+    assert fitter.step_size < float(z["threshold"])
+    # everything but the detach triple directly; the detach rate as a curve
+    keep = [0, 4, 5] + list(range(6, 6 + 2 * C))
+    assert np.max(np.abs(got[keep] - ref[keep])) <= 1e-4, (got, ref)
+    assert np.max(np.abs(_detach_curve(got, T) - _detach_curve(ref, T))) <= 1e-4, (got, ref)
+    assert math.isfinite(log_l)
+    assert abs(log_l - float(z["ref_log_l"])) <= 1e-6 * abs(float(z["ref_log_l"])) + 1e-3
+    # log_likelihood of the mirror agrees with the fit's own final value
+    assert abs(fitter.log_likelihood(z["rads"], fitted) - log_l) <= 1e-9 * abs(log_l)

@@ -1,6 +1,7 @@
 """Build the CUDA library in-tree: whatprot_gb300/_lib/libwhatprot_gb300.so.
 
-Every translation unit under csrc/ is compiled for sm_103a only
+Every translation unit under csrc/ (.cu device code, .cc host code) is
+compiled by nvcc for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``), in parallel, then linked into
 one shared library exporting the C ABI of include/whatprot_gb300.h.
 """
@@ -42,14 +43,14 @@ def _stale(target, sources):
 
 def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
-    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cc")))
     headers = sorted(glob.glob(os.path.join(CSRC, "*.cuh"))) + [
         os.path.join(REPO, "include", "whatprot_gb300.h")]
     cc = nvcc()
     objs = []
     jobs = []
     for s in srcs:
-        o = os.path.join(OUT_DIR, os.path.basename(s)[:-3] + ".o")
+        o = os.path.join(OUT_DIR, os.path.splitext(os.path.basename(s))[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             extra = ["-Xptxas", "-v"] if ptxas_info else []

@@ -28,7 +28,8 @@ STATUS = {0: "WP_OK", 1: "WP_ERR_INVALID", 2: "WP_ERR_OOM", 3: "WP_ERR_CUDA",
 EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload",
            "wp_peptides_upload", "wp_hmm_classify", "wp_hmm_classify_device",
            "wp_hmm_loglik_all", "wp_hmm_count_flops", "wp_launch_count", "wp_ctx_stream",
-           "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak", "wp_last_batch_stats"]
+           "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak", "wp_last_batch_stats",
+           "wp_fit_begin", "wp_fit_estep", "wp_hmm_fit", "wp_fit_offset_exponential"]
 
 
 class WpSeqModel(ctypes.Structure):
@@ -46,6 +47,58 @@ class WpSeqModel(ctypes.Structure):
                 ("sig", ctypes.c_void_p),
                 ("interactions", ctypes.c_void_p),
                 ("flat_interactions", ctypes.c_void_p)]
+
+
+class WpFitSums(ctypes.Structure):
+    """wp_fit_sums: the SequencingModelFitter fields of one E-step."""
+    _fields_ = [("p_edman_failure_num", ctypes.c_double),
+                ("p_edman_failure_den", ctypes.c_double),
+                ("p_detach_x", ctypes.c_double * WP_MAX_TIMESTEPS),
+                ("p_detach_n", ctypes.c_double * WP_MAX_TIMESTEPS),
+                ("p_initial_block_num", ctypes.c_double),
+                ("p_initial_block_den", ctypes.c_double),
+                ("p_cyclic_block_num", ctypes.c_double),
+                ("p_cyclic_block_den", ctypes.c_double),
+                ("p_bleach_num", ctypes.c_double * WP_MAX_CHANNELS),
+                ("p_bleach_den", ctypes.c_double * WP_MAX_CHANNELS),
+                ("p_dud_num", ctypes.c_double * WP_MAX_CHANNELS),
+                ("p_dud_den", ctypes.c_double * WP_MAX_CHANNELS)]
+
+    def as_dict(self, T: int, C: int) -> dict:
+        """Same keys as the oracle's fit sums."""
+        return {
+            "edman_num": self.p_edman_failure_num, "edman_den": self.p_edman_failure_den,
+            "detach_x": np.array(self.p_detach_x[:max(T - 1, 0)]),
+            "detach_n": np.array(self.p_detach_n[:max(T - 1, 0)]),
+            "init_block_num": self.p_initial_block_num, "init_block_den": self.p_initial_block_den,
+            "cyc_block_num": self.p_cyclic_block_num, "cyc_block_den": self.p_cyclic_block_den,
+            "bleach_num": np.array(self.p_bleach_num[:C]), "bleach_den": np.array(self.p_bleach_den[:C]),
+            "dud_num": np.array(self.p_dud_num[:C]), "dud_den": np.array(self.p_dud_den[:C]),
+        }
+
+
+class WpFitSettings(ctypes.Structure):
+    """wp_fit_settings: FitSettings / ChannelFitSettings holds."""
+    _fields_ = [("hold_p_edman_failure", ctypes.c_int),
+                ("hold_p_detach", ctypes.c_int),
+                ("hold_p_initial_detach", ctypes.c_int),
+                ("hold_p_initial_detach_decay", ctypes.c_int),
+                ("hold_p_initial_block", ctypes.c_int),
+                ("hold_p_cyclic_block", ctypes.c_int),
+                ("hold_p_bleach", ctypes.c_int * WP_MAX_CHANNELS),
+                ("hold_p_dud", ctypes.c_int * WP_MAX_CHANNELS)]
+
+
+class WpFitParams(ctypes.Structure):
+    """wp_fit_params: the fitted parameters of a SequencingModel."""
+    _fields_ = [("p_edman_failure", ctypes.c_double),
+                ("p_detach", ctypes.c_double),
+                ("p_initial_detach", ctypes.c_double),
+                ("p_initial_detach_decay", ctypes.c_double),
+                ("p_initial_block", ctypes.c_double),
+                ("p_cyclic_block", ctypes.c_double),
+                ("p_bleach", ctypes.c_double * WP_MAX_CHANNELS),
+                ("p_dud", ctypes.c_double * WP_MAX_CHANNELS)]
 
 
 class WpError(RuntimeError):
@@ -97,6 +150,16 @@ def load_library(path: Optional[str] = None):
     lib.wp_probe_fp32_peak.restype = I
     lib.wp_last_batch_stats.argtypes = [V, V]
     lib.wp_last_batch_stats.restype = I
+    lib.wp_fit_begin.argtypes = [V, V, I, V, I]
+    lib.wp_fit_begin.restype = I
+    lib.wp_fit_estep.argtypes = [V, ctypes.POINTER(WpFitSums), ctypes.POINTER(D), ctypes.POINTER(I)]
+    lib.wp_fit_estep.restype = I
+    lib.wp_hmm_fit.argtypes = [V, ctypes.POINTER(WpSeqModel), I, V, I, V, I,
+                               ctypes.POINTER(WpFitSettings), D, D, ctypes.POINTER(WpFitParams),
+                               ctypes.POINTER(D), ctypes.POINTER(D), ctypes.POINTER(I)]
+    lib.wp_hmm_fit.restype = I
+    lib.wp_fit_offset_exponential.argtypes = [V, V, I, V, V]
+    lib.wp_fit_offset_exponential.restype = I
     if path is None:
         _lib = lib
     return lib
@@ -104,6 +167,35 @@ def load_library(path: Optional[str] = None):
 
 def _ptr(a: Optional[np.ndarray]):
     return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def seq_model_struct(sm: SequencingModel):
+    """A WpSeqModel view of sm, with the arrays it points to (keep them alive)."""
+    C = sm.num_channels
+    arr = lambda xs: np.ascontiguousarray(np.asarray(xs, dtype=np.float64))
+    cms = sm.channel_models
+    keep = [arr([c.p_bleach for c in cms]), arr([c.p_dud for c in cms]),
+            arr([c.bg_sig for c in cms]), arr([c.mu for c in cms]), arr([c.sig for c in cms]),
+            arr([[c.interactions[o] for o in range(C)] for c in cms]).reshape(-1),
+            arr([[c.flat_interactions[o] for o in range(C)] for c in cms]).reshape(-1)]
+    m = WpSeqModel(C, sm.p_edman_failure, sm.p_detach, sm.p_initial_detach,
+                   sm.p_initial_detach_decay, sm.p_initial_block, sm.p_cyclic_block,
+                   *[k.ctypes.data for k in keep])
+    return m, keep
+
+
+def fit_offset_exponential(y, w, params, held=(False, False, False)):
+    """wp_fit_offset_exponential: the detach M-step's bounded least squares
+    (host code of the library; needs no GPU)."""
+    lib = load_library()
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    p = np.ascontiguousarray(params, dtype=np.float64).copy()
+    h = np.ascontiguousarray([1 if x else 0 for x in held], dtype=np.int32)
+    st = lib.wp_fit_offset_exponential(_ptr(y), _ptr(w), len(y), _ptr(h), _ptr(p))
+    if st != 0:
+        raise WpError(st, "wp_fit_offset_exponential")
+    return p
 
 
 class Context:
@@ -137,15 +229,7 @@ class Context:
 
     def upload_model(self, sm: SequencingModel, num_timesteps: int) -> None:
         C = sm.num_channels
-        arr = lambda xs: np.ascontiguousarray(np.asarray(xs, dtype=np.float64))
-        cms = sm.channel_models
-        keep = [arr([c.p_bleach for c in cms]), arr([c.p_dud for c in cms]),
-                arr([c.bg_sig for c in cms]), arr([c.mu for c in cms]), arr([c.sig for c in cms]),
-                arr([[c.interactions[o] for o in range(C)] for c in cms]).reshape(-1),
-                arr([[c.flat_interactions[o] for o in range(C)] for c in cms]).reshape(-1)]
-        m = WpSeqModel(C, sm.p_edman_failure, sm.p_detach, sm.p_initial_detach,
-                       sm.p_initial_detach_decay, sm.p_initial_block, sm.p_cyclic_block,
-                       *[k.ctypes.data for k in keep])
+        m, keep = seq_model_struct(sm)
         self._check(self.lib.wp_model_upload(self.h, ctypes.byref(m), num_timesteps))
         self.num_timesteps = num_timesteps
         self.num_channels = C
@@ -194,6 +278,57 @@ class Context:
         self._check(self.lib.wp_hmm_count_flops(self.h, _ptr(rads), rads.shape[0], dist_cutoff,
                                                 ctypes.byref(out)))
         return out.value
+
+    def fit_begin(self, dye_seq, rads: np.ndarray) -> None:
+        """wp_fit_begin: stage one dye-seq (int list, -1 unlabeled) and its
+        reads [R, T, C] (divided by mu) for E-steps."""
+        seq = np.ascontiguousarray(dye_seq, dtype=np.int16)
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        self._check(self.lib.wp_fit_begin(self.h, _ptr(seq) if len(seq) else None, len(seq),
+                                          _ptr(rads), rads.shape[0]))
+
+    def fit_estep(self):
+        """wp_fit_estep with the current model: (WpFitSums, sum log P, reads with P == 0)."""
+        s = WpFitSums()
+        sl = ctypes.c_double(0.0)
+        nz = ctypes.c_int(0)
+        self._check(self.lib.wp_fit_estep(self.h, ctypes.byref(s), ctypes.byref(sl), ctypes.byref(nz)))
+        return s, sl.value, nz.value
+
+    def hmm_fit(self, start: SequencingModel, num_timesteps: int, dye_seq, rads: np.ndarray,
+                stopping_threshold: float, max_runtime: float = 1e300, holds: Optional[dict] = None):
+        """wp_hmm_fit: (fitted SequencingModel, step size, log-likelihood, iterations)."""
+        import copy
+        m, keep = seq_model_struct(start)
+        seq = np.ascontiguousarray(dye_seq, dtype=np.int16)
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        fs = WpFitSettings()
+        for k, v in (holds or {}).items():
+            if k in ("hold_p_bleach", "hold_p_dud"):
+                arr = getattr(fs, k)
+                for c, h in enumerate(v):
+                    arr[c] = 1 if h else 0
+            else:
+                setattr(fs, k, 1 if v else 0)
+        out = WpFitParams()
+        step = ctypes.c_double(0.0)
+        ll = ctypes.c_double(0.0)
+        it = ctypes.c_int(0)
+        self._check(self.lib.wp_hmm_fit(self.h, ctypes.byref(m), num_timesteps,
+                                        _ptr(seq) if len(seq) else None, len(seq), _ptr(rads),
+                                        rads.shape[0], ctypes.byref(fs), stopping_threshold,
+                                        max_runtime, ctypes.byref(out), ctypes.byref(step),
+                                        ctypes.byref(ll), ctypes.byref(it)))
+        fitted = copy.deepcopy(start)
+        for k in ("p_edman_failure", "p_detach", "p_initial_detach", "p_initial_detach_decay",
+                  "p_initial_block", "p_cyclic_block"):
+            setattr(fitted, k, getattr(out, k))
+        for c, cm in enumerate(fitted.channel_models):
+            cm.p_bleach = out.p_bleach[c]
+            cm.p_dud = out.p_dud[c]
+        self.num_timesteps = num_timesteps
+        self.num_channels = start.num_channels
+        return fitted, step.value, ll.value, it.value
 
     def launch_count(self) -> int:
         return int(self.lib.wp_launch_count(self.h))
@@ -277,3 +412,44 @@ class HMMClassifier:
         ids, sc, tot, _ = self.ctx.classify(rads, self.dist_cutoff, cand, cand_off)
         res = [ScoredClassification(int(i), float(s), float(t)) for i, s, t in zip(ids, sc, tot)]
         return res[0] if single else res
+
+
+class HMMFitter:
+    """Host mirror of HMMFitter (fitters/hmm-fitter.h:35-150): Baum-Welch on
+    one dye-seq with GPU E-steps.  ``fit_settings`` maps the FitSettings hold
+    names (``hold_p_edman_failure`` ... ``hold_p_cyclic_block``,
+    ``hold_p_bleach`` / ``hold_p_dud`` as per-channel lists) to booleans."""
+
+    def __init__(self, num_timesteps: int, num_channels: int, stopping_threshold: float,
+                 max_runtime: float, seq_model: SequencingModel, fit_settings: Optional[dict],
+                 dye_seq, device: int = 0):
+        from .model import parse_dye_seq
+        self.num_timesteps = num_timesteps
+        self.num_channels = num_channels
+        self.stopping_threshold = stopping_threshold
+        self.max_runtime = max_runtime
+        self.seq_model = seq_model
+        self.fit_settings = dict(fit_settings or {})
+        self.dye_seq = (parse_dye_seq(dye_seq) if isinstance(dye_seq, str)
+                        else np.asarray(dye_seq, dtype=np.int16))
+        self.ctx = Context(device)
+        self.step_size = None
+        self.iterations = None
+
+    def fit(self, radiometries: np.ndarray):
+        """(fitted SequencingModel, log-likelihood); step size and iteration
+        count are kept in .step_size and .iterations."""
+        fitted, step, ll, it = self.ctx.hmm_fit(self.seq_model, self.num_timesteps, self.dye_seq,
+                                                radiometries, self.stopping_threshold,
+                                                self.max_runtime, self.fit_settings)
+        self.step_size = step
+        self.iterations = it
+        return fitted, ll
+
+    def log_likelihood(self, radiometries: np.ndarray, seq_model: SequencingModel) -> float:
+        """Sum of log P over the reads (fitters/hmm-fitter.h:119-142); -inf
+        when some read has P == 0."""
+        self.ctx.upload_model(seq_model, self.num_timesteps)
+        self.ctx.fit_begin(self.dye_seq, radiometries)
+        _, sl, nz = self.ctx.fit_estep()
+        return float("-inf") if nz else sl

@@ -45,6 +45,10 @@ cudaError_t wp_launch_dense(bool has_block, int threads, size_t smem, cudaStream
                             const BatchArgs& a);
 size_t wp_dense_smem_bytes(int T, int S_cap, int C, bool has_block, int warps);
 cudaError_t wp_launch_fma_probe(int blocks, int threads, int iters, cudaStream_t stream, float* sink);
+cudaError_t wp_launch_fit_estep(bool has_block, int grid, int threads, cudaStream_t s, const FitArgs& a);
+__global__ void wp_fit_reduce_kernel(const double*, long, int, double*);
+int wp_fit_nslots(int T, int C);
+long wp_fit_floats_per_thread(int T, int C, int S, bool has_block);
 
 namespace {
 
@@ -111,6 +115,14 @@ struct wp_ctx {
     long long t_n[4] = {0, 0, 0, 0};
     int last_engine_grid = 0;
     long long last_slots = 0;
+
+    // Staged Baum-Welch fit.
+    bool have_fit = false;
+    int fit_R = 0, fit_T = 0, fit_C = 0;
+    int fit_D[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+    int fit_dmax = 0;
+    std::vector<int16_t> fit_seq;
+    DevBuf d_fit_rads, d_fit_lo, d_fit_hi, d_fit_tab, d_fit_scratch, d_fit_sums, d_fit_out, d_fit_logp;
 
     // Per-batch scratch.
     DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_Lpk, d_Upk, d_allow, d_flags, d_table, d_res_mant, d_res_expo,
@@ -685,6 +697,157 @@ wp_status wp_hmm_loglik_all(wp_ctx* ctx, const double* rads, int R, double dist_
     if (st != WP_OK) return st;
     WP_CUDA(cudaMemcpyAsync(out_logp, ctx->d_logp.p, lbytes, cudaMemcpyDeviceToHost, ctx->stream), "copy logp");
     return finish(ctx);
+}
+
+}  // extern "C"
+
+// Error setter for host code in other translation units (wp_fitter.cc).
+wp_status wp_internal_fail(wp_ctx* ctx, wp_status code, const char* msg) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return fail(ctx, code, msg);
+}
+
+extern "C" {
+
+wp_status wp_fit_begin(wp_ctx* ctx, const int16_t* dye_seq, int length, const double* rads, int R) {
+    if (!ctx || length < 0 || R < 0 || (length > 0 && !dye_seq) || (R > 0 && !rads)) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if (!ctx->have_model) return fail(ctx, WP_ERR_STATE, "model not uploaded");
+    const int C = ctx->hm.C, T = ctx->hm.T;
+    int cnt[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+    for (int k = 0; k < length; k++) {
+        if (dye_seq[k] < -1 || dye_seq[k] >= C) return fail(ctx, WP_ERR_INVALID, "dye-seq channel out of range");
+        if (dye_seq[k] >= 0) cnt[dye_seq[k]]++;
+    }
+    ctx->fit_dmax = 0;
+    for (int c = 0; c < C; c++) {
+        if (cnt[c] > WP_MAX_DYES_PER_CHANNEL) return fail(ctx, WP_ERR_UNSUPPORTED, "more than 15 dyes on a channel");
+        ctx->fit_D[c] = cnt[c];
+        ctx->fit_dmax = std::max(ctx->fit_dmax, cnt[c]);
+    }
+    ctx->fit_seq.assign(dye_seq, dye_seq + length);
+    ctx->fit_R = R;
+    ctx->fit_T = T;
+    ctx->fit_C = C;
+    const size_t bytes = sizeof(double) * (size_t)R * T * C;
+    WP_CUDA(ctx->d_fit_rads.ensure(std::max<size_t>(bytes, 8)), "alloc fit reads");
+    if (R > 0) WP_CUDA(cudaMemcpyAsync(ctx->d_fit_rads.p, rads, bytes, cudaMemcpyHostToDevice, ctx->stream), "copy fit reads");
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    ctx->have_fit = true;
+    return WP_OK;
+}
+
+wp_status wp_fit_estep(wp_ctx* ctx, wp_fit_sums* out, double* sum_logp, int* num_zero) {
+    if (!ctx || !out) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if (!ctx->have_model) return fail(ctx, WP_ERR_STATE, "model not uploaded");
+    if (!ctx->have_fit) return fail(ctx, WP_ERR_STATE, "fit not staged (wp_fit_begin)");
+    if (ctx->hm.interacting) return fail(ctx, WP_ERR_UNSUPPORTED, "the GPU fit does not support channel interactions");
+    const int C = ctx->hm.C, T = ctx->hm.T, R = ctx->fit_R;
+    if (C != ctx->fit_C || T != ctx->fit_T)
+        return fail(ctx, WP_ERR_STATE, "model channels/timesteps differ from the staged reads");
+    const bool hb = ctx->hm.has_block != 0;
+    memset(out, 0, sizeof(*out));
+    if (sum_logp) *sum_logp = 0.0;
+    if (num_zero) *num_zero = 0;
+    if (R == 0) return WP_OK;
+    // Emission factors of every read, unpruned (run-fit.cc:59), with the
+    // HMMFitter's max_num_dyes (fitters/hmm-fitter.cc:30-52).
+    const int W = ctx->fit_dmax + 1;
+    const int entries = T * C * W;
+    WP_CUDA(ctx->d_fit_lo.ensure((size_t)R * T * C), "alloc");
+    WP_CUDA(ctx->d_fit_hi.ensure((size_t)R * T * C), "alloc");
+    WP_CUDA(ctx->d_fit_tab.ensure(sizeof(EmitEntry) * (size_t)R * entries), "alloc fit table");
+    {
+        long n = (long)R * T;
+        TimedLaunch tl(ctx, 1);
+        wp_prep_reads_kernel<<<(int)((n + 127) / 128), 128, 0, ctx->stream>>>(
+                ctx->d_model.as<DevModel>(), ctx->d_fit_rads.as<double>(), R, (unsigned)ctx->fit_dmax, DBL_MAX,
+                ctx->d_fit_lo.as<uint8_t>(), ctx->d_fit_hi.as<uint8_t>(), ctx->d_fit_tab.as<EmitEntry>(), entries);
+        ctx->launches++;
+        WP_CUDA(cudaGetLastError(), "fit prep launch");
+    }
+    int S = 1;
+    for (int c = 0; c < C; c++) S *= ctx->fit_D[c] + 1;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int threads = 128;
+    long want = std::min<long>((long)R, (long)sms * 4 * threads);
+    const long per = wp_fit_floats_per_thread(T, C, S, hb);
+    // keep the scratch under 16 GiB
+    while (want > threads && (double)want * per * 4.0 > 16.0 * (1u << 30)) want /= 2;
+    const int grid = (int)((want + threads - 1) / threads);
+    const long nth = (long)grid * threads;
+    const int nslots = wp_fit_nslots(T, C);
+    WP_CUDA(ctx->d_fit_scratch.ensure(sizeof(float) * (size_t)nth * per), "alloc fit scratch");
+    WP_CUDA(ctx->d_fit_sums.ensure(sizeof(double) * (size_t)nth * nslots), "alloc fit sums");
+    WP_CUDA(ctx->d_fit_out.ensure(sizeof(double) * nslots), "alloc fit sums");
+    WP_CUDA(ctx->d_fit_logp.ensure(sizeof(double) * R), "alloc fit logp");
+    FitArgs fa;
+    memset(&fa, 0, sizeof(fa));
+    fa.model = ctx->d_model.as<DevModel>();
+    fa.rads = ctx->d_fit_rads.as<double>();
+    fa.R = R;
+    for (int c = 0; c < C; c++) fa.D[c] = ctx->fit_D[c];
+    {
+        int rem[WP_MAX_CHANNELS];
+        for (int c = 0; c < WP_MAX_CHANNELS; c++) rem[c] = ctx->fit_D[c];
+        const int len = (int)ctx->fit_seq.size();
+        for (int e = 0; e < WP_MAX_TIMESTEPS; e++) {
+            int d = e < len ? ctx->fit_seq[e] : -1;
+            fa.dye[e] = (int8_t)d;
+            fa.tot[e] = (uint8_t)(d >= 0 ? rem[d] : 0);  // DyeTrack(e, d)
+            if (d >= 0) rem[d]--;
+        }
+    }
+    fa.tab = ctx->d_fit_tab.as<EmitEntry>();
+    fa.W = W;
+    fa.scratch = ctx->d_fit_scratch.as<float>();
+    fa.vec_floats = per;
+    fa.sums = ctx->d_fit_sums.as<double>();
+    fa.logp = ctx->d_fit_logp.as<double>();
+    fa.nslots = nslots;
+    {
+        TimedLaunch tl(ctx, 0);
+        WP_CUDA(wp_launch_fit_estep(hb, grid, threads, ctx->stream, fa), "fit E-step launch");
+        ctx->launches++;
+    }
+    wp_fit_reduce_kernel<<<(nslots + 63) / 64, 64, 0, ctx->stream>>>(fa.sums, nth, nslots, ctx->d_fit_out.as<double>());
+    ctx->launches++;
+    WP_CUDA(cudaGetLastError(), "fit reduce launch");
+    std::vector<double> sums(nslots), lp(R);
+    WP_CUDA(cudaMemcpyAsync(sums.data(), ctx->d_fit_out.p, sizeof(double) * nslots, cudaMemcpyDeviceToHost, ctx->stream), "copy sums");
+    WP_CUDA(cudaMemcpyAsync(lp.data(), ctx->d_fit_logp.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy logp");
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    // Slot layout of wp_fit.cu.
+    out->p_edman_failure_num = sums[0];
+    out->p_edman_failure_den = sums[1];
+    out->p_initial_block_num = sums[2];
+    out->p_initial_block_den = sums[3];
+    out->p_cyclic_block_num = sums[4];
+    out->p_cyclic_block_den = sums[5];
+    for (int t = 0; t + 1 < T; t++) {
+        out->p_detach_x[t] = sums[6 + 2 * t];
+        out->p_detach_n[t] = sums[7 + 2 * t];
+    }
+    for (int c = 0; c < C; c++) {
+        const int b = 6 + 2 * (T - 1) + 4 * c;
+        out->p_bleach_num[c] = sums[b];
+        out->p_bleach_den[c] = sums[b + 1];
+        out->p_dud_num[c] = sums[b + 2];
+        out->p_dud_den[c] = sums[b + 3];
+    }
+    double sl = 0.0;
+    int nz = 0;
+    for (int r = 0; r < R; r++) {
+        if (std::isfinite(lp[r])) sl += lp[r];
+        else nz++;
+    }
+    if (sum_logp) *sum_logp = sl;
+    if (num_zero) *num_zero = nz;
+    return WP_OK;
 }
 
 wp_status wp_hmm_count_flops(wp_ctx* ctx, const double* rads, int R, double dist_cutoff, double* out_flops) {

@@ -135,3 +135,20 @@ __device__ __forceinline__ void load_smem_model(SmemModel& S, const DevModel& m)
     }
     for (int t = threadIdx.x; t < m.T; t += blockDim.x) S.p_det[t] = m.p_det[t];
 }
+
+// Arguments of one Baum-Welch E-step (wp_fit.cu).
+struct FitArgs {
+    const DevModel* model;
+    const double* rads;     // [R][T][C]
+    int R;
+    int D[WP_MAX_CHANNELS];  // dyes per channel of the dye-seq
+    int8_t dye[WP_MAX_TIMESTEPS];
+    uint8_t tot[WP_MAX_TIMESTEPS];
+    const EmitEntry* tab;  // [R][T][C][W] emission factors (non-interacting)
+    int W;
+    float* scratch;        // per-thread state vectors, interleaved
+    long vec_floats;       // floats of one full vector (A and B of T*S states)
+    double* sums;          // [nthreads][nslots]
+    double* logp;          // [R] log P per read (nullable)
+    int nslots;
+};

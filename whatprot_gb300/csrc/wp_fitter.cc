@@ -1,0 +1,349 @@
+// wp_fitter.cc -- the host side of the Baum-Welch fit: HMMFitter::fit
+// (fitters/hmm-fitter.h:49-117) as a client of the C ABI.  Each iteration
+// uploads the current model, runs one GPU E-step over the staged reads
+// (wp_fit_estep), applies the dud hidden-count correction and the M-step on
+// the host, and stops on the largest parameter change or on wall time.
+//
+// The detach M-step fits base + initial * exp(-decay * t) by weighted least
+// squares with every parameter in [0, 1] (util/levmar-helper.cc:44-85).  The
+// reference calls levmar's box-constrained dlevmar_bc_der (levmar 2.6,
+// vendored by the reference); this file has its own projected
+// Levenberg-Marquardt (Levenberg 1944, Marquardt 1963; damping update of
+// Nielsen 1999) with the same bounds, the same 10-iteration cap and holds as
+// fixed parameters, so fitted detach rates agree with the reference to the
+// accuracy of the fit, not bit for bit.
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <vector>
+
+#include "whatprot_gb300.h"
+
+wp_status wp_internal_fail(wp_ctx* ctx, wp_status code, const char* msg);
+
+namespace {
+
+// Model of offset_exponential (util/levmar-helper.cc:23-42), weighted.
+void oe_residual(const double* p, const double* y, const double* sw, int n, double* r) {
+    for (int i = 0; i < n; i++) r[i] = sw[i] * (y[i] - (p[0] + p[1] * exp(-p[2] * i)));
+}
+
+void oe_normal(const double* p, const double* sw, const double* r, int n, double A[3][3], double g[3]) {
+    for (int a = 0; a < 3; a++) {
+        g[a] = 0.0;
+        for (int b = 0; b < 3; b++) A[a][b] = 0.0;
+    }
+    for (int i = 0; i < n; i++) {
+        const double e = exp(-p[2] * i);
+        const double J[3] = {sw[i], sw[i] * e, -sw[i] * p[1] * i * e};
+        for (int a = 0; a < 3; a++) {
+            g[a] += J[a] * r[i];
+            for (int b = 0; b < 3; b++) A[a][b] += J[a] * J[b];
+        }
+    }
+}
+
+double sumsq(const double* r, int n) {
+    double s = 0.0;
+    for (int i = 0; i < n; i++) s += r[i] * r[i];
+    return s;
+}
+
+// Solve M h = g on the free coordinates by Cholesky (M symmetric positive
+// definite there); fixed coordinates get h = 0.  False if M is not SPD.
+bool solve_free(const double M[3][3], const double g[3], const bool* fixed, double h[3]) {
+    int idx[3], m = 0;
+    for (int k = 0; k < 3; k++) {
+        h[k] = 0.0;
+        if (!fixed[k]) idx[m++] = k;
+    }
+    double L[3][3] = {{0}};
+    for (int i = 0; i < m; i++) {
+        for (int j = 0; j <= i; j++) {
+            double s = M[idx[i]][idx[j]];
+            for (int k = 0; k < j; k++) s -= L[i][k] * L[j][k];
+            if (i == j) {
+                if (!(s > 0.0)) return false;
+                L[i][i] = sqrt(s);
+            } else {
+                L[i][j] = s / L[j][j];
+            }
+        }
+    }
+    double z[3];
+    for (int i = 0; i < m; i++) {
+        double s = g[idx[i]];
+        for (int k = 0; k < i; k++) s -= L[i][k] * z[k];
+        z[i] = s / L[i][i];
+    }
+    for (int i = m - 1; i >= 0; i--) {
+        double s = z[i];
+        for (int k = i + 1; k < m; k++) s -= L[k][i] * h[idx[k]];
+        h[idx[i]] = s / L[i][i];
+    }
+    return true;
+}
+
+struct HostModel {
+    int C = 0;
+    double p_edman_failure = 0, p_detach = 0, p_initial_detach = 0, p_initial_detach_decay = 0;
+    double p_initial_block = 0, p_cyclic_block = 0;
+    double p_bleach[WP_MAX_CHANNELS] = {0}, p_dud[WP_MAX_CHANNELS] = {0};
+    double bg_sig[WP_MAX_CHANNELS] = {0}, mu[WP_MAX_CHANNELS] = {0}, sig[WP_MAX_CHANNELS] = {0};
+    std::vector<double> inter, flat;
+
+    wp_seq_model view() const {
+        wp_seq_model m;
+        m.num_channels = C;
+        m.p_edman_failure = p_edman_failure;
+        m.p_detach = p_detach;
+        m.p_initial_detach = p_initial_detach;
+        m.p_initial_detach_decay = p_initial_detach_decay;
+        m.p_initial_block = p_initial_block;
+        m.p_cyclic_block = p_cyclic_block;
+        m.p_bleach = p_bleach;
+        m.p_dud = p_dud;
+        m.bg_sig = bg_sig;
+        m.mu = mu;
+        m.sig = sig;
+        m.interactions = inter.empty() ? nullptr : inter.data();
+        m.flat_interactions = flat.empty() ? nullptr : flat.data();
+        return m;
+    }
+};
+
+// SequencingModel::distance (parameterization/model/sequencing-model.cc:153-166).
+double distance(const HostModel& a, const HostModel& b) {
+    double d = 0.0;
+    d = std::max(d, fabs(a.p_edman_failure - b.p_edman_failure));
+    d = std::max(d, fabs(a.p_detach - b.p_detach));
+    d = std::max(d, fabs(a.p_initial_detach - b.p_initial_detach));
+    d = std::max(d, fabs(a.p_initial_detach_decay - b.p_initial_detach_decay));
+    d = std::max(d, fabs(a.p_initial_block - b.p_initial_block));
+    d = std::max(d, fabs(a.p_cyclic_block - b.p_cyclic_block));
+    for (int c = 0; c < a.C; c++) {
+        d = std::max(d, fabs(a.p_bleach[c] - b.p_bleach[c]));
+        d = std::max(d, fabs(a.p_dud[c] - b.p_dud[c]));
+    }
+    return d;
+}
+
+}  // namespace
+
+extern "C" {
+
+wp_status wp_fit_offset_exponential(const double* y, const double* w, int n, const int* held, double* params) {
+    if (n < 0 || !params || (n > 0 && (!y || !w))) return WP_ERR_INVALID;
+    if (n == 0) return WP_OK;
+    double lb[3], ub[3];
+    bool fixed[3];
+    for (int k = 0; k < 3; k++) {
+        fixed[k] = held && held[k];
+        lb[k] = fixed[k] ? params[k] : 0.0;
+        ub[k] = fixed[k] ? params[k] : 1.0;
+    }
+    // Weighted problem: residual sqrt(w) * (y - model), as the reference
+    // scales both sides by sqrt(w).  Points with a non-finite target or
+    // weight carry no information and get weight 0.
+    std::vector<double> sw(n), yy(n), r(n), rn(n);
+    for (int i = 0; i < n; i++) {
+        const bool ok = isfinite(y[i]) && isfinite(w[i]) && w[i] > 0.0;
+        sw[i] = ok ? sqrt(w[i]) : 0.0;
+        yy[i] = ok ? y[i] : 0.0;
+    }
+    double p[3];
+    for (int k = 0; k < 3; k++) p[k] = std::min(std::max(params[k], lb[k]), ub[k]);
+    oe_residual(p, yy.data(), sw.data(), n, r.data());
+    double cost = sumsq(r.data(), n);
+    double A[3][3], g[3];
+    oe_normal(p, sw.data(), r.data(), n, A, g);
+    double amax = 0.0;
+    for (int k = 0; k < 3; k++)
+        if (!fixed[k]) amax = std::max(amax, A[k][k]);
+    double mu = 1e-3 * amax;
+    double nu = 2.0;
+    for (int it = 0; it < 10; it++) {  // itmax of levmar-helper.cc:79
+        // Active set: held parameters and those on a bound that the
+        // gradient pushes outward stay put this iteration.
+        bool act[3];
+        double gmax = 0.0;
+        for (int k = 0; k < 3; k++) {
+            act[k] = fixed[k] || (p[k] <= lb[k] && g[k] <= 0.0) || (p[k] >= ub[k] && g[k] >= 0.0);
+            if (!act[k]) gmax = std::max(gmax, fabs(g[k]));
+        }
+        if (gmax <= 1e-17) break;
+        double M[3][3];
+        memcpy(M, A, sizeof(M));
+        for (int k = 0; k < 3; k++) M[k][k] += mu;
+        double h[3];
+        if (!solve_free(M, g, act, h)) {
+            mu = mu > 0.0 ? mu * nu : 1e-3;
+            nu *= 2.0;
+            continue;
+        }
+        double pn[3], d[3], pnorm = 0.0, dnorm = 0.0;
+        for (int k = 0; k < 3; k++) {
+            pn[k] = std::min(std::max(p[k] + h[k], lb[k]), ub[k]);
+            d[k] = pn[k] - p[k];
+            pnorm += p[k] * p[k];
+            dnorm += d[k] * d[k];
+        }
+        if (dnorm <= 1e-34 * pnorm) break;
+        oe_residual(pn, yy.data(), sw.data(), n, rn.data());
+        const double costn = sumsq(rn.data(), n);
+        // Reduction predicted by the linearised model along the projected
+        // step: |r|^2 - |r - J d|^2 = 2 d.g - d.A.d.
+        double pred = 0.0;
+        for (int a = 0; a < 3; a++) {
+            pred += 2.0 * d[a] * g[a];
+            for (int b = 0; b < 3; b++) pred -= d[a] * A[a][b] * d[b];
+        }
+        const double rho = pred > 0.0 ? (cost - costn) / pred : -1.0;
+        if (rho > 0.0 && isfinite(costn)) {
+            memcpy(p, pn, sizeof(p));
+            r.swap(rn);
+            cost = costn;
+            oe_normal(p, sw.data(), r.data(), n, A, g);
+            const double q = 2.0 * rho - 1.0;
+            mu *= std::max(1.0 / 3.0, 1.0 - q * q * q);
+            nu = 2.0;
+        } else {
+            mu *= nu;
+            nu *= 2.0;
+        }
+    }
+    for (int k = 0; k < 3; k++) params[k] = p[k];
+    return WP_OK;
+}
+
+wp_status wp_hmm_fit(wp_ctx* ctx, const wp_seq_model* start, int T, const int16_t* dye_seq, int length,
+                     const double* rads, int R, const wp_fit_settings* settings, double stopping_threshold,
+                     double max_runtime, wp_fit_params* out, double* step_size, double* log_l, int* iterations) {
+    if (!ctx || !start || !out) return WP_ERR_INVALID;
+    const int C = start->num_channels;
+    if (C < 1 || C > WP_MAX_CHANNELS) return wp_internal_fail(ctx, WP_ERR_UNSUPPORTED, "num_channels out of range 1..4");
+    if (!start->p_bleach || !start->p_dud || !start->bg_sig || !start->mu || !start->sig)
+        return wp_internal_fail(ctx, WP_ERR_INVALID, "null per-channel array");
+    wp_fit_settings fs;
+    memset(&fs, 0, sizeof(fs));
+    if (settings) fs = *settings;
+
+    HostModel sm;
+    sm.C = C;
+    sm.p_edman_failure = start->p_edman_failure;
+    sm.p_detach = start->p_detach;
+    sm.p_initial_detach = start->p_initial_detach;
+    sm.p_initial_detach_decay = start->p_initial_detach_decay;
+    sm.p_initial_block = start->p_initial_block;
+    sm.p_cyclic_block = start->p_cyclic_block;
+    for (int c = 0; c < C; c++) {
+        sm.p_bleach[c] = start->p_bleach[c];
+        sm.p_dud[c] = start->p_dud[c];
+        sm.bg_sig[c] = start->bg_sig[c];
+        sm.mu[c] = start->mu[c];
+        sm.sig[c] = start->sig[c];
+    }
+    if (start->interactions) sm.inter.assign(start->interactions, start->interactions + C * C);
+    if (start->flat_interactions) sm.flat.assign(start->flat_interactions, start->flat_interactions + C * C);
+
+    wp_seq_model view = sm.view();
+    wp_status st = wp_model_upload(ctx, &view, T);
+    if (st != WP_OK) return st;
+    st = wp_fit_begin(ctx, dye_seq, length, rads, R);
+    if (st != WP_OK) return st;
+
+    // ratio_hidden = product of p_dud over the dye-seq's dyes
+    // (fitters/hmm-fitter.h:80-89).
+    auto hidden_ratio = [&](const HostModel& m) {
+        double ratio = 1.0;
+        for (int i = 0; i < length; i++)
+            if (dye_seq[i] != -1) ratio *= m.p_dud[dye_seq[i]];
+        return ratio;
+    };
+
+    const auto t0 = std::chrono::steady_clock::now();
+    HostModel x;
+    double step = 0.0;
+    int iters = 0;
+    while (true) {
+        if (iters > 0) {
+            view = sm.view();
+            st = wp_model_upload(ctx, &view, T);
+            if (st != WP_OK) return st;
+        }
+        wp_fit_sums s;
+        st = wp_fit_estep(ctx, &s, nullptr, nullptr);
+        if (st != WP_OK) return st;
+        iters++;
+        // Dud hidden-count correction (fitters/hmm-fitter.h:80-101).
+        const double magic = 1.0 / (1.0 - hidden_ratio(sm)) - 1.0;
+        const double hidden = magic * (double)R;
+        for (int i = 0; i < length; i++)
+            if (dye_seq[i] != -1) {
+                s.p_dud_num[dye_seq[i]] += hidden;
+                s.p_dud_den[dye_seq[i]] += hidden;
+            }
+        // M-step: SequencingModelFitter::get (sequencing-model-fitter.cc:
+        // 68-78) then update_with_holds (hmm-fitter.cc:63-97).
+        HostModel next = sm;
+        if (!fs.hold_p_edman_failure) next.p_edman_failure = s.p_edman_failure_num / s.p_edman_failure_den;
+        if (!fs.hold_p_initial_block) next.p_initial_block = s.p_initial_block_num / s.p_initial_block_den;
+        if (!fs.hold_p_cyclic_block) next.p_cyclic_block = s.p_cyclic_block_num / s.p_cyclic_block_den;
+        {
+            const int n = T - 1;
+            std::vector<double> y(std::max(n, 1)), w(std::max(n, 1));
+            for (int k = 0; k < n; k++) {
+                y[k] = s.p_detach_x[k] / s.p_detach_n[k];
+                w[k] = s.p_detach_n[k];
+            }
+            double p[3] = {sm.p_detach, sm.p_initial_detach, sm.p_initial_detach_decay};
+            const int held[3] = {fs.hold_p_detach, fs.hold_p_initial_detach, fs.hold_p_initial_detach_decay};
+            st = wp_fit_offset_exponential(y.data(), w.data(), n, held, p);
+            if (st != WP_OK) return st;
+            if (!fs.hold_p_detach) next.p_detach = p[0];
+            if (!fs.hold_p_initial_detach) next.p_initial_detach = p[1];
+            if (!fs.hold_p_initial_detach_decay) next.p_initial_detach_decay = p[2];
+        }
+        for (int c = 0; c < C; c++) {
+            if (!fs.hold_p_bleach[c]) next.p_bleach[c] = s.p_bleach_num[c] / s.p_bleach_den[c];
+            if (!fs.hold_p_dud[c]) next.p_dud[c] = s.p_dud_num[c] / s.p_dud_den[c];
+        }
+        step = distance(sm, next);
+        const double elapsed =
+                std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (step < stopping_threshold || elapsed > max_runtime) {
+            x = next;
+            break;
+        }
+        sm = next;
+    }
+    // log_likelihood(radiometries, x) (fitters/hmm-fitter.h:119-142).
+    view = x.view();
+    st = wp_model_upload(ctx, &view, T);
+    if (st != WP_OK) return st;
+    wp_fit_sums s;
+    double sl = 0.0;
+    int nz = 0;
+    st = wp_fit_estep(ctx, &s, &sl, &nz);
+    if (st != WP_OK) return st;
+
+    out->p_edman_failure = x.p_edman_failure;
+    out->p_detach = x.p_detach;
+    out->p_initial_detach = x.p_initial_detach;
+    out->p_initial_detach_decay = x.p_initial_detach_decay;
+    out->p_initial_block = x.p_initial_block;
+    out->p_cyclic_block = x.p_cyclic_block;
+    for (int c = 0; c < WP_MAX_CHANNELS; c++) {
+        out->p_bleach[c] = c < C ? x.p_bleach[c] : 0.0;
+        out->p_dud[c] = c < C ? x.p_dud[c] : 0.0;
+    }
+    if (step_size) *step_size = step;
+    if (log_l) *log_l = nz > 0 ? -INFINITY : sl;
+    if (iterations) *iterations = iters;
+    return WP_OK;
+}
+
+}  // extern "C"
