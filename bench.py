@@ -12,6 +12,14 @@ A step is one `classify hmm` pass over the batch: 100,000 x 1,000 =
 1e8 (read, peptide) forwards, argmax and count-weighted totals per read.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload classify|fit]
+
+`--workload fit` measures the Baum-Welch E-step instead (reads/s): one
+dye-seq of 20 positions with 4/3/3 dyes on 3 channels (positions seeded),
+200,000 reads simulated from the error model above, 16 timesteps, no
+pruning; a step is one E-step over all reads (the per-iteration work of
+HMMFitter::fit); the line adds one full fit to a 1e-6 step from a seeded
++-50% perturbation of the generating model.
 
 Prints one JSON line (rank 0).  `value` is measured with the reads already in
 device memory (CUDA events on the library's stream, L2 flushed between
@@ -43,6 +51,40 @@ UNIT = "fwd/s"
 T, C, P, READS, CUTOFF = 16, 3, 1000, 100_000, 5.0
 WORKLOAD = ("classify hmm: 3 channels x 16 timesteps, 1000 dye-seqs (8-30 positions, <=5 dyes "
             "per channel, >=1 dye), 100000 reads float64 [100000,16,3], pruning 5 sigma")
+
+
+FIT_METRIC = "Baum-Welch E-step reads/s (fit, 1 dye-seq 4/3/3 dyes, no pruning)"
+FIT_UNIT = "reads/s"
+FIT_READS, FIT_LEN = 200_000, 20
+FIT_WORKLOAD = ("fit: 3 channels x 16 timesteps, 1 dye-seq of 20 positions with 4/3/3 dyes "
+                "(positions seeded), 200000 reads float64 [200000,16,3], unpruned")
+
+
+def make_fit_data(seed: int, reads: int):
+    from whatprot_gb300.model import DyeSeqSet
+    from whatprot_gb300.simulate import paper_model, simulate_radiometries
+    sm = paper_model(C)
+    rng = np.random.default_rng(4)
+    seq = np.full(FIT_LEN, -1, np.int16)
+    pos = rng.permutation(FIT_LEN)[:10]
+    seq[pos[:4]] = 0
+    seq[pos[4:7]] = 1
+    seq[pos[7:]] = 2
+    ds = DyeSeqSet(C, [seq], np.array([0], np.int32), np.array([1], np.int32))
+    rads, _ = simulate_radiometries(sm, ds, T, int(reads * 1.1) + 64, seed=seed)
+    return sm, seq, rads[:reads].copy()
+
+
+def perturbed(sm, seed):
+    import copy
+    rng = np.random.default_rng(seed)
+    out = copy.deepcopy(sm)
+    out.p_edman_failure *= rng.uniform(0.5, 1.5)
+    out.p_detach *= rng.uniform(0.5, 1.5)
+    for cm in out.channel_models:
+        cm.p_bleach *= rng.uniform(0.5, 1.5)
+        cm.p_dud *= rng.uniform(0.5, 1.5)
+    return out
 
 
 def make_data(seed: int, reads: int):
@@ -179,6 +221,183 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_fit(args):
+    """The reference's E-step (PeptideHMM::improve_fit from its own sources,
+    oracle/_ref) over a bounded sample of the fit workload's reads, split
+    across all host threads; the oracle port where oracle/_ref is absent."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib
+    from whatprot_gb300.model import dye_seq_string
+    sm, seq, rads = make_fit_data(seed=99, reads=20000)
+    threads = os.cpu_count() or 1
+    kind = "port"
+    runner = None
+    if oracle_lib.Reference.available():
+        try:
+            ref = oracle_lib.Reference()
+            kind = "reference"
+            s = dye_seq_string(seq)
+
+            def runner(x):
+                ref.improve_fit_batch(sm, T, s, x, threads=threads)
+        except OSError:
+            runner = None
+    if runner is None:
+        o = oracle_lib.Oracle()
+
+        def runner(x):
+            o.improve_fit_batch(sm, T, seq, x, threads=threads)
+    n = max(threads * 2, 32)
+    t0 = time.perf_counter()
+    runner(rads[:n])
+    dt = time.perf_counter() - t0
+    n = int(min(len(rads), max(n, n * 8.0 / max(dt, 1e-3))))
+    for _ in range(args.warmup):
+        runner(rads[:n])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        runner(rads[:n])
+    dt = (time.perf_counter() - t0) / max(args.steps, 1)
+    value = n / dt
+    line = {"metric": FIT_METRIC, "value": value, "unit": FIT_UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded simulator)",
+            "config": {"workload": FIT_WORKLOAD, "sample_reads_per_step": n}, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": FIT_UNIT, "cores": threads, "kind": kind,
+                             "sample": f"{n} reads per step"},
+            "e2e": {"value": value, "unit": FIT_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_fit(sm, seq, rads, seconds_target=15.0):
+    """The CPU oracle's E-step on a bounded sample, all host threads."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from oracle_lib import Oracle
+    threads = os.cpu_count() or 1
+    o = Oracle()
+    n = max(threads * 2, 32)
+    t0 = time.perf_counter()
+    o.improve_fit_batch(sm, T, seq, rads[:n], threads=threads)
+    dt = time.perf_counter() - t0
+    n2 = int(min(len(rads), max(n, n * seconds_target / max(dt, 1e-3))))
+    t0 = time.perf_counter()
+    o.improve_fit_batch(sm, T, seq, rads[:n2], threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n2 / dt, "unit": FIT_UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n2} reads of the same workload, {dt:.1f} s, oracle/wp_oracle.c "
+                      f"wpo_improve_fit_batch with {threads} threads"}
+
+
+def run_fit(args):
+    import torch
+    from whatprot_gb300 import capi
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    reads = args.reads if args.reads != READS else FIT_READS
+    sm, seq, rads = make_fit_data(seed=3030 + rank, reads=reads)
+    R = rads.shape[0]
+    ctx = capi.Context(local)
+    start = perturbed(sm, 77)
+    ctx.upload_model(start, T)
+    h_rads = torch.from_numpy(rads).pin_memory()
+    h_np = h_rads.numpy()
+    ctx.fit_begin(seq, h_np)  # reads resident on the device from here
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=torch.device("cuda", local))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    for _ in range(args.warmup):
+        ctx.fit_estep()
+    torch.cuda.synchronize()
+    ctx.timing_enable(True)
+    launches0 = ctx.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        ctx.fit_estep()
+        ev1.record(stream)
+        ev1.synchronize()
+        total_ms += ev0.elapsed_time(ev1)
+    barrier()
+    clk = clocks.stop()
+    launches = ctx.launch_count() - launches0
+    k_ms, k_n = ctx.timing_read(ctx.KIND_FORWARD)
+    prep_ms, _ = ctx.timing_read(ctx.KIND_PREP)
+    ctx.timing_enable(False)
+    t_step = total_ms / args.steps
+    if dist:
+        t = torch.tensor([t_step], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+    value = R * world / (t_step * 1e-3)
+    # end to end: stage the host reads and run the E-step, every step
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.fit_begin(seq, h_np)
+        ctx.fit_estep()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e = {"value": R * world / e2e_s, "unit": FIT_UNIT, "h2d_bytes_per_step": int(rads.nbytes),
+           "d2h_bytes_per_step": int(R * 8 + 8 * (6 + 2 * (T - 1) + 4 * C))}
+    # one full fit from the perturbed start (stops on a 1e-6 step)
+    t0 = time.perf_counter()
+    fitted, step, log_l, iters = ctx.hmm_fit(start, T, seq, h_np, 1e-6, 600.0)
+    fit_s = time.perf_counter() - t0
+    # the detach rate enters as the curve base + initial * exp(-decay * t)
+    # (base and initial trade off when decay is 0), so compare the curve
+    curve = lambda m: [m.p_detach_at(t) for t in range(T - 1)]
+    err = max([abs(fitted.p_edman_failure - sm.p_edman_failure)]
+              + [abs(a - b) for a, b in zip(curve(fitted), curve(sm))]
+              + [abs(a.p_bleach - b.p_bleach) for a, b in zip(fitted.channel_models, sm.channel_models)]
+              + [abs(a.p_dud - b.p_dud) for a, b in zip(fitted.channel_models, sm.channel_models)])
+    k_avg = k_ms / max(k_n, 1)
+    line = {"metric": FIT_METRIC, "value": value, "unit": FIT_UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded simulator)",
+            "config": {"workload": FIT_WORKLOAD, "reads": R, "timesteps": T, "channels": C,
+                       "dye_seq": "".join("." if d < 0 else str(int(d)) for d in seq),
+                       "l2": "flushed between steps (512 MB write)"},
+            "roofline": {"bound": "memory", "kernel": "wp_fit_estep_kernel", "achieved": None,
+                         "peak": None, "unit": None, "frac": None, "traffic": None,
+                         "estep_kernel_ms": k_avg, "prep_ms_per_step": prep_ms / args.steps},
+            "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+            "fit": {"iterations": iters, "seconds": fit_s, "final_step": step, "log_l": log_l,
+                    "max_abs_error_vs_generating_model": err,
+                    "fitted": {"p_edman_failure": fitted.p_edman_failure, "p_detach": fitted.p_detach,
+                               "p_initial_detach": fitted.p_initial_detach,
+                               "p_initial_detach_decay": fitted.p_initial_detach_decay,
+                               "p_bleach": [c.p_bleach for c in fitted.channel_models],
+                               "p_dud": [c.p_dud for c in fitted.channel_models]}}}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_fit(sm, seq, rads)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -187,7 +406,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--reads", type=int, default=READS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="classify", choices=["classify", "fit"])
     args = ap.parse_args()
+    if args.workload == "fit":
+        return run_reference_fit(args) if args.impl == "reference" else run_fit(args)
     if args.impl == "reference":
         return run_reference(args)
 

@@ -179,6 +179,47 @@ double ref_improve_fit(const wpo_model* m, int T, const char* dye_seq,
     return p;
 }
 
+// One E-step of HMMFitter::fit (hmm-fitter.h:58-78) over R reads, the
+// reads split across OpenMP threads (the reference runs them serially),
+// each thread with its own SequencingModelFitter, added at the end.
+// Returns the sum of the edman denominators (a checksum).
+double ref_improve_fit_batch(const wpo_model* m, int T, const char* dye_seq,
+                             int R, const double* rads, int threads) {
+    int C = m->num_channels;
+    SequencingModel sm;
+    to_reference(m, &sm);
+    SequencingSettings ss;
+    ss.dist_cutoff = std::numeric_limits<double>::max();
+    DyeSeq ds(C, std::string(dye_seq));
+    unsigned max_num_dyes = 0;
+    for (int c = 0; c < C; c++) {
+        unsigned n = 0;
+        for (unsigned i = 0; i < ds.length; i++)
+            if (ds[i] == c) n++;
+        if (n > max_num_dyes) max_num_dyes = n;
+    }
+    UniversalPrecomputations up(sm, T, C);
+    up.set_max_num_dyes(max_num_dyes);
+    DyeSeqPrecomputations dsp(ds, sm, T, C);
+    FitSettings fs(C);
+    double total = 0.0;
+#pragma omp parallel num_threads(threads) reduction(+ : total)
+    {
+        SequencingModelFitter fitter(T, C, sm, fs);
+#pragma omp for schedule(dynamic, 4)
+        for (int r = 0; r < R; r++) {
+            Radiometry rad = make_radiometry(T, C, rads + (long)r * T * C);
+            RadiometryPrecomputations rp(rad, sm, ss, max_num_dyes);
+            PeptideHMM hmm(T, C, dsp, rp, up);
+            SequencingModelFitter pf(T, C, sm, fs);
+            hmm.improve_fit(&pf);
+            fitter += pf;
+        }
+        total += fitter.p_edman_failure_fit.denominator;
+    }
+    return total;
+}
+
 // HMMFitter::fit (hmm-fitter.h:49-116) with no holds and no pruning, as the
 // `fit` CLI runs it (run-fit.cc:55-95).  Returns log(L) of the fitted model.
 double ref_fit(const wpo_model* start, int T, const char* dye_seq, int R,

@@ -1199,3 +1199,103 @@ void wpo_loglik_all(const wpo_model* m, int T, const int16_t* seqs,
     j.out_logp = out_logp;
     run_batch(&j, threads);
 }
+
+/* ------------------------------------------------- Batched E-step (timing) */
+typedef struct {
+    const wpo_model* m;
+    int T;
+    const int16_t* seq;
+    int length;
+    const double* rads;
+    int R;
+    unsigned dmax;
+    double dist_cutoff;
+    int next;
+    pthread_mutex_t lock;
+    wpo_fit_sums* partial; /* one per thread */
+    double* logp;          /* [R], may be NULL */
+} fit_job;
+
+typedef struct {
+    fit_job* j;
+    int id;
+} fit_arg;
+
+static void* fit_worker(void* arg) {
+    fit_arg* a = (fit_arg*)arg;
+    fit_job* j = a->j;
+    int C = j->m->num_channels;
+    for (;;) {
+        pthread_mutex_lock(&j->lock);
+        int r = j->next++;
+        pthread_mutex_unlock(&j->lock);
+        if (r >= j->R) break;
+        double lp;
+        wpo_improve_fit(j->m, j->T, j->seq, j->length, j->rads + (long)r * j->T * C,
+                        j->dmax, j->dist_cutoff, &j->partial[a->id], &lp);
+        if (j->logp) j->logp[r] = lp;
+    }
+    return NULL;
+}
+
+/* HMMFitter's per-iteration E-step loop (fitters/hmm-fitter.h:58-78) over
+ * R reads on `threads` host threads; sums are added into *sums (per-thread
+ * partial sums, combined in thread order). */
+void wpo_improve_fit_batch(const wpo_model* m, int T, const int16_t* seq,
+                           int length, const double* rads, int R,
+                           double dist_cutoff, int threads, wpo_fit_sums* sums,
+                           double* logp) {
+    if (threads < 1) threads = 1;
+    fit_job j;
+    memset(&j, 0, sizeof(j));
+    j.m = m;
+    j.T = T;
+    j.seq = seq;
+    j.length = length;
+    j.rads = rads;
+    j.R = R;
+    j.dist_cutoff = dist_cutoff;
+    /* max_num_dyes of HMMFitter (fitters/hmm-fitter.cc:30-52) */
+    unsigned dmax = 0;
+    for (int c = 0; c < m->num_channels; c++) {
+        unsigned n = 0;
+        for (int i = 0; i < length; i++)
+            if (seq[i] == c) n++;
+        if (n > dmax) dmax = n;
+    }
+    j.dmax = dmax;
+    j.logp = logp;
+    j.partial = (wpo_fit_sums*)calloc(threads, sizeof(wpo_fit_sums));
+    fit_arg* args = (fit_arg*)calloc(threads, sizeof(fit_arg));
+    pthread_mutex_init(&j.lock, NULL);
+    pthread_t* th = (pthread_t*)calloc(threads, sizeof(pthread_t));
+    for (int i = 0; i < threads; i++) {
+        args[i].j = &j;
+        args[i].id = i;
+        pthread_create(&th[i], NULL, fit_worker, &args[i]);
+    }
+    for (int i = 0; i < threads; i++) pthread_join(th[i], NULL);
+    pthread_mutex_destroy(&j.lock);
+    for (int i = 0; i < threads; i++) {
+        const wpo_fit_sums* p = &j.partial[i];
+        sums->edman_num += p->edman_num;
+        sums->edman_den += p->edman_den;
+        for (int t = 0; t < WPO_MAX_TIMESTEPS; t++) {
+            sums->detach_x[t] += p->detach_x[t];
+            sums->detach_n[t] += p->detach_n[t];
+        }
+        sums->init_block_num += p->init_block_num;
+        sums->init_block_den += p->init_block_den;
+        sums->cyc_block_num += p->cyc_block_num;
+        sums->cyc_block_den += p->cyc_block_den;
+        for (int c = 0; c < WPO_MAX_CHANNELS; c++) {
+            sums->bleach_num[c] += p->bleach_num[c];
+            sums->bleach_den[c] += p->bleach_den[c];
+            sums->dud_num[c] += p->dud_num[c];
+            sums->dud_den[c] += p->dud_den[c];
+        }
+    }
+    free(th);
+    free(args);
+    free(j.partial);
+}

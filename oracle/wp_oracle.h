@@ -136,6 +136,12 @@ double wpo_improve_fit(const wpo_model* m, int num_timesteps,
                        const int16_t* seq, int length, const double* rad,
                        unsigned max_num_dyes, double dist_cutoff,
                        wpo_fit_sums* sums, double* log_p);
+/* The same over R reads [R][T][C] on `threads` host threads (the E-step of
+ * one HMMFitter iteration, fitters/hmm-fitter.h:58-78); logp may be NULL. */
+void wpo_improve_fit_batch(const wpo_model* m, int T, const int16_t* seq,
+                           int length, const double* rads, int R,
+                           double dist_cutoff, int threads, wpo_fit_sums* sums,
+                           double* logp);
 
 #ifdef __cplusplus
 }

@@ -115,6 +115,10 @@ class Oracle:
         L.wpo_loglik_all.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                      ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
+        L.wpo_improve_fit_batch.restype = None
+        L.wpo_improve_fit_batch.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p,
+                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                            ctypes.c_int, ctypes.POINTER(WpoFitSums), ctypes.c_void_p]
         L.wpo_improve_fit.restype = ctypes.c_double
         L.wpo_improve_fit.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p,
                                       ctypes.c_int, ctypes.c_void_p, ctypes.c_uint, ctypes.c_double,
@@ -178,6 +182,18 @@ class Oracle:
                                 cutoff, threads, _p(out))
         return out
 
+    def improve_fit_batch(self, sm, T, seq, rads, threads=8, cutoff=DBL_MAX):
+        """E-step over many reads on host threads: (WpoFitSums, log P [R])."""
+        m = to_wpo(sm)
+        seq = np.ascontiguousarray(seq, dtype=np.int16)
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        sums = WpoFitSums()
+        lp = np.zeros(rads.shape[0])
+        self.lib.wpo_improve_fit_batch(ctypes.byref(m), T, _p(seq) if len(seq) else None, len(seq),
+                                       _p(rads), rads.shape[0], cutoff, threads, ctypes.byref(sums),
+                                       _p(lp))
+        return sums, lp
+
     def improve_fit(self, sm, T, seq, rad, max_num_dyes, cutoff=DBL_MAX, sums=None):
         m = to_wpo(sm)
         seq = np.ascontiguousarray(seq, dtype=np.int16)
@@ -216,6 +232,9 @@ class Reference:
         L.ref_offset_exponential.restype = None
         L.ref_offset_exponential.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                              ctypes.c_void_p, ctypes.c_void_p]
+        L.ref_improve_fit_batch.restype = ctypes.c_double
+        L.ref_improve_fit_batch.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_char_p,
+                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
         L.ref_fit.restype = ctypes.c_double
         L.ref_fit.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                               ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.POINTER(WpoModel),
@@ -250,6 +269,14 @@ class Reference:
         p = self.lib.ref_improve_fit(ctypes.byref(m), T, seq_str.encode(), _p(rad), max_num_dyes,
                                      cutoff, ctypes.byref(sums))
         return p, sums
+
+    def improve_fit_batch(self, sm, T, seq_str, rads, threads=8):
+        """E-step over many reads (OpenMP over reads); returns the summed
+        edman denominator as a checksum."""
+        m = to_wpo(sm)
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        return self.lib.ref_improve_fit_batch(ctypes.byref(m), T, seq_str.encode(), rads.shape[0],
+                                              _p(rads), threads)
 
     def offset_exponential(self, y, w, params, held=(0, 0, 0)):
         y = np.ascontiguousarray(y, dtype=np.float64)
