@@ -213,6 +213,44 @@ wp_status wp_hmm_fit(wp_ctx* ctx, const wp_seq_model* start, int num_timesteps,
 wp_status wp_fit_offset_exponential(const double* y, const double* w, int n,
                                     const int* held, double* params);
 
+/* Upload the kNN training set: N unique dye-tracks, counts [N][T][C] (live
+ * dyes per timestep and channel), each with sources src_off[e] ..
+ * src_off[e+1] of (peptide id, peptide count, hits).  Replaces the
+ * dye_tracks vector NNClassifier and HybridClassifier take
+ * (classifiers/nn-classifier.cc:100-117, hybrid-classifier.cc:32-51;
+ * SourcedData<DyeTrack, SourceCountHitsList<int>>, common/sourced-data.h:
+ * 88-140).  Every track needs at least one hit; T * C <= 64.  Entry
+ * coordinates follow the context's model (recomputed after wp_model_upload). */
+wp_status wp_nn_tracks_upload(wp_ctx* ctx, const int16_t* counts, int num_tracks,
+                              int num_timesteps, int num_channels,
+                              const int32_t* src_off, const int32_t* src_id,
+                              const int32_t* src_count, const int32_t* src_hits);
+
+/* NNClassifier::classify(radiometry, h) (classifiers/nn-classifier.cc:
+ * 137-203) for R reads ([R][T][C] host doubles divided by mu): the k-hit
+ * nearest dye-tracks, Gaussian weights exp(-d^2 / 2 sig^2), per-id scores
+ * sum(weight * hits / count), and the top h ids.  Writes per read
+ * out_ncand[r] <= h, out_cand_id / out_cand_score [R][h] (ascending score,
+ * ties by ascending id) and out_total[r] = sum(weight * hits).  The k-hit
+ * set is the shortest distance-ordered prefix whose hits reach k (the
+ * reference's kd-tree search can keep a few more far tracks).  h <= 1024. */
+wp_status wp_nn_classify(wp_ctx* ctx, const double* rads, int num_reads, int k,
+                         double sig, int h, int32_t* out_ncand,
+                         int32_t* out_cand_id, double* out_cand_score,
+                         double* out_total);
+
+/* HybridClassifier::classify (classifiers/hybrid-classifier.cc:55-94):
+ * kNN top-h candidates (as wp_nn_classify), the HMM over those peptides in
+ * ascending kNN score (wp_hmm_classify with candidates; ties go to the
+ * lowest kNN score), its score multiplied by sum(adjusted kNN score x
+ * peptide count), NaN patched.  Peptides come from wp_peptides_upload;
+ * candidate ids absent from them map to peptide index 0 with count 0, as in
+ * the reference.  A read with no candidate gets (-1, 0, 1). */
+wp_status wp_hybrid_classify(wp_ctx* ctx, const double* rads, int num_reads,
+                             int k, double sig, int h, double dist_cutoff,
+                             int32_t* out_id, double* out_score,
+                             double* out_total);
+
 /* Kernel launches issued by this context since creation (all kinds). */
 long long wp_launch_count(const wp_ctx* ctx);
 
@@ -227,8 +265,8 @@ wp_status wp_last_batch_stats(wp_ctx* ctx, long long* stats4);
 void* wp_ctx_stream(const wp_ctx* ctx);
 
 /* Per-kernel timing with CUDA events recorded on the context's stream around
- * every launch while enabled.  kind: 0 forward, 1 prep, 2 combine, 3 flop
- * count.  wp_timing_read synchronises and returns the summed duration in ms
+ * every launch while enabled.  kind: 0 forward (and fit E-step), 1 prep,
+ * 2 combine, 3 flop count, 4 kNN distances, 5 kNN select.  wp_timing_read synchronises and returns the summed duration in ms
  * and the number of launches since the last enable.  No reference
  * counterpart (the reference only prints phase wall times,
  * main/cmd-line-out.cc). */

@@ -15,6 +15,9 @@
 #include <vector>
 
 #include "classifiers/hmm-classifier.h"
+#include "classifiers/hybrid-classifier.h"
+#include "classifiers/nn-classifier.h"
+#include "common/dye-track.h"
 #include "common/dye-seq.h"
 #include "common/radiometry.h"
 #include "common/scored-classification.h"
@@ -82,9 +85,106 @@ Radiometry make_radiometry(int T, int C, const double* rad) {
     return r;
 }
 
+typedef SourcedData<DyeTrack, SourceCountHitsList<int>> TrackData;
+
+// Dye-tracks [N][T][C] with CSR sources as the reference's deduplicated
+// training set (dedup-dye-tracks.cc:118-141).
+std::vector<TrackData> make_tracks(int T, int C, const int16_t* counts, int N,
+                                   const int32_t* src_off, const int32_t* src_id,
+                                   const int32_t* src_count, const int32_t* src_hits) {
+    std::vector<TrackData> out;
+    out.reserve(N);
+    std::vector<short> buf(T * C);
+    for (int e = 0; e < N; e++) {
+        for (int i = 0; i < T * C; i++) buf[i] = counts[(long)e * T * C + i];
+        int ns = src_off[e + 1] - src_off[e];
+        SourceCountHits<int>** srcs = new SourceCountHits<int>*[ns];
+        for (int j = 0; j < ns; j++) {
+            int s = src_off[e] + j;
+            srcs[j] = new SourceCountHits<int>(src_id[s], src_count[s], src_hits[s]);
+        }
+        out.push_back(TrackData(DyeTrack(T, C, buf.data()), SourceCountHitsList<int>(ns, srcs)));
+    }
+    return out;
+}
+
 }  // namespace
 
 extern "C" {
+
+// NNClassifier (nn-classifier.cc:100-215): for every read, classify(rad, h)
+// into [R][h] (ascending score, *ncand entries) and classify(rad) into
+// best_*; OpenMP over reads.
+void ref_nn_classify(const wpo_model* m, int T, const int16_t* counts, int N,
+                     const int32_t* src_off, const int32_t* src_id,
+                     const int32_t* src_count, const int32_t* src_hits,
+                     int R, const double* rads, int k, double sig, int h, int threads,
+                     int32_t* out_ncand, int32_t* out_cand_id, double* out_cand_score,
+                     double* out_cand_total, int32_t* out_best_id, double* out_best_score,
+                     double* out_best_total, double* seconds) {
+    int C = m->num_channels;
+    SequencingModel sm;
+    to_reference(m, &sm);
+    std::vector<TrackData> tracks = make_tracks(T, C, counts, N, src_off, src_id, src_count, src_hits);
+    NNClassifier nn(T, C, sm, k, sig, &tracks);
+    if (threads > 0) omp_set_num_threads(threads);
+    double t0 = omp_get_wtime();
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int r = 0; r < R; r++) {
+        Radiometry rad = make_radiometry(T, C, rads + (long)r * T * C);
+        std::vector<ScoredClassification> top = nn.classify(rad, (unsigned)h);
+        out_ncand[r] = (int)top.size();
+        for (size_t i = 0; i < top.size(); i++) {
+            out_cand_id[(long)r * h + i] = top[i].id;
+            out_cand_score[(long)r * h + i] = top[i].score;
+        }
+        out_cand_total[r] = top.empty() ? 0.0 : top[0].total;
+        ScoredClassification best = nn.classify(rad);
+        out_best_id[r] = best.id;
+        out_best_score[r] = best.score;
+        out_best_total[r] = best.total;
+    }
+    double t1 = omp_get_wtime();
+    if (seconds) *seconds = t1 - t0;
+}
+
+// HybridClassifier::classify(vector<Radiometry>) (hybrid-classifier.cc:
+// 55-94), OpenMP over reads as the CLI runs it.
+void ref_hybrid_classify(const wpo_model* m, int T, const int16_t* counts, int N,
+                         const int32_t* src_off, const int32_t* src_id,
+                         const int32_t* src_count, const int32_t* src_hits, int P,
+                         const char* const* seqs, const int* ids, const int* pcounts, int R,
+                         const double* rads, int k, double sig, int h, double dist_cutoff,
+                         int threads, int* out_id, double* out_score, double* out_total,
+                         double* seconds) {
+    int C = m->num_channels;
+    SequencingModel sm;
+    to_reference(m, &sm);
+    SequencingSettings ss;
+    ss.dist_cutoff = dist_cutoff;
+    std::vector<SourcedData<DyeSeq, SourceCount<int>>> dye_seqs;
+    dye_seqs.reserve(P);
+    for (int i = 0; i < P; i++)
+        dye_seqs.push_back(SourcedData<DyeSeq, SourceCount<int>>(
+                DyeSeq(C, std::string(seqs[i])), SourceCount<int>(ids[i], pcounts[i])));
+    std::vector<TrackData> tracks = make_tracks(T, C, counts, N, src_off, src_id, src_count, src_hits);
+    std::vector<Radiometry> radiometries;
+    radiometries.reserve(R);
+    for (int r = 0; r < R; r++)
+        radiometries.push_back(make_radiometry(T, C, rads + (long)r * T * C));
+    if (threads > 0) omp_set_num_threads(threads);
+    HybridClassifier hybrid(T, C, sm, ss, k, sig, &tracks, h, dye_seqs);
+    double t0 = omp_get_wtime();
+    std::vector<ScoredClassification> results = hybrid.classify(radiometries);
+    double t1 = omp_get_wtime();
+    if (seconds) *seconds = t1 - t0;
+    for (int r = 0; r < R; r++) {
+        out_id[r] = results[r].id;
+        out_score[r] = results[r].score;
+        out_total[r] = results[r].total;
+    }
+}
+
 
 // PeptideHMM(...).probability() for one pair, built as in
 // peptide-hmm.test.cc:154-188.

@@ -1299,3 +1299,218 @@ void wpo_improve_fit_batch(const wpo_model* m, int T, const int16_t* seq,
     free(args);
     free(j.partial);
 }
+
+/* ------------------------------------------------------- kNN classifier */
+/* NNClassifier (classifiers/nn-classifier.cc:59-215) over dye-tracks
+ * counts [N][T][C] with sources (id, count, hits) in CSR form.
+ *
+ * Entry coordinates: KDTEntry::operator[] (nn-classifier.cc:59-74), the
+ * adjusted mu of channel c given the counts of every channel at t; the
+ * query is the radiometry itself (KDTQuery, :94-98).  Squared distances
+ * follow LeafNode::consider (kd-tree/leaf-node.h:31-62): FP64, summed in
+ * groups of four then singly.
+ *
+ * Selection.  KBest::insert (kd-tree/k-best.h:26-42) keeps entries while the
+ * hits of all but the farthest reach k, popping at most one entry per
+ * insertion, so the set it ends with depends on the kd-tree's visiting
+ * order.  This restatement keeps the order-independent set KBest holds when
+ * entries arrive nearest first: the shortest prefix of the entries sorted by
+ * (squared distance, index) whose hits reach k (all entries if they never
+ * do).
+ *
+ * Scores: classify_helper (:137-163): weight exp(-d^2 / (2 sig^2)),
+ * score[id] += weight * hits / count, total += weight * hits, entries taken
+ * farthest first (the order KBest::fill returns them), sources in list order.
+ * Top h: classify(radiometry, h) (:183-203) returns up to h ids in ascending
+ * score; ids are ordered by (score, id) here, the reference's heap leaves
+ * equal scores in an unspecified order. */
+typedef struct {
+    double d2;
+    int idx;
+} nn_cand;
+
+static int nn_cand_cmp(const void* a, const void* b) {
+    const nn_cand* x = (const nn_cand*)a;
+    const nn_cand* y = (const nn_cand*)b;
+    if (x->d2 < y->d2) return -1;
+    if (x->d2 > y->d2) return 1;
+    return (x->idx > y->idx) - (x->idx < y->idx);
+}
+
+typedef struct {
+    int id;
+    double score;
+} nn_score;
+
+static int nn_score_cmp(const void* a, const void* b) {
+    const nn_score* x = (const nn_score*)a;
+    const nn_score* y = (const nn_score*)b;
+    if (x->score < y->score) return -1;
+    if (x->score > y->score) return 1;
+    return (x->id > y->id) - (x->id < y->id);
+}
+
+static int int_cmp(const void* a, const void* b) {
+    int x = *(const int*)a, y = *(const int*)b;
+    return (x > y) - (x < y);
+}
+
+void wpo_nn_coords(const wpo_model* m, int T, const int16_t* counts, int N, double* out) {
+    int C = m->num_channels;
+    for (long e = 0; e < N; e++)
+        for (int t = 0; t < T; t++) {
+            unsigned cts[WPO_MAX_CHANNELS];
+            for (int c = 0; c < C; c++) cts[c] = (unsigned)counts[(e * T + t) * C + c];
+            for (int c = 0; c < C; c++) out[(e * T + t) * C + c] = wpo_adjusted_mu(m, c, cts);
+        }
+}
+
+typedef struct {
+    const double* coords;
+    int N, D;
+    const int32_t *src_off, *src_id, *src_count, *src_hits;
+    const int32_t* uniq; /* sorted distinct source ids */
+    int U;
+    const double* rads;
+    int R, k, h;
+    double two_sig_sq;
+    int32_t* out_ncand;
+    int32_t* out_cand_id;
+    double* out_cand_score;
+    double* out_total;
+    int next;
+    pthread_mutex_t lock;
+} nn_job;
+
+static void nn_one(const nn_job* j, int r, nn_cand* cand, double* acc, nn_score* sc) {
+    const double* q = j->rads + (long)r * j->D;
+    const int D = j->D;
+    long total_hits = 0;
+    for (int e = 0; e < j->N; e++) {
+        const double* x = j->coords + (long)e * D;
+        double d2 = 0.0;
+        int i = 0;
+        while (i < D - 3) {
+            double x1 = q[i] - x[i], x2 = q[i + 1] - x[i + 1];
+            double x3 = q[i + 2] - x[i + 2], x4 = q[i + 3] - x[i + 3];
+            d2 += x1 * x1 + x2 * x2 + x3 * x3 + x4 * x4;
+            i += 4;
+        }
+        while (i < D) {
+            double xx = q[i] - x[i];
+            d2 += xx * xx;
+            i++;
+        }
+        cand[e].d2 = d2;
+        cand[e].idx = e;
+    }
+    qsort(cand, j->N, sizeof(nn_cand), nn_cand_cmp);
+    int m = 0;
+    for (; m < j->N;) {
+        int e = cand[m].idx;
+        for (int s = j->src_off[e]; s < j->src_off[e + 1]; s++) total_hits += j->src_hits[s];
+        m++;
+        if (total_hits >= j->k) break;
+    }
+    for (int u = 0; u < j->U; u++) acc[u] = 0.0;
+    double total = 0.0;
+    for (int i = m - 1; i >= 0; i--) { /* farthest first */
+        int e = cand[i].idx;
+        double w = exp(-cand[i].d2 / j->two_sig_sq);
+        for (int s = j->src_off[e]; s < j->src_off[e + 1]; s++) {
+            const int32_t* p = (const int32_t*)bsearch(&j->src_id[s], j->uniq, j->U, sizeof(int32_t), int_cmp);
+            int u = (int)(p - j->uniq);
+            double hits = (double)j->src_hits[s], count = (double)j->src_count[s];
+            total += w * hits;
+            acc[u] += w * hits / count;
+        }
+    }
+    int n = 0;
+    for (int i = 0; i < m; i++) {
+        int e = cand[i].idx;
+        for (int s = j->src_off[e]; s < j->src_off[e + 1]; s++) {
+            const int32_t* p = (const int32_t*)bsearch(&j->src_id[s], j->uniq, j->U, sizeof(int32_t), int_cmp);
+            int u = (int)(p - j->uniq);
+            if (acc[u] >= 0.0) { /* first visit: emit, then mark */
+                sc[n].id = j->uniq[u];
+                sc[n].score = acc[u];
+                n++;
+                acc[u] = -1.0 - acc[u];
+            }
+        }
+    }
+    qsort(sc, n, sizeof(nn_score), nn_score_cmp);
+    int keep = n < j->h ? n : j->h;
+    j->out_ncand[r] = keep;
+    for (int i = 0; i < keep; i++) {
+        j->out_cand_id[(long)r * j->h + i] = sc[n - keep + i].id;
+        j->out_cand_score[(long)r * j->h + i] = sc[n - keep + i].score;
+    }
+    j->out_total[r] = total;
+}
+
+static void* nn_worker(void* arg) {
+    nn_job* j = (nn_job*)arg;
+    nn_cand* cand = (nn_cand*)malloc(sizeof(nn_cand) * (j->N > 0 ? j->N : 1));
+    double* acc = (double*)malloc(sizeof(double) * (j->U > 0 ? j->U : 1));
+    long ns = j->N > 0 ? j->src_off[j->N] : 0;
+    nn_score* sc = (nn_score*)malloc(sizeof(nn_score) * (ns > 0 ? ns : 1));
+    for (;;) {
+        pthread_mutex_lock(&j->lock);
+        int r = j->next++;
+        pthread_mutex_unlock(&j->lock);
+        if (r >= j->R) break;
+        nn_one(j, r, cand, acc, sc);
+    }
+    free(cand);
+    free(acc);
+    free(sc);
+    return NULL;
+}
+
+void wpo_nn_classify_batch(const wpo_model* m, int T, const int16_t* track_counts, int N,
+                           const int32_t* src_off, const int32_t* src_id,
+                           const int32_t* src_count, const int32_t* src_hits,
+                           const double* rads, int R, int k, double sig, int h,
+                           int threads, int32_t* out_ncand, int32_t* out_cand_id,
+                           double* out_cand_score, double* out_total) {
+    if (threads < 1) threads = 1;
+    int C = m->num_channels;
+    nn_job j;
+    memset(&j, 0, sizeof(j));
+    j.D = T * C;
+    j.N = N;
+    double* coords = (double*)malloc(sizeof(double) * ((long)N * j.D + 1));
+    wpo_nn_coords(m, T, track_counts, N, coords);
+    j.coords = coords;
+    j.src_off = src_off;
+    j.src_id = src_id;
+    j.src_count = src_count;
+    j.src_hits = src_hits;
+    long ns = N > 0 ? src_off[N] : 0;
+    int32_t* uniq = (int32_t*)malloc(sizeof(int32_t) * (ns > 0 ? ns : 1));
+    memcpy(uniq, src_id, sizeof(int32_t) * ns);
+    qsort(uniq, ns, sizeof(int32_t), int_cmp);
+    int U = 0;
+    for (long i = 0; i < ns; i++)
+        if (U == 0 || uniq[U - 1] != uniq[i]) uniq[U++] = uniq[i];
+    j.uniq = uniq;
+    j.U = U;
+    j.rads = rads;
+    j.R = R;
+    j.k = k;
+    j.h = h;
+    j.two_sig_sq = 2.0 * sig * sig;
+    j.out_ncand = out_ncand;
+    j.out_cand_id = out_cand_id;
+    j.out_cand_score = out_cand_score;
+    j.out_total = out_total;
+    pthread_mutex_init(&j.lock, NULL);
+    pthread_t* th = (pthread_t*)calloc(threads, sizeof(pthread_t));
+    for (int i = 0; i < threads; i++) pthread_create(&th[i], NULL, nn_worker, &j);
+    for (int i = 0; i < threads; i++) pthread_join(th[i], NULL);
+    pthread_mutex_destroy(&j.lock);
+    free(th);
+    free(coords);
+    free(uniq);
+}

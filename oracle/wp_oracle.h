@@ -143,6 +143,21 @@ void wpo_improve_fit_batch(const wpo_model* m, int T, const int16_t* seq,
                            double dist_cutoff, int threads, wpo_fit_sums* sums,
                            double* logp);
 
+/* KDTEntry coordinates (nn-classifier.cc:59-74): out[(e*T + t)*C + c]. */
+void wpo_nn_coords(const wpo_model* m, int T, const int16_t* counts, int N, double* out);
+
+/* NNClassifier::classify(radiometry, h) (nn-classifier.cc:120-203) for R
+ * reads over N dye-tracks (counts [N][T][C], sources CSR src_off[N+1]);
+ * writes per read the number of candidates (<= h), their ids and scores in
+ * ascending score order ([R][h]) and the total score.  The k-hit set is the
+ * order-independent one (see wp_oracle.c). */
+void wpo_nn_classify_batch(const wpo_model* m, int T, const int16_t* track_counts, int N,
+                           const int32_t* src_off, const int32_t* src_id,
+                           const int32_t* src_count, const int32_t* src_hits,
+                           const double* rads, int R, int k, double sig, int h,
+                           int threads, int32_t* out_ncand, int32_t* out_cand_id,
+                           double* out_cand_score, double* out_total);
+
 #ifdef __cplusplus
 }
 #endif

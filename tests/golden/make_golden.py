@@ -103,10 +103,31 @@ def fit_fixture(name, C, T, seq_str, nreads, threshold, seed, block=False):
     print(name, rads.shape, "ref fit", params(out), ll, step, f"{secs:.1f}s")
 
 
+def nn_fixture(name, C, T, P, lmin, lmax, per_peptide, nreads, k, sig, h, cutoff, seed):
+    """NNClassifier and HybridClassifier of the reference on a simulated
+    dye-track training set."""
+    from whatprot_gb300.simulate import simulate_dye_track_set
+    sm = paper_model(C)
+    ds = random_dye_seqs(P, C, lmin, lmax, max_per_channel=5, min_total=1, seed=seed)
+    dts = simulate_dye_track_set(sm, ds, T, per_peptide, seed=seed + 1)
+    rads, true_ids = simulate_radiometries(sm, ds, T, nreads, seed=seed + 2)
+    ref = Reference()
+    nc, ids, sc, tot, bid, bsc, btot, _ = ref.nn_classify(sm, T, dts, rads, k, sig, h)
+    hid, hsc, htot, _ = ref.hybrid_classify(sm, T, dts, ds, rads, k, sig, h, cutoff)
+    flat, off = ragged(ds)
+    np.savez_compressed(os.path.join(HERE, name), C=C, T=T, k=k, sig=sig, h=h, cutoff=cutoff, seqs=flat,
+                        offsets=off, ids=ds.ids, counts=ds.counts, tracks=dts.tracks, src_off=dts.src_off,
+                        src_id=dts.src_id, src_count=dts.src_count, src_hits=dts.src_hits, rads=rads,
+                        true_ids=true_ids, nn_ncand=nc, nn_ids=ids, nn_scores=sc, nn_total=tot, nn_best_id=bid,
+                        nn_best_score=bsc, nn_best_total=btot, hy_id=hid, hy_score=hsc, hy_total=htot)
+    print(name, len(dts), "tracks,", rads.shape[0], "reads; hybrid top-1 vs truth",
+          float(np.mean(hid == true_ids)), "nn best vs truth", float(np.mean(bid == true_ids)))
+
+
 if __name__ == "__main__":
     if not Reference.available():
         sys.exit("oracle/_ref/libwpref.so missing: run `make -C oracle ref` where the reference is present")
-    which = sys.argv[1:] or ["classify", "pairs", "fit"]
+    which = sys.argv[1:] or ["classify", "pairs", "fit", "nn"]
     if "classify" in which:
         classify_fixture("classify_c2_t8.npz", 2, 8, 100, 6, 12, 300, 5.0, seed=101)
         classify_fixture("classify_c3_t16.npz", 3, 16, 60, 8, 30, 60, 5.0, seed=202, maxc=5, mint=1)
@@ -116,3 +137,6 @@ if __name__ == "__main__":
     if "fit" in which:
         fit_fixture("fit_c2_t8.npz", 2, 8, "..0.1.0..1", 400, 1e-6, seed=505)
         fit_fixture("fit_c2_t6_block.npz", 2, 6, "0.1.01", 300, 1e-6, seed=606, block=True)
+    if "nn" in which:
+        nn_fixture("nn_c2_t8.npz", 2, 8, 60, 6, 12, 100, 200, 300, 0.5, 20, 5.0, seed=707)
+        nn_fixture("nn_c3_t16.npz", 3, 16, 80, 8, 24, 60, 120, 200, 0.5, 30, 5.0, seed=808)

@@ -115,6 +115,10 @@ class Oracle:
         L.wpo_loglik_all.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                      ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
+        L.wpo_nn_classify_batch.restype = None
+        L.wpo_nn_classify_batch.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int] + [ctypes.c_void_p, ctypes.c_int] \
+            + [ctypes.c_void_p] * 5 + [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int] \
+            + [ctypes.c_void_p] * 4
         L.wpo_improve_fit_batch.restype = None
         L.wpo_improve_fit_batch.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p,
                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
@@ -182,6 +186,21 @@ class Oracle:
                                 cutoff, threads, _p(out))
         return out
 
+    def nn_classify(self, sm, T, dts, rads, k, sig, h, threads=8):
+        """kNN top-h per read: (ncand [R], ids [R,h], scores [R,h], total [R])."""
+        m = to_wpo(sm)
+        R = rads.shape[0]
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        tr = np.ascontiguousarray(dts.tracks, dtype=np.int16)
+        nc = np.zeros(R, np.int32)
+        ids = np.zeros((R, h), np.int32)
+        sc = np.zeros((R, h), np.float64)
+        tot = np.zeros(R, np.float64)
+        self.lib.wpo_nn_classify_batch(ctypes.byref(m), T, _p(tr), len(dts), _p(dts.src_off), _p(dts.src_id),
+                                       _p(dts.src_count), _p(dts.src_hits), _p(rads), R, k, sig, h, threads,
+                                       _p(nc), _p(ids), _p(sc), _p(tot))
+        return nc, ids, sc, tot
+
     def improve_fit_batch(self, sm, T, seq, rads, threads=8, cutoff=DBL_MAX):
         """E-step over many reads on host threads: (WpoFitSums, log P [R])."""
         m = to_wpo(sm)
@@ -235,6 +254,16 @@ class Reference:
         L.ref_improve_fit_batch.restype = ctypes.c_double
         L.ref_improve_fit_batch.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_char_p,
                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+        L.ref_nn_classify.restype = None
+        L.ref_nn_classify.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p, ctypes.c_int] \
+            + [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                       ctypes.c_int] + [ctypes.c_void_p] * 8
+        L.ref_hybrid_classify.restype = None
+        L.ref_hybrid_classify.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p, ctypes.c_int] \
+            + [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                       ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int] \
+            + [ctypes.c_void_p] * 4
         L.ref_fit.restype = ctypes.c_double
         L.ref_fit.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                               ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.POINTER(WpoModel),
@@ -269,6 +298,47 @@ class Reference:
         p = self.lib.ref_improve_fit(ctypes.byref(m), T, seq_str.encode(), _p(rad), max_num_dyes,
                                      cutoff, ctypes.byref(sums))
         return p, sums
+
+    def nn_classify(self, sm, T, dts, rads, k, sig, h, threads=8):
+        """NNClassifier: (ncand, ids [R,h], scores [R,h], total [R], best_id,
+        best_score, best_total, seconds)."""
+        m = to_wpo(sm)
+        R = rads.shape[0]
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        tr = np.ascontiguousarray(dts.tracks, dtype=np.int16)
+        nc = np.zeros(R, np.int32)
+        ids = np.zeros((R, h), np.int32)
+        sc = np.zeros((R, h), np.float64)
+        tot = np.zeros(R, np.float64)
+        bid = np.zeros(R, np.int32)
+        bsc = np.zeros(R, np.float64)
+        btot = np.zeros(R, np.float64)
+        secs = np.zeros(1, np.float64)
+        self.lib.ref_nn_classify(ctypes.byref(m), T, _p(tr), len(dts), _p(dts.src_off), _p(dts.src_id),
+                                 _p(dts.src_count), _p(dts.src_hits), R, _p(rads), k, sig, h, threads,
+                                 _p(nc), _p(ids), _p(sc), _p(tot), _p(bid), _p(bsc), _p(btot), _p(secs))
+        return nc, ids, sc, tot, bid, bsc, btot, float(secs[0])
+
+    def hybrid_classify(self, sm, T, dts, dye_seqs, rads, k, sig, h, cutoff, threads=8):
+        """HybridClassifier: (ids, scores, totals, seconds)."""
+        from whatprot_gb300.model import dye_seq_string
+        m = to_wpo(sm)
+        R = rads.shape[0]
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        tr = np.ascontiguousarray(dts.tracks, dtype=np.int16)
+        strs = [dye_seq_string(s).encode() for s in dye_seqs.seqs]
+        arr = (ctypes.c_char_p * len(strs))(*strs)
+        pid = np.ascontiguousarray(dye_seqs.ids, dtype=np.int32)
+        pc = np.ascontiguousarray(dye_seqs.counts, dtype=np.int32)
+        oid = np.zeros(R, np.int32)
+        osc = np.zeros(R, np.float64)
+        otot = np.zeros(R, np.float64)
+        secs = np.zeros(1, np.float64)
+        self.lib.ref_hybrid_classify(ctypes.byref(m), T, _p(tr), len(dts), _p(dts.src_off), _p(dts.src_id),
+                                     _p(dts.src_count), _p(dts.src_hits), len(strs), arr, _p(pid), _p(pc), R,
+                                     _p(rads), k, sig, h, cutoff, threads, _p(oid), _p(osc), _p(otot),
+                                     _p(secs))
+        return oid, osc, otot, float(secs[0])
 
     def improve_fit_batch(self, sm, T, seq_str, rads, threads=8):
         """E-step over many reads (OpenMP over reads); returns the summed

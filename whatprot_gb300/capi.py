@@ -7,6 +7,7 @@ g.build()"`` or ``python whatprot_gb300/build.py``.
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 import sys
 from typing import Optional, Tuple
@@ -29,7 +30,8 @@ EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload"
            "wp_peptides_upload", "wp_hmm_classify", "wp_hmm_classify_device",
            "wp_hmm_loglik_all", "wp_hmm_count_flops", "wp_launch_count", "wp_ctx_stream",
            "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak", "wp_last_batch_stats",
-           "wp_fit_begin", "wp_fit_estep", "wp_hmm_fit", "wp_fit_offset_exponential"]
+           "wp_fit_begin", "wp_fit_estep", "wp_hmm_fit", "wp_fit_offset_exponential",
+           "wp_nn_tracks_upload", "wp_nn_classify", "wp_hybrid_classify"]
 
 
 class WpSeqModel(ctypes.Structure):
@@ -160,6 +162,12 @@ def load_library(path: Optional[str] = None):
     lib.wp_hmm_fit.restype = I
     lib.wp_fit_offset_exponential.argtypes = [V, V, I, V, V]
     lib.wp_fit_offset_exponential.restype = I
+    lib.wp_nn_tracks_upload.argtypes = [V, V, I, I, I, V, V, V, V]
+    lib.wp_nn_tracks_upload.restype = I
+    lib.wp_nn_classify.argtypes = [V, V, I, I, D, I, V, V, V, V]
+    lib.wp_nn_classify.restype = I
+    lib.wp_hybrid_classify.argtypes = [V, V, I, I, D, I, D, V, V, V]
+    lib.wp_hybrid_classify.restype = I
     if path is None:
         _lib = lib
     return lib
@@ -330,6 +338,38 @@ class Context:
         self.num_channels = start.num_channels
         return fitted, step.value, ll.value, it.value
 
+    def upload_tracks(self, dts) -> None:
+        """wp_nn_tracks_upload: the kNN training set (io.DyeTrackSet)."""
+        tr = np.ascontiguousarray(dts.tracks, dtype=np.int16)
+        N, T, C = tr.shape
+        arr = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        off, sid, scnt, shit = arr(dts.src_off), arr(dts.src_id), arr(dts.src_count), arr(dts.src_hits)
+        self._check(self.lib.wp_nn_tracks_upload(self.h, _ptr(tr), N, T, C, _ptr(off), _ptr(sid), _ptr(scnt),
+                                                 _ptr(shit)))
+
+    def nn_classify(self, rads: np.ndarray, k: int, sig: float, h: int):
+        """wp_nn_classify: (ncand [R], ids [R,h], scores [R,h], total [R])."""
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        R = rads.shape[0]
+        nc = np.zeros(R, np.int32)
+        ids = np.zeros((R, h), np.int32)
+        sc = np.zeros((R, h), np.float64)
+        tot = np.zeros(R, np.float64)
+        self._check(self.lib.wp_nn_classify(self.h, _ptr(rads), R, k, sig, h, _ptr(nc), _ptr(ids), _ptr(sc),
+                                            _ptr(tot)))
+        return nc, ids, sc, tot
+
+    def hybrid_classify(self, rads: np.ndarray, k: int, sig: float, h: int, dist_cutoff: float):
+        """wp_hybrid_classify: (ids, scores, totals) per read."""
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        R = rads.shape[0]
+        ids = np.zeros(R, np.int32)
+        sc = np.zeros(R, np.float64)
+        tot = np.zeros(R, np.float64)
+        self._check(self.lib.wp_hybrid_classify(self.h, _ptr(rads), R, k, sig, h, dist_cutoff, _ptr(ids),
+                                                _ptr(sc), _ptr(tot)))
+        return ids, sc, tot
+
     def launch_count(self) -> int:
         return int(self.lib.wp_launch_count(self.h))
 
@@ -339,7 +379,7 @@ class Context:
     def timing_enable(self, on: bool = True) -> None:
         self._check(self.lib.wp_timing_enable(self.h, 1 if on else 0))
 
-    KIND_FORWARD, KIND_PREP, KIND_COMBINE, KIND_FLOPS = 0, 1, 2, 3
+    KIND_FORWARD, KIND_PREP, KIND_COMBINE, KIND_FLOPS, KIND_KNN_DIST, KIND_KNN_SELECT = 0, 1, 2, 3, 4, 5
 
     def timing_read(self, kind: int) -> Tuple[float, int]:
         ms = ctypes.c_double()
@@ -453,3 +493,63 @@ class HMMFitter:
         self.ctx.fit_begin(self.dye_seq, radiometries)
         _, sl, nz = self.ctx.fit_estep()
         return float("-inf") if nz else sl
+
+
+class NNClassifier:
+    """Host mirror of NNClassifier (classifiers/nn-classifier.h:60-82) on the
+    GPU kNN stage.  The reference's constructor moves the dye-tracks out of
+    the caller's vector; this one copies them to the device."""
+
+    def __init__(self, num_timesteps: int, num_channels: int, seq_model: SequencingModel, k: int,
+                 sig: float, dye_tracks, device: int = 0):
+        self.ctx = Context(device)
+        self.ctx.upload_model(seq_model, num_timesteps)
+        self.ctx.upload_tracks(dye_tracks)
+        self.k, self.sig = k, sig
+
+    def classify(self, radiometries: np.ndarray, h: Optional[int] = None):
+        """One read [T, C] or many [R, T, C].  Without h: the best
+        ScoredClassification per read (NaN patched, nn-classifier.cc:164-181);
+        with h: up to h ScoredClassifications per read in ascending score."""
+        rads = np.asarray(radiometries, dtype=np.float64)
+        single = rads.ndim == 2
+        if single:
+            rads = rads[None]
+        nc, ids, sc, tot = self.ctx.nn_classify(rads, self.k, self.sig, 1 if h is None else h)
+        out = []
+        for r in range(rads.shape[0]):
+            if h is None:
+                if nc[r] == 0:
+                    res = ScoredClassification(-1, -1.0, float(tot[r]))
+                else:
+                    res = ScoredClassification(int(ids[r, nc[r] - 1]), float(sc[r, nc[r] - 1]), float(tot[r]))
+                if math.isnan(res.adjusted_score()):
+                    res.score, res.total = 0.0, 1.0
+                out.append(res)
+            else:
+                out.append([ScoredClassification(int(ids[r, i]), float(sc[r, i]), float(tot[r]))
+                            for i in range(nc[r])])
+        return out[0] if single else out
+
+
+class HybridClassifier:
+    """Host mirror of HybridClassifier (classifiers/hybrid-classifier.h:31-51):
+    kNN candidates, then the HMM over them, on the GPU."""
+
+    def __init__(self, num_timesteps: int, num_channels: int, seq_model: SequencingModel,
+                 dist_cutoff: float, k: int, sig: float, dye_tracks, h: int, dye_seqs: DyeSeqSet,
+                 device: int = 0):
+        self.ctx = Context(device)
+        self.ctx.upload_model(seq_model, num_timesteps)
+        self.ctx.upload_peptides(dye_seqs)
+        self.ctx.upload_tracks(dye_tracks)
+        self.k, self.sig, self.h, self.dist_cutoff = k, sig, h, dist_cutoff
+
+    def classify(self, radiometries: np.ndarray):
+        rads = np.asarray(radiometries, dtype=np.float64)
+        single = rads.ndim == 2
+        if single:
+            rads = rads[None]
+        ids, sc, tot = self.ctx.hybrid_classify(rads, self.k, self.sig, self.h, self.dist_cutoff)
+        res = [ScoredClassification(int(i), float(s), float(t)) for i, s, t in zip(ids, sc, tot)]
+        return res[0] if single else res

@@ -46,6 +46,60 @@ cudaError_t wp_launch_dense(bool has_block, int threads, size_t smem, cudaStream
 size_t wp_dense_smem_bytes(int T, int S_cap, int C, bool has_block, int warps);
 cudaError_t wp_launch_fma_probe(int blocks, int threads, int iters, cudaStream_t stream, float* sink);
 cudaError_t wp_launch_fit_estep(bool has_block, int grid, int threads, cudaStream_t s, const FitArgs& a);
+struct NNArgs {
+    const float* queries;
+    int R;
+    int q0;
+    const float* coords;
+    const int* hits;
+    int N;
+    long long k;
+    int* qbin;
+    int* qbelow;
+    long long* qcap;
+    const long long* qoff;
+    int* cand_idx;
+    float* cand_d2;
+    int* err;
+};
+struct NNSelectArgs {
+    int R;
+    int q0;
+    const int* qbin;
+    const int* qbelow;
+    const long long* qcnt;
+    const long long* qoff;
+    const int* cand_idx;
+    const float* cand_d2;
+    const int* hits;
+    const int* src_off;
+    const int* src_dense;
+    const double* src_ratio;
+    const int* src_hits;
+    const int* dense_id;
+    const int* dense_pep;
+    const int* dense_count;
+    int U;
+    long long k;
+    float inv_two_sig_sq;
+    int h;
+    double* acc;
+    int* mark;
+    int* touched;
+    int* out_ncand;
+    int* out_cand_id;
+    int* out_cand_pep;
+    double* out_cand_score;
+    double* out_total;
+    double* out_subfrac;
+};
+cudaError_t wp_launch_nn_dist(int DP, bool hist, cudaStream_t s, const NNArgs& a);
+cudaError_t wp_launch_nn_select(int grid, cudaStream_t s, const NNSelectArgs& a);
+cudaError_t wp_launch_nn_queries(const double* rads, int R, int TC, int DP, float* out, cudaStream_t s);
+cudaError_t wp_launch_nn_ragged(const int* cand, int h, const int* off, int R, int* out, cudaStream_t s);
+int wp_nn_queries_per_block();
+int wp_nn_select_warps();
+int wp_nn_hmax();
 __global__ void wp_fit_reduce_kernel(const double*, long, int, double*);
 int wp_fit_nslots(int T, int C);
 long wp_fit_floats_per_thread(int T, int C, int S, bool has_block);
@@ -111,8 +165,9 @@ struct wp_ctx {
         cudaEvent_t a, b;
     };
     std::vector<Timed> timed;
-    double t_ms[4] = {0, 0, 0, 0};
-    long long t_n[4] = {0, 0, 0, 0};
+    double t_ms[6] = {0, 0, 0, 0, 0, 0};
+    long long t_n[6] = {0, 0, 0, 0, 0, 0};
+    size_t nn_acc_cleared = 0;  // bytes of the kNN accumulators known to be zero
     int last_engine_grid = 0;
     long long last_slots = 0;
 
@@ -123,6 +178,20 @@ struct wp_ctx {
     int fit_dmax = 0;
     std::vector<int16_t> fit_seq;
     DevBuf d_fit_rads, d_fit_lo, d_fit_hi, d_fit_tab, d_fit_scratch, d_fit_sums, d_fit_out, d_fit_logp;
+
+    // kNN training set (unique dye-tracks with sources).
+    long long model_version = 0;
+    bool have_tracks = false;
+    int nn_N = 0, nn_T = 0, nn_C = 0, nn_U = 0;
+    long long nn_coords_version = -1;
+    long long nn_pep_version = -1;
+    long long pep_version = 0;
+    std::vector<int16_t> nn_counts;
+    std::vector<int32_t> nn_src_off, nn_src_id, nn_src_count, nn_src_hits, nn_uniq;
+    DevBuf d_nn_coords, d_nn_hits, d_nn_src_off, d_nn_src_dense, d_nn_src_ratio, d_nn_src_hits, d_nn_dense_id,
+            d_nn_dense_pep, d_nn_dense_count, d_nn_queries, d_nn_qbin, d_nn_qbelow, d_nn_qcap, d_nn_qoff,
+            d_nn_cidx, d_nn_cd2, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
+            d_nn_cand_score, d_nn_total, d_nn_subfrac, d_nn_cand_off, d_nn_cand_flat, d_nn_err;
 
     // Per-batch scratch.
     DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_Lpk, d_Upk, d_allow, d_flags, d_table, d_res_mant, d_res_expo,
@@ -288,14 +357,17 @@ enum Mode { MODE_CLASSIFY, MODE_LOGP, MODE_FLOPS };
 wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff,
                     const int32_t* h_cand, const int32_t* h_cand_off, Mode mode, double* d_logp,
                     int32_t* d_out_id, double* d_out_score, double* d_out_total, double* d_out_log,
-                    double* d_flops) {
+                    double* d_flops, const int32_t* d_cand_in = nullptr, const int32_t* d_cand_off_in = nullptr) {
     const int C = ctx->hm.C, T = ctx->hm.T;
     wp_status st = plan_peptides(ctx);
     if (st != WP_OK) return st;
     const bool hb = ctx->hm.has_block != 0;
     const int W = ctx->dmax + 1;
     const int entries = wp_read_table_entries(T, C, W, ctx->hm.interacting);
-    long n_slots = h_cand ? (long)h_cand_off[R] : (long)R * ctx->P;
+    // Candidates: host lists (h_cand, h_cand_off) or device lists
+    // (d_cand_in, d_cand_off_in, with the host copy of the offsets).
+    const bool have_cand = h_cand || d_cand_in;
+    long n_slots = have_cand ? (long)h_cand_off[R] : (long)R * ctx->P;
     if (n_slots > INT32_MAX) return fail(ctx, WP_ERR_UNSUPPORTED, "too many (read, peptide) pairs in one batch");
     const size_t rtc = (size_t)R * T * C;
     WP_CUDA(ctx->d_lo.ensure(rtc), "alloc");
@@ -350,7 +422,10 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         WP_CUDA(cudaGetLastError(), "flops launch");
         return WP_OK;
     }
-    if (h_cand) {
+    if (d_cand_in) {
+        a.cand = d_cand_in;
+        a.slot_off = d_cand_off_in;
+    } else if (h_cand) {
         WP_CUDA(ctx->d_cand.ensure(sizeof(int) * std::max<long>(n_slots, 1)), "alloc cand");
         WP_CUDA(ctx->d_slot_off.ensure(sizeof(int) * (R + 1)), "alloc cand");
         for (long k = 0; k < n_slots; k++)
@@ -455,6 +530,245 @@ wp_status finish(wp_ctx* ctx) {
     return WP_OK;
 }
 
+// ChannelModel::adjusted_mu (parameterization/model/channel-model.h:35-54)
+// on the host, for the kNN entry coordinates.
+double host_adjusted_mu(const DevModel& m, int channel, const int* counts) {
+    double amu = m.mu[channel] * (double)counts[channel];
+    for (int c = 0; c < m.C; c++) {
+        const double fi = m.flat[channel][c], ii = m.inter[channel][c];
+        if (c == channel) {
+            if (counts[c] > 1) {
+                if (fi != 1.0) amu *= fi;
+                if (ii != 1.0) amu *= std::pow(ii, (double)(counts[c] - 1));
+            }
+        } else if (counts[c] > 0) {
+            if (fi != 1.0) amu *= fi;
+            if (ii != 1.0) amu *= std::pow(ii, (double)counts[c]);
+        }
+    }
+    return amu;
+}
+
+int nn_padded_dim(int TC) {
+    for (int dp : {16, 32, 48, 64})
+        if (TC <= dp) return dp;
+    return -1;
+}
+
+// Entry coordinates for the current model (KDTEntry::operator[],
+// nn-classifier.cc:59-74), as FP32 rows padded with zeros.
+wp_status nn_prepare(wp_ctx* ctx) {
+    const int T = ctx->nn_T, C = ctx->nn_C, N = ctx->nn_N;
+    const int DP = nn_padded_dim(T * C);
+    if (ctx->nn_coords_version != ctx->model_version) {
+        std::vector<float> coords((size_t)std::max(N, 1) * DP, 0.0f);
+        int cts[WP_MAX_CHANNELS];
+        for (long e = 0; e < N; e++)
+            for (int t = 0; t < T; t++) {
+                for (int c = 0; c < C; c++) cts[c] = ctx->nn_counts[(e * T + t) * C + c];
+                for (int c = 0; c < C; c++)
+                    coords[e * DP + t * C + c] = (float)host_adjusted_mu(ctx->hm, c, cts);
+            }
+        WP_CUDA(ctx->d_nn_coords.ensure(sizeof(float) * coords.size()), "alloc coords");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_coords.p, coords.data(), sizeof(float) * coords.size(),
+                                cudaMemcpyHostToDevice, ctx->stream), "copy coords");
+        WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        ctx->nn_coords_version = ctx->model_version;
+    }
+    return WP_OK;
+}
+
+// Peptide index and count of each source id for the hybrid classifier
+// (hybrid-classifier.cc:46-50); ids absent from the peptide set read as
+// index 0 and count 0, as the reference's unordered_map operator[] gives.
+wp_status nn_prepare_peptides(wp_ctx* ctx) {
+    if (ctx->nn_pep_version == ctx->pep_version) return WP_OK;
+    std::vector<std::pair<int, int>> idx;
+    idx.reserve(ctx->P);
+    for (int i = 0; i < ctx->P; i++) idx.push_back({ctx->ids[i], i});
+    std::sort(idx.begin(), idx.end());
+    std::vector<int> pep(std::max(ctx->nn_U, 1), 0), cnt(std::max(ctx->nn_U, 1), 0);
+    for (int u = 0; u < ctx->nn_U; u++) {
+        const int id = ctx->nn_uniq[u];
+        auto it = std::lower_bound(idx.begin(), idx.end(), std::make_pair(id, INT32_MIN));
+        // the map keeps the last peptide with a repeated id
+        int found = -1;
+        while (it != idx.end() && it->first == id) found = (it++)->second;
+        if (found >= 0) {
+            pep[u] = found;
+            cnt[u] = ctx->counts[found];
+        }
+    }
+    WP_CUDA(ctx->d_nn_dense_pep.ensure(sizeof(int) * pep.size()), "alloc");
+    WP_CUDA(ctx->d_nn_dense_count.ensure(sizeof(int) * cnt.size()), "alloc");
+    WP_CUDA(cudaMemcpyAsync(ctx->d_nn_dense_pep.p, pep.data(), sizeof(int) * pep.size(), cudaMemcpyHostToDevice,
+                            ctx->stream), "copy");
+    WP_CUDA(cudaMemcpyAsync(ctx->d_nn_dense_count.p, cnt.data(), sizeof(int) * cnt.size(), cudaMemcpyHostToDevice,
+                            ctx->stream), "copy");
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    ctx->nn_pep_version = ctx->pep_version;
+    return WP_OK;
+}
+
+// The kNN stage for R reads already on the device (FP64 [R][T][C]):
+// per read the top-h candidates in ascending (score, id) order, the total
+// and, when hybrid, candidate peptide indices and the subfraction.
+wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, int h, bool hybrid) {
+    const int T = ctx->nn_T, C = ctx->nn_C, N = ctx->nn_N;
+    const int DP = nn_padded_dim(T * C);
+    wp_status st = nn_prepare(ctx);
+    if (st != WP_OK) return st;
+    if (hybrid) {
+        st = nn_prepare_peptides(ctx);
+        if (st != WP_OK) return st;
+    }
+    const size_t Rz = (size_t)std::max(R, 1);
+    WP_CUDA(ctx->d_nn_queries.ensure(sizeof(float) * Rz * DP), "alloc queries");
+    WP_CUDA(ctx->d_nn_qbin.ensure(sizeof(int) * Rz), "alloc");
+    WP_CUDA(ctx->d_nn_qbelow.ensure(sizeof(int) * Rz), "alloc");
+    WP_CUDA(ctx->d_nn_qcap.ensure(sizeof(long long) * Rz), "alloc");
+    WP_CUDA(ctx->d_nn_qoff.ensure(sizeof(long long) * Rz), "alloc");
+    WP_CUDA(ctx->d_nn_ncand.ensure(sizeof(int) * Rz), "alloc");
+    WP_CUDA(ctx->d_nn_cand_id.ensure(sizeof(int) * Rz * h), "alloc");
+    WP_CUDA(ctx->d_nn_cand_pep.ensure(sizeof(int) * Rz * h), "alloc");
+    WP_CUDA(ctx->d_nn_cand_score.ensure(sizeof(double) * Rz * h), "alloc");
+    WP_CUDA(ctx->d_nn_total.ensure(sizeof(double) * Rz), "alloc");
+    WP_CUDA(ctx->d_nn_subfrac.ensure(sizeof(double) * Rz), "alloc");
+    WP_CUDA(ctx->d_nn_err.ensure(sizeof(int)), "alloc");
+    WP_CUDA(cudaMemsetAsync(ctx->d_nn_err.p, 0, sizeof(int), ctx->stream), "clear");
+    if (R == 0) return WP_OK;
+    if (N == 0) {
+        WP_CUDA(cudaMemsetAsync(ctx->d_nn_ncand.p, 0, sizeof(int) * R, ctx->stream), "clear");
+        WP_CUDA(cudaMemsetAsync(ctx->d_nn_total.p, 0, sizeof(double) * R, ctx->stream), "clear");
+        WP_CUDA(cudaMemsetAsync(ctx->d_nn_subfrac.p, 0, sizeof(double) * R, ctx->stream), "clear");
+        return WP_OK;
+    }
+    WP_CUDA(wp_launch_nn_queries(d_rads, R, T * C, DP, ctx->d_nn_queries.as<float>(), ctx->stream), "queries");
+    ctx->launches++;
+    NNArgs a;
+    memset(&a, 0, sizeof(a));
+    a.coords = ctx->d_nn_coords.as<float>();
+    a.hits = ctx->d_nn_hits.as<int>();
+    a.N = N;
+    a.k = k;
+    a.qbin = ctx->d_nn_qbin.as<int>();
+    a.qbelow = ctx->d_nn_qbelow.as<int>();
+    a.qcap = ctx->d_nn_qcap.as<long long>();
+    a.err = ctx->d_nn_err.as<int>();
+    // pass 1 over every read
+    a.queries = ctx->d_nn_queries.as<float>();
+    a.R = R;
+    a.q0 = 0;
+    {
+        TimedLaunch tl(ctx, 4);
+        WP_CUDA(wp_launch_nn_dist(DP, true, ctx->stream, a), "kNN histogram");
+        ctx->launches++;
+    }
+    std::vector<long long> cap(R);
+    WP_CUDA(cudaMemcpyAsync(cap.data(), a.qcap, sizeof(long long) * R, cudaMemcpyDeviceToHost, ctx->stream),
+            "copy caps");
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    // per-warp accumulators of the select kernel
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int sel_grid = sms * 4;
+    const long nwarps = (long)sel_grid * wp_nn_select_warps();
+    const int U = std::max(ctx->nn_U, 1);
+    WP_CUDA(ctx->d_nn_acc.ensure(sizeof(double) * nwarps * U), "alloc kNN accumulators");
+    WP_CUDA(ctx->d_nn_mark.ensure(sizeof(int) * nwarps * U), "alloc kNN accumulators");
+    WP_CUDA(ctx->d_nn_touched.ensure(sizeof(int) * nwarps * U), "alloc kNN accumulators");
+    // The select kernel leaves every accumulator it touched at zero again,
+    // so memory is cleared once, when first used.
+    if (sizeof(double) * nwarps * U > ctx->nn_acc_cleared) {
+        WP_CUDA(cudaMemsetAsync(ctx->d_nn_acc.p, 0, sizeof(double) * nwarps * U, ctx->stream), "clear");
+        WP_CUDA(cudaMemsetAsync(ctx->d_nn_mark.p, 0, sizeof(int) * nwarps * U, ctx->stream), "clear");
+        ctx->nn_acc_cleared = sizeof(double) * nwarps * U;
+    }
+    // chunks of reads whose candidate lists fit the budget
+    const long long budget = 256ll << 20;  // candidates per chunk (2 GiB of lists)
+    int r0 = 0;
+    std::vector<long long> off;
+    while (r0 < R) {
+        long long tot = 0;
+        int r1 = r0;
+        off.clear();
+        while (r1 < R && (r1 == r0 || tot + cap[r1] <= budget)) {
+            off.push_back(tot);
+            tot += cap[r1];
+            r1++;
+        }
+        const int nq = r1 - r0;
+        WP_CUDA(ctx->d_nn_cidx.ensure(sizeof(int) * std::max<long long>(tot, 1)), "alloc kNN candidates");
+        WP_CUDA(ctx->d_nn_cd2.ensure(sizeof(float) * std::max<long long>(tot, 1)), "alloc kNN candidates");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_qoff.p, off.data(), sizeof(long long) * nq, cudaMemcpyHostToDevice,
+                                ctx->stream), "copy offsets");
+        a.queries = ctx->d_nn_queries.as<float>() + (size_t)r0 * DP;
+        a.R = nq;
+        a.q0 = r0;
+        a.qoff = ctx->d_nn_qoff.as<long long>();
+        a.cand_idx = ctx->d_nn_cidx.as<int>();
+        a.cand_d2 = ctx->d_nn_cd2.as<float>();
+        {
+            TimedLaunch tl(ctx, 4);
+            WP_CUDA(wp_launch_nn_dist(DP, false, ctx->stream, a), "kNN collect");
+            ctx->launches++;
+        }
+        NNSelectArgs b;
+        memset(&b, 0, sizeof(b));
+        b.R = nq;
+        b.q0 = r0;
+        b.qbin = a.qbin;
+        b.qbelow = a.qbelow;
+        b.qcnt = a.qcap;
+        b.qoff = a.qoff;
+        b.cand_idx = a.cand_idx;
+        b.cand_d2 = a.cand_d2;
+        b.hits = a.hits;
+        b.src_off = ctx->d_nn_src_off.as<int>();
+        b.src_dense = ctx->d_nn_src_dense.as<int>();
+        b.src_ratio = ctx->d_nn_src_ratio.as<double>();
+        b.src_hits = ctx->d_nn_src_hits.as<int>();
+        b.dense_id = ctx->d_nn_dense_id.as<int>();
+        b.dense_pep = hybrid ? ctx->d_nn_dense_pep.as<int>() : nullptr;
+        b.dense_count = hybrid ? ctx->d_nn_dense_count.as<int>() : nullptr;
+        b.U = U;
+        b.k = k;
+        b.inv_two_sig_sq = (float)(1.0 / (2.0 * sig * sig));
+        b.h = h;
+        b.acc = ctx->d_nn_acc.as<double>();
+        b.mark = ctx->d_nn_mark.as<int>();
+        b.touched = ctx->d_nn_touched.as<int>();
+        b.out_ncand = ctx->d_nn_ncand.as<int>();
+        b.out_cand_id = ctx->d_nn_cand_id.as<int>();
+        b.out_cand_pep = hybrid ? ctx->d_nn_cand_pep.as<int>() : nullptr;
+        b.out_cand_score = ctx->d_nn_cand_score.as<double>();
+        b.out_total = ctx->d_nn_total.as<double>();
+        b.out_subfrac = hybrid ? ctx->d_nn_subfrac.as<double>() : nullptr;
+        {
+            TimedLaunch tl(ctx, 5);
+            WP_CUDA(wp_launch_nn_select(sel_grid, ctx->stream, b), "kNN select");
+            ctx->launches++;
+        }
+        WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        r0 = r1;
+    }
+    int err = 0;
+    WP_CUDA(cudaMemcpy(&err, ctx->d_nn_err.p, sizeof(int), cudaMemcpyDeviceToHost), "read err");
+    if (err) return fail(ctx, WP_ERR_CUDA, "internal: kNN candidate list overflow");
+    return WP_OK;
+}
+
+wp_status nn_check(wp_ctx* ctx, int k, double sig, int h) {
+    if (!ctx->have_model) return fail(ctx, WP_ERR_STATE, "model not uploaded");
+    if (!ctx->have_tracks) return fail(ctx, WP_ERR_STATE, "dye-tracks not uploaded");
+    if (ctx->nn_T != ctx->hm.T || ctx->nn_C != ctx->hm.C)
+        return fail(ctx, WP_ERR_STATE, "dye-track shape differs from the model's timesteps/channels");
+    if (k < 1) return fail(ctx, WP_ERR_INVALID, "k must be >= 1");
+    if (!(sig > 0.0)) return fail(ctx, WP_ERR_INVALID, "sig must be > 0");
+    if (h < 1 || h > wp_nn_hmax()) return fail(ctx, WP_ERR_UNSUPPORTED, "h must be in 1..1024");
+    return WP_OK;
+}
+
 wp_status upload_reads(wp_ctx* ctx, const double* rads, int R) {
     const size_t bytes = sizeof(double) * (size_t)R * ctx->hm.T * ctx->hm.C;
     WP_CUDA(ctx->d_rads.ensure(bytes), "alloc reads");
@@ -525,7 +839,7 @@ wp_status wp_timing_enable(wp_ctx* ctx, int enable) {
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
     collect_timing(ctx);
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < 6; k++) {
         ctx->t_ms[k] = 0.0;
         ctx->t_n[k] = 0;
     }
@@ -534,7 +848,7 @@ wp_status wp_timing_enable(wp_ctx* ctx, int enable) {
 }
 
 wp_status wp_timing_read(wp_ctx* ctx, int kind, double* total_ms, long long* launches) {
-    if (!ctx || kind < 0 || kind > 3) return WP_ERR_INVALID;
+    if (!ctx || kind < 0 || kind > 5) return WP_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
     collect_timing(ctx);
@@ -608,6 +922,7 @@ wp_status wp_model_upload(wp_ctx* ctx, const wp_seq_model* m, int T) {
             "copy model");
     WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync model");
     ctx->have_model = true;
+    ctx->model_version++;
     ctx->plan_C = ctx->plan_T = -1;
     return WP_OK;
 }
@@ -627,6 +942,7 @@ wp_status wp_peptides_upload(wp_ctx* ctx, const int16_t* dye_seqs, const int32_t
     ctx->counts.assign(counts, counts + P);
     ctx->P = P;
     ctx->have_peps = true;
+    ctx->pep_version++;
     ctx->plan_C = ctx->plan_T = -1;
     return WP_OK;
 }
@@ -847,6 +1163,150 @@ wp_status wp_fit_estep(wp_ctx* ctx, wp_fit_sums* out, double* sum_logp, int* num
     }
     if (sum_logp) *sum_logp = sl;
     if (num_zero) *num_zero = nz;
+    return WP_OK;
+}
+
+wp_status wp_nn_tracks_upload(wp_ctx* ctx, const int16_t* counts, int N, int T, int C, const int32_t* src_off,
+                              const int32_t* src_id, const int32_t* src_count, const int32_t* src_hits) {
+    if (!ctx || N < 0 || (N > 0 && (!counts || !src_off))) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if (C < 1 || C > WP_MAX_CHANNELS || T < 1 || T > WP_MAX_TIMESTEPS)
+        return fail(ctx, WP_ERR_UNSUPPORTED, "dye-track shape out of range");
+    if (nn_padded_dim(T * C) < 0) return fail(ctx, WP_ERR_UNSUPPORTED, "kNN needs timesteps x channels <= 64");
+    const int S = N > 0 ? src_off[N] : 0;
+    if (N > 0 && src_off[0] != 0) return fail(ctx, WP_ERR_INVALID, "src_off[0] must be 0");
+    if (S > 0 && (!src_id || !src_count || !src_hits)) return WP_ERR_INVALID;
+    std::vector<int> ehits(std::max(N, 1), 0);
+    for (int e = 0; e < N; e++) {
+        if (src_off[e + 1] < src_off[e]) return fail(ctx, WP_ERR_INVALID, "src_off not ascending");
+        long long hsum = 0;
+        for (int s2 = src_off[e]; s2 < src_off[e + 1]; s2++) {
+            if (src_hits[s2] < 0 || src_count[s2] < 0) return fail(ctx, WP_ERR_INVALID, "negative hits or count");
+            hsum += src_hits[s2];
+        }
+        if (hsum < 1 || hsum > INT32_MAX) return fail(ctx, WP_ERR_INVALID, "every dye-track needs 1..2^31-1 hits");
+        ehits[e] = (int)hsum;
+    }
+    ctx->nn_counts.assign(counts, counts + (size_t)N * T * C);
+    ctx->nn_src_off.assign(src_off, src_off + (N > 0 ? N + 1 : 0));
+    ctx->nn_src_id.assign(src_id, src_id + S);
+    ctx->nn_src_count.assign(src_count, src_count + S);
+    ctx->nn_src_hits.assign(src_hits, src_hits + S);
+    ctx->nn_uniq = ctx->nn_src_id;
+    std::sort(ctx->nn_uniq.begin(), ctx->nn_uniq.end());
+    ctx->nn_uniq.erase(std::unique(ctx->nn_uniq.begin(), ctx->nn_uniq.end()), ctx->nn_uniq.end());
+    ctx->nn_N = N;
+    ctx->nn_T = T;
+    ctx->nn_C = C;
+    ctx->nn_U = (int)ctx->nn_uniq.size();
+    std::vector<int> dense(std::max(S, 1), 0);
+    std::vector<double> ratio(std::max(S, 1), 0.0);
+    for (int i = 0; i < S; i++) {
+        dense[i] = (int)(std::lower_bound(ctx->nn_uniq.begin(), ctx->nn_uniq.end(), src_id[i]) - ctx->nn_uniq.begin());
+        ratio[i] = (double)src_hits[i] / (double)src_count[i];  // hits / count (nn-classifier.cc:154-158)
+    }
+    std::vector<int> off(ctx->nn_src_off);
+    if (off.empty()) off.push_back(0);
+    WP_CUDA(ctx->d_nn_hits.ensure(sizeof(int) * ehits.size()), "alloc");
+    WP_CUDA(ctx->d_nn_src_off.ensure(sizeof(int) * off.size()), "alloc");
+    WP_CUDA(ctx->d_nn_src_dense.ensure(sizeof(int) * dense.size()), "alloc");
+    WP_CUDA(ctx->d_nn_src_ratio.ensure(sizeof(double) * ratio.size()), "alloc");
+    WP_CUDA(ctx->d_nn_src_hits.ensure(sizeof(int) * std::max(S, 1)), "alloc");
+    WP_CUDA(ctx->d_nn_dense_id.ensure(sizeof(int) * std::max(ctx->nn_U, 1)), "alloc");
+    WP_CUDA(cudaMemcpyAsync(ctx->d_nn_hits.p, ehits.data(), sizeof(int) * ehits.size(), cudaMemcpyHostToDevice, ctx->stream), "copy");
+    WP_CUDA(cudaMemcpyAsync(ctx->d_nn_src_off.p, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, ctx->stream), "copy");
+    WP_CUDA(cudaMemcpyAsync(ctx->d_nn_src_dense.p, dense.data(), sizeof(int) * dense.size(), cudaMemcpyHostToDevice, ctx->stream), "copy");
+    WP_CUDA(cudaMemcpyAsync(ctx->d_nn_src_ratio.p, ratio.data(), sizeof(double) * ratio.size(), cudaMemcpyHostToDevice, ctx->stream), "copy");
+    if (S > 0)
+        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_src_hits.p, src_hits, sizeof(int) * S, cudaMemcpyHostToDevice, ctx->stream), "copy");
+    if (ctx->nn_U > 0)
+        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_dense_id.p, ctx->nn_uniq.data(), sizeof(int) * ctx->nn_U, cudaMemcpyHostToDevice, ctx->stream), "copy");
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    ctx->have_tracks = true;
+    ctx->nn_coords_version = -1;
+    ctx->nn_pep_version = -1;
+    return WP_OK;
+}
+
+wp_status wp_nn_classify(wp_ctx* ctx, const double* rads, int R, int k, double sig, int h, int32_t* out_ncand,
+                         int32_t* out_cand_id, double* out_cand_score, double* out_total) {
+    if (!ctx || R < 0 || (R > 0 && (!rads || !out_ncand || !out_cand_id || !out_cand_score || !out_total)))
+        return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    wp_status st = nn_check(ctx, k, sig, h);
+    if (st != WP_OK) return st;
+    if (R == 0) return WP_OK;
+    st = upload_reads(ctx, rads, R);
+    if (st != WP_OK) return st;
+    st = nn_run(ctx, ctx->d_rads.as<double>(), R, k, sig, h, false);
+    if (st != WP_OK) return st;
+    WP_CUDA(cudaMemcpyAsync(out_ncand, ctx->d_nn_ncand.p, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    WP_CUDA(cudaMemcpyAsync(out_total, ctx->d_nn_total.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    WP_CUDA(cudaMemcpyAsync(out_cand_id, ctx->d_nn_cand_id.p, sizeof(int) * (size_t)R * h, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    WP_CUDA(cudaMemcpyAsync(out_cand_score, ctx->d_nn_cand_score.p, sizeof(double) * (size_t)R * h, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    return WP_OK;
+}
+
+wp_status wp_hybrid_classify(wp_ctx* ctx, const double* rads, int R, int k, double sig, int h, double dist_cutoff,
+                             int32_t* out_id, double* out_score, double* out_total) {
+    if (!ctx || R < 0 || (R > 0 && (!rads || !out_id || !out_score || !out_total))) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    wp_status st = nn_check(ctx, k, sig, h);
+    if (st != WP_OK) return st;
+    st = check_ready(ctx);
+    if (st != WP_OK) return st;
+    if (ctx->P == 0) return fail(ctx, WP_ERR_INVALID, "the hybrid classifier needs at least one peptide");
+    if (R == 0) return WP_OK;
+    st = upload_reads(ctx, rads, R);
+    if (st != WP_OK) return st;
+    st = nn_run(ctx, ctx->d_rads.as<double>(), R, k, sig, h, true);
+    if (st != WP_OK) return st;
+    // ragged candidate lists (ascending kNN score) for the HMM stage
+    std::vector<int> ncand(R), off(R + 1, 0);
+    std::vector<double> subfrac(R);
+    WP_CUDA(cudaMemcpyAsync(ncand.data(), ctx->d_nn_ncand.p, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    WP_CUDA(cudaMemcpyAsync(subfrac.data(), ctx->d_nn_subfrac.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    for (int r = 0; r < R; r++) off[r + 1] = off[r] + ncand[r];
+    WP_CUDA(ctx->d_nn_cand_off.ensure(sizeof(int) * (R + 1)), "alloc");
+    WP_CUDA(ctx->d_nn_cand_flat.ensure(sizeof(int) * std::max(off[R], 1)), "alloc");
+    WP_CUDA(cudaMemcpyAsync(ctx->d_nn_cand_off.p, off.data(), sizeof(int) * (R + 1), cudaMemcpyHostToDevice, ctx->stream), "copy");
+    WP_CUDA(wp_launch_nn_ragged(ctx->d_nn_cand_pep.as<int>(), h, ctx->d_nn_cand_off.as<int>(), R,
+                                ctx->d_nn_cand_flat.as<int>(), ctx->stream), "ragged");
+    ctx->launches++;
+    WP_CUDA(ctx->d_out_id.ensure(sizeof(int) * R), "alloc outputs");
+    WP_CUDA(ctx->d_out_score.ensure(sizeof(double) * R), "alloc outputs");
+    WP_CUDA(ctx->d_out_total.ensure(sizeof(double) * R), "alloc outputs");
+    st = run_batch(ctx, ctx->d_rads.as<double>(), R, dist_cutoff, nullptr, off.data(), MODE_CLASSIFY, nullptr,
+                   ctx->d_out_id.as<int>(), ctx->d_out_score.as<double>(), ctx->d_out_total.as<double>(), nullptr,
+                   nullptr, ctx->d_nn_cand_flat.as<int>(), ctx->d_nn_cand_off.as<int>());
+    if (st != WP_OK) return st;
+    WP_CUDA(cudaMemcpyAsync(out_id, ctx->d_out_id.p, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    WP_CUDA(cudaMemcpyAsync(out_score, ctx->d_out_score.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    WP_CUDA(cudaMemcpyAsync(out_total, ctx->d_out_total.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    st = finish(ctx);
+    if (st != WP_OK) return st;
+    // HybridClassifier::classify (hybrid-classifier.cc:55-81): the HMM's
+    // score scaled by the candidates' kNN subfraction, NaN patched.  With no
+    // candidate the reference indexes past its lists; here the read gets
+    // (-1, 0, 1).
+    for (int r = 0; r < R; r++) {
+        if (ncand[r] == 0) {
+            out_id[r] = -1;
+            out_score[r] = 0.0;
+            out_total[r] = 1.0;
+            continue;
+        }
+        out_score[r] *= subfrac[r];
+        if (std::isnan(out_score[r] / out_total[r])) {
+            out_score[r] = 0.0;
+            out_total[r] = 1.0;
+        }
+    }
     return WP_OK;
 }
 

@@ -1,0 +1,617 @@
+// wp_nn.cu -- the kNN stage of NNClassifier / HybridClassifier
+// (classifiers/nn-classifier.cc:120-215, kd-tree/*) on the GPU.
+//
+// The reference searches a kd-tree for the entries (unique dye-tracks) whose
+// simulated hits add up to k, weights each by exp(-d^2 / 2 sig^2) and scores
+// every source peptide id.  Here the search is brute force, as a tiled FP32
+// contraction of queries against all entries, in three kernels:
+//
+//   wp_nn_hist_kernel     every (query, entry) squared distance, binned on a
+//                         log scale (4 bins per octave); per query a histogram
+//                         of hits per bin gives the bin b* where the running
+//                         hits reach k, the hits below it and an upper bound
+//                         on the entries at or below it.
+//   wp_nn_collect_kernel  the same distances again; each query (one thread)
+//                         appends the entries in bins <= b* to its candidate
+//                         list, in entry order (deterministic).
+//   wp_nn_select_kernel   one warp per query: the exact k-hit set (entries in
+//                         bins < b*, then those of bin b* by a hits-weighted
+//                         radix select on the distance bits, ties by entry
+//                         index), the weighted scores per peptide (per-id sums
+//                         formed in a fixed order), the total, and the top h
+//                         ids in ascending (score, id) order.
+//
+// The set is the shortest prefix of the entries sorted by (squared
+// distance, entry index) whose hits reach k: what KBest (k-best.h:26-42)
+// holds when entries arrive nearest first.  The kd-tree's visiting order can
+// leave a few more far entries in the reference's set.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "wp_common.cuh"
+
+#define NN_NB 64           // distance bins per query
+#define NN_TE 32           // entries per shared-memory tile
+#define NN_THREADS 128     // threads per CTA in the distance kernels
+#define NN_QPT 2           // queries per thread
+#define NN_QPB (NN_THREADS * NN_QPT)
+#define NN_SEL_WARPS 4     // warps per CTA in the select kernel
+#define NN_HMAX 1024       // largest h
+
+// Log-scale bin of a squared distance: bin 1 starts at 2^-6, four bins per
+// octave (the exponent and the top two mantissa bits of the float), bin 0
+// below, bin NB-1 open-ended.  Monotone in d2.
+__device__ __forceinline__ int nn_bin(float d2) {
+    const int b = (int)(__float_as_uint(d2) >> 21) - ((127 - 6) << 2) + 1;
+    return b < 0 ? 0 : (b > NN_NB - 1 ? NN_NB - 1 : b);
+}
+
+// Squared distance of a query (registers) to an entry (shared memory); the
+// same code in both distance kernels, so both see the same float.
+template <int DP>
+__device__ __forceinline__ float nn_d2(const float* q, const float* e) {
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+    for (int i = 0; i < DP; i += 4) {
+        const float4 v = *reinterpret_cast<const float4*>(e + i);
+        const float x0 = q[i] - v.x, x1 = q[i + 1] - v.y, x2 = q[i + 2] - v.z, x3 = q[i + 3] - v.w;
+        a0 = fmaf(x0, x0, a0);
+        a1 = fmaf(x1, x1, a1);
+        a2 = fmaf(x2, x2, a2);
+        a3 = fmaf(x3, x3, a3);
+    }
+    return (a0 + a1) + (a2 + a3);
+}
+
+struct NNArgs {
+    const float* queries;   // [R][DP]
+    int R;                  // queries in this launch (chunk)
+    int q0;                 // first query index of the chunk (into per-query arrays)
+    const float* coords;    // [N][DP]
+    const int* hits;        // [N] total hits per entry
+    int N;
+    long long k;
+    // per query (indexed by q0 + local)
+    int* qbin;
+    int* qbelow;            // hits in bins < b*
+    long long* qcap;        // hits in bins <= b* (>= entries there)
+    const long long* qoff;  // candidate list offset (chunk-relative)
+    int* cand_idx;
+    float* cand_d2;
+    int* err;
+};
+
+// Load a tile of entries (coords and hits) into shared memory.
+template <int DP>
+__device__ __forceinline__ void nn_load_tile(const NNArgs& a, int e0, float* tile, int* thits) {
+    const int n = min(NN_TE, a.N - e0);
+    const float4* src = reinterpret_cast<const float4*>(a.coords + (long)e0 * DP);
+    float4* dst = reinterpret_cast<float4*>(tile);
+    for (int i = threadIdx.x; i < NN_TE * DP / 4; i += blockDim.x)
+        dst[i] = (i < n * DP / 4) ? src[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = threadIdx.x; i < NN_TE; i += blockDim.x) thits[i] = i < n ? a.hits[e0 + i] : 0;
+}
+
+template <int DP>
+__global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
+    extern __shared__ __align__(16) unsigned char nn_smem[];
+    float* tile = reinterpret_cast<float*>(nn_smem);
+    int* thits = reinterpret_cast<int*>(tile + NN_TE * DP);
+    unsigned* hist = reinterpret_cast<unsigned*>(thits + NN_TE);  // [NN_QPB][NN_NB + 1]
+    const int qb = blockIdx.x * NN_QPB;
+    for (int i = threadIdx.x; i < NN_QPB * (NN_NB + 1); i += blockDim.x) hist[i] = 0u;
+    float q[NN_QPT][DP];
+    bool valid[NN_QPT];
+#pragma unroll
+    for (int j = 0; j < NN_QPT; j++) {
+        const int lq = threadIdx.x + j * NN_THREADS;
+        valid[j] = qb + lq < a.R;
+        const float* src = a.queries + (long)(valid[j] ? qb + lq : 0) * DP;
+#pragma unroll
+        for (int i = 0; i < DP; i++) q[j][i] = valid[j] ? src[i] : 0.f;
+    }
+    for (int e0 = 0; e0 < a.N; e0 += NN_TE) {
+        __syncthreads();
+        nn_load_tile<DP>(a, e0, tile, thits);
+        __syncthreads();
+        const int n = min(NN_TE, a.N - e0);
+        for (int e = 0; e < n; e++) {
+#pragma unroll
+            for (int j = 0; j < NN_QPT; j++) {
+                const float d2 = nn_d2<DP>(q[j], tile + e * DP);
+                if (valid[j])
+                    atomicAdd(&hist[(threadIdx.x + j * NN_THREADS) * (NN_NB + 1) + nn_bin(d2)], (unsigned)thits[e]);
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NN_QPT; j++) {
+        if (!valid[j]) continue;
+        const int lq = threadIdx.x + j * NN_THREADS;
+        const unsigned* h = hist + lq * (NN_NB + 1);
+        long long cum = 0, below = 0, cap = 0;
+        int b = NN_NB - 1;
+        bool found = false;
+        for (int i = 0; i < NN_NB; i++) {
+            if (!found && cum + h[i] >= a.k) {
+                found = true;
+                b = i;
+                below = cum;
+                cap = cum + h[i];
+            }
+            cum += h[i];
+        }
+        if (!found) {  // all hits stay below k: every entry is kept
+            b = NN_NB - 1;
+            below = cum - h[NN_NB - 1];
+            cap = cum;
+        }
+        const int gq = a.q0 + qb + lq;
+        a.qbin[gq] = b;
+        a.qbelow[gq] = (int)below;
+        a.qcap[gq] = cap;
+    }
+}
+
+template <int DP>
+__global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
+    extern __shared__ __align__(16) unsigned char nn_smem[];
+    float* tile = reinterpret_cast<float*>(nn_smem);
+    int* thits = reinterpret_cast<int*>(tile + NN_TE * DP);
+    const int qb = blockIdx.x * NN_QPB;
+    float q[NN_QPT][DP];
+    bool valid[NN_QPT];
+    int bstar[NN_QPT];
+    long long off[NN_QPT], cap[NN_QPT], cnt[NN_QPT];
+#pragma unroll
+    for (int j = 0; j < NN_QPT; j++) {
+        const int lq = threadIdx.x + j * NN_THREADS;
+        valid[j] = qb + lq < a.R;
+        const int l = valid[j] ? qb + lq : 0;
+        const float* src = a.queries + (long)l * DP;
+#pragma unroll
+        for (int i = 0; i < DP; i++) q[j][i] = valid[j] ? src[i] : 0.f;
+        bstar[j] = valid[j] ? a.qbin[a.q0 + l] : -1;
+        off[j] = valid[j] ? a.qoff[l] : 0;
+        cap[j] = valid[j] ? a.qcap[a.q0 + l] : 0;
+        cnt[j] = 0;
+    }
+    for (int e0 = 0; e0 < a.N; e0 += NN_TE) {
+        __syncthreads();
+        nn_load_tile<DP>(a, e0, tile, thits);
+        __syncthreads();
+        const int n = min(NN_TE, a.N - e0);
+        for (int e = 0; e < n; e++) {
+#pragma unroll
+            for (int j = 0; j < NN_QPT; j++) {
+                const float d2 = nn_d2<DP>(q[j], tile + e * DP);
+                if (nn_bin(d2) <= bstar[j]) {
+                    if (cnt[j] < cap[j]) {
+                        a.cand_idx[off[j] + cnt[j]] = e0 + e;
+                        a.cand_d2[off[j] + cnt[j]] = d2;
+                    } else {
+                        atomicExch(a.err, 1);
+                    }
+                    cnt[j]++;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NN_QPT; j++)
+        if (valid[j]) a.qcap[a.q0 + qb + threadIdx.x + j * NN_THREADS] = cnt[j];  // now: entries collected
+}
+
+struct NNSelectArgs {
+    int R;                      // queries in this chunk
+    int q0;
+    const int* qbin;
+    const int* qbelow;
+    const long long* qcnt;      // candidates per query (after collect)
+    const long long* qoff;
+    const int* cand_idx;
+    const float* cand_d2;
+    const int* hits;            // [N]
+    const int* src_off;         // [N + 1]
+    const int* src_dense;       // [S] dense id
+    const double* src_ratio;    // [S] hits / count
+    const int* src_hits;        // [S]
+    const int* dense_id;        // [U] original id
+    const int* dense_pep;       // [U] peptide index (hybrid), may be null
+    const int* dense_count;     // [U] peptide count (hybrid), may be null
+    int U;
+    long long k;
+    float inv_two_sig_sq;
+    int h;
+    double* acc;                // [warps][U] zero on entry, zero on exit
+    int* mark;                  // [warps][U]
+    int* touched;               // [warps][U]
+    // outputs, indexed by q0 + local
+    int* out_ncand;
+    int* out_cand_id;           // [R][h] original ids
+    int* out_cand_pep;          // [R][h] peptide indices (may be null)
+    double* out_cand_score;     // [R][h]
+    double* out_total;
+    double* out_subfrac;        // may be null
+};
+
+__device__ __forceinline__ unsigned long long nn_dbits(double v) { return (unsigned long long)__double_as_longlong(v); }
+
+// Warp-wide inclusive prefix sum.
+__device__ __forceinline__ long long warp_incl_scan(long long v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        long long t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelectArgs a) {
+    extern __shared__ __align__(16) unsigned char nn_sel_smem[];
+    unsigned long long(*s_hist)[256] = reinterpret_cast<unsigned long long(*)[256]>(nn_sel_smem);
+    double(*s_key)[NN_HMAX] = reinterpret_cast<double(*)[NN_HMAX]>(nn_sel_smem + sizeof(unsigned long long) * 256 * NN_SEL_WARPS);
+    int(*s_id)[NN_HMAX] = reinterpret_cast<int(*)[NN_HMAX]>(nn_sel_smem + sizeof(unsigned long long) * 256 * NN_SEL_WARPS
+                                                              + sizeof(double) * NN_HMAX * NN_SEL_WARPS);
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const long gw = (long)blockIdx.x * NN_SEL_WARPS + wib;
+    const long nw = (long)gridDim.x * NN_SEL_WARPS;
+    double* acc = a.acc + gw * a.U;
+    int* mark = a.mark + gw * a.U;
+    int* touched = a.touched + gw * a.U;
+    unsigned long long* hist = s_hist[wib];
+
+    for (long lq = gw; lq < a.R; lq += nw) {
+        const int gq = a.q0 + (int)lq;
+        const int bstar = a.qbin[gq];
+        const long long m = a.qcnt[gq];
+        const int* cidx = a.cand_idx + a.qoff[lq];
+        const float* cd2 = a.cand_d2 + a.qoff[lq];
+        long long need = a.k - a.qbelow[gq];  // hits still needed from bin b*
+
+        // ---- hits-weighted radix select over the float bits of d2 in bin b*.
+        unsigned prefix = 0u, pmask = 0u;
+        bool take_all = false;
+        for (int pass = 0; pass < 4 && !take_all; pass++) {
+            const int shift = 24 - 8 * pass;
+            for (int i = lane; i < 256; i += 32) hist[i] = 0ull;
+            __syncwarp();
+            for (long long i = lane; i < m; i += 32) {
+                const float d2 = cd2[i];
+                const unsigned key = __float_as_uint(d2);
+                if (nn_bin(d2) == bstar && (key & pmask) == prefix)
+                    atomicAdd(&hist[(key >> shift) & 255u], (unsigned long long)a.hits[cidx[i]]);
+            }
+            __syncwarp();
+            // find the digit where the running hits reach `need`
+            long long tot = 0;
+            for (int i = lane; i < 256; i += 32) tot += (long long)hist[i];
+            for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+            if (tot < need) {
+                take_all = true;  // hits of this prefix never reach k: keep them all
+                break;
+            }
+            // lane l covers digits [8l, 8l + 8)
+            long long mine = 0;
+            for (int i = 0; i < 8; i++) mine += (long long)hist[lane * 8 + i];
+            const long long incl = warp_incl_scan(mine);
+            const unsigned hit = __ballot_sync(0xffffffffu, incl >= need);
+            const int L = __ffs(hit) - 1;
+            long long before = __shfl_sync(0xffffffffu, incl - mine, L);
+            int digit = 0;
+            if (lane == L) {
+                long long c = before;
+                for (int i = 0; i < 8; i++) {
+                    const long long hb = (long long)hist[L * 8 + i];
+                    if (c + hb >= need) {
+                        digit = L * 8 + i;
+                        break;
+                    }
+                    c += hb;
+                }
+                before = c;
+            }
+            digit = __shfl_sync(0xffffffffu, digit, L);
+            before = __shfl_sync(0xffffffffu, before, L);
+            need -= before;
+            prefix |= (unsigned)digit << shift;
+            pmask |= 255u << shift;
+            __syncwarp();
+        }
+        const unsigned kstar = prefix;  // with take_all: unused
+        // ---- contributions of the kept entries, in candidate (entry) order.
+        double total_part = 0.0;
+        int ntouched = 0;
+        long long tie_cum = 0;  // hits of key == kstar entries seen so far
+        for (long long base = 0; base < m; base += 32) {
+            const long long i = base + lane;
+            bool keep = false;
+            int e = -1;
+            float d2 = 0.f;
+            bool tie = false;
+            if (i < m) {
+                e = cidx[i];
+                d2 = cd2[i];
+                const int b = nn_bin(d2);
+                const unsigned key = __float_as_uint(d2);
+                if (b < bstar || take_all) keep = true;
+                else if (key < kstar) keep = true;
+                else if (key == kstar) tie = true;
+            }
+            // ties at kstar: keep in entry order while the tie hits before
+            // this one are below `need`
+            const long long th = tie ? (long long)a.hits[e] : 0;
+            const long long incl = warp_incl_scan(th);
+            if (tie && tie_cum + incl - th < need) keep = true;
+            tie_cum += __shfl_sync(0xffffffffu, incl, 31);
+            // exp(-d2 / 2 sig^2) as 2^x: exp2f of the fraction, the integer
+            // part applied in FP64 so far entries keep a non-zero weight
+            double w = 0.0;
+            if (keep) {
+                const float x = -d2 * a.inv_two_sig_sq * 1.4426950408889634f;
+                const float fl = floorf(x);
+                w = ldexp((double)exp2f(x - fl), (int)fl);
+            }
+            const int s0 = keep ? a.src_off[e] : 0;
+            const int ns = keep ? a.src_off[e + 1] - s0 : 0;
+            int nmax = ns;
+            for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
+            for (int s = 0; s < nmax; s++) {
+                const bool act = s < ns;
+                int id = -1;
+                double val = 0.0;
+                if (act) {
+                    id = a.src_dense[s0 + s];
+                    val = w * a.src_ratio[s0 + s];
+                    total_part += w * (double)a.src_hits[s0 + s];
+                }
+                const unsigned actm = __ballot_sync(0xffffffffu, act);
+                if (actm == 0u) continue;
+                const unsigned grp = __match_any_sync(0xffffffffu, id);
+                // group sum in lane order, at the group's lowest lane
+                double gsum = 0.0;
+                unsigned gm = grp;
+                while (gm) {
+                    const int src = __ffs(gm) - 1;
+                    gm &= gm - 1;
+                    const double v = __shfl_sync(grp, val, src);
+                    gsum += v;
+                }
+                const bool leader = act && lane == __ffs(grp) - 1;
+                const bool fresh = leader && mark[id] == 0;
+                const unsigned fm = __ballot_sync(0xffffffffu, fresh);
+                if (fresh) {
+                    mark[id] = 1;
+                    touched[ntouched + __popc(fm & ((1u << lane) - 1u))] = id;
+                }
+                if (leader) acc[id] += gsum;
+                ntouched += __popc(fm);
+                __syncwarp();
+            }
+        }
+        // total, summed in a fixed tree order and broadcast from lane 0
+        double tot = total_part;
+        for (int o = 16; o > 0; o >>= 1) tot += __shfl_down_sync(0xffffffffu, tot, o);
+        tot = __shfl_sync(0xffffffffu, tot, 0);
+
+        // ---- top h of the touched ids by (score, id).
+        const int h = a.h;
+        int nsel = 0;
+        unsigned long long sthr = 0ull;  // keep ids with score bits > sthr, ties by id
+        int tie_keep = 0;                 // how many score == sthr ids to keep (largest ids)
+        bool all = ntouched <= h;
+        if (!all) {
+            // radix select of the h-th largest score (count based, 8 passes)
+            unsigned long long pre = 0ull, msk = 0ull;
+            long long want = h;  // from the top
+            for (int pass = 0; pass < 8; pass++) {
+                const int shift = 56 - 8 * pass;
+                for (int i = lane; i < 256; i += 32) hist[i] = 0ull;
+                __syncwarp();
+                for (int i = lane; i < ntouched; i += 32) {
+                    const unsigned long long kb = nn_dbits(acc[touched[i]]);
+                    if ((kb & msk) == pre) atomicAdd(&hist[(kb >> shift) & 255ull], 1ull);
+                }
+                __syncwarp();
+                // scan from the largest digit down: lane l covers digits
+                // [248 - 8l, 256 - 8l)
+                long long mine = 0;
+                for (int i = 0; i < 8; i++) mine += (long long)hist[255 - (lane * 8 + i)];
+                const long long incl = warp_incl_scan(mine);
+                const unsigned hit = __ballot_sync(0xffffffffu, incl >= want);
+                const int L = __ffs(hit) - 1;
+                long long before = __shfl_sync(0xffffffffu, incl - mine, L);
+                int digit = 0;
+                if (lane == L) {
+                    long long c = before;
+                    for (int i = 0; i < 8; i++) {
+                        const int d = 255 - (L * 8 + i);
+                        const long long hb = (long long)hist[d];
+                        if (c + hb >= want) {
+                            digit = d;
+                            break;
+                        }
+                        c += hb;
+                    }
+                    before = c;
+                }
+                digit = __shfl_sync(0xffffffffu, digit, L);
+                before = __shfl_sync(0xffffffffu, before, L);
+                want -= before;
+                pre |= (unsigned long long)digit << shift;
+                msk |= 255ull << shift;
+                __syncwarp();
+            }
+            sthr = pre;
+            tie_keep = (int)want;  // ids with score == sthr to keep, largest ids first
+        }
+        // gather the kept ids into shared memory (order fixed below by sort)
+        for (int base = 0; base < ntouched; base += 32) {
+            const int i = base + lane;
+            bool sel = false;
+            int id = 0;
+            double sc = 0.0;
+            if (i < ntouched) {
+                id = touched[i];
+                sc = acc[id];
+                if (all) sel = true;
+                else {
+                    const unsigned long long kb = nn_dbits(sc);
+                    if (kb > sthr) sel = true;
+                    else if (kb == sthr) {
+                        // keep the tie_keep largest ids among the ties: count
+                        // ties with a larger id
+                        int larger = 0;
+                        for (int j = 0; j < ntouched; j++) {
+                            const int oid = touched[j];
+                            if (oid > id && nn_dbits(acc[oid]) == sthr) larger++;
+                        }
+                        sel = larger < tie_keep;
+                    }
+                }
+            }
+            const unsigned sm = __ballot_sync(0xffffffffu, sel);
+            if (sel) {
+                const int pos = nsel + __popc(sm & ((1u << lane) - 1u));
+                s_key[wib][pos] = sc;
+                s_id[wib][pos] = id;
+            }
+            nsel += __popc(sm);
+        }
+        __syncwarp();
+        // bitonic sort ascending by (score, id) over the next power of two
+        int n2 = 1;
+        while (n2 < nsel) n2 <<= 1;
+        for (int i = nsel + lane; i < n2; i += 32) {
+            s_key[wib][i] = INFINITY;
+            s_id[wib][i] = 0x7fffffff;
+        }
+        __syncwarp();
+        for (int size = 2; size <= n2; size <<= 1) {
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int i = lane; i < n2; i += 32) {
+                    const int j = i ^ stride;
+                    if (j > i) {
+                        const bool up = (i & size) == 0;
+                        const double ki = s_key[wib][i], kj = s_key[wib][j];
+                        const int ii = s_id[wib][i], ij = s_id[wib][j];
+                        const bool gt = ki > kj || (ki == kj && ii > ij);
+                        if (gt == up) {
+                            s_key[wib][i] = kj;
+                            s_key[wib][j] = ki;
+                            s_id[wib][i] = ij;
+                            s_id[wib][j] = ii;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        // outputs
+        for (int i = lane; i < nsel; i += 32) {
+            const int u = s_id[wib][i];
+            a.out_cand_id[(long)gq * h + i] = a.dense_id[u];
+            a.out_cand_score[(long)gq * h + i] = s_key[wib][i];
+            if (a.out_cand_pep) a.out_cand_pep[(long)gq * h + i] = a.dense_pep[u];
+        }
+        if (lane == 0) {
+            a.out_ncand[gq] = nsel;
+            a.out_total[gq] = tot;
+            if (a.out_subfrac) {
+                // HybridClassifier: sum of adjusted score x peptide count, in
+                // candidate order (hybrid-classifier.cc:58-64)
+                double sf = 0.0;
+                for (int i = 0; i < nsel; i++)
+                    sf += (s_key[wib][i] / tot) * (double)a.dense_count[s_id[wib][i]];
+                a.out_subfrac[gq] = sf;
+            }
+        }
+        __syncwarp();
+        // reset the per-warp accumulators
+        for (int i = lane; i < ntouched; i += 32) {
+            const int id = touched[i];
+            acc[id] = 0.0;
+            mark[id] = 0;
+        }
+        __syncwarp();
+    }
+}
+
+// Queries as FP32 rows padded to DP (zeros beyond T * C).
+__global__ void wp_nn_queries_kernel(const double* __restrict__ rads, int R, int TC, int DP,
+                                     float* __restrict__ out) {
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long)R * DP) return;
+    const long r = i / DP;
+    const int d = (int)(i % DP);
+    out[i] = d < TC ? (float)rads[r * TC + d] : 0.f;
+}
+
+// Gather [R][h] candidate lists into one ragged array (offsets given).
+__global__ void wp_nn_ragged_kernel(const int* __restrict__ cand, int h, const int* __restrict__ off, int R,
+                                    int* __restrict__ out) {
+    const int r = blockIdx.x;
+    if (r >= R) return;
+    const int n = off[r + 1] - off[r];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) out[off[r] + i] = cand[(long)r * h + i];
+}
+
+size_t wp_nn_dist_smem_bytes(int DP, bool with_hist) {
+    size_t b = sizeof(float) * NN_TE * DP + sizeof(int) * NN_TE;
+    if (with_hist) b += sizeof(unsigned) * NN_QPB * (NN_NB + 1);
+    return b;
+}
+
+int wp_nn_queries_per_block() { return NN_QPB; }
+int wp_nn_select_warps() { return NN_SEL_WARPS; }
+int wp_nn_hmax() { return NN_HMAX; }
+
+template <int DP>
+static cudaError_t launch_dist(bool hist, int grid, cudaStream_t s, const NNArgs& a) {
+    const size_t smem = wp_nn_dist_smem_bytes(DP, hist);
+    if (hist) {
+        cudaFuncSetAttribute(wp_nn_hist_kernel<DP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        wp_nn_hist_kernel<DP><<<grid, NN_THREADS, smem, s>>>(a);
+    } else {
+        cudaFuncSetAttribute(wp_nn_collect_kernel<DP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        wp_nn_collect_kernel<DP><<<grid, NN_THREADS, smem, s>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+// DP: padded dimension, one of 16, 32, 48, 64.
+cudaError_t wp_launch_nn_dist(int DP, bool hist, cudaStream_t s, const NNArgs& a) {
+    const int grid = (a.R + NN_QPB - 1) / NN_QPB;
+    if (grid == 0) return cudaSuccess;
+    switch (DP) {
+        case 16: return launch_dist<16>(hist, grid, s, a);
+        case 32: return launch_dist<32>(hist, grid, s, a);
+        case 48: return launch_dist<48>(hist, grid, s, a);
+        case 64: return launch_dist<64>(hist, grid, s, a);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t wp_launch_nn_select(int grid, cudaStream_t s, const NNSelectArgs& a) {
+    const size_t smem = (sizeof(unsigned long long) * 256 + (sizeof(double) + sizeof(int)) * NN_HMAX) * NN_SEL_WARPS;
+    cudaFuncSetAttribute(wp_nn_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    wp_nn_select_kernel<<<grid, NN_SEL_WARPS * 32, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t wp_launch_nn_queries(const double* rads, int R, int TC, int DP, float* out, cudaStream_t s) {
+    const long n = (long)R * DP;
+    if (n == 0) return cudaSuccess;
+    wp_nn_queries_kernel<<<(int)((n + 255) / 256), 256, 0, s>>>(rads, R, TC, DP, out);
+    return cudaGetLastError();
+}
+
+cudaError_t wp_launch_nn_ragged(const int* cand, int h, const int* off, int R, int* out, cudaStream_t s) {
+    if (R == 0) return cudaSuccess;
+    wp_nn_ragged_kernel<<<R, 128, 0, s>>>(cand, h, off, R, out);
+    return cudaGetLastError();
+}

@@ -146,6 +146,47 @@ def simulate_radiometries(model: SequencingModel, dye_seqs: DyeSeqSet, num_times
     return rads, ids.astype(np.int32)
 
 
+def simulate_dye_track_set(model: SequencingModel, dye_seqs: DyeSeqSet, num_timesteps: int,
+                           per_peptide: int, seed: int = 0):
+    """The kNN training set: per_peptide dye-tracks for every peptide (times
+    its count), all-zero tracks dropped (generate-dye-tracks.cc:29-70), then
+    deduplicated into unique tracks with (id, count, hits) sources
+    (dedup-dye-tracks.cc:44-141).  Tracks come out in lexicographic order of
+    their counts and sources in ascending id (the reference's order is that
+    of its hash maps)."""
+    from .io import DyeTrackSet
+    rng = np.random.default_rng(seed)
+    C = model.num_channels
+    reps = np.repeat(np.arange(len(dye_seqs)), dye_seqs.counts.astype(np.int64) * per_peptide)
+    lengths = np.array([len(dye_seqs.seqs[i]) for i in reps], dtype=np.int64)
+    Lmax = max(1, int(lengths.max()) if len(lengths) else 1)
+    seqs = np.full((len(reps), Lmax), -1, dtype=np.int16)
+    for r, i in enumerate(reps):
+        s = dye_seqs.seqs[i]
+        seqs[r, : len(s)] = s
+    tracks = simulate_dye_tracks(model, seqs, lengths, num_timesteps, rng)
+    keep = np.any(tracks[:, 0, :] != 0, axis=1)
+    tracks = tracks[keep]
+    pep = reps[keep]
+    flat = tracks.reshape(len(tracks), -1)
+    uniq, inv = np.unique(flat, axis=0, return_inverse=True)
+    inv = inv.reshape(-1)
+    # hits per (unique track, peptide)
+    key = inv.astype(np.int64) * (len(dye_seqs) + 1) + pep
+    ukey, hits = np.unique(key, return_counts=True)
+    track_of = ukey // (len(dye_seqs) + 1)
+    pep_of = ukey % (len(dye_seqs) + 1)
+    src_off = np.zeros(len(uniq) + 1, np.int32)
+    np.add.at(src_off, track_of + 1, 1)
+    src_off = np.cumsum(src_off).astype(np.int32)
+    order = np.lexsort((dye_seqs.ids[pep_of], track_of))
+    src_id = dye_seqs.ids[pep_of][order].astype(np.int32)
+    src_count = dye_seqs.counts[pep_of][order].astype(np.int32)
+    src_hits = hits[order].astype(np.int32)
+    return DyeTrackSet(uniq.reshape(len(uniq), num_timesteps, C).astype(np.int16), src_off, src_id,
+                       src_count, src_hits)
+
+
 def paper_model(num_channels: int) -> SequencingModel:
     """The error model of the benchmark configurations: p_edman_failure 0.06,
     p_detach 0.05, no initial detach or blocking; per channel p_bleach 0.05,
