@@ -12,7 +12,7 @@ A step is one `classify hmm` pass over the batch: 100,000 x 1,000 =
 1e8 (read, peptide) forwards, argmax and count-weighted totals per read.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload classify|fit]
+                    [--workload classify|fit|hybrid]
 
 `--workload fit` measures the Baum-Welch E-step instead (reads/s): one
 dye-seq of 20 positions with 4/3/3 dyes on 3 channels (positions seeded),
@@ -20,6 +20,12 @@ dye-seq of 20 positions with 4/3/3 dyes on 3 channels (positions seeded),
 pruning; a step is one E-step over all reads (the per-iteration work of
 HMMFitter::fit); the line adds one full fit to a 1e-6 step from a seeded
 +-50% perturbation of the generating model.
+
+`--workload hybrid` measures the hybrid classifier (reads/s): 20,000
+dye-seqs as above, a dye-track training set of 100 simulated reads per
+dye-seq (about 945,000 unique tracks), kNN with k = 10,000 hits and sigma
+0.5, the top 1,000 candidates rescored by the HMM (pruning 5 sigma), 100,000
+query reads per step (--reads to change).
 
 Prints one JSON line (rank 0).  `value` is measured with the reads already in
 device memory (CUDA events on the library's stream, L2 flushed between
@@ -51,6 +57,205 @@ UNIT = "fwd/s"
 T, C, P, READS, CUTOFF = 16, 3, 1000, 100_000, 5.0
 WORKLOAD = ("classify hmm: 3 channels x 16 timesteps, 1000 dye-seqs (8-30 positions, <=5 dyes "
             "per channel, >=1 dye), 100000 reads float64 [100000,16,3], pruning 5 sigma")
+
+
+HY_METRIC = "hybrid classify reads/s (kNN k=10000 hits, sigma 0.5, H=1000 -> HMM -p 5)"
+HY_UNIT = "reads/s"
+HY_P, HY_PER, HY_K, HY_SIG, HY_H, HY_READS = 20_000, 100, 10_000, 0.5, 1000, 100_000
+HY_WORKLOAD = ("hybrid: 3 channels x 16 timesteps, 20000 dye-seqs (8-30 positions, <=5 dyes per channel), "
+               "dye-track training set of 100 simulated reads per dye-seq deduplicated, kNN k=10000 hits, "
+               "sigma 0.5, H=1000 candidates to the HMM with pruning 5 sigma")
+
+
+def make_hybrid_data(seed: int, reads: int):
+    from whatprot_gb300.simulate import (paper_model, random_dye_seqs, simulate_dye_track_set,
+                                         simulate_radiometries)
+    sm = paper_model(C)
+    ds = random_dye_seqs(HY_P, C, 8, 30, max_per_channel=5, min_total=1, seed=1234)
+    dts = simulate_dye_track_set(sm, ds, T, HY_PER, seed=4321)
+    rads, ids = simulate_radiometries(sm, ds, T, int(reads * 1.05) + 64, seed=seed)
+    return sm, ds, dts, rads[:reads].copy(), ids[:reads].copy()
+
+
+def run_hybrid(args):
+    import torch
+    from whatprot_gb300 import capi
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    reads = args.reads if args.reads != READS else HY_READS
+    t0 = time.perf_counter()
+    sm, ds, dts, rads, true_ids = make_hybrid_data(seed=5050 + rank, reads=reads)
+    gen_s = time.perf_counter() - t0
+    R = rads.shape[0]
+    ctx = capi.Context(local)
+    ctx.upload_model(sm, T)
+    ctx.upload_peptides(ds)
+    ctx.upload_tracks(dts)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=torch.device("cuda", local))
+    d_rads = torch.from_numpy(rads).to(f"cuda:{local}")
+    d_id = torch.empty(R, dtype=torch.int32, device=f"cuda:{local}")
+    d_sc = torch.empty(R, dtype=torch.float64, device=f"cuda:{local}")
+    d_tot = torch.empty(R, dtype=torch.float64, device=f"cuda:{local}")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    def step():
+        ctx.hybrid_classify_device(d_rads.data_ptr(), R, HY_K, HY_SIG, HY_H, CUTOFF, d_id.data_ptr(),
+                                   d_sc.data_ptr(), d_tot.data_ptr())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ctx.timing_enable(True)
+    launches0 = ctx.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        step()
+        ev1.record(stream)
+        ev1.synchronize()
+        total_ms += ev0.elapsed_time(ev1)
+    barrier()
+    clk = clocks.stop()
+    launches = ctx.launch_count() - launches0
+    kd_ms, kd_n = ctx.timing_read(ctx.KIND_KNN_DIST)
+    ks_ms, _ = ctx.timing_read(ctx.KIND_KNN_SELECT)
+    fw_ms, _ = ctx.timing_read(ctx.KIND_FORWARD)
+    pr_ms, _ = ctx.timing_read(ctx.KIND_PREP)
+    ctx.timing_enable(False)
+    t_step = total_ms / args.steps
+    if dist:
+        t = torch.tensor([t_step], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+    value = R * world / (t_step * 1e-3)
+    acc = float((d_id.cpu().numpy() == true_ids).mean())
+    # end to end through the host API (pinned reads)
+    h_rads = torch.from_numpy(rads).pin_memory().numpy()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.hybrid_classify(h_rads, HY_K, HY_SIG, HY_H, CUTOFF)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e = {"value": R * world / e2e_s, "unit": HY_UNIT, "h2d_bytes_per_step": int(rads.nbytes),
+           "d2h_bytes_per_step": int(R * (4 + 8 + 8))}
+    # the kNN distance stage: algorithmic work = one (query, track) squared
+    # distance per pair, 3 FP32 operations per dimension (sub, multiply-add)
+    N = len(dts)
+    algo = 3.0 * R * N * T * C
+    peak = ctx.fp32_peak_tflops()
+    kd_step = kd_ms / args.steps
+    achieved = algo / (kd_step * 1e-3) / 1e12 if kd_step > 0 else None
+    line = {"metric": HY_METRIC, "value": value, "unit": HY_UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded simulator)",
+            "config": {"workload": HY_WORKLOAD, "reads": R, "peptides": len(ds), "dye_tracks": N,
+                       "track_sources": int(dts.src_off[-1]), "k": HY_K, "sigma": HY_SIG, "h": HY_H,
+                       "dist_cutoff": CUTOFF, "l2": "flushed between steps (512 MB write)",
+                       "data_generation_s": gen_s},
+            "top1_vs_truth": acc,
+            "roofline": {"bound": "fp32", "kernel": "wp_nn_hist_kernel + wp_nn_collect_kernel",
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if (achieved and peak) else None, "traffic": None,
+                         "peak_source": "FP32 FMA loop measured live (wp_probe_fp32_peak)",
+                         "algorithmic_flops_per_step": algo,
+                         "knn_distance_ms_per_step": kd_step, "knn_select_ms_per_step": ks_ms / args.steps,
+                         "hmm_forward_ms_per_step": fw_ms / args.steps, "hmm_prep_ms_per_step": pr_ms / args.steps},
+            "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_hybrid(sm, ds, dts, rads)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def cpu_baseline_hybrid(sm, ds, dts, rads, seconds_target=15.0):
+    """The CPU oracle's hybrid classifier (brute-force FP64 kNN, then the HMM
+    over the candidates) on a bounded sample of the reads, all host threads."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from oracle_lib import Oracle
+    threads = os.cpu_count() or 1
+    o = Oracle()
+    n = threads
+    t0 = time.perf_counter()
+    o.hybrid_classify(sm, T, dts, ds, rads[:n], HY_K, HY_SIG, HY_H, CUTOFF, threads=threads)
+    dt = time.perf_counter() - t0
+    n2 = int(min(len(rads), max(n, n * seconds_target / max(dt, 1e-3))))
+    t0 = time.perf_counter()
+    o.hybrid_classify(sm, T, dts, ds, rads[:n2], HY_K, HY_SIG, HY_H, CUTOFF, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n2 / dt, "unit": HY_UNIT, "cores": threads, "kind": "port",
+            "sample": f"{n2} reads of the same workload, {dt:.1f} s, oracle/wp_oracle.c "
+                      f"wpo_hybrid_classify_batch (brute-force kNN) with {threads} threads"}
+
+
+def run_reference_hybrid(args):
+    """The reference's HybridClassifier (its own sources, oracle/_ref) on a
+    bounded sample of the hybrid workload, all host threads; the oracle port
+    where oracle/_ref is absent."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib
+    sm, ds, dts, rads, _ = make_hybrid_data(seed=99, reads=4096)
+    threads = os.cpu_count() or 1
+    kind = "port"
+    if oracle_lib.Reference.available():
+        ref = oracle_lib.Reference()
+        kind = "reference"
+
+        def runner(x):
+            return ref.hybrid_classify(sm, T, dts, ds, x, HY_K, HY_SIG, HY_H, CUTOFF, threads=threads)[3]
+    else:
+        o = oracle_lib.Oracle()
+
+        def runner(x):
+            t0 = time.perf_counter()
+            o.hybrid_classify(sm, T, dts, ds, x, HY_K, HY_SIG, HY_H, CUTOFF, threads=threads)
+            return time.perf_counter() - t0
+    n = threads
+    dt = runner(rads[:n])
+    n = int(min(len(rads), max(n, n * 8.0 / max(dt, 1e-3))))
+    for _ in range(args.warmup):
+        runner(rads[:n])
+    tot = 0.0
+    for _ in range(args.steps):
+        tot += runner(rads[:n])
+    dt = tot / max(args.steps, 1)
+    value = n / dt
+    line = {"metric": HY_METRIC, "value": value, "unit": HY_UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded simulator)",
+            "config": {"workload": HY_WORKLOAD, "sample_reads_per_step": n, "dye_tracks": len(dts),
+                       "timed": "classify call only (classifier construction excluded)"},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": HY_UNIT, "cores": threads, "kind": kind,
+                             "sample": f"{n} reads per step"},
+            "e2e": {"value": value, "unit": HY_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
 
 
 FIT_METRIC = "Baum-Welch E-step reads/s (fit, 1 dye-seq 4/3/3 dyes, no pruning)"
@@ -406,8 +611,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--reads", type=int, default=READS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="classify", choices=["classify", "fit"])
+    ap.add_argument("--workload", default="classify", choices=["classify", "fit", "hybrid"])
     args = ap.parse_args()
+    if args.workload == "hybrid":
+        return run_reference_hybrid(args) if args.impl == "reference" else run_hybrid(args)
     if args.workload == "fit":
         return run_reference_fit(args) if args.impl == "reference" else run_fit(args)
     if args.impl == "reference":

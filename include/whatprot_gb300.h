@@ -251,6 +251,14 @@ wp_status wp_hybrid_classify(wp_ctx* ctx, const double* rads, int num_reads,
                              int32_t* out_id, double* out_score,
                              double* out_total);
 
+/* wp_hybrid_classify with reads and outputs in device memory (d_rads
+ * [num_reads][T][C] doubles; d_out_* device arrays); returns after
+ * completion. */
+wp_status wp_hybrid_classify_device(wp_ctx* ctx, const double* d_rads,
+                                    int num_reads, int k, double sig, int h,
+                                    double dist_cutoff, int32_t* d_out_id,
+                                    double* d_out_score, double* d_out_total);
+
 /* Kernel launches issued by this context since creation (all kinds). */
 long long wp_launch_count(const wp_ctx* ctx);
 

@@ -1378,9 +1378,64 @@ typedef struct {
     int32_t* out_cand_id;
     double* out_cand_score;
     double* out_total;
+    /* hybrid (when seqs != NULL) */
+    const wpo_model* m;
+    int T;
+    const int16_t* seqs;
+    const int32_t* offsets;
+    const int32_t* pep_ids;
+    const int32_t* pep_counts;
+    int P;
+    unsigned dmax;
+    double dist_cutoff;
+    int32_t* hy_id;
+    double* hy_score;
+    double* hy_total;
     int next;
     pthread_mutex_t lock;
 } nn_job;
+
+/* HybridClassifier::classify (hybrid-classifier.cc:55-81) after the kNN
+ * stage of read r: peptide indices of the candidates through the id map
+ * (absent ids read as index 0 and count 0, unordered_map operator[]), the
+ * HMM over them in ascending kNN score, the score times the subfraction,
+ * the NaN patch. */
+static void hybrid_one(const nn_job* j, int r) {
+    int nc = j->out_ncand[r];
+    if (nc == 0) {
+        j->hy_id[r] = -1;
+        j->hy_score[r] = 0.0;
+        j->hy_total[r] = 1.0;
+        return;
+    }
+    int32_t* cand = (int32_t*)malloc(sizeof(int32_t) * nc);
+    double sub = 0.0;
+    double total = j->out_total[r];
+    for (int i = 0; i < nc; i++) {
+        int id = j->out_cand_id[(long)r * j->h + i];
+        int idx = 0, cnt = 0;
+        for (int p = 0; p < j->P; p++) /* the map keeps the last peptide with an id */
+            if (j->pep_ids[p] == id) {
+                idx = p;
+                cnt = j->pep_counts[p];
+            }
+        cand[i] = idx;
+        sub += (j->out_cand_score[(long)r * j->h + i] / total) * (double)cnt;
+    }
+    int32_t id;
+    double score, tot;
+    classify_with_dmax(j->m, j->T, j->seqs, j->offsets, j->pep_ids, j->pep_counts, j->P, cand, nc,
+                       j->rads + (long)r * j->D, j->dist_cutoff, j->dmax, &id, &score, &tot);
+    free(cand);
+    score *= sub;
+    if (isnan(score / tot)) {
+        score = 0.0;
+        tot = 1.0;
+    }
+    j->hy_id[r] = id;
+    j->hy_score[r] = score;
+    j->hy_total[r] = tot;
+}
 
 static void nn_one(const nn_job* j, int r, nn_cand* cand, double* acc, nn_score* sc) {
     const double* q = j->rads + (long)r * j->D;
@@ -1461,11 +1516,51 @@ static void* nn_worker(void* arg) {
         pthread_mutex_unlock(&j->lock);
         if (r >= j->R) break;
         nn_one(j, r, cand, acc, sc);
+        if (j->seqs) hybrid_one(j, r);
     }
     free(cand);
     free(acc);
     free(sc);
     return NULL;
+}
+
+static void nn_run_job(nn_job* j, const wpo_model* m, int T, const int16_t* track_counts, int N,
+                       const int32_t* src_off, const int32_t* src_id, const int32_t* src_count,
+                       const int32_t* src_hits, const double* rads, int R, int k, double sig, int h,
+                       int threads) {
+    if (threads < 1) threads = 1;
+    int C = m->num_channels;
+    j->D = T * C;
+    j->N = N;
+    double* coords = (double*)malloc(sizeof(double) * ((long)N * j->D + 1));
+    wpo_nn_coords(m, T, track_counts, N, coords);
+    j->coords = coords;
+    j->src_off = src_off;
+    j->src_id = src_id;
+    j->src_count = src_count;
+    j->src_hits = src_hits;
+    long ns = N > 0 ? src_off[N] : 0;
+    int32_t* uniq = (int32_t*)malloc(sizeof(int32_t) * (ns > 0 ? ns : 1));
+    memcpy(uniq, src_id, sizeof(int32_t) * ns);
+    qsort(uniq, ns, sizeof(int32_t), int_cmp);
+    int U = 0;
+    for (long i = 0; i < ns; i++)
+        if (U == 0 || uniq[U - 1] != uniq[i]) uniq[U++] = uniq[i];
+    j->uniq = uniq;
+    j->U = U;
+    j->rads = rads;
+    j->R = R;
+    j->k = k;
+    j->h = h;
+    j->two_sig_sq = 2.0 * sig * sig;
+    pthread_mutex_init(&j->lock, NULL);
+    pthread_t* th = (pthread_t*)calloc(threads, sizeof(pthread_t));
+    for (int i = 0; i < threads; i++) pthread_create(&th[i], NULL, nn_worker, j);
+    for (int i = 0; i < threads; i++) pthread_join(th[i], NULL);
+    pthread_mutex_destroy(&j->lock);
+    free(th);
+    free(coords);
+    free(uniq);
 }
 
 void wpo_nn_classify_batch(const wpo_model* m, int T, const int16_t* track_counts, int N,
@@ -1474,43 +1569,45 @@ void wpo_nn_classify_batch(const wpo_model* m, int T, const int16_t* track_count
                            const double* rads, int R, int k, double sig, int h,
                            int threads, int32_t* out_ncand, int32_t* out_cand_id,
                            double* out_cand_score, double* out_total) {
-    if (threads < 1) threads = 1;
-    int C = m->num_channels;
     nn_job j;
     memset(&j, 0, sizeof(j));
-    j.D = T * C;
-    j.N = N;
-    double* coords = (double*)malloc(sizeof(double) * ((long)N * j.D + 1));
-    wpo_nn_coords(m, T, track_counts, N, coords);
-    j.coords = coords;
-    j.src_off = src_off;
-    j.src_id = src_id;
-    j.src_count = src_count;
-    j.src_hits = src_hits;
-    long ns = N > 0 ? src_off[N] : 0;
-    int32_t* uniq = (int32_t*)malloc(sizeof(int32_t) * (ns > 0 ? ns : 1));
-    memcpy(uniq, src_id, sizeof(int32_t) * ns);
-    qsort(uniq, ns, sizeof(int32_t), int_cmp);
-    int U = 0;
-    for (long i = 0; i < ns; i++)
-        if (U == 0 || uniq[U - 1] != uniq[i]) uniq[U++] = uniq[i];
-    j.uniq = uniq;
-    j.U = U;
-    j.rads = rads;
-    j.R = R;
-    j.k = k;
-    j.h = h;
-    j.two_sig_sq = 2.0 * sig * sig;
     j.out_ncand = out_ncand;
     j.out_cand_id = out_cand_id;
     j.out_cand_score = out_cand_score;
     j.out_total = out_total;
-    pthread_mutex_init(&j.lock, NULL);
-    pthread_t* th = (pthread_t*)calloc(threads, sizeof(pthread_t));
-    for (int i = 0; i < threads; i++) pthread_create(&th[i], NULL, nn_worker, &j);
-    for (int i = 0; i < threads; i++) pthread_join(th[i], NULL);
-    pthread_mutex_destroy(&j.lock);
-    free(th);
-    free(coords);
-    free(uniq);
+    nn_run_job(&j, m, T, track_counts, N, src_off, src_id, src_count, src_hits, rads, R, k, sig, h,
+               threads);
+}
+
+void wpo_hybrid_classify_batch(const wpo_model* m, int T, const int16_t* track_counts, int N,
+                               const int32_t* src_off, const int32_t* src_id,
+                               const int32_t* src_count, const int32_t* src_hits,
+                               const int16_t* seqs, const int32_t* offsets, const int32_t* ids,
+                               const int32_t* counts, int P, const double* rads, int R, int k,
+                               double sig, int h, double dist_cutoff, int threads,
+                               int32_t* out_id, double* out_score, double* out_total) {
+    nn_job j;
+    memset(&j, 0, sizeof(j));
+    j.out_ncand = (int32_t*)malloc(sizeof(int32_t) * (R > 0 ? R : 1));
+    j.out_cand_id = (int32_t*)malloc(sizeof(int32_t) * ((long)R * h + 1));
+    j.out_cand_score = (double*)malloc(sizeof(double) * ((long)R * h + 1));
+    j.out_total = (double*)malloc(sizeof(double) * (R > 0 ? R : 1));
+    j.m = m;
+    j.T = T;
+    j.seqs = seqs;
+    j.offsets = offsets;
+    j.pep_ids = ids;
+    j.pep_counts = counts;
+    j.P = P;
+    j.dmax = max_num_dyes_of(m->num_channels, seqs, offsets, P, T);
+    j.dist_cutoff = dist_cutoff;
+    j.hy_id = out_id;
+    j.hy_score = out_score;
+    j.hy_total = out_total;
+    nn_run_job(&j, m, T, track_counts, N, src_off, src_id, src_count, src_hits, rads, R, k, sig, h,
+               threads);
+    free(j.out_ncand);
+    free(j.out_cand_id);
+    free(j.out_cand_score);
+    free(j.out_total);
 }

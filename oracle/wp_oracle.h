@@ -158,6 +158,17 @@ void wpo_nn_classify_batch(const wpo_model* m, int T, const int16_t* track_count
                            int threads, int32_t* out_ncand, int32_t* out_cand_id,
                            double* out_cand_score, double* out_total);
 
+/* HybridClassifier::classify (hybrid-classifier.cc:55-94) for R reads:
+ * the kNN stage above, then the HMM over the candidates (peptides ragged as
+ * in wpo_classify_batch). */
+void wpo_hybrid_classify_batch(const wpo_model* m, int T, const int16_t* track_counts, int N,
+                               const int32_t* src_off, const int32_t* src_id,
+                               const int32_t* src_count, const int32_t* src_hits,
+                               const int16_t* seqs, const int32_t* offsets, const int32_t* ids,
+                               const int32_t* counts, int P, const double* rads, int R, int k,
+                               double sig, int h, double dist_cutoff, int threads,
+                               int32_t* out_id, double* out_score, double* out_total);
+
 #ifdef __cplusplus
 }
 #endif

@@ -119,6 +119,10 @@ class Oracle:
         L.wpo_nn_classify_batch.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int] + [ctypes.c_void_p, ctypes.c_int] \
             + [ctypes.c_void_p] * 5 + [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int] \
             + [ctypes.c_void_p] * 4
+        L.wpo_hybrid_classify_batch.restype = None
+        L.wpo_hybrid_classify_batch.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p, ctypes.c_int] \
+            + [ctypes.c_void_p] * 8 + [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_int, ctypes.c_double, ctypes.c_int] + [ctypes.c_void_p] * 3
         L.wpo_improve_fit_batch.restype = None
         L.wpo_improve_fit_batch.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p,
                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
@@ -200,6 +204,24 @@ class Oracle:
                                        _p(dts.src_count), _p(dts.src_hits), _p(rads), R, k, sig, h, threads,
                                        _p(nc), _p(ids), _p(sc), _p(tot))
         return nc, ids, sc, tot
+
+    def hybrid_classify(self, sm, T, dts, dye_seqs, rads, k, sig, h, cutoff, threads=8):
+        """Hybrid per read: (ids, scores, totals)."""
+        m = to_wpo(sm)
+        R = rads.shape[0]
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        tr = np.ascontiguousarray(dts.tracks, dtype=np.int16)
+        flat, off = dye_seqs.ragged()
+        pid = np.ascontiguousarray(dye_seqs.ids, dtype=np.int32)
+        pc = np.ascontiguousarray(dye_seqs.counts, dtype=np.int32)
+        oid = np.zeros(R, np.int32)
+        osc = np.zeros(R, np.float64)
+        otot = np.zeros(R, np.float64)
+        self.lib.wpo_hybrid_classify_batch(ctypes.byref(m), T, _p(tr), len(dts), _p(dts.src_off),
+                                           _p(dts.src_id), _p(dts.src_count), _p(dts.src_hits), _p(flat),
+                                           _p(off), _p(pid), _p(pc), len(dye_seqs), _p(rads), R, k, sig, h,
+                                           cutoff, threads, _p(oid), _p(osc), _p(otot))
+        return oid, osc, otot
 
     def improve_fit_batch(self, sm, T, seq, rads, threads=8, cutoff=DBL_MAX):
         """E-step over many reads on host threads: (WpoFitSums, log P [R])."""

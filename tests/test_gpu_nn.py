@@ -74,6 +74,27 @@ def test_nn_vs_oracle(gpu_ctx, oracle, case):
     _compare(g, o, f"kNN {case}")
 
 
+def test_hybrid_vs_oracle(gpu_ctx, oracle):
+    """Same k-hit semantics on both sides: top-1 ids equal where the kNN
+    candidate lists are equal (>= 98 % of reads), scores to 2e-5."""
+    sm, ds, dts, rads, _ = _data(3, 16, 60, 40, 100, seed=44)
+    k, sig, h, cut = 150, 0.5, 30, 5.0
+    gpu_ctx.upload_model(sm, 16)
+    gpu_ctx.upload_peptides(ds)
+    gpu_ctx.upload_tracks(dts)
+    gnc, gid, gsc, gtot = gpu_ctx.nn_classify(rads, k, sig, h)
+    onc, oid, osc, otot = oracle.nn_classify(sm, 16, dts, rads, k, sig, h)
+    hid, hsc, htot = gpu_ctx.hybrid_classify(rads, k, sig, h, cut)
+    oh_id, oh_sc, oh_tot = oracle.hybrid_classify(sm, 16, dts, ds, rads, k, sig, h, cut)
+    same = 0
+    for r in range(len(gnc)):
+        if gnc[r] == onc[r] and np.array_equal(gid[r, :gnc[r]], oid[r, :onc[r]]):
+            same += 1
+            assert hid[r] == oh_id[r], r
+            assert abs(hsc[r] / htot[r] - oh_sc[r] / oh_tot[r]) <= REL * abs(oh_sc[r] / oh_tot[r]) + 1e-300
+    assert same >= 0.98 * len(gnc)
+
+
 def test_nn_deterministic(gpu_ctx):
     sm, ds, dts, rads, _ = _data(3, 16, 60, 40, 100, seed=5)
     gpu_ctx.upload_model(sm, 16)

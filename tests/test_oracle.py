@@ -126,3 +126,36 @@ def test_improve_fit_matches_reference_live(oracle, reference):
             x = np.concatenate([np.ravel(v) for v in a[k]])
             y = np.concatenate([np.ravel(v) for v in b[k]])
             np.testing.assert_allclose(x, y, rtol=1e-12, atol=1e-300)
+
+
+@pytest.mark.parametrize("name", ["nn_c2_t8.npz", "nn_c3_t16.npz"])
+def test_nn_oracle_vs_reference_fixture(oracle, name):
+    """The oracle's kNN keeps the order-independent k-hit set; the
+    reference's kd-tree search can keep a few more far tracks.  Decisions
+    agree: best kNN id and hybrid top-1 for >= 95 % of reads; where the
+    reference's candidates and total equal the oracle's, kNN scores agree to
+    1e-9 of the total and hybrid adjusted scores to 1e-9."""
+    from whatprot_gb300.io import DyeTrackSet
+    z, ds = load_fixture(name)
+    dts = DyeTrackSet(z["tracks"], z["src_off"], z["src_id"], z["src_count"], z["src_hits"])
+    C, T = int(z["C"]), int(z["T"])
+    k, sig, h, cut = int(z["k"]), float(z["sig"]), int(z["h"]), float(z["cutoff"])
+    sm = paper_model(C)
+    rads = z["rads"]
+    nc, ids, sc, tot = oracle.nn_classify(sm, T, dts, rads, k, sig, h)
+    best = np.array([ids[r, nc[r] - 1] for r in range(len(nc))])
+    assert np.mean(best == z["nn_best_id"]) >= 0.95
+    hid, hsc, htot = oracle.hybrid_classify(sm, T, dts, ds, rads, k, sig, h, cut)
+    assert np.mean(hid == z["hy_id"]) >= 0.95
+    same = 0
+    for r in range(len(nc)):
+        if (nc[r] == z["nn_ncand"][r] and set(ids[r, :nc[r]]) == set(z["nn_ids"][r, :nc[r]])
+                and abs(tot[r] - z["nn_total"][r]) <= 1e-9 * z["nn_total"][r]):
+            same += 1
+            # a far track the reference also kept moves tiny scores only
+            np.testing.assert_allclose(np.sort(sc[r, :nc[r]]), np.sort(z["nn_scores"][r, :nc[r]]), rtol=1e-9,
+                                       atol=1e-9 * tot[r])
+            if hid[r] == z["hy_id"][r]:
+                assert abs(hsc[r] / htot[r] - z["hy_score"][r] / z["hy_total"][r]) <= \
+                    1e-9 * abs(z["hy_score"][r] / z["hy_total"][r])
+    assert same >= 0.3 * len(nc)

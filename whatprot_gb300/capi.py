@@ -31,7 +31,7 @@ EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload"
            "wp_hmm_loglik_all", "wp_hmm_count_flops", "wp_launch_count", "wp_ctx_stream",
            "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak", "wp_last_batch_stats",
            "wp_fit_begin", "wp_fit_estep", "wp_hmm_fit", "wp_fit_offset_exponential",
-           "wp_nn_tracks_upload", "wp_nn_classify", "wp_hybrid_classify"]
+           "wp_nn_tracks_upload", "wp_nn_classify", "wp_hybrid_classify", "wp_hybrid_classify_device"]
 
 
 class WpSeqModel(ctypes.Structure):
@@ -168,6 +168,8 @@ def load_library(path: Optional[str] = None):
     lib.wp_nn_classify.restype = I
     lib.wp_hybrid_classify.argtypes = [V, V, I, I, D, I, D, V, V, V]
     lib.wp_hybrid_classify.restype = I
+    lib.wp_hybrid_classify_device.argtypes = [V, V, I, I, D, I, D, V, V, V]
+    lib.wp_hybrid_classify_device.restype = I
     if path is None:
         _lib = lib
     return lib
@@ -369,6 +371,13 @@ class Context:
         self._check(self.lib.wp_hybrid_classify(self.h, _ptr(rads), R, k, sig, h, dist_cutoff, _ptr(ids),
                                                 _ptr(sc), _ptr(tot)))
         return ids, sc, tot
+
+    def hybrid_classify_device(self, d_rads_ptr: int, R: int, k: int, sig: float, h: int, dist_cutoff: float,
+                               d_id: int, d_score: int, d_total: int) -> None:
+        """wp_hybrid_classify_device on device pointers (e.g. torch tensors)."""
+        self._check(self.lib.wp_hybrid_classify_device(self.h, ctypes.c_void_p(d_rads_ptr), R, k, sig, h,
+                                                       dist_cutoff, ctypes.c_void_p(d_id), ctypes.c_void_p(d_score),
+                                                       ctypes.c_void_p(d_total)))
 
     def launch_count(self) -> int:
         return int(self.lib.wp_launch_count(self.h))

@@ -61,13 +61,24 @@ struct NNArgs {
     int* cand_idx;
     float* cand_d2;
     int* err;
+    int slices;
+    int slice_len;
+    unsigned* shist;
+    int R_all;
+    long long* sliceoff;
+    long long* slicecap;
+    long long* slicecnt;
 };
 struct NNSelectArgs {
     int R;
     int q0;
     const int* qbin;
     const int* qbelow;
-    const long long* qcnt;
+    int slices;
+    int R_all;
+    const long long* sliceoff;
+    const long long* slicecnt;
+    const long long* slicecap;
     const long long* qoff;
     const int* cand_idx;
     const float* cand_d2;
@@ -95,8 +106,12 @@ struct NNSelectArgs {
 };
 cudaError_t wp_launch_nn_dist(int DP, bool hist, cudaStream_t s, const NNArgs& a);
 cudaError_t wp_launch_nn_select(int grid, cudaStream_t s, const NNSelectArgs& a);
+cudaError_t wp_launch_nn_threshold(cudaStream_t s, const NNArgs& a);
+int wp_nn_bins();
 cudaError_t wp_launch_nn_queries(const double* rads, int R, int TC, int DP, float* out, cudaStream_t s);
 cudaError_t wp_launch_nn_ragged(const int* cand, int h, const int* off, int R, int* out, cudaStream_t s);
+cudaError_t wp_launch_hybrid_finish(const int* ncand, const double* subfrac, int R, int* id, double* score,
+                                    double* total, cudaStream_t s);
 int wp_nn_queries_per_block();
 int wp_nn_select_warps();
 int wp_nn_hmax();
@@ -191,7 +206,8 @@ struct wp_ctx {
     DevBuf d_nn_coords, d_nn_hits, d_nn_src_off, d_nn_src_dense, d_nn_src_ratio, d_nn_src_hits, d_nn_dense_id,
             d_nn_dense_pep, d_nn_dense_count, d_nn_queries, d_nn_qbin, d_nn_qbelow, d_nn_qcap, d_nn_qoff,
             d_nn_cidx, d_nn_cd2, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
-            d_nn_cand_score, d_nn_total, d_nn_subfrac, d_nn_cand_off, d_nn_cand_flat, d_nn_err;
+            d_nn_cand_score, d_nn_total, d_nn_subfrac, d_nn_cand_off, d_nn_cand_flat, d_nn_err, d_nn_shist,
+            d_nn_sliceoff, d_nn_slicecap, d_nn_slicecnt;
 
     // Per-batch scratch.
     DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_Lpk, d_Upk, d_allow, d_flags, d_table, d_res_mant, d_res_expo,
@@ -655,6 +671,27 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
     a.qbelow = ctx->d_nn_qbelow.as<int>();
     a.qcap = ctx->d_nn_qcap.as<long long>();
     a.err = ctx->d_nn_err.as<int>();
+    // Entry slices: enough CTAs (query blocks x slices) for two waves of
+    // three CTAs per SM, each slice at least 1024 entries.
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    {
+        const int qblocks = (R + wp_nn_queries_per_block() - 1) / wp_nn_queries_per_block();
+        int slices = (6 * sms + qblocks - 1) / qblocks;
+        slices = std::max(1, std::min(slices, std::min(32, (N + 1023) / 1024)));
+        a.slices = slices;
+        a.slice_len = ((N + slices - 1) / slices + 31) / 32 * 32;
+        a.slices = (N + a.slice_len - 1) / a.slice_len;
+    }
+    a.R_all = R;
+    WP_CUDA(ctx->d_nn_shist.ensure(sizeof(unsigned) * (size_t)a.slices * R * wp_nn_bins()), "alloc kNN histograms");
+    WP_CUDA(ctx->d_nn_sliceoff.ensure(sizeof(long long) * (size_t)a.slices * R), "alloc");
+    WP_CUDA(ctx->d_nn_slicecap.ensure(sizeof(long long) * (size_t)a.slices * R), "alloc");
+    WP_CUDA(ctx->d_nn_slicecnt.ensure(sizeof(long long) * (size_t)a.slices * R), "alloc");
+    a.shist = ctx->d_nn_shist.as<unsigned>();
+    a.sliceoff = ctx->d_nn_sliceoff.as<long long>();
+    a.slicecap = ctx->d_nn_slicecap.as<long long>();
+    a.slicecnt = ctx->d_nn_slicecnt.as<long long>();
     // pass 1 over every read
     a.queries = ctx->d_nn_queries.as<float>();
     a.R = R;
@@ -664,13 +701,13 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
         WP_CUDA(wp_launch_nn_dist(DP, true, ctx->stream, a), "kNN histogram");
         ctx->launches++;
     }
+    WP_CUDA(wp_launch_nn_threshold(ctx->stream, a), "kNN threshold");
+    ctx->launches++;
     std::vector<long long> cap(R);
     WP_CUDA(cudaMemcpyAsync(cap.data(), a.qcap, sizeof(long long) * R, cudaMemcpyDeviceToHost, ctx->stream),
             "copy caps");
     WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
     // per-warp accumulators of the select kernel
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     const int sel_grid = sms * 4;
     const long nwarps = (long)sel_grid * wp_nn_select_warps();
     const int U = std::max(ctx->nn_U, 1);
@@ -719,7 +756,11 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
         b.q0 = r0;
         b.qbin = a.qbin;
         b.qbelow = a.qbelow;
-        b.qcnt = a.qcap;
+        b.slices = a.slices;
+        b.R_all = R;
+        b.sliceoff = a.sliceoff;
+        b.slicecnt = a.slicecnt;
+        b.slicecap = a.slicecap;
         b.qoff = a.qoff;
         b.cand_idx = a.cand_idx;
         b.cand_d2 = a.cand_d2;
@@ -766,6 +807,41 @@ wp_status nn_check(wp_ctx* ctx, int k, double sig, int h) {
     if (k < 1) return fail(ctx, WP_ERR_INVALID, "k must be >= 1");
     if (!(sig > 0.0)) return fail(ctx, WP_ERR_INVALID, "sig must be > 0");
     if (h < 1 || h > wp_nn_hmax()) return fail(ctx, WP_ERR_UNSUPPORTED, "h must be in 1..1024");
+    return WP_OK;
+}
+
+wp_status hybrid_check(wp_ctx* ctx, int k, double sig, int h) {
+    wp_status st = nn_check(ctx, k, sig, h);
+    if (st != WP_OK) return st;
+    st = check_ready(ctx);
+    if (st != WP_OK) return st;
+    if (ctx->P == 0) return fail(ctx, WP_ERR_INVALID, "the hybrid classifier needs at least one peptide");
+    return WP_OK;
+}
+
+// HybridClassifier::classify (hybrid-classifier.cc:55-81) for reads on the
+// device: kNN candidates, the HMM over them (ascending kNN score), then the
+// score scaled by the candidates' subfraction and NaN patched on the device.
+wp_status hybrid_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, int h, double dist_cutoff,
+                     int* d_out_id, double* d_out_score, double* d_out_total) {
+    wp_status st = nn_run(ctx, d_rads, R, k, sig, h, true);
+    if (st != WP_OK) return st;
+    std::vector<int> ncand(R), off(R + 1, 0);
+    WP_CUDA(cudaMemcpyAsync(ncand.data(), ctx->d_nn_ncand.p, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    for (int r = 0; r < R; r++) off[r + 1] = off[r] + ncand[r];
+    WP_CUDA(ctx->d_nn_cand_off.ensure(sizeof(int) * (R + 1)), "alloc");
+    WP_CUDA(ctx->d_nn_cand_flat.ensure(sizeof(int) * std::max(off[R], 1)), "alloc");
+    WP_CUDA(cudaMemcpyAsync(ctx->d_nn_cand_off.p, off.data(), sizeof(int) * (R + 1), cudaMemcpyHostToDevice, ctx->stream), "copy");
+    WP_CUDA(wp_launch_nn_ragged(ctx->d_nn_cand_pep.as<int>(), h, ctx->d_nn_cand_off.as<int>(), R,
+                                ctx->d_nn_cand_flat.as<int>(), ctx->stream), "ragged");
+    ctx->launches++;
+    st = run_batch(ctx, d_rads, R, dist_cutoff, nullptr, off.data(), MODE_CLASSIFY, nullptr, d_out_id, d_out_score,
+                   d_out_total, nullptr, nullptr, ctx->d_nn_cand_flat.as<int>(), ctx->d_nn_cand_off.as<int>());
+    if (st != WP_OK) return st;
+    WP_CUDA(wp_launch_hybrid_finish(ctx->d_nn_ncand.as<int>(), ctx->d_nn_subfrac.as<double>(), R, d_out_id,
+                                    d_out_score, d_out_total, ctx->stream), "hybrid finish");
+    ctx->launches++;
     return WP_OK;
 }
 
@@ -1255,59 +1331,35 @@ wp_status wp_hybrid_classify(wp_ctx* ctx, const double* rads, int R, int k, doub
     if (!ctx || R < 0 || (R > 0 && (!rads || !out_id || !out_score || !out_total))) return WP_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
-    wp_status st = nn_check(ctx, k, sig, h);
+    wp_status st = hybrid_check(ctx, k, sig, h);
     if (st != WP_OK) return st;
-    st = check_ready(ctx);
-    if (st != WP_OK) return st;
-    if (ctx->P == 0) return fail(ctx, WP_ERR_INVALID, "the hybrid classifier needs at least one peptide");
     if (R == 0) return WP_OK;
     st = upload_reads(ctx, rads, R);
     if (st != WP_OK) return st;
-    st = nn_run(ctx, ctx->d_rads.as<double>(), R, k, sig, h, true);
-    if (st != WP_OK) return st;
-    // ragged candidate lists (ascending kNN score) for the HMM stage
-    std::vector<int> ncand(R), off(R + 1, 0);
-    std::vector<double> subfrac(R);
-    WP_CUDA(cudaMemcpyAsync(ncand.data(), ctx->d_nn_ncand.p, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
-    WP_CUDA(cudaMemcpyAsync(subfrac.data(), ctx->d_nn_subfrac.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
-    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
-    for (int r = 0; r < R; r++) off[r + 1] = off[r] + ncand[r];
-    WP_CUDA(ctx->d_nn_cand_off.ensure(sizeof(int) * (R + 1)), "alloc");
-    WP_CUDA(ctx->d_nn_cand_flat.ensure(sizeof(int) * std::max(off[R], 1)), "alloc");
-    WP_CUDA(cudaMemcpyAsync(ctx->d_nn_cand_off.p, off.data(), sizeof(int) * (R + 1), cudaMemcpyHostToDevice, ctx->stream), "copy");
-    WP_CUDA(wp_launch_nn_ragged(ctx->d_nn_cand_pep.as<int>(), h, ctx->d_nn_cand_off.as<int>(), R,
-                                ctx->d_nn_cand_flat.as<int>(), ctx->stream), "ragged");
-    ctx->launches++;
     WP_CUDA(ctx->d_out_id.ensure(sizeof(int) * R), "alloc outputs");
     WP_CUDA(ctx->d_out_score.ensure(sizeof(double) * R), "alloc outputs");
     WP_CUDA(ctx->d_out_total.ensure(sizeof(double) * R), "alloc outputs");
-    st = run_batch(ctx, ctx->d_rads.as<double>(), R, dist_cutoff, nullptr, off.data(), MODE_CLASSIFY, nullptr,
-                   ctx->d_out_id.as<int>(), ctx->d_out_score.as<double>(), ctx->d_out_total.as<double>(), nullptr,
-                   nullptr, ctx->d_nn_cand_flat.as<int>(), ctx->d_nn_cand_off.as<int>());
+    st = hybrid_run(ctx, ctx->d_rads.as<double>(), R, k, sig, h, dist_cutoff, ctx->d_out_id.as<int>(),
+                    ctx->d_out_score.as<double>(), ctx->d_out_total.as<double>());
     if (st != WP_OK) return st;
     WP_CUDA(cudaMemcpyAsync(out_id, ctx->d_out_id.p, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
     WP_CUDA(cudaMemcpyAsync(out_score, ctx->d_out_score.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
     WP_CUDA(cudaMemcpyAsync(out_total, ctx->d_out_total.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
-    st = finish(ctx);
+    return finish(ctx);
+}
+
+wp_status wp_hybrid_classify_device(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, int h,
+                                    double dist_cutoff, int32_t* d_out_id, double* d_out_score,
+                                    double* d_out_total) {
+    if (!ctx || R < 0 || (R > 0 && (!d_rads || !d_out_id || !d_out_score || !d_out_total))) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    wp_status st = hybrid_check(ctx, k, sig, h);
     if (st != WP_OK) return st;
-    // HybridClassifier::classify (hybrid-classifier.cc:55-81): the HMM's
-    // score scaled by the candidates' kNN subfraction, NaN patched.  With no
-    // candidate the reference indexes past its lists; here the read gets
-    // (-1, 0, 1).
-    for (int r = 0; r < R; r++) {
-        if (ncand[r] == 0) {
-            out_id[r] = -1;
-            out_score[r] = 0.0;
-            out_total[r] = 1.0;
-            continue;
-        }
-        out_score[r] *= subfrac[r];
-        if (std::isnan(out_score[r] / out_total[r])) {
-            out_score[r] = 0.0;
-            out_total[r] = 1.0;
-        }
-    }
-    return WP_OK;
+    if (R == 0) return WP_OK;
+    st = hybrid_run(ctx, d_rads, R, k, sig, h, dist_cutoff, d_out_id, d_out_score, d_out_total);
+    if (st != WP_OK) return st;
+    return finish(ctx);
 }
 
 wp_status wp_hmm_count_flops(wp_ctx* ctx, const double* rads, int R, double dist_cutoff, double* out_flops) {

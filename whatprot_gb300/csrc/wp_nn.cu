@@ -80,12 +80,20 @@ struct NNArgs {
     int* cand_idx;
     float* cand_d2;
     int* err;
+    // entry slices (blockIdx.y): slice s covers entries [s * slice_len, ...)
+    int slices;
+    int slice_len;
+    unsigned* shist;        // [slices][R_all][NB] per-slice histograms (pass 1)
+    int R_all;              // queries in the whole batch (stride of shist / sliceoff)
+    long long* sliceoff;    // [slices][R_all] offset of slice s inside query q's list
+    long long* slicecap;    // [slices][R_all] room for slice s (its hits in bins <= b*)
+    long long* slicecnt;    // [slices][R_all] candidates slice s wrote (collect)
 };
 
 // Load a tile of entries (coords and hits) into shared memory.
 template <int DP>
-__device__ __forceinline__ void nn_load_tile(const NNArgs& a, int e0, float* tile, int* thits) {
-    const int n = min(NN_TE, a.N - e0);
+__device__ __forceinline__ void nn_load_tile(const NNArgs& a, int e0, int e_end, float* tile, int* thits) {
+    const int n = min(NN_TE, e_end - e0);
     const float4* src = reinterpret_cast<const float4*>(a.coords + (long)e0 * DP);
     float4* dst = reinterpret_cast<float4*>(tile);
     for (int i = threadIdx.x; i < NN_TE * DP / 4; i += blockDim.x)
@@ -100,6 +108,8 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
     int* thits = reinterpret_cast<int*>(tile + NN_TE * DP);
     unsigned* hist = reinterpret_cast<unsigned*>(thits + NN_TE);  // [NN_QPB][NN_NB + 1]
     const int qb = blockIdx.x * NN_QPB;
+    const int s = blockIdx.y;
+    const int e_lo = s * a.slice_len, e_hi = min(a.N, e_lo + a.slice_len);
     for (int i = threadIdx.x; i < NN_QPB * (NN_NB + 1); i += blockDim.x) hist[i] = 0u;
     float q[NN_QPT][DP];
     bool valid[NN_QPT];
@@ -111,11 +121,11 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
 #pragma unroll
         for (int i = 0; i < DP; i++) q[j][i] = valid[j] ? src[i] : 0.f;
     }
-    for (int e0 = 0; e0 < a.N; e0 += NN_TE) {
+    for (int e0 = e_lo; e0 < e_hi; e0 += NN_TE) {
         __syncthreads();
-        nn_load_tile<DP>(a, e0, tile, thits);
+        nn_load_tile<DP>(a, e0, e_hi, tile, thits);
         __syncthreads();
-        const int n = min(NN_TE, a.N - e0);
+        const int n = min(NN_TE, e_hi - e0);
         for (int e = 0; e < n; e++) {
 #pragma unroll
             for (int j = 0; j < NN_QPT; j++) {
@@ -126,32 +136,52 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
         }
     }
     __syncthreads();
-#pragma unroll
-    for (int j = 0; j < NN_QPT; j++) {
-        if (!valid[j]) continue;
-        const int lq = threadIdx.x + j * NN_THREADS;
-        const unsigned* h = hist + lq * (NN_NB + 1);
-        long long cum = 0, below = 0, cap = 0;
-        int b = NN_NB - 1;
-        bool found = false;
-        for (int i = 0; i < NN_NB; i++) {
-            if (!found && cum + h[i] >= a.k) {
-                found = true;
-                b = i;
-                below = cum;
-                cap = cum + h[i];
-            }
-            cum += h[i];
+    // this slice's histograms, query-major within the slice
+    for (int i = threadIdx.x; i < NN_QPB * NN_NB; i += blockDim.x) {
+        const int lq = i / NN_NB, b = i % NN_NB;
+        if (qb + lq < a.R)
+            a.shist[((long)s * a.R_all + a.q0 + qb + lq) * NN_NB + b] = hist[lq * (NN_NB + 1) + b];
+    }
+}
+
+// Per query: the slices' histograms summed, the bin b* where the running
+// hits reach k, hits below it, the candidate bound, and each slice's share
+// (offsets of the slices inside the query's list).
+__global__ void wp_nn_threshold_kernel(NNArgs a) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= a.R) return;
+    const int gq = a.q0 + q;
+    long long cum = 0, below = 0, cap = 0;
+    int b = NN_NB - 1;
+    bool found = false;
+    for (int i = 0; i < NN_NB; i++) {
+        long long hi = 0;
+        for (int s = 0; s < a.slices; s++) hi += a.shist[((long)s * a.R_all + gq) * NN_NB + i];
+        if (!found && cum + hi >= a.k) {
+            found = true;
+            b = i;
+            below = cum;
+            cap = cum + hi;
         }
-        if (!found) {  // all hits stay below k: every entry is kept
-            b = NN_NB - 1;
-            below = cum - h[NN_NB - 1];
-            cap = cum;
-        }
-        const int gq = a.q0 + qb + lq;
-        a.qbin[gq] = b;
-        a.qbelow[gq] = (int)below;
-        a.qcap[gq] = cap;
+        cum += hi;
+    }
+    if (!found) {  // all hits stay below k: every entry is kept
+        long long hl = 0;
+        for (int s = 0; s < a.slices; s++) hl += a.shist[((long)s * a.R_all + gq) * NN_NB + NN_NB - 1];
+        b = NN_NB - 1;
+        below = cum - hl;
+        cap = cum;
+    }
+    a.qbin[gq] = b;
+    a.qbelow[gq] = (int)below;
+    a.qcap[gq] = cap;
+    long long off = 0;
+    for (int s = 0; s < a.slices; s++) {
+        long long c = 0;
+        for (int i = 0; i <= b; i++) c += a.shist[((long)s * a.R_all + gq) * NN_NB + i];
+        a.sliceoff[(long)s * a.R_all + gq] = off;
+        a.slicecap[(long)s * a.R_all + gq] = c;
+        off += c;
     }
 }
 
@@ -161,6 +191,8 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
     float* tile = reinterpret_cast<float*>(nn_smem);
     int* thits = reinterpret_cast<int*>(tile + NN_TE * DP);
     const int qb = blockIdx.x * NN_QPB;
+    const int s = blockIdx.y;
+    const int e_lo = s * a.slice_len, e_hi = min(a.N, e_lo + a.slice_len);
     float q[NN_QPT][DP];
     bool valid[NN_QPT];
     int bstar[NN_QPT];
@@ -170,19 +202,20 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
         const int lq = threadIdx.x + j * NN_THREADS;
         valid[j] = qb + lq < a.R;
         const int l = valid[j] ? qb + lq : 0;
+        const int gq = a.q0 + l;
         const float* src = a.queries + (long)l * DP;
 #pragma unroll
         for (int i = 0; i < DP; i++) q[j][i] = valid[j] ? src[i] : 0.f;
-        bstar[j] = valid[j] ? a.qbin[a.q0 + l] : -1;
-        off[j] = valid[j] ? a.qoff[l] : 0;
-        cap[j] = valid[j] ? a.qcap[a.q0 + l] : 0;
+        bstar[j] = valid[j] ? a.qbin[gq] : -1;
+        off[j] = valid[j] ? a.qoff[l] + a.sliceoff[(long)s * a.R_all + gq] : 0;
+        cap[j] = valid[j] ? a.slicecap[(long)s * a.R_all + gq] : 0;
         cnt[j] = 0;
     }
-    for (int e0 = 0; e0 < a.N; e0 += NN_TE) {
+    for (int e0 = e_lo; e0 < e_hi; e0 += NN_TE) {
         __syncthreads();
-        nn_load_tile<DP>(a, e0, tile, thits);
+        nn_load_tile<DP>(a, e0, e_hi, tile, thits);
         __syncthreads();
-        const int n = min(NN_TE, a.N - e0);
+        const int n = min(NN_TE, e_hi - e0);
         for (int e = 0; e < n; e++) {
 #pragma unroll
             for (int j = 0; j < NN_QPT; j++) {
@@ -200,8 +233,11 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
         }
     }
 #pragma unroll
-    for (int j = 0; j < NN_QPT; j++)
-        if (valid[j]) a.qcap[a.q0 + qb + threadIdx.x + j * NN_THREADS] = cnt[j];  // now: entries collected
+    for (int j = 0; j < NN_QPT; j++) {
+        if (!valid[j]) continue;
+        a.slicecnt[(long)s * a.R_all + a.q0 + qb + threadIdx.x + j * NN_THREADS] = cnt[j];
+        if (cnt[j] > cap[j]) atomicExch(a.err, 1);
+    }
 }
 
 struct NNSelectArgs {
@@ -209,7 +245,11 @@ struct NNSelectArgs {
     int q0;
     const int* qbin;
     const int* qbelow;
-    const long long* qcnt;      // candidates per query (after collect)
+    int slices;
+    int R_all;
+    const long long* sliceoff;  // [slices][R_all]
+    const long long* slicecnt;  // [slices][R_all]
+    const long long* slicecap;  // [slices][R_all] (bounds slicecnt)
     const long long* qoff;
     const int* cand_idx;
     const float* cand_d2;
@@ -268,10 +308,9 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
     for (long lq = gw; lq < a.R; lq += nw) {
         const int gq = a.q0 + (int)lq;
         const int bstar = a.qbin[gq];
-        const long long m = a.qcnt[gq];
-        const int* cidx = a.cand_idx + a.qoff[lq];
-        const float* cd2 = a.cand_d2 + a.qoff[lq];
         long long need = a.k - a.qbelow[gq];  // hits still needed from bin b*
+        // The query's candidates: one segment per entry slice, in slice
+        // order (so in ascending entry index overall).
 
         // ---- hits-weighted radix select over the float bits of d2 in bin b*.
         unsigned prefix = 0u, pmask = 0u;
@@ -280,11 +319,15 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
             const int shift = 24 - 8 * pass;
             for (int i = lane; i < 256; i += 32) hist[i] = 0ull;
             __syncwarp();
-            for (long long i = lane; i < m; i += 32) {
-                const float d2 = cd2[i];
-                const unsigned key = __float_as_uint(d2);
-                if (nn_bin(d2) == bstar && (key & pmask) == prefix)
-                    atomicAdd(&hist[(key >> shift) & 255u], (unsigned long long)a.hits[cidx[i]]);
+            for (int sl = 0; sl < a.slices; sl++) {
+                const long long sb = a.qoff[lq] + a.sliceoff[(long)sl * a.R_all + gq];
+                const long long sn = min(a.slicecnt[(long)sl * a.R_all + gq], a.slicecap[(long)sl * a.R_all + gq]);
+                for (long long i = lane; i < sn; i += 32) {
+                    const float d2 = a.cand_d2[sb + i];
+                    const unsigned key = __float_as_uint(d2);
+                    if (nn_bin(d2) == bstar && (key & pmask) == prefix)
+                        atomicAdd(&hist[(key >> shift) & 255u], (unsigned long long)a.hits[a.cand_idx[sb + i]]);
+                }
             }
             __syncwarp();
             // find the digit where the running hits reach `need`
@@ -327,15 +370,18 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
         double total_part = 0.0;
         int ntouched = 0;
         long long tie_cum = 0;  // hits of key == kstar entries seen so far
-        for (long long base = 0; base < m; base += 32) {
+        for (int sl = 0; sl < a.slices; sl++) {
+          const long long sb = a.qoff[lq] + a.sliceoff[(long)sl * a.R_all + gq];
+          const long long sn = min(a.slicecnt[(long)sl * a.R_all + gq], a.slicecap[(long)sl * a.R_all + gq]);
+          for (long long base = 0; base < sn; base += 32) {
             const long long i = base + lane;
             bool keep = false;
             int e = -1;
             float d2 = 0.f;
             bool tie = false;
-            if (i < m) {
-                e = cidx[i];
-                d2 = cd2[i];
+            if (i < sn) {
+                e = a.cand_idx[sb + i];
+                d2 = a.cand_d2[sb + i];
                 const int b = nn_bin(d2);
                 const unsigned key = __float_as_uint(d2);
                 if (b < bstar || take_all) keep = true;
@@ -392,6 +438,7 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
                 ntouched += __popc(fm);
                 __syncwarp();
             }
+          }
         }
         // total, summed in a fixed tree order and broadcast from lane 0
         double tot = total_part;
@@ -560,18 +607,49 @@ __global__ void wp_nn_ragged_kernel(const int* __restrict__ cand, int h, const i
     for (int i = threadIdx.x; i < n; i += blockDim.x) out[off[r] + i] = cand[(long)r * h + i];
 }
 
+// HybridClassifier::classify's last steps (hybrid-classifier.cc:66-79): the
+// HMM score times the subfraction, NaN patched; no candidate: (-1, 0, 1).
+__global__ void wp_hybrid_finish_kernel(const int* __restrict__ ncand, const double* __restrict__ subfrac, int R,
+                                        int* __restrict__ id, double* __restrict__ score,
+                                        double* __restrict__ total) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    if (ncand[r] == 0) {
+        id[r] = -1;
+        score[r] = 0.0;
+        total[r] = 1.0;
+        return;
+    }
+    const double s = score[r] * subfrac[r];
+    if (isnan(s / total[r])) {
+        score[r] = 0.0;
+        total[r] = 1.0;
+    } else {
+        score[r] = s;
+    }
+}
+
+cudaError_t wp_launch_hybrid_finish(const int* ncand, const double* subfrac, int R, int* id, double* score,
+                                    double* total, cudaStream_t s) {
+    if (R == 0) return cudaSuccess;
+    wp_hybrid_finish_kernel<<<(R + 255) / 256, 256, 0, s>>>(ncand, subfrac, R, id, score, total);
+    return cudaGetLastError();
+}
+
 size_t wp_nn_dist_smem_bytes(int DP, bool with_hist) {
     size_t b = sizeof(float) * NN_TE * DP + sizeof(int) * NN_TE;
     if (with_hist) b += sizeof(unsigned) * NN_QPB * (NN_NB + 1);
     return b;
 }
 
+int wp_nn_bins() { return NN_NB; }
+
 int wp_nn_queries_per_block() { return NN_QPB; }
 int wp_nn_select_warps() { return NN_SEL_WARPS; }
 int wp_nn_hmax() { return NN_HMAX; }
 
 template <int DP>
-static cudaError_t launch_dist(bool hist, int grid, cudaStream_t s, const NNArgs& a) {
+static cudaError_t launch_dist(bool hist, dim3 grid, cudaStream_t s, const NNArgs& a) {
     const size_t smem = wp_nn_dist_smem_bytes(DP, hist);
     if (hist) {
         cudaFuncSetAttribute(wp_nn_hist_kernel<DP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -583,10 +661,12 @@ static cudaError_t launch_dist(bool hist, int grid, cudaStream_t s, const NNArgs
     return cudaGetLastError();
 }
 
-// DP: padded dimension, one of 16, 32, 48, 64.
+// DP: padded dimension, one of 16, 32, 48, 64.  Grid: query blocks x the
+// args' entry slices.
 cudaError_t wp_launch_nn_dist(int DP, bool hist, cudaStream_t s, const NNArgs& a) {
-    const int grid = (a.R + NN_QPB - 1) / NN_QPB;
-    if (grid == 0) return cudaSuccess;
+    const int qblocks = (a.R + NN_QPB - 1) / NN_QPB;
+    if (qblocks == 0) return cudaSuccess;
+    const dim3 grid(qblocks, a.slices);
     switch (DP) {
         case 16: return launch_dist<16>(hist, grid, s, a);
         case 32: return launch_dist<32>(hist, grid, s, a);
@@ -594,6 +674,12 @@ cudaError_t wp_launch_nn_dist(int DP, bool hist, cudaStream_t s, const NNArgs& a
         case 64: return launch_dist<64>(hist, grid, s, a);
         default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t wp_launch_nn_threshold(cudaStream_t s, const NNArgs& a) {
+    if (a.R == 0) return cudaSuccess;
+    wp_nn_threshold_kernel<<<(a.R + 127) / 128, 128, 0, s>>>(a);
+    return cudaGetLastError();
 }
 
 cudaError_t wp_launch_nn_select(int grid, cudaStream_t s, const NNSelectArgs& a) {

@@ -168,8 +168,14 @@ def simulate_dye_track_set(model: SequencingModel, dye_seqs: DyeSeqSet, num_time
     keep = np.any(tracks[:, 0, :] != 0, axis=1)
     tracks = tracks[keep]
     pep = reps[keep]
-    flat = tracks.reshape(len(tracks), -1)
-    uniq, inv = np.unique(flat, axis=0, return_inverse=True)
+    flat = np.ascontiguousarray(tracks.reshape(len(tracks), -1))
+    # rows as opaque byte strings: np.unique on them is much faster than
+    # axis=0; big-endian int16 bytes sort in the same order as the counts
+    # (all counts are non-negative)
+    be = flat.astype(">i2")
+    rows = be.view(np.dtype((np.void, be.dtype.itemsize * be.shape[1]))).reshape(-1)
+    _, first, inv = np.unique(rows, return_index=True, return_inverse=True)
+    uniq = flat[first]
     inv = inv.reshape(-1)
     # hits per (unique track, peptide)
     key = inv.astype(np.int64) * (len(dye_seqs) + 1) + pep
