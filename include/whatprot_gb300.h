@@ -259,6 +259,17 @@ wp_status wp_hybrid_classify_device(wp_ctx* ctx, const double* d_rads,
                                     double dist_cutoff, int32_t* d_out_id,
                                     double* d_out_score, double* d_out_total);
 
+/* BF16 tensor-core GEMM (tcgen05, TMEM accumulator), the building block of
+ * the learned proposal network, exposed for tests: C = act(A . B^T + bias)
+ * on device pointers, A [M][K] (pitch lda), B [N][K] (pitch ldb) BF16
+ * row-major, K a multiple of 64, pitches multiples of 8; C [M][ldc] FP32
+ * (c_fp32) or BF16; bias [N] FP32 or NULL; act 0 none, 1 GELU; Z (BF16
+ * pre-activation) or NULL.  Synchronous on the default stream.  No reference
+ * counterpart (the reference has no network). */
+wp_status wp_dev_gemm_bf16(const void* A, int lda, const void* B, int ldb,
+                           int M, int N, int K, void* C, int ldc, int c_fp32,
+                           const float* bias, int act, void* Z);
+
 /* Kernel launches issued by this context since creation (all kinds). */
 long long wp_launch_count(const wp_ctx* ctx);
 

@@ -31,7 +31,8 @@ EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload"
            "wp_hmm_loglik_all", "wp_hmm_count_flops", "wp_launch_count", "wp_ctx_stream",
            "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak", "wp_last_batch_stats",
            "wp_fit_begin", "wp_fit_estep", "wp_hmm_fit", "wp_fit_offset_exponential",
-           "wp_nn_tracks_upload", "wp_nn_classify", "wp_hybrid_classify", "wp_hybrid_classify_device"]
+           "wp_nn_tracks_upload", "wp_nn_classify", "wp_hybrid_classify", "wp_hybrid_classify_device",
+           "wp_dev_gemm_bf16"]
 
 
 class WpSeqModel(ctypes.Structure):
@@ -170,6 +171,8 @@ def load_library(path: Optional[str] = None):
     lib.wp_hybrid_classify.restype = I
     lib.wp_hybrid_classify_device.argtypes = [V, V, I, I, D, I, D, V, V, V]
     lib.wp_hybrid_classify_device.restype = I
+    lib.wp_dev_gemm_bf16.argtypes = [V, I, V, I, I, I, I, V, I, I, V, I, V]
+    lib.wp_dev_gemm_bf16.restype = I
     if path is None:
         _lib = lib
     return lib
@@ -192,6 +195,22 @@ def seq_model_struct(sm: SequencingModel):
                    sm.p_initial_detach_decay, sm.p_initial_block, sm.p_cyclic_block,
                    *[k.ctypes.data for k in keep])
     return m, keep
+
+
+def gemm_bf16(A, B, bias=None, act=0, out_fp32=True, want_z=False):
+    """wp_dev_gemm_bf16 on torch CUDA tensors: act(A @ B.T + bias)."""
+    import torch
+    lib = load_library()
+    M, K = A.shape
+    N = B.shape[0]
+    C = torch.empty(M, N, device=A.device, dtype=torch.float32 if out_fp32 else torch.bfloat16)
+    Z = torch.empty(M, N, device=A.device, dtype=torch.bfloat16) if want_z else None
+    st = lib.wp_dev_gemm_bf16(A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(0), M, N, K, C.data_ptr(), N,
+                              1 if out_fp32 else 0, bias.data_ptr() if bias is not None else None, act,
+                              Z.data_ptr() if Z is not None else None)
+    if st != 0:
+        raise WpError(st, "wp_dev_gemm_bf16")
+    return (C, Z) if want_z else C
 
 
 def fit_offset_exponential(y, w, params, held=(False, False, False)):

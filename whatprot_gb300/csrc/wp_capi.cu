@@ -108,6 +108,9 @@ cudaError_t wp_launch_nn_dist(int DP, bool hist, cudaStream_t s, const NNArgs& a
 cudaError_t wp_launch_nn_select(int grid, cudaStream_t s, const NNSelectArgs& a);
 cudaError_t wp_launch_nn_threshold(cudaStream_t s, const NNArgs& a);
 int wp_nn_bins();
+cudaError_t wp_gemm_bf16_tn(const void* A, int lda, const void* B, int ldb, int M, int N, int K, void* C, int ldc,
+                            int c_fp32, const float* bias, int act, void* Z, int accumulate, int* err,
+                            cudaStream_t s);
 cudaError_t wp_launch_nn_queries(const double* rads, int R, int TC, int DP, float* out, cudaStream_t s);
 cudaError_t wp_launch_nn_ragged(const int* cand, int h, const int* off, int R, int* out, cudaStream_t s);
 cudaError_t wp_launch_hybrid_finish(const int* ncand, const double* subfrac, int R, int* id, double* score,
@@ -1360,6 +1363,24 @@ wp_status wp_hybrid_classify_device(wp_ctx* ctx, const double* d_rads, int R, in
     st = hybrid_run(ctx, d_rads, R, k, sig, h, dist_cutoff, d_out_id, d_out_score, d_out_total);
     if (st != WP_OK) return st;
     return finish(ctx);
+}
+
+wp_status wp_dev_gemm_bf16(const void* A, int lda, const void* B, int ldb, int M, int N, int K, void* C, int ldc,
+                           int c_fp32, const float* bias, int act, void* Z) {
+    int* d_err = nullptr;
+    if (cudaMalloc(&d_err, sizeof(int)) != cudaSuccess) return WP_ERR_OOM;
+    cudaMemset(d_err, 0, sizeof(int));
+    cudaError_t e = wp_gemm_bf16_tn(A, lda, B, ldb, M, N, K, C, ldc, c_fp32, bias, act, Z, 0, d_err, 0);
+    if (e == cudaErrorInvalidValue) {
+        cudaFree(d_err);
+        return WP_ERR_INVALID;
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    int err = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d_err);
+    if (e != cudaSuccess) return WP_ERR_CUDA;
+    return err ? WP_ERR_TIMEOUT : WP_OK;
 }
 
 wp_status wp_hmm_count_flops(wp_ctx* ctx, const double* rads, int R, double dist_cutoff, double* out_flops) {
