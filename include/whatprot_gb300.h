@@ -259,6 +259,19 @@ wp_status wp_hybrid_classify_device(wp_ctx* ctx, const double* d_rads,
                                     double dist_cutoff, int32_t* d_out_id,
                                     double* d_out_score, double* d_out_total);
 
+/* Simulate reads on the device (simulation/generate-dye-track.cc:29-110,
+ * generate-radiometry.cc:28-62): num_reads reads of peptides drawn in
+ * proportion to their counts from the uploaded peptide set, with the
+ * context's model, counter-based Philox streams from `seed` (read r uses
+ * subsequence r).  out_rads [R][T][C] intensities (divided by mu),
+ * out_peptide[r] the peptide index, or -1 for a read whose first timestep
+ * shows no dye (the reference does not emit those), out_tracks [R][T][C]
+ * the live dye counts (may be NULL).  Dye-seqs longer than 256 positions are
+ * cut at 256. */
+wp_status wp_simulate_reads(wp_ctx* ctx, int num_reads, unsigned long long seed,
+                            double* out_rads, int32_t* out_peptide,
+                            uint8_t* out_tracks);
+
 /* BF16 tensor-core GEMM (tcgen05, TMEM accumulator), the building block of
  * the learned proposal network, exposed for tests: C = act(A . B^T + bias)
  * on device pointers, A [M][K] (pitch lda), B [N][K] (pitch ldb) BF16

@@ -31,6 +31,7 @@
 #include "parameterization/model/sequencing-model.h"
 #include "parameterization/settings/fit-settings.h"
 #include "parameterization/settings/sequencing-settings.h"
+#include "simulation/generate-dye-track.h"
 #include "util/levmar-helper.h"
 #include "wp_oracle.h"
 
@@ -361,6 +362,23 @@ void ref_offset_exponential(const double* y, const double* w, int n,
     for (int k = 0; k < 3; k++) hold[k] = held[k] != 0;
     least_squares_fit_of_offset_exponential(yv, wv, hold, &p);
     for (int k = 0; k < 3; k++) params[k] = p[k];
+}
+
+// generate_dye_track (simulation/generate-dye-track.cc:29-110) n times for
+// one dye-seq from std::default_random_engine(seed): counts [n][T][C].
+void ref_generate_dye_tracks(const wpo_model* m, int T, const char* dye_seq, int n, unsigned seed,
+                             int16_t* out) {
+    int C = m->num_channels;
+    SequencingModel sm;
+    to_reference(m, &sm);
+    DyeSeq ds(C, std::string(dye_seq));
+    std::default_random_engine gen(seed);
+    for (int i = 0; i < n; i++) {
+        DyeTrack dt(T, C);
+        generate_dye_track(sm, ds, T, C, &gen, &dt);
+        for (int t = 0; t < T; t++)
+            for (int c = 0; c < C; c++) out[((long)i * T + t) * C + c] = dt(t, c);
+    }
 }
 
 }  // extern "C"

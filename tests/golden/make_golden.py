@@ -124,10 +124,34 @@ def nn_fixture(name, C, T, P, lmin, lmax, per_peptide, nreads, k, sig, h, cutoff
           float(np.mean(hid == true_ids)), "nn best vs truth", float(np.mean(bid == true_ids)))
 
 
+def sim_fixture(name, seed):
+    """Statistics of the reference's generate_dye_track: per dye-seq the mean
+    live dye count per (t, c) and the fraction of undetectable tracks over
+    200,000 draws, for a model with blocks and initial detach."""
+    sm = paper_model(3)
+    sm.p_initial_block, sm.p_cyclic_block = 0.05, 0.02
+    sm.p_initial_detach, sm.p_initial_detach_decay = 0.04, 0.3
+    T = 12
+    seqs = ["0.1.2.0.1", ".00..1.22.0.1.2", "2..1..0"]
+    ref = Reference()
+    means, sq, trivial = [], [], []
+    n = 200000
+    for i, s in enumerate(seqs):
+        tr = ref.generate_dye_tracks(sm, T, s, n, seed + i).astype(np.float64)
+        means.append(tr.mean(axis=0))
+        sq.append((tr ** 2).mean(axis=0))
+        trivial.append(float(np.mean(np.all(tr[:, 0, :] == 0, axis=1))))
+    np.savez_compressed(os.path.join(HERE, name), T=T, seqs=np.array(seqs), n=n, mean=np.array(means),
+                        meansq=np.array(sq), trivial=np.array(trivial),
+                        model=np.array([sm.p_initial_block, sm.p_cyclic_block, sm.p_initial_detach,
+                                        sm.p_initial_detach_decay]))
+    print(name, "trivial fractions", trivial)
+
+
 if __name__ == "__main__":
     if not Reference.available():
         sys.exit("oracle/_ref/libwpref.so missing: run `make -C oracle ref` where the reference is present")
-    which = sys.argv[1:] or ["classify", "pairs", "fit", "nn"]
+    which = sys.argv[1:] or ["classify", "pairs", "fit", "nn", "sim"]
     if "classify" in which:
         classify_fixture("classify_c2_t8.npz", 2, 8, 100, 6, 12, 300, 5.0, seed=101)
         classify_fixture("classify_c3_t16.npz", 3, 16, 60, 8, 30, 60, 5.0, seed=202, maxc=5, mint=1)
@@ -140,3 +164,5 @@ if __name__ == "__main__":
     if "nn" in which:
         nn_fixture("nn_c2_t8.npz", 2, 8, 60, 6, 12, 100, 200, 300, 0.5, 20, 5.0, seed=707)
         nn_fixture("nn_c3_t16.npz", 3, 16, 80, 8, 24, 60, 120, 200, 0.5, 30, 5.0, seed=808)
+    if "sim" in which:
+        sim_fixture("sim_tracks_c3_t12.npz", seed=909)

@@ -286,6 +286,9 @@ class Reference:
                                        ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                        ctypes.c_double, ctypes.c_int, ctypes.c_double, ctypes.c_int] \
             + [ctypes.c_void_p] * 4
+        L.ref_generate_dye_tracks.restype = None
+        L.ref_generate_dye_tracks.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
+                                              ctypes.c_uint, ctypes.c_void_p]
         L.ref_fit.restype = ctypes.c_double
         L.ref_fit.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                               ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.POINTER(WpoModel),
@@ -369,6 +372,11 @@ class Reference:
         rads = np.ascontiguousarray(rads, dtype=np.float64)
         return self.lib.ref_improve_fit_batch(ctypes.byref(m), T, seq_str.encode(), rads.shape[0],
                                               _p(rads), threads)
+
+    def generate_dye_tracks(self, sm, T, seq_str, n, seed):
+        out = np.zeros((n, T, sm.num_channels), np.int16)
+        self.lib.ref_generate_dye_tracks(ctypes.byref(to_wpo(sm)), T, seq_str.encode(), n, seed, _p(out))
+        return out
 
     def offset_exponential(self, y, w, params, held=(0, 0, 0)):
         y = np.ascontiguousarray(y, dtype=np.float64)

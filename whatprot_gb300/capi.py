@@ -32,7 +32,7 @@ EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload"
            "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak", "wp_last_batch_stats",
            "wp_fit_begin", "wp_fit_estep", "wp_hmm_fit", "wp_fit_offset_exponential",
            "wp_nn_tracks_upload", "wp_nn_classify", "wp_hybrid_classify", "wp_hybrid_classify_device",
-           "wp_dev_gemm_bf16"]
+           "wp_dev_gemm_bf16", "wp_simulate_reads"]
 
 
 class WpSeqModel(ctypes.Structure):
@@ -171,6 +171,8 @@ def load_library(path: Optional[str] = None):
     lib.wp_hybrid_classify.restype = I
     lib.wp_hybrid_classify_device.argtypes = [V, V, I, I, D, I, D, V, V, V]
     lib.wp_hybrid_classify_device.restype = I
+    lib.wp_simulate_reads.argtypes = [V, I, ctypes.c_ulonglong, V, V, V]
+    lib.wp_simulate_reads.restype = I
     lib.wp_dev_gemm_bf16.argtypes = [V, I, V, I, I, I, I, V, I, I, V, I, V]
     lib.wp_dev_gemm_bf16.restype = I
     if path is None:
@@ -397,6 +399,16 @@ class Context:
         self._check(self.lib.wp_hybrid_classify_device(self.h, ctypes.c_void_p(d_rads_ptr), R, k, sig, h,
                                                        dist_cutoff, ctypes.c_void_p(d_id), ctypes.c_void_p(d_score),
                                                        ctypes.c_void_p(d_total)))
+
+    def simulate_reads(self, R: int, seed: int, tracks: bool = False):
+        """wp_simulate_reads: (rads [R,T,C], peptide index [R] (-1: not
+        detectable), tracks [R,T,C] uint8 or None)."""
+        T, C = self.num_timesteps, self.num_channels
+        rads = np.zeros((R, T, C), np.float64)
+        pep = np.zeros(R, np.int32)
+        trk = np.zeros((R, T, C), np.uint8) if tracks else None
+        self._check(self.lib.wp_simulate_reads(self.h, R, seed, _ptr(rads), _ptr(pep), _ptr(trk)))
+        return rads, pep, trk
 
     def launch_count(self) -> int:
         return int(self.lib.wp_launch_count(self.h))

@@ -46,68 +46,11 @@ cudaError_t wp_launch_dense(bool has_block, int threads, size_t smem, cudaStream
 size_t wp_dense_smem_bytes(int T, int S_cap, int C, bool has_block, int warps);
 cudaError_t wp_launch_fma_probe(int blocks, int threads, int iters, cudaStream_t stream, float* sink);
 cudaError_t wp_launch_fit_estep(bool has_block, int grid, int threads, cudaStream_t s, const FitArgs& a);
-struct NNArgs {
-    const float* queries;
-    int R;
-    int q0;
-    const float* coords;
-    const int* hits;
-    int N;
-    long long k;
-    int* qbin;
-    int* qbelow;
-    long long* qcap;
-    const long long* qoff;
-    int* cand_idx;
-    float* cand_d2;
-    int* err;
-    int slices;
-    int slice_len;
-    unsigned* shist;
-    int R_all;
-    long long* sliceoff;
-    long long* slicecap;
-    long long* slicecnt;
-};
-struct NNSelectArgs {
-    int R;
-    int q0;
-    const int* qbin;
-    const int* qbelow;
-    int slices;
-    int R_all;
-    const long long* sliceoff;
-    const long long* slicecnt;
-    const long long* slicecap;
-    const long long* qoff;
-    const int* cand_idx;
-    const float* cand_d2;
-    const int* hits;
-    const int* src_off;
-    const int* src_dense;
-    const double* src_ratio;
-    const int* src_hits;
-    const int* dense_id;
-    const int* dense_pep;
-    const int* dense_count;
-    int U;
-    long long k;
-    float inv_two_sig_sq;
-    int h;
-    double* acc;
-    int* mark;
-    int* touched;
-    int* out_ncand;
-    int* out_cand_id;
-    int* out_cand_pep;
-    double* out_cand_score;
-    double* out_total;
-    double* out_subfrac;
-};
 cudaError_t wp_launch_nn_dist(int DP, bool hist, cudaStream_t s, const NNArgs& a);
 cudaError_t wp_launch_nn_select(int grid, cudaStream_t s, const NNSelectArgs& a);
 cudaError_t wp_launch_nn_threshold(cudaStream_t s, const NNArgs& a);
 int wp_nn_bins();
+cudaError_t wp_launch_sim_reads(const SimParams& p, cudaStream_t s);
 cudaError_t wp_gemm_bf16_tn(const void* A, int lda, const void* B, int ldb, int M, int N, int K, void* C, int ldc,
                             int c_fp32, const float* bias, int act, void* Z, int accumulate, int* err,
                             cudaStream_t s);
@@ -162,6 +105,13 @@ struct wp_ctx {
 
     bool have_model = false;
     DevModel hm;
+    // the model's rates in FP64 (the simulator draws with them)
+    double raw_pf = 0, raw_pib = 0, raw_pcb = 0;
+    double raw_pdet[WP_MAX_TIMESTEPS] = {0};
+    double raw_pdud[WP_MAX_CHANNELS] = {0}, raw_pbleach[WP_MAX_CHANNELS] = {0};
+    // peptides as the simulator reads them
+    long long sim_pep_version = -1;
+    DevBuf d_sim_seqs, d_sim_off, d_sim_cum, d_sim_rads, d_sim_pep, d_sim_tracks;
     DevBuf d_model;
 
     bool have_peps = false;
@@ -848,6 +798,58 @@ wp_status hybrid_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig
     return WP_OK;
 }
 
+// Reads simulated on the device from the context's model and peptides.
+wp_status sim_device(wp_ctx* ctx, int R, unsigned long long seed, float* d_rads_f, double* d_rads_d, int* d_pep,
+                     uint8_t* d_tracks) {
+    if (ctx->sim_pep_version != ctx->pep_version) {
+        std::vector<int8_t> seqs(std::max<size_t>(ctx->seqs.size(), 1), -1);
+        for (size_t i = 0; i < ctx->seqs.size(); i++) seqs[i] = (int8_t)ctx->seqs[i];
+        std::vector<double> cum(std::max(ctx->P, 1), 0.0);
+        double acc = 0.0;
+        for (int i = 0; i < ctx->P; i++) {
+            acc += (double)ctx->counts[i];
+            cum[i] = acc;
+        }
+        if (ctx->P > 0 && !(acc > 0.0)) return fail(ctx, WP_ERR_INVALID, "peptide counts sum to zero");
+        WP_CUDA(ctx->d_sim_seqs.ensure(seqs.size()), "alloc");
+        WP_CUDA(ctx->d_sim_off.ensure(sizeof(int) * ctx->offsets.size()), "alloc");
+        WP_CUDA(ctx->d_sim_cum.ensure(sizeof(double) * cum.size()), "alloc");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_sim_seqs.p, seqs.data(), seqs.size(), cudaMemcpyHostToDevice, ctx->stream), "copy");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_sim_off.p, ctx->offsets.data(), sizeof(int) * ctx->offsets.size(),
+                                cudaMemcpyHostToDevice, ctx->stream), "copy");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_sim_cum.p, cum.data(), sizeof(double) * cum.size(), cudaMemcpyHostToDevice,
+                                ctx->stream), "copy");
+        WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        ctx->sim_pep_version = ctx->pep_version;
+    }
+    SimParams p;
+    memset(&p, 0, sizeof(p));
+    p.T = ctx->hm.T;
+    p.C = ctx->hm.C;
+    p.P = ctx->P;
+    p.R = R;
+    p.seed = seed;
+    p.p_edman_failure = ctx->raw_pf;
+    p.p_initial_block = ctx->raw_pib;
+    p.p_cyclic_block = ctx->raw_pcb;
+    for (int t = 0; t < WP_MAX_TIMESTEPS; t++) p.p_detach[t] = ctx->raw_pdet[t];
+    for (int c = 0; c < WP_MAX_CHANNELS; c++) {
+        p.p_dud[c] = ctx->raw_pdud[c];
+        p.p_bleach[c] = ctx->raw_pbleach[c];
+    }
+    p.model = ctx->d_model.as<DevModel>();
+    p.seqs = ctx->d_sim_seqs.as<int8_t>();
+    p.offsets = ctx->d_sim_off.as<int>();
+    p.cum = ctx->d_sim_cum.as<double>();
+    p.rads_f = d_rads_f;
+    p.rads_d = d_rads_d;
+    p.pep = d_pep;
+    p.tracks = d_tracks;
+    WP_CUDA(wp_launch_sim_reads(p, ctx->stream), "simulator launch");
+    ctx->launches++;
+    return WP_OK;
+}
+
 wp_status upload_reads(wp_ctx* ctx, const double* rads, int R) {
     const size_t bytes = sizeof(double) * (size_t)R * ctx->hm.T * ctx->hm.C;
     WP_CUDA(ctx->d_rads.ensure(bytes), "alloc reads");
@@ -982,8 +984,17 @@ wp_status wp_model_upload(wp_ctx* ctx, const wp_seq_model* m, int T) {
     h.p_ib = (float)m->p_initial_block;
     h.p_cb = (float)m->p_cyclic_block;
     h.has_block = (m->p_initial_block != 0.0 || m->p_cyclic_block != 0.0) ? 1 : 0;
-    for (int t = 0; t < T; t++)  // DecayingRateModel (decaying-rate-model.cc:47-50)
-        h.p_det[t] = (float)(m->p_detach + m->p_initial_detach * std::exp(-(double)t * m->p_initial_detach_decay));
+    for (int t = 0; t < T; t++) {  // DecayingRateModel (decaying-rate-model.cc:47-50)
+        ctx->raw_pdet[t] = m->p_detach + m->p_initial_detach * std::exp(-(double)t * m->p_initial_detach_decay);
+        h.p_det[t] = (float)ctx->raw_pdet[t];
+    }
+    ctx->raw_pf = m->p_edman_failure;
+    ctx->raw_pib = m->p_initial_block;
+    ctx->raw_pcb = m->p_cyclic_block;
+    for (int c = 0; c < C; c++) {
+        ctx->raw_pdud[c] = m->p_dud[c];
+        ctx->raw_pbleach[c] = m->p_bleach[c];
+    }
     h.interacting = 0;
     for (int c = 0; c < C; c++) {
         binomial_table(m->p_dud[c], WP_MAX_DYES_PER_CHANNEL, h.dud[c]);
@@ -1363,6 +1374,30 @@ wp_status wp_hybrid_classify_device(wp_ctx* ctx, const double* d_rads, int R, in
     st = hybrid_run(ctx, d_rads, R, k, sig, h, dist_cutoff, d_out_id, d_out_score, d_out_total);
     if (st != WP_OK) return st;
     return finish(ctx);
+}
+
+wp_status wp_simulate_reads(wp_ctx* ctx, int R, unsigned long long seed, double* out_rads, int32_t* out_pep,
+                            uint8_t* out_tracks) {
+    if (!ctx || R < 0 || (R > 0 && (!out_rads || !out_pep))) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    wp_status st = check_ready(ctx);
+    if (st != WP_OK) return st;
+    if (ctx->P == 0) return fail(ctx, WP_ERR_INVALID, "no peptides to simulate");
+    if (R == 0) return WP_OK;
+    const size_t TC = (size_t)ctx->hm.T * ctx->hm.C;
+    WP_CUDA(ctx->d_sim_rads.ensure(sizeof(double) * R * TC), "alloc");
+    WP_CUDA(ctx->d_sim_pep.ensure(sizeof(int) * R), "alloc");
+    if (out_tracks) WP_CUDA(ctx->d_sim_tracks.ensure(R * TC), "alloc");
+    st = sim_device(ctx, R, seed, nullptr, ctx->d_sim_rads.as<double>(), ctx->d_sim_pep.as<int>(),
+                    out_tracks ? ctx->d_sim_tracks.as<uint8_t>() : nullptr);
+    if (st != WP_OK) return st;
+    WP_CUDA(cudaMemcpyAsync(out_rads, ctx->d_sim_rads.p, sizeof(double) * R * TC, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    WP_CUDA(cudaMemcpyAsync(out_pep, ctx->d_sim_pep.p, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    if (out_tracks)
+        WP_CUDA(cudaMemcpyAsync(out_tracks, ctx->d_sim_tracks.p, R * TC, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    return WP_OK;
 }
 
 wp_status wp_dev_gemm_bf16(const void* A, int lda, const void* B, int ldb, int M, int N, int K, void* C, int ldc,

@@ -152,3 +152,81 @@ struct FitArgs {
     double* logp;          // [R] log P per read (nullable)
     int nslots;
 };
+
+// ---- kNN stage (wp_nn.cu) -------------------------------------------------
+struct NNArgs {
+    const float* queries;   // [R][DP]
+    int R;                  // queries in this launch (chunk)
+    int q0;                 // first query index of the chunk (into per-query arrays)
+    const float* coords;    // [N][DP]
+    const int* hits;        // [N] total hits per entry
+    int N;
+    long long k;
+    int* qbin;              // per query (indexed by q0 + local): bin b*
+    int* qbelow;            // hits in bins < b*
+    long long* qcap;        // hits in bins <= b* (>= entries there)
+    const long long* qoff;  // candidate list offset (chunk-relative)
+    int* cand_idx;
+    float* cand_d2;
+    int* err;
+    int slices;             // entry slices (blockIdx.y)
+    int slice_len;
+    unsigned* shist;        // [slices][R_all][NB] per-slice histograms
+    int R_all;              // queries in the whole batch
+    long long* sliceoff;    // [slices][R_all] offset of slice s inside query q's list
+    long long* slicecap;    // [slices][R_all] room for slice s (its hits in bins <= b*)
+    long long* slicecnt;    // [slices][R_all] candidates slice s wrote
+};
+
+struct NNSelectArgs {
+    int R;                      // queries in this chunk
+    int q0;
+    const int* qbin;
+    const int* qbelow;
+    int slices;
+    int R_all;
+    const long long* sliceoff;  // [slices][R_all]
+    const long long* slicecnt;  // [slices][R_all]
+    const long long* slicecap;  // [slices][R_all] (bounds slicecnt)
+    const long long* qoff;
+    const int* cand_idx;
+    const float* cand_d2;
+    const int* hits;            // [N]
+    const int* src_off;         // [N + 1]
+    const int* src_dense;       // [S] dense id
+    const double* src_ratio;    // [S] hits / count
+    const int* src_hits;        // [S]
+    const int* dense_id;        // [U] original id
+    const int* dense_pep;       // [U] peptide index (hybrid), may be null
+    const int* dense_count;     // [U] peptide count (hybrid), may be null
+    int U;
+    long long k;
+    float inv_two_sig_sq;
+    int h;
+    double* acc;                // [warps][U] zero on entry, zero on exit
+    int* mark;                  // [warps][U]
+    int* touched;               // [warps][U]
+    int* out_ncand;             // outputs, indexed by q0 + local
+    int* out_cand_id;           // [R][h] original ids
+    int* out_cand_pep;          // [R][h] peptide indices (may be null)
+    double* out_cand_score;     // [R][h]
+    double* out_total;
+    double* out_subfrac;        // may be null
+};
+
+// ---- read simulator (wp_sim.cu) -------------------------------------------
+struct SimParams {
+    int T, C, P, R;
+    unsigned long long seed;
+    double p_edman_failure, p_initial_block, p_cyclic_block;
+    double p_detach[WP_MAX_TIMESTEPS];
+    double p_dud[WP_MAX_CHANNELS], p_bleach[WP_MAX_CHANNELS];
+    const DevModel* model;     // emission model
+    const int8_t* seqs;        // ragged dye-seqs (channel or -1)
+    const int* offsets;        // [P + 1]
+    const double* cum;         // [P] cumulative peptide counts (last = total)
+    float* rads_f;             // [R][T*C] or null
+    double* rads_d;            // [R][T*C] or null
+    int* pep;                  // [R] peptide index or -1
+    uint8_t* tracks;           // [R][T*C] or null
+};

@@ -64,31 +64,6 @@ __device__ __forceinline__ float nn_d2(const float* q, const float* e) {
     return (a0 + a1) + (a2 + a3);
 }
 
-struct NNArgs {
-    const float* queries;   // [R][DP]
-    int R;                  // queries in this launch (chunk)
-    int q0;                 // first query index of the chunk (into per-query arrays)
-    const float* coords;    // [N][DP]
-    const int* hits;        // [N] total hits per entry
-    int N;
-    long long k;
-    // per query (indexed by q0 + local)
-    int* qbin;
-    int* qbelow;            // hits in bins < b*
-    long long* qcap;        // hits in bins <= b* (>= entries there)
-    const long long* qoff;  // candidate list offset (chunk-relative)
-    int* cand_idx;
-    float* cand_d2;
-    int* err;
-    // entry slices (blockIdx.y): slice s covers entries [s * slice_len, ...)
-    int slices;
-    int slice_len;
-    unsigned* shist;        // [slices][R_all][NB] per-slice histograms (pass 1)
-    int R_all;              // queries in the whole batch (stride of shist / sliceoff)
-    long long* sliceoff;    // [slices][R_all] offset of slice s inside query q's list
-    long long* slicecap;    // [slices][R_all] room for slice s (its hits in bins <= b*)
-    long long* slicecnt;    // [slices][R_all] candidates slice s wrote (collect)
-};
 
 // Load a tile of entries (coords and hits) into shared memory.
 template <int DP>
@@ -240,42 +215,6 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
     }
 }
 
-struct NNSelectArgs {
-    int R;                      // queries in this chunk
-    int q0;
-    const int* qbin;
-    const int* qbelow;
-    int slices;
-    int R_all;
-    const long long* sliceoff;  // [slices][R_all]
-    const long long* slicecnt;  // [slices][R_all]
-    const long long* slicecap;  // [slices][R_all] (bounds slicecnt)
-    const long long* qoff;
-    const int* cand_idx;
-    const float* cand_d2;
-    const int* hits;            // [N]
-    const int* src_off;         // [N + 1]
-    const int* src_dense;       // [S] dense id
-    const double* src_ratio;    // [S] hits / count
-    const int* src_hits;        // [S]
-    const int* dense_id;        // [U] original id
-    const int* dense_pep;       // [U] peptide index (hybrid), may be null
-    const int* dense_count;     // [U] peptide count (hybrid), may be null
-    int U;
-    long long k;
-    float inv_two_sig_sq;
-    int h;
-    double* acc;                // [warps][U] zero on entry, zero on exit
-    int* mark;                  // [warps][U]
-    int* touched;               // [warps][U]
-    // outputs, indexed by q0 + local
-    int* out_ncand;
-    int* out_cand_id;           // [R][h] original ids
-    int* out_cand_pep;          // [R][h] peptide indices (may be null)
-    double* out_cand_score;     // [R][h]
-    double* out_total;
-    double* out_subfrac;        // may be null
-};
 
 __device__ __forceinline__ unsigned long long nn_dbits(double v) { return (unsigned long long)__double_as_longlong(v); }
 

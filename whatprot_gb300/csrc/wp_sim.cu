@@ -1,0 +1,119 @@
+// wp_sim.cu -- seeded read simulator on the GPU (`simulate rad`):
+// generate_dye_track (simulation/generate-dye-track.cc:29-110) and
+// generate_radiometry (simulation/generate-radiometry.cc:28-62), one thread
+// per read, counter-based Philox streams (read r uses subsequence r of the
+// seed, so results do not depend on the launch shape).
+//
+// Per read: a peptide drawn with probability proportional to its count, its
+// dyes made duds (per channel p_dud), an initial block, then per timestep:
+// record the live dye counts; cyclic block; detach (the read is empty from
+// then on); unless blocked, an Edman cycle that succeeds with
+// 1 - p_edman_failure and removes the dye at the cut position; bleaching of
+// every remaining dye past the cut.  A read whose timestep-0 counts are all
+// zero is not detectable and gets peptide index -1 (the reference drops it).
+// Intensities are Normal(adjusted_mu, sigma(adjusted_mu)) per (t, c), with
+// ChannelModel's interactions (channel-model.h:35-70).
+//
+// The reference draws from std::default_random_engine in a different order,
+// so parity with it is statistical (tests compare distributions).
+#include <cuda_runtime.h>
+#include <curand_kernel.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "wp_common.cuh"
+
+#define SIM_MAX_LEN 256
+
+
+__device__ double sim_adjusted_mu(const DevModel& m, int channel, const int* counts) {
+    double amu = m.mu[channel] * (double)counts[channel];
+    for (int c = 0; c < m.C; c++) {
+        const double fi = m.flat[channel][c], ii = m.inter[channel][c];
+        if (c == channel) {
+            if (counts[c] > 1) {
+                if (fi != 1.0) amu *= fi;
+                if (ii != 1.0) amu *= pow(ii, (double)(counts[c] - 1));
+            }
+        } else if (counts[c] > 0) {
+            if (fi != 1.0) amu *= fi;
+            if (ii != 1.0) amu *= pow(ii, (double)counts[c]);
+        }
+    }
+    return amu;
+}
+
+__global__ void wp_sim_reads_kernel(SimParams p) {
+    const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= p.R) return;
+    curandStatePhilox4_32_10_t st;
+    curand_init(p.seed, (unsigned long long)r, 0ull, &st);
+    // peptide by count weight (upper bound of u * total in the prefix sums)
+    const double total = p.cum[p.P - 1];
+    const double u = curand_uniform_double(&st) * total;  // (0, total]
+    int lo = 0, hi = p.P - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (p.cum[mid] >= u) hi = mid;
+        else lo = mid + 1;
+    }
+    const int pep = lo;
+    const int L = min(p.offsets[pep + 1] - p.offsets[pep], SIM_MAX_LEN);
+    int8_t ds[SIM_MAX_LEN];
+    for (int i = 0; i < L; i++) ds[i] = p.seqs[p.offsets[pep] + i];
+    // duds
+    for (int i = 0; i < L; i++)
+        if (ds[i] >= 0 && curand_uniform_double(&st) <= p.p_dud[ds[i]]) ds[i] = -1;
+    int counts[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+    for (int i = 0; i < L; i++)
+        if (ds[i] >= 0) counts[ds[i]]++;
+    int e = 0;
+    bool block = curand_uniform_double(&st) <= p.p_initial_block;
+    uint8_t trk[WP_MAX_TIMESTEPS * WP_MAX_CHANNELS];
+    bool gone = false;
+    for (int t = 0; t < p.T; t++) {
+        if (!gone && e < L) {
+            for (int c = 0; c < p.C; c++) trk[t * p.C + c] = (uint8_t)counts[c];
+            if (curand_uniform_double(&st) <= p.p_cyclic_block) block = true;
+            if (curand_uniform_double(&st) <= p.p_detach[t]) {
+                gone = true;
+                continue;
+            }
+            if (!block && !(curand_uniform_double(&st) <= p.p_edman_failure)) {
+                if (ds[e] >= 0) counts[ds[e]]--;
+                e++;
+            }
+            for (int i = e; i < L; i++)
+                if (ds[i] >= 0 && curand_uniform_double(&st) <= p.p_bleach[ds[i]]) {
+                    counts[ds[i]]--;
+                    ds[i] = -1;
+                }
+        } else {
+            for (int c = 0; c < p.C; c++) trk[t * p.C + c] = 0;
+        }
+    }
+    bool trivial = true;
+    for (int c = 0; c < p.C; c++)
+        if (trk[c] != 0) trivial = false;
+    p.pep[r] = trivial ? -1 : pep;
+    const DevModel& m = *p.model;
+    const int TC = p.T * p.C;
+    for (int t = 0; t < p.T; t++) {
+        int cts[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+        for (int c = 0; c < p.C; c++) cts[c] = trk[t * p.C + c];
+        for (int c = 0; c < p.C; c++) {
+            const double mu = sim_adjusted_mu(m, c, cts);
+            const double sg = sqrt(m.bg_sig[c] * m.bg_sig[c] + mu * m.sig[c] * m.sig[c]);
+            const double x = mu + sg * curand_normal_double(&st);
+            if (p.rads_f) p.rads_f[r * TC + t * p.C + c] = (float)x;
+            if (p.rads_d) p.rads_d[r * TC + t * p.C + c] = x;
+            if (p.tracks) p.tracks[r * TC + t * p.C + c] = trk[t * p.C + c];
+        }
+    }
+}
+
+cudaError_t wp_launch_sim_reads(const SimParams& p, cudaStream_t s) {
+    if (p.R == 0) return cudaSuccess;
+    wp_sim_reads_kernel<<<(p.R + 127) / 128, 128, 0, s>>>(p);
+    return cudaGetLastError();
+}
