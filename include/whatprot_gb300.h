@@ -283,6 +283,69 @@ wp_status wp_dev_gemm_bf16(const void* A, int lda, const void* B, int ldb,
                            int M, int N, int K, void* C, int ldc, int c_fp32,
                            const float* bias, int act, void* Z);
 
+/* ---- Learned proposal network (no reference counterpart).  An MLP from a
+ * radiometry (T*C <= 64 intensities, zero padded to 64) to logits over the
+ * context's peptides: GELU(W1 x + b1) -> GELU(W2 h + b2) -> W3 h + b3, hidden
+ * width `hidden`, BF16 weights and activations, FP32 accumulation on the
+ * tensor cores, FP32 master weights and Adam.  It proposes the top-h
+ * peptides that the HMM rescores, in place of the kNN stage of the hybrid.
+ * A network belongs to the context's device and is tied to the peptide set
+ * and read shape it was built for (WP_ERR_STATE otherwise). */
+typedef struct wp_mlp wp_mlp;
+wp_status wp_mlp_create(wp_ctx* ctx, int hidden, unsigned long long seed,
+                        wp_mlp** out);
+void wp_mlp_destroy(wp_mlp* mlp);
+
+/* Train on num_reads reads simulated on the device from the context's model
+ * and peptides (wp_simulate_reads; fresh reads every step, streams derived
+ * from seed), in steps of `batch` (a multiple of 64) with Adam at rate lr.
+ * Undetectable reads count as no example.  *out_loss (nullable): the mean
+ * cross-entropy of the last step. */
+wp_status wp_mlp_train(wp_ctx* ctx, wp_mlp* mlp, long long num_reads, int batch,
+                       float lr, unsigned long long seed, double* out_loss);
+
+/* One step on a device batch: d_x [B][T*C] FP32, d_labels [B] peptide
+ * indices (-1: skip), B a multiple of 64.  lr 0 computes the gradients only
+ * (wp_mlp_get with grad = 1 reads them). */
+wp_status wp_mlp_train_step(wp_ctx* ctx, wp_mlp* mlp, const float* d_x,
+                            const int32_t* d_labels, int B, float lr,
+                            double* out_loss);
+
+/* Parameter tensors: 0 W1 [hidden][64], 1 b1 [hidden], 2 W2 [hidden][hidden],
+ * 3 b2, 4 W3 [Ppad][hidden], 5 b3 [Ppad] (Ppad = peptides rounded up to 64;
+ * padded rows are zero).  Get copies the FP32 master (grad = 0) or the last
+ * gradient (grad = 1) to host; set replaces the master. */
+wp_status wp_mlp_shape(const wp_mlp* mlp, int which, long long* rows,
+                       long long* cols);
+wp_status wp_mlp_get(wp_mlp* mlp, int which, int grad, float* out);
+wp_status wp_mlp_set(wp_ctx* ctx, wp_mlp* mlp, int which, const float* in);
+
+/* Logits [R][P] for reads [R][T][C] (host doubles divided by mu). */
+wp_status wp_mlp_logits(wp_ctx* ctx, wp_mlp* mlp, const double* rads,
+                        int num_reads, float* out);
+
+/* The top h peptides per read: indices [R][h] in ascending logit (ties by
+ * index), their softmax probabilities, and (nullable) the candidates'
+ * sum of probability x peptide count.  h <= min(1024, peptides). */
+wp_status wp_mlp_propose(wp_ctx* ctx, wp_mlp* mlp, const double* rads,
+                         int num_reads, int h, int32_t* out_idx,
+                         float* out_prob, double* out_mass);
+
+/* The hybrid classifier with the network's proposals in place of the kNN
+ * stage: the HMM over the top h peptides (ascending logit; ties go to the
+ * lower logit), its score times the candidates' probability mass (sum of
+ * softmax probability x count, the analogue of the kNN subfraction), NaN
+ * patched. */
+wp_status wp_mlp_hybrid_classify(wp_ctx* ctx, wp_mlp* mlp, const double* rads,
+                                 int num_reads, int h, double dist_cutoff,
+                                 int32_t* out_id, double* out_score,
+                                 double* out_total);
+wp_status wp_mlp_hybrid_classify_device(wp_ctx* ctx, wp_mlp* mlp,
+                                        const double* d_rads, int num_reads,
+                                        int h, double dist_cutoff,
+                                        int32_t* d_out_id, double* d_out_score,
+                                        double* d_out_total);
+
 /* Kernel launches issued by this context since creation (all kinds). */
 long long wp_launch_count(const wp_ctx* ctx);
 

@@ -1,0 +1,87 @@
+"""The learned proposal network on the GPU (wp_mlp_*): logits and gradients
+against the CPU oracle (oracle/mlp_oracle.py, FP64 with BF16 rounding at the
+GPU's rounding points), and what training gains.
+
+Tolerance: the oracle rounds to BF16 where the GPU does, so only the
+tensor cores' FP32 summation order differs (and the BF16 roundings it can
+tip): logits within 1e-3 of the largest logit magnitude, each gradient
+within 2 % relative Frobenius error and a cosine similarity above 0.9995."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from whatprot_gb300 import capi
+from whatprot_gb300.simulate import paper_model, random_dye_seqs
+
+pytestmark = pytest.mark.gpu
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+
+
+def _ctx(P, C=2, T=8, seed=5):
+    sm = paper_model(C)
+    ds = random_dye_seqs(P, C, 6, 14, max_per_channel=4, min_total=1, seed=seed)
+    ctx = capi.Context(0)
+    ctx.upload_model(sm, T)
+    ctx.upload_peptides(ds)
+    return ctx, sm, ds
+
+
+def test_gradients_match_oracle():
+    import torch
+    import mlp_oracle
+    ctx, sm, ds = _ctx(100)
+    try:
+        net = capi.ProposalNet(ctx, hidden=256, seed=3)
+        B = 128
+        rads, pep, _ = ctx.simulate_reads(B, seed=11)
+        x = rads.reshape(B, -1).astype(np.float32)
+        params = {n: net.get(i).astype(np.float64) for i, n in enumerate(capi.ProposalNet.PARAMS)}
+        d_x = torch.from_numpy(x).cuda()
+        d_y = torch.from_numpy(pep.astype(np.int32)).cuda()
+        loss = net.train_step(d_x.data_ptr(), d_y.data_ptr(), B, 0.0)
+        ora_loss, g, L = mlp_oracle.gradients(params, x.astype(np.float64), pep, len(ds))
+        assert abs(loss - ora_loss) <= 1e-3 * max(1.0, abs(ora_loss))
+        logits = net.logits(rads)
+        assert np.max(np.abs(logits - L[:, :len(ds)])) <= 1e-3 * np.max(np.abs(L))
+        for i, n in enumerate(capi.ProposalNet.PARAMS):
+            gg = net.get(i, grad=True).astype(np.float64).reshape(g[n].shape)
+            rel = np.linalg.norm(gg - g[n]) / max(np.linalg.norm(g[n]), 1e-30)
+            cos = float(np.sum(gg * g[n]) / max(np.linalg.norm(gg) * np.linalg.norm(g[n]), 1e-30))
+            assert rel <= 0.02 and cos >= 0.9995, (n, rel, cos)
+        net.close()
+    finally:
+        ctx.close()
+
+
+def test_training_gains_recall_and_feeds_the_hmm():
+    """Training on GPU-simulated reads lowers the loss and raises recall@h
+    well above the untrained network; the HMM over the proposals then picks
+    the same peptide as the full HMM for most reads."""
+    P, T = 150, 8
+    ctx, sm, ds = _ctx(P, T=T, seed=9)
+    try:
+        net = capi.ProposalNet(ctx, hidden=512, seed=4)
+        rads, pep, _ = ctx.simulate_reads(3000, seed=99)
+        ok = pep >= 0
+        rads, pep = rads[ok], pep[ok]
+        h = 15
+
+        def recall():
+            idx, prob, mass = net.propose(rads, h)
+            return float(np.mean([pep[r] in idx[r] for r in range(len(pep))]))
+
+        r0 = recall()
+        first = net.train(16384, batch=1024, lr=1e-3, seed=1)
+        last = net.train(400000, batch=1024, lr=1e-3, seed=2)
+        r1 = recall()
+        assert last < first - 0.5, (first, last)
+        assert r1 >= r0 + 0.3 and r1 >= 0.7, (r0, r1)
+        full_id, _, _, _ = ctx.classify(rads, 5.0)
+        mid, msc, mtot = net.hybrid_classify(rads, h, 5.0)
+        agree = float(np.mean(mid == full_id))
+        assert agree >= 0.85, agree
+        net.close()
+    finally:
+        ctx.close()

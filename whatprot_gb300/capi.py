@@ -32,7 +32,9 @@ EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload"
            "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak", "wp_last_batch_stats",
            "wp_fit_begin", "wp_fit_estep", "wp_hmm_fit", "wp_fit_offset_exponential",
            "wp_nn_tracks_upload", "wp_nn_classify", "wp_hybrid_classify", "wp_hybrid_classify_device",
-           "wp_dev_gemm_bf16", "wp_simulate_reads"]
+           "wp_dev_gemm_bf16", "wp_simulate_reads", "wp_mlp_create", "wp_mlp_destroy", "wp_mlp_train",
+           "wp_mlp_train_step", "wp_mlp_shape", "wp_mlp_get", "wp_mlp_set", "wp_mlp_logits", "wp_mlp_propose",
+           "wp_mlp_hybrid_classify", "wp_mlp_hybrid_classify_device"]
 
 
 class WpSeqModel(ctypes.Structure):
@@ -173,6 +175,29 @@ def load_library(path: Optional[str] = None):
     lib.wp_hybrid_classify_device.restype = I
     lib.wp_simulate_reads.argtypes = [V, I, ctypes.c_ulonglong, V, V, V]
     lib.wp_simulate_reads.restype = I
+    LL, U64, F = ctypes.c_longlong, ctypes.c_ulonglong, ctypes.c_float
+    lib.wp_mlp_create.argtypes = [V, I, U64, ctypes.POINTER(V)]
+    lib.wp_mlp_create.restype = I
+    lib.wp_mlp_destroy.argtypes = [V]
+    lib.wp_mlp_destroy.restype = None
+    lib.wp_mlp_train.argtypes = [V, V, LL, I, F, U64, ctypes.POINTER(D)]
+    lib.wp_mlp_train.restype = I
+    lib.wp_mlp_train_step.argtypes = [V, V, V, V, I, F, ctypes.POINTER(D)]
+    lib.wp_mlp_train_step.restype = I
+    lib.wp_mlp_shape.argtypes = [V, I, ctypes.POINTER(LL), ctypes.POINTER(LL)]
+    lib.wp_mlp_shape.restype = I
+    lib.wp_mlp_get.argtypes = [V, I, I, V]
+    lib.wp_mlp_get.restype = I
+    lib.wp_mlp_set.argtypes = [V, V, I, V]
+    lib.wp_mlp_set.restype = I
+    lib.wp_mlp_logits.argtypes = [V, V, V, I, V]
+    lib.wp_mlp_logits.restype = I
+    lib.wp_mlp_propose.argtypes = [V, V, V, I, I, V, V, V]
+    lib.wp_mlp_propose.restype = I
+    lib.wp_mlp_hybrid_classify.argtypes = [V, V, V, I, I, D, V, V, V]
+    lib.wp_mlp_hybrid_classify.restype = I
+    lib.wp_mlp_hybrid_classify_device.argtypes = [V, V, V, I, I, D, V, V, V]
+    lib.wp_mlp_hybrid_classify_device.restype = I
     lib.wp_dev_gemm_bf16.argtypes = [V, I, V, I, I, I, I, V, I, I, V, I, V]
     lib.wp_dev_gemm_bf16.restype = I
     if path is None:
@@ -593,3 +618,89 @@ class HybridClassifier:
         ids, sc, tot = self.ctx.hybrid_classify(rads, self.k, self.sig, self.h, self.dist_cutoff)
         res = [ScoredClassification(int(i), float(s), float(t)) for i, s, t in zip(ids, sc, tot)]
         return res[0] if single else res
+
+
+class ProposalNet:
+    """The learned proposal network on a Context (wp_mlp_*): built for the
+    context's current model and peptide set."""
+
+    PARAMS = ("W1", "b1", "W2", "b2", "W3", "b3")
+
+    def __init__(self, ctx: "Context", hidden: int = 1024, seed: int = 1):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = ctypes.c_void_p()
+        ctx._check(self.lib.wp_mlp_create(ctx.h, hidden, seed, ctypes.byref(h)))
+        self.h = h
+        self.hidden = hidden
+
+    def close(self):
+        if self.h:
+            self.lib.wp_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def train(self, num_reads: int, batch: int = 4096, lr: float = 1e-3, seed: int = 7) -> float:
+        loss = ctypes.c_double(0.0)
+        self.ctx._check(self.lib.wp_mlp_train(self.ctx.h, self.h, num_reads, batch, lr, seed, ctypes.byref(loss)))
+        return loss.value
+
+    def train_step(self, d_x_ptr: int, d_labels_ptr: int, B: int, lr: float) -> float:
+        loss = ctypes.c_double(0.0)
+        self.ctx._check(self.lib.wp_mlp_train_step(self.ctx.h, self.h, ctypes.c_void_p(d_x_ptr),
+                                                   ctypes.c_void_p(d_labels_ptr), B, lr, ctypes.byref(loss)))
+        return loss.value
+
+    def shape(self, which: int):
+        r, c = ctypes.c_longlong(), ctypes.c_longlong()
+        self.lib.wp_mlp_shape(self.h, which, ctypes.byref(r), ctypes.byref(c))
+        return int(r.value), int(c.value)
+
+    def get(self, which: int, grad: bool = False) -> np.ndarray:
+        r, c = self.shape(which)
+        out = np.zeros((r, c), np.float32)
+        st = self.lib.wp_mlp_get(self.h, which, 1 if grad else 0, _ptr(out))
+        if st != 0:
+            raise WpError(st, "wp_mlp_get")
+        return out if c > 1 else out.reshape(-1)
+
+    def set(self, which: int, value: np.ndarray) -> None:
+        v = np.ascontiguousarray(value, dtype=np.float32)
+        self.ctx._check(self.lib.wp_mlp_set(self.ctx.h, self.h, which, _ptr(v)))
+
+    def logits(self, rads: np.ndarray) -> np.ndarray:
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        out = np.zeros((rads.shape[0], self.ctx.num_peptides), np.float32)
+        self.ctx._check(self.lib.wp_mlp_logits(self.ctx.h, self.h, _ptr(rads), rads.shape[0], _ptr(out)))
+        return out
+
+    def propose(self, rads: np.ndarray, h: int):
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        R = rads.shape[0]
+        idx = np.zeros((R, h), np.int32)
+        prob = np.zeros((R, h), np.float32)
+        mass = np.zeros(R, np.float64)
+        self.ctx._check(self.lib.wp_mlp_propose(self.ctx.h, self.h, _ptr(rads), R, h, _ptr(idx), _ptr(prob),
+                                                _ptr(mass)))
+        return idx, prob, mass
+
+    def hybrid_classify(self, rads: np.ndarray, h: int, dist_cutoff: float):
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        R = rads.shape[0]
+        ids = np.zeros(R, np.int32)
+        sc = np.zeros(R, np.float64)
+        tot = np.zeros(R, np.float64)
+        self.ctx._check(self.lib.wp_mlp_hybrid_classify(self.ctx.h, self.h, _ptr(rads), R, h, dist_cutoff, _ptr(ids),
+                                                        _ptr(sc), _ptr(tot)))
+        return ids, sc, tot
+
+    def hybrid_classify_device(self, d_rads_ptr: int, R: int, h: int, dist_cutoff: float, d_id: int, d_score: int,
+                               d_total: int) -> None:
+        self.ctx._check(self.lib.wp_mlp_hybrid_classify_device(self.ctx.h, self.h, ctypes.c_void_p(d_rads_ptr), R, h,
+                                                               dist_cutoff, ctypes.c_void_p(d_id),
+                                                               ctypes.c_void_p(d_score), ctypes.c_void_p(d_total)))

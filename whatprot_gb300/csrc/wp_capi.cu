@@ -51,6 +51,21 @@ cudaError_t wp_launch_nn_select(int grid, cudaStream_t s, const NNSelectArgs& a)
 cudaError_t wp_launch_nn_threshold(cudaStream_t s, const NNArgs& a);
 int wp_nn_bins();
 cudaError_t wp_launch_sim_reads(const SimParams& p, cudaStream_t s);
+#include <cuda_bf16.h>
+cudaError_t wp_mlp_launch_input(const float* xf, const double* xd, int B, int TC, __nv_bfloat16* X, cudaStream_t s);
+cudaError_t wp_mlp_launch_transpose(const __nv_bfloat16* in, int rows, int cols, int ld_in, __nv_bfloat16* out,
+                                    int ld_out, cudaStream_t s);
+cudaError_t wp_mlp_launch_softmax_ce(const float* logits, int B, int P, int ld, const int* labels, float scale,
+                                     __nv_bfloat16* dL, double* loss, cudaStream_t s);
+cudaError_t wp_mlp_launch_gelu_bwd(const float* dH, const __nv_bfloat16* Z, long n, __nv_bfloat16* dZ, cudaStream_t s);
+cudaError_t wp_mlp_launch_colsum(const __nv_bfloat16* M, int rows, int cols, int ld, float* out, cudaStream_t s);
+cudaError_t wp_mlp_launch_adam(float* w, const float* g, float* m, float* v, long n, float lr, float b1, float b2,
+                               float eps, float bc1, float bc2, __nv_bfloat16* wb, cudaStream_t s);
+cudaError_t wp_mlp_launch_to_bf16(const float* in, long n, __nv_bfloat16* out, cudaStream_t s);
+cudaError_t wp_mlp_launch_init(float* w, long rows, long cols, long valid_rows, float std, unsigned long long seed,
+                               cudaStream_t s);
+cudaError_t wp_mlp_launch_topk(const float* logits, int R, int P, int ld, int h, const int* counts, int* idx,
+                               float* prob, double* mass, cudaStream_t s);
 cudaError_t wp_gemm_bf16_tn(const void* A, int lda, const void* B, int ldb, int M, int N, int K, void* C, int ldc,
                             int c_fp32, const float* bias, int act, void* Z, int accumulate, int* err,
                             cudaStream_t s);
@@ -1440,6 +1455,456 @@ wp_status wp_hmm_count_flops(wp_ctx* ctx, const double* rads, int R, double dist
     for (double v : per) s += v;
     *out_flops = s;
     return WP_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ learned proposal
+struct wp_mlp {
+    int device = 0;
+    int P = 0, Ppad = 0, H = 0, TC = 0;
+    int cap = 0;              // batch capacity of the activation buffers
+    long long steps = 0;      // Adam steps taken
+    // FP32: W1 b1 W2 b2 W3 b3, each with grad, Adam m, v
+    DevBuf w[6], g[6], m[6], v[6];
+    long n[6] = {0, 0, 0, 0, 0, 0};
+    DevBuf W1b, W2b, W3b, W2T, W3T;  // BF16 copies
+    DevBuf X, XT, Z1, H1, H1T, Z2, H2, H2T, dL, dLT, dZ2, dZ2T, dZ1, dZ1T, L, dH2, dH1, loss, labels, xsim, err;
+    DevBuf topi, topp, mass, counts, loss_sum;
+};
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+#define MLP_CUDA(call, what)                                    \
+    do {                                                        \
+        cudaError_t _e = (call);                                \
+        if (_e != cudaSuccess) return cuda_fail(ctx, _e, what); \
+    } while (0)
+
+wp_status mlp_gemm(wp_ctx* ctx, wp_mlp* m, const void* A, int lda, const void* B, int ldb, int M, int N, int K,
+                   void* C, int ldc, int c_fp32, const float* bias, int act, void* Z) {
+    cudaError_t e = wp_gemm_bf16_tn(A, lda, B, ldb, M, N, K, C, ldc, c_fp32, bias, act, Z, 0, m->err.as<int>(),
+                                    ctx->stream);
+    ctx->launches++;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "tensor-core GEMM launch");
+    return WP_OK;
+}
+
+wp_status mlp_ensure(wp_ctx* ctx, wp_mlp* m, int B) {
+    if (B <= m->cap) return WP_OK;
+    const size_t b = (size_t)B, H = m->H, Pp = m->Ppad;
+    MLP_CUDA(m->X.ensure(sizeof(bf16) * b * 64), "alloc");
+    MLP_CUDA(m->XT.ensure(sizeof(bf16) * b * 64), "alloc");
+    for (DevBuf* d : {&m->Z1, &m->H1, &m->H1T, &m->Z2, &m->H2, &m->H2T, &m->dZ2, &m->dZ2T, &m->dZ1, &m->dZ1T})
+        MLP_CUDA(d->ensure(sizeof(bf16) * b * H), "alloc activations");
+    MLP_CUDA(m->dL.ensure(sizeof(bf16) * b * Pp), "alloc logits gradient");
+    MLP_CUDA(m->dLT.ensure(sizeof(bf16) * b * Pp), "alloc logits gradient");
+    MLP_CUDA(m->L.ensure(sizeof(float) * b * Pp), "alloc logits");
+    MLP_CUDA(m->dH2.ensure(sizeof(float) * b * H), "alloc");
+    MLP_CUDA(m->dH1.ensure(sizeof(float) * b * H), "alloc");
+    MLP_CUDA(m->loss.ensure(sizeof(double) * b), "alloc");
+    MLP_CUDA(m->labels.ensure(sizeof(int) * b), "alloc");
+    MLP_CUDA(m->xsim.ensure(sizeof(float) * b * m->TC), "alloc");
+    m->cap = B;
+    return WP_OK;
+}
+
+// BF16 copies (and transposes) of the master weights.
+wp_status mlp_refresh(wp_ctx* ctx, wp_mlp* m) {
+    MLP_CUDA(wp_mlp_launch_to_bf16(m->w[0].as<float>(), m->n[0], m->W1b.as<bf16>(), ctx->stream), "bf16");
+    MLP_CUDA(wp_mlp_launch_to_bf16(m->w[2].as<float>(), m->n[2], m->W2b.as<bf16>(), ctx->stream), "bf16");
+    MLP_CUDA(wp_mlp_launch_to_bf16(m->w[4].as<float>(), m->n[4], m->W3b.as<bf16>(), ctx->stream), "bf16");
+    MLP_CUDA(wp_mlp_launch_transpose(m->W2b.as<bf16>(), m->H, m->H, m->H, m->W2T.as<bf16>(), m->H, ctx->stream), "T");
+    MLP_CUDA(wp_mlp_launch_transpose(m->W3b.as<bf16>(), m->Ppad, m->H, m->H, m->W3T.as<bf16>(), m->Ppad, ctx->stream),
+             "T");
+    ctx->launches += 5;
+    return WP_OK;
+}
+
+// Logits of B inputs already in m->X.
+wp_status mlp_forward(wp_ctx* ctx, wp_mlp* m, int B) {
+    const int H = m->H, Pp = m->Ppad;
+    wp_status st = mlp_gemm(ctx, m, m->X.p, 64, m->W1b.p, 64, B, H, 64, m->H1.p, H, 0, m->w[1].as<float>(), 1, m->Z1.p);
+    if (st != WP_OK) return st;
+    st = mlp_gemm(ctx, m, m->H1.p, H, m->W2b.p, H, B, H, H, m->H2.p, H, 0, m->w[3].as<float>(), 1, m->Z2.p);
+    if (st != WP_OK) return st;
+    return mlp_gemm(ctx, m, m->H2.p, H, m->W3b.p, H, B, Pp, H, m->L.p, Pp, 1, m->w[5].as<float>(), 0, nullptr);
+}
+
+// One optimiser step on B inputs in m->X with labels in m->labels (lr 0:
+// gradients only).
+wp_status mlp_step(wp_ctx* ctx, wp_mlp* m, int B, float lr) {
+    const int H = m->H, Pp = m->Ppad;
+    cudaStream_t s = ctx->stream;
+    wp_status st = mlp_forward(ctx, m, B);
+    if (st != WP_OK) return st;
+    MLP_CUDA(wp_mlp_launch_softmax_ce(m->L.as<float>(), B, m->P, Pp, m->labels.as<int>(), 1.0f / (float)B,
+                                      m->dL.as<bf16>(), m->loss.as<double>(), s), "softmax");
+    MLP_CUDA(wp_mlp_launch_transpose(m->dL.as<bf16>(), B, Pp, Pp, m->dLT.as<bf16>(), B, s), "T");
+    MLP_CUDA(wp_mlp_launch_transpose(m->H2.as<bf16>(), B, H, H, m->H2T.as<bf16>(), B, s), "T");
+    ctx->launches += 3;
+    st = mlp_gemm(ctx, m, m->dLT.p, B, m->H2T.p, B, Pp, H, B, m->g[4].p, H, 1, nullptr, 0, nullptr);  // dW3
+    if (st != WP_OK) return st;
+    MLP_CUDA(wp_mlp_launch_colsum(m->dL.as<bf16>(), B, Pp, Pp, m->g[5].as<float>(), s), "colsum");
+    st = mlp_gemm(ctx, m, m->dL.p, Pp, m->W3T.p, Pp, B, H, Pp, m->dH2.p, H, 1, nullptr, 0, nullptr);  // dH2
+    if (st != WP_OK) return st;
+    MLP_CUDA(wp_mlp_launch_gelu_bwd(m->dH2.as<float>(), m->Z2.as<bf16>(), (long)B * H, m->dZ2.as<bf16>(), s), "gelu'");
+    MLP_CUDA(wp_mlp_launch_transpose(m->dZ2.as<bf16>(), B, H, H, m->dZ2T.as<bf16>(), B, s), "T");
+    MLP_CUDA(wp_mlp_launch_transpose(m->H1.as<bf16>(), B, H, H, m->H1T.as<bf16>(), B, s), "T");
+    ctx->launches += 4;
+    st = mlp_gemm(ctx, m, m->dZ2T.p, B, m->H1T.p, B, H, H, B, m->g[2].p, H, 1, nullptr, 0, nullptr);  // dW2
+    if (st != WP_OK) return st;
+    MLP_CUDA(wp_mlp_launch_colsum(m->dZ2.as<bf16>(), B, H, H, m->g[3].as<float>(), s), "colsum");
+    st = mlp_gemm(ctx, m, m->dZ2.p, H, m->W2T.p, H, B, H, H, m->dH1.p, H, 1, nullptr, 0, nullptr);  // dH1
+    if (st != WP_OK) return st;
+    MLP_CUDA(wp_mlp_launch_gelu_bwd(m->dH1.as<float>(), m->Z1.as<bf16>(), (long)B * H, m->dZ1.as<bf16>(), s), "gelu'");
+    MLP_CUDA(wp_mlp_launch_transpose(m->dZ1.as<bf16>(), B, H, H, m->dZ1T.as<bf16>(), B, s), "T");
+    MLP_CUDA(wp_mlp_launch_transpose(m->X.as<bf16>(), B, 64, 64, m->XT.as<bf16>(), B, s), "T");
+    ctx->launches += 4;
+    st = mlp_gemm(ctx, m, m->dZ1T.p, B, m->XT.p, B, H, 64, B, m->g[0].p, 64, 1, nullptr, 0, nullptr);  // dW1
+    if (st != WP_OK) return st;
+    MLP_CUDA(wp_mlp_launch_colsum(m->dZ1.as<bf16>(), B, H, H, m->g[1].as<float>(), s), "colsum");
+    ctx->launches++;
+    if (lr > 0.0f) {
+        m->steps++;
+        const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+        const float bc1 = 1.0f - powf(b1, (float)m->steps), bc2 = 1.0f - powf(b2, (float)m->steps);
+        bf16* wb[6] = {m->W1b.as<bf16>(), nullptr, m->W2b.as<bf16>(), nullptr, m->W3b.as<bf16>(), nullptr};
+        for (int i = 0; i < 6; i++) {
+            MLP_CUDA(wp_mlp_launch_adam(m->w[i].as<float>(), m->g[i].as<float>(), m->m[i].as<float>(),
+                                        m->v[i].as<float>(), m->n[i], lr, b1, b2, eps, bc1, bc2, wb[i], s), "adam");
+            ctx->launches++;
+        }
+        MLP_CUDA(wp_mlp_launch_transpose(m->W2b.as<bf16>(), H, H, H, m->W2T.as<bf16>(), H, s), "T");
+        MLP_CUDA(wp_mlp_launch_transpose(m->W3b.as<bf16>(), Pp, H, H, m->W3T.as<bf16>(), Pp, s), "T");
+        ctx->launches += 2;
+    }
+    return WP_OK;
+}
+
+wp_status mlp_check(wp_ctx* ctx, wp_mlp* m) {
+    if (!m) return WP_ERR_INVALID;
+    if (!ctx->have_model || !ctx->have_peps) return fail(ctx, WP_ERR_STATE, "model or peptides not uploaded");
+    if (ctx->P != m->P || ctx->hm.T * ctx->hm.C != m->TC)
+        return fail(ctx, WP_ERR_STATE, "the network was built for another peptide set or read shape");
+    return WP_OK;
+}
+
+wp_status mlp_finish(wp_ctx* ctx, wp_mlp* m) {
+    MLP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    int err = 0;
+    MLP_CUDA(cudaMemcpy(&err, m->err.p, sizeof(int), cudaMemcpyDeviceToHost), "read err");
+    if (err) return fail(ctx, WP_ERR_TIMEOUT, "a tensor-core GEMM pipeline wait expired");
+    return WP_OK;
+}
+
+// Top-h proposals for R reads on the device (FP64 [R][TC]), in chunks of
+// the batch capacity: ascending peptide indices by logit in d_idx [R][h],
+// probabilities in d_prob, candidate mass (sum prob x count) in d_mass.
+wp_status mlp_propose_dev(wp_ctx* ctx, wp_mlp* m, const double* d_rads, int R, int h, int* d_idx, float* d_prob,
+                          double* d_mass) {
+    const int chunk = 8192;
+    wp_status st = mlp_ensure(ctx, m, chunk);
+    if (st != WP_OK) return st;
+    MLP_CUDA(m->counts.ensure(sizeof(int) * std::max(ctx->P, 1)), "alloc");
+    MLP_CUDA(cudaMemcpyAsync(m->counts.p, ctx->counts.data(), sizeof(int) * ctx->P, cudaMemcpyHostToDevice,
+                             ctx->stream), "copy");
+    for (int r0 = 0; r0 < R; r0 += chunk) {
+        const int n = std::min(chunk, R - r0);
+        MLP_CUDA(wp_mlp_launch_input(nullptr, d_rads + (size_t)r0 * m->TC, n, m->TC, m->X.as<bf16>(), ctx->stream),
+                 "input");
+        ctx->launches++;
+        {
+            TimedLaunch tl(ctx, 4);
+            st = mlp_forward(ctx, m, n);
+            if (st != WP_OK) return st;
+        }
+        TimedLaunch tl(ctx, 5);
+        MLP_CUDA(wp_mlp_launch_topk(m->L.as<float>(), n, m->P, m->Ppad, h, m->counts.as<int>(), d_idx + (size_t)r0 * h,
+                                    d_prob + (size_t)r0 * h, d_mass + r0, ctx->stream), "top-k");
+        ctx->launches++;
+    }
+    return WP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+wp_status wp_mlp_create(wp_ctx* ctx, int hidden, unsigned long long seed, wp_mlp** out) {
+    if (!ctx || !out || hidden < 64 || hidden % 64) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if (!ctx->have_model || !ctx->have_peps) return fail(ctx, WP_ERR_STATE, "model or peptides not uploaded");
+    if (ctx->P < 1) return fail(ctx, WP_ERR_INVALID, "no peptides");
+    const int TC = ctx->hm.T * ctx->hm.C;
+    if (TC > 64) return fail(ctx, WP_ERR_UNSUPPORTED, "the network takes timesteps x channels <= 64");
+    wp_mlp* m = new wp_mlp();
+    m->device = ctx->device;
+    m->P = ctx->P;
+    m->Ppad = (ctx->P + 63) / 64 * 64;
+    m->H = hidden;
+    m->TC = TC;
+    const long H = hidden, Pp = m->Ppad;
+    const long sizes[6] = {H * 64, H, H * H, H, Pp * H, Pp};
+    for (int i = 0; i < 6; i++) {
+        m->n[i] = sizes[i];
+        for (DevBuf* d : {&m->w[i], &m->g[i], &m->m[i], &m->v[i]}) {
+            if (d->ensure(sizeof(float) * sizes[i]) != cudaSuccess) {
+                delete m;
+                return fail(ctx, WP_ERR_OOM, "alloc network");
+            }
+            cudaMemsetAsync(d->p, 0, sizeof(float) * sizes[i], ctx->stream);
+        }
+    }
+    if (m->W1b.ensure(sizeof(bf16) * H * 64) || m->W2b.ensure(sizeof(bf16) * H * H) ||
+        m->W3b.ensure(sizeof(bf16) * Pp * H) || m->W2T.ensure(sizeof(bf16) * H * H) ||
+        m->W3T.ensure(sizeof(bf16) * Pp * H) || m->err.ensure(sizeof(int)) || m->loss_sum.ensure(sizeof(double))) {
+        delete m;
+        return fail(ctx, WP_ERR_OOM, "alloc network");
+    }
+    cudaMemsetAsync(m->err.p, 0, sizeof(int), ctx->stream);
+    // He-style initialisation: N(0, 2 / fan_in) for the GELU layers,
+    // N(0, 1 / fan_in) for the logits; biases zero; padded classes zero.
+    cudaError_t e = wp_mlp_launch_init(m->w[0].as<float>(), H, 64, H, sqrtf(2.0f / (float)TC), seed, ctx->stream);
+    if (e == cudaSuccess) e = wp_mlp_launch_init(m->w[2].as<float>(), H, H, H, sqrtf(2.0f / (float)H), seed + 1, ctx->stream);
+    if (e == cudaSuccess) e = wp_mlp_launch_init(m->w[4].as<float>(), Pp, H, m->P, sqrtf(1.0f / (float)H), seed + 2, ctx->stream);
+    ctx->launches += 3;
+    if (e != cudaSuccess) {
+        delete m;
+        return cuda_fail(ctx, e, "init network");
+    }
+    wp_status st = mlp_refresh(ctx, m);
+    if (st == WP_OK) st = mlp_finish(ctx, m);
+    if (st != WP_OK) {
+        delete m;
+        return st;
+    }
+    *out = m;
+    return WP_OK;
+}
+
+void wp_mlp_destroy(wp_mlp* m) {
+    if (!m) return;
+    cudaSetDevice(m->device);
+    delete m;
+}
+
+wp_status wp_mlp_train(wp_ctx* ctx, wp_mlp* m, long long num_reads, int batch, float lr, unsigned long long seed,
+                       double* out_mean_loss) {
+    if (!ctx || !m || num_reads < 0 || batch < 64 || batch % 64 || !(lr >= 0.0f)) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    wp_status st = mlp_check(ctx, m);
+    if (st != WP_OK) return st;
+    st = mlp_ensure(ctx, m, batch);
+    if (st != WP_OK) return st;
+    const long long steps = (num_reads + batch - 1) / batch;
+    std::vector<double> hl(batch);
+    double loss_sum = 0.0;
+    long long counted = 0;
+    for (long long k = 0; k < steps; k++) {
+        // fresh reads for every step: subsequence streams of seed + k
+        st = sim_device(ctx, batch, seed + (unsigned long long)k * 0x9E3779B97F4A7C15ull, m->xsim.as<float>(),
+                        nullptr, m->labels.as<int>(), nullptr);
+        if (st != WP_OK) return st;
+        MLP_CUDA(wp_mlp_launch_input(m->xsim.as<float>(), nullptr, batch, m->TC, m->X.as<bf16>(), ctx->stream), "input");
+        ctx->launches++;
+        {
+            TimedLaunch tl(ctx, 0);
+            st = mlp_step(ctx, m, batch, lr);
+            if (st != WP_OK) return st;
+        }
+        if (out_mean_loss && (k + 1 == steps || (k & 63) == 0)) {
+            // sample the loss every 64 steps and at the end
+            MLP_CUDA(cudaMemcpyAsync(hl.data(), m->loss.p, sizeof(double) * batch, cudaMemcpyDeviceToHost, ctx->stream),
+                     "copy loss");
+            MLP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+            double sl = 0.0;
+            for (double x : hl) sl += x;
+            loss_sum = sl / batch;
+            counted++;
+        }
+    }
+    st = mlp_finish(ctx, m);
+    if (st != WP_OK) return st;
+    if (out_mean_loss) *out_mean_loss = counted ? loss_sum : 0.0;
+    return WP_OK;
+}
+
+wp_status wp_mlp_train_step(wp_ctx* ctx, wp_mlp* m, const float* d_x, const int32_t* d_labels, int B, float lr,
+                            double* out_loss) {
+    if (!ctx || !m || !d_x || !d_labels || B < 64 || B % 64 || !(lr >= 0.0f)) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    wp_status st = mlp_check(ctx, m);
+    if (st != WP_OK) return st;
+    st = mlp_ensure(ctx, m, B);
+    if (st != WP_OK) return st;
+    MLP_CUDA(wp_mlp_launch_input(d_x, nullptr, B, m->TC, m->X.as<bf16>(), ctx->stream), "input");
+    MLP_CUDA(cudaMemcpyAsync(m->labels.p, d_labels, sizeof(int) * B, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
+    ctx->launches++;
+    st = mlp_step(ctx, m, B, lr);
+    if (st != WP_OK) return st;
+    st = mlp_finish(ctx, m);
+    if (st != WP_OK) return st;
+    if (out_loss) {
+        std::vector<double> hl(B);
+        MLP_CUDA(cudaMemcpy(hl.data(), m->loss.p, sizeof(double) * B, cudaMemcpyDeviceToHost), "copy loss");
+        double sl = 0.0;
+        for (double x : hl) sl += x;
+        *out_loss = sl / B;
+    }
+    return WP_OK;
+}
+
+wp_status wp_mlp_get(wp_mlp* m, int which, int grad, float* out) {
+    if (!m || which < 0 || which > 5 || !out) return WP_ERR_INVALID;
+    cudaSetDevice(m->device);
+    DevBuf& b = grad ? m->g[which] : m->w[which];
+    if (cudaMemcpy(out, b.p, sizeof(float) * m->n[which], cudaMemcpyDeviceToHost) != cudaSuccess) return WP_ERR_CUDA;
+    return WP_OK;
+}
+
+wp_status wp_mlp_set(wp_ctx* ctx, wp_mlp* m, int which, const float* in) {
+    if (!ctx || !m || which < 0 || which > 5 || !in) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    MLP_CUDA(cudaMemcpyAsync(m->w[which].p, in, sizeof(float) * m->n[which], cudaMemcpyHostToDevice, ctx->stream),
+             "copy");
+    wp_status st = mlp_refresh(ctx, m);
+    if (st != WP_OK) return st;
+    return mlp_finish(ctx, m);
+}
+
+wp_status wp_mlp_shape(const wp_mlp* m, int which, long long* rows, long long* cols) {
+    if (!m || which < 0 || which > 5) return WP_ERR_INVALID;
+    const long long r[6] = {m->H, m->H, m->H, m->H, m->Ppad, m->Ppad};
+    const long long c[6] = {64, 1, m->H, 1, m->H, 1};
+    if (rows) *rows = r[which];
+    if (cols) *cols = c[which];
+    return WP_OK;
+}
+
+wp_status wp_mlp_logits(wp_ctx* ctx, wp_mlp* m, const double* rads, int R, float* out) {
+    if (!ctx || !m || R < 0 || (R > 0 && (!rads || !out))) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    wp_status st = mlp_check(ctx, m);
+    if (st != WP_OK) return st;
+    if (R == 0) return WP_OK;
+    st = upload_reads(ctx, rads, R);
+    if (st != WP_OK) return st;
+    const int chunk = 8192;
+    st = mlp_ensure(ctx, m, chunk);
+    if (st != WP_OK) return st;
+    for (int r0 = 0; r0 < R; r0 += chunk) {
+        const int n = std::min(chunk, R - r0);
+        MLP_CUDA(wp_mlp_launch_input(nullptr, ctx->d_rads.as<double>() + (size_t)r0 * m->TC, n, m->TC, m->X.as<bf16>(),
+                                     ctx->stream), "input");
+        st = mlp_forward(ctx, m, n);
+        if (st != WP_OK) return st;
+        MLP_CUDA(cudaMemcpy2DAsync(out + (size_t)r0 * m->P, sizeof(float) * m->P, m->L.p, sizeof(float) * m->Ppad,
+                                   sizeof(float) * m->P, n, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    }
+    return mlp_finish(ctx, m);
+}
+
+wp_status wp_mlp_propose(wp_ctx* ctx, wp_mlp* m, const double* rads, int R, int h, int32_t* out_idx, float* out_prob,
+                         double* out_mass) {
+    if (!ctx || !m || R < 0 || h < 1 || h > 1024 || (R > 0 && (!rads || !out_idx || !out_prob))) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    wp_status st = mlp_check(ctx, m);
+    if (st != WP_OK) return st;
+    if (R == 0) return WP_OK;
+    if (h > m->P) return fail(ctx, WP_ERR_INVALID, "h exceeds the number of peptides");
+    st = upload_reads(ctx, rads, R);
+    if (st != WP_OK) return st;
+    MLP_CUDA(ctx->d_nn_cand_pep.ensure(sizeof(int) * (size_t)R * h), "alloc");
+    MLP_CUDA(ctx->d_nn_cand_score.ensure(sizeof(float) * (size_t)R * h), "alloc");
+    MLP_CUDA(ctx->d_nn_subfrac.ensure(sizeof(double) * R), "alloc");
+    st = mlp_propose_dev(ctx, m, ctx->d_rads.as<double>(), R, h, ctx->d_nn_cand_pep.as<int>(),
+                         reinterpret_cast<float*>(ctx->d_nn_cand_score.p), ctx->d_nn_subfrac.as<double>());
+    if (st != WP_OK) return st;
+    MLP_CUDA(cudaMemcpyAsync(out_idx, ctx->d_nn_cand_pep.p, sizeof(int) * (size_t)R * h, cudaMemcpyDeviceToHost,
+                             ctx->stream), "copy");
+    MLP_CUDA(cudaMemcpyAsync(out_prob, ctx->d_nn_cand_score.p, sizeof(float) * (size_t)R * h, cudaMemcpyDeviceToHost,
+                             ctx->stream), "copy");
+    if (out_mass)
+        MLP_CUDA(cudaMemcpyAsync(out_mass, ctx->d_nn_subfrac.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream),
+                 "copy");
+    return mlp_finish(ctx, m);
+}
+
+static wp_status mlp_hybrid_run(wp_ctx* ctx, wp_mlp* m, const double* d_rads, int R, int h, double dist_cutoff,
+                                int* d_id, double* d_score, double* d_total) {
+    MLP_CUDA(ctx->d_nn_cand_pep.ensure(sizeof(int) * (size_t)R * h), "alloc");
+    MLP_CUDA(ctx->d_nn_cand_score.ensure(sizeof(float) * (size_t)R * h), "alloc");
+    MLP_CUDA(ctx->d_nn_subfrac.ensure(sizeof(double) * R), "alloc");
+    MLP_CUDA(ctx->d_nn_ncand.ensure(sizeof(int) * R), "alloc");
+    wp_status st = mlp_propose_dev(ctx, m, d_rads, R, h, ctx->d_nn_cand_pep.as<int>(),
+                                   reinterpret_cast<float*>(ctx->d_nn_cand_score.p), ctx->d_nn_subfrac.as<double>());
+    if (st != WP_OK) return st;
+    // every read has h candidates: [R][h] is already the ragged layout
+    std::vector<int> off(R + 1), nc(R, h);
+    for (int r = 0; r <= R; r++) off[r] = r * h;
+    MLP_CUDA(ctx->d_nn_cand_off.ensure(sizeof(int) * (R + 1)), "alloc");
+    MLP_CUDA(cudaMemcpyAsync(ctx->d_nn_cand_off.p, off.data(), sizeof(int) * (R + 1), cudaMemcpyHostToDevice,
+                             ctx->stream), "copy");
+    MLP_CUDA(cudaMemcpyAsync(ctx->d_nn_ncand.p, nc.data(), sizeof(int) * R, cudaMemcpyHostToDevice, ctx->stream), "copy");
+    st = run_batch(ctx, d_rads, R, dist_cutoff, nullptr, off.data(), MODE_CLASSIFY, nullptr, d_id, d_score, d_total,
+                   nullptr, nullptr, ctx->d_nn_cand_pep.as<int>(), ctx->d_nn_cand_off.as<int>());
+    if (st != WP_OK) return st;
+    MLP_CUDA(wp_launch_hybrid_finish(ctx->d_nn_ncand.as<int>(), ctx->d_nn_subfrac.as<double>(), R, d_id, d_score,
+                                     d_total, ctx->stream), "finish");
+    ctx->launches++;
+    return WP_OK;
+}
+
+wp_status wp_mlp_hybrid_classify(wp_ctx* ctx, wp_mlp* m, const double* rads, int R, int h, double dist_cutoff,
+                                 int32_t* out_id, double* out_score, double* out_total) {
+    if (!ctx || !m || R < 0 || h < 1 || h > 1024 || (R > 0 && (!rads || !out_id || !out_score || !out_total)))
+        return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    wp_status st = mlp_check(ctx, m);
+    if (st != WP_OK) return st;
+    if (R == 0) return WP_OK;
+    if (h > m->P) return fail(ctx, WP_ERR_INVALID, "h exceeds the number of peptides");
+    st = upload_reads(ctx, rads, R);
+    if (st != WP_OK) return st;
+    MLP_CUDA(ctx->d_out_id.ensure(sizeof(int) * R), "alloc");
+    MLP_CUDA(ctx->d_out_score.ensure(sizeof(double) * R), "alloc");
+    MLP_CUDA(ctx->d_out_total.ensure(sizeof(double) * R), "alloc");
+    st = mlp_hybrid_run(ctx, m, ctx->d_rads.as<double>(), R, h, dist_cutoff, ctx->d_out_id.as<int>(),
+                        ctx->d_out_score.as<double>(), ctx->d_out_total.as<double>());
+    if (st != WP_OK) return st;
+    MLP_CUDA(cudaMemcpyAsync(out_id, ctx->d_out_id.p, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    MLP_CUDA(cudaMemcpyAsync(out_score, ctx->d_out_score.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    MLP_CUDA(cudaMemcpyAsync(out_total, ctx->d_out_total.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    st = finish(ctx);
+    if (st != WP_OK) return st;
+    return mlp_finish(ctx, m);
+}
+
+wp_status wp_mlp_hybrid_classify_device(wp_ctx* ctx, wp_mlp* m, const double* d_rads, int R, int h,
+                                        double dist_cutoff, int32_t* d_id, double* d_score, double* d_total) {
+    if (!ctx || !m || R < 0 || h < 1 || h > 1024 || (R > 0 && (!d_rads || !d_id || !d_score || !d_total)))
+        return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    wp_status st = mlp_check(ctx, m);
+    if (st != WP_OK) return st;
+    if (R == 0) return WP_OK;
+    if (h > m->P) return fail(ctx, WP_ERR_INVALID, "h exceeds the number of peptides");
+    st = mlp_hybrid_run(ctx, m, d_rads, R, h, dist_cutoff, d_id, d_score, d_total);
+    if (st != WP_OK) return st;
+    st = finish(ctx);
+    if (st != WP_OK) return st;
+    return mlp_finish(ctx, m);
 }
 
 }  // extern "C"

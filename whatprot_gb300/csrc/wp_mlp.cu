@@ -1,0 +1,333 @@
+// wp_mlp.cu -- the learned proposal network: an MLP from a radiometry
+// (T*C intensities, zero-padded to 64) to logits over the peptide set,
+//
+//     x -> GELU(W1 x + b1) -> GELU(W2 h1 + b2) -> W3 h2 + b3     (1024 wide)
+//
+// with BF16 weights and activations and FP32 accumulation on the tensor
+// cores (wp_gemm.cu), trained with softmax cross-entropy and Adam on reads
+// simulated on the GPU (wp_sim.cu), used to propose the top-H peptides that
+// the HMM then rescores, in place of the kNN stage of the hybrid classifier.
+// The reference has no such network; this file has no reference
+// counterpart.
+//
+// All products are C = A . B^T with K-major operands (wp_gemm_bf16_tn), so
+// the backward pass keeps transposed BF16 copies where an operand's
+// reduction dimension would otherwise be strided:
+//     dH2 = dL . W3         uses W3^T  [1024][P]
+//     dW3 = dL^T . H2       uses dL^T [P][B] and H2^T [1024][B]
+//     dH1 = dZ2 . W2        uses W2^T
+//     dW2 = dZ2^T . H1      uses dZ2^T, H1^T
+//     dW1 = dZ1^T . X       uses dZ1^T, X^T
+// Master weights, gradients and Adam moments are FP32.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <curand_kernel.h>
+#include <math.h>
+#include <stdint.h>
+
+typedef __nv_bfloat16 bf16;
+
+// Radiometries (FP32 or FP64, [B][TC]) to BF16 inputs [B][64] (zero padded).
+__global__ void wp_mlp_input_kernel(const float* __restrict__ xf, const double* __restrict__ xd, int B, int TC,
+                                    bf16* __restrict__ X) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long)B * 64) return;
+    const long b = i / 64;
+    const int d = (int)(i % 64);
+    float v = 0.f;
+    if (d < TC) v = xf ? xf[b * TC + d] : (float)xd[b * TC + d];
+    X[i] = __float2bfloat16_rn(v);
+}
+
+// out[c][r] = in[r][c] for a rows x cols BF16 matrix (pitches in elements).
+__global__ void wp_transpose_bf16_kernel(const bf16* __restrict__ in, int rows, int cols, int ld_in,
+                                         bf16* __restrict__ out, int ld_out) {
+    __shared__ unsigned short tile[32][33];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int r = r0 + j, c = c0 + threadIdx.x;
+        tile[j][threadIdx.x] = (r < rows && c < cols) ? __bfloat16_as_ushort(in[(long)r * ld_in + c]) : 0;
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int c = c0 + j, r = r0 + threadIdx.x;
+        if (c < cols && r < rows) out[(long)c * ld_out + r] = __ushort_as_bfloat16(tile[threadIdx.x][j]);
+    }
+}
+
+// Block-wide reductions in a fixed order (warp trees, then warp 0).
+__device__ float block_max(float v, float* sh) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = l < (int)(blockDim.x >> 5) ? sh[l] : -INFINITY;
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (l == 0) sh[0] = v;
+    }
+    __syncthreads();
+    return sh[0];
+}
+
+__device__ float block_sum(float v, float* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = l < (int)(blockDim.x >> 5) ? sh[l] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (l == 0) sh[0] = v;
+    }
+    __syncthreads();
+    return sh[0];
+}
+
+// One CTA per row: softmax over the first P logits, cross-entropy against
+// the label (rows with label < 0 are skipped: loss 0, gradient 0), and the
+// logit gradient (softmax - onehot) * scale as BF16 (zero past P).
+__global__ void wp_softmax_ce_kernel(const float* __restrict__ logits, int P, int ld, const int* __restrict__ labels,
+                                     float scale, bf16* __restrict__ dL, double* __restrict__ loss) {
+    __shared__ float sh[32];
+    const long row = blockIdx.x;
+    const float* l = logits + row * ld;
+    const int y = labels[row];
+    float mx = -INFINITY;
+    for (int j = threadIdx.x; j < P; j += blockDim.x) mx = fmaxf(mx, l[j]);
+    mx = block_max(mx, sh);
+    float s = 0.f;
+    for (int j = threadIdx.x; j < P; j += blockDim.x) s += expf(l[j] - mx);
+    s = block_sum(s, sh);
+    const float inv = 1.0f / s;
+    bf16* g = dL + row * ld;
+    for (int j = threadIdx.x; j < ld; j += blockDim.x) {
+        float v = 0.f;
+        if (y >= 0 && j < P) v = (expf(l[j] - mx) * inv - (j == y ? 1.f : 0.f)) * scale;
+        g[j] = __float2bfloat16_rn(v);
+    }
+    if (threadIdx.x == 0) loss[row] = y >= 0 ? (double)(logf(s) + mx - l[y]) : 0.0;
+}
+
+// dZ = dH * GELU'(Z), GELU(z) = z Phi(z):  GELU'(z) = Phi(z) + z phi(z).
+__global__ void wp_gelu_bwd_kernel(const float* __restrict__ dH, const bf16* __restrict__ Z, long n,
+                                   bf16* __restrict__ dZ) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float z = __bfloat162float(Z[i]);
+    const float d = 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+    dZ[i] = __float2bfloat16_rn(dH[i] * d);
+}
+
+// Column sums of a BF16 [rows][ld] matrix, one thread per column, rows in
+// order (deterministic).
+__global__ void wp_colsum_bf16_kernel(const bf16* __restrict__ M, int rows, int cols, int ld, float* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cols) return;
+    float s = 0.f;
+    for (int r = 0; r < rows; r++) s += __bfloat162float(M[(long)r * ld + c]);
+    out[c] = s;
+}
+
+// Adam (Kingma & Ba 2015) on FP32 master weights; refreshes the BF16 copy.
+__global__ void wp_adam_kernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                               float* __restrict__ v, long n, float lr, float b1, float b2, float eps, float bc1,
+                               float bc2, bf16* __restrict__ wb) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    w[i] = wi;
+    if (wb) wb[i] = __float2bfloat16_rn(wi);
+}
+
+__global__ void wp_f32_to_bf16_kernel(const float* __restrict__ in, long n, bf16* __restrict__ out) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = __float2bfloat16_rn(in[i]);
+}
+
+// Gaussian initialisation N(0, std^2) of rows [0, valid_rows) of a
+// [rows][cols] matrix (others zero), Philox stream per element.
+__global__ void wp_init_normal_kernel(float* __restrict__ w, long rows, long cols, long valid_rows, float std,
+                                      unsigned long long seed) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * cols) return;
+    if (i / cols >= valid_rows) {
+        w[i] = 0.f;
+        return;
+    }
+    curandStatePhilox4_32_10_t st;
+    curand_init(seed, (unsigned long long)i, 0ull, &st);
+    w[i] = std * curand_normal(&st);
+}
+
+// Sortable unsigned key of a float (ascending order of the floats).
+__device__ __forceinline__ unsigned fkey(float f) {
+    const unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// One CTA (256 threads) per read: the h largest of the first P logits by
+// (logit, index), by radix select on the sortable keys, then sorted
+// ascending; writes peptide indices and softmax probabilities, and the sum
+// of probability x peptide count over the candidates.
+__global__ void wp_topk_kernel(const float* __restrict__ logits, int P, int ld, int h, const int* __restrict__ counts,
+                               int* __restrict__ out_idx, float* __restrict__ out_prob, double* __restrict__ out_mass) {
+    __shared__ unsigned hist[256];
+    __shared__ float sh[32];
+    __shared__ unsigned long long skey[1024];
+    __shared__ int sidx[1024];
+    __shared__ int nsel;
+    const long row = blockIdx.x;
+    const float* l = logits + row * ld;
+    // softmax normaliser
+    float mx = -INFINITY;
+    for (int j = threadIdx.x; j < P; j += blockDim.x) mx = fmaxf(mx, l[j]);
+    mx = block_max(mx, sh);
+    float s = 0.f;
+    for (int j = threadIdx.x; j < P; j += blockDim.x) s += expf(l[j] - mx);
+    s = block_sum(s, sh);
+    // radix select of the h-th largest key (count based, from the top)
+    unsigned prefix = 0u, mask = 0u;
+    int want = min(h, P);
+    for (int pass = 0; pass < 4; pass++) {
+        const int shift = 24 - 8 * pass;
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0u;
+        __syncthreads();
+        for (int j = threadIdx.x; j < P; j += blockDim.x) {
+            const unsigned k = fkey(l[j]);
+            if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        __shared__ int sdigit, sbefore;
+        if (threadIdx.x == 0) {
+            int c = 0, d = 255;
+            for (; d > 0; d--) {
+                if (c + (int)hist[d] >= want) break;
+                c += (int)hist[d];
+            }
+            sdigit = d;
+            sbefore = c;
+        }
+        __syncthreads();
+        prefix |= (unsigned)sdigit << shift;
+        mask |= 255u << shift;
+        want -= sbefore;
+        __syncthreads();
+    }
+    // keys above the threshold, plus `want` of those equal to it with the
+    // largest indices (one thread walks the ties from the top index down)
+    if (threadIdx.x == 0) nsel = 0;
+    __syncthreads();
+    for (int j = threadIdx.x; j < P; j += blockDim.x) {
+        const unsigned k = fkey(l[j]);
+        if (k > prefix) {
+            const int pos = atomicAdd(&nsel, 1);
+            skey[pos] = ((unsigned long long)k << 32) | (unsigned)j;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int taken = 0;
+        for (int j = P - 1; j >= 0 && taken < want; j--)
+            if (fkey(l[j]) == prefix) {
+                skey[nsel++] = ((unsigned long long)prefix << 32) | (unsigned)j;
+                taken++;
+            }
+    }
+    __syncthreads();
+    const int n = nsel;
+    int n2 = 1;
+    while (n2 < n) n2 <<= 1;
+    for (int i = n + threadIdx.x; i < n2; i += blockDim.x) skey[i] = ~0ull;
+    __syncthreads();
+    for (int size = 2; size <= n2; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+                const int j = i ^ stride;
+                if (j > i) {
+                    const bool up = (i & size) == 0;
+                    const unsigned long long a = skey[i], b = skey[j];
+                    if ((a > b) == up) {
+                        skey[i] = b;
+                        skey[j] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int j = (int)(skey[i] & 0xffffffffu);
+        out_idx[row * h + i] = j;
+        out_prob[row * h + i] = expf(l[j] - mx) / s;
+        sidx[i] = j;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double mass = 0.0;
+        for (int i = 0; i < n; i++) mass += (double)(expf(l[sidx[i]] - mx) / s) * (double)counts[sidx[i]];
+        out_mass[row] = mass;
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+cudaError_t wp_mlp_launch_input(const float* xf, const double* xd, int B, int TC, bf16* X, cudaStream_t s) {
+    const long n = (long)B * 64;
+    if (n == 0) return cudaSuccess;
+    wp_mlp_input_kernel<<<(int)((n + 255) / 256), 256, 0, s>>>(xf, xd, B, TC, X);
+    return cudaGetLastError();
+}
+
+cudaError_t wp_mlp_launch_transpose(const bf16* in, int rows, int cols, int ld_in, bf16* out, int ld_out,
+                                    cudaStream_t s) {
+    dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
+    wp_transpose_bf16_kernel<<<grid, block, 0, s>>>(in, rows, cols, ld_in, out, ld_out);
+    return cudaGetLastError();
+}
+
+cudaError_t wp_mlp_launch_softmax_ce(const float* logits, int B, int P, int ld, const int* labels, float scale,
+                                     bf16* dL, double* loss, cudaStream_t s) {
+    wp_softmax_ce_kernel<<<B, 256, 0, s>>>(logits, P, ld, labels, scale, dL, loss);
+    return cudaGetLastError();
+}
+
+cudaError_t wp_mlp_launch_gelu_bwd(const float* dH, const bf16* Z, long n, bf16* dZ, cudaStream_t s) {
+    wp_gelu_bwd_kernel<<<(int)((n + 255) / 256), 256, 0, s>>>(dH, Z, n, dZ);
+    return cudaGetLastError();
+}
+
+cudaError_t wp_mlp_launch_colsum(const bf16* M, int rows, int cols, int ld, float* out, cudaStream_t s) {
+    wp_colsum_bf16_kernel<<<(cols + 255) / 256, 256, 0, s>>>(M, rows, cols, ld, out);
+    return cudaGetLastError();
+}
+
+cudaError_t wp_mlp_launch_adam(float* w, const float* g, float* m, float* v, long n, float lr, float b1, float b2,
+                               float eps, float bc1, float bc2, bf16* wb, cudaStream_t s) {
+    wp_adam_kernel<<<(int)((n + 255) / 256), 256, 0, s>>>(w, g, m, v, n, lr, b1, b2, eps, bc1, bc2, wb);
+    return cudaGetLastError();
+}
+
+cudaError_t wp_mlp_launch_to_bf16(const float* in, long n, bf16* out, cudaStream_t s) {
+    wp_f32_to_bf16_kernel<<<(int)((n + 255) / 256), 256, 0, s>>>(in, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t wp_mlp_launch_init(float* w, long rows, long cols, long valid_rows, float std, unsigned long long seed,
+                               cudaStream_t s) {
+    const long n = rows * cols;
+    wp_init_normal_kernel<<<(int)((n + 255) / 256), 256, 0, s>>>(w, rows, cols, valid_rows, std, seed);
+    return cudaGetLastError();
+}
+
+cudaError_t wp_mlp_launch_topk(const float* logits, int R, int P, int ld, int h, const int* counts, int* idx,
+                               float* prob, double* mass, cudaStream_t s) {
+    if (R == 0) return cudaSuccess;
+    wp_topk_kernel<<<R, 256, 0, s>>>(logits, P, ld, h, counts, idx, prob, mass);
+    return cudaGetLastError();
+}
