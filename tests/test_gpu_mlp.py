@@ -56,9 +56,11 @@ def test_gradients_match_oracle():
 
 
 def test_training_gains_recall_and_feeds_the_hmm():
-    """Training on GPU-simulated reads lowers the loss and raises recall@h
-    well above the untrained network; the HMM over the proposals then picks
-    the same peptide as the full HMM for most reads."""
+    """What the trained network gains: recall@h of the true peptide far
+    above the untrained network's, and the HMM over its proposals finds the
+    full HMM's best probability for almost every read (many peptides share
+    a dye-seq prefix and so tie exactly; which of the tied ids is reported is
+    not compared) at the full HMM's top-1 accuracy."""
     P, T = 150, 8
     ctx, sm, ds = _ctx(P, T=T, seed=9)
     try:
@@ -66,7 +68,7 @@ def test_training_gains_recall_and_feeds_the_hmm():
         rads, pep, _ = ctx.simulate_reads(3000, seed=99)
         ok = pep >= 0
         rads, pep = rads[ok], pep[ok]
-        h = 15
+        h = 40
 
         def recall():
             idx, prob, mass = net.propose(rads, h)
@@ -77,11 +79,18 @@ def test_training_gains_recall_and_feeds_the_hmm():
         last = net.train(400000, batch=1024, lr=1e-3, seed=2)
         r1 = recall()
         assert last < first - 0.5, (first, last)
-        assert r1 >= r0 + 0.3 and r1 >= 0.7, (r0, r1)
+        assert r0 <= 0.5 and r1 >= 0.95, (r0, r1)
+        logp = ctx.loglik_all(rads, 5.0)
         full_id, _, _, _ = ctx.classify(rads, 5.0)
         mid, msc, mtot = net.hybrid_classify(rads, h, 5.0)
-        agree = float(np.mean(mid == full_id))
-        assert agree >= 0.85, agree
+        index = {int(i): n for n, i in enumerate(ds.ids)}
+        best = logp.max(axis=1)
+        got = np.array([logp[r, index[int(mid[r])]] for r in range(len(mid))])
+        found = float(np.mean(got >= best - 1e-5))
+        assert found >= 0.95, found
+        acc_full = float(np.mean(full_id == ds.ids[pep]))
+        acc_hyb = float(np.mean(mid == ds.ids[pep]))
+        assert acc_hyb >= acc_full - 0.02, (acc_hyb, acc_full)
         net.close()
     finally:
         ctx.close()
