@@ -12,7 +12,7 @@ A step is one `classify hmm` pass over the batch: 100,000 x 1,000 =
 1e8 (read, peptide) forwards, argmax and count-weighted totals per read.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload classify|fit|hybrid]
+                    [--workload classify|fit|hybrid|learned]
 
 `--workload fit` measures the Baum-Welch E-step instead (reads/s): one
 dye-seq of 20 positions with 4/3/3 dyes on 3 channels (positions seeded),
@@ -26,6 +26,11 @@ dye-seqs as above, a dye-track training set of 100 simulated reads per
 dye-seq (about 945,000 unique tracks), kNN with k = 10,000 hits and sigma
 0.5, the top 1,000 candidates rescored by the HMM (pruning 5 sigma), 100,000
 query reads per step (--reads to change).
+
+`--workload learned` trains the proposal network (--epochs of 10,000,000
+reads simulated on the GPU) and measures the hybrid with its top-200
+proposals in place of the kNN stage on the hybrid workload's reads, next to
+the kNN hybrid's accuracy and speed on the same reads.
 
 Prints one JSON line (rank 0).  `value` is measured with the reads already in
 device memory (CUDA events on the library's stream, L2 flushed between
@@ -256,6 +261,118 @@ def run_reference_hybrid(args):
                              "sample": f"{n} reads per step"},
             "e2e": {"value": value, "unit": HY_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+LP_METRIC = "learned-proposal hybrid reads/s (MLP 48-1024-1024-20000 BF16, H=200 -> HMM -p 5)"
+LP_H, LP_HIDDEN, LP_EPOCH_READS, LP_BATCH = 200, 1024, 10_000_000, 4096
+LP_WORKLOAD = ("learned proposal: the hybrid workload's 20000 dye-seqs and query reads; MLP 48 -> 1024 -> 1024 -> "
+               "20000 logits (GELU), BF16 weights and activations, FP32 accumulation on the tensor cores, trained "
+               "with cross-entropy and Adam on 10,000,000 reads per epoch simulated on the GPU; top 200 proposals "
+               "rescored by the HMM (-p 5)")
+
+
+def run_learned(args):
+    import torch
+    from whatprot_gb300 import capi
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    torch.cuda.set_device(local)
+    reads = args.reads if args.reads != READS else HY_READS
+    sm, ds, dts, rads, true_ids = make_hybrid_data(seed=5050 + rank, reads=reads)
+    R = rads.shape[0]
+    ctx = capi.Context(local)
+    ctx.upload_model(sm, T)
+    ctx.upload_peptides(ds)
+    net = capi.ProposalNet(ctx, hidden=LP_HIDDEN, seed=11)
+    t0 = time.perf_counter()
+    losses = []
+    for ep in range(args.epochs):
+        losses.append(net.train(LP_EPOCH_READS, batch=LP_BATCH, lr=1e-3 if ep < args.epochs - 1 else 3e-4,
+                                seed=1000 + ep))
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=torch.device("cuda", local))
+    d_rads = torch.from_numpy(rads).to(f"cuda:{local}")
+    d_id = torch.empty(R, dtype=torch.int32, device=f"cuda:{local}")
+    d_sc = torch.empty(R, dtype=torch.float64, device=f"cuda:{local}")
+    d_tot = torch.empty(R, dtype=torch.float64, device=f"cuda:{local}")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def step():
+        net.hybrid_classify_device(d_rads.data_ptr(), R, LP_H, CUTOFF, d_id.data_ptr(), d_sc.data_ptr(),
+                                   d_tot.data_ptr())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ctx.timing_enable(True)
+    launches0 = ctx.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        step()
+        ev1.record(stream)
+        ev1.synchronize()
+        total_ms += ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    launches = ctx.launch_count() - launches0
+    fw_ms, _ = ctx.timing_read(4)
+    tk_ms, _ = ctx.timing_read(5)
+    hmm_ms, _ = ctx.timing_read(ctx.KIND_FORWARD)
+    ctx.timing_enable(False)
+    t_step = total_ms / args.steps
+    value = R / (t_step * 1e-3)
+    ids = d_id.cpu().numpy()
+    acc = float((ids == true_ids).mean())
+    idx, prob, mass = net.propose(rads, LP_H)
+    index = {int(i): n for n, i in enumerate(ds.ids)}
+    tidx = np.array([index[int(i)] for i in true_ids])
+    recall = float(np.mean(np.any(idx == tidx[:, None], axis=1)))
+    # the plain kNN hybrid on the same reads, for the comparison at matched accuracy
+    ctx.upload_tracks(dts)
+    t0 = time.perf_counter()
+    kid, _, _ = ctx.hybrid_classify(rads, HY_K, HY_SIG, HY_H, CUTOFF)
+    knn_s = time.perf_counter() - t0
+    knn_acc = float((kid == true_ids).mean())
+    h_rads = torch.from_numpy(rads).pin_memory().numpy()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        net.hybrid_classify(h_rads, LP_H, CUTOFF)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    fwd_flops = 2.0 * R * (64 * LP_HIDDEN + LP_HIDDEN * LP_HIDDEN + LP_HIDDEN * ((len(ds) + 63) // 64 * 64))
+    fw_step = fw_ms / args.steps
+    peak = None
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peak = json.load(f).get("bf16_tflops")
+    except OSError:
+        pass
+    achieved = fwd_flops / (fw_step * 1e-3) / 1e12 if fw_step > 0 else None
+    line = {"metric": LP_METRIC, "value": value, "unit": HY_UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 (network) / fp32 (HMM)", "data": "synthetic (seeded simulator)",
+            "config": {"workload": LP_WORKLOAD, "reads": R, "peptides": len(ds), "h": LP_H, "epochs": args.epochs,
+                       "epoch_reads": LP_EPOCH_READS, "batch": LP_BATCH, "l2": "flushed between steps (512 MB write)"},
+            "top1_vs_truth": acc, "recall_at_h": recall, "train_seconds": train_s, "train_loss_per_epoch": losses,
+            "knn_hybrid": {"reads_per_s_e2e": R / knn_s, "top1_vs_truth": knn_acc, "k": HY_K, "h": HY_H},
+            "roofline": {"bound": "tensor", "kernel": "wp_gemm_tn_kernel (forward layers)", "achieved": achieved,
+                         "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if (achieved and peak) else None,
+                         "traffic": None, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)",
+                         "algorithmic_flops_per_step": fwd_flops, "forward_ms_per_step": fw_step,
+                         "topk_ms_per_step": tk_ms / args.steps, "hmm_forward_ms_per_step": hmm_ms / args.steps},
+            "e2e": {"value": R / e2e_s, "unit": HY_UNIT, "h2d_bytes_per_step": int(rads.nbytes),
+                    "d2h_bytes_per_step": int(R * 20)},
+            "gpu_launches": launches, "clocks": clk}
+    print(json.dumps(line), flush=True)
+    net.close()
+    ctx.close()
 
 
 FIT_METRIC = "Baum-Welch E-step reads/s (fit, 1 dye-seq 4/3/3 dyes, no pruning)"
@@ -611,8 +728,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--reads", type=int, default=READS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="classify", choices=["classify", "fit", "hybrid"])
+    ap.add_argument("--workload", default="classify", choices=["classify", "fit", "hybrid", "learned"])
+    ap.add_argument("--epochs", type=int, default=3)
     args = ap.parse_args()
+    if args.workload == "learned":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned proposal"}))
+            return
+        return run_learned(args)
     if args.workload == "hybrid":
         return run_reference_hybrid(args) if args.impl == "reference" else run_hybrid(args)
     if args.workload == "fit":
