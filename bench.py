@@ -375,6 +375,44 @@ def run_learned(args):
     ctx.close()
 
 
+def run_gemm(args):
+    """The tensor-core GEMM alone on the proposal network's largest product
+    (logits of 8192 reads: M 8192, N 20032, K 1024), BF16 in, FP32 out."""
+    import torch
+    from whatprot_gb300 import capi
+    torch.cuda.set_device(0)
+    M, N, K = 8192, 20032, 1024
+    g = torch.Generator(device="cuda").manual_seed(1)
+    A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
+    for _ in range(args.warmup):
+        capi.gemm_bf16(A, B)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        capi.gemm_bf16(A, B)
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    t = sorted(ms)[len(ms) // 2]
+    flops = 2.0 * M * N * K
+    peak = None
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peak = json.load(f).get("bf16_tflops")
+    except OSError:
+        pass
+    tf = flops / (t * 1e-3) / 1e12
+    print(json.dumps({"metric": "tcgen05 BF16 GEMM TFLOP/s (M 8192, N 20032, K 1024, FP32 out)", "value": tf,
+                      "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t,
+                      "higher_is_better": True, "dtype": "bf16", "data": "synthetic",
+                      "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s",
+                                   "frac": tf / peak if peak else None, "traffic": None,
+                                   "kernel": "wp_gemm_tn_kernel"}}), flush=True)
+
+
 FIT_METRIC = "Baum-Welch E-step reads/s (fit, 1 dye-seq 4/3/3 dyes, no pruning)"
 FIT_UNIT = "reads/s"
 FIT_READS, FIT_LEN = 200_000, 20
@@ -728,9 +766,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--reads", type=int, default=READS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="classify", choices=["classify", "fit", "hybrid", "learned"])
+    ap.add_argument("--workload", default="classify", choices=["classify", "fit", "hybrid", "learned", "gemm"])
     ap.add_argument("--epochs", type=int, default=3)
     args = ap.parse_args()
+    if args.workload == "gemm":
+        return run_gemm(args)
     if args.workload == "learned":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the reference has no learned proposal"}))

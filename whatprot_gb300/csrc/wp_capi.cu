@@ -1417,18 +1417,21 @@ wp_status wp_simulate_reads(wp_ctx* ctx, int R, unsigned long long seed, double*
 
 wp_status wp_dev_gemm_bf16(const void* A, int lda, const void* B, int ldb, int M, int N, int K, void* C, int ldc,
                            int c_fp32, const float* bias, int act, void* Z) {
-    int* d_err = nullptr;
-    if (cudaMalloc(&d_err, sizeof(int)) != cudaSuccess) return WP_ERR_OOM;
-    cudaMemset(d_err, 0, sizeof(int));
-    cudaError_t e = wp_gemm_bf16_tn(A, lda, B, ldb, M, N, K, C, ldc, c_fp32, bias, act, Z, 0, d_err, 0);
-    if (e == cudaErrorInvalidValue) {
-        cudaFree(d_err);
-        return WP_ERR_INVALID;
+    // one error word per device, allocated on first use
+    static std::mutex mu;
+    static int* d_err[64] = {nullptr};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return WP_ERR_INVALID;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!d_err[dev] && cudaMalloc(&d_err[dev], sizeof(int)) != cudaSuccess) return WP_ERR_OOM;
     }
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaMemsetAsync(d_err[dev], 0, sizeof(int), 0);
+    cudaError_t e = wp_gemm_bf16_tn(A, lda, B, ldb, M, N, K, C, ldc, c_fp32, bias, act, Z, 0, d_err[dev], 0);
+    if (e == cudaErrorInvalidValue) return WP_ERR_INVALID;
     int err = 0;
-    if (e == cudaSuccess) e = cudaMemcpy(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost);
-    cudaFree(d_err);
+    if (e == cudaSuccess) e = cudaMemcpy(&err, d_err[dev], sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return WP_ERR_CUDA;
     return err ? WP_ERR_TIMEOUT : WP_OK;
 }

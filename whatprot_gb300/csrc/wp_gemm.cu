@@ -8,18 +8,21 @@
 // block of the learned proposal network (forward layers, and with
 // transposed operands its backward products).
 //
-// One CTA computes one 128 x 256 tile with 6 warps:
+// A persistent CTA per SM walks 128 x 256 output tiles with 6 warps:
 //   warp 0 (one thread)  TMA producer: 64-wide K slices of A and B into a
 //                        4-stage shared-memory ring (128-byte swizzle),
 //                        signalled on the stage's `full` mbarrier;
 //   warp 1 (one thread)  MMA issuer: four tcgen05.mma (M128 N256 K16) per
-//                        stage into a 256-column TMEM accumulator, then
+//                        stage into one of two 256-column TMEM accumulators,
 //                        tcgen05.commit onto the stage's `empty` mbarrier so
-//                        the producer can refill it; a last commit signals
-//                        the accumulator; warp 1 also owns the TMEM
-//                        allocation;
+//                        the producer can refill it, and onto the
+//                        accumulator's `full` mbarrier after the last K
+//                        slice; warp 1 also owns the TMEM allocation;
 //   warps 2-5            epilogue: each reads its 32 TMEM lanes (rows) in
-//                        32-column chunks with tcgen05.ld.
+//                        32-column chunks with tcgen05.ld, stages them in
+//                        shared memory, stores rows contiguously, and frees
+//                        the accumulator (its `empty` mbarrier) for the
+//                        tile after next.
 // Every mbarrier wait is bounded; on expiry the CTA records an error code,
 // stops issuing work, waits (bounded) for what it issued and frees its TMEM.
 #include <cuda.h>
@@ -27,6 +30,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+
+#include <algorithm>
 
 #define GEMM_BM 128
 #define GEMM_BN 256
@@ -37,6 +42,9 @@
 #define GEMM_A_STAGE (GEMM_BM * GEMM_BK * 2)  // 16 KB
 #define GEMM_B_STAGE (GEMM_BN * GEMM_BK * 2)  // 32 KB
 #define GEMM_WAIT_LIMIT (1L << 22)
+#define GEMM_SROW 36  // floats per row of the epilogue staging tile (32 + 4: conflict-free float4)
+
+typedef __nv_bfloat16 bf16_t;
 
 struct GemmParams {
     int M, N, K;
@@ -46,7 +54,7 @@ struct GemmParams {
     const float* bias;  // [N] or null
     int act;            // 0 none, 1 GELU (erf form)
     __nv_bfloat16* Z;   // pre-activation [M][ldc] BF16, or null
-    int accumulate;     // 1: C (FP32 only) += result
+    int accumulate;     // unused (must be 0)
     int* err;
 };
 
@@ -144,6 +152,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r) {
 
 __device__ __forceinline__ float gelu_erf(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Persistent: CTA b takes tiles b, b + gridDim.x, ... (M blocks fastest, so
+// the CTAs running at once share B tiles in L2).  Two TMEM accumulators
+// (2 x 256 columns): the MMA thread fills one while the epilogue warps drain
+// the other.  Epilogue stores go through a per-warp shared-memory tile so
+// that global stores are row-contiguous.
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
         wp_gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                           GemmParams p) {
@@ -151,28 +168,37 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(gemm_smem_raw) + 1023) & ~(uintptr_t)1023);
     uint8_t* sA = smem;
     uint8_t* sB = smem + GEMM_STAGES * GEMM_A_STAGE;
-    uint64_t* full = reinterpret_cast<uint64_t*>(sB + GEMM_STAGES * GEMM_B_STAGE);
+    float* stage_out = reinterpret_cast<float*>(sB + GEMM_STAGES * GEMM_B_STAGE);  // [4 warps][32][GEMM_SROW]
+    uint64_t* full = reinterpret_cast<uint64_t*>(stage_out + 4 * 32 * GEMM_SROW);
     uint64_t* empty = full + GEMM_STAGES;
-    uint64_t* accb = empty + GEMM_STAGES;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accb + 1);
+    uint64_t* acc_full = empty + GEMM_STAGES;  // [2]
+    uint64_t* acc_empty = acc_full + 2;        // [2]
+    uint64_t* done = acc_empty + 2;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n0 = blockIdx.x * GEMM_BN, m0 = blockIdx.y * GEMM_BM;
     const int nk = p.K / GEMM_BK;
+    const int mblocks = (p.M + GEMM_BM - 1) / GEMM_BM;
+    const int nblocks = (p.N + GEMM_BN - 1) / GEMM_BN;
+    const int ntiles = mblocks * nblocks;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < GEMM_STAGES; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(accb, 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4);
+        }
+        mbar_init(done, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(GEMM_TMEM_COLS)
+                     "r"(2 * GEMM_TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -183,49 +209,76 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 
     if (warp == 0) {
         if (lane == 0) {
-            // TMA producer
-            for (int kt = 0; kt < nk; kt++) {
-                const int s = kt % GEMM_STAGES, round = kt / GEMM_STAGES;
-                if (*abort_flag || !mbar_wait(&empty[s], (round & 1) ^ 1, p.err, 101)) {
-                    *abort_flag = 1;
-                    break;
+            // TMA producer over every (tile, k) of this CTA
+            int it = 0;
+            for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+                const int m0 = (t % mblocks) * GEMM_BM, n0 = (t / mblocks) * GEMM_BN;
+                for (int kt = 0; kt < nk; kt++, it++) {
+                    const int s = it % GEMM_STAGES, round = it / GEMM_STAGES;
+                    if (*abort_flag || !mbar_wait(&empty[s], (round & 1) ^ 1, p.err, 101)) {
+                        *abort_flag = 1;
+                        break;
+                    }
+                    mbar_expect_tx(&full[s], GEMM_A_STAGE + GEMM_B_STAGE);
+                    tma_load_2d(sA + s * GEMM_A_STAGE, &tmA, kt * GEMM_BK, m0, &full[s]);
+                    tma_load_2d(sB + s * GEMM_B_STAGE, &tmB, kt * GEMM_BK, n0, &full[s]);
                 }
-                mbar_expect_tx(&full[s], GEMM_A_STAGE + GEMM_B_STAGE);
-                tma_load_2d(sA + s * GEMM_A_STAGE, &tmA, kt * GEMM_BK, m0, &full[s]);
-                tma_load_2d(sB + s * GEMM_B_STAGE, &tmB, kt * GEMM_BK, n0, &full[s]);
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
             // MMA issuer
             const uint32_t idesc = gemm_idesc(GEMM_BM, GEMM_BN);
-            for (int kt = 0; kt < nk; kt++) {
-                const int s = kt % GEMM_STAGES, round = kt / GEMM_STAGES;
-                if (*abort_flag || !mbar_wait(&full[s], round & 1, p.err, 102)) {
+            int it = 0, li = 0;
+            for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x, li++) {
+                const int b = li & 1, use = li >> 1;
+                if (!mbar_wait(&acc_empty[b], (use & 1) ^ 1, p.err, 105)) {
                     *abort_flag = 1;
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t a0 = smem_u32(sA + s * GEMM_A_STAGE), b0 = smem_u32(sB + s * GEMM_B_STAGE);
+                const uint32_t acc = tmem + (uint32_t)(b * GEMM_TMEM_COLS);
+                bool ok = true;
+                for (int kt = 0; kt < nk; kt++, it++) {
+                    const int s = it % GEMM_STAGES, round = it / GEMM_STAGES;
+                    if (*abort_flag || !mbar_wait(&full[s], round & 1, p.err, 102)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t a0 = smem_u32(sA + s * GEMM_A_STAGE), b0 = smem_u32(sB + s * GEMM_B_STAGE);
 #pragma unroll
-                for (int k = 0; k < GEMM_BK / 16; k++)
-                    mma_bf16(tmem, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), idesc, (kt | k) != 0 ? 1u : 0u);
-                mma_commit(&empty[s]);
+                    for (int k = 0; k < GEMM_BK / 16; k++)
+                        mma_bf16(acc, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), idesc, (kt | k) != 0 ? 1u : 0u);
+                    mma_commit(&empty[s]);
+                }
+                if (!ok) {
+                    *abort_flag = 1;
+                    break;
+                }
+                mma_commit(&acc_full[b]);
             }
-            mma_commit(accb);  // always: the accumulator (or the teardown) waits on it
+            mma_commit(done);  // every MMA this thread issued has completed when this arrives
         }
     } else {
         // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31
         const int q = warp & 3;
-        const bool ok = mbar_wait(accb, 0, p.err, 103);
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (ok && !*abort_flag) {
-            const int row = m0 + 32 * q + lane;
+        float* st = stage_out + q * 32 * GEMM_SROW;
+        int li = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, li++) {
+            const int b = li & 1, use = li >> 1;
+            const int m0 = (t % mblocks) * GEMM_BM, n0 = (t / mblocks) * GEMM_BN;
+            if (*abort_flag || !mbar_wait(&acc_full[b], use & 1, p.err, 103)) {
+                *abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int rbase = m0 + 32 * q;
             for (int ch = 0; ch < GEMM_BN / 32; ch++) {
                 uint32_t r[32];
-                tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(ch * 32), r);
+                tmem_ld32(tmem + (uint32_t)(b * GEMM_TMEM_COLS) + ((uint32_t)(32 * q) << 16) + (uint32_t)(ch * 32), r);
                 const int c0 = n0 + ch * 32;
-                if (row >= p.M || c0 >= p.N) continue;
+                if (c0 >= p.N || rbase >= p.M) continue;  // warp-uniform
                 float v[32];
 #pragma unroll
                 for (int j = 0; j < 32; j++) {
@@ -233,47 +286,90 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                     if (p.bias) x += (c0 + j < p.N) ? p.bias[c0 + j] : 0.0f;
                     v[j] = x;
                 }
-                const long rowoff = (long)row * p.ldc;
-                if (p.Z) {
-                    __nv_bfloat16* z = p.Z + rowoff + c0;
-                    for (int j = 0; j < 32; j++)
-                        if (c0 + j < p.N) z[j] = __float2bfloat16_rn(v[j]);
-                }
-                if (p.act == 1) {
+                // two passes through the staging tile: pre-activation, output
+                for (int pass = p.Z ? 0 : 1; pass < 2; pass++) {
+                    float o[32];
 #pragma unroll
-                    for (int j = 0; j < 32; j++) v[j] = gelu_erf(v[j]);
-                }
-                if (p.c_fp32) {
-                    float* c = reinterpret_cast<float*>(p.C) + rowoff + c0;
-                    for (int j = 0; j < 32; j++)
-                        if (c0 + j < p.N) c[j] = p.accumulate ? c[j] + v[j] : v[j];
-                } else {
-                    __nv_bfloat16* c = reinterpret_cast<__nv_bfloat16*>(p.C) + rowoff + c0;
-                    if (c0 + 32 <= p.N && (p.ldc % 8) == 0) {
-                        // 4 x 16-byte stores of 8 BF16 each
+                    for (int j = 0; j < 32; j++) o[j] = (pass == 1 && p.act == 1) ? gelu_erf(v[j]) : v[j];
+                    const bool f32 = pass == 1 && p.c_fp32;
+                    __syncwarp();
+                    if (f32) {
 #pragma unroll
-                        for (int g = 0; g < 4; g++) {
-                            __align__(16) __nv_bfloat16 t[8];
+                        for (int j = 0; j < 32; j += 4)
+                            *reinterpret_cast<float4*>(st + lane * GEMM_SROW + j) = make_float4(o[j], o[j + 1], o[j + 2], o[j + 3]);
+                    } else {
+                        uint32_t* su = reinterpret_cast<uint32_t*>(st + lane * GEMM_SROW);
 #pragma unroll
-                            for (int j = 0; j < 8; j++) t[j] = __float2bfloat16_rn(v[g * 8 + j]);
-                            *reinterpret_cast<uint4*>(c + g * 8) = *reinterpret_cast<const uint4*>(t);
+                        for (int j = 0; j < 16; j += 4) {
+                            uint4 u;
+                            __nv_bfloat162 h0 = __floats2bfloat162_rn(o[2 * j], o[2 * j + 1]);
+                            __nv_bfloat162 h1 = __floats2bfloat162_rn(o[2 * j + 2], o[2 * j + 3]);
+                            __nv_bfloat162 h2 = __floats2bfloat162_rn(o[2 * j + 4], o[2 * j + 5]);
+                            __nv_bfloat162 h3 = __floats2bfloat162_rn(o[2 * j + 6], o[2 * j + 7]);
+                            u.x = *reinterpret_cast<uint32_t*>(&h0);
+                            u.y = *reinterpret_cast<uint32_t*>(&h1);
+                            u.z = *reinterpret_cast<uint32_t*>(&h2);
+                            u.w = *reinterpret_cast<uint32_t*>(&h3);
+                            *reinterpret_cast<uint4*>(su + j) = u;
+                        }
+                    }
+                    __syncwarp();
+                    // row-contiguous stores: FP32 rows are 8 x 16 B (8 lanes
+                    // per row, 4 rows per pass), BF16 rows 4 x 16 B
+                    const bool full_cols = c0 + 32 <= p.N;
+                    if (f32) {
+                        float* C = reinterpret_cast<float*>(p.C);
+                        for (int i = 0; i < 8; i++) {
+                            const int rr = i * 4 + (lane >> 3), cc = (lane & 7) * 4;
+                            const int row = rbase + rr;
+                            if (row >= p.M) continue;
+                            const float4 val = *reinterpret_cast<const float4*>(st + rr * GEMM_SROW + cc);
+                            float* dst = C + (long)row * p.ldc + c0 + cc;
+                            if (full_cols && (p.ldc & 3) == 0) {
+                                *reinterpret_cast<float4*>(dst) = val;
+                            } else {
+                                const float e4[4] = {val.x, val.y, val.z, val.w};
+                                for (int j = 0; j < 4; j++)
+                                    if (c0 + cc + j < p.N) dst[j] = e4[j];
+                            }
                         }
                     } else {
-                        for (int j = 0; j < 32; j++)
-                            if (c0 + j < p.N) c[j] = __float2bfloat16_rn(v[j]);
+                        bf16_t* D = pass == 0 ? p.Z : reinterpret_cast<bf16_t*>(p.C);
+                        const uint32_t* su = reinterpret_cast<const uint32_t*>(st);
+                        for (int i = 0; i < 4; i++) {
+                            const int rr = i * 8 + (lane >> 2), cw = (lane & 3) * 4;  // 4 words = 8 BF16
+                            const int row = rbase + rr;
+                            if (row >= p.M) continue;
+                            const uint4 val = *reinterpret_cast<const uint4*>(su + rr * GEMM_SROW + cw);
+                            bf16_t* dst = D + (long)row * p.ldc + c0 + 2 * cw;
+                            if (full_cols && (p.ldc & 7) == 0) {
+                                *reinterpret_cast<uint4*>(dst) = val;
+                            } else {
+                                const uint32_t w4[4] = {val.x, val.y, val.z, val.w};
+                                for (int j = 0; j < 8; j++)
+                                    if (c0 + 2 * cw + j < p.N) {
+                                        const uint32_t wv = w4[j >> 1];
+                                        const unsigned short hv = (j & 1) ? (unsigned short)(wv >> 16) : (unsigned short)(wv & 0xffffu);
+                                        dst[j] = __ushort_as_bfloat16(hv);
+                                    }
+                            }
+                        }
                     }
                 }
             }
+            // this accumulator may be refilled
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[b]);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 1) {
-        // the MMAs must be done before the columns are freed (bounded wait;
-        // the accumulator phase has completed once the epilogue read it)
-        if (*abort_flag) mbar_wait(accb, 0, p.err, 104);
+        // free the columns only after every issued MMA has completed
+        mbar_wait(done, 0, p.err, 104);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(GEMM_TMEM_COLS)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * GEMM_TMEM_COLS)
                      : "memory");
     }
 }
@@ -310,7 +406,7 @@ static bool make_map(CUtensorMap* map, const void* ptr, int rows, int K, int ld,
 }
 
 size_t wp_gemm_smem_bytes() {
-    return 1024 + GEMM_STAGES * (GEMM_A_STAGE + GEMM_B_STAGE) + (2 * GEMM_STAGES + 1) * 8 + 16;
+    return 1024 + GEMM_STAGES * (GEMM_A_STAGE + GEMM_B_STAGE) + 4 * 32 * GEMM_SROW * 4 + (2 * GEMM_STAGES + 5) * 8 + 16;
 }
 
 // C = act(A . B^T + bias).  A: [M][K] (pitch lda), B: [N][K] (pitch ldb),
@@ -321,7 +417,7 @@ cudaError_t wp_gemm_bf16_tn(const void* A, int lda, const void* B, int ldb, int 
                             int c_fp32, const float* bias, int act, void* Z, int accumulate, int* err,
                             cudaStream_t s) {
     if (M <= 0 || N <= 0 || K <= 0 || K % GEMM_BK != 0 || lda % 8 || ldb % 8 || lda < K || ldb < K || ldc < N ||
-        ((uintptr_t)A & 15) || ((uintptr_t)B & 15) || (accumulate && !c_fp32))
+        ((uintptr_t)A & 15) || ((uintptr_t)B & 15) || accumulate)
         return cudaErrorInvalidValue;
     CUtensorMap ma, mb;
     if (!make_map(&ma, A, M, K, lda, GEMM_BM) || !make_map(&mb, B, N, K, ldb, GEMM_BN)) return cudaErrorInvalidValue;
@@ -339,7 +435,12 @@ cudaError_t wp_gemm_bf16_tn(const void* A, int lda, const void* B, int ldb, int 
     p.err = err;
     const size_t smem = wp_gemm_smem_bytes();
     cudaFuncSetAttribute(wp_gemm_tn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    dim3 grid((N + GEMM_BN - 1) / GEMM_BN, (M + GEMM_BM - 1) / GEMM_BM);
+    static int sms[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && sms[dev] == 0) cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    const int tiles = ((M + GEMM_BM - 1) / GEMM_BM) * ((N + GEMM_BN - 1) / GEMM_BN);
+    const int grid = std::min(tiles, (dev >= 0 && dev < 64 && sms[dev] > 0) ? sms[dev] : 148);
     wp_gemm_tn_kernel<<<grid, GEMM_THREADS, smem, s>>>(ma, mb, p);
     return cudaGetLastError();
 }
