@@ -159,6 +159,11 @@ wp_status wp_fit_begin(wp_ctx* ctx, const int16_t* dye_seq, int length,
 wp_status wp_fit_estep(wp_ctx* ctx, wp_fit_sums* out, double* sum_logp,
                        int* num_zero);
 
+/* E-step kernel choice: 0 (default) one CTA per read with its vectors in
+ * shared memory when they fit, else one thread per read; 1 always one
+ * thread per read (tests compare the two).  No reference counterpart. */
+wp_status wp_fit_set_kernel(wp_ctx* ctx, int kind);
+
 /* Which parameters a fit holds at their starting values: FitSettings and
  * ChannelFitSettings (parameterization/settings/fit-settings.h,
  * channel-fit-settings.h).  Non-zero = hold. */

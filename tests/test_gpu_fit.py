@@ -70,9 +70,11 @@ ESTEP_CASES = [
 ]
 
 
+@pytest.mark.parametrize("kernel", [0, 1], ids=["cta", "thread"])
 @pytest.mark.parametrize("case", ESTEP_CASES, ids=[f"C{c[0]}T{c[1]}{'B' if c[4] else ''}" for c in ESTEP_CASES])
-def test_estep_vs_oracle(gpu_ctx, oracle, case):
+def test_estep_vs_oracle(gpu_ctx, oracle, case, kernel):
     C, T, seq_str, n, block = case
+    gpu_ctx.fit_set_kernel(kernel)
     sm = _model(C, block)
     seq = parse_dye_seq(seq_str)
     rads = _reads(sm, seq, T, n, seed=7 * len(seq_str) + C)
@@ -83,6 +85,7 @@ def test_estep_vs_oracle(gpu_ctx, oracle, case):
     gpu_ctx.upload_model(sm, T)
     gpu_ctx.fit_begin(seq, rads)
     s, sl, nz = gpu_ctx.fit_estep()
+    gpu_ctx.fit_set_kernel(0)
     g = s.as_dict(T, C)
     o, lps = _oracle_sums(oracle, sm, T, seq, rads)
     assert nz == int(np.sum(~np.isfinite(lps)))

@@ -30,7 +30,7 @@ EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload"
            "wp_peptides_upload", "wp_hmm_classify", "wp_hmm_classify_device",
            "wp_hmm_loglik_all", "wp_hmm_count_flops", "wp_launch_count", "wp_ctx_stream",
            "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak", "wp_last_batch_stats",
-           "wp_fit_begin", "wp_fit_estep", "wp_hmm_fit", "wp_fit_offset_exponential",
+           "wp_fit_begin", "wp_fit_estep", "wp_hmm_fit", "wp_fit_offset_exponential", "wp_fit_set_kernel",
            "wp_nn_tracks_upload", "wp_nn_classify", "wp_hybrid_classify", "wp_hybrid_classify_device",
            "wp_dev_gemm_bf16", "wp_simulate_reads", "wp_mlp_create", "wp_mlp_destroy", "wp_mlp_train",
            "wp_mlp_train_step", "wp_mlp_shape", "wp_mlp_get", "wp_mlp_set", "wp_mlp_logits", "wp_mlp_propose",
@@ -155,6 +155,8 @@ def load_library(path: Optional[str] = None):
     lib.wp_probe_fp32_peak.restype = I
     lib.wp_last_batch_stats.argtypes = [V, V]
     lib.wp_last_batch_stats.restype = I
+    lib.wp_fit_set_kernel.argtypes = [V, I]
+    lib.wp_fit_set_kernel.restype = I
     lib.wp_fit_begin.argtypes = [V, V, I, V, I]
     lib.wp_fit_begin.restype = I
     lib.wp_fit_estep.argtypes = [V, ctypes.POINTER(WpFitSums), ctypes.POINTER(D), ctypes.POINTER(I)]
@@ -342,6 +344,10 @@ class Context:
         rads = np.ascontiguousarray(rads, dtype=np.float64)
         self._check(self.lib.wp_fit_begin(self.h, _ptr(seq) if len(seq) else None, len(seq),
                                           _ptr(rads), rads.shape[0]))
+
+    def fit_set_kernel(self, kind: int) -> None:
+        """wp_fit_set_kernel: 0 CTA per read where it fits (default), 1 thread per read."""
+        self._check(self.lib.wp_fit_set_kernel(self.h, kind))
 
     def fit_estep(self):
         """wp_fit_estep with the current model: (WpFitSums, sum log P, reads with P == 0)."""

@@ -78,6 +78,11 @@ int wp_nn_select_warps();
 int wp_nn_hmax();
 __global__ void wp_fit_reduce_kernel(const double*, long, int, double*);
 int wp_fit_nslots(int T, int C);
+size_t wp_fit_cta_smem_bytes(int T, int C, int S, bool has_block);
+long wp_fit_cta_ckpt_floats(int T, int S, bool has_block);
+cudaError_t wp_launch_fit_cta(bool has_block, int grid, size_t smem, cudaStream_t s, const FitArgs& a, float* ckpt,
+                              long ck_stride);
+int wp_fit_cta_ctas_per_sm(bool has_block, size_t smem);
 long wp_fit_floats_per_thread(int T, int C, int S, bool has_block);
 
 namespace {
@@ -156,6 +161,7 @@ struct wp_ctx {
 
     // Staged Baum-Welch fit.
     bool have_fit = false;
+    bool fit_force_thread = false;  // tests: run the thread-per-read E-step
     int fit_R = 0, fit_T = 0, fit_C = 0;
     int fit_D[WP_MAX_CHANNELS] = {0, 0, 0, 0};
     int fit_dmax = 0;
@@ -1130,6 +1136,13 @@ wp_status wp_internal_fail(wp_ctx* ctx, wp_status code, const char* msg) {
 
 extern "C" {
 
+wp_status wp_fit_set_kernel(wp_ctx* ctx, int kind) {
+    if (!ctx || kind < 0 || kind > 1) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->fit_force_thread = kind == 1;
+    return WP_OK;
+}
+
 wp_status wp_fit_begin(wp_ctx* ctx, const int16_t* dye_seq, int length, const double* rads, int R) {
     if (!ctx || length < 0 || R < 0 || (length > 0 && !dye_seq) || (R > 0 && !rads)) return WP_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -1194,15 +1207,32 @@ wp_status wp_fit_estep(wp_ctx* ctx, wp_fit_sums* out, double* sum_logp, int* num
     for (int c = 0; c < C; c++) S *= ctx->fit_D[c] + 1;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    const int threads = 128;
-    long want = std::min<long>((long)R, (long)sms * 4 * threads);
-    const long per = wp_fit_floats_per_thread(T, C, S, hb);
-    // keep the scratch under 16 GiB
-    while (want > threads && (double)want * per * 4.0 > 16.0 * (1u << 30)) want /= 2;
-    const int grid = (int)((want + threads - 1) / threads);
-    const long nth = (long)grid * threads;
     const int nslots = wp_fit_nslots(T, C);
-    WP_CUDA(ctx->d_fit_scratch.ensure(sizeof(float) * (size_t)nth * per), "alloc fit scratch");
+    // CTA-per-read kernel when a read's vectors fit shared memory, else the
+    // thread-per-read kernel over a global slab.
+    const size_t cta_smem = wp_fit_cta_smem_bytes(T, C, S, hb);
+    // (the kernel also holds the binomial tables in static shared memory)
+    const int cta_per_sm = (long)cta_smem + (long)sizeof(SmemModel) <= (long)ctx->smem_optin
+                                   ? wp_fit_cta_ctas_per_sm(hb, cta_smem)
+                                   : 0;
+    const bool use_cta = cta_per_sm > 0 && !ctx->fit_force_thread;
+    const int threads = 128;
+    int grid = 0;
+    long nth = 0, per = 0, ck_stride = 0;
+    if (use_cta) {
+        grid = (int)std::min<long>((long)R, (long)sms * cta_per_sm);
+        nth = grid;
+        ck_stride = wp_fit_cta_ckpt_floats(T, S, hb);
+        WP_CUDA(ctx->d_fit_scratch.ensure(sizeof(float) * (size_t)grid * ck_stride), "alloc fit checkpoints");
+    } else {
+        long want = std::min<long>((long)R, (long)sms * 4 * threads);
+        per = wp_fit_floats_per_thread(T, C, S, hb);
+        // keep the scratch under 16 GiB
+        while (want > threads && (double)want * per * 4.0 > 16.0 * (1u << 30)) want /= 2;
+        grid = (int)((want + threads - 1) / threads);
+        nth = (long)grid * threads;
+        WP_CUDA(ctx->d_fit_scratch.ensure(sizeof(float) * (size_t)nth * per), "alloc fit scratch");
+    }
     WP_CUDA(ctx->d_fit_sums.ensure(sizeof(double) * (size_t)nth * nslots), "alloc fit sums");
     WP_CUDA(ctx->d_fit_out.ensure(sizeof(double) * nslots), "alloc fit sums");
     WP_CUDA(ctx->d_fit_logp.ensure(sizeof(double) * R), "alloc fit logp");
@@ -1232,7 +1262,11 @@ wp_status wp_fit_estep(wp_ctx* ctx, wp_fit_sums* out, double* sum_logp, int* num
     fa.nslots = nslots;
     {
         TimedLaunch tl(ctx, 0);
-        WP_CUDA(wp_launch_fit_estep(hb, grid, threads, ctx->stream, fa), "fit E-step launch");
+        if (use_cta)
+            WP_CUDA(wp_launch_fit_cta(hb, grid, cta_smem, ctx->stream, fa, ctx->d_fit_scratch.as<float>(), ck_stride),
+                    "fit E-step launch");
+        else
+            WP_CUDA(wp_launch_fit_estep(hb, grid, threads, ctx->stream, fa), "fit E-step launch");
         ctx->launches++;
     }
     wp_fit_reduce_kernel<<<(nslots + 63) / 64, 64, 0, ctx->stream>>>(fa.sums, nth, nslots, ctx->d_fit_out.as<double>());

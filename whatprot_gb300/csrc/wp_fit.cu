@@ -575,3 +575,611 @@ cudaError_t wp_launch_fit_estep(bool has_block, int grid, int threads, cudaStrea
         wp_fit_estep_kernel<false><<<grid, threads, 0, s>>>(a);
     return cudaGetLastError();
 }
+
+// ===========================================================================
+// CTA-per-read E-step.  The same computation as wp_fit_estep_kernel, with
+// one read per CTA at a time (persistent over reads) and the states spread
+// over the CTA's threads: the backward vectors of one timestep, the current
+// backward vector and two forward vectors live in shared memory; only the
+// T+1 checkpoints go to global memory (per-CTA slots, L2-resident for a
+// persistent grid).  Per-term FP32 partials are reduced across the CTA once
+// per timestep in a fixed order and accumulated in FP64 per CTA; the CTAs'
+// sums are added in CTA order by wp_fit_reduce_kernel.
+// ===========================================================================
+#define FIT_NT 256
+#define FIT_MAXTERMS (6 + 2 * WP_MAX_CHANNELS)
+
+// Loop over state indices i = tid, tid + NT, ... < n with the slice e = i / S
+// and dye-count index j = i % S kept incrementally (no division per state).
+#define FOR_STATES(n, S, i, e, j)                                                                  \
+    for (long i = threadIdx.x, e = threadIdx.x / (S), j = threadIdx.x % (S); i < (n);              \
+         i += blockDim.x, e += blockDim.x / (S), j += blockDim.x % (S), e += (j >= (S)) ? 1 : 0, \
+              j -= (j >= (S)) ? (S) : 0)
+
+struct SVec {
+    float* A;
+    float* B;
+    float* pd;
+};
+
+__device__ __forceinline__ int fcoord(const uint32_t* coords, int j, int c) { return (coords[j] >> (4 * c)) & 15; }
+
+// Sum (or max) of n values per thread across the CTA, fixed order: shuffle
+// tree per warp, then warp 0 over the warps.  Result in out[0..n) for all.
+template <bool MAX>
+__device__ void cta_reduce(float* v, int n, float* red, float* out) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = 0; k < n; k++) {
+        float x = v[k];
+        for (int o = 16; o > 0; o >>= 1) {
+            const float y = __shfl_down_sync(0xffffffffu, x, o);
+            x = MAX ? fmaxf(x, y) : x + y;
+        }
+        if (lane == 0) red[k * 32 + w] = x;
+    }
+    __syncthreads();
+    if (w == 0) {
+        for (int k = 0; k < n; k++) {
+            float x = lane < nw ? red[k * 32 + lane] : (MAX ? -INFINITY : 0.f);
+            for (int o = 16; o > 0; o >>= 1) {
+                const float y = __shfl_down_sync(0xffffffffu, x, o);
+                x = MAX ? fmaxf(x, y) : x + y;
+            }
+            if (lane == 0) out[k] = x;
+        }
+    }
+    __syncthreads();
+}
+
+template <bool HB>
+__device__ __forceinline__ void cta_emit(const SVec& in, const SVec& out, const float* w, int S, long n) {
+    FOR_STATES(n, S, i, e, j) {
+        const float f = w[j];
+        out.A[i] = f * in.A[i];
+        if (HB) out.B[i] = f * in.B[i];
+    }
+    if (threadIdx.x == 0) *out.pd = w[0] * *in.pd;
+    __syncthreads();
+}
+
+// Binomial along channel c over E slices: forward (out[x] = sum_{from >= x}
+// p(from, x) in[from]) or its transpose.
+template <bool HB>
+__device__ void cta_binomial(const SVec& in, const SVec& out, const uint32_t* coords, int S, int E, int c, int Wc,
+                             int stc, const float* tab, bool backward) {
+    const long n = (long)E * S;
+    FOR_STATES(n, S, i, e, j) {
+        const int x = fcoord(coords, (int)j, c);
+        float acc = 0.f, accb = 0.f;
+        if (!backward) {
+            for (int from = x; from < Wc; from++) {
+                const float p = tab[from * (from + 1) / 2 + x];
+                const long k = i + (long)(from - x) * stc;
+                acc = fmaf(p, in.A[k], acc);
+                if (HB) accb = fmaf(p, in.B[k], accb);
+            }
+        } else {
+            for (int to = 0; to <= x; to++) {
+                const float p = tab[x * (x + 1) / 2 + to];
+                const long k = i - (long)(x - to) * stc;
+                acc = fmaf(p, in.A[k], acc);
+                if (HB) accb = fmaf(p, in.B[k], accb);
+            }
+        }
+        out.A[i] = acc;
+        if (HB) out.B[i] = accb;
+    }
+    if (threadIdx.x == 0) *out.pd = *in.pd;
+    __syncthreads();
+}
+
+template <bool HB>
+__global__ void __launch_bounds__(FIT_NT) wp_fit_cta_kernel(FitArgs a, float* ckpt, long ck_stride) {
+    __shared__ SmemModel M;
+    extern __shared__ __align__(16) unsigned char fit_smem[];
+    const DevModel& m = *a.model;
+    const int T = m.T, C = m.C;
+    int W[WP_MAX_CHANNELS], st[WP_MAX_CHANNELS];
+    int S = 1;
+    for (int c = C - 1; c >= 0; c--) {
+        W[c] = a.D[c] + 1;
+        st[c] = S;
+        S *= W[c];
+    }
+    const long cap = (long)T * S;
+    const long VS = (((HB ? 2 : 1) * cap + 1) + 3) / 4 * 4;
+    const int NV = C + 8;
+    float* vbase = reinterpret_cast<float*>(fit_smem);
+    float* wemit = vbase + NV * VS;                     // [T][S]
+    uint32_t* coords = reinterpret_cast<uint32_t*>(wemit + (long)T * S);  // [S]
+    float* red = reinterpret_cast<float*>(coords + S);  // [FIT_MAXTERMS][32]
+    float* rout = red + FIT_MAXTERMS * 32;              // [FIT_MAXTERMS]
+    int* kmx = reinterpret_cast<int*>(rout + FIT_MAXTERMS);  // [T]
+    int* Eb = kmx + WP_MAX_TIMESTEPS;                   // [T + 1]
+    double* acc = reinterpret_cast<double*>(((reinterpret_cast<uintptr_t>(Eb + WP_MAX_TIMESTEPS + 2)) + 7) & ~(uintptr_t)7);
+    auto vec = [&](int slot) {
+        SVec v;
+        v.A = vbase + (long)slot * VS;
+        v.B = v.A + cap;
+        v.pd = v.A + (HB ? 2 : 1) * cap;
+        return v;
+    };
+    auto gvec = [&](int t) {  // checkpoint t of this CTA (global)
+        SVec v;
+        v.A = ckpt + (long)blockIdx.x * ck_stride + (long)t * VS;
+        v.B = v.A + cap;
+        v.pd = v.A + (HB ? 2 : 1) * cap;
+        return v;
+    };
+    load_smem_model(M, m);
+    for (int j = threadIdx.x; j < S; j += blockDim.x) {
+        uint32_t pk = 0;
+        for (int c = 0; c < C; c++) pk |= (uint32_t)((j / st[c]) % W[c]) << (4 * c);
+        coords[j] = pk;
+    }
+    for (int k = threadIdx.x; k < a.nslots; k += blockDim.x) acc[k] = 0.0;
+    __syncthreads();
+    const float pf = m.pf, qf = 1.0f - m.pf;
+    const int BV = 0, CUR = C + 5, F0 = C + 6, F1 = C + 7;
+
+    for (long r = blockIdx.x; r < a.R; r += gridDim.x) {
+        const EmitEntry* tab = a.tab + r * (long)T * C * a.W;
+        // ---- emission weights per (t, j), normalised by 2^kmax[t]
+        for (int t = threadIdx.x; t < T; t += blockDim.x) {
+            int kmax = 0;
+            for (int c = 0; c < C; c++) {
+                int km = WP_EXPO_ZERO;
+                for (int n = 0; n < W[c]; n++) {
+                    const EmitEntry en = tab[(t * C + c) * a.W + n];
+                    if (en.mant != 0.0f) km = max(km, en.expo);
+                }
+                if (km == WP_EXPO_ZERO) {
+                    kmax = WP_EXPO_ZERO;
+                    break;
+                }
+                kmax += km;
+            }
+            kmx[t] = kmax;
+        }
+        __syncthreads();
+        bool dead = false;
+        for (int t = 0; t < T; t++)
+            if (kmx[t] == WP_EXPO_ZERO) dead = true;
+        if (dead) {  // some timestep emits nothing: P = 0
+            if (threadIdx.x == 0 && a.logp) a.logp[r] = -INFINITY;
+            __syncthreads();
+            continue;
+        }
+        for (long i = threadIdx.x; i < (long)T * S; i += blockDim.x) {
+            const int t = (int)(i / S), j = (int)(i % S);
+            float mm = 1.0f;
+            int ks = 0;
+            for (int c = 0; c < C; c++) {
+                const EmitEntry en = tab[(t * C + c) * a.W + fcoord(coords, j, c)];
+                mm *= en.mant;
+                ks += en.expo;
+            }
+            wemit[i] = mm != 0.0f ? mm * exp2i(max(ks - kmx[t], -200)) : 0.0f;
+        }
+        __syncthreads();
+
+        // Backward through timestep t's chain from CUR into bv[0..C+4]:
+        // bv0 in(CB) bv1 in(DT) bv2+c in(BL c) bv2+C in(ED) bv3+C in(EM).
+        auto backward_timestep = [&](int t) {
+            const SVec out_v = vec(CUR);
+            const long n1 = (long)(t + 1) * S, n0 = (long)t * S;
+            cta_emit<HB>(out_v, vec(BV + 3 + C), wemit + (long)t * S, S, n1);
+            const SVec e3 = vec(BV + 3 + C), e2 = vec(BV + 2 + C);
+            FOR_STATES(n0, S, i, e, j) {
+                const int dc = a.dye[e];
+                float v = pf * e3.A[i];
+                if (dc < 0) {
+                    v = fmaf(qf, e3.A[i + S], v);
+                } else {
+                    const float tot = (float)a.tot[e];
+                    const int nc = fcoord(coords, (int)j, dc);
+                    if ((float)nc < tot) v = fmaf(qf * (1.0f - (float)nc / tot), e3.A[i + S], v);
+                    if (nc >= 1) v = fmaf(qf * ((float)nc / tot), e3.A[i + S - st[dc]], v);
+                }
+                e2.A[i] = v;
+                if (HB) e2.B[i] = e3.B[i];
+            }
+            if (threadIdx.x == 0) *e2.pd = *e3.pd;
+            __syncthreads();
+            for (int c = C - 1; c >= 0; c--)
+                cta_binomial<HB>(vec(BV + 3 + c), vec(BV + 2 + c), coords, S, t, c, W[c], st[c], M.bleach[c], true);
+            const float pdt = M.p_det[t - 1];
+            const SVec b2 = vec(BV + 2), b1 = vec(BV + 1), b0 = vec(BV);
+            const float pd2 = *b2.pd;
+            for (long i = threadIdx.x; i < n0; i += blockDim.x) {
+                b1.A[i] = fmaf(1.0f - pdt, b2.A[i], pdt * pd2);
+                if (HB) b1.B[i] = fmaf(1.0f - pdt, b2.B[i], pdt * pd2);
+            }
+            if (threadIdx.x == 0) *b1.pd = pd2;
+            __syncthreads();
+            for (long i = threadIdx.x; i < n0; i += blockDim.x) {
+                if (HB) {
+                    b0.A[i] = fmaf(m.p_cb, b1.B[i], (1.0f - m.p_cb) * b1.A[i]);
+                    b0.B[i] = b1.B[i];
+                } else {
+                    b0.A[i] = (1.0f - m.p_cb) * b1.A[i];
+                }
+            }
+            if (threadIdx.x == 0) *b0.pd = *b1.pd;
+            __syncthreads();
+        };
+        // t = 0: d0 in(IB) d1+c in(DD c) d1+C in(EM0), from CUR.
+        auto backward_t0 = [&]() {
+            cta_emit<HB>(vec(CUR), vec(BV + 1 + C), wemit, S, S);
+            for (int c = C - 1; c >= 0; c--)
+                cta_binomial<HB>(vec(BV + 2 + c), vec(BV + 1 + c), coords, S, 1, c, W[c], st[c], M.dud[c], true);
+            const SVec b1 = vec(BV + 1), b0 = vec(BV);
+            for (int j = threadIdx.x; j < S; j += blockDim.x) {
+                if (HB) {
+                    b0.A[j] = fmaf(m.p_ib, b1.B[j], (1.0f - m.p_ib) * b1.A[j]);
+                    b0.B[j] = b1.B[j];
+                } else {
+                    b0.A[j] = (1.0f - m.p_ib) * b1.A[j];
+                }
+            }
+            if (threadIdx.x == 0) *b0.pd = *b1.pd;
+            __syncthreads();
+        };
+        auto copy_vec = [&](const SVec& src, const SVec& dst, long n, float scale) {
+            for (long i = threadIdx.x; i < n; i += blockDim.x) {
+                dst.A[i] = src.A[i] * scale;
+                if (HB) dst.B[i] = src.B[i] * scale;
+            }
+            if (threadIdx.x == 0) *dst.pd = *src.pd * scale;
+            __syncthreads();
+        };
+
+        // ---- backward pass with checkpoints cp[t] (input of timestep t's chain)
+        {
+            const SVec cur = vec(CUR);
+            for (long i = threadIdx.x; i < cap; i += blockDim.x) {
+                cur.A[i] = 1.0f;
+                if (HB) cur.B[i] = 1.0f;
+            }
+            if (threadIdx.x == 0) {
+                *cur.pd = 1.0f;
+                Eb[T] = 0;
+            }
+            __syncthreads();
+            for (int t = T - 1; t >= 1; t--) {
+                backward_timestep(t);
+                const long n0 = (long)t * S;
+                const SVec b0 = vec(BV);
+                float mx = 0.f;
+                for (long i = threadIdx.x; i < n0; i += blockDim.x) {
+                    mx = fmaxf(mx, b0.A[i]);
+                    if (HB) mx = fmaxf(mx, b0.B[i]);
+                }
+                if (threadIdx.x == 0) mx = fmaxf(mx, *b0.pd);
+                cta_reduce<true>(&mx, 1, red, rout);
+                int k = 0;
+                if (rout[0] > 0.f) frexpf(rout[0], &k);
+                const float sc = exp2i(-k);
+                copy_vec(b0, gvec(t), n0, sc);
+                copy_vec(b0, vec(CUR), n0, sc);
+                if (threadIdx.x == 0) Eb[t] = Eb[t + 1] + kmx[t] + k;
+                __syncthreads();
+            }
+            backward_t0();
+            if (threadIdx.x == 0) Eb[0] = Eb[1] + kmx[0];
+            __syncthreads();
+        }
+        const float Ps = vec(BV).A[S - 1];
+        if (!(Ps > 0.0f)) {
+            if (threadIdx.x == 0 && a.logp) a.logp[r] = -INFINITY;
+            __syncthreads();
+            continue;
+        }
+        int EP;
+        const float Pm = frexpf(Ps, &EP);
+        EP += Eb[0];
+        if (threadIdx.x == 0 && a.logp) a.logp[r] = log((double)Pm) + (double)EP * 0.69314718055994530942;
+        auto scale_of = [&](int Ea, int Ebc) { return ldexp(1.0 / (double)Pm, Ea + Ebc - EP); };
+
+        // ---- forward sweep with the expected counts
+        int fa = F0, fb = F1;
+        int Ea = 0;
+        float part[FIT_MAXTERMS];
+        {
+            // t = 0 (the backward vectors of timestep 0 are still in bv)
+            const SVec al = vec(fa);
+            for (long i = threadIdx.x; i < S; i += blockDim.x) {
+                al.A[i] = (i == S - 1) ? 1.0f : 0.0f;
+                if (HB) al.B[i] = 0.0f;
+            }
+            if (threadIdx.x == 0) *al.pd = 0.0f;
+            __syncthreads();
+            const double sc = scale_of(Ea, Eb[0]);
+            for (int k = 0; k < FIT_MAXTERMS; k++) part[k] = 0.f;
+            // initial block EM and transition
+            for (int j = threadIdx.x; j < S; j += blockDim.x) {
+                const float f = al.A[j];
+                if (HB) part[0] = fmaf(f * m.p_ib, vec(BV + 1).B[j], part[0]);
+                part[1] = fmaf(f, vec(BV).A[j], part[1]);
+            }
+            __syncthreads();
+            for (int j = threadIdx.x; j < S; j += blockDim.x) {
+                const float f = al.A[j];
+                if (HB) al.B[j] = al.B[j] + m.p_ib * f;
+                al.A[j] = (1.0f - m.p_ib) * f;
+            }
+            __syncthreads();
+            for (int c = 0; c < C; c++) {
+                const SVec f = vec(fa), b = vec(BV + 1 + c), nb = vec(BV + 2 + c);
+                float n32 = 0.f, d32 = 0.f;
+                for (int i = threadIdx.x; i < S; i += blockDim.x) {
+                    const int from = fcoord(coords, i, c);
+                    if (from < 1) continue;
+                    d32 = fmaf(f.A[i] * b.A[i], (float)from, d32);
+                    if (HB) d32 = fmaf(f.B[i] * b.B[i], (float)from, d32);
+                    for (int to = 0; to < from; to++) {
+                        const float p = M.dud[c][from * (from + 1) / 2 + to];
+                        const long kk = i - (long)(from - to) * st[c];
+                        n32 = fmaf(f.A[i] * p * nb.A[kk], (float)(from - to), n32);
+                        if (HB) n32 = fmaf(f.B[i] * p * nb.B[kk], (float)(from - to), n32);
+                    }
+                }
+                part[2 + 2 * c] = n32;
+                part[3 + 2 * c] = d32;
+                __syncthreads();
+                cta_binomial<HB>(vec(fa), vec(fb), coords, S, 1, c, W[c], st[c], M.dud[c], false);
+                const int tmp = fa;
+                fa = fb;
+                fb = tmp;
+            }
+            const int nt = 2 + 2 * C;
+            cta_reduce<false>(part, nt, red, rout);
+            if (threadIdx.x == 0) {
+                acc[FS_IB_NUM] += (double)rout[0] * sc;
+                acc[FS_IB_DEN] += (double)rout[1] * sc;
+                for (int c = 0; c < C; c++) {
+                    acc[fs_dud_num(T, c)] += (double)rout[2 + 2 * c] * sc;
+                    acc[fs_dud_den(T, c)] += (double)rout[3 + 2 * c] * sc;
+                }
+            }
+            // emission 0 and rescale
+            cta_emit<HB>(vec(fa), vec(fa), wemit, S, S);
+            const SVec al2 = vec(fa);
+            float tot = 0.f;
+            for (int j = threadIdx.x; j < S; j += blockDim.x) {
+                tot += al2.A[j];
+                if (HB) tot += al2.B[j];
+            }
+            if (threadIdx.x == 0) tot += *al2.pd;
+            cta_reduce<false>(&tot, 1, red, rout);
+            int k = 0;
+            if (rout[0] > 0.f) frexpf(rout[0], &k);
+            Ea += kmx[0];
+            copy_vec(al2, al2, S, exp2i(-k));
+            Ea += k;
+        }
+        for (int t = 1; t < T; t++) {
+            // backward vectors of timestep t from checkpoint t + 1
+            {
+                const long nn = (long)(t + 1) * S;
+                if (t + 1 == T) {
+                    const SVec cur = vec(CUR);
+                    for (long i = threadIdx.x; i < cap; i += blockDim.x) {
+                        cur.A[i] = 1.0f;
+                        if (HB) cur.B[i] = 1.0f;
+                    }
+                    if (threadIdx.x == 0) *cur.pd = 1.0f;
+                    __syncthreads();
+                } else {
+                    copy_vec(gvec(t + 1), vec(CUR), nn, 1.0f);
+                }
+            }
+            backward_timestep(t);
+            const double sc = scale_of(Ea, Eb[t + 1] + kmx[t]);
+            const long n0 = (long)t * S;
+            for (int k = 0; k < FIT_MAXTERMS; k++) part[k] = 0.f;
+            // cyclic block EM and transition
+            {
+                const SVec al = vec(fa), b0 = vec(BV), b1 = vec(BV + 1);
+                for (long i = threadIdx.x; i < n0; i += blockDim.x) {
+                    const float f = al.A[i];
+                    if (HB) part[0] = fmaf(f * m.p_cb, b1.B[i], part[0]);
+                    part[1] = fmaf(f, b0.A[i], part[1]);
+                }
+                __syncthreads();
+                for (long i = threadIdx.x; i < n0; i += blockDim.x) {
+                    const float f = al.A[i];
+                    if (HB) al.B[i] = al.B[i] + m.p_cb * f;
+                    al.A[i] = (1.0f - m.p_cb) * f;
+                }
+                __syncthreads();
+            }
+            // detach EM (skipping each slice's all-zero state) and transition
+            float pd2 = 0.f;
+            {
+                const SVec al = vec(fa), b1 = vec(BV + 1), b2 = vec(BV + 2);
+                const float pdt = M.p_det[t - 1];
+                pd2 = *b2.pd;
+                float fs = 0.f, fbv = 0.f, all = 0.f;
+                FOR_STATES(n0, S, i, e, j) {
+                    const float f = al.A[i];
+                    all += f;
+                    if (j != 0) {
+                        fs += f;
+                        fbv = fmaf(f, b1.A[i], fbv);
+                    }
+                    if (HB) {
+                        const float g = al.B[i];
+                        all += g;
+                        if (j != 0) {
+                            fs += g;
+                            fbv = fmaf(g, b1.B[i], fbv);
+                        }
+                    }
+                }
+                part[2] = fs * pdt;
+                part[3] = fbv;
+                part[4] = all;
+                cta_reduce<false>(part + 2, 3, red, rout);
+                const float allsum = rout[2];
+                part[2] = 0.f;  // reduced below from rout
+                const float red_fs = rout[0], red_fb = rout[1];
+                for (long i = threadIdx.x; i < n0; i += blockDim.x) {
+                    al.A[i] *= 1.0f - pdt;
+                    if (HB) al.B[i] *= 1.0f - pdt;
+                }
+                if (threadIdx.x == 0) {
+                    *al.pd = *al.pd + pdt * allsum;
+                    acc[fs_det_x(t - 1)] += (double)red_fs * (double)pd2 * sc;
+                    acc[fs_det_n(t - 1)] += (double)red_fb * sc;
+                }
+                __syncthreads();
+            }
+            // bleach per channel
+            for (int c = 0; c < C; c++) {
+                const SVec f = vec(fa), b = vec(BV + 2 + c), nb = vec(BV + 3 + c);
+                float n32 = 0.f, d32 = 0.f;
+                FOR_STATES(n0, S, i, e, j) {
+                    const int from = fcoord(coords, (int)j, c);
+                    if (from < 1) continue;
+                    d32 = fmaf(f.A[i] * b.A[i], (float)from, d32);
+                    if (HB) d32 = fmaf(f.B[i] * b.B[i], (float)from, d32);
+                    for (int to = 0; to < from; to++) {
+                        const float p = M.bleach[c][from * (from + 1) / 2 + to];
+                        const long kk = i - (long)(from - to) * st[c];
+                        n32 = fmaf(f.A[i] * p * nb.A[kk], (float)(from - to), n32);
+                        if (HB) n32 = fmaf(f.B[i] * p * nb.B[kk], (float)(from - to), n32);
+                    }
+                }
+                part[6 + 2 * c] = n32;
+                part[7 + 2 * c] = d32;
+                __syncthreads();
+                cta_binomial<HB>(vec(fa), vec(fb), coords, S, t, c, W[c], st[c], M.bleach[c], false);
+                const int tmp = fa;
+                fa = fb;
+                fb = tmp;
+            }
+            // Edman EM (skipping each slice's all-zero state) and transition
+            {
+                const SVec al = vec(fa), e2 = vec(BV + 2 + C), e3 = vec(BV + 3 + C), an = vec(fb);
+                float n32 = 0.f, d32 = 0.f;
+                FOR_STATES(n0, S, i, e, j) {
+                    if (j == 0) continue;
+                    const float f = al.A[i];
+                    n32 = fmaf(f * pf, e3.A[i], n32);
+                    d32 = fmaf(f, e2.A[i], d32);
+                }
+                part[4] = n32;
+                part[5] = d32;
+                const long n1 = (long)(t + 1) * S;
+                FOR_STATES(n1, S, i, e, j) {
+                    float v = e < t ? pf * al.A[i] : 0.0f;
+                    if (e >= 1) {
+                        const int dc = a.dye[e - 1];
+                        const float xin = al.A[i - S];
+                        if (dc < 0) {
+                            v = fmaf(qf, xin, v);
+                        } else {
+                            const float tot = (float)a.tot[e - 1];
+                            const int nc = fcoord(coords, (int)j, dc);
+                            if ((float)nc < tot) v = fmaf(qf * (1.0f - (float)nc / tot), xin, v);
+                            if (nc + 1 < W[dc]) v = fmaf(qf * ((float)(nc + 1) / tot), al.A[i - S + st[dc]], v);
+                        }
+                    }
+                    an.A[i] = v;
+                    if (HB) an.B[i] = e < t ? al.B[i] : 0.0f;
+                }
+                if (threadIdx.x == 0) *an.pd = *al.pd;
+                __syncthreads();
+                const int tmp = fa;
+                fa = fb;
+                fb = tmp;
+            }
+            // the timestep's remaining terms: block (0, 1), Edman (4, 5),
+            // bleach (6 ..)
+            {
+                float v[FIT_MAXTERMS];
+                int nt = 0;
+                v[nt++] = part[0];
+                v[nt++] = part[1];
+                v[nt++] = part[4];
+                v[nt++] = part[5];
+                for (int c = 0; c < C; c++) {
+                    v[nt++] = part[6 + 2 * c];
+                    v[nt++] = part[7 + 2 * c];
+                }
+                cta_reduce<false>(v, nt, red, rout);
+                if (threadIdx.x == 0) {
+                    acc[FS_CB_NUM] += (double)rout[0] * sc;
+                    acc[FS_CB_DEN] += (double)rout[1] * sc;
+                    acc[FS_EDMAN_NUM] += (double)rout[2] * sc;
+                    acc[FS_EDMAN_DEN] += (double)rout[3] * sc;
+                    for (int c = 0; c < C; c++) {
+                        acc[fs_bleach_num(T, c)] += (double)rout[4 + 2 * c] * sc;
+                        acc[fs_bleach_den(T, c)] += (double)rout[5 + 2 * c] * sc;
+                    }
+                }
+            }
+            // emission t and rescale
+            {
+                const long n1 = (long)(t + 1) * S;
+                cta_emit<HB>(vec(fa), vec(fa), wemit + (long)t * S, S, n1);
+                const SVec al = vec(fa);
+                float tot = 0.f;
+                for (long i = threadIdx.x; i < n1; i += blockDim.x) {
+                    tot += al.A[i];
+                    if (HB) tot += al.B[i];
+                }
+                if (threadIdx.x == 0) tot += *al.pd;
+                cta_reduce<false>(&tot, 1, red, rout);
+                int k = 0;
+                if (rout[0] > 0.f) frexpf(rout[0], &k);
+                Ea += kmx[t];
+                copy_vec(al, al, n1, exp2i(-k));
+                Ea += k;
+            }
+        }
+        __syncthreads();
+    }
+    // this CTA's sums, slot-major [nslots][grid]
+    for (int k = threadIdx.x; k < a.nslots; k += blockDim.x) a.sums[(long)k * gridDim.x + blockIdx.x] = acc[k];
+}
+
+size_t wp_fit_cta_smem_bytes(int T, int C, int S, bool has_block) {
+    const long cap = (long)T * S;
+    const long VS = (((has_block ? 2 : 1) * cap + 1) + 3) / 4 * 4;
+    size_t b = sizeof(float) * ((size_t)(C + 8) * VS + (size_t)T * S) + sizeof(uint32_t) * S +
+               sizeof(float) * (FIT_MAXTERMS * 32 + FIT_MAXTERMS) + sizeof(int) * (2 * WP_MAX_TIMESTEPS + 2) + 8 +
+               sizeof(double) * fit_nslots(T, C);
+    return b;
+}
+
+long wp_fit_cta_ckpt_floats(int T, int S, bool has_block) {
+    const long cap = (long)T * S;
+    const long VS = (((has_block ? 2 : 1) * cap + 1) + 3) / 4 * 4;
+    return (long)(T + 1) * VS;
+}
+
+cudaError_t wp_launch_fit_cta(bool has_block, int grid, size_t smem, cudaStream_t s, const FitArgs& a, float* ckpt,
+                              long ck_stride) {
+    if (has_block) {
+        cudaFuncSetAttribute(wp_fit_cta_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        wp_fit_cta_kernel<true><<<grid, FIT_NT, smem, s>>>(a, ckpt, ck_stride);
+    } else {
+        cudaFuncSetAttribute(wp_fit_cta_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        wp_fit_cta_kernel<false><<<grid, FIT_NT, smem, s>>>(a, ckpt, ck_stride);
+    }
+    return cudaGetLastError();
+}
+
+int wp_fit_cta_ctas_per_sm(bool has_block, size_t smem) {
+    int n = 0;
+    if (has_block) {
+        cudaFuncSetAttribute(wp_fit_cta_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wp_fit_cta_kernel<true>, FIT_NT, smem);
+    } else {
+        cudaFuncSetAttribute(wp_fit_cta_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, wp_fit_cta_kernel<false>, FIT_NT, smem);
+    }
+    return n;
+}
