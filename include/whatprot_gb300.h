@@ -208,6 +208,28 @@ wp_status wp_hmm_fit(wp_ctx* ctx, const wp_seq_model* start, int num_timesteps,
                      wp_fit_params* out, double* step_size, double* log_l,
                      int* iterations);
 
+/* bootstrap_fit (fitters/bootstrap-fit.cc:37-173): num_rounds fits
+ * (wp_hmm_fit) on reads resampled with replacement (indices from a 64-bit
+ * Mersenne twister seeded with `seed`; the reference seeds from the clock),
+ * one fit on all reads (out_best, its step size and log-likelihood), and
+ * per parameter the bounds of the central confidence_interval of the round
+ * results (sorted; lower index floor((1-ci)/2 * rounds), upper floor((1 -
+ * (1-ci)/2) * rounds), clamped to the last round).  out_rounds /
+ * out_log_ls hold num_rounds entries; ci and worst-step outputs may be
+ * NULL. */
+wp_status wp_hmm_bootstrap_fit(wp_ctx* ctx, const wp_seq_model* start,
+                               int num_timesteps, const int16_t* dye_seq,
+                               int length, const double* rads, int num_reads,
+                               const wp_fit_settings* settings,
+                               double stopping_threshold, double max_runtime,
+                               int num_rounds, double confidence_interval,
+                               unsigned long long seed,
+                               wp_fit_params* out_rounds, double* out_log_ls,
+                               wp_fit_params* out_best, double* out_step_size,
+                               double* out_best_log_l, wp_fit_params* out_ci_min,
+                               wp_fit_params* out_ci_max,
+                               double* out_worst_round_step);
+
 /* Box-constrained weighted least-squares fit of base + initial *
  * exp(-decay * i), i = 0..n-1, to y with weights w, parameters in [0, 1] and
  * held ones fixed (held[k] != 0), at most 10 Levenberg-Marquardt iterations

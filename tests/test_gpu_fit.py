@@ -182,3 +182,45 @@ def test_fit_vs_reference(name):
     assert abs(log_l - float(z["ref_log_l"])) <= 1e-6 * abs(float(z["ref_log_l"])) + 1e-3
     # log_likelihood of the mirror agrees with the fit's own final value
     assert abs(fitter.log_likelihood(z["rads"], fitted) - log_l) <= 1e-9 * abs(log_l)
+
+
+def test_bootstrap_fit(tmp_path):
+    """bootstrap_fit: the fit on all reads equals wp_hmm_fit's, rounds are
+    reproducible from the seed and scatter around it, the bounds bracket the
+    rounds, and the params CSV has the reference's layout."""
+    import os
+    from conftest import GOLDEN
+    from whatprot_gb300.io import write_params
+    z = np.load(os.path.join(GOLDEN, "fit_c2_t8.npz"))
+    C, T = int(z["C"]), int(z["T"])
+    st = z["start"]
+    sm = paper_model(C)
+    (sm.p_edman_failure, sm.p_detach, sm.p_initial_detach, sm.p_initial_detach_decay,
+     sm.p_initial_block, sm.p_cyclic_block) = st[:6]
+    for c in range(C):
+        sm.channel_models[c].p_bleach = st[6 + c]
+        sm.channel_models[c].p_dud = st[6 + C + c]
+    ctx = capi.Context(0)
+    try:
+        res = ctx.bootstrap_fit(sm, T, z["seq"], z["rads"], 1e-5, 6, 0.9, seed=5)
+        fitted, step, ll, _ = ctx.hmm_fit(sm, T, z["seq"], z["rads"], 1e-5)
+        assert np.allclose(_params(res["best"]), _params(fitted), atol=1e-12)
+        assert res["log_l"] == ll
+        again = ctx.bootstrap_fit(sm, T, z["seq"], z["rads"], 1e-5, 6, 0.9, seed=5)
+        assert all(np.array_equal(_params(a), _params(b)) for a, b in zip(res["models"], again["models"]))
+        other = ctx.bootstrap_fit(sm, T, z["seq"], z["rads"], 1e-5, 6, 0.9, seed=6)
+        assert not np.array_equal(_params(res["models"][0]), _params(other["models"][0]))
+        P = np.array([_params(m) for m in res["models"]])
+        lo, hi = _params(res["ci_min"]), _params(res["ci_max"])
+        assert np.all(lo <= hi)
+        assert np.all(P.min(axis=0) <= lo + 1e-15) and np.all(hi <= P.max(axis=0) + 1e-15)
+        # rounds scatter around the full fit by a few percent of the rates
+        assert np.all(np.abs(P[:, [0, 6, 7, 8, 9]] - _params(fitted)[[0, 6, 7, 8, 9]]) < 0.05)
+        path = tmp_path / "params.csv"
+        write_params(path, C, res["models"], res["log_ls"])
+        lines = open(path).read().splitlines()
+        assert lines[0] == ("p_edman_failure,p_detach,p_initial_detach,p_initial_detach_decay,p_initial_block,"
+                            "p_cyclic_block,ch0:p_bleach,ch0:p_dud,ch1:p_bleach,ch1:p_dud,log(L)")
+        assert len(lines) == 7 and len(lines[1].split(",")) == 11
+    finally:
+        ctx.close()

@@ -31,6 +31,7 @@ EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload"
            "wp_hmm_loglik_all", "wp_hmm_count_flops", "wp_launch_count", "wp_ctx_stream",
            "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak", "wp_last_batch_stats",
            "wp_fit_begin", "wp_fit_estep", "wp_hmm_fit", "wp_fit_offset_exponential", "wp_fit_set_kernel",
+           "wp_hmm_bootstrap_fit",
            "wp_nn_tracks_upload", "wp_nn_classify", "wp_hybrid_classify", "wp_hybrid_classify_device",
            "wp_dev_gemm_bf16", "wp_simulate_reads", "wp_mlp_create", "wp_mlp_destroy", "wp_mlp_train",
            "wp_mlp_train_step", "wp_mlp_shape", "wp_mlp_get", "wp_mlp_set", "wp_mlp_logits", "wp_mlp_propose",
@@ -165,6 +166,11 @@ def load_library(path: Optional[str] = None):
                                ctypes.POINTER(WpFitSettings), D, D, ctypes.POINTER(WpFitParams),
                                ctypes.POINTER(D), ctypes.POINTER(D), ctypes.POINTER(I)]
     lib.wp_hmm_fit.restype = I
+    P_ = ctypes.POINTER
+    lib.wp_hmm_bootstrap_fit.argtypes = [V, P_(WpSeqModel), I, V, I, V, I, P_(WpFitSettings), D, D, I, D,
+                                         ctypes.c_ulonglong, V, V, P_(WpFitParams), P_(D), P_(D), P_(WpFitParams),
+                                         P_(WpFitParams), P_(D)]
+    lib.wp_hmm_bootstrap_fit.restype = I
     lib.wp_fit_offset_exponential.argtypes = [V, V, I, V, V]
     lib.wp_fit_offset_exponential.restype = I
     lib.wp_nn_tracks_upload.argtypes = [V, V, I, I, I, V, V, V, V]
@@ -440,6 +446,52 @@ class Context:
         trk = np.zeros((R, T, C), np.uint8) if tracks else None
         self._check(self.lib.wp_simulate_reads(self.h, R, seed, _ptr(rads), _ptr(pep), _ptr(trk)))
         return rads, pep, trk
+
+    @staticmethod
+    def _params_to_model(start: SequencingModel, out: "WpFitParams") -> SequencingModel:
+        import copy
+        m = copy.deepcopy(start)
+        for k in ("p_edman_failure", "p_detach", "p_initial_detach", "p_initial_detach_decay",
+                  "p_initial_block", "p_cyclic_block"):
+            setattr(m, k, getattr(out, k))
+        for c, cm in enumerate(m.channel_models):
+            cm.p_bleach = out.p_bleach[c]
+            cm.p_dud = out.p_dud[c]
+        return m
+
+    def bootstrap_fit(self, start: SequencingModel, num_timesteps: int, dye_seq, rads: np.ndarray,
+                      stopping_threshold: float, num_rounds: int, confidence_interval: float, seed: int = 1,
+                      max_runtime: float = 1e300, holds: Optional[dict] = None) -> dict:
+        """wp_hmm_bootstrap_fit: per-round models and log-likelihoods, the fit
+        on all reads, and the confidence bounds."""
+        m, keep = seq_model_struct(start)
+        seq = np.ascontiguousarray(dye_seq, dtype=np.int16)
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        fs = WpFitSettings()
+        for k, v in (holds or {}).items():
+            if k in ("hold_p_bleach", "hold_p_dud"):
+                arr = getattr(fs, k)
+                for c, h in enumerate(v):
+                    arr[c] = 1 if h else 0
+            else:
+                setattr(fs, k, 1 if v else 0)
+        rounds = (WpFitParams * num_rounds)()
+        lls = np.zeros(num_rounds, np.float64)
+        best, lo, hi = WpFitParams(), WpFitParams(), WpFitParams()
+        step, bll, worst = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.wp_hmm_bootstrap_fit(self.h, ctypes.byref(m), num_timesteps,
+                                                  _ptr(seq) if len(seq) else None, len(seq), _ptr(rads),
+                                                  rads.shape[0], ctypes.byref(fs), stopping_threshold, max_runtime,
+                                                  num_rounds, confidence_interval, seed, ctypes.byref(rounds),
+                                                  _ptr(lls), ctypes.byref(best), ctypes.byref(step),
+                                                  ctypes.byref(bll), ctypes.byref(lo), ctypes.byref(hi),
+                                                  ctypes.byref(worst)))
+        self.num_timesteps = num_timesteps
+        self.num_channels = start.num_channels
+        return {"models": [self._params_to_model(start, rounds[i]) for i in range(num_rounds)],
+                "log_ls": lls, "best": self._params_to_model(start, best), "step_size": step.value,
+                "log_l": bll.value, "ci_min": self._params_to_model(start, lo),
+                "ci_max": self._params_to_model(start, hi), "worst_round_step": worst.value}
 
     def launch_count(self) -> int:
         return int(self.lib.wp_launch_count(self.h))

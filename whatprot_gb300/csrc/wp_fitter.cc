@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <random>
 #include <vector>
 
 #include "whatprot_gb300.h"
@@ -343,6 +344,73 @@ wp_status wp_hmm_fit(wp_ctx* ctx, const wp_seq_model* start, int T, const int16_
     if (step_size) *step_size = step;
     if (log_l) *log_l = nz > 0 ? -INFINITY : sl;
     if (iterations) *iterations = iters;
+    return WP_OK;
+}
+
+// bootstrap_fit (fitters/bootstrap-fit.cc:37-173): num_rounds fits on reads
+// resampled with replacement, one fit on all reads, and per parameter the
+// confidence bounds from the sorted round results.  The reference seeds its
+// resampling from the clock; here the caller gives the seed (a 64-bit
+// Mersenne twister draws the indices).
+wp_status wp_hmm_bootstrap_fit(wp_ctx* ctx, const wp_seq_model* start, int T, const int16_t* dye_seq, int length,
+                               const double* rads, int R, const wp_fit_settings* settings, double stopping_threshold,
+                               double max_runtime, int num_rounds, double confidence_interval,
+                               unsigned long long seed, wp_fit_params* out_rounds, double* out_log_ls,
+                               wp_fit_params* out_best, double* out_step_size, double* out_best_log_l,
+                               wp_fit_params* out_ci_min, wp_fit_params* out_ci_max,
+                               double* out_worst_round_step) {
+    if (!ctx || !start || !rads || R < 1 || num_rounds < 1 || !out_rounds || !out_log_ls || !out_best ||
+        !(confidence_interval >= 0.0 && confidence_interval <= 1.0))
+        return WP_ERR_INVALID;
+    const int C = start->num_channels;
+    const size_t TC = (size_t)T * C;
+    std::mt19937_64 gen(seed);
+    std::uniform_int_distribution<int> pick(0, R - 1);  // inclusive bounds, as the reference's
+    std::vector<double> sub((size_t)R * TC);
+    double worst = 0.0;
+    for (int i = 0; i < num_rounds; i++) {
+        for (int j = 0; j < R; j++) {
+            const int src = pick(gen);
+            memcpy(&sub[(size_t)j * TC], rads + (size_t)src * TC, sizeof(double) * TC);
+        }
+        double step = 0.0;
+        wp_status st = wp_hmm_fit(ctx, start, T, dye_seq, length, sub.data(), R, settings, stopping_threshold,
+                                  max_runtime, &out_rounds[i], &step, &out_log_ls[i], nullptr);
+        if (st != WP_OK) return st;
+        worst = std::max(worst, step);
+    }
+    double best_step = 0.0, best_ll = 0.0;
+    wp_status st = wp_hmm_fit(ctx, start, T, dye_seq, length, rads, R, settings, stopping_threshold, max_runtime,
+                              out_best, &best_step, &best_ll, nullptr);
+    if (st != WP_OK) return st;
+    if (out_step_size) *out_step_size = best_step;
+    if (out_best_log_l) *out_best_log_l = best_ll;
+    if (out_worst_round_step) *out_worst_round_step = worst;
+    // confidence bounds per parameter (bootstrap-fit.cc:95-167); the upper
+    // index is clamped to the last round (the reference reads one past the
+    // end when the product is integral at confidence 1)
+    const int lo = std::min(num_rounds - 1, (int)((1.0 - confidence_interval) / 2.0 * (double)num_rounds));
+    const int hi = std::min(num_rounds - 1, (int)((1.0 - (1.0 - confidence_interval) / 2.0) * (double)num_rounds));
+    auto bounds = [&](auto get, auto set) {
+        std::vector<double> v(num_rounds);
+        for (int i = 0; i < num_rounds; i++) v[i] = get(out_rounds[i]);
+        std::sort(v.begin(), v.end());
+        if (out_ci_min) set(*out_ci_min, v[lo]);
+        if (out_ci_max) set(*out_ci_max, v[hi]);
+    };
+    if (out_ci_min) memset(out_ci_min, 0, sizeof(*out_ci_min));
+    if (out_ci_max) memset(out_ci_max, 0, sizeof(*out_ci_max));
+    bounds([](const wp_fit_params& p) { return p.p_edman_failure; }, [](wp_fit_params& p, double x) { p.p_edman_failure = x; });
+    bounds([](const wp_fit_params& p) { return p.p_detach; }, [](wp_fit_params& p, double x) { p.p_detach = x; });
+    bounds([](const wp_fit_params& p) { return p.p_initial_detach; }, [](wp_fit_params& p, double x) { p.p_initial_detach = x; });
+    bounds([](const wp_fit_params& p) { return p.p_initial_detach_decay; },
+           [](wp_fit_params& p, double x) { p.p_initial_detach_decay = x; });
+    bounds([](const wp_fit_params& p) { return p.p_initial_block; }, [](wp_fit_params& p, double x) { p.p_initial_block = x; });
+    bounds([](const wp_fit_params& p) { return p.p_cyclic_block; }, [](wp_fit_params& p, double x) { p.p_cyclic_block = x; });
+    for (int c = 0; c < C; c++) {
+        bounds([c](const wp_fit_params& p) { return p.p_bleach[c]; }, [c](wp_fit_params& p, double x) { p.p_bleach[c] = x; });
+        bounds([c](const wp_fit_params& p) { return p.p_dud[c]; }, [c](wp_fit_params& p, double x) { p.p_dud[c] = x; });
+    }
     return WP_OK;
 }
 

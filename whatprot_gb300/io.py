@@ -153,3 +153,20 @@ def write_dye_tracks(path, dts: DyeTrackSet) -> None:
             for j in range(a, b):
                 trip.append(f"{dts.src_id[j]}\t{dts.src_count[j]}\t{dts.src_hits[j]}")
             f.write("\t".join(trip) + "\n")
+
+
+def write_params(path, num_channels: int, models, log_ls) -> None:
+    """params-io.cc:32-56: the bootstrap rounds' parameters and log(L), CSV,
+    17 significant digits."""
+    cols = ["p_edman_failure", "p_detach", "p_initial_detach", "p_initial_detach_decay", "p_initial_block",
+            "p_cyclic_block"]
+    for c in range(num_channels):
+        cols += [f"ch{c}:p_bleach", f"ch{c}:p_dud"]
+    with open(path, "w") as f:
+        f.write(",".join(cols) + ",log(L)\n")
+        for m, ll in zip(models, log_ls):
+            vals = [m.p_edman_failure, m.p_detach, m.p_initial_detach, m.p_initial_detach_decay,
+                    m.p_initial_block, m.p_cyclic_block]
+            for c in range(num_channels):
+                vals += [m.channel_models[c].p_bleach, m.channel_models[c].p_dud]
+            f.write(",".join(f"{v:.17g}" for v in vals) + f",{ll:.17g}\n")
