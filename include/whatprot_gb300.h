@@ -208,6 +208,18 @@ wp_status wp_hmm_fit(wp_ctx* ctx, const wp_seq_model* start, int num_timesteps,
                      wp_fit_params* out, double* step_size, double* log_l,
                      int* iterations);
 
+/* One M-step of HMMFitter::fit (fitters/hmm-fitter.h:80-116) from E-step
+ * sums: the dud hidden-count correction for num_reads reads, p = num/den,
+ * the detach curve (wp_fit_offset_exponential), holds (settings may be
+ * NULL), and the step size (SequencingModel::distance).  Host only: a
+ * caller that shards the reads over GPUs adds the shards' wp_fit_estep sums
+ * (an all-reduce) and every rank takes the same step. */
+wp_status wp_fit_mstep(const wp_fit_sums* sums, int num_channels,
+                       int num_timesteps, const int16_t* dye_seq, int length,
+                       long long num_reads, const wp_fit_params* current,
+                       const wp_fit_settings* settings, wp_fit_params* next,
+                       double* step_size);
+
 /* bootstrap_fit (fitters/bootstrap-fit.cc:37-173): num_rounds fits
  * (wp_hmm_fit) on reads resampled with replacement (indices from a 64-bit
  * Mersenne twister seeded with `seed`; the reference seeds from the clock),

@@ -31,7 +31,7 @@ EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload"
            "wp_hmm_loglik_all", "wp_hmm_count_flops", "wp_launch_count", "wp_ctx_stream",
            "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak", "wp_last_batch_stats",
            "wp_fit_begin", "wp_fit_estep", "wp_hmm_fit", "wp_fit_offset_exponential", "wp_fit_set_kernel",
-           "wp_hmm_bootstrap_fit",
+           "wp_hmm_bootstrap_fit", "wp_fit_mstep",
            "wp_nn_tracks_upload", "wp_nn_classify", "wp_hybrid_classify", "wp_hybrid_classify_device",
            "wp_dev_gemm_bf16", "wp_simulate_reads", "wp_mlp_create", "wp_mlp_destroy", "wp_mlp_train",
            "wp_mlp_train_step", "wp_mlp_shape", "wp_mlp_get", "wp_mlp_set", "wp_mlp_logits", "wp_mlp_propose",
@@ -167,6 +167,9 @@ def load_library(path: Optional[str] = None):
                                ctypes.POINTER(D), ctypes.POINTER(D), ctypes.POINTER(I)]
     lib.wp_hmm_fit.restype = I
     P_ = ctypes.POINTER
+    lib.wp_fit_mstep.argtypes = [P_(WpFitSums), I, I, V, I, ctypes.c_longlong, P_(WpFitParams), P_(WpFitSettings),
+                                 P_(WpFitParams), P_(D)]
+    lib.wp_fit_mstep.restype = I
     lib.wp_hmm_bootstrap_fit.argtypes = [V, P_(WpSeqModel), I, V, I, V, I, P_(WpFitSettings), D, D, I, D,
                                          ctypes.c_ulonglong, V, V, P_(WpFitParams), P_(D), P_(D), P_(WpFitParams),
                                          P_(WpFitParams), P_(D)]

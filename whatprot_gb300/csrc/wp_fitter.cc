@@ -132,9 +132,107 @@ double distance(const HostModel& a, const HostModel& b) {
     return d;
 }
 
+wp_fit_params to_params(const HostModel& m) {
+    wp_fit_params p;
+    memset(&p, 0, sizeof(p));
+    p.p_edman_failure = m.p_edman_failure;
+    p.p_detach = m.p_detach;
+    p.p_initial_detach = m.p_initial_detach;
+    p.p_initial_detach_decay = m.p_initial_detach_decay;
+    p.p_initial_block = m.p_initial_block;
+    p.p_cyclic_block = m.p_cyclic_block;
+    for (int c = 0; c < m.C; c++) {
+        p.p_bleach[c] = m.p_bleach[c];
+        p.p_dud[c] = m.p_dud[c];
+    }
+    return p;
+}
+
+void from_params(const wp_fit_params& p, HostModel* m) {
+    m->p_edman_failure = p.p_edman_failure;
+    m->p_detach = p.p_detach;
+    m->p_initial_detach = p.p_initial_detach;
+    m->p_initial_detach_decay = p.p_initial_detach_decay;
+    m->p_initial_block = p.p_initial_block;
+    m->p_cyclic_block = p.p_cyclic_block;
+    for (int c = 0; c < m->C; c++) {
+        m->p_bleach[c] = p.p_bleach[c];
+        m->p_dud[c] = p.p_dud[c];
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+// One M-step from E-step sums (fitters/hmm-fitter.h:80-116): the dud
+// hidden-count correction for num_reads reads, p = num/den, the detach
+// curve by bounded least squares, holds, and the step (model distance).
+wp_status wp_fit_mstep(const wp_fit_sums* sums_in, int C, int T, const int16_t* dye_seq, int length,
+                       long long num_reads, const wp_fit_params* cur, const wp_fit_settings* settings,
+                       wp_fit_params* next, double* step_size) {
+    if (!sums_in || !cur || !next || C < 1 || C > WP_MAX_CHANNELS || T < 1 || T > WP_MAX_TIMESTEPS || length < 0 ||
+        (length > 0 && !dye_seq))
+        return WP_ERR_INVALID;
+    for (int i = 0; i < length; i++)
+        if (dye_seq[i] < -1 || dye_seq[i] >= C) return WP_ERR_INVALID;
+    wp_fit_settings fs;
+    memset(&fs, 0, sizeof(fs));
+    if (settings) fs = *settings;
+    wp_fit_sums s = *sums_in;
+    // Dud hidden-count correction (fitters/hmm-fitter.h:80-101): the ratio
+    // of all-dud peptides, per dye of the dye-seq.
+    double ratio = 1.0;
+    for (int i = 0; i < length; i++)
+        if (dye_seq[i] != -1) ratio *= cur->p_dud[dye_seq[i]];
+    const double hidden = (1.0 / (1.0 - ratio) - 1.0) * (double)num_reads;
+    for (int i = 0; i < length; i++)
+        if (dye_seq[i] != -1) {
+            s.p_dud_num[dye_seq[i]] += hidden;
+            s.p_dud_den[dye_seq[i]] += hidden;
+        }
+    // SequencingModelFitter::get (sequencing-model-fitter.cc:68-78), then
+    // update_with_holds (hmm-fitter.cc:63-97).
+    *next = *cur;
+    if (!fs.hold_p_edman_failure) next->p_edman_failure = s.p_edman_failure_num / s.p_edman_failure_den;
+    if (!fs.hold_p_initial_block) next->p_initial_block = s.p_initial_block_num / s.p_initial_block_den;
+    if (!fs.hold_p_cyclic_block) next->p_cyclic_block = s.p_cyclic_block_num / s.p_cyclic_block_den;
+    {
+        const int n = T - 1;
+        std::vector<double> y(std::max(n, 1)), w(std::max(n, 1));
+        for (int k = 0; k < n; k++) {
+            y[k] = s.p_detach_x[k] / s.p_detach_n[k];
+            w[k] = s.p_detach_n[k];
+        }
+        double p[3] = {cur->p_detach, cur->p_initial_detach, cur->p_initial_detach_decay};
+        const int held[3] = {fs.hold_p_detach, fs.hold_p_initial_detach, fs.hold_p_initial_detach_decay};
+        wp_status st = wp_fit_offset_exponential(y.data(), w.data(), n, held, p);
+        if (st != WP_OK) return st;
+        if (!fs.hold_p_detach) next->p_detach = p[0];
+        if (!fs.hold_p_initial_detach) next->p_initial_detach = p[1];
+        if (!fs.hold_p_initial_detach_decay) next->p_initial_detach_decay = p[2];
+    }
+    for (int c = 0; c < C; c++) {
+        if (!fs.hold_p_bleach[c]) next->p_bleach[c] = s.p_bleach_num[c] / s.p_bleach_den[c];
+        if (!fs.hold_p_dud[c]) next->p_dud[c] = s.p_dud_num[c] / s.p_dud_den[c];
+    }
+    if (step_size) {
+        // SequencingModel::distance (sequencing-model.cc:153-166)
+        double d = 0.0;
+        d = std::max(d, fabs(cur->p_edman_failure - next->p_edman_failure));
+        d = std::max(d, fabs(cur->p_detach - next->p_detach));
+        d = std::max(d, fabs(cur->p_initial_detach - next->p_initial_detach));
+        d = std::max(d, fabs(cur->p_initial_detach_decay - next->p_initial_detach_decay));
+        d = std::max(d, fabs(cur->p_initial_block - next->p_initial_block));
+        d = std::max(d, fabs(cur->p_cyclic_block - next->p_cyclic_block));
+        for (int c = 0; c < C; c++) {
+            d = std::max(d, fabs(cur->p_bleach[c] - next->p_bleach[c]));
+            d = std::max(d, fabs(cur->p_dud[c] - next->p_dud[c]));
+        }
+        *step_size = d;
+    }
+    return WP_OK;
+}
 
 wp_status wp_fit_offset_exponential(const double* y, const double* w, int n, const int* held, double* params) {
     if (n < 0 || !params || (n > 0 && (!y || !w))) return WP_ERR_INVALID;
@@ -256,15 +354,6 @@ wp_status wp_hmm_fit(wp_ctx* ctx, const wp_seq_model* start, int T, const int16_
     st = wp_fit_begin(ctx, dye_seq, length, rads, R);
     if (st != WP_OK) return st;
 
-    // ratio_hidden = product of p_dud over the dye-seq's dyes
-    // (fitters/hmm-fitter.h:80-89).
-    auto hidden_ratio = [&](const HostModel& m) {
-        double ratio = 1.0;
-        for (int i = 0; i < length; i++)
-            if (dye_seq[i] != -1) ratio *= m.p_dud[dye_seq[i]];
-        return ratio;
-    };
-
     const auto t0 = std::chrono::steady_clock::now();
     HostModel x;
     double step = 0.0;
@@ -279,40 +368,13 @@ wp_status wp_hmm_fit(wp_ctx* ctx, const wp_seq_model* start, int T, const int16_
         st = wp_fit_estep(ctx, &s, nullptr, nullptr);
         if (st != WP_OK) return st;
         iters++;
-        // Dud hidden-count correction (fitters/hmm-fitter.h:80-101).
-        const double magic = 1.0 / (1.0 - hidden_ratio(sm)) - 1.0;
-        const double hidden = magic * (double)R;
-        for (int i = 0; i < length; i++)
-            if (dye_seq[i] != -1) {
-                s.p_dud_num[dye_seq[i]] += hidden;
-                s.p_dud_den[dye_seq[i]] += hidden;
-            }
-        // M-step: SequencingModelFitter::get (sequencing-model-fitter.cc:
-        // 68-78) then update_with_holds (hmm-fitter.cc:63-97).
         HostModel next = sm;
-        if (!fs.hold_p_edman_failure) next.p_edman_failure = s.p_edman_failure_num / s.p_edman_failure_den;
-        if (!fs.hold_p_initial_block) next.p_initial_block = s.p_initial_block_num / s.p_initial_block_den;
-        if (!fs.hold_p_cyclic_block) next.p_cyclic_block = s.p_cyclic_block_num / s.p_cyclic_block_den;
         {
-            const int n = T - 1;
-            std::vector<double> y(std::max(n, 1)), w(std::max(n, 1));
-            for (int k = 0; k < n; k++) {
-                y[k] = s.p_detach_x[k] / s.p_detach_n[k];
-                w[k] = s.p_detach_n[k];
-            }
-            double p[3] = {sm.p_detach, sm.p_initial_detach, sm.p_initial_detach_decay};
-            const int held[3] = {fs.hold_p_detach, fs.hold_p_initial_detach, fs.hold_p_initial_detach_decay};
-            st = wp_fit_offset_exponential(y.data(), w.data(), n, held, p);
+            wp_fit_params cur = to_params(sm), nx;
+            st = wp_fit_mstep(&s, C, T, dye_seq, length, (long long)R, &cur, &fs, &nx, &step);
             if (st != WP_OK) return st;
-            if (!fs.hold_p_detach) next.p_detach = p[0];
-            if (!fs.hold_p_initial_detach) next.p_initial_detach = p[1];
-            if (!fs.hold_p_initial_detach_decay) next.p_initial_detach_decay = p[2];
+            from_params(nx, &next);
         }
-        for (int c = 0; c < C; c++) {
-            if (!fs.hold_p_bleach[c]) next.p_bleach[c] = s.p_bleach_num[c] / s.p_bleach_den[c];
-            if (!fs.hold_p_dud[c]) next.p_dud[c] = s.p_dud_num[c] / s.p_dud_den[c];
-        }
-        step = distance(sm, next);
         const double elapsed =
                 std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (step < stopping_threshold || elapsed > max_runtime) {
