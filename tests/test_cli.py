@@ -41,3 +41,15 @@ def test_option_forms():
     assert pos == ["classify", "hmm"]
     assert opts == {"seqparams": "p.json", "dyeseqs": "s.tsv", "radiometries": "r.tsv", "results": "y",
                     "hmmprune": 5.0}
+
+
+def test_dye_seq_file_round_trip_with_an_empty_dye_seq(tmp_path):
+    import numpy as np
+    from whatprot_gb300 import io
+    from whatprot_gb300.model import DyeSeqSet, parse_dye_seq
+    ds = DyeSeqSet(2, [parse_dye_seq("..0.1"), parse_dye_seq("...."), parse_dye_seq("1")],
+                   np.array([4, 5, 6], np.int32), np.array([1, 2, 3], np.int32))
+    io.write_dye_seqs(tmp_path / "d.tsv", ds)
+    back = io.read_dye_seqs(tmp_path / "d.tsv")
+    assert [list(s) for s in back.seqs] == [list(s) for s in ds.seqs]
+    assert np.array_equal(back.ids, ds.ids) and np.array_equal(back.counts, ds.counts)

@@ -41,10 +41,13 @@ def read_dye_seqs(path) -> DyeSeqSet:
 
 
 def write_dye_seqs(path, ds: DyeSeqSet) -> None:
+    """dye-seqs-io.cc:63-89.  A dye-seq without any dye is written as "."
+    (the reader trims trailing '.'): an empty field would be skipped by a
+    whitespace-token reader, here and in the reference."""
     with open(path, "w") as f:
         f.write(f"{ds.num_channels}\n{len(ds)}\n")
         for s, cnt, i in zip(ds.seqs, ds.counts, ds.ids):
-            f.write(f"{dye_seq_string(s)}\t{int(cnt)}\t{int(i)}\n")
+            f.write(f"{dye_seq_string(s) or '.'}\t{int(cnt)}\t{int(i)}\n")
 
 
 def read_radiometries(path, true_model: SequencingModel) -> Tuple[int, int, np.ndarray]:
