@@ -125,6 +125,26 @@ wp_status wp_hmm_classify_device(wp_ctx* ctx, const double* d_rads,
                                  int32_t* d_out_id, double* d_out_score,
                                  double* d_out_total, int async);
 
+/* Launch sequence of wp_hmm_classify_device captured in a CUDA graph: the
+ * second call with the same arguments (reads and output pointers, size,
+ * cutoff, model and peptides) captures it, later ones replay it.  On by
+ * default; not used while per-kernel timing is enabled. */
+wp_status wp_ctx_set_graphs(wp_ctx* ctx, int enable);
+
+/* Engine launch shapes {pass-1 threads, pass-1 CTAs per SM, pass-2 threads,
+ * pass-2 CTAs per SM} (threads a multiple of 32 up to 256, CTAs 1..4); NULL
+ * returns to the tuned or default shapes.  Results do not depend on them. */
+wp_status wp_set_engine_config(wp_ctx* ctx, const int32_t* cfg4);
+
+/* Autotuner: times the classify of a sample of reads ([R][T][C] host,
+ * divided by mu) under every feasible engine launch shape and keeps the
+ * fastest for this context's shape key (channels, blocking, max dyes,
+ * timesteps); later batches with that key use it.  Writes the chosen shape
+ * (cfg4, nullable) and its time in ms. */
+wp_status wp_autotune(wp_ctx* ctx, const double* rads, int num_reads,
+                      double dist_cutoff, int32_t* out_cfg4,
+                      double* out_best_ms);
+
 /* log P for every (read, peptide) pair: out_logp[r * P + p] (host), -inf
  * where P == 0.  PeptideHMM::probability (hmm/hmm/peptide-hmm.cc:94-100),
  * per pair, computed in FP32 with exact power-of-two rescaling. */

@@ -33,7 +33,8 @@ EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload"
            "wp_fit_begin", "wp_fit_estep", "wp_hmm_fit", "wp_fit_offset_exponential", "wp_fit_set_kernel",
            "wp_hmm_bootstrap_fit", "wp_fit_mstep",
            "wp_nn_tracks_upload", "wp_nn_classify", "wp_hybrid_classify", "wp_hybrid_classify_device",
-           "wp_dev_gemm_bf16", "wp_simulate_reads", "wp_mlp_create", "wp_mlp_destroy", "wp_mlp_train",
+           "wp_dev_gemm_bf16", "wp_simulate_reads", "wp_ctx_set_graphs", "wp_set_engine_config",
+           "wp_autotune", "wp_mlp_create", "wp_mlp_destroy", "wp_mlp_train",
            "wp_mlp_train_step", "wp_mlp_shape", "wp_mlp_get", "wp_mlp_set", "wp_mlp_logits", "wp_mlp_propose",
            "wp_mlp_hybrid_classify", "wp_mlp_hybrid_classify_device"]
 
@@ -184,6 +185,12 @@ def load_library(path: Optional[str] = None):
     lib.wp_hybrid_classify.restype = I
     lib.wp_hybrid_classify_device.argtypes = [V, V, I, I, D, I, D, V, V, V]
     lib.wp_hybrid_classify_device.restype = I
+    lib.wp_ctx_set_graphs.argtypes = [V, I]
+    lib.wp_ctx_set_graphs.restype = I
+    lib.wp_set_engine_config.argtypes = [V, V]
+    lib.wp_set_engine_config.restype = I
+    lib.wp_autotune.argtypes = [V, V, I, D, V, ctypes.POINTER(D)]
+    lib.wp_autotune.restype = I
     lib.wp_simulate_reads.argtypes = [V, I, ctypes.c_ulonglong, V, V, V]
     lib.wp_simulate_reads.restype = I
     LL, U64, F = ctypes.c_longlong, ctypes.c_ulonglong, ctypes.c_float
@@ -439,6 +446,23 @@ class Context:
         self._check(self.lib.wp_hybrid_classify_device(self.h, ctypes.c_void_p(d_rads_ptr), R, k, sig, h,
                                                        dist_cutoff, ctypes.c_void_p(d_id), ctypes.c_void_p(d_score),
                                                        ctypes.c_void_p(d_total)))
+
+    def set_graphs(self, enable: bool) -> None:
+        self._check(self.lib.wp_ctx_set_graphs(self.h, 1 if enable else 0))
+
+    def set_engine_config(self, cfg=None) -> None:
+        """(pass-1 threads, pass-1 CTAs/SM, pass-2 threads, pass-2 CTAs/SM) or None."""
+        arr = None if cfg is None else np.ascontiguousarray(cfg, dtype=np.int32)
+        self._check(self.lib.wp_set_engine_config(self.h, _ptr(arr)))
+
+    def autotune(self, rads: np.ndarray, dist_cutoff: float = DBL_MAX):
+        """wp_autotune on a sample of reads: (chosen shape, its ms)."""
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        cfg = np.zeros(4, np.int32)
+        ms = ctypes.c_double()
+        self._check(self.lib.wp_autotune(self.h, _ptr(rads), rads.shape[0], dist_cutoff, _ptr(cfg),
+                                         ctypes.byref(ms)))
+        return tuple(int(x) for x in cfg), ms.value
 
     def simulate_reads(self, R: int, seed: int, tracks: bool = False):
         """wp_simulate_reads: (rads [R,T,C], peptide index [R] (-1: not

@@ -50,6 +50,7 @@ cudaError_t wp_launch_nn_dist(int DP, bool hist, cudaStream_t s, const NNArgs& a
 cudaError_t wp_launch_nn_select(int grid, cudaStream_t s, const NNSelectArgs& a);
 cudaError_t wp_launch_nn_threshold(cudaStream_t s, const NNArgs& a);
 int wp_nn_bins();
+int wp_engine_max_threads();
 cudaError_t wp_launch_sim_reads(const SimParams& p, cudaStream_t s);
 #include <cuda_bf16.h>
 cudaError_t wp_mlp_launch_input(const float* xf, const double* xd, int B, int TC, __nv_bfloat16* X, cudaStream_t s);
@@ -87,14 +88,20 @@ long wp_fit_floats_per_thread(int T, int C, int S, bool has_block);
 
 namespace {
 
+// Incremented whenever a device buffer is (re)allocated: a captured graph
+// holds buffer addresses, so it is only replayed while this is unchanged.
+long long g_alloc_epoch = 0;
+
 struct DevBuf {
     void* p = nullptr;
     size_t cap = 0;
     ~DevBuf() {
         if (p) cudaFree(p);
+        g_alloc_epoch++;
     }
     cudaError_t ensure(size_t bytes) {
         if (bytes <= cap) return cudaSuccess;
+        g_alloc_epoch++;
         if (p) cudaFree(p);
         p = nullptr;
         cap = 0;
@@ -114,6 +121,29 @@ constexpr int kPass1Threads = 256;
 constexpr int kPass2Threads = 256;
 
 }  // namespace
+
+// Launch shape of the two engine passes: threads per CTA and CTAs per SM
+// (the slab per thread follows from them), chosen by wp_autotune per
+// (channels, blocking, max dyes, timesteps) or the default below.
+struct EngineCfg {
+    int t1 = 256, s1 = 2, t2 = 256, s2 = 1;
+    bool operator==(const EngineCfg& o) const { return t1 == o.t1 && s1 == o.s1 && t2 == o.t2 && s2 == o.s2; }
+};
+
+// Arguments a captured classify graph was built for.
+struct GraphKey {
+    const double* rads = nullptr;
+    int R = -1;
+    double cutoff = 0;
+    void* out[3] = {nullptr, nullptr, nullptr};
+    long long model_version = -1, pep_version = -1, alloc_epoch = -1;
+    EngineCfg cfg;
+    bool operator==(const GraphKey& o) const {
+        return rads == o.rads && R == o.R && cutoff == o.cutoff && out[0] == o.out[0] && out[1] == o.out[1] &&
+               out[2] == o.out[2] && model_version == o.model_version && pep_version == o.pep_version &&
+               alloc_epoch == o.alloc_epoch && cfg == o.cfg;
+    }
+};
 
 struct wp_ctx {
     int device = 0;
@@ -156,6 +186,15 @@ struct wp_ctx {
     double t_ms[6] = {0, 0, 0, 0, 0, 0};
     long long t_n[6] = {0, 0, 0, 0, 0, 0};
     size_t nn_acc_cleared = 0;  // bytes of the kNN accumulators known to be zero
+
+    // engine launch shapes (autotuned per shape key) and classify graphs
+    std::vector<std::pair<long long, EngineCfg>> tuned;
+    bool force_cfg = false;
+    EngineCfg forced;
+    bool graphs = true;
+    GraphKey gkey, gpending;
+    cudaGraphExec_t gexec = nullptr;
+    long long graph_launches = 0;  // kernels in the captured graph
     int last_engine_grid = 0;
     long long last_slots = 0;
 
@@ -339,6 +378,18 @@ int slab_half_for(wp_ctx* ctx, int threads, int per_sm, bool hb) {
     return (int)((budget - fixed) / (2 * elem * threads));
 }
 
+long long cfg_key(const wp_ctx* ctx) {
+    return ((long long)ctx->hm.C * 2 + (ctx->hm.has_block ? 1 : 0)) * 100000 + (long long)ctx->dmax * 100 + ctx->hm.T;
+}
+
+EngineCfg cfg_for(const wp_ctx* ctx) {
+    if (ctx->force_cfg) return ctx->forced;
+    const long long k = cfg_key(ctx);
+    for (const auto& kv : ctx->tuned)
+        if (kv.first == k) return kv.second;
+    return EngineCfg();
+}
+
 enum Mode { MODE_CLASSIFY, MODE_LOGP, MODE_FLOPS };
 
 // Everything between "reads are on the device" and "per-read outputs are
@@ -461,24 +512,26 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
                 dense_warps = w;
                 break;
             }
-        // Pass 1: two CTAs of 256 threads per SM; pass 2: one CTA of 256
-        // with twice the slab; the dense kernel takes what is left.
-        int half1 = slab_half_for(ctx, kPass1Threads, 2, hb);
-        int half2 = slab_half_for(ctx, kPass2Threads, 1, hb);
+        // Pass 1 and pass 2 launch shapes (default: 2 CTAs of 256 threads
+        // per SM, then 1 CTA of 256 with twice the slab); the dense kernel
+        // takes what is left.
+        const EngineCfg cfg = cfg_for(ctx);
+        int half1 = slab_half_for(ctx, cfg.t1, cfg.s1, hb);
+        int half2 = slab_half_for(ctx, cfg.t2, cfg.s2, hb);
         if (half1 < 4 || half2 < 4)
             return fail(ctx, WP_ERR_UNSUPPORTED, "shared memory too small for the pair engine");
         {
             TimedLaunch tl(ctx, 0);
-            size_t smem = wp_engine_smem_bytes(half1, 0, hb, kPass1Threads);
-            WP_CUDA(wp_launch_engine(C, hb, kPass1Threads, smem, ctx->stream, a, a.work, cnt + 0, cnt + 1,
+            size_t smem = wp_engine_smem_bytes(half1, 0, hb, cfg.t1);
+            WP_CUDA(wp_launch_engine(C, hb, cfg.t1, smem, ctx->stream, a, a.work, cnt + 0, cnt + 1,
                                      ctx->d_ovf1.as<int2>(), cnt + 2, half1, 0, 0,
                                      &ctx->last_engine_grid), "engine pass 1");
             ctx->launches++;
         }
         {
             TimedLaunch tl(ctx, 0);
-            size_t smem = wp_engine_smem_bytes(half2, 0, hb, kPass2Threads);
-            WP_CUDA(wp_launch_engine(C, hb, kPass2Threads, smem, ctx->stream, a, ctx->d_ovf1.as<int2>(),
+            size_t smem = wp_engine_smem_bytes(half2, 0, hb, cfg.t2);
+            WP_CUDA(wp_launch_engine(C, hb, cfg.t2, smem, ctx->stream, a, ctx->d_ovf1.as<int2>(),
                                      cnt + 2, cnt + 3, ctx->d_ovf2.as<int2>(), cnt + 4, half2, 0, dense_warps == 0 ? 1 : 0, nullptr), "engine pass 2");
             ctx->launches++;
         }
@@ -909,6 +962,7 @@ void wp_ctx_destroy(wp_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     collect_timing(ctx);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -1101,11 +1155,178 @@ wp_status wp_hmm_classify_device(wp_ctx* ctx, const double* d_rads, int R, doubl
     if (st != WP_OK) return st;
     if (R == 0) return WP_OK;
     if (ctx->P == 0) return fail(ctx, WP_ERR_INVALID, "no peptides");
-    st = run_batch(ctx, d_rads, R, dist_cutoff, nullptr, nullptr, MODE_CLASSIFY, nullptr, d_out_id,
-                   d_out_score, d_out_total, nullptr, nullptr);
+    st = plan_peptides(ctx);
     if (st != WP_OK) return st;
+    // CUDA graph of the launch sequence: the second call with the same
+    // arguments captures it, later ones replay it (buffers are allocated by
+    // the first, uncaptured call).  Not while per-kernel timing is on.
+    GraphKey key;
+    key.rads = d_rads;
+    key.R = R;
+    key.cutoff = dist_cutoff;
+    key.out[0] = d_out_id;
+    key.out[1] = d_out_score;
+    key.out[2] = d_out_total;
+    key.model_version = ctx->model_version;
+    key.pep_version = ctx->pep_version;
+    key.alloc_epoch = g_alloc_epoch;
+    key.cfg = cfg_for(ctx);
+    const bool use_graph = ctx->graphs && !ctx->timing;
+    if (use_graph && ctx->gexec && key == ctx->gkey) {
+        WP_CUDA(cudaGraphLaunch(ctx->gexec, ctx->stream), "graph launch");
+        ctx->launches += ctx->graph_launches;
+    } else if (use_graph && key == ctx->gpending) {
+        if (ctx->gexec) {
+            cudaGraphExecDestroy(ctx->gexec);
+            ctx->gexec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        WP_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        const long long l0 = ctx->launches;
+        st = run_batch(ctx, d_rads, R, dist_cutoff, nullptr, nullptr, MODE_CLASSIFY, nullptr, d_out_id,
+                       d_out_score, d_out_total, nullptr, nullptr);
+        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+        if (st != WP_OK) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "end capture");
+        if (g_alloc_epoch != key.alloc_epoch) {
+            // a buffer moved while capturing: run directly this time
+            cudaGraphDestroy(g);
+            ctx->gpending = GraphKey();
+            st = run_batch(ctx, d_rads, R, dist_cutoff, nullptr, nullptr, MODE_CLASSIFY, nullptr, d_out_id,
+                           d_out_score, d_out_total, nullptr, nullptr);
+            if (st != WP_OK) return st;
+            return async ? WP_OK : finish(ctx);
+        }
+        ctx->graph_launches = ctx->launches - l0;
+        ce = cudaGraphInstantiate(&ctx->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            ctx->gexec = nullptr;
+            return cuda_fail(ctx, ce, "graph instantiate");
+        }
+        ctx->gkey = key;
+        ctx->launches -= ctx->graph_launches;  // counted when they run
+        WP_CUDA(cudaGraphLaunch(ctx->gexec, ctx->stream), "graph launch");
+        ctx->launches += ctx->graph_launches;
+    } else {
+        st = run_batch(ctx, d_rads, R, dist_cutoff, nullptr, nullptr, MODE_CLASSIFY, nullptr, d_out_id,
+                       d_out_score, d_out_total, nullptr, nullptr);
+        if (st != WP_OK) return st;
+        ctx->gpending = key;
+    }
     if (async) return WP_OK;
     return finish(ctx);
+}
+
+wp_status wp_ctx_set_graphs(wp_ctx* ctx, int enable) {
+    if (!ctx) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->graphs = enable != 0;
+    return WP_OK;
+}
+
+wp_status wp_set_engine_config(wp_ctx* ctx, const int32_t* cfg4) {
+    if (!ctx) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (!cfg4) {
+        ctx->force_cfg = false;
+        return WP_OK;
+    }
+    for (int i = 0; i < 4; i += 2)
+        if (cfg4[i] < 32 || cfg4[i] > wp_engine_max_threads() || cfg4[i] % 32 || cfg4[i + 1] < 1 || cfg4[i + 1] > 4)
+            return fail(ctx, WP_ERR_INVALID, "engine config out of range");
+    ctx->forced.t1 = cfg4[0];
+    ctx->forced.s1 = cfg4[1];
+    ctx->forced.t2 = cfg4[2];
+    ctx->forced.s2 = cfg4[3];
+    ctx->force_cfg = true;
+    return WP_OK;
+}
+
+wp_status wp_autotune(wp_ctx* ctx, const double* rads, int R, double dist_cutoff, int32_t* out_cfg4,
+                      double* out_best_ms) {
+    if (!ctx || R < 1 || !rads) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    wp_status st = check_ready(ctx);
+    if (st != WP_OK) return st;
+    if (ctx->P == 0) return fail(ctx, WP_ERR_INVALID, "no peptides");
+    st = upload_reads(ctx, rads, R);
+    if (st != WP_OK) return st;
+    st = plan_peptides(ctx);
+    if (st != WP_OK) return st;
+    WP_CUDA(ctx->d_out_id.ensure(sizeof(int) * R), "alloc");
+    WP_CUDA(ctx->d_out_score.ensure(sizeof(double) * R), "alloc");
+    WP_CUDA(ctx->d_out_total.ensure(sizeof(double) * R), "alloc");
+    const bool was_forced = ctx->force_cfg, was_timing = ctx->timing;
+    const EngineCfg was = ctx->forced;
+    ctx->timing = false;
+    EngineCfg best;
+    double best_ms = 1e300;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int threads[2] = {128, 256};
+    for (int t1 : threads)
+        for (int s1 = 1; s1 <= 3; s1++)
+            for (int t2 : threads) {
+                EngineCfg c;
+                c.t1 = t1;
+                c.s1 = s1;
+                c.t2 = t2;
+                c.s2 = 1;
+                const bool hb = ctx->hm.has_block != 0;
+                if (slab_half_for(ctx, c.t1, c.s1, hb) < 4 || slab_half_for(ctx, c.t2, c.s2, hb) < 4) continue;
+                ctx->forced = c;
+                ctx->force_cfg = true;
+                double ms_best_c = 1e300;
+                bool ok = true;
+                for (int rep = 0; rep < 3 && ok; rep++) {  // first run warms up
+                    cudaEventRecord(e0, ctx->stream);
+                    if (run_batch(ctx, ctx->d_rads.as<double>(), R, dist_cutoff, nullptr, nullptr, MODE_CLASSIFY,
+                                  nullptr, ctx->d_out_id.as<int>(), ctx->d_out_score.as<double>(),
+                                  ctx->d_out_total.as<double>(), nullptr, nullptr) != WP_OK ||
+                        finish(ctx) != WP_OK) {
+                        ok = false;
+                        break;
+                    }
+                    cudaEventRecord(e1, ctx->stream);
+                    cudaEventSynchronize(e1);
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (rep > 0) ms_best_c = std::min(ms_best_c, (double)ms);
+                }
+                if (ok && ms_best_c < best_ms) {
+                    best_ms = ms_best_c;
+                    best = c;
+                }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->force_cfg = was_forced;
+    ctx->forced = was;
+    ctx->timing = was_timing;
+    ctx->err.clear();
+    if (best_ms >= 1e300) return fail(ctx, WP_ERR_UNSUPPORTED, "no engine configuration ran");
+    const long long k = cfg_key(ctx);
+    bool found = false;
+    for (auto& kv : ctx->tuned)
+        if (kv.first == k) {
+            kv.second = best;
+            found = true;
+        }
+    if (!found) ctx->tuned.push_back({k, best});
+    if (out_cfg4) {
+        out_cfg4[0] = best.t1;
+        out_cfg4[1] = best.s1;
+        out_cfg4[2] = best.t2;
+        out_cfg4[3] = best.s2;
+    }
+    if (out_best_ms) *out_best_ms = best_ms;
+    return WP_OK;
 }
 
 wp_status wp_hmm_loglik_all(wp_ctx* ctx, const double* rads, int R, double dist_cutoff, double* out_logp) {
