@@ -338,6 +338,7 @@ wp_status plan_peptides(wp_ctx* ctx) {
             rec.tot[e] = (uint8_t)(d >= 0 ? rem[d] : 0);
             if (d >= 0) rem[d]--;
         }
+        wp_pack_peptide(rec);
     }
     // Shape order (Edman-slice size, then dye counts) for the compaction.
     std::vector<int> perm(P);

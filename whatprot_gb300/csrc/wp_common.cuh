@@ -45,7 +45,22 @@ struct PeptideRec {
     uint8_t D[WP_MAX_CHANNELS];
     int8_t dye[WP_MAX_TIMESTEPS];
     uint8_t tot[WP_MAX_TIMESTEPS];
+    // Positions 0..15 packed 4 bits each (the engine reads these when
+    // T <= 17): dye_pk nibble e = dye[e] + 1, tot_pk nibble e = tot[e].
+    uint64_t dye_pk;
+    uint64_t tot_pk;
 };
+
+// Fills dye_pk / tot_pk from dye[] and tot[] (tot <= 15 per channel).
+__host__ __device__ inline void wp_pack_peptide(PeptideRec& r) {
+    uint64_t d = 0, t = 0;
+    for (int e = 0; e < 16 && e < WP_MAX_TIMESTEPS; e++) {
+        d |= (uint64_t)((r.dye[e] + 1) & 15) << (4 * e);
+        t |= (uint64_t)(r.tot[e] & 15) << (4 * e);
+    }
+    r.dye_pk = d;
+    r.tot_pk = t;
+}
 
 // Emission factor of one table entry: value = mant * 2^expo exactly as the
 // reference's FP64 product, mant in [0.5, 1) rounded to FP32; mant == 0 means
@@ -73,6 +88,13 @@ struct SmemModel {
     float dud[WP_MAX_CHANNELS][WP_TRI];
     float bleach[WP_MAX_CHANNELS][WP_TRI];
     float p_det[WP_MAX_TIMESTEPS];
+    // Edman success coefficients (edman-transition.cc:62-162) at
+    // [tot * 16 + n]: for a state with n dyes left of the channel cut at a
+    // position with tot dyes of that channel remaining, x = (1 - p_fail) *
+    // (tot - n) / tot (the cut dye was another one) and y = (1 - p_fail) *
+    // (n + 1) / tot (the state one dye up lost the cut dye).  Row tot = 0
+    // (no dye at the position): x = 1 - p_fail, y = 0.
+    float2 edman[16 * 16];
 };
 
 // Everything one batch of reads needs on the device.  Per-read arrays are
@@ -134,6 +156,17 @@ __device__ __forceinline__ void load_smem_model(SmemModel& S, const DevModel& m)
         S.bleach[c][k] = m.bleach[c][k];
     }
     for (int t = threadIdx.x; t < m.T; t += blockDim.x) S.p_det[t] = m.p_det[t];
+    for (int i = threadIdx.x; i < 16 * 16; i += blockDim.x) {
+        const int tot = i >> 4, n = i & 15;
+        const float qf = 1.0f - m.pf;
+        float2 v = make_float2(qf, 0.0f);
+        if (tot > 0) {
+            const float c1 = qf * __frcp_rn((float)tot);
+            v.x = n < tot ? fmaf(-(float)n, c1, qf) : 0.0f;
+            v.y = (float)(n + 1) * c1;
+        }
+        S.edman[i] = v;
+    }
 }
 
 // Arguments of one Baum-Welch E-step (wp_fit.cu).

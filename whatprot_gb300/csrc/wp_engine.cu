@@ -24,6 +24,17 @@
 // channels) are out of line too.  This keeps the timestep loop small enough
 // for the instruction cache.
 //
+// Two shortcuts follow from the box statistics of real workloads, where
+// most timesteps of most pairs have a one-state emission box: a dud or
+// bleach step along a channel that is one wide on both sides is a single
+// coefficient, carried to the next emission multiply instead of a pass over
+// the state; and a one-state emission box runs Edman and emission as one
+// loop over the Edman slices.  Edman coefficients come from a per-CTA table
+// indexed by (remaining dyes of the cut channel, dye count of the state).
+// All lanes of a warp process the same timestep together (lanes are pairs
+// of one read), so a warp pays for every path any of its lanes takes in a
+// timestep; the number of distinct paths is kept small for that reason.
+//
 // With blocking (p_initial_block or p_cyclic_block nonzero) each state holds
 // the normal and the broken-N value as a float2.
 #include <cuda_runtime.h>
@@ -254,8 +265,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
 #pragma unroll
     for (int c = 0; c < C; c++) D1 = bset(D1, c, pep.D[c] + 1);
     // Emission box of timestep t: [L_t, min(U_t, D + 1)), packed.
-    auto emission_box = [&](int t) {
-        const uint32_t lw = Lpk[t], uw = Upk[t];
+    auto box_of = [&](uint32_t lw, uint32_t uw) {
         PBox b;
         b.lo = lw & 0x7f7f7f7fu;  // bit 31 of the word is the allow flag
         b.w = 0;
@@ -263,6 +273,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         for (int c = 0; c < C; c++) b.w = bset(b.w, c, min(bget(uw, c), bget(D1, c)) - bget(b.lo, c));
         return b;
     };
+    auto emission_box = [&](int t) { return box_of(Lpk[t], Upk[t]); };
 
     // First pass: the largest box any step of this pair uses (emission box
     // Nx_t, bleach output / Edman input box [L_t, min(U_t + 1, U_{t-1}))
@@ -292,13 +303,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
     // Dye channel and remaining dyes of that channel per Edman position,
     // packed 4 bits each (positions < 16) so the Edman loop reads registers.
     const bool pk = T <= 17;
-    uint64_t dye_pk = 0, tot_pk = 0;
-    if (pk) {
-        for (int e = 0; e + 1 < T; e++) {
-            dye_pk |= (uint64_t)((pep.dye[e] + 1) & 15) << (4 * e);
-            tot_pk |= (uint64_t)(pep.tot[e] & 15) << (4 * e);
-        }
-    }
+    const uint64_t dye_pk = pep.dye_pk, tot_pk = pep.tot_pk;
 
     V* cur = slab;
     V* nxt = slab + half * stride;
@@ -321,15 +326,24 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         }
         cur[(v - 1) * stride] = start;
     }
+    // A binomial step along a channel whose input and output boxes are both
+    // one wide is one coefficient for the whole state: it is carried in
+    // bscale and applied with the next emission multiply instead of a pass.
+    float bscale = 1.0f;
     {
         const PBox n0 = emission_box(0);
 #pragma unroll 1
         for (int c = 0; c < C; c++) {
             const int wout = bget(n0.w, c);
-            binomial_step<C, V>(cur, nxt, stride, 1, bx, c, bget(bx.lo, c), wout, M.dud[c]);
-            V* tmp = cur;
-            cur = nxt;
-            nxt = tmp;
+            if (bget(bx.w, c) == 1 && wout == 1) {
+                const int from = bget(bx.lo, c), to = bget(bx.lo, c);
+                bscale *= M.dud[c][from * (from + 1) / 2 + to];
+            } else {
+                binomial_step<C, V>(cur, nxt, stride, 1, bx, c, bget(bx.lo, c), wout, M.dud[c]);
+                V* tmp = cur;
+                cur = nxt;
+                nxt = tmp;
+            }
             bx.w = bset(bx.w, c, wout);
         }
     }
@@ -338,10 +352,55 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
     float pd = 0.0f;        // detached state, in the rescaled frame
     int k_prev = 0;         // exponent removed at the last rescale
     float fac_prev = 1.0f;  // (1 - p_detach) pending from the last timestep
-    for (int t = 0; t < T; t++) {
-        const PBox nx = emission_box(t);
-        const bool allow_t = (Lpk[t] >> 31) != 0;
+    // Closes timestep t after its emission multiply: the detached state
+    // (kept only while the box includes zero, peptide-emission.cc:218-223),
+    // the exact power-of-two rescale and the next timestep's detach folded
+    // into the rescaled frame (detach-transition.cc:36-68).  Returns true
+    // when the pair is finished (result written).
+    auto close_step = [&](int t, float part, float em0, int kmax, bool allow_t) -> bool {
+        pd = allow_t ? pd * em0 : 0.0f;
+        expo += kmax;
+        const float tot = part + pd;
+        if (!(tot > 0.0f) || !isfinite(tot)) {
+            *out_mant = 0.0f;
+            *out_expo = 0;
+            return true;
+        }
+        int k;
+        const float fm = frexpf(tot, &k);
+        if (t == T - 1) {
+            *out_mant = fm;
+            *out_expo = expo + k;
+            return true;
+        }
+        expo += k;
+        const float f = exp2i(-k);
+        // p_detached += p * sum of the states
+        pd = (pd + M.p_det[t] * part) * f;
+        k_prev = k;
+        fac_prev = 1.0f - M.p_det[t];
+        return false;
+    };
+    uint32_t lw_next = Lpk[0], uw_next = Upk[0];
+    int t = 0;
+    for (;;) {
+        // this timestep's box words; the next timestep's are fetched now so
+        // their latency hides behind this timestep's work
+        const uint32_t lw = lw_next, uw = uw_next;
+        if (t + 1 < T) {
+            lw_next = Lpk[t + 1];
+            uw_next = Upk[t + 1];
+        }
+        const PBox nx = box_of(lw, uw);
+        const bool allow_t = (lw >> 31) != 0;
+        // One-state emission box: Edman and emission run as one loop over
+        // the Edman slices (most timesteps of most pairs).
+        const bool single = t > 0 && pk && !m.interacting && bvol<C>(nx.w) == 1;
+        int kmax = 0;
+        float part = 0.0f;
+        float em0 = 0.0f;
         if (t > 0) {
+            bscale = 1.0f;
             // Cyclic block (block-transition.cc:33-62) over e < t and the
             // previous emission box.
             if constexpr (HB) {
@@ -361,17 +420,22 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             for (int c = 0; c < C; c++) {
                 const int ln = bget(nx.lo, c);
                 const int bu = min(ln + bget(nx.w, c) + 1, bget(bx.lo, c) + bget(bx.w, c));
-                binomial_step<C, V>(cur, nxt, stride, t, bx, c, ln, bu - ln, M.bleach[c]);
-                V* tmp = cur;
-                cur = nxt;
-                nxt = tmp;
+                if (bget(bx.w, c) == 1 && bu - ln == 1) {
+                    const int from = bget(bx.lo, c);
+                    bscale *= from >= ln ? M.bleach[c][from * (from + 1) / 2 + ln] : 0.0f;
+                } else {
+                    binomial_step<C, V>(cur, nxt, stride, t, bx, c, ln, bu - ln, M.bleach[c]);
+                    V* tmp = cur;
+                    cur = nxt;
+                    nxt = tmp;
+                }
                 bx.lo = bset(bx.lo, c, ln);
                 bx.w = bset(bx.w, c, bu - ln);
             }
             // Edman (edman-transition.cc:62-162) as a gather from slices e-1
             // (success) and e (failure) of the bleached box into the
             // emission box; both boxes share the lower corner L_t.
-            {
+            if (!single) {
                 const float pf = m.pf, qf = 1.0f - m.pf;
                 int stb[C];
                 int vb = 1;
@@ -392,8 +456,8 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
                             tot_i = pep.tot[e - 1];
                         }
                     }
-                    // (1 - p_fail) / DyeTrack(e - 1, dc): one reciprocal per slice.
-                    const float c1 = dc >= 0 ? qf * __frcp_rn((float)tot_i) : 0.0f;
+                    // Edman coefficients of this slice: row DyeTrack(e - 1, dc)
+                    const float2* ed = M.edman + tot_i * 16;
                     int d_lo = 0, d_wb = 0, d_st = 0;
 #pragma unroll
                     for (int c = 0; c < C; c++)
@@ -435,7 +499,8 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
                                 for (int c = 0; c < C; c++)
                                     if (c == dc) jd = jc[c];
                                 const int nc = d_lo + jd;
-                                add = nc < tot_i ? fmaf(-(float)nc, c1, qf) * xin : 0.0f;
+                                const float2 cf = ed[nc];
+                                add = cf.x * xin;
                                 if (jd + 1 < d_wb) {
                                     float xr;
                                     if constexpr (HB) {
@@ -443,7 +508,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
                                     } else {
                                         xr = succ_row[(ib + d_st) * stride];
                                     }
-                                    add = fmaf((float)(nc + 1) * c1, xr, add);
+                                    add = fmaf(cf.y, xr, add);
                                 }
                             }
                             if constexpr (HB) {
@@ -473,13 +538,90 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         // ---- Emission t (peptide-emission.cc:212-243).  Factors normalised
         // by the largest exponent over the pair's box (a power of two, carried
         // in expo); the pending rescale is folded into the multiplier.
-        int kmax = 0;
-        float part = 0.0f;
-        float em0 = 0.0f;
         bool narrow = !m.interacting;
 #pragma unroll
         for (int c = 0; c < C; c++) narrow = narrow && bget(nx.w, c) <= 4;
-        if (narrow) {
+        if (single) {
+            // The box's one state has factor prod_c mant_c * 2^(sum_c expo_c);
+            // the multiplier also carries the pending rescale and bscale.
+            float wv = fac_prev * bscale * exp2i(min(-k_prev, 127));
+            float g1 = 1.0f;
+            bool dead = false;
+#pragma unroll
+            for (int c = 0; c < C; c++) {
+                const EmitEntry en = tab[(t * C + c) * a.W + bget(nx.lo, c)];
+                dead = dead || en.mant == 0.0f;
+                wv *= en.mant;
+                g1 *= en.mant;
+                kmax += en.expo;
+            }
+            if (dead) {
+                *out_mant = 0.0f;
+                *out_expo = 0;
+                return 0;
+            }
+            if (allow_t) em0 = g1;
+            // Edman gather into the one state (the bleached box has width 1
+            // or 2 per channel, lower corner L_t), times the emission factor.
+            const float pf = m.pf;
+            uint32_t stpk = 0;  // the bleached box's strides, one byte per channel (<= 8)
+            int vb = 1;
+#pragma unroll
+            for (int c = C - 1; c >= 0; c--) {
+                stpk = bset(stpk, c, vb);
+                vb *= bget(bx.w, c);
+            }
+            uint64_t dp = dye_pk, tp = tot_pk;
+            V xprev = vzero(V());
+            for (int e = 0; e <= t; e++) {
+                const V f = e < t ? cur[e * vb * stride] : vzero(V());
+                V v;
+                if constexpr (HB) {
+                    v = make_float2(pf * f.x, f.y);  // broken-N copied unchanged
+                } else {
+                    v = pf * f;
+                }
+                if (e >= 1) {
+                    const int d4 = (int)(dp & 15);  // dye channel + 1 (0: no dye)
+                    const int tot_i = (int)(tp & 15);
+                    dp >>= 4;
+                    tp >>= 4;
+                    float xin;
+                    if constexpr (HB) {
+                        xin = xprev.x;
+                    } else {
+                        xin = xprev;
+                    }
+                    const int sh = 8 * max(d4 - 1, 0);
+                    const int nc = (int)((bx.lo >> sh) & 0xffu);
+                    const float2 cf = M.edman[(d4 ? tot_i : 0) * 16 + nc];
+                    float add = cf.x * xin;
+                    if (d4 && ((bx.w >> sh) & 0xffu) > 1) {
+                        const int ir = (e - 1) * vb + (int)((stpk >> sh) & 0xffu);
+                        float xr;
+                        if constexpr (HB) {
+                            xr = cur[ir * stride].x;
+                        } else {
+                            xr = cur[ir * stride];
+                        }
+                        add = fmaf(cf.y, xr, add);
+                    }
+                    if constexpr (HB) {
+                        v.x += add;
+                    } else {
+                        v += add;
+                    }
+                }
+                xprev = f;
+                const V s = vmul(wv, v);
+                nxt[e * stride] = s;
+                part += vtotal(s);
+            }
+            V* tmp = cur;
+            cur = nxt;
+            nxt = tmp;
+            bx = nx;
+        } else if (narrow) {
             // Per channel: the box's entries normalised by their largest
             // exponent, in registers; the factor of state n is
             // prod_c g[c][n_c - L_t] * 2^kmax.
@@ -515,7 +657,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
                 for (int c = 0; c < C; c++) em0 *= g[c][0];
             }
             // the pending rescale 2^-k_prev (1 - p) of the last timestep
-            const float sf = fac_prev * exp2i(min(-k_prev, 127));
+            const float sf = fac_prev * bscale * exp2i(min(-k_prev, 127));
             const int vn = bvol<C>(nx.w);
             int jc[C];
 #pragma unroll
@@ -540,7 +682,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
                 }
             }
         } else {
-            part = emission_table<C, V>(cur, stride, t, nx, a.W, tab, m.interacting != 0, fac_prev, k_prev,
+            part = emission_table<C, V>(cur, stride, t, nx, a.W, tab, m.interacting != 0, fac_prev * bscale, k_prev,
                                         &kmax, &em0);
             if (kmax == WP_EXPO_ZERO) {
                 *out_mant = 0.0f;
@@ -549,34 +691,9 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             }
             if (!allow_t) em0 = 0.0f;
         }
-        // Detached state: kept only while the box includes zero
-        // (peptide-emission.cc:218-223).
-        pd = allow_t ? pd * em0 : 0.0f;
-        expo += kmax;
-        const float tot = part + pd;
-        if (!(tot > 0.0f) || !isfinite(tot)) {
-            *out_mant = 0.0f;
-            *out_expo = 0;
-            return 0;
-        }
-        int k;
-        const float fm = frexpf(tot, &k);
-        if (t == T - 1) {
-            *out_mant = fm;
-            *out_expo = expo + k;
-            return 0;
-        }
-        expo += k;
-        const float f = exp2i(-k);
-        // Detach of the next timestep in the rescaled frame
-        // (detach-transition.cc:36-68): p_detached += p * sum of the states.
-        pd = (pd + M.p_det[t] * part) * f;
-        k_prev = k;
-        fac_prev = 1.0f - M.p_det[t];
+        if (close_step(t, part, em0, kmax, allow_t)) return 0;
+        ++t;
     }
-    *out_mant = 0.0f;
-    *out_expo = 0;
-    return 0;
 }
 
 // Lists one engine pass reads and spills to.
@@ -633,6 +750,8 @@ __global__ void __launch_bounds__(WP_ENGINE_THREADS) wp_engine_kernel(BatchArgs 
     }
 }
 
+// Shared memory of one engine CTA: the model, two slab halves per thread
+// and scr_floats more words per thread.
 size_t wp_engine_smem_bytes(int slab_half, int scr_floats, bool has_block, int threads) {
     size_t elem = has_block ? sizeof(float2) : sizeof(float);
     return ((sizeof(SmemModel) + 15) & ~(size_t)15) + (size_t)2 * slab_half * threads * elem +

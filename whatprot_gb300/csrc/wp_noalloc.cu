@@ -71,6 +71,7 @@ __global__ void wp_noalloc_peptides_kernel(const int16_t* __restrict__ seqs,
         rec.tot[e] = (uint8_t)(d >= 0 ? cnt[d] : 0);  // DyeTrack(e, d)
         if (d >= 0) cnt[d]--;
     }
+    wp_pack_peptide(rec);
     out[i] = rec;
 }
 
