@@ -500,12 +500,6 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
     a.ovf_head = cnt + 5;
     a.dense_S_cap = ((ctx->S_max + 31) / 32) * 32;
     if (n_slots > 0) {
-        {
-            TimedLaunch tl(ctx, 1);
-            wp_compact_kernel<<<R, 256, 0, ctx->stream>>>(a);
-            ctx->launches++;
-            WP_CUDA(cudaGetLastError(), "compact launch");
-        }
         // Dense fallback shape: as many warps as fit (0: unavailable).
         int dense_warps = 0;
         for (int w = 16; w >= 1; w--)
@@ -521,6 +515,18 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         int half2 = slab_half_for(ctx, cfg.t2, cfg.s2, hb);
         if (half1 < 4 || half2 < 4)
             return fail(ctx, WP_ERR_UNSUPPORTED, "shared memory too small for the pair engine");
+        // the compaction sends each pair to the first pass whose slab holds it
+        a.route_half1 = half1;
+        a.route_half2 = std::max(half1, half2);
+        a.route_dense = dense_warps > 0 ? 1 : 0;
+        a.mid = ctx->d_ovf1.as<int2>();
+        a.mid_count = cnt + 2;
+        {
+            TimedLaunch tl(ctx, 1);
+            wp_compact_kernel<<<R, 256, 0, ctx->stream>>>(a);
+            ctx->launches++;
+            WP_CUDA(cudaGetLastError(), "compact launch");
+        }
         {
             TimedLaunch tl(ctx, 0);
             size_t smem = wp_engine_smem_bytes(half1, 0, hb, cfg.t1);
@@ -1084,6 +1090,7 @@ wp_status wp_model_upload(wp_ctx* ctx, const wp_seq_model* m, int T) {
             if (h.inter[c][o] != 1.0 || h.flat[c][o] != 1.0) h.interacting = 1;
         }
     }
+    wp_fill_emission_tables(h);
     WP_CUDA(cudaMemcpyAsync(ctx->d_model.p, &h, sizeof(DevModel), cudaMemcpyHostToDevice, ctx->stream),
             "copy model");
     WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync model");

@@ -12,6 +12,7 @@
 //                   factors as (mantissa, exponent) pairs -- per (t, c, n)
 //                   when the channels do not interact, else per (t, n-vector).
 #pragma once
+#include <math.h>
 #include <stdint.h>
 
 #include "../../include/whatprot_gb300.h"
@@ -37,7 +38,33 @@ struct DevModel {
     double mu[WP_MAX_CHANNELS];
     double inter[WP_MAX_CHANNELS][WP_MAX_CHANNELS];
     double flat[WP_MAX_CHANNELS][WP_MAX_CHANNELS];
+    // Without interactions ChannelModel's per-count quantities depend on the
+    // channel and the count n alone (channel-model.h:35-70), so they are
+    // tabulated once per model for n = 0 .. WP_W: adjusted mu, sigma,
+    // 1 / (sigma sqrt(2 pi)) and 2 sigma^2 (wp_fill_emission_tables).
+    double e_amu[WP_MAX_CHANNELS][WP_W + 1];
+    double e_sig[WP_MAX_CHANNELS][WP_W + 1];
+    double e_norm[WP_MAX_CHANNELS][WP_W + 1];
+    double e_den[WP_MAX_CHANNELS][WP_W + 1];
 };
+
+// Host side: fills the e_* tables of a non-interacting model from mu, sig
+// and bg_sig with the operations and order of ChannelModel::adjusted_mu,
+// sigma and pdf_helper.
+inline void wp_fill_emission_tables(DevModel& m) {
+    const double pi = 3.141592653589793238;
+    for (int c = 0; c < m.C; c++)
+        for (int n = 0; n <= WP_W; n++) {
+            const double amu = m.mu[c] * (double)n;
+            const double bg2 = m.bg_sig[c] * m.bg_sig[c];
+            const double var = amu * m.sig[c] * m.sig[c];
+            const double s = sqrt(bg2 + var);
+            m.e_amu[c][n] = amu;
+            m.e_sig[c][n] = s;
+            m.e_norm[c][n] = 1.0 / (s * sqrt(2.0 * pi));
+            m.e_den[c][n] = 2.0 * s * s;
+        }
+}
 
 // One peptide.  dye[e] is the channel removed by a successful Edman cycle at
 // position e (-1 none), tot[e] = DyeTrack(e, dye[e]).
@@ -132,7 +159,52 @@ struct BatchArgs {
     int* err;
     int slab_half;             // per-thread slab half, in state elements
     int dense_S_cap;           // overflow kernel: max states per Edman slice
+    // Routing by the compaction (route_half1 == 0: every live pair to
+    // `work`).  A pair whose largest box (pair_vmax) fits route_half1 goes to
+    // `work` (engine pass 1), one that fits route_half2 to `mid` (pass 2),
+    // the rest to `ovf` (the dense kernel; route_dense == 0: none, the pair
+    // gets P = 0 and err = 2).
+    int route_half1;
+    int route_half2;
+    int route_dense;
+    int2* mid;
+    int* mid_count;
 };
+
+// Largest state box, in elements with the Edman slices counted, that any
+// step of a pair uses: the start box [L_0, D + 1), and per timestep t >= 1
+// the previous emission box, the bleach output / Edman input box
+// [L_t, min(U_t + 1, U_{t-1})), the boxes in between (channels bleached so
+// far at their new width, the others at the old) and the emission box,
+// with U clamped to D + 1.  Lw / Uw are the read's packed box words.
+__device__ inline int pair_vmax(int C, int T, const uint32_t* Lw, const uint32_t* Uw, const uint8_t* D) {
+    int lo_p[WP_MAX_CHANNELS], w_p[WP_MAX_CHANNELS];
+    int vmax = 1;
+    for (int c = 0; c < C; c++) {
+        const int d1 = D[c] + 1;
+        const int l = (int)((Lw[0] >> (8 * c)) & 0x7fu);
+        lo_p[c] = l;
+        w_p[c] = min((int)((Uw[0] >> (8 * c)) & 0xffu), d1) - l;
+        vmax *= d1 - l;
+    }
+    for (int t = 1; t < T; t++) {
+        const uint32_t lw = Lw[t], uw = Uw[t];
+        int vp = t, vb = t, vn = t + 1, vm = t;
+        for (int c = 0; c < C; c++) {
+            const int ln = (int)((lw >> (8 * c)) & 0x7fu);
+            const int wn = min((int)((uw >> (8 * c)) & 0xffu), D[c] + 1) - ln;
+            const int wb = min(ln + wn + 1, lo_p[c] + w_p[c]) - ln;
+            vp *= w_p[c];
+            vb *= wb;
+            vn *= wn;
+            vm *= max(wb, w_p[c]);
+            lo_p[c] = ln;
+            w_p[c] = wn;
+        }
+        vmax = max(vmax, max(max(vp, vb), max(vn, vm)));
+    }
+    return vmax;
+}
 
 __host__ __device__ inline int slot_begin(const BatchArgs& a, int r) {
     return a.slot_off ? a.slot_off[r] : r * a.P;

@@ -14,8 +14,11 @@
 // lower corner).  Each thread owns a slab of shared memory holding two such
 // boxes (ping-pong); slabs are interleaved across the CTA's threads (element
 // k of thread i at k * blockDim.x + i) so every access of a warp hits 32
-// distinct banks whatever the index.  A pair whose largest box does not fit
-// its slab is handed to the next pass's list (wp_capi.cu).
+// distinct banks whatever the index.  The compaction (wp_prep.cu) routes
+// each pair to the first pass whose slab holds its largest box and leaves
+// that box's size in the pair's result slot; a pass checks it against its
+// slab before any write and hands a pair that does not fit to the next
+// pass's list.
 //
 // Boxes are kept packed, one byte per channel in a 32-bit word (lower
 // corner) and another (width), so that the per-channel loops need no
@@ -254,7 +257,7 @@ __device__ __noinline__ float emission_table(V* cur, int stride, int t, PBox nx,
 template <int C, bool HB>
 __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
                            const PeptideRec& pep, typename StateOf<HB>::V* slab, int stride,
-                           int half, float* out_mant, int* out_expo) {
+                           int half, int vmax, float* out_mant, int* out_expo) {
     using V = typename StateOf<HB>::V;
     const DevModel& m = *a.model;
     const int T = m.T;
@@ -275,31 +278,10 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
     };
     auto emission_box = [&](int t) { return box_of(Lpk[t], Upk[t]); };
 
-    // First pass: the largest box any step of this pair uses (emission box
-    // Nx_t, bleach output / Edman input box [L_t, min(U_t + 1, U_{t-1}))
-    // and the mixed boxes in between).
-    {
-        PBox p = emission_box(0);
-        int vmax = 1;
-#pragma unroll
-        for (int c = 0; c < C; c++) vmax *= bget(D1, c) - bget(p.lo, c);
-        for (int t = 1; t < T; t++) {
-            const PBox n = emission_box(t);
-            int vp = t, vb = t, vn = t + 1, vm = t;
-#pragma unroll
-            for (int c = 0; c < C; c++) {
-                const int wp = bget(p.w, c), ln = bget(n.lo, c), wn = bget(n.w, c);
-                const int wb = min(ln + wn + 1, bget(p.lo, c) + wp) - ln;
-                vp *= wp;
-                vb *= wb;
-                vn *= wn;
-                vm *= max(wb, wp);
-            }
-            vmax = max(vmax, max(max(vp, vb), max(vn, vm)));
-            p = n;
-        }
-        if (vmax > half) return 1;
-    }
+    // The largest box any step of this pair uses (pair_vmax, left in the
+    // pair's result slot by the compaction) must fit the slab half; a pair
+    // that does not is handed to the next pass before anything is written.
+    if (vmax > half) return 1;
     // Dye channel and remaining dyes of that channel per Edman position,
     // packed 4 bits each (positions < 16) so the Edman loop reads registers.
     const bool pk = T <= 17;
@@ -732,7 +714,8 @@ __global__ void __launch_bounds__(WP_ENGINE_THREADS) wp_engine_kernel(BatchArgs 
             const int p = slot_pep(a, rg.x, rg.y);
             float mant;
             int ex;
-            int ov = engine_pair<C, HB>(a, M, rg.x, a.peps[p], slab, nt, L.slab_half, &mant, &ex);
+            int ov = engine_pair<C, HB>(a, M, rg.x, a.peps[p], slab, nt, L.slab_half, a.res_expo[rg.y], &mant,
+                                        &ex);
             if (ov) {
                 if (L.spill_error) {
                     atomicExch(a.err, 2);

@@ -153,6 +153,7 @@ extern "C" wp_status wp_hmm_classify_noalloc(int device, const wp_seq_model* m, 
             if (hm.inter[c][o] != 1.0 || hm.flat[c][o] != 1.0) hm.interacting = 1;
         }
     }
+    wp_fill_emission_tables(hm);
     const int entries = wp_read_table_entries(T, C, W, hm.interacting);
     const long n_slots = (long)R * P;
     const size_t rtc = (size_t)R * T * C;
@@ -252,9 +253,6 @@ extern "C" wp_status wp_hmm_classify_noalloc(int device, const wp_seq_model* m, 
     WP_NA(cudaGetLastError());
     wp_read_summary_kernel<<<(R + 127) / 128, 128, 0, s>>>(a);
     WP_NA(cudaGetLastError());
-    wp_compact_kernel<<<R, 256, 0, s>>>(a);
-    WP_NA(cudaGetLastError());
-
     // Engine passes: the shapes the allocating path uses (two CTAs of 256
     // threads per SM, then one of 128), then the dense fallback.
     auto half_for = [&](int threads, int per_sm) {
@@ -272,6 +270,14 @@ extern "C" wp_status wp_hmm_classify_noalloc(int device, const wp_seq_model* m, 
             dense_warps = w;
             break;
         }
+    // the compaction sends each pair to the first pass whose slab holds it
+    a.route_half1 = half1;
+    a.route_half2 = half1 > half2 ? half1 : half2;
+    a.route_dense = dense_warps > 0 ? 1 : 0;
+    a.mid = reinterpret_cast<int2*>(base + o_ovf1);
+    a.mid_count = cnt + 2;
+    wp_compact_kernel<<<R, 256, 0, s>>>(a);
+    WP_NA(cudaGetLastError());
     WP_NA(wp_launch_engine(C, hb, 256, wp_engine_smem_bytes(half1, scr, hb, 256), s, a, a.work, cnt + 0,
                            cnt + 1, reinterpret_cast<int2*>(base + o_ovf1), cnt + 2, half1, scr, 0, nullptr));
     WP_NA(wp_launch_engine(C, hb, 128, wp_engine_smem_bytes(half2, scr, hb, 128), s, a,

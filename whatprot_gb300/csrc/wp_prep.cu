@@ -14,7 +14,9 @@
 //   wp_compact_kernel       one CTA per read: pairs whose pruned range is
 //                           empty get probability 0 (PeptideHMM::probability,
 //                           hmm/hmm/peptide-hmm.cc:94-100); the others are
-//                           appended to the work list of the pair engine.
+//                           appended to the work list of the first engine
+//                           pass whose per-thread slab holds their largest
+//                           box (pair_vmax), or to the dense kernel's list.
 //
 // Pruning.  After the reference's forward and backward prune passes
 // (hmm/hmm/peptide-hmm.cc:63-83) the box of emission t of a pair is
@@ -113,16 +115,23 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
         // The reference loops to a fixed point without a bound and cycles
         // forever for intensities below about -0.5 mu; stop after 1000
         // rounds (the oracle uses the same bound).
+        const bool tabled = !m.interacting;  // per-count quantities from the model's tables
         while (did_change && guard < 1000) {
             did_change = false;
             guard++;
             for (int c = 0; c < C; c++) {
                 unsigned old = counts_hi[c];
-                counts_hi[c] = 1;
-                double mu1 = dev_adjusted_mu(m, c, counts_hi);
-                counts_hi[c] = old;
-                double mu = dev_adjusted_mu(m, c, counts_hi);
-                double s = dist_cutoff * dev_sigma(m, c, mu);
+                double mu1, s;
+                if (tabled) {
+                    mu1 = m.e_amu[c][1];
+                    s = dist_cutoff * m.e_sig[c][old];
+                } else {
+                    counts_hi[c] = 1;
+                    mu1 = dev_adjusted_mu(m, c, counts_hi);
+                    counts_hi[c] = old;
+                    double mu = dev_adjusted_mu(m, c, counts_hi);
+                    s = dist_cutoff * dev_sigma(m, c, mu);
+                }
                 unsigned new_cts = (unsigned)lround((rad[t * C + c] + s) / mu1);
                 if (new_cts > max_num_dyes + 1) new_cts = max_num_dyes + 1;
                 if (new_cts != counts_hi[c]) {
@@ -135,8 +144,14 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
             unsigned cmin = max_num_dyes + 1;
             for (unsigned d = 0; d < max_num_dyes + 1; d++) {
                 counts_lo[c] = d;
-                double mu = dev_adjusted_mu(m, c, counts_lo);
-                double s = dist_cutoff * dev_sigma(m, c, mu);
+                double mu, s;
+                if (tabled) {
+                    mu = m.e_amu[c][d];
+                    s = dist_cutoff * m.e_sig[c][d];
+                } else {
+                    mu = dev_adjusted_mu(m, c, counts_lo);
+                    s = dist_cutoff * dev_sigma(m, c, mu);
+                }
                 if (mu + s > rad[t * C + c]) {
                     cmin = d;
                     break;
@@ -147,8 +162,14 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
             unsigned old = counts_hi[c];
             for (unsigned d = cmin; d < max_num_dyes + 1; d++) {
                 counts_hi[c] = d;
-                double mu = dev_adjusted_mu(m, c, counts_hi);
-                double s = dist_cutoff * dev_sigma(m, c, mu);
+                double mu, s;
+                if (tabled) {
+                    mu = m.e_amu[c][d];
+                    s = dist_cutoff * m.e_sig[c][d];
+                } else {
+                    mu = dev_adjusted_mu(m, c, counts_hi);
+                    s = dist_cutoff * dev_sigma(m, c, mu);
+                }
                 if (mu - s > rad[t * C + c]) {
                     cmax = d;
                     break;
@@ -173,9 +194,9 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
             for (int n = 0; n < W; n++) {
                 double v = 0.0;
                 if ((unsigned)n >= lo[c] && (unsigned)n < hi[c]) {
-                    unsigned counts[WP_MAX_CHANNELS] = {0, 0, 0, 0};
-                    counts[c] = (unsigned)n;
-                    v = dev_pdf(m, c, rad[t * C + c], counts);
+                    // pdf_helper (channel-model.h:61-70) from the tables
+                    const double offset = rad[t * C + c] - m.e_amu[c][n];
+                    v = m.e_norm[c][n] * exp(-offset * offset / m.e_den[c][n]);
                 }
                 out[(t * C + c) * W + n] = make_entry(v);
             }
@@ -254,29 +275,56 @@ __global__ void wp_compact_kernel(BatchArgs a) {
     int minD[WP_MAX_CHANNELS] = {0, 0, 0, 0};
     for (int c = 0; c < C; c++) minD[c] = a.Lsuf[(long)r * m.T * C + c];  // L_0
     const int lane = threadIdx.x & 31;
+    // the read's box words, shared by all its pairs
+    __shared__ uint32_t sL[WP_MAX_TIMESTEPS], sU[WP_MAX_TIMESTEPS];
+    for (int t = threadIdx.x; t < m.T; t += blockDim.x) {
+        sL[t] = a.Lpk[(long)r * m.T + t];
+        sU[t] = a.Upk[(long)r * m.T + t];
+    }
+    __syncthreads();
     for (int base = g0; base < g1; base += blockDim.x) {
         // In all-peptides mode walk the peptides in shape order, so that the
         // engine's warps get pairs of similar size; results still go to
         // their own slots, so the candidate order (ties) is unchanged.
         int g = base + threadIdx.x;
         if (g < g1 && a.perm) g = g0 + a.perm[g - g0];
-        bool live = false;
+        int dest = -1;  // 0: work (pass 1), 1: mid (pass 2), 2: ovf (dense)
         if (base + threadIdx.x < g1) {
             int p = slot_pep(a, r, g);
             const PeptideRec& pep = a.peps[p];
-            live = !read_empty;
+            bool live = !read_empty;
             for (int c = 0; c < C; c++)
                 if (pep.D[c] < minD[c]) live = false;
-            if (!live) {
+            if (live) {
+                // the pair's largest box waits in its result slot for the
+                // engine, which checks it against its slab before any write
+                const int vm = pair_vmax(C, m.T, sL, sU, pep.D);
+                a.res_expo[g] = vm;
+                dest = 0;
+                if (a.route_half1 > 0) {
+                    dest = vm <= a.route_half1 ? 0 : vm <= a.route_half2 ? 1 : 2;
+                    if (dest == 2 && !a.route_dense) {
+                        atomicExch(a.err, 2);  // no shape holds this pair
+                        dest = -1;
+                    }
+                }
+            }
+            if (dest < 0) {
                 a.res_mant[g] = 0.0f;
                 a.res_expo[g] = 0;
             }
         }
-        unsigned mask = __ballot_sync(0xffffffffu, live);
-        int n = __popc(mask);
-        int pos = 0;
-        if (lane == 0 && n) pos = atomicAdd(a.work_count, n);
-        pos = __shfl_sync(0xffffffffu, pos, 0);
-        if (live) a.work[pos + __popc(mask & ((1u << lane) - 1))] = make_int2(r, g);
+        // warp-aggregated appends, one per list
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const unsigned mask = __ballot_sync(0xffffffffu, dest == k);
+            if (!mask) continue;
+            int* count = k == 0 ? a.work_count : k == 1 ? a.mid_count : a.ovf_count;
+            int2* list = k == 0 ? a.work : k == 1 ? a.mid : a.ovf;
+            int pos = 0;
+            if (lane == 0) pos = atomicAdd(count, __popc(mask));
+            pos = __shfl_sync(0xffffffffu, pos, 0);
+            if (dest == k) list[pos + __popc(mask & ((1u << lane) - 1))] = make_int2(r, g);
+        }
     }
 }
