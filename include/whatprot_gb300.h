@@ -410,8 +410,8 @@ long long wp_launch_count(const wp_ctx* ctx);
 
 /* Work statistics of the last batch run on this context (synchronises):
  * stats[0] (read, peptide) slots, [1] slots the pruning left non-empty,
- * [2] pairs spilled past the first engine pass, [3] pairs spilled past the
- * second to the dense fallback.  No reference counterpart. */
+ * [2] pairs run by the second engine pass (too large for the first pass's
+ * slab), [3] pairs run by the dense fallback.  No reference counterpart. */
 wp_status wp_last_batch_stats(wp_ctx* ctx, long long* stats4);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that order their

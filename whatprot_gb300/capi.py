@@ -540,8 +540,7 @@ class Context:
     def last_batch_stats(self) -> dict:
         out = np.zeros(4, np.int64)
         self._check(self.lib.wp_last_batch_stats(self.h, _ptr(out)))
-        return {"slots": int(out[0]), "nonempty": int(out[1]), "spilled_pass2": int(out[2]),
-                "spilled_dense": int(out[3])}
+        return {"slots": int(out[0]), "nonempty": int(out[1]), "pass2": int(out[2]), "dense": int(out[3])}
 
     def fp32_peak_tflops(self) -> float:
         out = ctypes.c_double()

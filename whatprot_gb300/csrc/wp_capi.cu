@@ -224,7 +224,7 @@ struct wp_ctx {
 
     // Per-batch scratch.
     DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_Lpk, d_Upk, d_allow, d_flags, d_table, d_res_mant, d_res_expo,
-            d_work, d_ovf1, d_ovf2, d_counters, d_cand, d_slot_off, d_out_id, d_out_score,
+            d_work, d_ovf1, d_ovf2, d_ovf3, d_counters, d_cand, d_slot_off, d_out_id, d_out_score,
             d_out_total, d_out_log, d_logp, d_flops, d_err;
 };
 
@@ -487,8 +487,11 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
     WP_CUDA(ctx->d_work.ensure(sizeof(int2) * ns), "alloc work list");
     WP_CUDA(ctx->d_ovf1.ensure(sizeof(int2) * ns), "alloc work list");
     WP_CUDA(ctx->d_ovf2.ensure(sizeof(int2) * ns), "alloc work list");
-    WP_CUDA(ctx->d_counters.ensure(sizeof(int) * 8), "alloc counters");
-    WP_CUDA(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(int) * 8, ctx->stream), "clear counters");
+    WP_CUDA(ctx->d_ovf3.ensure(sizeof(int2) * ns), "alloc work list");
+    // counters: [0, 1] pass-1 list count / head, [2, 3] pass 2, [6, 7]
+    // pass 3, [4, 5] dense, [8] non-empty pairs
+    WP_CUDA(ctx->d_counters.ensure(sizeof(int) * 12), "alloc counters");
+    WP_CUDA(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(int) * 12, ctx->stream), "clear counters");
     int* cnt = ctx->d_counters.as<int>();
     a.res_mant = ctx->d_res_mant.as<float>();
     a.res_expo = ctx->d_res_expo.as<int>();
@@ -515,12 +518,20 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         int half2 = slab_half_for(ctx, cfg.t2, cfg.s2, hb);
         if (half1 < 4 || half2 < 4)
             return fail(ctx, WP_ERR_UNSUPPORTED, "shared memory too small for the pair engine");
+        // A middle pass of 3 CTAs of 128 threads per SM takes the pairs just
+        // too large for pass 1 with more warps per SM than the last pass.
+        const int hmid = slab_half_for(ctx, 128, 3, hb);
+        const bool three = hmid > half1 && hmid < half2;
         // the compaction sends each pair to the first pass whose slab holds it
         a.route_half1 = half1;
-        a.route_half2 = std::max(half1, half2);
+        a.route_half2 = three ? hmid : std::max(half1, half2);
+        a.route_half3 = three ? half2 : 0;
         a.route_dense = dense_warps > 0 ? 1 : 0;
         a.mid = ctx->d_ovf1.as<int2>();
         a.mid_count = cnt + 2;
+        a.mid2 = ctx->d_ovf3.as<int2>();
+        a.mid2_count = cnt + 6;
+        a.live_count = cnt + 8;
         {
             TimedLaunch tl(ctx, 1);
             wp_compact_kernel<<<R, 256, 0, ctx->stream>>>(a);
@@ -535,11 +546,21 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
                                      &ctx->last_engine_grid), "engine pass 1");
             ctx->launches++;
         }
+        if (three) {
+            TimedLaunch tl(ctx, 0);
+            size_t smem = wp_engine_smem_bytes(hmid, 0, hb, 128);
+            WP_CUDA(wp_launch_engine(C, hb, 128, smem, ctx->stream, a, ctx->d_ovf1.as<int2>(), cnt + 2, cnt + 3,
+                                     ctx->d_ovf3.as<int2>(), cnt + 6, hmid, 0, 0, nullptr), "engine pass 2");
+            ctx->launches++;
+        }
         {
             TimedLaunch tl(ctx, 0);
             size_t smem = wp_engine_smem_bytes(half2, 0, hb, cfg.t2);
-            WP_CUDA(wp_launch_engine(C, hb, cfg.t2, smem, ctx->stream, a, ctx->d_ovf1.as<int2>(),
-                                     cnt + 2, cnt + 3, ctx->d_ovf2.as<int2>(), cnt + 4, half2, 0, dense_warps == 0 ? 1 : 0, nullptr), "engine pass 2");
+            int2* in = three ? ctx->d_ovf3.as<int2>() : ctx->d_ovf1.as<int2>();
+            int* in_count = three ? cnt + 6 : cnt + 2;
+            WP_CUDA(wp_launch_engine(C, hb, cfg.t2, smem, ctx->stream, a, in, in_count, in_count + 1,
+                                     ctx->d_ovf2.as<int2>(), cnt + 4, half2, 0, dense_warps == 0 ? 1 : 0, nullptr),
+                    "engine last pass");
             ctx->launches++;
         }
         if (dense_warps > 0) {
@@ -985,14 +1006,14 @@ wp_status wp_last_batch_stats(wp_ctx* ctx, long long* stats) {
     if (!ctx || !stats) return WP_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
-    int c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int c[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (ctx->d_counters.p) {
         WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
         WP_CUDA(cudaMemcpy(c, ctx->d_counters.p, sizeof(c), cudaMemcpyDeviceToHost), "read counters");
     }
     stats[0] = ctx->last_slots;
-    stats[1] = c[0];
-    stats[2] = c[2];
+    stats[1] = c[8];
+    stats[2] = c[2] + c[6];
     stats[3] = c[4];
     return WP_OK;
 }

@@ -162,13 +162,18 @@ struct BatchArgs {
     // Routing by the compaction (route_half1 == 0: every live pair to
     // `work`).  A pair whose largest box (pair_vmax) fits route_half1 goes to
     // `work` (engine pass 1), one that fits route_half2 to `mid` (pass 2),
-    // the rest to `ovf` (the dense kernel; route_dense == 0: none, the pair
-    // gets P = 0 and err = 2).
+    // one that fits route_half3 to `mid2` (pass 3; route_half3 == 0: no
+    // such pass), the rest to `ovf` (the dense kernel; route_dense == 0:
+    // none, the pair gets P = 0 and err = 2).
     int route_half1;
     int route_half2;
+    int route_half3;
     int route_dense;
     int2* mid;
     int* mid_count;
+    int2* mid2;
+    int* mid2_count;
+    int* live_count;           // non-empty pairs (nullable)
 };
 
 // Largest state box, in elements with the Edman slices counted, that any
@@ -215,10 +220,9 @@ __host__ __device__ inline int slot_pep(const BatchArgs& a, int r, int g) {
 
 // 2^x as a float for x <= 127 (0 below the subnormal range).
 __device__ __forceinline__ float exp2i(int x) {
-    if (x > 127) x = 127;
-    if (x >= -126) return __int_as_float((x + 127) << 23);
-    if (x >= -149) return ldexpf(1.0f, x);
-    return 0.0f;
+    x = min(x, 127);
+    if (x >= -126) return __int_as_float((x + 127) << 23);  // normal: the exponent field alone
+    return x >= -149 ? __int_as_float(1 << (x + 149)) : 0.0f;  // subnormal: one mantissa bit
 }
 
 __device__ __forceinline__ void load_smem_model(SmemModel& S, const DevModel& m) {
