@@ -1300,7 +1300,7 @@ wp_status wp_autotune(wp_ctx* ctx, const double* rads, int R, double dist_cutoff
     cudaEventCreate(&e1);
     const int threads[2] = {128, 256};
     for (int t1 : threads)
-        for (int s1 = 1; s1 <= 3; s1++)
+        for (int s1 = 1; s1 <= 4; s1++)
             for (int t2 : threads) {
                 EngineCfg c;
                 c.t1 = t1;
