@@ -224,7 +224,7 @@ struct wp_ctx {
 
     // Per-batch scratch.
     DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_Lpk, d_Upk, d_allow, d_flags, d_table, d_res_mant, d_res_expo,
-            d_work, d_ovf1, d_ovf2, d_ovf3, d_counters, d_cand, d_slot_off, d_out_id, d_out_score,
+            d_work, d_ovf1, d_ovf2, d_ovf3, d_ovf4, d_counters, d_cand, d_slot_off, d_out_id, d_out_score,
             d_out_total, d_out_log, d_logp, d_flops, d_err;
 };
 
@@ -488,8 +488,9 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
     WP_CUDA(ctx->d_ovf1.ensure(sizeof(int2) * ns), "alloc work list");
     WP_CUDA(ctx->d_ovf2.ensure(sizeof(int2) * ns), "alloc work list");
     WP_CUDA(ctx->d_ovf3.ensure(sizeof(int2) * ns), "alloc work list");
-    // counters: [0, 1] pass-1 list count / head, [2, 3] pass 2, [6, 7]
-    // pass 3, [4, 5] dense, [8] non-empty pairs
+    WP_CUDA(ctx->d_ovf4.ensure(sizeof(int2) * ns), "alloc work list");
+    // counters: [2k, 2k + 1] list count / head of engine pass k (k < 4),
+    // [8, 9] the dense kernel's, [10] non-empty pairs
     WP_CUDA(ctx->d_counters.ensure(sizeof(int) * 12), "alloc counters");
     WP_CUDA(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(int) * 12, ctx->stream), "clear counters");
     int* cnt = ctx->d_counters.as<int>();
@@ -499,8 +500,8 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
     a.work_count = cnt + 0;
     a.work_head = cnt + 1;
     a.ovf = ctx->d_ovf2.as<int2>();
-    a.ovf_count = cnt + 4;
-    a.ovf_head = cnt + 5;
+    a.ovf_count = cnt + 8;
+    a.ovf_head = cnt + 9;
     a.dense_S_cap = ((ctx->S_max + 31) / 32) * 32;
     if (n_slots > 0) {
         // Dense fallback shape: as many warps as fit (0: unavailable).
@@ -518,49 +519,47 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         int half2 = slab_half_for(ctx, cfg.t2, cfg.s2, hb);
         if (half1 < 4 || half2 < 4)
             return fail(ctx, WP_ERR_UNSUPPORTED, "shared memory too small for the pair engine");
-        // A middle pass of 3 CTAs of 128 threads per SM takes the pairs just
-        // too large for pass 1 with more warps per SM than the last pass.
+        // Engine passes ("tiers") in order of growing slab: pass 1, a middle
+        // pass of 3 CTAs of 128 threads per SM for the pairs just too large
+        // for pass 1, the last configured pass, and a pass of one CTA of 128
+        // threads per SM for what is left short of the dense kernel.
+        struct Tier {
+            int threads, per_sm, half;
+        };
+        Tier tiers[WP_MAX_TIERS];
+        int nt = 0;
+        tiers[nt++] = {cfg.t1, cfg.s1, half1};
         const int hmid = slab_half_for(ctx, 128, 3, hb);
-        const bool three = hmid > half1 && hmid < half2;
+        if (hmid > half1 && hmid < half2) tiers[nt++] = {128, 3, hmid};
+        if (half2 > tiers[nt - 1].half) tiers[nt++] = {cfg.t2, cfg.s2, half2};
+        const int hbig = slab_half_for(ctx, 128, 1, hb);
+        if (hbig > tiers[nt - 1].half) tiers[nt++] = {128, 1, hbig};
+        DevBuf* lists[WP_MAX_TIERS] = {&ctx->d_work, &ctx->d_ovf1, &ctx->d_ovf3, &ctx->d_ovf4};
         // the compaction sends each pair to the first pass whose slab holds it
-        a.route_half1 = half1;
-        a.route_half2 = three ? hmid : std::max(half1, half2);
-        a.route_half3 = three ? half2 : 0;
+        a.n_tiers = nt;
+        for (int k = 0; k < nt; k++) {
+            a.tier_half[k] = tiers[k].half;
+            a.tier_list[k] = lists[k]->as<int2>();
+            a.tier_count[k] = cnt + 2 * k;
+        }
         a.route_dense = dense_warps > 0 ? 1 : 0;
-        a.mid = ctx->d_ovf1.as<int2>();
-        a.mid_count = cnt + 2;
-        a.mid2 = ctx->d_ovf3.as<int2>();
-        a.mid2_count = cnt + 6;
-        a.live_count = cnt + 8;
+        a.live_count = cnt + 10;
         {
             TimedLaunch tl(ctx, 1);
             wp_compact_kernel<<<R, 256, 0, ctx->stream>>>(a);
             ctx->launches++;
             WP_CUDA(cudaGetLastError(), "compact launch");
         }
-        {
+        for (int k = 0; k < nt; k++) {
             TimedLaunch tl(ctx, 0);
-            size_t smem = wp_engine_smem_bytes(half1, 0, hb, cfg.t1);
-            WP_CUDA(wp_launch_engine(C, hb, cfg.t1, smem, ctx->stream, a, a.work, cnt + 0, cnt + 1,
-                                     ctx->d_ovf1.as<int2>(), cnt + 2, half1, 0, 0,
-                                     &ctx->last_engine_grid), "engine pass 1");
-            ctx->launches++;
-        }
-        if (three) {
-            TimedLaunch tl(ctx, 0);
-            size_t smem = wp_engine_smem_bytes(hmid, 0, hb, 128);
-            WP_CUDA(wp_launch_engine(C, hb, 128, smem, ctx->stream, a, ctx->d_ovf1.as<int2>(), cnt + 2, cnt + 3,
-                                     ctx->d_ovf3.as<int2>(), cnt + 6, hmid, 0, 0, nullptr), "engine pass 2");
-            ctx->launches++;
-        }
-        {
-            TimedLaunch tl(ctx, 0);
-            size_t smem = wp_engine_smem_bytes(half2, 0, hb, cfg.t2);
-            int2* in = three ? ctx->d_ovf3.as<int2>() : ctx->d_ovf1.as<int2>();
-            int* in_count = three ? cnt + 6 : cnt + 2;
-            WP_CUDA(wp_launch_engine(C, hb, cfg.t2, smem, ctx->stream, a, in, in_count, in_count + 1,
-                                     ctx->d_ovf2.as<int2>(), cnt + 4, half2, 0, dense_warps == 0 ? 1 : 0, nullptr),
-                    "engine last pass");
+            const bool last = k + 1 == nt;
+            size_t smem = wp_engine_smem_bytes(tiers[k].half, 0, hb, tiers[k].threads);
+            WP_CUDA(wp_launch_engine(C, hb, tiers[k].threads, smem, ctx->stream, a, lists[k]->as<int2>(),
+                                     cnt + 2 * k, cnt + 2 * k + 1,
+                                     last ? ctx->d_ovf2.as<int2>() : lists[k + 1]->as<int2>(),
+                                     last ? cnt + 8 : cnt + 2 * (k + 1), tiers[k].half, 0,
+                                     last && dense_warps == 0 ? 1 : 0, k == 0 ? &ctx->last_engine_grid : nullptr),
+                    "engine pass");
             ctx->launches++;
         }
         if (dense_warps > 0) {
@@ -1012,9 +1011,9 @@ wp_status wp_last_batch_stats(wp_ctx* ctx, long long* stats) {
         WP_CUDA(cudaMemcpy(c, ctx->d_counters.p, sizeof(c), cudaMemcpyDeviceToHost), "read counters");
     }
     stats[0] = ctx->last_slots;
-    stats[1] = c[8];
-    stats[2] = c[2] + c[6];
-    stats[3] = c[4];
+    stats[1] = c[10];
+    stats[2] = c[2] + c[4] + c[6];
+    stats[3] = c[8];
     return WP_OK;
 }
 

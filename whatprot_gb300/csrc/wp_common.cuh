@@ -19,6 +19,7 @@
 
 #define WP_W (WP_MAX_DYES_PER_CHANNEL + 1)      // extent cap per channel
 #define WP_TRI (WP_W * (WP_W + 1) / 2)          // triangular table size
+#define WP_MAX_TIERS 4                          // engine passes the compaction routes to
 
 struct DevModel {
     int C;
@@ -159,20 +160,16 @@ struct BatchArgs {
     int* err;
     int slab_half;             // per-thread slab half, in state elements
     int dense_S_cap;           // overflow kernel: max states per Edman slice
-    // Routing by the compaction (route_half1 == 0: every live pair to
-    // `work`).  A pair whose largest box (pair_vmax) fits route_half1 goes to
-    // `work` (engine pass 1), one that fits route_half2 to `mid` (pass 2),
-    // one that fits route_half3 to `mid2` (pass 3; route_half3 == 0: no
-    // such pass), the rest to `ovf` (the dense kernel; route_dense == 0:
-    // none, the pair gets P = 0 and err = 2).
-    int route_half1;
-    int route_half2;
-    int route_half3;
+    // Routing by the compaction over the engine passes ("tiers", in launch
+    // order; n_tiers == 0: every live pair to `work`): a pair goes to the
+    // list of the first tier whose slab half holds its largest box
+    // (pair_vmax), else to `ovf` (the dense kernel; route_dense == 0: none,
+    // the pair gets P = 0 and err = 2).
+    int n_tiers;
+    int tier_half[WP_MAX_TIERS];
+    int2* tier_list[WP_MAX_TIERS];
+    int* tier_count[WP_MAX_TIERS];
     int route_dense;
-    int2* mid;
-    int* mid_count;
-    int2* mid2;
-    int* mid2_count;
     int* live_count;           // non-empty pairs (nullable)
 };
 

@@ -271,11 +271,14 @@ extern "C" wp_status wp_hmm_classify_noalloc(int device, const wp_seq_model* m, 
             break;
         }
     // the compaction sends each pair to the first pass whose slab holds it
-    a.route_half1 = half1;
-    a.route_half2 = half1 > half2 ? half1 : half2;
+    a.n_tiers = half2 > half1 ? 2 : 1;
+    a.tier_half[0] = half1;
+    a.tier_list[0] = a.work;
+    a.tier_count[0] = cnt + 0;
+    a.tier_half[1] = half2;
+    a.tier_list[1] = reinterpret_cast<int2*>(base + o_ovf1);
+    a.tier_count[1] = cnt + 2;
     a.route_dense = dense_warps > 0 ? 1 : 0;
-    a.mid = reinterpret_cast<int2*>(base + o_ovf1);
-    a.mid_count = cnt + 2;
     wp_compact_kernel<<<R, 256, 0, s>>>(a);
     WP_NA(cudaGetLastError());
     WP_NA(wp_launch_engine(C, hb, 256, wp_engine_smem_bytes(half1, scr, hb, 256), s, a, a.work, cnt + 0,

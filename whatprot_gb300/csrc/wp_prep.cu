@@ -288,7 +288,7 @@ __global__ void wp_compact_kernel(BatchArgs a) {
         // their own slots, so the candidate order (ties) is unchanged.
         int g = base + threadIdx.x;
         if (g < g1 && a.perm) g = g0 + a.perm[g - g0];
-        int dest = -1;  // 0: work (pass 1), 1: mid (pass 2), 3: mid2 (pass 3), 2: ovf (dense)
+        int dest = -1;  // tier index, WP_MAX_TIERS: the dense kernel's list
         if (base + threadIdx.x < g1) {
             int p = slot_pep(a, r, g);
             const PeptideRec& pep = a.peps[p];
@@ -301,12 +301,11 @@ __global__ void wp_compact_kernel(BatchArgs a) {
                 const int vm = pair_vmax(C, m.T, sL, sU, pep.D);
                 a.res_expo[g] = vm;
                 dest = 0;
-                if (a.route_half1 > 0) {
-                    dest = vm <= a.route_half1   ? 0
-                           : vm <= a.route_half2 ? 1
-                           : vm <= a.route_half3 ? 3
-                                                 : 2;
-                    if (dest == 2 && !a.route_dense) {
+                if (a.n_tiers > 0) {
+                    dest = WP_MAX_TIERS;
+                    for (int k = a.n_tiers - 1; k >= 0; k--)
+                        if (vm <= a.tier_half[k]) dest = k;
+                    if (dest == WP_MAX_TIERS && !a.route_dense) {
                         atomicExch(a.err, 2);  // no shape holds this pair
                         dest = -1;
                     }
@@ -322,12 +321,12 @@ __global__ void wp_compact_kernel(BatchArgs a) {
             if (lane == 0 && lm) atomicAdd(a.live_count, __popc(lm));
         }
         // warp-aggregated appends, one per list
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
+        for (int k = 0; k <= WP_MAX_TIERS; k++) {
             const unsigned mask = __ballot_sync(0xffffffffu, dest == k);
             if (!mask) continue;
-            int* count = k == 0 ? a.work_count : k == 1 ? a.mid_count : k == 2 ? a.ovf_count : a.mid2_count;
-            int2* list = k == 0 ? a.work : k == 1 ? a.mid : k == 2 ? a.ovf : a.mid2;
+            const bool dense = k == WP_MAX_TIERS;
+            int* count = dense ? a.ovf_count : a.n_tiers > 0 ? a.tier_count[k] : a.work_count;
+            int2* list = dense ? a.ovf : a.n_tiers > 0 ? a.tier_list[k] : a.work;
             int pos = 0;
             if (lane == 0) pos = atomicAdd(count, __popc(mask));
             pos = __shfl_sync(0xffffffffu, pos, 0);
