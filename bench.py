@@ -731,6 +731,36 @@ def run_fit(args):
               + [abs(a - b) for a, b in zip(curve(fitted), curve(sm))]
               + [abs(a.p_bleach - b.p_bleach) for a, b in zip(fitted.channel_models, sm.channel_models)]
               + [abs(a.p_dud - b.p_dud) for a, b in zip(fitted.channel_models, sm.channel_models)])
+    # every parameter, mu / sig / bg_sig included (fit_emission; the reference
+    # fits the rates only), from a start with each of them perturbed too
+    rng = np.random.default_rng(78)
+    start_e = perturbed(sm, 77)
+    for cm in start_e.channel_models:
+        cm.mu *= float(rng.uniform(0.5, 1.5))
+        cm.sig *= float(rng.uniform(0.5, 1.5))
+        cm.bg_sig *= float(rng.uniform(0.5, 1.5))
+    ctx.upload_model(start_e, T)
+    ctx.fit_begin(seq, h_np)
+    ctx.fit_set_emission(True)
+    ctx.fit_estep()  # warm
+    t0 = time.perf_counter()
+    ctx.fit_estep()
+    est_e_s = time.perf_counter() - t0
+    ctx.fit_set_emission(False)
+    t0 = time.perf_counter()
+    fitted_e, step_e, log_l_e, iters_e = ctx.hmm_fit(start_e, T, seq, h_np, 1e-6, 600.0, fit_emission=True)
+    fit_e_s = time.perf_counter() - t0
+    rel = lambda a, b: abs(a - b) / abs(b)
+    err_e = {"rates_max_abs": max([abs(fitted_e.p_edman_failure - sm.p_edman_failure)]
+                                  + [abs(a - b) for a, b in zip(curve(fitted_e), curve(sm))]
+                                  + [abs(a.p_bleach - b.p_bleach) for a, b in zip(fitted_e.channel_models,
+                                                                                   sm.channel_models)]
+                                  + [abs(a.p_dud - b.p_dud) for a, b in zip(fitted_e.channel_models,
+                                                                             sm.channel_models)]),
+             "mu_max_rel": max(rel(a.mu, b.mu) for a, b in zip(fitted_e.channel_models, sm.channel_models)),
+             "sig_max_rel": max(rel(a.sig, b.sig) for a, b in zip(fitted_e.channel_models, sm.channel_models)),
+             "bg_sig_max_rel": max(rel(a.bg_sig, b.bg_sig)
+                                   for a, b in zip(fitted_e.channel_models, sm.channel_models))}
     k_avg = k_ms / max(k_n, 1)
     line = {"metric": FIT_METRIC, "value": value, "unit": FIT_UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
@@ -748,7 +778,12 @@ def run_fit(args):
                                "p_initial_detach": fitted.p_initial_detach,
                                "p_initial_detach_decay": fitted.p_initial_detach_decay,
                                "p_bleach": [c.p_bleach for c in fitted.channel_models],
-                               "p_dud": [c.p_dud for c in fitted.channel_models]}}}
+                               "p_dud": [c.p_dud for c in fitted.channel_models]}},
+            "fit_all_params": {"iterations": iters_e, "seconds": fit_e_s, "final_step": step_e, "log_l": log_l_e,
+                               "estep_with_emission_statistics_s": est_e_s, "error_vs_generating_model": err_e,
+                               "fitted_mu": [c.mu for c in fitted_e.channel_models],
+                               "fitted_sig": [c.sig for c in fitted_e.channel_models],
+                               "fitted_bg_sig": [c.bg_sig for c in fitted_e.channel_models]}}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_fit(sm, seq, rads)
     if rank == 0:

@@ -196,10 +196,17 @@ typedef struct {
     int hold_p_cyclic_block;
     int hold_p_bleach[WP_MAX_CHANNELS];
     int hold_p_dud[WP_MAX_CHANNELS];
+    /* Non-zero: also fit each channel's mu, sig and bg_sig from the E-step's
+     * emission statistics (wp_fit_emission_mstep).  No reference
+     * counterpart: the reference never fits them (fitters/hmm-fitter.cc:
+     * 94-95, peptide-emission.h:47-54); 0 keeps its behaviour. */
+    int fit_emission;
 } wp_fit_settings;
 
-/* The fitted parameters of a SequencingModel (bg_sig, mu, sig and the
- * interactions are never fitted: fitters/hmm-fitter.cc:94-95). */
+/* The fitted parameters of a SequencingModel.  The reference fits the rates
+ * only (bg_sig, mu, sig and the interactions are never fitted:
+ * fitters/hmm-fitter.cc:94-95); mu, sig and bg_sig change here only under
+ * wp_fit_settings.fit_emission and are otherwise the starting model's. */
 typedef struct {
     double p_edman_failure;
     double p_detach;
@@ -209,7 +216,42 @@ typedef struct {
     double p_cyclic_block;
     double p_bleach[WP_MAX_CHANNELS];
     double p_dud[WP_MAX_CHANNELS];
+    double mu[WP_MAX_CHANNELS];
+    double sig[WP_MAX_CHANNELS];
+    double bg_sig[WP_MAX_CHANNELS];
 } wp_fit_params;
+
+/* Emission statistics of one E-step: per channel c and dye count n, the
+ * posterior weight w of "channel c shows n live dyes" at an emission,
+ * summed over reads and timesteps (the detached state shows 0 on every
+ * channel), and that weight times the intensity (x) and its square (xx).
+ * No reference counterpart (PeptideEmission's improve_fit is a no-op,
+ * hmm/step/peptide-emission.cc:255-260). */
+typedef struct {
+    double w[WP_MAX_CHANNELS][WP_MAX_DYES_PER_CHANNEL + 1];
+    double x[WP_MAX_CHANNELS][WP_MAX_DYES_PER_CHANNEL + 1];
+    double xx[WP_MAX_CHANNELS][WP_MAX_DYES_PER_CHANNEL + 1];
+} wp_emission_sums;
+
+/* Non-zero: the following wp_fit_estep calls also gather the emission
+ * statistics (read them with wp_fit_emission_sums). */
+wp_status wp_fit_set_emission(wp_ctx* ctx, int enable);
+
+/* The emission statistics of the last wp_fit_estep (zeros when it did not
+ * gather them). */
+wp_status wp_fit_emission_sums(wp_ctx* ctx, wp_emission_sums* out);
+
+/* Emission M-step, per channel: the mu, sig and bg_sig that maximise the
+ * expected log-likelihood of the intensities under ChannelModel's
+ * N(mu n, bg_sig^2 + mu n sig^2) (channel-model.h:35-70, no interactions)
+ * given the statistics: sum_n [-w_n/2 log v_n - (xx_n - 2 m_n x_n +
+ * m_n^2 w_n) / (2 v_n)], m_n = mu n, v_n = bg_sig^2 + mu n sig^2.  Solved
+ * by damped Newton in the logarithms of the three parameters from the
+ * current values; a channel without weight at n >= 1 fits bg_sig only.
+ * Copies every other field of *cur into *next; *step_size (nullable)
+ * receives the largest change of the three parameters over the channels. */
+wp_status wp_fit_emission_mstep(const wp_emission_sums* sums, int num_channels, const wp_fit_params* cur,
+                                wp_fit_params* next, double* step_size);
 
 /* HMMFitter::fit (fitters/hmm-fitter.h:49-117) with its log_likelihood
  * (:119-142): Baum-Welch from `start` on one dye-seq and R reads

@@ -335,6 +335,7 @@ typedef struct {
     double* dud_tab[WPO_MAX_CHANNELS];
     double* bleach_tab[WPO_MAX_CHANNELS];
     double p_detach[WPO_MAX_TIMESTEPS];
+    const double* rad; /* the read, [T][C] */
 } hmm;
 
 /* Edman ranges (hmm/step/edman-transition.cc:28-60). */
@@ -467,6 +468,7 @@ static void hmm_build(hmm* h, const wpo_model* m, int T, const int16_t* seq,
     h->m = m;
     h->seq = seq;
     h->length = length;
+    h->rad = rad;
     wpo_dye_track(T, C, seq, length, h->track);
     for (int c = 0; c < C; c++) {
         h->dud_tab[c] = (double*)calloc((max_num_dyes + 1) * (max_num_dyes + 2) / 2,
@@ -970,8 +972,30 @@ static void step_improve_fit(const hmm* h, const step* s, const psv* fw,
         binomial_fit_tensor(s, &fw->b, &bw->b, &nbw->b, P, num, den);
         break;
     }
-    case S_EMIT: /* peptide-emission.cc:255-260: no-op */
+    case S_EMIT: { /* peptide-emission.cc:255-260 is a no-op; the emission
+                      statistics: posterior f * b / P of each state at this
+                      emission, binned by each channel's dye count */
+        const double* x = h->rad + (long)s->t * h->C;
+        for (kit_begin(&it, &s->r1); !it.done; kit_next(&it)) {
+            double g = fw->a.v[tensor_index(&fw->a, it.loc)] * bw->a.v[tensor_index(&bw->a, it.loc)] / P;
+            g += fw->b.v[tensor_index(&fw->b, it.loc)] * bw->b.v[tensor_index(&bw->b, it.loc)] / P;
+            for (int c = 0; c < h->C; c++) {
+                const unsigned n = it.loc[1 + c];
+                sums->emis_w[c][n] += g;
+                sums->emis_x[c][n] += g * x[c];
+                sums->emis_xx[c][n] += g * x[c] * x[c];
+            }
+        }
+        {
+            const double g = fw->pd * bw->pd / P;
+            for (int c = 0; c < h->C; c++) {
+                sums->emis_w[c][0] += g;
+                sums->emis_x[c][0] += g * x[c];
+                sums->emis_xx[c][0] += g * x[c] * x[c];
+            }
+        }
         break;
+    }
     case S_DETACH:
         detach_fit_tensor(s, &fw->a, &bw->a, nbw->pd, P, sums);
         detach_fit_tensor(s, &fw->b, &bw->b, nbw->pd, P, sums);
@@ -1293,6 +1317,11 @@ void wpo_improve_fit_batch(const wpo_model* m, int T, const int16_t* seq,
             sums->bleach_den[c] += p->bleach_den[c];
             sums->dud_num[c] += p->dud_num[c];
             sums->dud_den[c] += p->dud_den[c];
+            for (int n = 0; n < 16; n++) {
+                sums->emis_w[c][n] += p->emis_w[c][n];
+                sums->emis_x[c][n] += p->emis_x[c][n];
+                sums->emis_xx[c][n] += p->emis_xx[c][n];
+            }
         }
     }
     free(th);

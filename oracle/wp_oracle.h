@@ -58,6 +58,14 @@ typedef struct {
     double cyc_block_num, cyc_block_den;
     double bleach_num[WPO_MAX_CHANNELS], bleach_den[WPO_MAX_CHANNELS];
     double dud_num[WPO_MAX_CHANNELS], dud_den[WPO_MAX_CHANNELS];
+    /* Emission statistics (no reference counterpart: PeptideEmission's
+     * improve_fit is a no-op, peptide-emission.cc:255-260): per channel c
+     * and dye count n, the posterior weight of "channel c shows n live dyes"
+     * at an emission, summed over timesteps (the detached state shows 0 on
+     * every channel), and that weight times the intensity and its square. */
+    double emis_w[WPO_MAX_CHANNELS][16];
+    double emis_x[WPO_MAX_CHANNELS][16];
+    double emis_xx[WPO_MAX_CHANNELS][16];
 } wpo_fit_sums;
 
 /* Channel model (channel-model.h:35-70, channel-model.cc:35-49). */

@@ -44,7 +44,9 @@ class WpoFitSums(ctypes.Structure):
                 ("init_block_num", ctypes.c_double), ("init_block_den", ctypes.c_double),
                 ("cyc_block_num", ctypes.c_double), ("cyc_block_den", ctypes.c_double),
                 ("bleach_num", ctypes.c_double * MAXC), ("bleach_den", ctypes.c_double * MAXC),
-                ("dud_num", ctypes.c_double * MAXC), ("dud_den", ctypes.c_double * MAXC)]
+                ("dud_num", ctypes.c_double * MAXC), ("dud_den", ctypes.c_double * MAXC),
+                ("emis_w", (ctypes.c_double * 16) * MAXC), ("emis_x", (ctypes.c_double * 16) * MAXC),
+                ("emis_xx", (ctypes.c_double * 16) * MAXC)]
 
     def as_dict(self, T, C):
         return {
@@ -55,6 +57,9 @@ class WpoFitSums(ctypes.Structure):
             "cyc_block": (self.cyc_block_num, self.cyc_block_den),
             "bleach": (np.array(self.bleach_num[:C]), np.array(self.bleach_den[:C])),
             "dud": (np.array(self.dud_num[:C]), np.array(self.dud_den[:C])),
+            "emis_w": np.array([list(self.emis_w[c]) for c in range(C)]),
+            "emis_x": np.array([list(self.emis_x[c]) for c in range(C)]),
+            "emis_xx": np.array([list(self.emis_xx[c]) for c in range(C)]),
         }
 
 

@@ -82,3 +82,43 @@ def test_matches_reference_levmar_fixed_point(reference):
             settled += 1
             assert np.max(np.abs(a - b)) < 1e-6, (trial, a, b)
     assert settled >= 50
+
+
+def test_emission_mstep_matches_scipy():
+    """wp_fit_emission_mstep reaches the maximum of the expected
+    log-likelihood that an independent optimiser (scipy Nelder-Mead on the
+    same objective) finds, from a far start; a channel with weight at n = 0
+    only fits bg_sig and keeps mu and sig."""
+    from scipy.optimize import minimize
+    rng = np.random.default_rng(1)
+    C, N = 3, 16
+    mu_t, sig_t, bg_t = np.array([1.1, 0.9, 1.0]), np.array([0.15, 0.2, 0.1]), np.array([0.01, 0.02, 0.03])
+    w = np.zeros((C, N))
+    x = np.zeros((C, N))
+    xx = np.zeros((C, N))
+    for c in range(C):
+        for n in range(5 if c < 2 else 1):
+            v = bg_t[c] ** 2 + mu_t[c] * n * sig_t[c] ** 2
+            s = rng.normal(mu_t[c] * n, np.sqrt(v), 4000)
+            w[c, n], x[c, n], xx[c, n] = len(s), s.sum(), (s * s).sum()
+    mu0, sig0, bg0 = [1.5, 0.6, 1.2], [0.1, 0.3, 0.2], [0.03, 0.01, 0.05]
+    mu, sig, bg, step = capi.emission_mstep(w, x, xx, mu0, sig0, bg0)
+
+    def negq(th, c):
+        m_, s_, b_ = np.exp(th)
+        q = 0.0
+        for n in range(N):
+            if w[c, n] <= 0:
+                continue
+            mm, v = m_ * n, b_ ** 2 + m_ * n * s_ ** 2
+            q += -0.5 * w[c, n] * np.log(v) - (xx[c, n] - 2 * mm * x[c, n] + mm * mm * w[c, n]) / (2 * v)
+        return -q
+
+    for c in range(2):
+        res = minimize(negq, np.log([1.0, 0.1, 0.01]), args=(c,), method="Nelder-Mead",
+                       options={"xatol": 1e-12, "fatol": 1e-12, "maxiter": 20000, "maxfev": 40000})
+        assert -negq(np.log([mu[c], sig[c], bg[c]]), c) >= -res.fun - 1e-6
+        assert np.allclose([mu[c], sig[c], bg[c]], np.exp(res.x), rtol=1e-5)
+    assert mu[2] == mu0[2] and sig[2] == sig0[2]
+    assert abs(bg[2] - np.sqrt(xx[2, 0] / w[2, 0])) <= 1e-8
+    assert step >= abs(mu[0] - mu0[0])

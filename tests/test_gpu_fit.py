@@ -224,3 +224,71 @@ def test_bootstrap_fit(tmp_path):
         assert len(lines) == 7 and len(lines[1].split(",")) == 11
     finally:
         ctx.close()
+
+
+# ---- emission statistics and the mu / sig / bg_sig fit (no reference
+# counterpart: the reference never fits them; the oracle's FP64 E-step and
+# the generating model are the checks).
+EMIS_CASES = [
+    (2, 8, "..0.1.0..1", 48, False),
+    (2, 6, "0.1.01", 40, True),
+    (3, 16, "0.1.2.0..1.2.0..1.2.0", 16, False),
+]
+
+
+@pytest.mark.parametrize("kernel", [0, 1], ids=["cta", "thread"])
+@pytest.mark.parametrize("case", EMIS_CASES, ids=[f"C{c[0]}T{c[1]}{'B' if c[4] else ''}" for c in EMIS_CASES])
+def test_emission_statistics_vs_oracle(gpu_ctx, oracle, case, kernel):
+    """Posterior weight per (channel, dye count) at the emissions and its
+    intensity moments: within 1e-5 of the total weight (reads x timesteps)
+    of the oracle's FP64 sums; the weights of each channel sum to it."""
+    C, T, seq_str, n, block = case
+    gpu_ctx.fit_set_kernel(kernel)
+    gpu_ctx.fit_set_emission(True)
+    sm = _model(C, block)
+    seq = parse_dye_seq(seq_str)
+    rads = _reads(sm, seq, T, n, seed=11 * len(seq_str) + C)
+    sm.channel_models[0].sig *= 1.2
+    gpu_ctx.upload_model(sm, T)
+    gpu_ctx.fit_begin(seq, rads)
+    gpu_ctx.fit_estep()
+    w, x, xx = gpu_ctx.fit_emission_sums().arrays(C)
+    gpu_ctx.fit_set_emission(False)
+    gpu_ctx.fit_set_kernel(0)
+    o, lps = _oracle_sums(oracle, sm, T, seq, rads)
+    live = int(np.sum(np.isfinite(lps)))
+    total = float(live * T)
+    assert np.allclose(w.sum(axis=1), total, rtol=1e-5, atol=0)
+    xs = float(np.max(np.abs(rads))) + 1.0
+    _close(w, o["emis_w"][:, :w.shape[1]], total, "emission weight")
+    _close(x, o["emis_x"][:, :w.shape[1]], total * xs, "emission x")
+    _close(xx, o["emis_xx"][:, :w.shape[1]], total * xs * xs, "emission xx")
+
+
+def test_fit_emission_recovers_generating_model(gpu_ctx):
+    """fit_emission on reads of a known model from a +-30 % start: every rate
+    and each channel's mu, sig and bg_sig back to the generating values
+    within the statistical error of 20,000 reads."""
+    C, T = 2, 8
+    truth = _model(C)
+    truth.channel_models[0].mu, truth.channel_models[1].mu = 1.0, 0.8
+    truth.channel_models[0].sig, truth.channel_models[1].sig = 0.16, 0.12
+    truth.channel_models[0].bg_sig, truth.channel_models[1].bg_sig = 0.05, 0.04
+    seq = parse_dye_seq("..0.1.0..1.1")
+    rads = _reads(truth, seq, T, 20000, seed=5)
+    start = _model(C)
+    for cm, f in zip(start.channel_models, (1.3, 0.7)):
+        cm.mu, cm.sig, cm.bg_sig = 0.9 * f, 0.14 * f, 0.06 / f
+    fitted, step, ll, iters = gpu_ctx.hmm_fit(start, T, seq, rads, 1e-6, 600.0, fit_emission=True)
+    assert step < 1e-6 and math.isfinite(ll) and iters > 2
+    for c, (cf, ct) in enumerate(zip(fitted.channel_models, truth.channel_models)):
+        assert abs(cf.mu - ct.mu) <= 0.01 * ct.mu, (c, cf.mu, ct.mu)
+        assert abs(cf.sig - ct.sig) <= 0.05 * ct.sig, (c, cf.sig, ct.sig)
+        assert abs(cf.bg_sig - ct.bg_sig) <= 0.08 * ct.bg_sig, (c, cf.bg_sig, ct.bg_sig)
+        assert abs(cf.p_bleach - ct.p_bleach) <= 0.01
+        assert abs(cf.p_dud - ct.p_dud) <= 0.02
+    assert abs(fitted.p_edman_failure - truth.p_edman_failure) <= 0.01
+    # without fit_emission the emission parameters stay the start's
+    held, _, _, _ = gpu_ctx.hmm_fit(start, T, seq, rads[:2000], 1e-4, 600.0)
+    assert all(h.mu == s.mu and h.sig == s.sig and h.bg_sig == s.bg_sig
+               for h, s in zip(held.channel_models, start.channel_models))

@@ -123,6 +123,8 @@ def test_improve_fit_matches_reference_live(oracle, reference):
         _, sr = reference.improve_fit(sm, 6, dye_seq_string(s), rads[i], dmax)
         a, b = so.as_dict(6, 2), sr.as_dict(6, 2)
         for k in a:
+            if k.startswith("emis"):  # emission statistics: no reference counterpart
+                continue
             x = np.concatenate([np.ravel(v) for v in a[k]])
             y = np.concatenate([np.ravel(v) for v in b[k]])
             np.testing.assert_allclose(x, y, rtol=1e-12, atol=1e-300)
@@ -159,3 +161,25 @@ def test_nn_oracle_vs_reference_fixture(oracle, name):
                 assert abs(hsc[r] / htot[r] - z["hy_score"][r] / z["hy_total"][r]) <= \
                     1e-9 * abs(z["hy_score"][r] / z["hy_total"][r])
     assert same >= 0.3 * len(nc)
+
+
+def test_oracle_emission_posteriors_sum_to_timesteps():
+    """The oracle's emission statistics: at every emission the posterior over
+    each channel's dye count (detached state at 0) sums to 1, so each
+    channel's weights sum to reads x timesteps, and the weighted mean
+    intensity of count n is near n mu for the generating model."""
+    from oracle_lib import Oracle, WpoFitSums
+    from whatprot_gb300.model import DyeSeqSet, parse_dye_seq
+    from whatprot_gb300.simulate import paper_model, simulate_radiometries
+    sm = paper_model(2)
+    seq = parse_dye_seq("..0.1.0..1")
+    one = DyeSeqSet(2, [seq], np.array([0], np.int32), np.array([1], np.int32))
+    rads, _ = simulate_radiometries(sm, one, 8, 300, seed=13)
+    s = WpoFitSums()
+    for r in rads:
+        Oracle().improve_fit(sm, 8, seq, r, 2, sums=s)
+    d = s.as_dict(8, 2)
+    assert np.allclose(d["emis_w"].sum(axis=1), 300 * 8, rtol=1e-12)
+    for c in range(2):
+        for n in (1, 2):
+            assert abs(d["emis_x"][c, n] / d["emis_w"][c, n] - n) < 0.05

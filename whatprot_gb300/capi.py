@@ -31,7 +31,8 @@ EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload"
            "wp_hmm_loglik_all", "wp_hmm_count_flops", "wp_launch_count", "wp_ctx_stream",
            "wp_timing_enable", "wp_timing_read", "wp_probe_fp32_peak", "wp_last_batch_stats",
            "wp_fit_begin", "wp_fit_estep", "wp_hmm_fit", "wp_fit_offset_exponential", "wp_fit_set_kernel",
-           "wp_hmm_bootstrap_fit", "wp_fit_mstep",
+           "wp_hmm_bootstrap_fit", "wp_fit_mstep", "wp_fit_set_emission", "wp_fit_emission_sums",
+           "wp_fit_emission_mstep",
            "wp_nn_tracks_upload", "wp_nn_classify", "wp_hybrid_classify", "wp_hybrid_classify_device",
            "wp_dev_gemm_bf16", "wp_simulate_reads", "wp_ctx_set_graphs", "wp_set_engine_config",
            "wp_autotune", "wp_mlp_create", "wp_mlp_destroy", "wp_mlp_train",
@@ -93,7 +94,8 @@ class WpFitSettings(ctypes.Structure):
                 ("hold_p_initial_block", ctypes.c_int),
                 ("hold_p_cyclic_block", ctypes.c_int),
                 ("hold_p_bleach", ctypes.c_int * WP_MAX_CHANNELS),
-                ("hold_p_dud", ctypes.c_int * WP_MAX_CHANNELS)]
+                ("hold_p_dud", ctypes.c_int * WP_MAX_CHANNELS),
+                ("fit_emission", ctypes.c_int)]
 
 
 class WpFitParams(ctypes.Structure):
@@ -105,7 +107,25 @@ class WpFitParams(ctypes.Structure):
                 ("p_initial_block", ctypes.c_double),
                 ("p_cyclic_block", ctypes.c_double),
                 ("p_bleach", ctypes.c_double * WP_MAX_CHANNELS),
-                ("p_dud", ctypes.c_double * WP_MAX_CHANNELS)]
+                ("p_dud", ctypes.c_double * WP_MAX_CHANNELS),
+                ("mu", ctypes.c_double * WP_MAX_CHANNELS),
+                ("sig", ctypes.c_double * WP_MAX_CHANNELS),
+                ("bg_sig", ctypes.c_double * WP_MAX_CHANNELS)]
+
+
+WP_EMIS_N = 16  # dye counts 0..15
+
+
+class WpEmissionSums(ctypes.Structure):
+    """wp_emission_sums: posterior weight per (channel, dye count) at the
+    emissions and its intensity moments (no reference counterpart)."""
+    _fields_ = [("w", (ctypes.c_double * WP_EMIS_N) * WP_MAX_CHANNELS),
+                ("x", (ctypes.c_double * WP_EMIS_N) * WP_MAX_CHANNELS),
+                ("xx", (ctypes.c_double * WP_EMIS_N) * WP_MAX_CHANNELS)]
+
+    def arrays(self, C: int):
+        return (np.array([list(self.w[c]) for c in range(C)]), np.array([list(self.x[c]) for c in range(C)]),
+                np.array([list(self.xx[c]) for c in range(C)]))
 
 
 class WpError(RuntimeError):
@@ -177,6 +197,12 @@ def load_library(path: Optional[str] = None):
     lib.wp_hmm_bootstrap_fit.restype = I
     lib.wp_fit_offset_exponential.argtypes = [V, V, I, V, V]
     lib.wp_fit_offset_exponential.restype = I
+    lib.wp_fit_set_emission.argtypes = [V, I]
+    lib.wp_fit_set_emission.restype = I
+    lib.wp_fit_emission_sums.argtypes = [V, P_(WpEmissionSums)]
+    lib.wp_fit_emission_sums.restype = I
+    lib.wp_fit_emission_mstep.argtypes = [P_(WpEmissionSums), I, P_(WpFitParams), P_(WpFitParams), P_(D)]
+    lib.wp_fit_emission_mstep.restype = I
     lib.wp_nn_tracks_upload.argtypes = [V, V, I, I, I, V, V, V, V]
     lib.wp_nn_tracks_upload.restype = I
     lib.wp_nn_classify.argtypes = [V, V, I, I, D, I, V, V, V, V]
@@ -272,6 +298,29 @@ def fit_offset_exponential(y, w, params, held=(False, False, False)):
     return p
 
 
+def emission_mstep(w, x, xx, mu, sig, bg_sig):
+    """wp_fit_emission_mstep (host code, no GPU): per channel the mu, sig and
+    bg_sig maximising the expected log-likelihood of the intensities given
+    the emission statistics w, x, xx [C, n], from the current values.
+    Returns (mu, sig, bg_sig, step)."""
+    lib = load_library()
+    w, x, xx = (np.asarray(v, dtype=np.float64) for v in (w, x, xx))
+    C = w.shape[0]
+    s = WpEmissionSums()
+    for c in range(C):
+        for n in range(min(w.shape[1], WP_EMIS_N)):
+            s.w[c][n], s.x[c][n], s.xx[c][n] = w[c, n], x[c, n], xx[c, n]
+    cur = WpFitParams()
+    for c in range(C):
+        cur.mu[c], cur.sig[c], cur.bg_sig[c] = mu[c], sig[c], bg_sig[c]
+    nxt = WpFitParams()
+    step = ctypes.c_double(0.0)
+    st = lib.wp_fit_emission_mstep(ctypes.byref(s), C, ctypes.byref(cur), ctypes.byref(nxt), ctypes.byref(step))
+    if st != 0:
+        raise WpError(st, "wp_fit_emission_mstep")
+    return (np.array(nxt.mu[:C]), np.array(nxt.sig[:C]), np.array(nxt.bg_sig[:C]), step.value)
+
+
 class Context:
     """One wp_ctx on one CUDA device (the C ABI's handle)."""
 
@@ -365,6 +414,16 @@ class Context:
         """wp_fit_set_kernel: 0 CTA per read where it fits (default), 1 thread per read."""
         self._check(self.lib.wp_fit_set_kernel(self.h, kind))
 
+    def fit_set_emission(self, enable: bool) -> None:
+        """wp_fit_set_emission: later E-steps also gather the emission statistics."""
+        self._check(self.lib.wp_fit_set_emission(self.h, 1 if enable else 0))
+
+    def fit_emission_sums(self) -> "WpEmissionSums":
+        """wp_fit_emission_sums: the emission statistics of the last E-step."""
+        s = WpEmissionSums()
+        self._check(self.lib.wp_fit_emission_sums(self.h, ctypes.byref(s)))
+        return s
+
     def fit_estep(self):
         """wp_fit_estep with the current model: (WpFitSums, sum log P, reads with P == 0)."""
         s = WpFitSums()
@@ -374,8 +433,11 @@ class Context:
         return s, sl.value, nz.value
 
     def hmm_fit(self, start: SequencingModel, num_timesteps: int, dye_seq, rads: np.ndarray,
-                stopping_threshold: float, max_runtime: float = 1e300, holds: Optional[dict] = None):
-        """wp_hmm_fit: (fitted SequencingModel, step size, log-likelihood, iterations)."""
+                stopping_threshold: float, max_runtime: float = 1e300, holds: Optional[dict] = None,
+                fit_emission: bool = False):
+        """wp_hmm_fit: (fitted SequencingModel, step size, log-likelihood, iterations).
+        fit_emission also fits each channel's mu, sig and bg_sig (no
+        reference counterpart)."""
         import copy
         m, keep = seq_model_struct(start)
         seq = np.ascontiguousarray(dye_seq, dtype=np.int16)
@@ -388,6 +450,7 @@ class Context:
                     arr[c] = 1 if h else 0
             else:
                 setattr(fs, k, 1 if v else 0)
+        fs.fit_emission = 1 if fit_emission else 0
         out = WpFitParams()
         step = ctypes.c_double(0.0)
         ll = ctypes.c_double(0.0)
@@ -397,13 +460,7 @@ class Context:
                                         rads.shape[0], ctypes.byref(fs), stopping_threshold,
                                         max_runtime, ctypes.byref(out), ctypes.byref(step),
                                         ctypes.byref(ll), ctypes.byref(it)))
-        fitted = copy.deepcopy(start)
-        for k in ("p_edman_failure", "p_detach", "p_initial_detach", "p_initial_detach_decay",
-                  "p_initial_block", "p_cyclic_block"):
-            setattr(fitted, k, getattr(out, k))
-        for c, cm in enumerate(fitted.channel_models):
-            cm.p_bleach = out.p_bleach[c]
-            cm.p_dud = out.p_dud[c]
+        fitted = self._params_to_model(start, out)
         self.num_timesteps = num_timesteps
         self.num_channels = start.num_channels
         return fitted, step.value, ll.value, it.value
@@ -484,11 +541,14 @@ class Context:
         for c, cm in enumerate(m.channel_models):
             cm.p_bleach = out.p_bleach[c]
             cm.p_dud = out.p_dud[c]
+            cm.mu = out.mu[c]
+            cm.sig = out.sig[c]
+            cm.bg_sig = out.bg_sig[c]
         return m
 
     def bootstrap_fit(self, start: SequencingModel, num_timesteps: int, dye_seq, rads: np.ndarray,
                       stopping_threshold: float, num_rounds: int, confidence_interval: float, seed: int = 1,
-                      max_runtime: float = 1e300, holds: Optional[dict] = None) -> dict:
+                      max_runtime: float = 1e300, holds: Optional[dict] = None, fit_emission: bool = False) -> dict:
         """wp_hmm_bootstrap_fit: per-round models and log-likelihoods, the fit
         on all reads, and the confidence bounds."""
         m, keep = seq_model_struct(start)
@@ -502,6 +562,7 @@ class Context:
                     arr[c] = 1 if h else 0
             else:
                 setattr(fs, k, 1 if v else 0)
+        fs.fit_emission = 1 if fit_emission else 0
         rounds = (WpFitParams * num_rounds)()
         lls = np.zeros(num_rounds, np.float64)
         best, lo, hi = WpFitParams(), WpFitParams(), WpFitParams()

@@ -220,6 +220,8 @@ def _fit_settings(path, C):
     if "channel_settings" in data:
         holds["hold_p_bleach"] = [bool(ch.get("hold_p_bleach", False)) for ch in data["channel_settings"]]
         holds["hold_p_dud"] = [bool(ch.get("hold_p_dud", False)) for ch in data["channel_settings"]]
+    # extension, no reference counterpart: also fit mu, sig and bg_sig
+    holds["fit_emission"] = bool(data.get("fit_emission", False))
     return holds
 
 
@@ -240,6 +242,7 @@ def run_fit(L, max_runtime_s, x, P, F, R, b, c, Y):
     t0 = _t()
     true, sm = _load_model(P)
     holds = _fit_settings(F, sm.num_channels)
+    fit_emission = holds.pop("fit_emission", False)
     seq = parse_dye_seq(x)
     print(f"Finished basic setup ({_t() - t0} seconds).")
     t0 = _t()
@@ -248,12 +251,12 @@ def run_fit(L, max_runtime_s, x, P, F, R, b, c, Y):
     ctx = capi.Context(0)
     if c == 0.0:
         t0 = _t()
-        fitted, step, log_l, _ = ctx.hmm_fit(sm, T, seq, rads, L, max_runtime_s, holds)
+        fitted, step, log_l, _ = ctx.hmm_fit(sm, T, seq, rads, L, max_runtime_s, holds, fit_emission=fit_emission)
         print(f"Finished fitting parameters ({_t() - t0}seconds).")
     else:
         t0 = _t()
         res = ctx.bootstrap_fit(sm, T, seq, rads, L, b, c, seed=int(time.time()), max_runtime=max_runtime_s,
-                                holds=holds)
+                                holds=holds, fit_emission=fit_emission)
         print(f"lower bounds: {_debug_string(res['ci_min'])}")
         print(f"upper bounds: {_debug_string(res['ci_max'])}")
         print(f"worst bootstrap step size: {res['worst_round_step']}")
@@ -265,6 +268,9 @@ def run_fit(L, max_runtime_s, x, P, F, R, b, c, Y):
             print(f"Finished saving results ({_t() - t0} seconds).")
     ctx.close()
     print(f"Parameters:\n{_debug_string(fitted)}\n")
+    if fit_emission:  # extension: the emission parameters, in the units of the reads divided by mu
+        print(", ".join(f"Channel {c} emission: (mu: {cm.mu:.6f}, sig: {cm.sig:.6f}, bg_sig: {cm.bg_sig:.6f})"
+                        for c, cm in enumerate(fitted.channel_models)) + "\n")
     print(f"log(L): {log_l:.17g}\n")
     print(f"Final step-size: {step} (under inf-norm)")
     print(f"Total run time: {_t() - t_all} seconds.")

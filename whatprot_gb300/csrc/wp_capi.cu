@@ -78,8 +78,8 @@ int wp_nn_queries_per_block();
 int wp_nn_select_warps();
 int wp_nn_hmax();
 __global__ void wp_fit_reduce_kernel(const double*, long, int, double*);
-int wp_fit_nslots(int T, int C);
-size_t wp_fit_cta_smem_bytes(int T, int C, int S, bool has_block);
+int wp_fit_nslots(int T, int C, bool emission);
+size_t wp_fit_cta_smem_bytes(int T, int C, int S, bool has_block, bool emission);
 long wp_fit_cta_ckpt_floats(int T, int S, bool has_block);
 cudaError_t wp_launch_fit_cta(bool has_block, int grid, size_t smem, cudaStream_t s, const FitArgs& a, float* ckpt,
                               long ck_stride);
@@ -201,6 +201,8 @@ struct wp_ctx {
     // Staged Baum-Welch fit.
     bool have_fit = false;
     bool fit_force_thread = false;  // tests: run the thread-per-read E-step
+    bool fit_emission = false;      // E-steps also gather the emission statistics
+    wp_emission_sums fit_emis_last{};  // those of the last E-step
     int fit_R = 0, fit_T = 0, fit_C = 0;
     int fit_D[WP_MAX_CHANNELS] = {0, 0, 0, 0};
     int fit_dmax = 0;
@@ -1392,6 +1394,20 @@ wp_status wp_fit_set_kernel(wp_ctx* ctx, int kind) {
     return WP_OK;
 }
 
+wp_status wp_fit_set_emission(wp_ctx* ctx, int enable) {
+    if (!ctx) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->fit_emission = enable != 0;
+    return WP_OK;
+}
+
+wp_status wp_fit_emission_sums(wp_ctx* ctx, wp_emission_sums* out) {
+    if (!ctx || !out) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    *out = ctx->fit_emis_last;
+    return WP_OK;
+}
+
 wp_status wp_fit_begin(wp_ctx* ctx, const int16_t* dye_seq, int length, const double* rads, int R) {
     if (!ctx || length < 0 || R < 0 || (length > 0 && !dye_seq) || (R > 0 && !rads)) return WP_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -1456,10 +1472,11 @@ wp_status wp_fit_estep(wp_ctx* ctx, wp_fit_sums* out, double* sum_logp, int* num
     for (int c = 0; c < C; c++) S *= ctx->fit_D[c] + 1;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    const int nslots = wp_fit_nslots(T, C);
+    const bool emis = ctx->fit_emission;
+    const int nslots = wp_fit_nslots(T, C, emis);
     // CTA-per-read kernel when a read's vectors fit shared memory, else the
     // thread-per-read kernel over a global slab.
-    const size_t cta_smem = wp_fit_cta_smem_bytes(T, C, S, hb);
+    const size_t cta_smem = wp_fit_cta_smem_bytes(T, C, S, hb, emis);
     // (the kernel also holds the binomial tables in static shared memory)
     const int cta_per_sm = (long)cta_smem + (long)sizeof(SmemModel) <= (long)ctx->smem_optin
                                    ? wp_fit_cta_ctas_per_sm(hb, cta_smem)
@@ -1509,6 +1526,7 @@ wp_status wp_fit_estep(wp_ctx* ctx, wp_fit_sums* out, double* sum_logp, int* num
     fa.sums = ctx->d_fit_sums.as<double>();
     fa.logp = ctx->d_fit_logp.as<double>();
     fa.nslots = nslots;
+    fa.emission = emis ? 1 : 0;
     {
         TimedLaunch tl(ctx, 0);
         if (use_cta)
@@ -1542,6 +1560,17 @@ wp_status wp_fit_estep(wp_ctx* ctx, wp_fit_sums* out, double* sum_logp, int* num
         out->p_bleach_den[c] = sums[b + 1];
         out->p_dud_num[c] = sums[b + 2];
         out->p_dud_den[c] = sums[b + 3];
+    }
+    memset(&ctx->fit_emis_last, 0, sizeof(ctx->fit_emis_last));
+    if (emis) {
+        // slots after the rates: [kind][c][n], kind w / x / xx (wp_fit.cu)
+        const int base = 6 + 2 * (T - 1) + 4 * C, N = WP_MAX_DYES_PER_CHANNEL + 1;
+        for (int c = 0; c < C; c++)
+            for (int n = 0; n < N; n++) {
+                ctx->fit_emis_last.w[c][n] = sums[base + (0 * C + c) * N + n];
+                ctx->fit_emis_last.x[c][n] = sums[base + (1 * C + c) * N + n];
+                ctx->fit_emis_last.xx[c][n] = sums[base + (2 * C + c) * N + n];
+            }
     }
     double sl = 0.0;
     int nz = 0;

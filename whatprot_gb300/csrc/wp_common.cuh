@@ -257,6 +257,7 @@ struct FitArgs {
     double* sums;          // [nthreads][nslots]
     double* logp;          // [R] log P per read (nullable)
     int nslots;
+    int emission;           // also gather the emission statistics (slots fs_emis)
 };
 
 // ---- kNN stage (wp_nn.cu) -------------------------------------------------

@@ -26,8 +26,17 @@
 
 #include "wp_common.cuh"
 
-// Sum slots per thread (doubles): see fit_slot_*.
-__host__ __device__ inline int fit_nslots(int T, int C) { return 6 + 2 * (T - 1) + 4 * C; }
+// Sum slots per thread (doubles): the fitted rates' terms (FS_*, fs_*), then
+// with the emission statistics 3 x C x WP_EMIS_N more (fs_emis).
+#define WP_EMIS_N (WP_MAX_DYES_PER_CHANNEL + 1)
+__host__ __device__ inline int fit_nslots_rates(int T, int C) { return 6 + 2 * (T - 1) + 4 * C; }
+__host__ __device__ inline int fit_nslots(int T, int C, bool emission) {
+    return fit_nslots_rates(T, C) + (emission ? 3 * C * WP_EMIS_N : 0);
+}
+// kind 0: posterior weight, 1: weight x intensity, 2: weight x intensity^2
+__host__ __device__ inline int fs_emis(int T, int C, int kind, int c, int n) {
+    return fit_nslots_rates(T, C) + (kind * C + c) * WP_EMIS_N + n;
+}
 #define FS_EDMAN_NUM 0
 #define FS_EDMAN_DEN 1
 #define FS_IB_NUM 2
@@ -337,6 +346,33 @@ __device__ double fit_read(const FitArgs& a, const SmemModel& M, int r, const Sh
     // the scaled vectors into f*b/P.
     auto scale_of = [&](int Ea, int Ebc) { return ldexp(1.0 / (double)Pm, Ea + Ebc - EP); };
 
+    // Emission statistics at emission t (no reference counterpart): the
+    // posterior f * b / P of each state (f the forward vector before the
+    // emission, b the backward vector at its input), binned by each
+    // channel's dye count; the detached state shows 0 on every channel.
+    auto emis_gather = [&](int t, const Vec& f, const Vec& b, long n1, double sc) {
+        const double* x = a.rads + ((long)r * T + t) * C;
+        for (long i = 0; i < n1; i++) {
+            float g = f.A(i) * b.A(i);
+            if (HB) g = fmaf(f.B(i), b.B(i), g);
+            if (g == 0.0f) continue;
+            const double gs = (double)g * sc;
+            const int j = (int)(i % S);
+            for (int c = 0; c < C; c++) {
+                const int n = coord(sh, j, c);
+                sums[fs_emis(T, C, 0, c, n) * nt] += gs;
+                sums[fs_emis(T, C, 1, c, n) * nt] += gs * x[c];
+                sums[fs_emis(T, C, 2, c, n) * nt] += gs * x[c] * x[c];
+            }
+        }
+        const double gd = (double)(f.pd() * b.pd()) * sc;
+        for (int c = 0; c < C; c++) {
+            sums[fs_emis(T, C, 0, c, 0) * nt] += gd;
+            sums[fs_emis(T, C, 1, c, 0) * nt] += gd * x[c];
+            sums[fs_emis(T, C, 2, c, 0) * nt] += gd * x[c] * x[c];
+        }
+    };
+
     // ---- forward sweep with the expected counts.
     Vec al = vec(AL0), an = vec(AL0 + 1);
     // t = 0 chain: initial block, duds, emission 0.
@@ -374,6 +410,7 @@ __device__ double fit_read(const FitArgs& a, const SmemModel& M, int r, const Sh
             al = an;
             an = tmp;
         }
+        if (a.emission) emis_gather(0, al, bv[1 + C], S, sc);
         // emission 0 and rescale
         const int kmax = kmx[0];
         float tot = 0.0f;
@@ -500,6 +537,7 @@ __device__ double fit_read(const FitArgs& a, const SmemModel& M, int r, const Sh
             al = an;
             an = tmp;
         }
+        if (a.emission) emis_gather(t, al, bv[3 + C], (long)(t + 1) * S, sc);
         // emission t and rescale
         {
             const int kmax = kmx[t];
@@ -560,7 +598,7 @@ __global__ void wp_fit_reduce_kernel(const double* __restrict__ sums, long nthre
     out[k] = s;
 }
 
-int wp_fit_nslots(int T, int C) { return fit_nslots(T, C); }
+int wp_fit_nslots(int T, int C, bool emission) { return fit_nslots(T, C, emission); }
 
 // Floats of scratch per thread: (T + 1) checkpoints, C + 5 boundary
 // vectors and 2 forward vectors, each (1 or 2) * T * S + 1 floats.
@@ -588,6 +626,7 @@ cudaError_t wp_launch_fit_estep(bool has_block, int grid, int threads, cudaStrea
 // ===========================================================================
 #define FIT_NT 256
 #define FIT_MAXTERMS (6 + 2 * WP_MAX_CHANNELS)
+#define FIT_EMIS_BUCKETS (WP_MAX_CHANNELS * WP_EMIS_N)
 
 // Loop over state indices i = tid, tid + NT, ... < n with the slice e = i / S
 // and dye-count index j = i % S kept incrementally (no division per state).
@@ -627,6 +666,39 @@ __device__ void cta_reduce(float* v, int n, float* red, float* out) {
             }
             if (lane == 0) out[k] = x;
         }
+    }
+    __syncthreads();
+}
+
+// Emission statistics of one emission (no reference counterpart): g = f * b
+// per state (f the forward vector before the emission, b the backward vector
+// at its input) into the scratch g, then warp w sums buckets w, w + nw, ...
+// (bucket k = channel c, dye count n, channels in order) over the states in
+// a fixed order into ebk[k].
+template <bool HB>
+__device__ void cta_emission_buckets(const SVec& f, const SVec& b, float* g, long n1, int S, int C, const int* W,
+                                     const uint32_t* coords, float* ebk) {
+    for (long i = threadIdx.x; i < n1; i += blockDim.x) {
+        float v = f.A[i] * b.A[i];
+        if (HB) v = fmaf(f.B[i], b.B[i], v);
+        g[i] = v;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int nb = 0;
+    for (int c = 0; c < C; c++) nb += W[c];
+    for (int k = w; k < nb; k += nw) {
+        int c = 0, n = k;
+        while (n >= W[c]) {
+            n -= W[c];
+            c++;
+        }
+        float sum = 0.0f;
+        for (int j = lane; j < S; j += 32)
+            if (fcoord(coords, j, c) == n)
+                for (long i = j; i < n1; i += S) sum += g[i];
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+        if (lane == 0) ebk[k] = sum;
     }
     __syncthreads();
 }
@@ -694,7 +766,8 @@ __global__ void __launch_bounds__(FIT_NT) wp_fit_cta_kernel(FitArgs a, float* ck
     uint32_t* coords = reinterpret_cast<uint32_t*>(wemit + (long)T * S);  // [S]
     float* red = reinterpret_cast<float*>(coords + S);  // [FIT_MAXTERMS][32]
     float* rout = red + FIT_MAXTERMS * 32;              // [FIT_MAXTERMS]
-    int* kmx = reinterpret_cast<int*>(rout + FIT_MAXTERMS);  // [T]
+    float* ebk = rout + FIT_MAXTERMS;                    // [FIT_EMIS_BUCKETS]
+    int* kmx = reinterpret_cast<int*>(ebk + FIT_EMIS_BUCKETS);  // [T]
     int* Eb = kmx + WP_MAX_TIMESTEPS;                   // [T + 1]
     double* acc = reinterpret_cast<double*>(((reinterpret_cast<uintptr_t>(Eb + WP_MAX_TIMESTEPS + 2)) + 7) & ~(uintptr_t)7);
     auto vec = [&](int slot) {
@@ -881,6 +954,21 @@ __global__ void __launch_bounds__(FIT_NT) wp_fit_cta_kernel(FitArgs a, float* ck
         if (threadIdx.x == 0 && a.logp) a.logp[r] = log((double)Pm) + (double)EP * 0.69314718055994530942;
         auto scale_of = [&](int Ea, int Ebc) { return ldexp(1.0 / (double)Pm, Ea + Ebc - EP); };
 
+        // emission statistics of emission t from the buckets (thread 0, FP64)
+        auto emis_add = [&](int t, const SVec& f, const SVec& b, double sc) {
+            if (threadIdx.x == 0) {
+                const double* x = a.rads + ((long)r * T + t) * C;
+                const double gd = (double)(*f.pd * *b.pd) * sc;
+                int k = 0;
+                for (int c = 0; c < C; c++)
+                    for (int n = 0; n < W[c]; n++, k++) {
+                        const double gs = (double)ebk[k] * sc + (n == 0 ? gd : 0.0);
+                        acc[fs_emis(T, C, 0, c, n)] += gs;
+                        acc[fs_emis(T, C, 1, c, n)] += gs * x[c];
+                        acc[fs_emis(T, C, 2, c, n)] += gs * x[c] * x[c];
+                    }
+            }
+        };
         // ---- forward sweep with the expected counts
         int fa = F0, fb = F1;
         int Ea = 0;
@@ -941,6 +1029,10 @@ __global__ void __launch_bounds__(FIT_NT) wp_fit_cta_kernel(FitArgs a, float* ck
                     acc[fs_dud_num(T, c)] += (double)rout[2 + 2 * c] * sc;
                     acc[fs_dud_den(T, c)] += (double)rout[3 + 2 * c] * sc;
                 }
+            }
+            if (a.emission) {
+                cta_emission_buckets<HB>(vec(fa), vec(BV + 1 + C), vec(fb).A, S, S, C, W, coords, ebk);
+                emis_add(0, vec(fa), vec(BV + 1 + C), sc);
             }
             // emission 0 and rescale
             cta_emit<HB>(vec(fa), vec(fa), wemit, S, S);
@@ -1120,6 +1212,11 @@ __global__ void __launch_bounds__(FIT_NT) wp_fit_cta_kernel(FitArgs a, float* ck
                     }
                 }
             }
+            if (a.emission) {
+                cta_emission_buckets<HB>(vec(fa), vec(BV + 3 + C), vec(fb).A, (long)(t + 1) * S, S, C, W, coords,
+                                         ebk);
+                emis_add(t, vec(fa), vec(BV + 3 + C), sc);
+            }
             // emission t and rescale
             {
                 const long n1 = (long)(t + 1) * S;
@@ -1145,12 +1242,12 @@ __global__ void __launch_bounds__(FIT_NT) wp_fit_cta_kernel(FitArgs a, float* ck
     for (int k = threadIdx.x; k < a.nslots; k += blockDim.x) a.sums[(long)k * gridDim.x + blockIdx.x] = acc[k];
 }
 
-size_t wp_fit_cta_smem_bytes(int T, int C, int S, bool has_block) {
+size_t wp_fit_cta_smem_bytes(int T, int C, int S, bool has_block, bool emission) {
     const long cap = (long)T * S;
     const long VS = (((has_block ? 2 : 1) * cap + 1) + 3) / 4 * 4;
     size_t b = sizeof(float) * ((size_t)(C + 8) * VS + (size_t)T * S) + sizeof(uint32_t) * S +
                sizeof(float) * (FIT_MAXTERMS * 32 + FIT_MAXTERMS) + sizeof(int) * (2 * WP_MAX_TIMESTEPS + 2) + 8 +
-               sizeof(double) * fit_nslots(T, C);
+               sizeof(float) * FIT_EMIS_BUCKETS + sizeof(double) * fit_nslots(T, C, emission);
     return b;
 }
 

@@ -132,6 +132,79 @@ double distance(const HostModel& a, const HostModel& b) {
     return d;
 }
 
+// Expected log-likelihood (up to a constant) of one channel's intensities
+// given the emission statistics w, x, xx over dye counts n < nmax, at
+// th = (log mu, log sig, log bg_sig), and its gradient in th (nullable).
+double emission_q(const double* w, const double* x, const double* xx, int nmax, const double th[3], double g[3]) {
+    const double mu = exp(th[0]), sg = exp(th[1]), bg = exp(th[2]);
+    double q = 0.0, gmu = 0.0, gsg = 0.0, gbg = 0.0;
+    for (int n = 0; n < nmax; n++) {
+        if (!(w[n] > 0.0)) continue;
+        const double m = mu * n, v = bg * bg + mu * n * sg * sg;
+        const double r = xx[n] - 2.0 * m * x[n] + m * m * w[n];
+        q += -0.5 * w[n] * log(v) - r / (2.0 * v);
+        const double dm = (x[n] - m * w[n]) / v;            // dq / dm_n
+        const double dv = -0.5 * w[n] / v + r / (2.0 * v * v);  // dq / dv_n
+        gmu += n * dm + n * sg * sg * dv;
+        gsg += 2.0 * mu * n * sg * dv;
+        gbg += 2.0 * bg * dv;
+    }
+    if (g) {
+        g[0] = mu * gmu;
+        g[1] = sg * gsg;
+        g[2] = bg * gbg;
+    }
+    return q;
+}
+
+// Maximises emission_q over th from its current value: damped Newton
+// (Levenberg 1944 damping on the negated Hessian, which comes from central
+// differences of the analytic gradient), fixed coordinates left alone.
+void emission_fit_channel(const double* w, const double* x, const double* xx, int nmax, double th[3],
+                          const bool fixed[3]) {
+    if (fixed[0] && fixed[1] && fixed[2]) return;
+    double lambda = 1e-3;
+    double g[3];
+    double q = emission_q(w, x, xx, nmax, th, g);
+    if (!isfinite(q)) return;
+    for (int it = 0; it < 200; it++) {
+        double H[3][3];
+        const double h = 1e-5;
+        for (int k = 0; k < 3; k++) {
+            double tp[3] = {th[0], th[1], th[2]}, tm[3] = {th[0], th[1], th[2]};
+            tp[k] += h;
+            tm[k] -= h;
+            double gp[3], gm[3];
+            emission_q(w, x, xx, nmax, tp, gp);
+            emission_q(w, x, xx, nmax, tm, gm);
+            for (int a = 0; a < 3; a++) H[a][k] = (gp[a] - gm[a]) / (2.0 * h);
+        }
+        bool moved = false;
+        while (lambda < 1e12) {
+            double M[3][3];
+            for (int a = 0; a < 3; a++)
+                for (int b = 0; b < 3; b++) M[a][b] = -0.5 * (H[a][b] + H[b][a]);
+            for (int a = 0; a < 3; a++) M[a][a] += lambda * std::max(fabs(M[a][a]), 1e-12);
+            double d[3];
+            if (solve_free(M, g, fixed, d)) {
+                const double tn[3] = {th[0] + d[0], th[1] + d[1], th[2] + d[2]};
+                double gn[3];
+                const double qn = emission_q(w, x, xx, nmax, tn, gn);
+                if (isfinite(qn) && qn >= q) {
+                    const double dmax = std::max(fabs(d[0]), std::max(fabs(d[1]), fabs(d[2])));
+                    for (int k = 0; k < 3; k++) th[k] = tn[k], g[k] = gn[k];
+                    q = qn;
+                    lambda = std::max(lambda * 0.1, 1e-12);
+                    moved = dmax > 1e-13;
+                    break;
+                }
+            }
+            lambda *= 10.0;
+        }
+        if (!moved) break;
+    }
+}
+
 wp_fit_params to_params(const HostModel& m) {
     wp_fit_params p;
     memset(&p, 0, sizeof(p));
@@ -144,6 +217,9 @@ wp_fit_params to_params(const HostModel& m) {
     for (int c = 0; c < m.C; c++) {
         p.p_bleach[c] = m.p_bleach[c];
         p.p_dud[c] = m.p_dud[c];
+        p.mu[c] = m.mu[c];
+        p.sig[c] = m.sig[c];
+        p.bg_sig[c] = m.bg_sig[c];
     }
     return p;
 }
@@ -158,6 +234,9 @@ void from_params(const wp_fit_params& p, HostModel* m) {
     for (int c = 0; c < m->C; c++) {
         m->p_bleach[c] = p.p_bleach[c];
         m->p_dud[c] = p.p_dud[c];
+        m->mu[c] = p.mu[c];
+        m->sig[c] = p.sig[c];
+        m->bg_sig[c] = p.bg_sig[c];
     }
 }
 
@@ -231,6 +310,32 @@ wp_status wp_fit_mstep(const wp_fit_sums* sums_in, int C, int T, const int16_t* 
         }
         *step_size = d;
     }
+    return WP_OK;
+}
+
+wp_status wp_fit_emission_mstep(const wp_emission_sums* sums, int C, const wp_fit_params* cur, wp_fit_params* next,
+                                double* step_size) {
+    if (!sums || !cur || !next || C < 1 || C > WP_MAX_CHANNELS) return WP_ERR_INVALID;
+    const wp_fit_params in = *cur;
+    *next = in;
+    double step = 0.0;
+    const int nmax = WP_MAX_DYES_PER_CHANNEL + 1;
+    for (int c = 0; c < C; c++) {
+        double above = 0.0;  // weight at n >= 1: what identifies mu and sig
+        for (int n = 1; n < nmax; n++) above += sums->w[c][n];
+        const bool fixed[3] = {!(above > 0.0) || !(in.mu[c] > 0.0), !(above > 0.0) || !(in.sig[c] > 0.0),
+                               !(in.bg_sig[c] > 0.0)};
+        double th[3] = {in.mu[c] > 0.0 ? log(in.mu[c]) : 0.0, in.sig[c] > 0.0 ? log(in.sig[c]) : 0.0,
+                        in.bg_sig[c] > 0.0 ? log(in.bg_sig[c]) : 0.0};
+        emission_fit_channel(sums->w[c], sums->x[c], sums->xx[c], nmax, th, fixed);
+        if (!fixed[0]) next->mu[c] = exp(th[0]);
+        if (!fixed[1]) next->sig[c] = exp(th[1]);
+        if (!fixed[2]) next->bg_sig[c] = exp(th[2]);
+        step = std::max(step, fabs(next->mu[c] - in.mu[c]));
+        step = std::max(step, fabs(next->sig[c] - in.sig[c]));
+        step = std::max(step, fabs(next->bg_sig[c] - in.bg_sig[c]));
+    }
+    if (step_size) *step_size = step;
     return WP_OK;
 }
 
@@ -353,6 +458,8 @@ wp_status wp_hmm_fit(wp_ctx* ctx, const wp_seq_model* start, int T, const int16_
     if (st != WP_OK) return st;
     st = wp_fit_begin(ctx, dye_seq, length, rads, R);
     if (st != WP_OK) return st;
+    st = wp_fit_set_emission(ctx, fs.fit_emission ? 1 : 0);
+    if (st != WP_OK) return st;
 
     const auto t0 = std::chrono::steady_clock::now();
     HostModel x;
@@ -373,6 +480,17 @@ wp_status wp_hmm_fit(wp_ctx* ctx, const wp_seq_model* start, int T, const int16_
             wp_fit_params cur = to_params(sm), nx;
             st = wp_fit_mstep(&s, C, T, dye_seq, length, (long long)R, &cur, &fs, &nx, &step);
             if (st != WP_OK) return st;
+            if (fs.fit_emission) {
+                wp_emission_sums es;
+                st = wp_fit_emission_sums(ctx, &es);
+                if (st != WP_OK) return st;
+                wp_fit_params nx2;
+                double estep = 0.0;
+                st = wp_fit_emission_mstep(&es, C, &nx, &nx2, &estep);
+                if (st != WP_OK) return st;
+                nx = nx2;
+                step = std::max(step, estep);
+            }
             from_params(nx, &next);
         }
         const double elapsed =
@@ -402,6 +520,9 @@ wp_status wp_hmm_fit(wp_ctx* ctx, const wp_seq_model* start, int T, const int16_
     for (int c = 0; c < WP_MAX_CHANNELS; c++) {
         out->p_bleach[c] = c < C ? x.p_bleach[c] : 0.0;
         out->p_dud[c] = c < C ? x.p_dud[c] : 0.0;
+        out->mu[c] = c < C ? x.mu[c] : 0.0;
+        out->sig[c] = c < C ? x.sig[c] : 0.0;
+        out->bg_sig[c] = c < C ? x.bg_sig[c] : 0.0;
     }
     if (step_size) *step_size = step;
     if (log_l) *log_l = nz > 0 ? -INFINITY : sl;
@@ -472,6 +593,9 @@ wp_status wp_hmm_bootstrap_fit(wp_ctx* ctx, const wp_seq_model* start, int T, co
     for (int c = 0; c < C; c++) {
         bounds([c](const wp_fit_params& p) { return p.p_bleach[c]; }, [c](wp_fit_params& p, double x) { p.p_bleach[c] = x; });
         bounds([c](const wp_fit_params& p) { return p.p_dud[c]; }, [c](wp_fit_params& p, double x) { p.p_dud[c] = x; });
+        bounds([c](const wp_fit_params& p) { return p.mu[c]; }, [c](wp_fit_params& p, double x) { p.mu[c] = x; });
+        bounds([c](const wp_fit_params& p) { return p.sig[c]; }, [c](wp_fit_params& p, double x) { p.sig[c] = x; });
+        bounds([c](const wp_fit_params& p) { return p.bg_sig[c]; }, [c](wp_fit_params& p, double x) { p.bg_sig[c] = x; });
     }
     return WP_OK;
 }
