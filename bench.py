@@ -160,7 +160,7 @@ def run_hybrid(args):
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        ctx.hybrid_classify(h_rads, HY_K, HY_SIG, HY_H, CUTOFF)
+        last_gpu = ctx.hybrid_classify(h_rads, HY_K, HY_SIG, HY_H, CUTOFF)
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e = {"value": R * world / e2e_s, "unit": HY_UNIT, "h2d_bytes_per_step": int(rads.nbytes),
            "d2h_bytes_per_step": int(R * (4 + 8 + 8))}
@@ -188,7 +188,8 @@ def run_hybrid(args):
                          "hmm_forward_ms_per_step": fw_ms / args.steps, "hmm_prep_ms_per_step": pr_ms / args.steps},
             "e2e": e2e, "gpu_launches": launches, "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_hybrid(sm, ds, dts, rads)
+        line["cpu_baseline"], o_out = cpu_baseline_hybrid(sm, ds, dts, rads)
+        line["parity_vs_oracle"] = sample_parity(last_gpu, o_out)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -209,11 +210,12 @@ def cpu_baseline_hybrid(sm, ds, dts, rads, seconds_target=15.0):
     dt = time.perf_counter() - t0
     n2 = int(min(len(rads), max(n, n * seconds_target / max(dt, 1e-3))))
     t0 = time.perf_counter()
-    o.hybrid_classify(sm, T, dts, ds, rads[:n2], HY_K, HY_SIG, HY_H, CUTOFF, threads=threads)
+    out = o.hybrid_classify(sm, T, dts, ds, rads[:n2], HY_K, HY_SIG, HY_H, CUTOFF, threads=threads)
     dt = time.perf_counter() - t0
-    return {"value": n2 / dt, "unit": HY_UNIT, "cores": threads, "kind": "port",
+    info = {"value": n2 / dt, "unit": HY_UNIT, "cores": threads, "kind": "port",
             "sample": f"{n2} reads of the same workload, {dt:.1f} s, oracle/wp_oracle.c "
                       f"wpo_hybrid_classify_batch (brute-force kNN) with {threads} threads"}
+    return info, out[:3]
 
 
 def run_reference_hybrid(args):
@@ -522,11 +524,34 @@ def cpu_baseline(sm, ds, rads, seconds_target=15.0):
     # grow the sample to about seconds_target of work
     n2 = int(min(len(rads), max(n, n * seconds_target / max(dt, 1e-3))))
     t0 = time.perf_counter()
-    o.classify(sm, T, ds, rads[:n2], CUTOFF, threads=threads)
+    oid, osc, otot = o.classify(sm, T, ds, rads[:n2], CUTOFF, threads=threads)
     dt = time.perf_counter() - t0
-    return {"value": n2 * len(ds) / dt, "unit": UNIT, "cores": threads, "kind": "port",
+    info = {"value": n2 * len(ds) / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{n2} reads x {len(ds)} dye-seqs of the same workload, "
                       f"{dt:.1f} s, oracle/wp_oracle.c with {threads} threads"}
+    return info, (oid, osc, otot)
+
+
+def sample_parity(gpu, oracle_out):
+    """The GPU's classify results against the oracle's FP64 results on the
+    baseline's sample: top-1 agreement, and the largest relative difference
+    of the adjusted score (P_best / total) where the ids agree."""
+    gid, gsc, gtot = gpu
+    oid, osc, otot = oracle_out
+    n = len(oid)
+    gid, gsc, gtot = gid[:n], gsc[:n], gtot[:n]
+    same = gid == oid
+    ga = np.where(gtot > 0, gsc / np.where(gtot > 0, gtot, 1), 0.0)
+    oa = np.where(otot > 0, osc / np.where(otot > 0, otot, 1), 0.0)
+    rel = np.abs(ga - oa) / np.maximum(np.abs(oa), 1e-300)
+    # a different id whose probability equals the oracle's best within the
+    # tolerance is a tie of the reference's own scores (first index wins
+    # there; FP32 rounding may pick the other)
+    tie = ~same & (np.abs(gsc - osc) <= 1e-5 * np.maximum(np.abs(osc), 1e-300))
+    return {"reads": int(n), "top1_identical": float(np.mean(same)),
+            "top1_identical_or_tied": float(np.mean(same | tie)),
+            "max_rel_err_adjusted_score": float(np.max(rel[same])) if np.any(same) else None,
+            "tolerance": 1e-5}
 
 
 def run_reference(args):
@@ -917,7 +942,7 @@ def main():
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        ctx.classify(h_np, CUTOFF)
+        last_gpu = ctx.classify(h_np, CUTOFF)[:3]
     e2e_s = (time.perf_counter() - t0) / args.steps
     if dist:
         t = torch.tensor([e2e_s], device=f"cuda:{local}")
@@ -949,7 +974,8 @@ def main():
                        "cuda_graph": "launch sequence captured and replayed in the timed steps"},
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(sm, ds, rads)
+        line["cpu_baseline"], o_out = cpu_baseline(sm, ds, rads)
+        line["parity_vs_oracle"] = sample_parity(last_gpu, o_out)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
