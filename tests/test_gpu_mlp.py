@@ -94,3 +94,31 @@ def test_training_gains_recall_and_feeds_the_hmm():
         net.close()
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("P,h", [(3000, 200), (3000, 1000), (700, 64), (5000, 1)])
+def test_topk_matches_numpy(P, h):
+    """wp_mlp_propose's selection against numpy on the network's own logits:
+    the h largest by (logit, index) with ties to the larger index, written
+    ascending; softmax probabilities within 1e-5 relative of an FP64 softmax;
+    the candidate mass (sum of probability x count) to the same tolerance.
+    Shapes cover the warp kernel's threshold path, its all-keys path (P at
+    most the buffer) and the exact fallback (h too large for the threshold
+    buffer)."""
+    ctx, sm, ds = _ctx(P, seed=P + h)
+    net = capi.ProposalNet(ctx, hidden=256, seed=3)
+    rng = np.random.default_rng(P)
+    rads = rng.normal(1.0, 0.7, size=(300, 8, 2))
+    L = net.logits(rads)[:, :P].astype(np.float64)
+    idx, prob, mass = net.propose(rads, h)
+    counts = np.asarray(ds.counts, np.float64)
+    for r in range(rads.shape[0]):
+        order = np.lexsort((np.arange(P), L[r]))  # ascending by (logit, index)
+        want = order[-h:]
+        assert np.array_equal(idx[r], want), r
+        z = L[r] - L[r].max()
+        p = np.exp(z) / np.exp(z).sum()
+        assert np.allclose(prob[r], p[want], rtol=1e-5, atol=1e-30), r
+        assert abs(mass[r] - float(np.sum(p[want] * counts[want]))) <= 1e-5 * max(mass[r], 1e-30), r
+    net.close()
+    ctx.close()

@@ -66,7 +66,7 @@ cudaError_t wp_mlp_launch_to_bf16(const float* in, long n, __nv_bfloat16* out, c
 cudaError_t wp_mlp_launch_init(float* w, long rows, long cols, long valid_rows, float std, unsigned long long seed,
                                cudaStream_t s);
 cudaError_t wp_mlp_launch_topk(const float* logits, int R, int P, int ld, int h, const int* counts, int* idx,
-                               float* prob, double* mass, cudaStream_t s);
+                               float* prob, double* mass, int* fail, cudaStream_t s);
 cudaError_t wp_gemm_bf16_tn(const void* A, int lda, const void* B, int ldb, int M, int N, int K, void* C, int ldc,
                             int c_fp32, const float* bias, int act, void* Z, int accumulate, int* err,
                             cudaStream_t s);
@@ -1785,7 +1785,7 @@ struct wp_mlp {
     long n[6] = {0, 0, 0, 0, 0, 0};
     DevBuf W1b, W2b, W3b, W2T, W3T;  // BF16 copies
     DevBuf X, XT, Z1, H1, H1T, Z2, H2, H2T, dL, dLT, dZ2, dZ2T, dZ1, dZ1T, L, dH2, dH1, loss, labels, xsim, err;
-    DevBuf topi, topp, mass, counts, loss_sum;
+    DevBuf topi, topp, mass, counts, loss_sum, tkfail;
 };
 
 namespace {
@@ -1937,8 +1937,10 @@ wp_status mlp_propose_dev(wp_ctx* ctx, wp_mlp* m, const double* d_rads, int R, i
             if (st != WP_OK) return st;
         }
         TimedLaunch tl(ctx, 5);
+        MLP_CUDA(m->tkfail.ensure(sizeof(int) * ((size_t)chunk + 1)), "alloc top-k scratch");
         MLP_CUDA(wp_mlp_launch_topk(m->L.as<float>(), n, m->P, m->Ppad, h, m->counts.as<int>(), d_idx + (size_t)r0 * h,
-                                    d_prob + (size_t)r0 * h, d_mass + r0, ctx->stream), "top-k");
+                                    d_prob + (size_t)r0 * h, d_mass + r0, m->tkfail.as<int>(), ctx->stream),
+                 "top-k");
         ctx->launches++;
     }
     return WP_OK;

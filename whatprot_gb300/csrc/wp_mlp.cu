@@ -21,6 +21,9 @@
 // Master weights, gradients and Adam moments are FP32.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <mutex>
 #include <curand_kernel.h>
 #include <math.h>
 #include <stdint.h>
@@ -173,18 +176,21 @@ __device__ __forceinline__ unsigned fkey(float f) {
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
-// One CTA (256 threads) per read: the h largest of the first P logits by
-// (logit, index), by radix select on the sortable keys, then sorted
-// ascending; writes peptide indices and softmax probabilities, and the sum
-// of probability x peptide count over the candidates.
+// The exact fallback of the top-h selection, one CTA (256 threads) per read
+// of the list rows[0 .. *nrows) (persistent over it): the h largest of the
+// first P logits by (logit, index), by radix select on the sortable keys,
+// then sorted ascending; writes peptide indices and softmax probabilities,
+// and the sum of probability x peptide count over the candidates.
 __global__ void wp_topk_kernel(const float* __restrict__ logits, int P, int ld, int h, const int* __restrict__ counts,
-                               int* __restrict__ out_idx, float* __restrict__ out_prob, double* __restrict__ out_mass) {
+                               int* __restrict__ out_idx, float* __restrict__ out_prob, double* __restrict__ out_mass,
+                               const int* __restrict__ rows, const int* __restrict__ nrows) {
     __shared__ unsigned hist[256];
     __shared__ float sh[32];
     __shared__ unsigned long long skey[1024];
     __shared__ int sidx[1024];
     __shared__ int nsel;
-    const long row = blockIdx.x;
+  for (int it = blockIdx.x; it < *nrows; it += gridDim.x) {
+    const long row = rows[it];
     const float* l = logits + row * ld;
     // softmax normaliser
     float mx = -INFINITY;
@@ -274,6 +280,178 @@ __global__ void wp_topk_kernel(const float* __restrict__ logits, int P, int ld, 
         for (int i = 0; i < n; i++) mass += (double)(expf(l[sidx[i]] - mx) / s) * (double)counts[sidx[i]];
         out_mass[row] = mass;
     }
+    __syncthreads();
+  }
+}
+
+// The top-h selection, one warp per read (persistent over the reads): a
+// sample of TK_SAMPLE logits at a fixed stride gives, by a bitwise search
+// for its order statistic, a threshold that about 2 h of the read's logits
+// reach; one pass over the logits
+// keeps those at or above it (composite key: sortable logit bits, then the
+// index) in the warp's shared buffer and forms the softmax normaliser
+// online; the buffer, sorted, yields the h largest, written ascending as the
+// fallback kernel does.  A read whose kept set is smaller than h or larger
+// than the buffer goes to fail_rows for the exact fallback kernel.
+#define TK_WARPS 8
+#define TK_CAP 1024
+#define TK_SAMPLE 1024
+
+// Bitonic sort, descending, of buf[0 .. n) (n a power of two) by one warp.
+__device__ __forceinline__ void tk_warp_sort_desc(unsigned long long* buf, int n) {
+    const int lane = threadIdx.x & 31;
+    for (int size = 2; size <= n; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = lane; i < n; i += 32) {
+                const int j = i ^ stride;
+                if (j > i) {
+                    const bool desc = (i & size) == 0;
+                    const unsigned long long a = buf[i], b = buf[j];
+                    if ((a < b) == desc) {
+                        buf[i] = b;
+                        buf[j] = a;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+}
+
+__global__ void __launch_bounds__(TK_WARPS * 32) wp_topk_warp_kernel(const float* __restrict__ logits, int R, int P,
+                                                                      int ld, int h, const int* __restrict__ counts,
+                                                                      int* __restrict__ out_idx,
+                                                                      float* __restrict__ out_prob,
+                                                                      double* __restrict__ out_mass,
+                                                                      int* __restrict__ fail_rows,
+                                                                      int* __restrict__ fail_count, int vec4) {
+    extern __shared__ unsigned long long tk_smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned long long* buf = tk_smem + (size_t)warp * TK_CAP;
+    const unsigned lt = (1u << lane) - 1u;
+    for (long row = (long)blockIdx.x * TK_WARPS + warp; row < R; row += (long)gridDim.x * TK_WARPS) {
+        const float* l = logits + row * ld;
+        // threshold: the composite key that about 2.5 h logits reach
+        unsigned long long tau = 0ull;
+        if (P > TK_CAP) {
+            // the rank-th largest sample key, bit by bit from the top: the
+            // largest t with at least `rank` sample keys >= t
+            // TK_SAMPLE / 4 blocks of four neighbouring logits at a fixed
+            // stride (one 16-byte load each)
+            unsigned sk[TK_SAMPLE / 32];
+#pragma unroll
+            for (int u = 0; u < TK_SAMPLE / 128; u++) {
+                const int b = u * 32 + lane;
+                int j = (int)(((long)b * P) / (TK_SAMPLE / 4)) & ~3;
+                j = min(j, (P - 4) & ~3);  // a multiple of 4 (16-byte aligned), j + 3 < P
+                float4 v;
+                if (vec4) {
+                    v = *reinterpret_cast<const float4*>(l + j);
+                } else {
+                    v = make_float4(l[j], l[j + 1], l[j + 2], l[j + 3]);
+                }
+                sk[4 * u] = fkey(v.x);
+                sk[4 * u + 1] = fkey(v.y);
+                sk[4 * u + 2] = fkey(v.z);
+                sk[4 * u + 3] = fkey(v.w);
+            }
+            const int rank = min(TK_SAMPLE, (int)ceilf(2.0f * (float)h * (float)TK_SAMPLE / (float)P) + 4);
+            unsigned t = 0u;
+#pragma unroll 1
+            for (int bit = 31; bit >= 0; bit--) {
+                const unsigned cand = t | (1u << bit);
+                int c = 0;
+#pragma unroll
+                for (int u = 0; u < TK_SAMPLE / 32; u++) c += sk[u] >= cand ? 1 : 0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+                if (c >= rank) t = cand;
+            }
+            tau = (unsigned long long)t << 32;  // every index of a key at the threshold
+        }
+        // the float at the threshold key: x >= tf keeps every key >= tau
+        // (and possibly -0.0 at +0.0, harmless: extra keys are sorted out)
+        const unsigned th = (unsigned)(tau >> 32);
+        const float tf = P > TK_CAP ? __uint_as_float((th & 0x80000000u) ? (th & 0x7fffffffu) : ~th) : -INFINITY;
+        // one pass: keep keys >= tau; online max and sum of exp
+        int cnt = 0;
+        float m = -INFINITY, sum = 0.0f;
+        // element j: online softmax, then kept when its key reaches tau
+        // (the normaliser uses the fast exponential: relative error near
+        // 1e-6 over the logit range; the probabilities written use expf)
+        auto visit = [&](int j, float x, bool in) {
+            if (in) {
+                if (x > m) {
+                    sum = sum * __expf(m - x) + 1.0f;
+                    m = x;
+                } else {
+                    sum += __expf(x - m);
+                }
+            }
+            const bool keep = in && x >= tf;
+            const unsigned ball = __ballot_sync(0xffffffffu, keep);
+            if (ball) {
+                if (keep) {
+                    const int pos = cnt + __popc(ball & lt);
+                    if (pos < TK_CAP) buf[pos] = ((unsigned long long)fkey(x) << 32) | (unsigned)j;
+                }
+                cnt += __popc(ball);
+            }
+        };
+        int j0 = 0;
+        if (vec4) {  // 16-byte rows: eight float4 per lane in flight
+            const float4* l4 = reinterpret_cast<const float4*>(l);
+            for (; j0 + 1024 <= P; j0 += 1024) {
+                float4 v[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) v[u] = l4[(j0 >> 2) + 32 * u + lane];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int ja = j0 + 128 * u + 4 * lane;
+                    visit(ja, v[u].x, true);
+                    visit(ja + 1, v[u].y, true);
+                    visit(ja + 2, v[u].z, true);
+                    visit(ja + 3, v[u].w, true);
+                }
+            }
+        }
+        for (; j0 < P; j0 += 32) {
+            const int j = j0 + lane;
+            visit(j, j < P ? l[j] : -INFINITY, j < P);
+        }
+        // warp-wide softmax normaliser
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float m2 = __shfl_xor_sync(0xffffffffu, m, o), s2 = __shfl_xor_sync(0xffffffffu, sum, o);
+            const float mm = fmaxf(m, m2);
+            sum = (m == -INFINITY ? 0.0f : sum * __expf(m - mm)) + (m2 == -INFINITY ? 0.0f : s2 * __expf(m2 - mm));
+            m = mm;
+        }
+        if (cnt < min(h, P) || cnt > TK_CAP) {
+            if (lane == 0) fail_rows[atomicAdd(fail_count, 1)] = (int)row;
+            __syncwarp();
+            continue;
+        }
+        __syncwarp();
+        int n2 = 1;
+        while (n2 < cnt) n2 <<= 1;
+        for (int i = cnt + lane; i < n2; i += 32) buf[i] = 0ull;
+        __syncwarp();
+        tk_warp_sort_desc(buf, n2);
+        // the h largest, written ascending by (logit, index)
+        const int hh = min(h, P);
+        double part = 0.0;  // this lane's share of the candidate mass
+        for (int i = lane; i < hh; i += 32) {
+            const int j = (int)(buf[hh - 1 - i] & 0xffffffffu);
+            const float pr = expf(l[j] - m) / sum;
+            out_idx[row * h + i] = j;
+            out_prob[row * h + i] = pr;
+            part += (double)pr * (double)counts[j];
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+        if (lane == 0) out_mass[row] = part;
+        __syncwarp();
+    }
 }
 
 // ------------------------------------------------------------------ launchers
@@ -325,9 +503,41 @@ cudaError_t wp_mlp_launch_init(float* w, long rows, long cols, long valid_rows, 
     return cudaGetLastError();
 }
 
+// fail: scratch of R + 1 ints (the fallback's row list, then its count).
 cudaError_t wp_mlp_launch_topk(const float* logits, int R, int P, int ld, int h, const int* counts, int* idx,
-                               float* prob, double* mass, cudaStream_t s) {
+                               float* prob, double* mass, int* fail, cudaStream_t s) {
     if (R == 0) return cudaSuccess;
-    wp_topk_kernel<<<R, 256, 0, s>>>(logits, P, ld, h, counts, idx, prob, mass);
+    if (h > 1024) return cudaErrorInvalidValue;
+    int* fail_count = fail + R;
+    cudaError_t e = cudaMemsetAsync(fail_count, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    const size_t smem = sizeof(unsigned long long) * TK_WARPS * TK_CAP;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    // launch shape, once per device
+    static int shape_sms[64] = {0}, shape_per_sm[64] = {0};
+    static std::mutex shape_mu;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(shape_mu);
+    if (shape_sms[dev] == 0) {
+        e = cudaFuncSetAttribute(wp_topk_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        int sms0 = 0, per0 = 0;
+        cudaDeviceGetAttribute(&sms0, cudaDevAttrMultiProcessorCount, dev);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, wp_topk_warp_kernel, TK_WARPS * 32, smem);
+        if (e != cudaSuccess) return e;
+        shape_per_sm[dev] = per0;
+        shape_sms[dev] = sms0;
+    }
+    const int sms = shape_sms[dev], per_sm = shape_per_sm[dev];
+    const int grid = std::max(1, std::min(sms * std::max(per_sm, 1), (R + TK_WARPS - 1) / TK_WARPS));
+    const int vec4 = (ld % 4 == 0 && ((uintptr_t)logits & 15u) == 0) ? 1 : 0;
+    wp_topk_warp_kernel<<<grid, TK_WARPS * 32, smem, s>>>(logits, R, P, ld, h, counts, idx, prob, mass, fail,
+                                                         fail_count, vec4);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // exact fallback for the reads the threshold missed (usually none)
+    wp_topk_kernel<<<std::max(1, std::min(R, 2 * sms)), 256, 0, s>>>(logits, P, ld, h, counts, idx, prob, mass, fail,
+                                                                       fail_count);
     return cudaGetLastError();
 }
