@@ -174,7 +174,7 @@ struct wp_ctx {
     int S_max = 1;       // max over peptides of prod_c (D_c + 1)
     int scr_floats = 1;  // max over peptides of sum_c (D_c + 1)
     std::vector<PeptideRec> recs;
-    DevBuf d_peps, d_ids, d_counts, d_perm;
+    DevBuf d_peps, d_ids, d_counts, d_perm, d_shape_rank;
 
     // Kernel timing.
     bool timing = false;
@@ -352,6 +352,11 @@ wp_status plan_peptides(wp_ctx* ctx) {
         return k;
     };
     std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return key(x) < key(y); });
+    std::vector<int> rank(P);
+    for (int i = 0; i < P; i++) rank[perm[i]] = i;
+    WP_CUDA(ctx->d_shape_rank.ensure(sizeof(int) * std::max(P, 1)), "alloc shape rank");
+    WP_CUDA(cudaMemcpyAsync(ctx->d_shape_rank.p, rank.data(), sizeof(int) * P, cudaMemcpyHostToDevice, ctx->stream),
+            "copy shape rank");
     WP_CUDA(ctx->d_perm.ensure(sizeof(int) * std::max(P, 1)), "alloc perm");
     WP_CUDA(cudaMemcpyAsync(ctx->d_perm.p, perm.data(), sizeof(int) * P, cudaMemcpyHostToDevice, ctx->stream),
             "copy perm");
@@ -482,6 +487,7 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
     } else {
         a.perm = ctx->d_perm.as<int>();
     }
+    if (a.cand) a.shape_rank = ctx->d_shape_rank.as<int>();
     ctx->last_slots = n_slots;
     const size_t ns = (size_t)std::max<long>(n_slots, 1);
     WP_CUDA(ctx->d_res_mant.ensure(sizeof(float) * ns), "alloc results");

@@ -148,6 +148,7 @@ struct BatchArgs {
     const EmitEntry* tab;      // per read: emission factors
     const int* cand;           // per slot: peptide index (null: all peptides)
     const int* perm;           // all-peptides mode: peptides in shape order (or null)
+    const int* shape_rank;     // candidate mode: each peptide's position in that order (or null)
     const int* slot_off;       // [R + 1] or null
     float* res_mant;           // per slot: P = res_mant * 2^res_expo
     int* res_expo;

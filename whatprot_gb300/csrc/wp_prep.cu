@@ -33,6 +33,8 @@
 
 #include "wp_common.cuh"
 
+#define WP_COMPACT_SORT 1024  // candidate slots per read the compaction orders by shape
+
 
 // ChannelModel::adjusted_mu (parameterization/model/channel-model.h:35-54).
 __device__ double dev_adjusted_mu(const DevModel& m, int channel, const unsigned* counts) {
@@ -281,13 +283,44 @@ __global__ void wp_compact_kernel(BatchArgs a) {
         sL[t] = a.Lpk[(long)r * m.T + t];
         sU[t] = a.Upk[(long)r * m.T + t];
     }
+    // Candidate mode: the read's slots in the peptides' shape order (up to
+    // WP_COMPACT_SORT slots; more keep their order), sorted here by a
+    // bitonic sort of (shape rank, slot) keys.
+    __shared__ unsigned long long order[WP_COMPACT_SORT];
+    const int ns = g1 - g0;
+    const bool sorted = a.cand && a.shape_rank && ns <= WP_COMPACT_SORT;
+    if (sorted) {
+        int n2 = 1;
+        while (n2 < ns) n2 <<= 1;
+        for (int i = threadIdx.x; i < n2; i += blockDim.x)
+            order[i] = i < ns ? ((unsigned long long)(unsigned)a.shape_rank[a.cand[g0 + i]] << 32) | (unsigned)i
+                              : ~0ull;
+        __syncthreads();
+        for (int size = 2; size <= n2; size <<= 1)
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+                    const int j = i ^ stride;
+                    if (j > i) {
+                        const bool up = (i & size) == 0;
+                        const unsigned long long x = order[i], y = order[j];
+                        if ((x > y) == up) {
+                            order[i] = y;
+                            order[j] = x;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+    }
     __syncthreads();
     for (int base = g0; base < g1; base += blockDim.x) {
-        // In all-peptides mode walk the peptides in shape order, so that the
+        // Walk the peptides in shape order (all-peptides mode: the global
+        // order; candidate mode: the read's sorted slots), so that the
         // engine's warps get pairs of similar size; results still go to
         // their own slots, so the candidate order (ties) is unchanged.
         int g = base + threadIdx.x;
         if (g < g1 && a.perm) g = g0 + a.perm[g - g0];
+        if (g < g1 && sorted) g = g0 + (int)(order[g - g0] & 0xffffffffu);
         int dest = -1;  // tier index, WP_MAX_TIERS: the dense kernel's list
         if (base + threadIdx.x < g1) {
             int p = slot_pep(a, r, g);
