@@ -252,6 +252,188 @@ __device__ __noinline__ float emission_table(V* cur, int stride, int t, PBox nx,
     return part;
 }
 
+// Edman (edman-transition.cc:62-162) as a gather from slices e-1 (success)
+// and e (failure) of the bleached box bx (E = t slices in cur) into the
+// emission box nx (t + 1 slices in nxt); both boxes share the lower corner
+// L_t.  Out of line: a quarter of the timesteps take it, and the one-state
+// path's code stays compact in the instruction cache.
+template <int C, bool HB>
+__device__ __noinline__ void edman_gather(const typename StateOf<HB>::V* __restrict__ cur,
+                                          typename StateOf<HB>::V* __restrict__ nxt, int stride, int t, PBox bx,
+                                          PBox nx, bool pk, uint64_t dye_pk, uint64_t tot_pk,
+                                          const PeptideRec& pep, const float2* __restrict__ edman, float pf) {
+    using V = typename StateOf<HB>::V;
+    const float qf = 1.0f - pf;
+    int stb[C];
+    int vb = 1;
+#pragma unroll
+    for (int c = C - 1; c >= 0; c--) {
+        stb[c] = vb;
+        vb *= bget(bx.w, c);
+    }
+    const int vn = bvol<C>(nx.w);
+    for (int e = 0; e <= t; e++) {
+        int dc = -1, tot_i = 1;
+        if (e >= 1) {
+            if (pk) {
+                dc = (int)((dye_pk >> (4 * (e - 1))) & 15) - 1;
+                tot_i = (int)((tot_pk >> (4 * (e - 1))) & 15);
+            } else {
+                dc = pep.dye[e - 1];
+                tot_i = pep.tot[e - 1];
+            }
+        }
+        // Edman coefficients of this slice: row DyeTrack(e - 1, dc)
+        const float2* ed = edman + tot_i * 16;
+        int d_lo = 0, d_wb = 0, d_st = 0;
+#pragma unroll
+        for (int c = 0; c < C; c++)
+            if (c == dc) {
+                d_lo = bget(nx.lo, c);
+                d_wb = bget(bx.w, c);
+                d_st = stb[c];
+            }
+        int jc[C];
+#pragma unroll
+        for (int c = 0; c < C; c++) jc[c] = 0;
+        int ib = 0;
+        const V* fail_row = cur + e * vb * stride;
+        const V* succ_row = cur + (e - 1) * vb * stride;
+        V* out_row = nxt + e * vn * stride;
+        for (int j = 0; j < vn; j++) {
+            V v = vzero(V());
+            if (e < t) {
+                const V f = fail_row[ib * stride];
+                if constexpr (HB) {
+                    v = make_float2(pf * f.x, f.y);  // broken-N copied unchanged
+                } else {
+                    v = pf * f;
+                }
+            }
+            if (e >= 1) {
+                float xin;
+                if constexpr (HB) {
+                    xin = succ_row[ib * stride].x;
+                } else {
+                    xin = succ_row[ib * stride];
+                }
+                float add;
+                if (dc < 0) {
+                    add = qf * xin;
+                } else {
+                    int jd = 0;
+#pragma unroll
+                    for (int c = 0; c < C; c++)
+                        if (c == dc) jd = jc[c];
+                    const int nc = d_lo + jd;
+                    const float2 cf = ed[nc];
+                    add = cf.x * xin;
+                    if (jd + 1 < d_wb) {
+                        float xr;
+                        if constexpr (HB) {
+                            xr = succ_row[(ib + d_st) * stride].x;
+                        } else {
+                            xr = succ_row[(ib + d_st) * stride];
+                        }
+                        add = fmaf(cf.y, xr, add);
+                    }
+                }
+                if constexpr (HB) {
+                    v.x += add;
+                } else {
+                    v += add;
+                }
+            }
+            out_row[j * stride] = v;
+            // advance the multi-index over the emission box
+#pragma unroll
+            for (int c = C - 1; c >= 0; c--) {
+                jc[c]++;
+                ib += stb[c];
+                if (jc[c] < bget(nx.w, c)) break;
+                ib -= stb[c] * bget(nx.w, c);
+                jc[c] = 0;
+            }
+        }
+    }
+}
+
+// Emission multiply for boxes at most 4 wide per channel without
+// interactions (peptide-emission.cc:212-243): per channel the box's entries
+// normalised by their largest exponent, in registers; the factor of state n
+// is prod_c g[c][n_c - L_t] * 2^kmax, times sf (the pending rescale and
+// folded coefficients).  Returns the sum of the multiplied states;
+// *kmax_out receives the normalising exponent (WP_EXPO_ZERO: every factor
+// of some channel is zero), *em0_out the all-zero state's factor when
+// allow_t.  Out of line, as edman_gather.
+template <int C, class V>
+__device__ __noinline__ float emission_narrow(V* cur, int stride, int t, PBox nx, const EmitEntry* __restrict__ tab,
+                                              int W, bool allow_t, float sf, int* kmax_out, float* em0_out) {
+    int kmax = 0;
+    float part = 0.0f;
+    float em0 = 0.0f;
+    // Per channel: the box's entries normalised by their largest
+    // exponent, in registers; the factor of state n is
+    // prod_c g[c][n_c - L_t] * 2^kmax.
+    float g[C][4];
+    bool dead = false;
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+        const EmitEntry* row = tab + (t * C + c) * W + bget(nx.lo, c);
+        const int wc = bget(nx.w, c);
+        EmitEntry en[4];
+        int km = WP_EXPO_ZERO;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            en[k].mant = 0.0f;
+            en[k].expo = WP_EXPO_ZERO;
+            if (k < wc) en[k] = row[k];
+            if (en[k].mant != 0.0f) km = max(km, en[k].expo);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            g[c][k] = en[k].mant != 0.0f ? en[k].mant * exp2i(max(en[k].expo - km, -200)) : 0.0f;
+        if (km == WP_EXPO_ZERO) dead = true;
+        kmax += km;
+    }
+    if (dead) {
+        *kmax_out = WP_EXPO_ZERO;
+        return 0.0f;
+    }
+    if (allow_t) {
+        em0 = 1.0f;
+#pragma unroll
+        for (int c = 0; c < C; c++) em0 *= g[c][0];
+    }
+    // the pending rescale 2^-k_prev (1 - p) of the last timestep
+    const int vn = bvol<C>(nx.w);
+    int jc[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) jc[c] = 0;
+    for (int j = 0; j < vn; j++) {
+        float w = sf;
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+            const int k = jc[c];
+            w *= k == 0 ? g[c][0] : k == 1 ? g[c][1] : k == 2 ? g[c][2] : g[c][3];
+        }
+        V* col = cur + j * stride;
+        for (int e = 0; e <= t; e++) {
+            V s = vmul(w, col[e * vn * stride]);
+            col[e * vn * stride] = s;
+            part += vtotal(s);
+        }
+#pragma unroll
+        for (int c = C - 1; c >= 0; c--) {
+            if (++jc[c] < bget(nx.w, c)) break;
+            jc[c] = 0;
+        }
+    }
+    *kmax_out = kmax;
+    *em0_out = em0;
+    return part;
+}
+
 // Runs one pair.  Returns 1 when its boxes exceed the slab (nothing
 // written), else 0 with P = *mant * 2^*expo (mant == 0: P == 0).
 template <int C, bool HB>
@@ -418,99 +600,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             // (success) and e (failure) of the bleached box into the
             // emission box; both boxes share the lower corner L_t.
             if (!single) {
-                const float pf = m.pf, qf = 1.0f - m.pf;
-                int stb[C];
-                int vb = 1;
-#pragma unroll
-                for (int c = C - 1; c >= 0; c--) {
-                    stb[c] = vb;
-                    vb *= bget(bx.w, c);
-                }
-                const int vn = bvol<C>(nx.w);
-                for (int e = 0; e <= t; e++) {
-                    int dc = -1, tot_i = 1;
-                    if (e >= 1) {
-                        if (pk) {
-                            dc = (int)((dye_pk >> (4 * (e - 1))) & 15) - 1;
-                            tot_i = (int)((tot_pk >> (4 * (e - 1))) & 15);
-                        } else {
-                            dc = pep.dye[e - 1];
-                            tot_i = pep.tot[e - 1];
-                        }
-                    }
-                    // Edman coefficients of this slice: row DyeTrack(e - 1, dc)
-                    const float2* ed = M.edman + tot_i * 16;
-                    int d_lo = 0, d_wb = 0, d_st = 0;
-#pragma unroll
-                    for (int c = 0; c < C; c++)
-                        if (c == dc) {
-                            d_lo = bget(nx.lo, c);
-                            d_wb = bget(bx.w, c);
-                            d_st = stb[c];
-                        }
-                    int jc[C];
-#pragma unroll
-                    for (int c = 0; c < C; c++) jc[c] = 0;
-                    int ib = 0;
-                    const V* fail_row = cur + e * vb * stride;
-                    const V* succ_row = cur + (e - 1) * vb * stride;
-                    V* out_row = nxt + e * vn * stride;
-                    for (int j = 0; j < vn; j++) {
-                        V v = vzero(V());
-                        if (e < t) {
-                            const V f = fail_row[ib * stride];
-                            if constexpr (HB) {
-                                v = make_float2(pf * f.x, f.y);  // broken-N copied unchanged
-                            } else {
-                                v = pf * f;
-                            }
-                        }
-                        if (e >= 1) {
-                            float xin;
-                            if constexpr (HB) {
-                                xin = succ_row[ib * stride].x;
-                            } else {
-                                xin = succ_row[ib * stride];
-                            }
-                            float add;
-                            if (dc < 0) {
-                                add = qf * xin;
-                            } else {
-                                int jd = 0;
-#pragma unroll
-                                for (int c = 0; c < C; c++)
-                                    if (c == dc) jd = jc[c];
-                                const int nc = d_lo + jd;
-                                const float2 cf = ed[nc];
-                                add = cf.x * xin;
-                                if (jd + 1 < d_wb) {
-                                    float xr;
-                                    if constexpr (HB) {
-                                        xr = succ_row[(ib + d_st) * stride].x;
-                                    } else {
-                                        xr = succ_row[(ib + d_st) * stride];
-                                    }
-                                    add = fmaf(cf.y, xr, add);
-                                }
-                            }
-                            if constexpr (HB) {
-                                v.x += add;
-                            } else {
-                                v += add;
-                            }
-                        }
-                        out_row[j * stride] = v;
-                        // advance the multi-index over the emission box
-#pragma unroll
-                        for (int c = C - 1; c >= 0; c--) {
-                            jc[c]++;
-                            ib += stb[c];
-                            if (jc[c] < bget(nx.w, c)) break;
-                            ib -= stb[c] * bget(nx.w, c);
-                            jc[c] = 0;
-                        }
-                    }
-                }
+                edman_gather<C, HB>(cur, nxt, stride, t, bx, nx, pk, dye_pk, tot_pk, pep, M.edman, m.pf);
                 V* tmp = cur;
                 cur = nxt;
                 nxt = tmp;
@@ -604,64 +694,12 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             nxt = tmp;
             bx = nx;
         } else if (narrow) {
-            // Per channel: the box's entries normalised by their largest
-            // exponent, in registers; the factor of state n is
-            // prod_c g[c][n_c - L_t] * 2^kmax.
-            float g[C][4];
-            bool dead = false;
-#pragma unroll
-            for (int c = 0; c < C; c++) {
-                const EmitEntry* row = tab + (t * C + c) * a.W + bget(nx.lo, c);
-                const int wc = bget(nx.w, c);
-                EmitEntry en[4];
-                int km = WP_EXPO_ZERO;
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    en[k].mant = 0.0f;
-                    en[k].expo = WP_EXPO_ZERO;
-                    if (k < wc) en[k] = row[k];
-                    if (en[k].mant != 0.0f) km = max(km, en[k].expo);
-                }
-#pragma unroll
-                for (int k = 0; k < 4; k++)
-                    g[c][k] = en[k].mant != 0.0f ? en[k].mant * exp2i(max(en[k].expo - km, -200)) : 0.0f;
-                if (km == WP_EXPO_ZERO) dead = true;
-                kmax += km;
-            }
-            if (dead) {
+            part = emission_narrow<C, V>(cur, stride, t, nx, tab, a.W, allow_t,
+                                         fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
+            if (kmax == WP_EXPO_ZERO) {
                 *out_mant = 0.0f;
                 *out_expo = 0;
                 return 0;
-            }
-            if (allow_t) {
-                em0 = 1.0f;
-#pragma unroll
-                for (int c = 0; c < C; c++) em0 *= g[c][0];
-            }
-            // the pending rescale 2^-k_prev (1 - p) of the last timestep
-            const float sf = fac_prev * bscale * exp2i(min(-k_prev, 127));
-            const int vn = bvol<C>(nx.w);
-            int jc[C];
-#pragma unroll
-            for (int c = 0; c < C; c++) jc[c] = 0;
-            for (int j = 0; j < vn; j++) {
-                float w = sf;
-#pragma unroll
-                for (int c = 0; c < C; c++) {
-                    const int k = jc[c];
-                    w *= k == 0 ? g[c][0] : k == 1 ? g[c][1] : k == 2 ? g[c][2] : g[c][3];
-                }
-                V* col = cur + j * stride;
-                for (int e = 0; e <= t; e++) {
-                    V s = vmul(w, col[e * vn * stride]);
-                    col[e * vn * stride] = s;
-                    part += vtotal(s);
-                }
-#pragma unroll
-                for (int c = C - 1; c >= 0; c--) {
-                    if (++jc[c] < bget(nx.w, c)) break;
-                    jc[c] = 0;
-                }
             }
         } else {
             part = emission_table<C, V>(cur, stride, t, nx, a.W, tab, m.interacting != 0, fac_prev * bscale, k_prev,
