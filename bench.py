@@ -532,6 +532,25 @@ def cpu_baseline(sm, ds, rads, seconds_target=15.0):
     return info, (oid, osc, otot)
 
 
+def unpruned_forward_flops(seqs, T, C):
+    """The unpruned forward's op count per read summed over the dye-seqs
+    (the context figure of the visited-state count): per dye-seq with D_c
+    dyes per channel, S = prod_c (D_c + 1) states per Edman slice and
+    B = sum_c (D_c + 2), the duds S * B at t = 0 and (t + 1) * S * (3 + [t > 0]
+    * (8 + B)) at every timestep (emission and rescale 3; detach 2, Edman 6
+    and the binomial steps about B per state)."""
+    total = 0.0
+    for seq in seqs:
+        D = [int(np.sum(np.asarray(seq) == c)) for c in range(C)]
+        S = float(np.prod([d + 1 for d in D]))
+        B = float(sum(d + 2 for d in D))
+        f = S * B
+        for t in range(T):
+            f += (t + 1) * S * (3.0 + ((8.0 + B) if t > 0 else 0.0))
+        total += f
+    return total
+
+
 def sample_parity(gpu, oracle_out):
     """The GPU's classify results against the oracle's FP64 results on the
     baseline's sample: top-1 agreement, and the largest relative difference
@@ -787,14 +806,21 @@ def run_fit(args):
              "bg_sig_max_rel": max(rel(a.bg_sig, b.bg_sig)
                                    for a, b in zip(fitted_e.channel_models, sm.channel_models))}
     k_avg = k_ms / max(k_n, 1)
+    fit_flops = 3.0 * R * unpruned_forward_flops([seq], T, C)
+    fit_peak = ctx.fp32_peak_tflops()
+    fit_achieved = fit_flops / (k_avg * 1e-3) / 1e12 if k_avg > 0 else None
     line = {"metric": FIT_METRIC, "value": value, "unit": FIT_UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded simulator)",
             "config": {"workload": FIT_WORKLOAD, "reads": R, "timesteps": T, "channels": C,
                        "dye_seq": "".join("." if d < 0 else str(int(d)) for d in seq),
                        "l2": "flushed between steps (512 MB write)"},
-            "roofline": {"bound": "memory", "kernel": "wp_fit_estep_kernel", "achieved": None,
-                         "peak": None, "unit": None, "frac": None, "traffic": None,
+            "roofline": {"bound": "fp32", "kernel": "wp_fit_cta_kernel", "achieved": fit_achieved,
+                         "peak": fit_peak, "unit": "TFLOP/s",
+                         "frac": (fit_achieved / fit_peak) if (fit_achieved and fit_peak) else None,
+                         "traffic": None, "algorithmic_flops_per_step": fit_flops,
+                         "flop_model": "3 x the unpruned forward op count of the dye-seq per read "
+                                       "(forward, backward from the checkpoints, expected counts)",
                          "estep_kernel_ms": k_avg, "prep_ms_per_step": prep_ms / args.steps},
             "e2e": e2e, "gpu_launches": launches, "clocks": clk,
             "fit": {"iterations": iters, "seconds": fit_s, "final_step": step, "log_l": log_l,
@@ -960,6 +986,7 @@ def main():
                 "kernel": "wp_forward_kernel",
                 "peak_source": "FP32 FMA loop measured live (wp_probe_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                 "algorithmic_flops_per_step": algo_flops,
+                "unpruned_flops_per_step": float(R) * unpruned_forward_flops(ds.seqs, T, C),
                 "forward_ms_per_step": fwd_ms / split_steps, "prep_ms_per_step": prep_ms / split_steps,
                 "forward_launches_per_step": fwd_n / split_steps, "work": work}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
