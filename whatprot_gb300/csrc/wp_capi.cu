@@ -24,6 +24,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "wp_common.cuh"
@@ -174,7 +175,8 @@ struct wp_ctx {
     int S_max = 1;       // max over peptides of prod_c (D_c + 1)
     int scr_floats = 1;  // max over peptides of sum_c (D_c + 1)
     std::vector<PeptideRec> recs;
-    DevBuf d_peps, d_ids, d_counts, d_perm, d_shape_rank;
+    DevBuf d_peps, d_ids, d_counts, d_perm, d_shape_rank, d_uniq_D, d_pep_u;
+    int n_uniq_D = 0;
 
     // Kernel timing.
     bool timing = false;
@@ -342,6 +344,31 @@ wp_status plan_peptides(wp_ctx* ctx) {
         }
         wp_pack_peptide(rec);
     }
+    // Distinct dye-count vectors (the compaction sizes a pair's boxes once
+    // per read and distinct vector) and each peptide's vector.
+    {
+        std::vector<uint32_t> uniq;
+        std::vector<int> pu(P);
+        std::unordered_map<uint32_t, int> at;
+        for (int i = 0; i < P; i++) {
+            uint32_t k = 0;
+            for (int c = 0; c < WP_MAX_CHANNELS; c++) k |= (uint32_t)ctx->recs[i].D[c] << (8 * c);
+            auto it = at.find(k);
+            if (it == at.end()) {
+                it = at.emplace(k, (int)uniq.size()).first;
+                uniq.push_back(k);
+            }
+            pu[i] = it->second;
+        }
+        ctx->n_uniq_D = (int)uniq.size();
+        WP_CUDA(ctx->d_uniq_D.ensure(sizeof(uint32_t) * std::max<size_t>(uniq.size(), 1)), "alloc dye-count vectors");
+        WP_CUDA(ctx->d_pep_u.ensure(sizeof(int) * std::max(P, 1)), "alloc dye-count vectors");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_uniq_D.p, uniq.data(), sizeof(uint32_t) * uniq.size(), cudaMemcpyHostToDevice,
+                                ctx->stream), "copy dye-count vectors");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_pep_u.p, pu.data(), sizeof(int) * P, cudaMemcpyHostToDevice, ctx->stream),
+                "copy dye-count vectors");
+        WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    }
     // Shape order (Edman-slice size, then dye counts) for the compaction.
     std::vector<int> perm(P);
     for (int i = 0; i < P; i++) perm[i] = i;
@@ -488,6 +515,9 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         a.perm = ctx->d_perm.as<int>();
     }
     if (a.cand) a.shape_rank = ctx->d_shape_rank.as<int>();
+    a.uniq_D = ctx->d_uniq_D.as<uint32_t>();
+    a.pep_u = ctx->d_pep_u.as<int>();
+    a.n_uniq = ctx->n_uniq_D;
     ctx->last_slots = n_slots;
     const size_t ns = (size_t)std::max<long>(n_slots, 1);
     WP_CUDA(ctx->d_res_mant.ensure(sizeof(float) * ns), "alloc results");

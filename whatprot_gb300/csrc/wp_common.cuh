@@ -149,6 +149,9 @@ struct BatchArgs {
     const int* cand;           // per slot: peptide index (null: all peptides)
     const int* perm;           // all-peptides mode: peptides in shape order (or null)
     const int* shape_rank;     // candidate mode: each peptide's position in that order (or null)
+    const uint32_t* uniq_D;    // distinct dye-count vectors, byte c = channel c (or null)
+    const int* pep_u;          // per peptide: its vector's index in uniq_D
+    int n_uniq;
     const int* slot_off;       // [R + 1] or null
     float* res_mant;           // per slot: P = res_mant * 2^res_expo
     int* res_expo;

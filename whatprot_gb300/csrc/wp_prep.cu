@@ -34,6 +34,7 @@
 #include "wp_common.cuh"
 
 #define WP_COMPACT_SORT 1024  // candidate slots per read the compaction orders by shape
+#define WP_COMPACT_UNIQ 1024  // distinct dye-count vectors the compaction tabulates per read
 
 
 // ChannelModel::adjusted_mu (parameterization/model/channel-model.h:35-54).
@@ -283,6 +284,22 @@ __global__ void wp_compact_kernel(BatchArgs a) {
         sL[t] = a.Lpk[(long)r * m.T + t];
         sU[t] = a.Upk[(long)r * m.T + t];
     }
+    __syncthreads();
+    // The largest box of this read's pairs per distinct dye-count vector
+    // (pair_vmax depends on the peptide through its dye counts only).
+    __shared__ int s_vmax[WP_COMPACT_UNIQ];
+    const bool vtab = a.uniq_D && a.n_uniq > 0 && a.n_uniq <= WP_COMPACT_UNIQ && !read_empty;
+    if (vtab) {
+        for (int u = threadIdx.x; u < a.n_uniq; u += blockDim.x) {
+            uint8_t D[WP_MAX_CHANNELS];
+            bool ok = true;
+            for (int c = 0; c < WP_MAX_CHANNELS; c++) {
+                D[c] = (uint8_t)((a.uniq_D[u] >> (8 * c)) & 0xffu);
+                if (c < C && D[c] < minD[c]) ok = false;
+            }
+            s_vmax[u] = ok ? pair_vmax(C, m.T, sL, sU, D) : 0;
+        }
+    }
     // Candidate mode: the read's slots in the peptides' shape order (up to
     // WP_COMPACT_SORT slots; more keep their order), sorted here by a
     // bitonic sort of (shape rank, slot) keys.
@@ -331,7 +348,7 @@ __global__ void wp_compact_kernel(BatchArgs a) {
             if (live) {
                 // the pair's largest box waits in its result slot for the
                 // engine, which checks it against its slab before any write
-                const int vm = pair_vmax(C, m.T, sL, sU, pep.D);
+                const int vm = vtab ? s_vmax[a.pep_u[p]] : pair_vmax(C, m.T, sL, sU, pep.D);
                 a.res_expo[g] = vm;
                 dest = 0;
                 if (a.n_tiers > 0) {
