@@ -72,3 +72,25 @@ def test_simulate_then_classify_nn_hybrid_and_fit(tmp_path, capsys):
     assert cli.main(["fit", "-P", P, "-L", "1e-4", "-x", str(fz["seq_str"]), "-R", Rf]) == 0
     out = capsys.readouterr().out
     assert "Parameters:" in out and "log(L): " in out and "Final step-size: " in out
+
+
+def test_fit_with_emission_settings(tmp_path, capsys):
+    """`fit -F settings.json` with "fit_emission": true (an extension) fits
+    mu, sig and bg_sig too and prints them after the reference's parameter
+    line; the reference's own settings keys still apply (a held rate stays
+    at its start)."""
+    sm = paper_model(2)
+    P = tmp_path / "seq-params.json"
+    with open(P, "w") as f:
+        json.dump(sm.to_json_dict(), f)
+    fz = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "fit_c2_t8.npz"))
+    Rf = str(tmp_path / "fit-rads.tsv")
+    io.write_radiometries(Rf, sm, fz["rads"])
+    F = tmp_path / "fit-settings.json"
+    with open(F, "w") as f:
+        json.dump({"hold_p_edman_failure": True, "fit_emission": True}, f)
+    capsys.readouterr()
+    assert cli.main(["fit", "-P", str(P), "-L", "1e-4", "-x", str(fz["seq_str"]), "-R", Rf, "-F", str(F)]) == 0
+    out = capsys.readouterr().out
+    assert "Channel 0 emission: (mu: " in out and "Channel 1 emission: (mu: " in out
+    assert f"Edman failure rate: {sm.p_edman_failure:.6f}" in out
