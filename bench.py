@@ -12,7 +12,7 @@ A step is one `classify hmm` pass over the batch: 100,000 x 1,000 =
 1e8 (read, peptide) forwards, argmax and count-weighted totals per read.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload classify|fit|hybrid|learned]
+                    [--workload classify|fit|hybrid|learned|tracks]
 
 `--workload fit` measures the Baum-Welch E-step instead (reads/s): one
 dye-seq of 20 positions with 4/3/3 dyes on 3 channels (positions seeded),
@@ -26,6 +26,11 @@ dye-seqs as above, a dye-track training set of 100 simulated reads per
 dye-seq (about 945,000 unique tracks), kNN with k = 10,000 hits and sigma
 0.5, the top 1,000 candidates rescored by the HMM (pruning 5 sigma), 100,000
 query reads per step (--reads to change).
+
+`--workload tracks` measures `simulate dt` (dye-tracks/s): the hybrid
+workload's training set, 100 dye-tracks for each of the 20,000 dye-seqs
+(2,000,000 instances), generated and deduplicated on the device; the CPU
+baseline is the oracle's single-threaded generate + dedup on a sample.
 
 `--workload learned` trains the proposal network (--epochs of 10,000,000
 reads simulated on the GPU) and measures the hybrid with its top-200
@@ -262,6 +267,206 @@ def run_reference_hybrid(args):
             "cpu_baseline": {"value": value, "unit": HY_UNIT, "cores": threads, "kind": kind,
                              "sample": f"{n} reads per step"},
             "e2e": {"value": value, "unit": HY_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+DT_METRIC = "dye-tracks generated and deduplicated per second (simulate dt)"
+DT_UNIT = "tracks/s"
+DT_WORKLOAD = ("simulate dt: the hybrid workload's kNN training set -- 20000 dye-seqs (8-30 positions, <=5 dyes per "
+               "channel, >=1 dye), 3 channels x 16 timesteps, 100 dye-tracks per dye-seq (2,000,000 instances) "
+               "generated from the error model and deduplicated into unique tracks with (id, count, hits) sources")
+
+
+def make_tracks_data():
+    from whatprot_gb300.simulate import paper_model, random_dye_seqs
+    return paper_model(C), random_dye_seqs(HY_P, C, 8, 30, max_per_channel=5, min_total=1, seed=1234)
+
+
+def cpu_baseline_tracks(sm, ds, seconds_target=15.0):
+    """The oracle's single-threaded generate_dye_tracks + dedup (C, as the
+    reference runs them) on a bounded sample of the dye-seqs."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from oracle_lib import Oracle
+    from whatprot_gb300.model import DyeSeqSet
+    o = Oracle()
+
+    def sample(m):
+        return DyeSeqSet(ds.num_channels, ds.seqs[:m], ds.ids[:m], ds.counts[:m])
+
+    m = 500
+    t0 = time.perf_counter()
+    o.simulate_dt(sm, T, sample(m), HY_PER, 11)
+    dt = time.perf_counter() - t0
+    m = int(min(len(ds), max(m, m * seconds_target / max(dt, 1e-3))))
+    t0 = time.perf_counter()
+    _, kept = o.simulate_dt(sm, T, sample(m), HY_PER, 12)
+    dt = time.perf_counter() - t0
+    n = m * HY_PER
+    return {"value": n / dt, "unit": DT_UNIT, "cores": 1, "kind": "port",
+            "sample": f"{m} dye-seqs x {HY_PER} tracks ({n} instances, {kept} detectable), {dt:.1f} s, "
+                      f"oracle/wp_oracle.c wpo_simulate_dt (generate + sort-based dedup, one thread)"}
+
+
+def run_tracks(args):
+    import torch
+    from whatprot_gb300 import capi
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sm, ds = make_tracks_data()
+    n = HY_PER * int(ds.counts.sum())
+    ctx = capi.Context(local)
+    ctx.upload_model(sm, T)
+    ctx.upload_peptides(ds)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=torch.device("cuda", local))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    seed = 100 + 1000003 * rank
+
+    def step(i):
+        ctx.simulate_dye_track_set(HY_PER, seed=seed + i, download=False)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    ctx.timing_enable(True)
+    launches0 = ctx.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    total_ms = 0.0
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        step(args.warmup + i)
+        ev1.record(stream)
+        ev1.synchronize()
+        total_ms += ev0.elapsed_time(ev1)
+    barrier()
+    clk = clocks.stop()
+    launches = ctx.launch_count() - launches0
+    sim_ms, _ = ctx.timing_read(ctx.KIND_SIM)
+    dd_ms, _ = ctx.timing_read(ctx.KIND_DEDUP)
+    ctx.timing_enable(False)
+    t_step = total_ms / args.steps
+    if dist:
+        t = torch.tensor([t_step], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+    value = n * world / (t_step * 1e-3)
+    # end to end through the public call: generate, dedup and download the set
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        dts = ctx.simulate_dye_track_set(HY_PER, seed=seed + 7 * i)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    U, S = len(dts), int(dts.src_off[-1])
+    TC = T * C
+    e2e = {"value": n * world / e2e_s, "unit": DT_UNIT, "h2d_bytes_per_step": 0,
+           "d2h_bytes_per_step": int(U * TC * 2 + (U + 1) * 4 + 3 * S * 4 + 8)}
+    # rooflines (HBM): the simulator's algorithmic traffic is its output,
+    # n x (T*C track bytes + 4-byte peptide index); the dedup's is one read of
+    # the instances (T*C bytes + 4-byte peptide index) and one write of the
+    # set (int16 tracks, CSR offsets, 3 ints per source) -- what any dedup
+    # must move; the sort passes in between are the dedup's own overhead
+    peak = None
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peak = json.load(f).get("hbm_gbs")
+    except OSError:
+        pass
+    sim_step, dd_step = sim_ms / args.steps, dd_ms / args.steps
+    sim_bytes = n * (TC + 4)
+    dd_bytes = n * (TC + 4) + U * TC * 2 + (U + 1) * 4 + 3 * S * 4
+    phases = {"simulator": {"kernel": "wp_sim_reads_kernel", "ms_per_step": sim_step,
+                            "algorithmic_bytes": sim_bytes,
+                            "achieved_gbs": sim_bytes / (sim_step * 1e-3) / 1e9 if sim_step > 0 else None},
+              "dedup": {"kernel": "dd_* kernels + CUB radix sorts and scans", "ms_per_step": dd_step,
+                        "algorithmic_bytes": dd_bytes,
+                        "achieved_gbs": dd_bytes / (dd_step * 1e-3) / 1e9 if dd_step > 0 else None}}
+    dom = "simulator" if sim_step >= dd_step else "dedup"
+    ach = phases[dom]["achieved_gbs"]
+    line = {"metric": DT_METRIC, "value": value, "unit": DT_UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8/int16 counts, fp64 draws", "data": "synthetic (seeded simulator)",
+            "config": {"workload": DT_WORKLOAD, "peptides": len(ds), "per_peptide": HY_PER, "instances": n,
+                       "unique_tracks": U, "sources": S, "l2": "flushed between steps (512 MB write)"},
+            "roofline": {"bound": "hbm", "kernel": phases[dom]["kernel"], "achieved": ach, "peak": peak,
+                         "unit": "GB/s", "frac": ach / peak if (ach and peak) else None, "traffic": None,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)", "phases": phases},
+            "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_tracks(sm, ds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_reference_tracks(args):
+    """The reference's generate_dye_tracks + dedup_dye_tracks (its own
+    sources and MapReduce-MPI, oracle/_ref) on a bounded sample of the
+    dye-seqs, one thread as it runs; the oracle port where oracle/_ref is
+    absent."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    import oracle_lib
+    from whatprot_gb300.model import DyeSeqSet
+    sm, ds = make_tracks_data()
+    kind = "port"
+    if oracle_lib.Reference.available():
+        ref = oracle_lib.Reference()
+        kind = "reference"
+
+        def runner(sub, s):
+            return ref.simulate_dt(sm, T, sub, HY_PER, s)[0]
+    else:
+        o = oracle_lib.Oracle()
+
+        def runner(sub, s):
+            t0 = time.perf_counter()
+            o.simulate_dt(sm, T, sub, HY_PER, s)
+            return time.perf_counter() - t0
+
+    def sample(m):
+        return DyeSeqSet(ds.num_channels, ds.seqs[:m], ds.ids[:m], ds.counts[:m])
+
+    m = 500
+    dt = runner(sample(m), 1)
+    m = int(min(len(ds), max(m, m * 8.0 / max(dt, 1e-3))))
+    for i in range(args.warmup):
+        runner(sample(m), 2 + i)
+    tot = 0.0
+    for i in range(args.steps):
+        tot += runner(sample(m), 100 + i)
+    dt = tot / max(args.steps, 1)
+    n = m * HY_PER
+    value = n / dt
+    line = {"metric": DT_METRIC, "value": value, "unit": DT_UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int16 counts, fp64 draws", "data": "synthetic (seeded simulator)",
+            "config": {"workload": DT_WORKLOAD, "sample_peptides_per_step": m, "sample_instances_per_step": n},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": DT_UNIT, "cores": 1, "kind": kind,
+                             "sample": f"{m} dye-seqs x {HY_PER} tracks per step"},
+            "e2e": {"value": value, "unit": DT_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -852,7 +1057,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--reads", type=int, default=READS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="classify", choices=["classify", "fit", "hybrid", "learned", "gemm"])
+    ap.add_argument("--workload", default="classify",
+                    choices=["classify", "fit", "hybrid", "learned", "gemm", "tracks"])
     ap.add_argument("--epochs", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true",
                     help="classify: skip the engine autotuner and use the default launch shapes")
@@ -868,6 +1074,8 @@ def main():
         return run_learned(args)
     if args.workload == "hybrid":
         return run_reference_hybrid(args) if args.impl == "reference" else run_hybrid(args)
+    if args.workload == "tracks":
+        return run_reference_tracks(args) if args.impl == "reference" else run_tracks(args)
     if args.workload == "fit":
         return run_reference_fit(args) if args.impl == "reference" else run_fit(args)
     if args.impl == "reference":

@@ -373,6 +373,46 @@ wp_status wp_simulate_reads(wp_ctx* ctx, int num_reads, unsigned long long seed,
                             double* out_rads, int32_t* out_peptide,
                             uint8_t* out_tracks);
 
+/* ---- Dye-track sets (the kNN training data) on the device.  The result of
+ * the last of the two calls below stays on the device: wp_dye_tracks_download
+ * copies it out, wp_dye_tracks_to_nn makes it the kNN / hybrid training set
+ * (as wp_nn_tracks_upload would).  Tracks come out in lexicographic order of
+ * their counts and each track's sources in ascending id; the reference's
+ * order is that of its hash tables. */
+
+/* dedup_dye_tracks (simulation/dedup-dye-tracks.cc:35-61): num_tracks
+ * dye-tracks counts [N][T][C] (non-negative), instance i from source
+ * (ids[i], src_counts[i]) -> the distinct tracks, each with one
+ * (id, count, hits) per distinct source id: count that of the id's first
+ * instance, hits the number of its instances.  All-zero tracks are kept, as
+ * the reference keeps them.  Writes the numbers of distinct tracks and of
+ * sources. */
+wp_status wp_dedup_dye_tracks(wp_ctx* ctx, const int16_t* counts, const int32_t* ids,
+                              const int32_t* src_counts, int num_tracks, int T, int C,
+                              int* out_num_tracks, int* out_num_sources);
+
+/* generate_dye_tracks (simulation/generate-dye-tracks.cc:32-70) followed by
+ * the dedup above, as `simulate dt` runs them (main/run-simulate-dt.cc:
+ * 61-81): per_peptide dye-tracks for each of the count copies of every
+ * uploaded dye-seq (instance r of copy r / per_peptide, Philox subsequence r
+ * of `seed`), the context's model and timesteps; instances with no dye at
+ * the first timestep are dropped.  out_instance_tracks [n][T][C] and
+ * out_instance_peptide [n] (peptide index, -1 for a dropped instance), n =
+ * per_peptide x the sum of the counts, return the instances (may be NULL). */
+wp_status wp_simulate_dye_tracks(wp_ctx* ctx, int per_peptide, unsigned long long seed,
+                                 int* out_num_tracks, int* out_num_sources,
+                                 uint8_t* out_instance_tracks,
+                                 int32_t* out_instance_peptide);
+
+/* Copies the last dye-track set out: counts [U][T][C], src_off [U + 1],
+ * src_id / src_count / src_hits [S]. */
+wp_status wp_dye_tracks_download(wp_ctx* ctx, int16_t* counts, int32_t* src_off,
+                                 int32_t* src_id, int32_t* src_count,
+                                 int32_t* src_hits);
+
+/* Makes the last dye-track set the kNN / hybrid training set. */
+wp_status wp_dye_tracks_to_nn(wp_ctx* ctx);
+
 /* BF16 tensor-core GEMM (tcgen05, TMEM accumulator), the building block of
  * the learned proposal network, exposed for tests: C = act(A . B^T + bias)
  * on device pointers, A [M][K] (pitch lda), B [N][K] (pitch ldb) BF16
@@ -462,7 +502,9 @@ void* wp_ctx_stream(const wp_ctx* ctx);
 
 /* Per-kernel timing with CUDA events recorded on the context's stream around
  * every launch while enabled.  kind: 0 forward (and fit E-step), 1 prep,
- * 2 combine, 3 flop count, 4 kNN distances, 5 kNN select.  wp_timing_read synchronises and returns the summed duration in ms
+ * 2 combine, 3 flop count, 4 kNN distances, 5 kNN select, 6 simulator,
+ * 7 dye-track dedup (all its kernels and sorts).  wp_timing_read
+ * synchronises and returns the summed duration in ms
  * and the number of launches since the last enable.  No reference
  * counterpart (the reference only prints phase wall times,
  * main/cmd-line-out.cc). */

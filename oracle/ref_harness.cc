@@ -31,7 +31,9 @@
 #include "parameterization/model/sequencing-model.h"
 #include "parameterization/settings/fit-settings.h"
 #include "parameterization/settings/sequencing-settings.h"
+#include "simulation/dedup-dye-tracks.h"
 #include "simulation/generate-dye-track.h"
+#include "simulation/generate-dye-tracks.h"
 #include "util/levmar-helper.h"
 #include "wp_oracle.h"
 
@@ -379,6 +381,70 @@ void ref_generate_dye_tracks(const wpo_model* m, int T, const char* dye_seq, int
         for (int t = 0; t < T; t++)
             for (int c = 0; c < C; c++) out[((long)i * T + t) * C + c] = dt(t, c);
     }
+}
+
+// dedup_dye_tracks (simulation/dedup-dye-tracks.cc:35-61, on the vendored
+// MapReduce-MPI with its serial stubs) over n given dye-tracks [n][T][C]
+// with sources (ids[i], cnts[i]), as run-simulate-dt.cc:63-78 calls it.
+// Writes the unique tracks, in the order the reference produces them, with
+// CSR sources; the out arrays hold at least n tracks and n sources.
+void ref_dedup_dye_tracks(int T, int C, int n, const int16_t* counts, const int* ids, const int* cnts,
+                          int* out_num_tracks, int* out_num_sources, int16_t* out_counts, int* out_src_off,
+                          int* out_src_id, int* out_src_count, int* out_src_hits) {
+    std::vector<SourcedData<DyeTrack, SourceCount<int>>> in;
+    in.reserve(n);
+    for (int i = 0; i < n; i++) {
+        DyeTrack dt(T, C);
+        for (int t = 0; t < T; t++)
+            for (int c = 0; c < C; c++) dt(t, c) = counts[((long)i * T + t) * C + c];
+        in.push_back(SourcedData<DyeTrack, SourceCount<int>>(std::move(dt), SourceCount<int>(ids[i], cnts[i])));
+    }
+    std::vector<SourcedData<DyeTrack, SourceCountHitsList<int>>> out;
+    dedup_dye_tracks(T, C, &in, &out);
+    int s = 0;
+    out_src_off[0] = 0;
+    for (size_t u = 0; u < out.size(); u++) {
+        for (int t = 0; t < T; t++)
+            for (int c = 0; c < C; c++) out_counts[((long)u * T + t) * C + c] = out[u].value(t, c);
+        for (int k = 0; k < out[u].source.num_sources; k++, s++) {
+            out_src_id[s] = out[u].source.sources[k]->source;
+            out_src_count[s] = out[u].source.sources[k]->count;
+            out_src_hits[s] = out[u].source.sources[k]->hits;
+        }
+        out_src_off[u + 1] = s;
+    }
+    *out_num_tracks = (int)out.size();
+    *out_num_sources = s;
+}
+
+// `simulate dt` (main/run-simulate-dt.cc:61-81): generate_dye_tracks over P
+// dye-seqs with (ids, counts), per_peptide tracks per peptide copy, from
+// std::default_random_engine(seed), then dedup_dye_tracks.  Returns the
+// wall seconds of the two calls; writes the numbers of kept instances,
+// distinct tracks and sources.
+double ref_simulate_dt(const wpo_model* m, int T, int P, const char* const* seqs, const int* ids,
+                       const int* counts, int per_peptide, unsigned seed, int* out_instances,
+                       int* out_num_tracks, int* out_num_sources) {
+    int C = m->num_channels;
+    SequencingModel sm;
+    to_reference(m, &sm);
+    std::vector<SourcedData<DyeSeq, SourceCount<int>>> dye_seqs;
+    for (int i = 0; i < P; i++)
+        dye_seqs.push_back(SourcedData<DyeSeq, SourceCount<int>>(DyeSeq(C, std::string(seqs[i])),
+                                                                 SourceCount<int>(ids[i], counts[i])));
+    std::default_random_engine gen(seed);
+    double t0 = omp_get_wtime();
+    std::vector<SourcedData<DyeTrack, SourceCount<int>>> tracks;
+    generate_dye_tracks(sm, dye_seqs, T, C, per_peptide, &gen, &tracks);
+    std::vector<SourcedData<DyeTrack, SourceCountHitsList<int>>> out;
+    dedup_dye_tracks(T, C, &tracks, &out);
+    double t1 = omp_get_wtime();
+    int s = 0;
+    for (auto& d : out) s += d.source.num_sources;
+    *out_instances = (int)tracks.size();
+    *out_num_tracks = (int)out.size();
+    *out_num_sources = s;
+    return t1 - t0;
 }
 
 }  // extern "C"

@@ -1640,3 +1640,170 @@ void wpo_hybrid_classify_batch(const wpo_model* m, int T, const int16_t* track_c
     free(j.out_cand_score);
     free(j.out_total);
 }
+
+/* ---- dye-track dedup (simulation/dedup-dye-tracks.cc:35-141) ----------- */
+
+typedef struct {
+    const int16_t* counts;
+    const int32_t* ids;
+    int TC;
+} dedup_ctx;
+
+static dedup_ctx g_dedup;  /* qsort has no context argument in C11 */
+
+static int dedup_cmp(const void* a, const void* b) {
+    const int i = *(const int*)a, j = *(const int*)b;
+    const int16_t* x = g_dedup.counts + (long)i * g_dedup.TC;
+    const int16_t* y = g_dedup.counts + (long)j * g_dedup.TC;
+    for (int k = 0; k < g_dedup.TC; k++)
+        if (x[k] != y[k]) return x[k] < y[k] ? -1 : 1;
+    if (g_dedup.ids[i] != g_dedup.ids[j]) return g_dedup.ids[i] < g_dedup.ids[j] ? -1 : 1;
+    return i < j ? -1 : (i > j);  /* first instance of an id first */
+}
+
+int wpo_dedup_dye_tracks(int T, int C, int n, const int16_t* counts, const int32_t* ids,
+                         const int32_t* cnts, int16_t* out_counts, int32_t* out_src_off,
+                         int32_t* out_src_id, int32_t* out_src_count, int32_t* out_src_hits,
+                         int32_t* out_num_sources) {
+    const int TC = T * C;
+    int* order = (int*)malloc(sizeof(int) * (n > 0 ? n : 1));
+    for (int i = 0; i < n; i++) order[i] = i;
+    g_dedup.counts = counts;
+    g_dedup.ids = ids;
+    g_dedup.TC = TC;
+    qsort(order, n, sizeof(int), dedup_cmp);
+    int u = 0, s = 0;
+    out_src_off[0] = 0;
+    for (int a = 0; a < n;) {
+        /* one distinct track: the key of the reference's map-reduce */
+        const int16_t* key = counts + (long)order[a] * TC;
+        int b = a;
+        while (b < n && memcmp(counts + (long)order[b] * TC, key, sizeof(int16_t) * TC) == 0) b++;
+        memcpy(out_counts + (long)u * TC, key, sizeof(int16_t) * TC);
+        /* reduce_dye_tracks_helper: one entry per source id */
+        for (int i = a; i < b;) {
+            int j = i;
+            while (j < b && ids[order[j]] == ids[order[i]]) j++;
+            out_src_id[s] = ids[order[i]];
+            out_src_count[s] = cnts[order[i]];
+            out_src_hits[s] = j - i;
+            s++;
+            i = j;
+        }
+        out_src_off[++u] = s;
+        a = b;
+    }
+    free(order);
+    *out_num_sources = s;
+    return u;
+}
+
+/* ---- dye-track generation (simulation/generate-dye-track.cc:29-110) ---- */
+
+typedef struct {
+    uint64_t s[4];
+} xoshiro;
+
+static uint64_t splitmix64(uint64_t* x) {
+    uint64_t z = (*x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static uint64_t rotl64(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+/* xoshiro256** (Blackman and Vigna) -> uniform double in [0, 1) */
+static double xo_uniform(xoshiro* g) {
+    uint64_t* s = g->s;
+    const uint64_t r = rotl64(s[1] * 5, 7) * 9, t = s[1] << 17;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = rotl64(s[3], 45);
+    return (double)(r >> 11) * 0x1.0p-53;
+}
+
+/* bernoulli_distribution(p)(gen) */
+static int xo_bernoulli(xoshiro* g, double p) { return xo_uniform(g) < p; }
+
+/* generate_dye_track for one dye-seq of length L: counts [T][C]. */
+static void gen_dye_track(const wpo_model* m, const double* p_det, int T, const int16_t* seq, int L,
+                          xoshiro* g, int16_t* ds, int16_t* out) {
+    const int C = m->num_channels;
+    memcpy(ds, seq, sizeof(int16_t) * L);
+    for (int i = 0; i < L; i++)  /* duds */
+        if (ds[i] != -1 && xo_bernoulli(g, m->p_dud[ds[i]])) ds[i] = -1;
+    int16_t cnt[WPO_MAX_CHANNELS] = {0};
+    for (int i = 0; i < L; i++)
+        if (ds[i] != -1) cnt[ds[i]]++;
+    int e = 0;
+    int block = xo_bernoulli(g, m->p_initial_block);
+    for (int t = 0; t < T; t++) {
+        if (e < L) {
+            for (int c = 0; c < C; c++) out[t * C + c] = cnt[c];
+            if (xo_bernoulli(g, m->p_cyclic_block)) block = 1;
+            if (xo_bernoulli(g, p_det[t])) {  /* detach */
+                e = L;
+                continue;
+            }
+            if (!block && !xo_bernoulli(g, m->p_edman_failure)) {
+                if (ds[e] != -1) cnt[ds[e]]--;
+                e++;
+            }
+            for (int i = e; i < L; i++)  /* bleaching */
+                if (ds[i] != -1 && xo_bernoulli(g, m->p_bleach[ds[i]])) {
+                    cnt[ds[i]]--;
+                    ds[i] = -1;
+                }
+        } else {
+            for (int c = 0; c < C; c++) out[t * C + c] = 0;
+        }
+    }
+}
+
+int wpo_simulate_dt(const wpo_model* m, int T, const int16_t* seqs, const int32_t* offsets,
+                    const int32_t* ids, const int32_t* counts, int P, int per_peptide,
+                    uint64_t seed, int16_t* out_counts, int32_t* out_src_off,
+                    int32_t* out_src_id, int32_t* out_src_count, int32_t* out_src_hits,
+                    int32_t* out_num_sources, int32_t* out_instances) {
+    const int C = m->num_channels, TC = T * C;
+    long n = 0;
+    int Lmax = 1;
+    for (int p = 0; p < P; p++) {
+        n += (long)counts[p] * per_peptide;
+        if (offsets[p + 1] - offsets[p] > Lmax) Lmax = offsets[p + 1] - offsets[p];
+    }
+    double p_det[WPO_MAX_TIMESTEPS];
+    for (int t = 0; t < T; t++) p_det[t] = wpo_p_detach_at(m, (unsigned)t);
+    xoshiro g;
+    uint64_t sm = seed;
+    for (int k = 0; k < 4; k++) g.s[k] = splitmix64(&sm);
+    int16_t* tracks = (int16_t*)malloc(sizeof(int16_t) * (n > 0 ? n : 1) * TC);
+    int32_t* tid = (int32_t*)malloc(sizeof(int32_t) * (n > 0 ? n : 1));
+    int32_t* tcnt = (int32_t*)malloc(sizeof(int32_t) * (n > 0 ? n : 1));
+    int16_t* ds = (int16_t*)malloc(sizeof(int16_t) * Lmax);
+    long kept = 0;
+    for (int p = 0; p < P; p++)
+        for (long r = 0; r < (long)counts[p] * per_peptide; r++) {
+            int16_t* tr = tracks + kept * TC;
+            gen_dye_track(m, p_det, T, seqs + offsets[p], offsets[p + 1] - offsets[p], &g, ds, tr);
+            int nontrivial = 0;
+            for (int c = 0; c < C; c++) nontrivial |= tr[c] != 0;
+            if (nontrivial) {
+                tid[kept] = ids[p];
+                tcnt[kept] = counts[p];
+                kept++;
+            }
+        }
+    const int u = wpo_dedup_dye_tracks(T, C, (int)kept, tracks, tid, tcnt, out_counts, out_src_off, out_src_id,
+                                       out_src_count, out_src_hits, out_num_sources);
+    *out_instances = (int32_t)kept;
+    free(tracks);
+    free(tid);
+    free(tcnt);
+    free(ds);
+    return u;
+}

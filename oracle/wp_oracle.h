@@ -177,6 +177,32 @@ void wpo_hybrid_classify_batch(const wpo_model* m, int T, const int16_t* track_c
                                double sig, int h, double dist_cutoff, int threads,
                                int32_t* out_id, double* out_score, double* out_total);
 
+/* dedup_dye_tracks (simulation/dedup-dye-tracks.cc:35-141): n dye-tracks
+ * [n][T][C] with sources (ids[i], cnts[i]) -> the distinct tracks, each with
+ * one (id, count, hits) per distinct source id: count is that of the id's
+ * first instance (dedup-dye-tracks.cc:119-124), hits the number of
+ * instances.  The reference's output order is that of its hash tables; this
+ * one is canonical: tracks in lexicographic order of their counts, sources
+ * in ascending id.  The out arrays hold at least n tracks and n sources;
+ * returns the number of tracks and writes the number of sources. */
+int wpo_dedup_dye_tracks(int T, int C, int n, const int16_t* counts, const int32_t* ids,
+                         const int32_t* cnts, int16_t* out_counts, int32_t* out_src_off,
+                         int32_t* out_src_id, int32_t* out_src_count, int32_t* out_src_hits,
+                         int32_t* out_num_sources);
+
+/* `simulate dt` (main/run-simulate-dt.cc:61-81): generate_dye_tracks
+ * (simulation/generate-dye-tracks.cc:32-70; per dye-seq, per_peptide tracks
+ * for each of its count copies, generate_dye_track, generate-dye-track.cc:
+ * 29-110; instances with no dye at t = 0 dropped) from a seeded xoshiro256**
+ * stream, then wpo_dedup_dye_tracks.  Single-threaded, as the reference.
+ * The out arrays hold per_peptide x sum(counts) tracks and sources; returns
+ * the number of distinct tracks, writes the sources and kept instances. */
+int wpo_simulate_dt(const wpo_model* m, int T, const int16_t* seqs, const int32_t* offsets,
+                    const int32_t* ids, const int32_t* counts, int P, int per_peptide,
+                    uint64_t seed, int16_t* out_counts, int32_t* out_src_off,
+                    int32_t* out_src_id, int32_t* out_src_count, int32_t* out_src_hits,
+                    int32_t* out_num_sources, int32_t* out_instances);
+
 #ifdef __cplusplus
 }
 #endif

@@ -148,10 +148,39 @@ def sim_fixture(name, seed):
     print(name, "trivial fractions", trivial)
 
 
+def dedup_fixture(name, seed):
+    """The reference's dedup_dye_tracks (on its vendored MapReduce-MPI) over
+    dye-tracks from its own generate_dye_track: six dye-seqs, ids repeated
+    across dye-seqs and counts that differ between instances of one id (the
+    reduce keeps the first instance's count), plus a few all-zero tracks
+    (dedup keeps them; only generate_dye_tracks drops them).  Output in
+    canonical order (tracks lexicographic, sources by id)."""
+    sm = paper_model(3)
+    T = 10
+    seqs = ["0.1.2.0.1", ".00..1.22.0.1.2", "2..1..0", "0..1", "22.1", "1.1.1..0"]
+    seq_ids = [5, 9, 5, -3, 7, 9]
+    ref = Reference()
+    rng = np.random.default_rng(seed)
+    tracks, ids, cnts = [], [], []
+    for i, s in enumerate(seqs):
+        tr = ref.generate_dye_tracks(sm, T, s, 500, seed + i)
+        tracks.append(tr)
+        ids += [seq_ids[i]] * len(tr)
+        cnts += list(rng.integers(1, 4, len(tr)))
+    tracks = np.concatenate(tracks)
+    perm = rng.permutation(len(tracks))
+    tracks, ids, cnts = tracks[perm], np.array(ids, np.int32)[perm], np.array(cnts, np.int32)[perm]
+    out = ref.dedup_dye_tracks(tracks, ids, cnts)
+    np.savez_compressed(os.path.join(HERE, name), T=T, C=3, tracks=tracks, ids=ids, cnts=cnts,
+                        out_tracks=out.tracks, out_src_off=out.src_off, out_src_id=out.src_id,
+                        out_src_count=out.src_count, out_src_hits=out.src_hits)
+    print(name, len(tracks), "instances ->", len(out), "tracks,", len(out.src_id), "sources")
+
+
 if __name__ == "__main__":
     if not Reference.available():
         sys.exit("oracle/_ref/libwpref.so missing: run `make -C oracle ref` where the reference is present")
-    which = sys.argv[1:] or ["classify", "pairs", "fit", "nn", "sim"]
+    which = sys.argv[1:] or ["classify", "pairs", "fit", "nn", "sim", "dedup"]
     if "classify" in which:
         classify_fixture("classify_c2_t8.npz", 2, 8, 100, 6, 12, 300, 5.0, seed=101)
         classify_fixture("classify_c3_t16.npz", 3, 16, 60, 8, 30, 60, 5.0, seed=202, maxc=5, mint=1)
@@ -166,3 +195,5 @@ if __name__ == "__main__":
         nn_fixture("nn_c3_t16.npz", 3, 16, 80, 8, 24, 60, 120, 200, 0.5, 30, 5.0, seed=808)
     if "sim" in which:
         sim_fixture("sim_tracks_c3_t12.npz", seed=909)
+    if "dedup" in which:
+        dedup_fixture("dedup_c3_t10.npz", seed=1010)

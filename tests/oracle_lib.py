@@ -93,6 +93,47 @@ def _p(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None else None
 
 
+def canonical_dye_tracks(counts, src_off, src_id, src_count, src_hits):
+    """A dye-track set with tracks in lexicographic order of their counts and
+    each track's sources in ascending id (the reference's own order is that
+    of its hash tables)."""
+    from whatprot_gb300.io import DyeTrackSet
+    N = counts.shape[0]
+    order = np.lexsort(counts.reshape(N, -1).T[::-1]) if N else np.zeros(0, np.int64)
+    off, ids, cnt, hits = [0], [], [], []
+    for u in order:
+        a, b = int(src_off[u]), int(src_off[u + 1])
+        srt = np.argsort(src_id[a:b], kind="stable")
+        ids.extend(src_id[a:b][srt])
+        cnt.extend(src_count[a:b][srt])
+        hits.extend(src_hits[a:b][srt])
+        off.append(len(ids))
+    return DyeTrackSet(counts[order].astype(np.int16), np.array(off, np.int32), np.array(ids, np.int32),
+                       np.array(cnt, np.int32), np.array(hits, np.int32))
+
+
+def _dedup_call(fn, counts, ids, cnts, canonical):
+    counts = np.ascontiguousarray(counts, dtype=np.int16)
+    n, T, C = counts.shape
+    ids = np.ascontiguousarray(ids, dtype=np.int32)
+    cnts = np.ascontiguousarray(cnts, dtype=np.int32)
+    m = max(n, 1)
+    oc = np.zeros((m, T, C), np.int16)
+    off = np.zeros(m + 1, np.int32)
+    sid, scnt, shits = (np.zeros(m, np.int32) for _ in range(3))
+    if canonical:
+        ns = ctypes.c_int32(0)
+        u = fn(T, C, n, _p(counts), _p(ids), _p(cnts), _p(oc), _p(off), _p(sid), _p(scnt), _p(shits),
+               ctypes.byref(ns))
+        ns = ns.value
+    else:
+        nu, nsv = ctypes.c_int(0), ctypes.c_int(0)
+        fn(T, C, n, _p(counts), _p(ids), _p(cnts), ctypes.byref(nu), ctypes.byref(nsv), _p(oc), _p(off),
+           _p(sid), _p(scnt), _p(shits))
+        u, ns = nu.value, nsv.value
+    return canonical_dye_tracks(oc[:u], off[:u + 1], sid[:ns], scnt[:ns], shits[:ns])
+
+
 class Oracle:
     def __init__(self):
         if not os.path.exists(ORACLE_SO):
@@ -128,6 +169,11 @@ class Oracle:
         L.wpo_hybrid_classify_batch.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p, ctypes.c_int] \
             + [ctypes.c_void_p] * 8 + [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_int, ctypes.c_double, ctypes.c_int] + [ctypes.c_void_p] * 3
+        L.wpo_simulate_dt.restype = ctypes.c_int
+        L.wpo_simulate_dt.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int] + [ctypes.c_void_p] * 4 \
+            + [ctypes.c_int, ctypes.c_int, ctypes.c_uint64] + [ctypes.c_void_p] * 7
+        L.wpo_dedup_dye_tracks.restype = ctypes.c_int
+        L.wpo_dedup_dye_tracks.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p] * 9
         L.wpo_improve_fit_batch.restype = None
         L.wpo_improve_fit_batch.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p,
                                             ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
@@ -228,6 +274,30 @@ class Oracle:
                                            cutoff, threads, _p(oid), _p(osc), _p(otot))
         return oid, osc, otot
 
+    def dedup_dye_tracks(self, counts, ids, cnts):
+        """Canonical dedup (tracks lexicographic, sources by id) of counts
+        [n, T, C] with sources (ids, cnts); returns a DyeTrackSet."""
+        return _dedup_call(self.lib.wpo_dedup_dye_tracks, counts, ids, cnts, canonical=True)
+
+    def simulate_dt(self, sm, T, dye_seqs, per_peptide, seed):
+        """generate_dye_tracks + dedup (single thread, seeded); returns the
+        DyeTrackSet and the number of kept (detectable) instances."""
+        from whatprot_gb300.io import DyeTrackSet
+        flat, off = dye_seqs.ragged()
+        ids = np.ascontiguousarray(dye_seqs.ids, dtype=np.int32)
+        cnt = np.ascontiguousarray(dye_seqs.counts, dtype=np.int32)
+        C = sm.num_channels
+        n = max(int(per_peptide) * int(cnt.sum()), 1)
+        oc = np.zeros((n, T, C), np.int16)
+        soff = np.zeros(n + 1, np.int32)
+        sid, scnt, shits = (np.zeros(n, np.int32) for _ in range(3))
+        ns, kept = ctypes.c_int32(0), ctypes.c_int32(0)
+        u = self.lib.wpo_simulate_dt(ctypes.byref(to_wpo(sm)), T, _p(flat), _p(off), _p(ids), _p(cnt),
+                                     len(dye_seqs), per_peptide, seed, _p(oc), _p(soff), _p(sid), _p(scnt),
+                                     _p(shits), ctypes.byref(ns), ctypes.byref(kept))
+        ns = ns.value
+        return DyeTrackSet(oc[:u], soff[:u + 1], sid[:ns], scnt[:ns], shits[:ns]), kept.value
+
     def improve_fit_batch(self, sm, T, seq, rads, threads=8, cutoff=DBL_MAX):
         """E-step over many reads on host threads: (WpoFitSums, log P [R])."""
         m = to_wpo(sm)
@@ -294,6 +364,12 @@ class Reference:
         L.ref_generate_dye_tracks.restype = None
         L.ref_generate_dye_tracks.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                                               ctypes.c_uint, ctypes.c_void_p]
+        L.ref_simulate_dt.restype = ctypes.c_double
+        L.ref_simulate_dt.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_char_p), ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_int, ctypes.c_uint] + [ctypes.POINTER(ctypes.c_int)] * 3
+        L.ref_dedup_dye_tracks.restype = None
+        L.ref_dedup_dye_tracks.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p] * 10
         L.ref_fit.restype = ctypes.c_double
         L.ref_fit.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                               ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.POINTER(WpoModel),
@@ -377,6 +453,24 @@ class Reference:
         rads = np.ascontiguousarray(rads, dtype=np.float64)
         return self.lib.ref_improve_fit_batch(ctypes.byref(m), T, seq_str.encode(), rads.shape[0],
                                               _p(rads), threads)
+
+    def dedup_dye_tracks(self, counts, ids, cnts):
+        """The reference's dedup_dye_tracks on counts [n, T, C] with sources
+        (ids, cnts), canonicalised (tracks lexicographic, sources by id)."""
+        return _dedup_call(self.lib.ref_dedup_dye_tracks, counts, ids, cnts, canonical=False)
+
+    def simulate_dt(self, sm, T, dye_seqs, per_peptide, seed):
+        """The reference's generate_dye_tracks + dedup_dye_tracks over a
+        dye-seq set; returns (seconds, kept instances, tracks, sources)."""
+        from whatprot_gb300.model import dye_seq_string
+        strs = [dye_seq_string(s).encode() for s in dye_seqs.seqs]
+        arr = (ctypes.c_char_p * len(strs))(*strs)
+        ids = np.ascontiguousarray(dye_seqs.ids, dtype=np.int32)
+        cnt = np.ascontiguousarray(dye_seqs.counts, dtype=np.int32)
+        ni, nu, ns = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        secs = self.lib.ref_simulate_dt(ctypes.byref(to_wpo(sm)), T, len(strs), arr, _p(ids), _p(cnt),
+                                        per_peptide, seed, ctypes.byref(ni), ctypes.byref(nu), ctypes.byref(ns))
+        return secs, ni.value, nu.value, ns.value
 
     def generate_dye_tracks(self, sm, T, seq_str, n, seed):
         out = np.zeros((n, T, sm.num_channels), np.int16)

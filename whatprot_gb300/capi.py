@@ -37,7 +37,8 @@ EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload"
            "wp_dev_gemm_bf16", "wp_simulate_reads", "wp_ctx_set_graphs", "wp_set_engine_config",
            "wp_autotune", "wp_mlp_create", "wp_mlp_destroy", "wp_mlp_train",
            "wp_mlp_train_step", "wp_mlp_shape", "wp_mlp_get", "wp_mlp_set", "wp_mlp_logits", "wp_mlp_propose",
-           "wp_mlp_hybrid_classify", "wp_mlp_hybrid_classify_device"]
+           "wp_mlp_hybrid_classify", "wp_mlp_hybrid_classify_device", "wp_dedup_dye_tracks",
+           "wp_simulate_dye_tracks", "wp_dye_tracks_download", "wp_dye_tracks_to_nn"]
 
 
 class WpSeqModel(ctypes.Structure):
@@ -219,6 +220,15 @@ def load_library(path: Optional[str] = None):
     lib.wp_autotune.restype = I
     lib.wp_simulate_reads.argtypes = [V, I, ctypes.c_ulonglong, V, V, V]
     lib.wp_simulate_reads.restype = I
+    PI = ctypes.POINTER(I)
+    lib.wp_dedup_dye_tracks.argtypes = [V, V, V, V, I, I, I, PI, PI]
+    lib.wp_dedup_dye_tracks.restype = I
+    lib.wp_simulate_dye_tracks.argtypes = [V, I, ctypes.c_ulonglong, PI, PI, V, V]
+    lib.wp_simulate_dye_tracks.restype = I
+    lib.wp_dye_tracks_download.argtypes = [V, V, V, V, V, V]
+    lib.wp_dye_tracks_download.restype = I
+    lib.wp_dye_tracks_to_nn.argtypes = [V]
+    lib.wp_dye_tracks_to_nn.restype = I
     LL, U64, F = ctypes.c_longlong, ctypes.c_ulonglong, ctypes.c_float
     lib.wp_mlp_create.argtypes = [V, I, U64, ctypes.POINTER(V)]
     lib.wp_mlp_create.restype = I
@@ -364,6 +374,7 @@ class Context:
         self._check(self.lib.wp_peptides_upload(self.h, _ptr(flat), _ptr(off), _ptr(ids),
                                                 _ptr(counts), len(ds)))
         self.num_peptides = len(ds)
+        self._pep_counts = counts.copy()
 
     def classify(self, rads: np.ndarray, dist_cutoff: float = DBL_MAX,
                  cand: Optional[np.ndarray] = None, cand_off: Optional[np.ndarray] = None):
@@ -473,6 +484,51 @@ class Context:
         off, sid, scnt, shit = arr(dts.src_off), arr(dts.src_id), arr(dts.src_count), arr(dts.src_hits)
         self._check(self.lib.wp_nn_tracks_upload(self.h, _ptr(tr), N, T, C, _ptr(off), _ptr(sid), _ptr(scnt),
                                                  _ptr(shit)))
+
+    def dedup_dye_tracks(self, counts: np.ndarray, ids: np.ndarray, src_counts: np.ndarray):
+        """wp_dedup_dye_tracks on dye-tracks counts [n, T, C] from sources
+        (ids, src_counts); returns the deduplicated io.DyeTrackSet."""
+        tr = np.ascontiguousarray(counts, dtype=np.int16)
+        n, T, C = tr.shape
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        cnt = np.ascontiguousarray(src_counts, dtype=np.int32)
+        if ids.shape != (n,) or cnt.shape != (n,):
+            raise ValueError("ids and src_counts need one entry per dye-track")
+        nu, ns = ctypes.c_int(0), ctypes.c_int(0)
+        self._check(self.lib.wp_dedup_dye_tracks(self.h, _ptr(tr), _ptr(ids), _ptr(cnt), n, T, C,
+                                                 ctypes.byref(nu), ctypes.byref(ns)))
+        return self._download_dye_tracks(nu.value, ns.value, T, C)
+
+    def simulate_dye_track_set(self, per_peptide: int, seed: int = 0, instances: bool = False,
+                               to_nn: bool = False, download: bool = True):
+        """wp_simulate_dye_tracks: the kNN training set of per_peptide
+        dye-tracks per peptide copy, generated and deduplicated on the device
+        with the uploaded model and peptides.  Returns the io.DyeTrackSet
+        (None when download is False), plus the instances (tracks [n, T, C]
+        uint8, peptide index [n]) when asked; to_nn makes the set the kNN /
+        hybrid training set without a host round trip of the caller's."""
+        T, C = self.num_timesteps, self.num_channels
+        n = int(per_peptide) * int(np.sum(getattr(self, "_pep_counts", np.zeros(0)), dtype=np.int64))
+        itr = np.zeros((max(n, 1), T, C), np.uint8) if instances else None
+        ipep = np.zeros(max(n, 1), np.int32) if instances else None
+        nu, ns = ctypes.c_int(0), ctypes.c_int(0)
+        self._check(self.lib.wp_simulate_dye_tracks(self.h, int(per_peptide), ctypes.c_ulonglong(seed),
+                                                    ctypes.byref(nu), ctypes.byref(ns), _ptr(itr), _ptr(ipep)))
+        if to_nn:
+            self._check(self.lib.wp_dye_tracks_to_nn(self.h))
+        dts = self._download_dye_tracks(nu.value, ns.value, T, C) if download else None
+        if instances:
+            return dts, itr[:n], ipep[:n]
+        return dts
+
+    def _download_dye_tracks(self, U: int, S: int, T: int, C: int):
+        from .io import DyeTrackSet
+        counts = np.zeros((max(U, 1), T, C), np.int16)
+        off = np.zeros(U + 1, np.int32)
+        sid, scnt, shit = (np.zeros(max(S, 1), np.int32) for _ in range(3))
+        self._check(self.lib.wp_dye_tracks_download(self.h, _ptr(counts), _ptr(off), _ptr(sid), _ptr(scnt),
+                                                    _ptr(shit)))
+        return DyeTrackSet(counts[:U], off, sid[:S], scnt[:S], shit[:S])
 
     def nn_classify(self, rads: np.ndarray, k: int, sig: float, h: int):
         """wp_nn_classify: (ncand [R], ids [R,h], scores [R,h], total [R])."""
@@ -591,6 +647,7 @@ class Context:
         self._check(self.lib.wp_timing_enable(self.h, 1 if on else 0))
 
     KIND_FORWARD, KIND_PREP, KIND_COMBINE, KIND_FLOPS, KIND_KNN_DIST, KIND_KNN_SELECT = 0, 1, 2, 3, 4, 5
+    KIND_SIM, KIND_DEDUP = 6, 7
 
     def timing_read(self, kind: int) -> Tuple[float, int]:
         ms = ctypes.c_double()

@@ -301,7 +301,6 @@ def run_simulate_rad(t, g, P, S, R, Y):
 
 
 def run_simulate_dt(t, g, P, S, T_):
-    from .simulate import simulate_dye_track_set
     t_all = _t()
     t0 = _t()
     true, sm = _load_model(P)
@@ -310,9 +309,17 @@ def run_simulate_dt(t, g, P, S, T_):
     ds = io.read_dye_seqs(S)
     print(f"Read {len(ds)} dye seqs ({_t() - t0} seconds).")
     t0 = _t()
-    dts = simulate_dye_track_set(sm, ds, t, g, seed=int(time.time() * 1e6) & 0xFFFFFFFF)
-    print(f"Finished generating {int(dts.src_hits.sum())} dye tracks ({_t() - t0}seconds).")
-    print(f"Finished deduping {len(dts)} unique dye tracks ({_t() - t0} seconds).")
+    # generated and deduplicated on the device (wp_simulate_dye_tracks)
+    ctx = capi.Context(0)
+    ctx.upload_model(sm, t)
+    ctx.upload_peptides(ds)
+    ctx.timing_enable(True)
+    dts = ctx.simulate_dye_track_set(g, seed=int(time.time() * 1e6) & 0xFFFFFFFFFFFF)
+    gen_ms, _ = ctx.timing_read(ctx.KIND_SIM)
+    dedup_ms, _ = ctx.timing_read(ctx.KIND_DEDUP)
+    ctx.close()
+    print(f"Finished generating {int(dts.src_hits.sum())} dye tracks ({gen_ms * 1e-3}seconds).")
+    print(f"Finished deduping {len(dts)} unique dye tracks ({dedup_ms * 1e-3}seconds).")
     t0 = _t()
     io.write_dye_tracks(T_, dts)
     print(f"Finished saving results ({_t() - t0} seconds).")

@@ -53,6 +53,9 @@ cudaError_t wp_launch_nn_threshold(cudaStream_t s, const NNArgs& a);
 int wp_nn_bins();
 int wp_engine_max_threads();
 cudaError_t wp_launch_sim_reads(const SimParams& p, cudaStream_t s);
+size_t wp_dedup_temp_bytes(int n);
+cudaError_t wp_launch_dedup_range(const int16_t* c, size_t total, int* minmax, cudaStream_t s);
+cudaError_t wp_launch_dedup(const DedupArgs& a, cudaStream_t s, int* launches);
 #include <cuda_bf16.h>
 cudaError_t wp_mlp_launch_input(const float* xf, const double* xd, int B, int TC, __nv_bfloat16* X, cudaStream_t s);
 cudaError_t wp_mlp_launch_transpose(const __nv_bfloat16* in, int rows, int cols, int ld_in, __nv_bfloat16* out,
@@ -162,8 +165,15 @@ struct wp_ctx {
     double raw_pdud[WP_MAX_CHANNELS] = {0}, raw_pbleach[WP_MAX_CHANNELS] = {0};
     // peptides as the simulator reads them
     long long sim_pep_version = -1;
-    DevBuf d_sim_seqs, d_sim_off, d_sim_cum, d_sim_rads, d_sim_pep, d_sim_tracks;
+    DevBuf d_sim_seqs, d_sim_off, d_sim_cum, d_sim_rads, d_sim_pep, d_sim_tracks, d_sim_ids, d_sim_cnts;
+    int sim_max_dyes = 0;  // most dyes of one channel in one peptide
     DevBuf d_model;
+    // dye-track dedup (wp_dedup.cu): scratch, and the last result, which
+    // stays on the device until downloaded or made the kNN training set
+    DevBuf d_dd_in, d_dd_words, d_dd_k0, d_dd_k1, d_dd_p0, d_dd_p1, d_dd_id, d_dd_cnt, d_dd_ft, d_dd_fs, d_dd_st,
+            d_dd_ss, d_dd_start, d_dd_temp, d_dd_counts, d_dd_off, d_dd_sid, d_dd_scnt, d_dd_hits, d_dd_sizes;
+    bool dd_valid = false;
+    int dd_U = 0, dd_S = 0, dd_T = 0, dd_C = 0;
 
     bool have_peps = false;
     std::vector<int16_t> seqs;
@@ -185,8 +195,8 @@ struct wp_ctx {
         cudaEvent_t a, b;
     };
     std::vector<Timed> timed;
-    double t_ms[6] = {0, 0, 0, 0, 0, 0};
-    long long t_n[6] = {0, 0, 0, 0, 0, 0};
+    double t_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    long long t_n[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     size_t nn_acc_cleared = 0;  // bytes of the kNN accumulators known to be zero
 
     // engine launch shapes (autotuned per shape key) and classify graphs
@@ -939,7 +949,7 @@ wp_status hybrid_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig
 
 // Reads simulated on the device from the context's model and peptides.
 wp_status sim_device(wp_ctx* ctx, int R, unsigned long long seed, float* d_rads_f, double* d_rads_d, int* d_pep,
-                     uint8_t* d_tracks) {
+                     uint8_t* d_tracks, int per_peptide = 0) {
     if (ctx->sim_pep_version != ctx->pep_version) {
         std::vector<int8_t> seqs(std::max<size_t>(ctx->seqs.size(), 1), -1);
         for (size_t i = 0; i < ctx->seqs.size(); i++) seqs[i] = (int8_t)ctx->seqs[i];
@@ -950,6 +960,19 @@ wp_status sim_device(wp_ctx* ctx, int R, unsigned long long seed, float* d_rads_
             cum[i] = acc;
         }
         if (ctx->P > 0 && !(acc > 0.0)) return fail(ctx, WP_ERR_INVALID, "peptide counts sum to zero");
+        int most = 0;
+        for (int i = 0; i < ctx->P; i++) {
+            int per[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+            for (int j = ctx->offsets[i]; j < ctx->offsets[i + 1]; j++)
+                if (ctx->seqs[j] >= 0 && ctx->seqs[j] < WP_MAX_CHANNELS) most = std::max(most, ++per[ctx->seqs[j]]);
+        }
+        ctx->sim_max_dyes = most;
+        WP_CUDA(ctx->d_sim_ids.ensure(sizeof(int) * std::max(ctx->P, 1)), "alloc");
+        WP_CUDA(ctx->d_sim_cnts.ensure(sizeof(int) * std::max(ctx->P, 1)), "alloc");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_sim_ids.p, ctx->ids.data(), sizeof(int) * ctx->P, cudaMemcpyHostToDevice,
+                                ctx->stream), "copy");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_sim_cnts.p, ctx->counts.data(), sizeof(int) * ctx->P, cudaMemcpyHostToDevice,
+                                ctx->stream), "copy");
         WP_CUDA(ctx->d_sim_seqs.ensure(seqs.size()), "alloc");
         WP_CUDA(ctx->d_sim_off.ensure(sizeof(int) * ctx->offsets.size()), "alloc");
         WP_CUDA(ctx->d_sim_cum.ensure(sizeof(double) * cum.size()), "alloc");
@@ -984,6 +1007,8 @@ wp_status sim_device(wp_ctx* ctx, int R, unsigned long long seed, float* d_rads_
     p.rads_d = d_rads_d;
     p.pep = d_pep;
     p.tracks = d_tracks;
+    p.per_peptide = per_peptide;
+    TimedLaunch tl(ctx, 6);
     WP_CUDA(wp_launch_sim_reads(p, ctx->stream), "simulator launch");
     ctx->launches++;
     return WP_OK;
@@ -1060,7 +1085,7 @@ wp_status wp_timing_enable(wp_ctx* ctx, int enable) {
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
     collect_timing(ctx);
-    for (int k = 0; k < 6; k++) {
+    for (int k = 0; k < 8; k++) {
         ctx->t_ms[k] = 0.0;
         ctx->t_n[k] = 0;
     }
@@ -1069,7 +1094,7 @@ wp_status wp_timing_enable(wp_ctx* ctx, int enable) {
 }
 
 wp_status wp_timing_read(wp_ctx* ctx, int kind, double* total_ms, long long* launches) {
-    if (!ctx || kind < 0 || kind > 5) return WP_ERR_INVALID;
+    if (!ctx || kind < 0 || kind > 7) return WP_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
     collect_timing(ctx);
@@ -1619,11 +1644,10 @@ wp_status wp_fit_estep(wp_ctx* ctx, wp_fit_sums* out, double* sum_logp, int* num
     return WP_OK;
 }
 
-wp_status wp_nn_tracks_upload(wp_ctx* ctx, const int16_t* counts, int N, int T, int C, const int32_t* src_off,
-                              const int32_t* src_id, const int32_t* src_count, const int32_t* src_hits) {
-    if (!ctx || N < 0 || (N > 0 && (!counts || !src_off))) return WP_ERR_INVALID;
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    cudaSetDevice(ctx->device);
+// Validates and installs a dye-track set as the kNN training set (caller
+// holds the context lock).
+wp_status nn_install(wp_ctx* ctx, const int16_t* counts, int N, int T, int C, const int32_t* src_off,
+                     const int32_t* src_id, const int32_t* src_count, const int32_t* src_hits) {
     if (C < 1 || C > WP_MAX_CHANNELS || T < 1 || T > WP_MAX_TIMESTEPS)
         return fail(ctx, WP_ERR_UNSUPPORTED, "dye-track shape out of range");
     if (nn_padded_dim(T * C) < 0) return fail(ctx, WP_ERR_UNSUPPORTED, "kNN needs timesteps x channels <= 64");
@@ -1680,6 +1704,224 @@ wp_status wp_nn_tracks_upload(wp_ctx* ctx, const int16_t* counts, int N, int T, 
     ctx->nn_coords_version = -1;
     ctx->nn_pep_version = -1;
     return WP_OK;
+}
+
+wp_status wp_nn_tracks_upload(wp_ctx* ctx, const int16_t* counts, int N, int T, int C, const int32_t* src_off,
+                              const int32_t* src_id, const int32_t* src_count, const int32_t* src_hits) {
+    if (!ctx || N < 0 || (N > 0 && (!counts || !src_off))) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return nn_install(ctx, counts, N, T, C, src_off, src_id, src_count, src_hits);
+}
+
+// ---- dye-track generation and dedup ---------------------------------------
+
+namespace {
+
+int field_bits(int most) {
+    int b = 1;
+    while ((1 << b) <= most) b++;
+    return b;
+}
+
+// Runs the dedup of n instances already on the device (d_dd_in as int16, or
+// in_u8 with per-instance peptide indices) and keeps the result.
+wp_status dedup_run(wp_ctx* ctx, int n, int T, int C, int bits, const uint8_t* in_u8, const int* pep,
+                    bool drop_zero) {
+    const int TC = T * C, k = 64 / bits, W = (TC + k - 1) / k;
+    const size_t nn = (size_t)std::max(n, 1);
+    WP_CUDA(ctx->d_dd_words.ensure(sizeof(uint64_t) * W * nn), "alloc dedup");
+    WP_CUDA(ctx->d_dd_k0.ensure(sizeof(uint64_t) * nn), "alloc dedup");
+    WP_CUDA(ctx->d_dd_k1.ensure(sizeof(uint64_t) * nn), "alloc dedup");
+    for (DevBuf* b : {&ctx->d_dd_p0, &ctx->d_dd_p1, &ctx->d_dd_id, &ctx->d_dd_cnt, &ctx->d_dd_ft, &ctx->d_dd_fs,
+                      &ctx->d_dd_st, &ctx->d_dd_ss, &ctx->d_dd_start, &ctx->d_dd_sid, &ctx->d_dd_scnt,
+                      &ctx->d_dd_hits})
+        WP_CUDA(b->ensure(sizeof(int) * nn), "alloc dedup");
+    WP_CUDA(ctx->d_dd_off.ensure(sizeof(int) * (nn + 1)), "alloc dedup");
+    WP_CUDA(ctx->d_dd_counts.ensure(sizeof(int16_t) * TC * nn), "alloc dedup");
+    WP_CUDA(ctx->d_dd_sizes.ensure(sizeof(int) * 2), "alloc dedup");
+    const size_t tb = wp_dedup_temp_bytes(n);
+    WP_CUDA(ctx->d_dd_temp.ensure(tb), "alloc dedup");
+    ctx->dd_valid = false;
+    int sizes[2] = {0, 0};
+    if (n > 0) {
+        DedupArgs a;
+        memset(&a, 0, sizeof(a));
+        a.n = n;
+        a.TC = TC;
+        a.bits = bits;
+        a.W = W;
+        a.drop_zero = drop_zero ? 1 : 0;
+        a.in_u8 = in_u8;
+        a.in_i16 = in_u8 ? nullptr : ctx->d_dd_in.as<int16_t>();
+        a.pep = pep;
+        a.pep_ids = ctx->d_sim_ids.as<int>();
+        a.pep_cnts = ctx->d_sim_cnts.as<int>();
+        a.inst_id = ctx->d_dd_id.as<int>();
+        a.inst_cnt = ctx->d_dd_cnt.as<int>();
+        a.words = ctx->d_dd_words.as<uint64_t>();
+        a.keys0 = ctx->d_dd_k0.as<uint64_t>();
+        a.keys1 = ctx->d_dd_k1.as<uint64_t>();
+        a.perm0 = ctx->d_dd_p0.as<int>();
+        a.perm1 = ctx->d_dd_p1.as<int>();
+        a.flag_t = ctx->d_dd_ft.as<int>();
+        a.flag_s = ctx->d_dd_fs.as<int>();
+        a.scan_t = ctx->d_dd_st.as<int>();
+        a.scan_s = ctx->d_dd_ss.as<int>();
+        a.start = ctx->d_dd_start.as<int>();
+        a.temp = ctx->d_dd_temp.p;
+        a.temp_bytes = tb;
+        a.out_counts = ctx->d_dd_counts.as<int16_t>();
+        a.out_src_off = ctx->d_dd_off.as<int>();
+        a.out_src_id = ctx->d_dd_sid.as<int>();
+        a.out_src_count = ctx->d_dd_scnt.as<int>();
+        a.out_src_hits = ctx->d_dd_hits.as<int>();
+        a.out_sizes = ctx->d_dd_sizes.as<int>();
+        int nl = 0;
+        {
+            TimedLaunch tl(ctx, 7);
+            WP_CUDA(wp_launch_dedup(a, ctx->stream, &nl), "dedup launch");
+        }
+        ctx->launches += nl;
+        WP_CUDA(cudaMemcpyAsync(sizes, a.out_sizes, sizeof(sizes), cudaMemcpyDeviceToHost, ctx->stream), "copy");
+    } else {
+        WP_CUDA(cudaMemsetAsync(ctx->d_dd_off.p, 0, sizeof(int), ctx->stream), "clear");
+    }
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync dedup");
+    ctx->dd_U = sizes[0];
+    ctx->dd_S = sizes[1];
+    ctx->dd_T = T;
+    ctx->dd_C = C;
+    ctx->dd_valid = true;
+    return WP_OK;
+}
+
+}  // namespace
+
+wp_status wp_dedup_dye_tracks(wp_ctx* ctx, const int16_t* counts, const int32_t* ids, const int32_t* src_counts,
+                              int N, int T, int C, int* out_num_tracks, int* out_num_sources) {
+    if (!ctx || N < 0 || (N > 0 && (!counts || !ids || !src_counts))) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if (C < 1 || C > WP_MAX_CHANNELS || T < 1 || T > WP_MAX_TIMESTEPS)
+        return fail(ctx, WP_ERR_UNSUPPORTED, "dye-track shape out of range");
+    const size_t total = (size_t)N * T * C;
+    const size_t nn = (size_t)std::max(N, 1);
+    WP_CUDA(ctx->d_dd_in.ensure(sizeof(int16_t) * std::max<size_t>(total, 1)), "alloc dedup");
+    WP_CUDA(ctx->d_dd_id.ensure(sizeof(int) * nn), "alloc dedup");
+    WP_CUDA(ctx->d_dd_cnt.ensure(sizeof(int) * nn), "alloc dedup");
+    WP_CUDA(ctx->d_dd_sizes.ensure(sizeof(int) * 2), "alloc dedup");
+    int bits = 1;
+    if (N > 0) {
+        WP_CUDA(cudaMemcpyAsync(ctx->d_dd_in.p, counts, sizeof(int16_t) * total, cudaMemcpyHostToDevice, ctx->stream),
+                "copy");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_dd_id.p, ids, sizeof(int) * N, cudaMemcpyHostToDevice, ctx->stream), "copy");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_dd_cnt.p, src_counts, sizeof(int) * N, cudaMemcpyHostToDevice, ctx->stream),
+                "copy");
+        WP_CUDA(wp_launch_dedup_range(ctx->d_dd_in.as<int16_t>(), total, ctx->d_dd_sizes.as<int>(), ctx->stream),
+                "dedup range");
+        ctx->launches++;
+        int mm[2];
+        WP_CUDA(cudaMemcpyAsync(mm, ctx->d_dd_sizes.p, sizeof(mm), cudaMemcpyDeviceToHost, ctx->stream), "copy");
+        WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        if (mm[0] < 0) return fail(ctx, WP_ERR_INVALID, "negative dye count");
+        bits = field_bits(mm[1]);
+    }
+    wp_status st = dedup_run(ctx, N, T, C, bits, nullptr, nullptr, false);
+    if (st != WP_OK) return st;
+    if (out_num_tracks) *out_num_tracks = ctx->dd_U;
+    if (out_num_sources) *out_num_sources = ctx->dd_S;
+    return WP_OK;
+}
+
+wp_status wp_simulate_dye_tracks(wp_ctx* ctx, int per_peptide, unsigned long long seed, int* out_num_tracks,
+                                 int* out_num_sources, uint8_t* out_instance_tracks, int32_t* out_instance_pep) {
+    if (!ctx || per_peptide < 0) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    wp_status st = check_ready(ctx);
+    if (st != WP_OK) return st;
+    long long copies = 0;
+    for (int i = 0; i < ctx->P; i++) {
+        if (ctx->counts[i] < 0) return fail(ctx, WP_ERR_INVALID, "negative peptide count");
+        copies += ctx->counts[i];
+    }
+    const long long n64 = copies * per_peptide;
+    if (n64 > INT32_MAX) return fail(ctx, WP_ERR_UNSUPPORTED, "more than 2^31-1 dye-tracks to generate");
+    const int n = (int)n64;
+    const int T = ctx->hm.T, C = ctx->hm.C, TC = T * C;
+    if (n > 0) {
+        WP_CUDA(ctx->d_sim_pep.ensure(sizeof(int) * n), "alloc");
+        WP_CUDA(ctx->d_sim_tracks.ensure((size_t)n * TC), "alloc");
+        st = sim_device(ctx, n, seed, nullptr, nullptr, ctx->d_sim_pep.as<int>(), ctx->d_sim_tracks.as<uint8_t>(),
+                        per_peptide);
+        if (st != WP_OK) return st;
+        if (ctx->sim_max_dyes > 255) return fail(ctx, WP_ERR_UNSUPPORTED, "more than 255 dyes of one channel");
+    }
+    st = dedup_run(ctx, n, T, C, field_bits(ctx->sim_max_dyes), ctx->d_sim_tracks.as<uint8_t>(),
+                   ctx->d_sim_pep.as<int>(), true);
+    if (st != WP_OK) return st;
+    if (n > 0 && out_instance_tracks)
+        WP_CUDA(cudaMemcpyAsync(out_instance_tracks, ctx->d_sim_tracks.p, (size_t)n * TC, cudaMemcpyDeviceToHost,
+                                ctx->stream), "copy");
+    if (n > 0 && out_instance_pep)
+        WP_CUDA(cudaMemcpyAsync(out_instance_pep, ctx->d_sim_pep.p, sizeof(int) * n, cudaMemcpyDeviceToHost,
+                                ctx->stream), "copy");
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    if (out_num_tracks) *out_num_tracks = ctx->dd_U;
+    if (out_num_sources) *out_num_sources = ctx->dd_S;
+    return WP_OK;
+}
+
+wp_status wp_dye_tracks_download(wp_ctx* ctx, int16_t* counts, int32_t* src_off, int32_t* src_id,
+                                 int32_t* src_count, int32_t* src_hits) {
+    if (!ctx) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if (!ctx->dd_valid) return fail(ctx, WP_ERR_INVALID, "no dye-track set to download");
+    const int U = ctx->dd_U, S = ctx->dd_S;
+    if (!src_off || (U > 0 && !counts) || (S > 0 && (!src_id || !src_count || !src_hits))) return WP_ERR_INVALID;
+    const size_t TC = (size_t)ctx->dd_T * ctx->dd_C;
+    if (U > 0)
+        WP_CUDA(cudaMemcpyAsync(counts, ctx->d_dd_counts.p, sizeof(int16_t) * TC * U, cudaMemcpyDeviceToHost,
+                                ctx->stream), "copy");
+    WP_CUDA(cudaMemcpyAsync(src_off, ctx->d_dd_off.p, sizeof(int) * (U + 1), cudaMemcpyDeviceToHost, ctx->stream),
+            "copy");
+    if (S > 0) {
+        WP_CUDA(cudaMemcpyAsync(src_id, ctx->d_dd_sid.p, sizeof(int) * S, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+        WP_CUDA(cudaMemcpyAsync(src_count, ctx->d_dd_scnt.p, sizeof(int) * S, cudaMemcpyDeviceToHost, ctx->stream),
+                "copy");
+        WP_CUDA(cudaMemcpyAsync(src_hits, ctx->d_dd_hits.p, sizeof(int) * S, cudaMemcpyDeviceToHost, ctx->stream),
+                "copy");
+    }
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    return WP_OK;
+}
+
+wp_status wp_dye_tracks_to_nn(wp_ctx* ctx) {
+    if (!ctx) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if (!ctx->dd_valid) return fail(ctx, WP_ERR_INVALID, "no dye-track set to install");
+    const int U = ctx->dd_U, S = ctx->dd_S;
+    const size_t TC = (size_t)ctx->dd_T * ctx->dd_C;
+    std::vector<int16_t> counts(std::max<size_t>(TC * U, 1));
+    std::vector<int32_t> off(U + 1), id(std::max(S, 1)), cnt(std::max(S, 1)), hits(std::max(S, 1));
+    if (U > 0)
+        WP_CUDA(cudaMemcpyAsync(counts.data(), ctx->d_dd_counts.p, sizeof(int16_t) * TC * U, cudaMemcpyDeviceToHost,
+                                ctx->stream), "copy");
+    WP_CUDA(cudaMemcpyAsync(off.data(), ctx->d_dd_off.p, sizeof(int) * (U + 1), cudaMemcpyDeviceToHost, ctx->stream),
+            "copy");
+    if (S > 0) {
+        WP_CUDA(cudaMemcpyAsync(id.data(), ctx->d_dd_sid.p, sizeof(int) * S, cudaMemcpyDeviceToHost, ctx->stream),
+                "copy");
+        WP_CUDA(cudaMemcpyAsync(cnt.data(), ctx->d_dd_scnt.p, sizeof(int) * S, cudaMemcpyDeviceToHost, ctx->stream),
+                "copy");
+        WP_CUDA(cudaMemcpyAsync(hits.data(), ctx->d_dd_hits.p, sizeof(int) * S, cudaMemcpyDeviceToHost, ctx->stream),
+                "copy");
+    }
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    return nn_install(ctx, counts.data(), U, ctx->dd_T, ctx->dd_C, off.data(), id.data(), cnt.data(), hits.data());
 }
 
 wp_status wp_nn_classify(wp_ctx* ctx, const double* rads, int R, int k, double sig, int h, int32_t* out_ncand,

@@ -340,4 +340,44 @@ struct SimParams {
     double* rads_d;            // [R][T*C] or null
     int* pep;                  // [R] peptide index or -1
     uint8_t* tracks;           // [R][T*C] or null
+    int per_peptide;           // > 0: instance r is a dye-track of the peptide
+                               // holding copy r / per_peptide (in the order
+                               // of the counts), as generate_dye_tracks
+                               // enumerates them; 0: peptide drawn by count
+};
+
+// ---- dye-track dedup (wp_dedup.cu) ----------------------------------------
+// n dye-track instances are packed into W 64-bit words each, stored word-
+// major ([W][n]): count j of the track (j = t * C + c) is a field of `bits`
+// bits at position j % k of word j / k (k = 64 / bits fields per word, the
+// first field most significant), so that comparing the words in order
+// compares the tracks lexicographically.
+struct DedupArgs {
+    int n, TC, bits, W;
+    int drop_zero;             // leave out the all-zero track
+    const uint8_t* in_u8;      // [n][TC] instance tracks, or
+    const int16_t* in_i16;     // [n][TC] (exactly one of the two)
+    const int* pep;            // [n] peptide index (-1: none), or null when
+    const int* pep_ids;        //     inst_id / inst_cnt are given
+    const int* pep_cnts;
+    int* inst_id;              // [n] source id / count of each instance
+    int* inst_cnt;
+    uint64_t* words;           // [W][n]
+    uint64_t* keys0;           // [n] sort keys (ping-pong)
+    uint64_t* keys1;
+    int* perm0;                // [n] instance order (ping-pong)
+    int* perm1;
+    int* flag_t;               // [n] first instance of a track / of a source
+    int* flag_s;
+    int* scan_t;               // [n] inclusive sums of the flags
+    int* scan_s;
+    int* start;                // [n] first sorted position of each source
+    void* temp;                // CUB scratch
+    size_t temp_bytes;
+    int16_t* out_counts;       // [n][TC] distinct tracks (first U rows)
+    int* out_src_off;          // [n + 1]
+    int* out_src_id;           // [n] (first S entries)
+    int* out_src_count;
+    int* out_src_hits;
+    int* out_sizes;            // [2]: U, S
 };

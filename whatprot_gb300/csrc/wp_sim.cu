@@ -14,6 +14,10 @@
 // Intensities are Normal(adjusted_mu, sigma(adjusted_mu)) per (t, c), with
 // ChannelModel's interactions (channel-model.h:35-70).
 //
+// With per_peptide > 0 the kernel makes the dye-track instances of the kNN
+// training set instead (generate-dye-tracks.cc:32-70): instance r belongs to
+// peptide copy r / per_peptide, and only the tracks are written.
+//
 // The reference draws from std::default_random_engine in a different order,
 // so parity with it is statistical (tests compare distributions).
 #include <cuda_runtime.h>
@@ -48,9 +52,13 @@ __global__ void wp_sim_reads_kernel(SimParams p) {
     if (r >= p.R) return;
     curandStatePhilox4_32_10_t st;
     curand_init(p.seed, (unsigned long long)r, 0ull, &st);
-    // peptide by count weight (upper bound of u * total in the prefix sums)
+    // peptide by count weight (upper bound of u * total in the prefix sums),
+    // or the peptide of copy r / per_peptide: generate_dye_tracks
+    // (generate-dye-tracks.cc:40-47) makes per_peptide tracks for each of
+    // the count copies of every dye-seq, in order
     const double total = p.cum[p.P - 1];
-    const double u = curand_uniform_double(&st) * total;  // (0, total]
+    const double u = p.per_peptide > 0 ? (double)(r / p.per_peptide) + 1.0
+                                       : curand_uniform_double(&st) * total;  // (0, total]
     int lo = 0, hi = p.P - 1;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
@@ -96,8 +104,11 @@ __global__ void wp_sim_reads_kernel(SimParams p) {
     for (int c = 0; c < p.C; c++)
         if (trk[c] != 0) trivial = false;
     p.pep[r] = trivial ? -1 : pep;
-    const DevModel& m = *p.model;
     const int TC = p.T * p.C;
+    if (p.tracks)
+        for (int i = 0; i < TC; i++) p.tracks[r * TC + i] = trk[i];
+    if (!p.rads_f && !p.rads_d) return;  // dye-tracks only
+    const DevModel& m = *p.model;
     for (int t = 0; t < p.T; t++) {
         int cts[WP_MAX_CHANNELS] = {0, 0, 0, 0};
         for (int c = 0; c < p.C; c++) cts[c] = trk[t * p.C + c];
@@ -107,7 +118,6 @@ __global__ void wp_sim_reads_kernel(SimParams p) {
             const double x = mu + sg * curand_normal_double(&st);
             if (p.rads_f) p.rads_f[r * TC + t * p.C + c] = (float)x;
             if (p.rads_d) p.rads_d[r * TC + t * p.C + c] = x;
-            if (p.tracks) p.tracks[r * TC + t * p.C + c] = trk[t * p.C + c];
         }
     }
 }

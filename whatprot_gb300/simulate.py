@@ -151,10 +151,7 @@ def simulate_dye_track_set(model: SequencingModel, dye_seqs: DyeSeqSet, num_time
     """The kNN training set: per_peptide dye-tracks for every peptide (times
     its count), all-zero tracks dropped (generate-dye-tracks.cc:29-70), then
     deduplicated into unique tracks with (id, count, hits) sources
-    (dedup-dye-tracks.cc:44-141).  Tracks come out in lexicographic order of
-    their counts and sources in ascending id (the reference's order is that
-    of its hash maps)."""
-    from .io import DyeTrackSet
+    (dedup_dye_tracks below)."""
     rng = np.random.default_rng(seed)
     C = model.num_channels
     reps = np.repeat(np.arange(len(dye_seqs)), dye_seqs.counts.astype(np.int64) * per_peptide)
@@ -168,7 +165,21 @@ def simulate_dye_track_set(model: SequencingModel, dye_seqs: DyeSeqSet, num_time
     keep = np.any(tracks[:, 0, :] != 0, axis=1)
     tracks = tracks[keep]
     pep = reps[keep]
-    flat = np.ascontiguousarray(tracks.reshape(len(tracks), -1))
+    return dedup_dye_tracks(tracks, dye_seqs.ids[pep], dye_seqs.counts[pep])
+
+
+def dedup_dye_tracks(tracks: np.ndarray, ids: np.ndarray, counts: np.ndarray):
+    """dedup_dye_tracks (dedup-dye-tracks.cc:35-141) on the host: dye-tracks
+    [n, T, C] from sources (ids[i], counts[i]) -> the distinct tracks, each
+    with one (id, count, hits) per distinct source id (count of the id's
+    first instance, hits its number of instances).  Tracks come out in
+    lexicographic order of their counts, sources in ascending id."""
+    from .io import DyeTrackSet
+    n, T, C = tracks.shape
+    if n == 0:
+        return DyeTrackSet(np.zeros((0, T, C), np.int16), np.zeros(1, np.int32), np.zeros(0, np.int32),
+                           np.zeros(0, np.int32), np.zeros(0, np.int32))
+    flat = np.ascontiguousarray(tracks.reshape(n, -1))
     # rows as opaque byte strings: np.unique on them is much faster than
     # axis=0; big-endian int16 bytes sort in the same order as the counts
     # (all counts are non-negative)
@@ -177,20 +188,19 @@ def simulate_dye_track_set(model: SequencingModel, dye_seqs: DyeSeqSet, num_time
     _, first, inv = np.unique(rows, return_index=True, return_inverse=True)
     uniq = flat[first]
     inv = inv.reshape(-1)
-    # hits per (unique track, peptide)
-    key = inv.astype(np.int64) * (len(dye_seqs) + 1) + pep
-    ukey, hits = np.unique(key, return_counts=True)
-    track_of = ukey // (len(dye_seqs) + 1)
-    pep_of = ukey % (len(dye_seqs) + 1)
-    src_off = np.zeros(len(uniq) + 1, np.int32)
-    np.add.at(src_off, track_of + 1, 1)
-    src_off = np.cumsum(src_off).astype(np.int32)
-    order = np.lexsort((dye_seqs.ids[pep_of], track_of))
-    src_id = dye_seqs.ids[pep_of][order].astype(np.int32)
-    src_count = dye_seqs.counts[pep_of][order].astype(np.int32)
-    src_hits = hits[order].astype(np.int32)
-    return DyeTrackSet(uniq.reshape(len(uniq), num_timesteps, C).astype(np.int16), src_off, src_id,
-                       src_count, src_hits)
+    ids = np.asarray(ids, np.int64)
+    # instances by (track, id, instance): runs of one id within a track
+    order = np.lexsort((np.arange(n), ids, inv))
+    inv_s, id_s = inv[order], ids[order]
+    new = np.ones(n, bool)
+    new[1:] = (inv_s[1:] != inv_s[:-1]) | (id_s[1:] != id_s[:-1])
+    starts = np.flatnonzero(new)
+    hits = np.diff(np.append(starts, n))
+    src_off = np.zeros(len(uniq) + 1, np.int64)
+    np.add.at(src_off, inv_s[starts] + 1, 1)
+    return DyeTrackSet(uniq.reshape(len(uniq), T, C).astype(np.int16), np.cumsum(src_off).astype(np.int32),
+                       id_s[starts].astype(np.int32), np.asarray(counts)[order][starts].astype(np.int32),
+                       hits.astype(np.int32))
 
 
 def paper_model(num_channels: int) -> SequencingModel:
