@@ -991,13 +991,19 @@ wp_status sim_device(wp_ctx* ctx, int R, unsigned long long seed, float* d_rads_
     p.P = ctx->P;
     p.R = R;
     p.seed = seed;
-    p.p_edman_failure = ctx->raw_pf;
-    p.p_initial_block = ctx->raw_pib;
-    p.p_cyclic_block = ctx->raw_pcb;
-    for (int t = 0; t < WP_MAX_TIMESTEPS; t++) p.p_detach[t] = ctx->raw_pdet[t];
+    // ceil(p * 2^32) (exact in FP64), 0 for p <= 0, 2^32 for p >= 1
+    auto thr = [](double q) -> unsigned long long {
+        if (!(q > 0.0)) return 0ull;
+        if (q >= 1.0) return 1ull << 32;
+        return (unsigned long long)ceil(q * 4294967296.0);
+    };
+    p.thr_fail = thr(ctx->raw_pf);
+    p.thr_initial_block = thr(ctx->raw_pib);
+    p.thr_cyclic_block = thr(ctx->raw_pcb);
+    for (int t = 0; t < WP_MAX_TIMESTEPS; t++) p.thr_detach[t] = thr(ctx->raw_pdet[t]);
     for (int c = 0; c < WP_MAX_CHANNELS; c++) {
-        p.p_dud[c] = ctx->raw_pdud[c];
-        p.p_bleach[c] = ctx->raw_pbleach[c];
+        p.thr_dud[c] = thr(ctx->raw_pdud[c]);
+        p.thr_bleach[c] = thr(ctx->raw_pbleach[c]);
     }
     p.model = ctx->d_model.as<DevModel>();
     p.seqs = ctx->d_sim_seqs.as<int8_t>();

@@ -326,12 +326,15 @@ struct NNSelectArgs {
 };
 
 // ---- read simulator (wp_sim.cu) -------------------------------------------
+// Event probabilities are 33-bit thresholds: an event with probability p
+// happens when a uniform 32-bit draw u satisfies u < ceil(p * 2^32), i.e.
+// u / 2^32 < p as bernoulli_distribution tests a uniform in [0, 1).
 struct SimParams {
     int T, C, P, R;
     unsigned long long seed;
-    double p_edman_failure, p_initial_block, p_cyclic_block;
-    double p_detach[WP_MAX_TIMESTEPS];
-    double p_dud[WP_MAX_CHANNELS], p_bleach[WP_MAX_CHANNELS];
+    unsigned long long thr_fail, thr_initial_block, thr_cyclic_block;
+    unsigned long long thr_detach[WP_MAX_TIMESTEPS];
+    unsigned long long thr_dud[WP_MAX_CHANNELS], thr_bleach[WP_MAX_CHANNELS];
     const DevModel* model;     // emission model
     const int8_t* seqs;        // ragged dye-seqs (channel or -1)
     const int* offsets;        // [P + 1]

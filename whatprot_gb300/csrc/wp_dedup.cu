@@ -31,20 +31,49 @@
 
 namespace {
 
+// Packs fields into words in track order (field f of word w at bits
+// [64 - bits (f + 1), 64 - bits f)).
+struct FieldPacker {
+    DedupArgs& a;
+    int i, w = 0, f = 0, k;
+    uint64_t word = 0;
+    __device__ FieldPacker(DedupArgs& a_, int i_) : a(a_), i(i_), k(64 / a_.bits) {}
+    __device__ void push(unsigned v) {
+        word |= (uint64_t)v << (64 - a.bits * (f + 1));
+        if (++f == k) flush();
+    }
+    __device__ void flush() {
+        if (f == 0) return;
+        a.words[(size_t)w * a.n + i] = word;
+        w++;
+        f = 0;
+        word = 0;
+    }
+};
+
 template <class In>
 __global__ void dd_pack_kernel(DedupArgs a, const In* tracks) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n) return;
     const In* tr = tracks + (size_t)i * a.TC;
-    const int k = 64 / a.bits;
-    for (int w = 0; w < a.W; w++) {
-        uint64_t word = 0;
-        for (int f = 0; f < k; f++) {
-            const int j = w * k + f;
-            if (j < a.TC) word |= (uint64_t)(uint16_t)tr[j] << (64 - a.bits * (f + 1));
+    FieldPacker fp(a, i);
+    if (((size_t)a.TC * sizeof(In)) % 16 == 0) {
+        // rows start on 16-byte boundaries: 16-byte loads
+        const uint4* v = reinterpret_cast<const uint4*>(tr);
+        constexpr int per = 16 / sizeof(In);
+        for (int q = 0; q < a.TC / per; q++) {
+            const uint4 x = v[q];
+            const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
+            for (int h = 0; h < per; h++) {
+                const uint32_t lane = xs[h * sizeof(In) / 4];
+                const int sh = (h * (int)sizeof(In) * 8) & 31;
+                fp.push((lane >> sh) & (sizeof(In) == 1 ? 0xffu : 0xffffu));
+            }
         }
-        a.words[(size_t)w * a.n + i] = word;
+    } else {
+        for (int j = 0; j < a.TC; j++) fp.push((unsigned)(uint16_t)tr[j]);
     }
+    fp.flush();
     int id;
     if (a.pep) {
         const int p = a.pep[i];
@@ -96,12 +125,29 @@ __global__ void dd_scatter_kernel(DedupArgs a, const int* perm) {
     if (!a.flag_t[i]) return;
     const int u = a.scan_t[i] - 1;
     a.out_src_off[u] = s;
+    // unpack the fields in track order, stored 8 at a time (16 bytes) when
+    // the rows start on 16-byte boundaries
     const int k = 64 / a.bits;
-    const uint64_t mask = (a.bits == 64) ? ~0ull : ((1ull << a.bits) - 1);
+    const uint64_t mask = (1ull << a.bits) - 1;
     int16_t* out = a.out_counts + (size_t)u * a.TC;
+    const bool vec = (a.TC * 2) % 16 == 0;
+    int w = 0, f = 0;
+    uint64_t word = a.words[e];
+    uint32_t pack[4];
     for (int j = 0; j < a.TC; j++) {
-        const uint64_t word = a.words[(size_t)(j / k) * a.n + e];
-        out[j] = (int16_t)((word >> (64 - a.bits * (j % k + 1))) & mask);
+        const uint32_t v = (uint32_t)((word >> (64 - a.bits * (f + 1))) & mask);
+        if (++f == k && j + 1 < a.TC) {
+            f = 0;
+            word = a.words[(size_t)(++w) * a.n + e];
+        }
+        if (vec) {
+            const int h = j & 7;
+            if (h & 1) pack[h >> 1] |= v << 16;
+            else pack[h >> 1] = v;
+            if (h == 7) reinterpret_cast<uint4*>(out)[j >> 3] = make_uint4(pack[0], pack[1], pack[2], pack[3]);
+        } else {
+            out[j] = (int16_t)v;
+        }
     }
 }
 

@@ -12,7 +12,10 @@
 // every remaining dye past the cut.  A read whose timestep-0 counts are all
 // zero is not detectable and gets peptide index -1 (the reference drops it).
 // Intensities are Normal(adjusted_mu, sigma(adjusted_mu)) per (t, c), with
-// ChannelModel's interactions (channel-model.h:35-70).
+// ChannelModel's interactions (channel-model.h:35-70), drawn in FP64 (in
+// FP32 when only FP32 reads are asked for, as for network training).  Each
+// Bernoulli event is one 32-bit draw against a precomputed threshold: the
+// track part of the kernel does no floating-point work.
 //
 // With per_peptide > 0 the kernel makes the dye-track instances of the kNN
 // training set instead (generate-dye-tracks.cc:32-70): instance r belongs to
@@ -47,6 +50,25 @@ __device__ double sim_adjusted_mu(const DevModel& m, int channel, const int* cou
     return amu;
 }
 
+// The same in FP32, for the FP32 reads the proposal network trains on.
+__device__ float sim_adjusted_mu_f(const DevModel& m, int channel, const int* counts) {
+    float amu = (float)m.mu[channel] * (float)counts[channel];
+    for (int c = 0; c < m.C; c++) {
+        const float fi = (float)m.flat[channel][c], ii = (float)m.inter[channel][c];
+        const int n = c == channel ? counts[c] - 1 : counts[c];
+        if (n > 0) {
+            if (fi != 1.0f) amu *= fi;
+            if (ii != 1.0f) amu *= powf(ii, (float)n);
+        }
+    }
+    return amu;
+}
+
+// bernoulli_distribution(p) with p as a 33-bit threshold; no draw for p = 0.
+__device__ __forceinline__ bool sim_event(curandStatePhilox4_32_10_t* st, unsigned long long thr) {
+    return thr != 0ull && (unsigned long long)curand(st) < thr;
+}
+
 __global__ void wp_sim_reads_kernel(SimParams p) {
     const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= p.R) return;
@@ -68,31 +90,32 @@ __global__ void wp_sim_reads_kernel(SimParams p) {
     const int pep = lo;
     const int L = min(p.offsets[pep + 1] - p.offsets[pep], SIM_MAX_LEN);
     int8_t ds[SIM_MAX_LEN];
-    for (int i = 0; i < L; i++) ds[i] = p.seqs[p.offsets[pep] + i];
     // duds
-    for (int i = 0; i < L; i++)
-        if (ds[i] >= 0 && curand_uniform_double(&st) <= p.p_dud[ds[i]]) ds[i] = -1;
     int counts[WP_MAX_CHANNELS] = {0, 0, 0, 0};
-    for (int i = 0; i < L; i++)
-        if (ds[i] >= 0) counts[ds[i]]++;
+    for (int i = 0; i < L; i++) {
+        int8_t d = p.seqs[p.offsets[pep] + i];
+        if (d >= 0 && sim_event(&st, p.thr_dud[d])) d = -1;
+        ds[i] = d;
+        if (d >= 0) counts[d]++;
+    }
     int e = 0;
-    bool block = curand_uniform_double(&st) <= p.p_initial_block;
+    bool block = sim_event(&st, p.thr_initial_block);
     uint8_t trk[WP_MAX_TIMESTEPS * WP_MAX_CHANNELS];
     bool gone = false;
     for (int t = 0; t < p.T; t++) {
         if (!gone && e < L) {
             for (int c = 0; c < p.C; c++) trk[t * p.C + c] = (uint8_t)counts[c];
-            if (curand_uniform_double(&st) <= p.p_cyclic_block) block = true;
-            if (curand_uniform_double(&st) <= p.p_detach[t]) {
+            if (sim_event(&st, p.thr_cyclic_block)) block = true;
+            if (sim_event(&st, p.thr_detach[t])) {
                 gone = true;
                 continue;
             }
-            if (!block && !(curand_uniform_double(&st) <= p.p_edman_failure)) {
+            if (!block && !sim_event(&st, p.thr_fail)) {
                 if (ds[e] >= 0) counts[ds[e]]--;
                 e++;
             }
             for (int i = e; i < L; i++)
-                if (ds[i] >= 0 && curand_uniform_double(&st) <= p.p_bleach[ds[i]]) {
+                if (ds[i] >= 0 && sim_event(&st, p.thr_bleach[ds[i]])) {
                     counts[ds[i]]--;
                     ds[i] = -1;
                 }
@@ -109,15 +132,23 @@ __global__ void wp_sim_reads_kernel(SimParams p) {
         for (int i = 0; i < TC; i++) p.tracks[r * TC + i] = trk[i];
     if (!p.rads_f && !p.rads_d) return;  // dye-tracks only
     const DevModel& m = *p.model;
+    const bool fp32 = !p.rads_d;  // FP32 reads only: FP32 draws
     for (int t = 0; t < p.T; t++) {
         int cts[WP_MAX_CHANNELS] = {0, 0, 0, 0};
         for (int c = 0; c < p.C; c++) cts[c] = trk[t * p.C + c];
         for (int c = 0; c < p.C; c++) {
-            const double mu = sim_adjusted_mu(m, c, cts);
-            const double sg = sqrt(m.bg_sig[c] * m.bg_sig[c] + mu * m.sig[c] * m.sig[c]);
-            const double x = mu + sg * curand_normal_double(&st);
-            if (p.rads_f) p.rads_f[r * TC + t * p.C + c] = (float)x;
-            if (p.rads_d) p.rads_d[r * TC + t * p.C + c] = x;
+            if (fp32) {
+                const float mu = sim_adjusted_mu_f(m, c, cts);
+                const float bg = (float)m.bg_sig[c], sg1 = (float)m.sig[c];
+                const float sg = sqrtf(bg * bg + mu * sg1 * sg1);
+                p.rads_f[r * TC + t * p.C + c] = mu + sg * curand_normal(&st);
+            } else {
+                const double mu = sim_adjusted_mu(m, c, cts);
+                const double sg = sqrt(m.bg_sig[c] * m.bg_sig[c] + mu * m.sig[c] * m.sig[c]);
+                const double x = mu + sg * curand_normal_double(&st);
+                if (p.rads_f) p.rads_f[r * TC + t * p.C + c] = (float)x;
+                p.rads_d[r * TC + t * p.C + c] = x;
+            }
         }
     }
 }
