@@ -1733,8 +1733,13 @@ int field_bits(int most) {
 // Runs the dedup of n instances already on the device (d_dd_in as int16, or
 // in_u8 with per-instance peptide indices) and keeps the result.
 wp_status dedup_run(wp_ctx* ctx, int n, int T, int C, int bits, const uint8_t* in_u8, const int* pep,
-                    bool drop_zero) {
+                    bool drop_zero, long long id_min, long long id_max) {
     const int TC = T * C, k = 64 / bits, W = (TC + k - 1) / k;
+    // fold the id offset into the last word when it fits below the fields
+    const int last_bits = bits * (TC - (W - 1) * k);
+    int id_bits = 0;
+    while (id_bits < 33 && ((id_max - id_min) >> id_bits) != 0) id_bits++;
+    const bool fold = last_bits + id_bits <= 64;
     const size_t nn = (size_t)std::max(n, 1);
     WP_CUDA(ctx->d_dd_words.ensure(sizeof(uint64_t) * W * nn), "alloc dedup");
     WP_CUDA(ctx->d_dd_k0.ensure(sizeof(uint64_t) * nn), "alloc dedup");
@@ -1758,6 +1763,10 @@ wp_status dedup_run(wp_ctx* ctx, int n, int T, int C, int bits, const uint8_t* i
         a.bits = bits;
         a.W = W;
         a.drop_zero = drop_zero ? 1 : 0;
+        a.fold_id = fold ? 1 : 0;
+        a.id_shift = 64 - last_bits - id_bits;
+        a.id_min = id_min;
+        a.last_mask = ~0ull << (64 - last_bits);
         a.in_u8 = in_u8;
         a.in_i16 = in_u8 ? nullptr : ctx->d_dd_in.as<int16_t>();
         a.pep = pep;
@@ -1833,7 +1842,13 @@ wp_status wp_dedup_dye_tracks(wp_ctx* ctx, const int16_t* counts, const int32_t*
         if (mm[0] < 0) return fail(ctx, WP_ERR_INVALID, "negative dye count");
         bits = field_bits(mm[1]);
     }
-    wp_status st = dedup_run(ctx, N, T, C, bits, nullptr, nullptr, false);
+    long long id_min = 0, id_max = 0;
+    if (N > 0) {
+        auto mm = std::minmax_element(ids, ids + N);
+        id_min = *mm.first;
+        id_max = *mm.second;
+    }
+    wp_status st = dedup_run(ctx, N, T, C, bits, nullptr, nullptr, false, id_min, id_max);
     if (st != WP_OK) return st;
     if (out_num_tracks) *out_num_tracks = ctx->dd_U;
     if (out_num_sources) *out_num_sources = ctx->dd_S;
@@ -1864,8 +1879,14 @@ wp_status wp_simulate_dye_tracks(wp_ctx* ctx, int per_peptide, unsigned long lon
         if (st != WP_OK) return st;
         if (ctx->sim_max_dyes > 255) return fail(ctx, WP_ERR_UNSUPPORTED, "more than 255 dyes of one channel");
     }
+    long long id_min = 0, id_max = 0;
+    if (ctx->P > 0) {
+        auto mm = std::minmax_element(ctx->ids.begin(), ctx->ids.end());
+        id_min = *mm.first;
+        id_max = *mm.second;
+    }
     st = dedup_run(ctx, n, T, C, field_bits(ctx->sim_max_dyes), ctx->d_sim_tracks.as<uint8_t>(),
-                   ctx->d_sim_pep.as<int>(), true);
+                   ctx->d_sim_pep.as<int>(), true, id_min, id_max);
     if (st != WP_OK) return st;
     if (n > 0 && out_instance_tracks)
         WP_CUDA(cudaMemcpyAsync(out_instance_tracks, ctx->d_sim_tracks.p, (size_t)n * TC, cudaMemcpyDeviceToHost,

@@ -354,10 +354,16 @@ struct SimParams {
 // major ([W][n]): count j of the track (j = t * C + c) is a field of `bits`
 // bits at position j % k of word j / k (k = 64 / bits fields per word, the
 // first field most significant), so that comparing the words in order
-// compares the tracks lexicographically.
+// compares the tracks lexicographically.  When the source ids span few
+// enough values, their offsets ride in the last word's spare low bits, so
+// that sorting that word also sorts by id.
 struct DedupArgs {
     int n, TC, bits, W;
     int drop_zero;             // leave out the all-zero track
+    int fold_id;               // the source id's offset from id_min sits in
+    int id_shift;              // the last word's spare low bits at id_shift
+    long long id_min;          // (else a separate sort by id)
+    uint64_t last_mask;        // the field bits of the last word
     const uint8_t* in_u8;      // [n][TC] instance tracks, or
     const int16_t* in_i16;     // [n][TC] (exactly one of the two)
     const int* pep;            // [n] peptide index (-1: none), or null when

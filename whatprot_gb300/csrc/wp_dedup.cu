@@ -5,8 +5,9 @@
 //   pack      each instance's T x C counts into W words of `bits`-bit fields,
 //             most significant first (word-major [W][n]), and its source id
 //   sort      stable LSD radix sorts of an instance permutation: by source
-//             id, then by word W-1, ..., word 0 (CUB onesweep), so that the
-//             permutation orders instances by (track, id, instance index)
+//             id (or with the id folded into word W-1), then by word W-1,
+//             ..., word 0 (CUB onesweep), so that the permutation orders
+//             instances by (track, id, instance index)
 //   flag      first sorted instance of each distinct track and of each
 //             (track, id) run; with drop_zero, the all-zero track (the
 //             undetectable instances that generate_dye_tracks drops,
@@ -77,15 +78,23 @@ __global__ void dd_pack_kernel(DedupArgs a, const In* tracks) {
     int id;
     if (a.pep) {
         const int p = a.pep[i];
-        id = p >= 0 ? a.pep_ids[p] : 0;
+        id = p >= 0 ? a.pep_ids[p] : (int)a.id_min;
         a.inst_id[i] = id;
         a.inst_cnt[i] = p >= 0 ? a.pep_cnts[p] : 0;
     } else {
         id = a.inst_id[i];
     }
-    // signed id -> unsigned key of the same order
-    reinterpret_cast<uint32_t*>(a.keys0)[i] = (uint32_t)id ^ 0x80000000u;
+    if (a.fold_id)
+        a.words[(size_t)(a.W - 1) * a.n + i] |= (uint64_t)(uint32_t)((long long)id - a.id_min) << a.id_shift;
+    else  // signed id -> unsigned key of the same order
+        reinterpret_cast<uint32_t*>(a.keys0)[i] = (uint32_t)id ^ 0x80000000u;
     a.perm0[i] = i;
+}
+
+// Word w of instance e without the folded id bits.
+__device__ __forceinline__ uint64_t dd_word(const DedupArgs& a, int w, int e) {
+    const uint64_t x = a.words[(size_t)w * a.n + e];
+    return w == a.W - 1 ? (x & a.last_mask) : x;
 }
 
 __global__ void dd_gather_kernel(const uint64_t* word, const int* perm, uint64_t* keys, int n) {
@@ -99,13 +108,13 @@ __global__ void dd_flag_kernel(DedupArgs a, const int* perm) {
     const int e = perm[i];
     int ft = 0, fs = 0;
     bool drop = a.drop_zero;
-    for (int w = 0; w < a.W && drop; w++) drop = a.words[(size_t)w * a.n + e] == 0;
+    for (int w = 0; w < a.W && drop; w++) drop = dd_word(a, w, e) == 0;
     if (!drop) {
         if (i == 0) {
             ft = fs = 1;
         } else {
             const int pe = perm[i - 1];
-            for (int w = 0; w < a.W && !ft; w++) ft = a.words[(size_t)w * a.n + e] != a.words[(size_t)w * a.n + pe];
+            for (int w = 0; w < a.W && !ft; w++) ft = dd_word(a, w, e) != dd_word(a, w, pe);
             fs = ft || a.inst_id[e] != a.inst_id[pe];
         }
     }
@@ -217,7 +226,7 @@ cudaError_t wp_launch_dedup(const DedupArgs& a, cudaStream_t s, int* launches) {
     int nl = 1;
     size_t tb = a.temp_bytes;
     cub::DoubleBuffer<int> perm(a.perm0, a.perm1);
-    {
+    if (!a.fold_id) {
         cub::DoubleBuffer<uint32_t> k32(reinterpret_cast<uint32_t*>(a.keys0), reinterpret_cast<uint32_t*>(a.keys1));
         e = cub::DeviceRadixSort::SortPairs(a.temp, tb, k32, perm, a.n, 0, 32, s);
         if (e != cudaSuccess) return e;
@@ -228,10 +237,12 @@ cudaError_t wp_launch_dedup(const DedupArgs& a, cudaStream_t s, int* launches) {
         dd_gather_kernel<<<g, T, 0, s>>>(a.words + (size_t)w * a.n, perm.Current(), k64.Current(), a.n);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         nl++;
-        // the fields of a word sit in its top bits; the bits below them are 0
+        // the fields of a word sit in its top bits, then the folded id (last
+        // word); the bits below are 0
         const int nf = std::min(k, a.TC - w * k);
+        const int lo = (a.fold_id && w == a.W - 1) ? a.id_shift : 64 - a.bits * nf;
         tb = a.temp_bytes;
-        e = cub::DeviceRadixSort::SortPairs(a.temp, tb, k64, perm, a.n, 64 - a.bits * nf, 64, s);
+        e = cub::DeviceRadixSort::SortPairs(a.temp, tb, k64, perm, a.n, lo, 64, s);
         if (e != cudaSuccess) return e;
     }
     dd_flag_kernel<<<g, T, 0, s>>>(a, perm.Current());

@@ -69,6 +69,100 @@ __device__ __forceinline__ bool sim_event(curandStatePhilox4_32_10_t* st, unsign
     return thr != 0ull && (unsigned long long)curand(st) < thr;
 }
 
+// generate_dye_track for one instance, every labeled position kept as a bit
+// of a per-channel 64-bit mask of live dyes (at most 64 labeled positions):
+// the live count of a channel is the mask's population, the Edman cut clears
+// the bit of the next labeled position when it reaches it, bleaching draws
+// once per set bit.  Writes the live counts [T][C] to trk.
+__device__ void sim_track_masks(const SimParams& p, curandStatePhilox4_32_10_t* st, const int8_t* seq, int L,
+                                int nlab, uint8_t* trk) {
+    uint8_t lpos[64];
+    uint64_t live[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+    int k = 0;
+    for (int i = 0; i < L; i++) {
+        const int d = seq[i];
+        if (d < 0) continue;
+        lpos[k] = (uint8_t)i;
+        if (!sim_event(st, p.thr_dud[d])) {  // duds
+#pragma unroll
+            for (int c = 0; c < WP_MAX_CHANNELS; c++)
+                if (c == d) live[c] |= 1ull << k;
+        }
+        k++;
+    }
+    int e = 0, nk = 0, npos = nlab > 0 ? lpos[0] : L;
+    bool block = sim_event(st, p.thr_initial_block), gone = false;
+    for (int t = 0; t < p.T; t++) {
+        if (!gone && e < L) {
+#pragma unroll
+            for (int c = 0; c < WP_MAX_CHANNELS; c++)
+                if (c < p.C) trk[t * p.C + c] = (uint8_t)__popcll(live[c]);
+            if (sim_event(st, p.thr_cyclic_block)) block = true;
+            if (sim_event(st, p.thr_detach[t])) {
+                gone = true;
+                continue;
+            }
+            if (!block && !sim_event(st, p.thr_fail)) {
+                if (e == npos) {  // the cut removes the dye at position e
+                    const uint64_t keep = ~(1ull << nk);
+#pragma unroll
+                    for (int c = 0; c < WP_MAX_CHANNELS; c++) live[c] &= keep;
+                    nk++;
+                    npos = nk < nlab ? lpos[nk] : L;
+                }
+                e++;
+            }
+#pragma unroll
+            for (int c = 0; c < WP_MAX_CHANNELS; c++) {  // bleaching past the cut
+                uint64_t m = c < p.C ? live[c] : 0ull;
+                while (m) {
+                    const int b = __ffsll((long long)m) - 1;
+                    m &= m - 1;
+                    if (sim_event(st, p.thr_bleach[c])) live[c] &= ~(1ull << b);
+                }
+            }
+        } else {
+            for (int c = 0; c < p.C; c++) trk[t * p.C + c] = 0;
+        }
+    }
+}
+
+// The same walking every position (any number of labeled positions).
+__device__ void sim_track_positions(const SimParams& p, curandStatePhilox4_32_10_t* st, const int8_t* seq, int L,
+                                    uint8_t* trk) {
+    int8_t ds[SIM_MAX_LEN];
+    int counts[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+    for (int i = 0; i < L; i++) {
+        int8_t d = seq[i];
+        if (d >= 0 && sim_event(st, p.thr_dud[d])) d = -1;  // duds
+        ds[i] = d;
+        if (d >= 0) counts[d]++;
+    }
+    int e = 0;
+    bool block = sim_event(st, p.thr_initial_block), gone = false;
+    for (int t = 0; t < p.T; t++) {
+        if (!gone && e < L) {
+            for (int c = 0; c < p.C; c++) trk[t * p.C + c] = (uint8_t)counts[c];
+            if (sim_event(st, p.thr_cyclic_block)) block = true;
+            if (sim_event(st, p.thr_detach[t])) {
+                gone = true;
+                continue;
+            }
+            if (!block && !sim_event(st, p.thr_fail)) {
+                if (ds[e] >= 0) counts[ds[e]]--;
+                e++;
+            }
+            for (int i = e; i < L; i++)
+                if (ds[i] >= 0 && sim_event(st, p.thr_bleach[ds[i]])) {
+                    counts[ds[i]]--;
+                    ds[i] = -1;
+                }
+        } else {
+            for (int c = 0; c < p.C; c++) trk[t * p.C + c] = 0;
+        }
+    }
+}
+
 __global__ void wp_sim_reads_kernel(SimParams p) {
     const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= p.R) return;
@@ -89,47 +183,25 @@ __global__ void wp_sim_reads_kernel(SimParams p) {
     }
     const int pep = lo;
     const int L = min(p.offsets[pep + 1] - p.offsets[pep], SIM_MAX_LEN);
-    int8_t ds[SIM_MAX_LEN];
-    // duds
-    int counts[WP_MAX_CHANNELS] = {0, 0, 0, 0};
-    for (int i = 0; i < L; i++) {
-        int8_t d = p.seqs[p.offsets[pep] + i];
-        if (d >= 0 && sim_event(&st, p.thr_dud[d])) d = -1;
-        ds[i] = d;
-        if (d >= 0) counts[d]++;
-    }
-    int e = 0;
-    bool block = sim_event(&st, p.thr_initial_block);
-    uint8_t trk[WP_MAX_TIMESTEPS * WP_MAX_CHANNELS];
-    bool gone = false;
-    for (int t = 0; t < p.T; t++) {
-        if (!gone && e < L) {
-            for (int c = 0; c < p.C; c++) trk[t * p.C + c] = (uint8_t)counts[c];
-            if (sim_event(&st, p.thr_cyclic_block)) block = true;
-            if (sim_event(&st, p.thr_detach[t])) {
-                gone = true;
-                continue;
-            }
-            if (!block && !sim_event(&st, p.thr_fail)) {
-                if (ds[e] >= 0) counts[ds[e]]--;
-                e++;
-            }
-            for (int i = e; i < L; i++)
-                if (ds[i] >= 0 && sim_event(&st, p.thr_bleach[ds[i]])) {
-                    counts[ds[i]]--;
-                    ds[i] = -1;
-                }
-        } else {
-            for (int c = 0; c < p.C; c++) trk[t * p.C + c] = 0;
-        }
-    }
+    const int8_t* seq = p.seqs + p.offsets[pep];
+    __align__(16) uint8_t trk[WP_MAX_TIMESTEPS * WP_MAX_CHANNELS];
+    int nlab = 0;
+    for (int i = 0; i < L; i++) nlab += seq[i] >= 0;
+    if (nlab <= 64) sim_track_masks(p, &st, seq, L, nlab, trk);
+    else sim_track_positions(p, &st, seq, L, trk);
     bool trivial = true;
     for (int c = 0; c < p.C; c++)
         if (trk[c] != 0) trivial = false;
     p.pep[r] = trivial ? -1 : pep;
     const int TC = p.T * p.C;
-    if (p.tracks)
-        for (int i = 0; i < TC; i++) p.tracks[r * TC + i] = trk[i];
+    if (p.tracks) {
+        if (TC % 16 == 0) {  // rows on 16-byte boundaries
+            uint4* dst = reinterpret_cast<uint4*>(p.tracks + r * TC);
+            for (int q = 0; q < TC / 16; q++) dst[q] = reinterpret_cast<const uint4*>(trk)[q];
+        } else {
+            for (int i = 0; i < TC; i++) p.tracks[r * TC + i] = trk[i];
+        }
+    }
     if (!p.rads_f && !p.rads_d) return;  // dye-tracks only
     const DevModel& m = *p.model;
     const bool fp32 = !p.rads_d;  // FP32 reads only: FP32 draws
