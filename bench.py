@@ -277,9 +277,9 @@ DT_WORKLOAD = ("simulate dt: the hybrid workload's kNN training set -- 20000 dye
                "generated from the error model and deduplicated into unique tracks with (id, count, hits) sources")
 
 
-def make_tracks_data():
+def make_tracks_data(num=HY_P):
     from whatprot_gb300.simulate import paper_model, random_dye_seqs
-    return paper_model(C), random_dye_seqs(HY_P, C, 8, 30, max_per_channel=5, min_total=1, seed=1234)
+    return paper_model(C), random_dye_seqs(num, C, 8, 30, max_per_channel=5, min_total=1, seed=1234)
 
 
 def cpu_baseline_tracks(sm, ds, seconds_target=15.0):
@@ -325,7 +325,7 @@ def run_tracks(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    sm, ds = make_tracks_data()
+    sm, ds = make_tracks_data(args.dye_seqs)
     n = HY_PER * int(ds.counts.sum())
     ctx = capi.Context(local)
     ctx.upload_model(sm, T)
@@ -368,16 +368,20 @@ def run_tracks(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_step = float(t.item())
     value = n * world / (t_step * 1e-3)
-    # end to end through the public call: generate, dedup and download the set
+    # end to end through the public call: generate, dedup and download the
+    # set into reusable page-locked host buffers
+    bufs = capi.DyeTrackBuffers(n, n, T, C)
+    ctx.simulate_dye_track_set(HY_PER, seed=seed, into=bufs)
     barrier()
     t0 = time.perf_counter()
     for i in range(args.steps):
-        dts = ctx.simulate_dye_track_set(HY_PER, seed=seed + 7 * i)
+        dts = ctx.simulate_dye_track_set(HY_PER, seed=seed + 7 * i, into=bufs)
     e2e_s = (time.perf_counter() - t0) / args.steps
     U, S = len(dts), int(dts.src_off[-1])
     TC = T * C
     e2e = {"value": n * world / e2e_s, "unit": DT_UNIT, "h2d_bytes_per_step": 0,
-           "d2h_bytes_per_step": int(U * TC * 2 + (U + 1) * 4 + 3 * S * 4 + 8)}
+           "d2h_bytes_per_step": int(U * TC * 2 + (U + 1) * 4 + 3 * S * 4 + 8),
+           "host_buffers": "page-locked, reused (capi.DyeTrackBuffers)"}
     # rooflines (HBM): the simulator's algorithmic traffic is its output,
     # n x (T*C track bytes + 4-byte peptide index); the dedup's is one read of
     # the instances (T*C bytes + 4-byte peptide index) and one write of the
@@ -403,7 +407,8 @@ def run_tracks(args):
     line = {"metric": DT_METRIC, "value": value, "unit": DT_UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8/int16 counts, fp64 draws", "data": "synthetic (seeded simulator)",
-            "config": {"workload": DT_WORKLOAD, "peptides": len(ds), "per_peptide": HY_PER, "instances": n,
+            "config": {"workload": DT_WORKLOAD if len(ds) == HY_P else f"{DT_WORKLOAD} (here {len(ds)} dye-seqs)",
+                       "peptides": len(ds), "per_peptide": HY_PER, "instances": n,
                        "unique_tracks": U, "sources": S, "l2": "flushed between steps (512 MB write)"},
             "roofline": {"bound": "hbm", "kernel": phases[dom]["kernel"], "achieved": ach, "peak": peak,
                          "unit": "GB/s", "frac": ach / peak if (ach and peak) else None, "traffic": None,
@@ -1060,6 +1065,8 @@ def main():
     ap.add_argument("--workload", default="classify",
                     choices=["classify", "fit", "hybrid", "learned", "gemm", "tracks"])
     ap.add_argument("--epochs", type=int, default=3)
+    ap.add_argument("--dye-seqs", type=int, default=HY_P,
+                    help="tracks: number of dye-seqs (a smaller case for profiling)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="classify: skip the engine autotuner and use the default launch shapes")
     ap.add_argument("--engine-shape", default=None,

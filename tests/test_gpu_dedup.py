@@ -78,9 +78,12 @@ def test_simulated_set_is_the_dedup_of_its_instances(gpu_ctx, oracle):
     assert np.all(itr[~det] == 0)
     want = oracle.dedup_dye_tracks(itr[det].astype(np.int16), ds.ids[expect[det]], ds.counts[expect[det]])
     assert same_set(dts, want)
-    # same seed, same set; another seed, another set
+    # same seed, same set (also through reusable page-locked buffers);
+    # another seed, another set
     again = gpu_ctx.simulate_dye_track_set(per, seed=77)
     assert same_set(again, dts)
+    bufs = capi.DyeTrackBuffers(n, n, T, 3)
+    assert same_set(gpu_ctx.simulate_dye_track_set(per, seed=77, into=bufs), dts)
     other = gpu_ctx.simulate_dye_track_set(per, seed=78)
     assert not same_set(other, dts)
 

@@ -331,6 +331,33 @@ def emission_mstep(w, x, xx, mu, sig, bg_sig):
     return (np.array(nxt.mu[:C]), np.array(nxt.sig[:C]), np.array(nxt.bg_sig[:C]), step.value)
 
 
+class DyeTrackBuffers:
+    """Reusable host buffers for downloaded dye-track sets, page-locked when
+    torch is importable (device-to-host copies then run at the link's
+    rate): up to max_tracks tracks of T x C counts and max_sources sources."""
+
+    def __init__(self, max_tracks: int, max_sources: int, T: int, C: int, pinned: bool = True):
+        def alloc(n, dtype):
+            if pinned:
+                try:
+                    import torch
+                    tdt = {np.int16: torch.int16, np.int32: torch.int32}[dtype]
+                    return torch.empty(max(n, 1), dtype=tdt, pin_memory=True).numpy()
+                except Exception:
+                    pass
+            return np.zeros(max(n, 1), dtype)
+        self.max_tracks, self.max_sources, self.T, self.C = max_tracks, max_sources, T, C
+        self.counts = alloc(max_tracks * T * C, np.int16)
+        self.off = alloc(max_tracks + 1, np.int32)
+        self.sid, self.scnt, self.shit = (alloc(max_sources, np.int32) for _ in range(3))
+
+    def views(self, U: int, S: int, T: int, C: int):
+        if U > self.max_tracks or S > self.max_sources or (T, C) != (self.T, self.C):
+            raise ValueError("dye-track set larger than the buffers")
+        return (self.counts[: max(U, 1) * T * C].reshape(max(U, 1), T, C), self.off[: U + 1], self.sid,
+                self.scnt, self.shit)
+
+
 class Context:
     """One wp_ctx on one CUDA device (the C ABI's handle)."""
 
@@ -500,13 +527,16 @@ class Context:
         return self._download_dye_tracks(nu.value, ns.value, T, C)
 
     def simulate_dye_track_set(self, per_peptide: int, seed: int = 0, instances: bool = False,
-                               to_nn: bool = False, download: bool = True):
+                               to_nn: bool = False, download: bool = True, into=None):
         """wp_simulate_dye_tracks: the kNN training set of per_peptide
         dye-tracks per peptide copy, generated and deduplicated on the device
         with the uploaded model and peptides.  Returns the io.DyeTrackSet
         (None when download is False), plus the instances (tracks [n, T, C]
         uint8, peptide index [n]) when asked; to_nn makes the set the kNN /
-        hybrid training set without a host round trip of the caller's."""
+        hybrid training set without a host round trip of the caller's.
+        `into` (a DyeTrackBuffers) receives the set in reusable (pinned)
+        host memory; the returned arrays are views of it, valid until its
+        next use."""
         T, C = self.num_timesteps, self.num_channels
         n = int(per_peptide) * int(np.sum(getattr(self, "_pep_counts", np.zeros(0)), dtype=np.int64))
         itr = np.zeros((max(n, 1), T, C), np.uint8) if instances else None
@@ -516,19 +546,22 @@ class Context:
                                                     ctypes.byref(nu), ctypes.byref(ns), _ptr(itr), _ptr(ipep)))
         if to_nn:
             self._check(self.lib.wp_dye_tracks_to_nn(self.h))
-        dts = self._download_dye_tracks(nu.value, ns.value, T, C) if download else None
+        dts = self._download_dye_tracks(nu.value, ns.value, T, C, into) if download else None
         if instances:
             return dts, itr[:n], ipep[:n]
         return dts
 
-    def _download_dye_tracks(self, U: int, S: int, T: int, C: int):
+    def _download_dye_tracks(self, U: int, S: int, T: int, C: int, into=None):
         from .io import DyeTrackSet
-        counts = np.zeros((max(U, 1), T, C), np.int16)
-        off = np.zeros(U + 1, np.int32)
-        sid, scnt, shit = (np.zeros(max(S, 1), np.int32) for _ in range(3))
+        if into is not None:
+            counts, off, sid, scnt, shit = into.views(U, S, T, C)
+        else:
+            counts = np.zeros((max(U, 1), T, C), np.int16)
+            off = np.zeros(U + 1, np.int32)
+            sid, scnt, shit = (np.zeros(max(S, 1), np.int32) for _ in range(3))
         self._check(self.lib.wp_dye_tracks_download(self.h, _ptr(counts), _ptr(off), _ptr(sid), _ptr(scnt),
                                                     _ptr(shit)))
-        return DyeTrackSet(counts[:U], off, sid[:S], scnt[:S], shit[:S])
+        return DyeTrackSet(counts[:U], off[:U + 1], sid[:S], scnt[:S], shit[:S])
 
     def nn_classify(self, rads: np.ndarray, k: int, sig: float, h: int):
         """wp_nn_classify: (ncand [R], ids [R,h], scores [R,h], total [R])."""
