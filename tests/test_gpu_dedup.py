@@ -145,3 +145,26 @@ def test_large_simulated_set_properties(gpu_ctx):
     assert np.all(d[inner] > 0)
     assert int(dts.src_hits.sum()) == int(np.sum(ipep >= 0))
     assert np.all(np.any(dts.tracks[:, 0, :] != 0, axis=1))
+
+
+def test_most_labeled_positions(gpu_ctx, oracle):
+    """A dye-seq with 15 dyes on each of 4 channels (60 labeled positions,
+    the most an uploaded dye-seq carries): mean live counts per (t, c) of the
+    device's instances against the oracle's generator (itself checked
+    against the reference's), within 5 standard errors."""
+    sm = paper_model(4)
+    T, n = 10, 100000
+    seq = np.full(72, -1, np.int16)
+    seq[6:66] = np.arange(60) % 4
+    ds = DyeSeqSet(4, [seq], np.array([1], np.int32), np.array([1], np.int32))
+    gpu_ctx.upload_model(sm, T)
+    gpu_ctx.upload_peptides(ds)
+    _, itr, ipep = gpu_ctx.simulate_dye_track_set(n, seed=31, instances=True)
+    g = itr.astype(np.float64)
+    odts, kept = oracle.simulate_dt(sm, T, ds, n, seed=41)
+    w = odts.src_hits.astype(np.float64)[:, None, None]
+    om = (w * odts.tracks).sum(axis=0) / n
+    ov = (w * odts.tracks.astype(np.float64) ** 2).sum(axis=0) / n - om ** 2
+    se = np.sqrt(g.var(axis=0) / n + ov / n) + 1e-12
+    assert np.all(np.abs(g.mean(axis=0) - om) <= 5 * se), np.max(np.abs(g.mean(axis=0) - om) / se)
+    assert abs(np.mean(ipep >= 0) - kept / n) <= 5 * np.sqrt(0.25 / n) + 1e-4

@@ -70,7 +70,7 @@ __device__ __forceinline__ bool sim_event(curandStatePhilox4_32_10_t* st, unsign
 }
 
 // generate_dye_track for one instance, every labeled position kept as a bit
-// of a per-channel 64-bit mask of live dyes (at most 64 labeled positions):
+// of a per-channel 64-bit mask of live dyes (nlab <= 64 labeled positions):
 // the live count of a channel is the mask's population, the Edman cut clears
 // the bit of the next labeled position when it reaches it, bleaching draws
 // once per set bit.  Writes the live counts [T][C] to trk.
@@ -79,7 +79,7 @@ __device__ void sim_track_masks(const SimParams& p, curandStatePhilox4_32_10_t* 
     uint8_t lpos[64];
     uint64_t live[WP_MAX_CHANNELS] = {0, 0, 0, 0};
     int k = 0;
-    for (int i = 0; i < L; i++) {
+    for (int i = 0; i < L && k < nlab; i++) {
         const int d = seq[i];
         if (d < 0) continue;
         lpos[k] = (uint8_t)i;
@@ -127,42 +127,6 @@ __device__ void sim_track_masks(const SimParams& p, curandStatePhilox4_32_10_t* 
     }
 }
 
-// The same walking every position (any number of labeled positions).
-__device__ void sim_track_positions(const SimParams& p, curandStatePhilox4_32_10_t* st, const int8_t* seq, int L,
-                                    uint8_t* trk) {
-    int8_t ds[SIM_MAX_LEN];
-    int counts[WP_MAX_CHANNELS] = {0, 0, 0, 0};
-    for (int i = 0; i < L; i++) {
-        int8_t d = seq[i];
-        if (d >= 0 && sim_event(st, p.thr_dud[d])) d = -1;  // duds
-        ds[i] = d;
-        if (d >= 0) counts[d]++;
-    }
-    int e = 0;
-    bool block = sim_event(st, p.thr_initial_block), gone = false;
-    for (int t = 0; t < p.T; t++) {
-        if (!gone && e < L) {
-            for (int c = 0; c < p.C; c++) trk[t * p.C + c] = (uint8_t)counts[c];
-            if (sim_event(st, p.thr_cyclic_block)) block = true;
-            if (sim_event(st, p.thr_detach[t])) {
-                gone = true;
-                continue;
-            }
-            if (!block && !sim_event(st, p.thr_fail)) {
-                if (ds[e] >= 0) counts[ds[e]]--;
-                e++;
-            }
-            for (int i = e; i < L; i++)
-                if (ds[i] >= 0 && sim_event(st, p.thr_bleach[ds[i]])) {
-                    counts[ds[i]]--;
-                    ds[i] = -1;
-                }
-        } else {
-            for (int c = 0; c < p.C; c++) trk[t * p.C + c] = 0;
-        }
-    }
-}
-
 __global__ void wp_sim_reads_kernel(SimParams p) {
     const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= p.R) return;
@@ -185,10 +149,11 @@ __global__ void wp_sim_reads_kernel(SimParams p) {
     const int L = min(p.offsets[pep + 1] - p.offsets[pep], SIM_MAX_LEN);
     const int8_t* seq = p.seqs + p.offsets[pep];
     __align__(16) uint8_t trk[WP_MAX_TIMESTEPS * WP_MAX_CHANNELS];
+    // uploaded dye-seqs carry at most 15 dyes on each of at most 4 channels,
+    // so at most 60 labeled positions
     int nlab = 0;
     for (int i = 0; i < L; i++) nlab += seq[i] >= 0;
-    if (nlab <= 64) sim_track_masks(p, &st, seq, L, nlab, trk);
-    else sim_track_positions(p, &st, seq, L, trk);
+    sim_track_masks(p, &st, seq, L, min(nlab, 64), trk);
     bool trivial = true;
     for (int c = 0; c < p.C; c++)
         if (trk[c] != 0) trivial = false;
