@@ -50,6 +50,7 @@ cudaError_t wp_launch_fit_estep(bool has_block, int grid, int threads, cudaStrea
 cudaError_t wp_launch_nn_dist(int DP, bool hist, cudaStream_t s, const NNArgs& a);
 cudaError_t wp_launch_nn_select(int grid, cudaStream_t s, const NNSelectArgs& a);
 cudaError_t wp_launch_nn_threshold(cudaStream_t s, const NNArgs& a);
+cudaError_t wp_launch_nn_estimate(int DP, cudaStream_t s, const NNArgs& a);
 int wp_nn_bins();
 int wp_engine_max_threads();
 cudaError_t wp_launch_sim_reads(const SimParams& p, cudaStream_t s);
@@ -225,13 +226,14 @@ struct wp_ctx {
     long long model_version = 0;
     bool have_tracks = false;
     int nn_N = 0, nn_T = 0, nn_C = 0, nn_U = 0;
+    long long nn_hits_total = 0;
     long long nn_coords_version = -1;
     long long nn_pep_version = -1;
     long long pep_version = 0;
     std::vector<int16_t> nn_counts;
     std::vector<int32_t> nn_src_off, nn_src_id, nn_src_count, nn_src_hits, nn_uniq;
     DevBuf d_nn_coords, d_nn_hits, d_nn_src_off, d_nn_src_dense, d_nn_src_ratio, d_nn_src_hits, d_nn_dense_id,
-            d_nn_dense_pep, d_nn_dense_count, d_nn_queries, d_nn_qbin, d_nn_qbelow, d_nn_qcap, d_nn_qoff,
+            d_nn_dense_pep, d_nn_dense_count, d_nn_queries, d_nn_qbin, d_nn_qbase, d_nn_qbelow, d_nn_qcap, d_nn_qoff,
             d_nn_cidx, d_nn_cd2, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
             d_nn_cand_score, d_nn_total, d_nn_subfrac, d_nn_cand_off, d_nn_cand_flat, d_nn_err, d_nn_shist,
             d_nn_sliceoff, d_nn_slicecap, d_nn_slicecnt;
@@ -743,6 +745,7 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
     const size_t Rz = (size_t)std::max(R, 1);
     WP_CUDA(ctx->d_nn_queries.ensure(sizeof(float) * Rz * DP), "alloc queries");
     WP_CUDA(ctx->d_nn_qbin.ensure(sizeof(int) * Rz), "alloc");
+    WP_CUDA(ctx->d_nn_qbase.ensure(sizeof(int) * Rz), "alloc");
     WP_CUDA(ctx->d_nn_qbelow.ensure(sizeof(int) * Rz), "alloc");
     WP_CUDA(ctx->d_nn_qcap.ensure(sizeof(long long) * Rz), "alloc");
     WP_CUDA(ctx->d_nn_qoff.ensure(sizeof(long long) * Rz), "alloc");
@@ -773,6 +776,10 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
     a.qbelow = ctx->d_nn_qbelow.as<int>();
     a.qcap = ctx->d_nn_qcap.as<long long>();
     a.err = ctx->d_nn_err.as<int>();
+    a.qbase = ctx->d_nn_qbase.as<int>();
+    a.sample_n = std::min(N, 4096);
+    a.sample_stride = N / a.sample_n;
+    a.hits_total = ctx->nn_hits_total;
     // Entry slices: enough CTAs (query blocks x slices) for two waves of
     // three CTAs per SM, each slice at least 1024 entries.
     int sms = 0;
@@ -794,10 +801,16 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
     a.sliceoff = ctx->d_nn_sliceoff.as<long long>();
     a.slicecap = ctx->d_nn_slicecap.as<long long>();
     a.slicecnt = ctx->d_nn_slicecnt.as<long long>();
-    // pass 1 over every read
+    // pass 1 over every read: the bins' origins from a sample, then the
+    // histograms
     a.queries = ctx->d_nn_queries.as<float>();
     a.R = R;
     a.q0 = 0;
+    {
+        TimedLaunch tl(ctx, 4);
+        WP_CUDA(wp_launch_nn_estimate(DP, ctx->stream, a), "kNN estimate");
+        ctx->launches++;
+    }
     {
         TimedLaunch tl(ctx, 4);
         WP_CUDA(wp_launch_nn_dist(DP, true, ctx->stream, a), "kNN histogram");
@@ -857,6 +870,7 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
         b.R = nq;
         b.q0 = r0;
         b.qbin = a.qbin;
+        b.qbase = a.qbase;
         b.qbelow = a.qbelow;
         b.slices = a.slices;
         b.R_all = R;
@@ -1671,6 +1685,8 @@ wp_status nn_install(wp_ctx* ctx, const int16_t* counts, int N, int T, int C, co
         if (hsum < 1 || hsum > INT32_MAX) return fail(ctx, WP_ERR_INVALID, "every dye-track needs 1..2^31-1 hits");
         ehits[e] = (int)hsum;
     }
+    ctx->nn_hits_total = 0;
+    for (int e = 0; e < N; e++) ctx->nn_hits_total += ehits[e];
     ctx->nn_counts.assign(counts, counts + (size_t)N * T * C);
     ctx->nn_src_off.assign(src_off, src_off + (N > 0 ? N + 1 : 0));
     ctx->nn_src_id.assign(src_id, src_id + S);

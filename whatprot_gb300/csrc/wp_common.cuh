@@ -287,12 +287,17 @@ struct NNArgs {
     long long* sliceoff;    // [slices][R_all] offset of slice s inside query q's list
     long long* slicecap;    // [slices][R_all] room for slice s (its hits in bins <= b*)
     long long* slicecnt;    // [slices][R_all] candidates slice s wrote
+    int* qbase;             // [R_all] per query: float bits >> 19 where its bin 1 starts
+    int sample_stride;      // the estimate samples entries 0, stride, 2 stride, ...
+    int sample_n;
+    long long hits_total;   // hits over all entries
 };
 
 struct NNSelectArgs {
     int R;                      // queries in this chunk
     int q0;
     const int* qbin;
+    const int* qbase;           // per query bin origin (as NNArgs)
     const int* qbelow;
     int slices;
     int R_all;

@@ -4,10 +4,12 @@
 // The reference searches a kd-tree for the entries (unique dye-tracks) whose
 // simulated hits add up to k, weights each by exp(-d^2 / 2 sig^2) and scores
 // every source peptide id.  Here the search is brute force, as a tiled FP32
-// contraction of queries against all entries, in three kernels:
+// contraction of queries against all entries, in four kernels:
 //
+//   wp_nn_estimate_kernel distances to a sample of the entries place each
+//                         query's distance bins around its k-hit radius
 //   wp_nn_hist_kernel     every (query, entry) squared distance, binned on a
-//                         log scale (4 bins per octave); per query a histogram
+//                         log scale (16 bins per octave); per query a histogram
 //                         of hits per bin gives the bin b* where the running
 //                         hits reach k, the hits below it and an upper bound
 //                         on the entries at or below it.
@@ -39,11 +41,21 @@
 #define NN_SEL_WARPS 4     // warps per CTA in the select kernel
 #define NN_HMAX 1024       // largest h
 
-// Log-scale bin of a squared distance: bin 1 starts at 2^-6, four bins per
-// octave (the exponent and the top two mantissa bits of the float), bin 0
-// below, bin NB-1 open-ended.  Monotone in d2.
-__device__ __forceinline__ int nn_bin(float d2) {
+// Coarse log-scale bin of a squared distance, for the estimate: bin 1
+// starts at 2^-6, four bins per octave (the exponent and the top two
+// mantissa bits of the float), bin 0 below, bin NB-1 open-ended.
+__device__ __forceinline__ int nn_coarse_bin(float d2) {
     const int b = (int)(__float_as_uint(d2) >> 21) - ((127 - 6) << 2) + 1;
+    return b < 0 ? 0 : (b > NN_NB - 1 ? NN_NB - 1 : b);
+}
+
+// Fine bin of a squared distance for one query: sixteen bins per octave
+// (exponent and top four mantissa bits), bin 1 starting at the query's
+// origin `base` (in units of float bits >> 19), bin 0 below, bin NB-1
+// open-ended: 62 fine bins span almost four octaves around the query's
+// estimated k-hit radius.  Monotone in d2.
+__device__ __forceinline__ int nn_bin(float d2, int base) {
+    const int b = (int)(__float_as_uint(d2) >> 19) - base + 1;
     return b < 0 ? 0 : (b > NN_NB - 1 ? NN_NB - 1 : b);
 }
 
@@ -88,6 +100,7 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
     for (int i = threadIdx.x; i < NN_QPB * (NN_NB + 1); i += blockDim.x) hist[i] = 0u;
     float q[NN_QPT][DP];
     bool valid[NN_QPT];
+    int base[NN_QPT];
 #pragma unroll
     for (int j = 0; j < NN_QPT; j++) {
         const int lq = threadIdx.x + j * NN_THREADS;
@@ -95,6 +108,7 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
         const float* src = a.queries + (long)(valid[j] ? qb + lq : 0) * DP;
 #pragma unroll
         for (int i = 0; i < DP; i++) q[j][i] = valid[j] ? src[i] : 0.f;
+        base[j] = valid[j] ? a.qbase[a.q0 + qb + lq] : 0;
     }
     for (int e0 = e_lo; e0 < e_hi; e0 += NN_TE) {
         __syncthreads();
@@ -106,7 +120,8 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
             for (int j = 0; j < NN_QPT; j++) {
                 const float d2 = nn_d2<DP>(q[j], tile + e * DP);
                 if (valid[j])
-                    atomicAdd(&hist[(threadIdx.x + j * NN_THREADS) * (NN_NB + 1) + nn_bin(d2)], (unsigned)thits[e]);
+                    atomicAdd(&hist[(threadIdx.x + j * NN_THREADS) * (NN_NB + 1) + nn_bin(d2, base[j])],
+                              (unsigned)thits[e]);
             }
         }
     }
@@ -116,6 +131,74 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
         const int lq = i / NN_NB, b = i % NN_NB;
         if (qb + lq < a.R)
             a.shist[((long)s * a.R_all + a.q0 + qb + lq) * NN_NB + b] = hist[lq * (NN_NB + 1) + b];
+    }
+}
+
+// Per query: where its k-hit radius lies, from a sample of the entries
+// (every sample_stride-th): a coarse histogram of the sample's hits, the
+// coarse bin where the running sample hits reach k x (sample hits / all
+// hits), and the fine-bin origin two octaves below that bin's start.  Only
+// the bins move with the estimate; the selection stays exact whatever it
+// says (a poor estimate only leaves more candidates).
+template <int DP>
+__global__ void __launch_bounds__(NN_THREADS) wp_nn_estimate_kernel(NNArgs a) {
+    extern __shared__ __align__(16) unsigned char nn_smem[];
+    float* tile = reinterpret_cast<float*>(nn_smem);
+    int* thits = reinterpret_cast<int*>(tile + NN_TE * DP);
+    unsigned* hist = reinterpret_cast<unsigned*>(thits + NN_TE);  // [NN_QPB][NN_NB + 1]
+    const int qb = blockIdx.x * NN_QPB;
+    for (int i = threadIdx.x; i < NN_QPB * (NN_NB + 1); i += blockDim.x) hist[i] = 0u;
+    float q[NN_QPT][DP];
+    bool valid[NN_QPT];
+#pragma unroll
+    for (int j = 0; j < NN_QPT; j++) {
+        const int lq = threadIdx.x + j * NN_THREADS;
+        valid[j] = qb + lq < a.R;
+        const float* src = a.queries + (long)(valid[j] ? qb + lq : 0) * DP;
+#pragma unroll
+        for (int i = 0; i < DP; i++) q[j][i] = valid[j] ? src[i] : 0.f;
+    }
+    long long hs = 0;  // the sample's hits
+    for (int s0 = 0; s0 < a.sample_n; s0 += NN_TE) {
+        __syncthreads();
+        const int n = min(NN_TE, a.sample_n - s0);
+        for (int i = threadIdx.x; i < NN_TE * DP / 4; i += blockDim.x) {
+            const int e = i / (DP / 4), part = i % (DP / 4);
+            reinterpret_cast<float4*>(tile)[i] =
+                e < n ? reinterpret_cast<const float4*>(a.coords + (long)(s0 + e) * a.sample_stride * DP)[part]
+                      : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        for (int i = threadIdx.x; i < NN_TE; i += blockDim.x)
+            thits[i] = i < n ? a.hits[(long)(s0 + i) * a.sample_stride] : 0;
+        __syncthreads();
+        for (int e = 0; e < n; e++) {
+            hs += thits[e];
+#pragma unroll
+            for (int j = 0; j < NN_QPT; j++) {
+                const float d2 = nn_d2<DP>(q[j], tile + e * DP);
+                if (valid[j])
+                    atomicAdd(&hist[(threadIdx.x + j * NN_THREADS) * (NN_NB + 1) + nn_coarse_bin(d2)],
+                              (unsigned)thits[e]);
+            }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NN_QPT; j++) {
+        if (!valid[j]) continue;
+        const unsigned* h = hist + (threadIdx.x + j * NN_THREADS) * (NN_NB + 1);
+        long long run = 0;
+        int b = NN_NB - 1;
+        for (int i = 0; i < NN_NB; i++) {
+            run += h[i];
+            if (run * a.hits_total >= a.k * hs) {
+                b = i;
+                break;
+            }
+        }
+        // coarse bin b starts at float bits >> 21 == b - 1 + ((127 - 6) << 2)
+        const int ck = b - 1 + ((127 - 6) << 2);
+        a.qbase[a.q0 + qb + threadIdx.x + j * NN_THREADS] = 4 * ck - 32;
     }
 }
 
@@ -170,7 +253,7 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
     const int e_lo = s * a.slice_len, e_hi = min(a.N, e_lo + a.slice_len);
     float q[NN_QPT][DP];
     bool valid[NN_QPT];
-    int bstar[NN_QPT];
+    int bstar[NN_QPT], base[NN_QPT];
     long long off[NN_QPT], cap[NN_QPT], cnt[NN_QPT];
 #pragma unroll
     for (int j = 0; j < NN_QPT; j++) {
@@ -182,6 +265,7 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
 #pragma unroll
         for (int i = 0; i < DP; i++) q[j][i] = valid[j] ? src[i] : 0.f;
         bstar[j] = valid[j] ? a.qbin[gq] : -1;
+        base[j] = valid[j] ? a.qbase[gq] : 0;
         off[j] = valid[j] ? a.qoff[l] + a.sliceoff[(long)s * a.R_all + gq] : 0;
         cap[j] = valid[j] ? a.slicecap[(long)s * a.R_all + gq] : 0;
         cnt[j] = 0;
@@ -195,7 +279,7 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
 #pragma unroll
             for (int j = 0; j < NN_QPT; j++) {
                 const float d2 = nn_d2<DP>(q[j], tile + e * DP);
-                if (nn_bin(d2) <= bstar[j]) {
+                if (nn_bin(d2, base[j]) <= bstar[j]) {
                     if (cnt[j] < cap[j]) {
                         a.cand_idx[off[j] + cnt[j]] = e0 + e;
                         a.cand_d2[off[j] + cnt[j]] = d2;
@@ -246,7 +330,7 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
 
     for (long lq = gw; lq < a.R; lq += nw) {
         const int gq = a.q0 + (int)lq;
-        const int bstar = a.qbin[gq];
+        const int bstar = a.qbin[gq], base = a.qbase[gq];
         long long need = a.k - a.qbelow[gq];  // hits still needed from bin b*
         // The query's candidates: one segment per entry slice, in slice
         // order (so in ascending entry index overall).
@@ -264,7 +348,7 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
                 for (long long i = lane; i < sn; i += 32) {
                     const float d2 = a.cand_d2[sb + i];
                     const unsigned key = __float_as_uint(d2);
-                    if (nn_bin(d2) == bstar && (key & pmask) == prefix)
+                    if (nn_bin(d2, base) == bstar && (key & pmask) == prefix)
                         atomicAdd(&hist[(key >> shift) & 255u], (unsigned long long)a.hits[a.cand_idx[sb + i]]);
                 }
             }
@@ -321,7 +405,7 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
             if (i < sn) {
                 e = a.cand_idx[sb + i];
                 d2 = a.cand_d2[sb + i];
-                const int b = nn_bin(d2);
+                const int b = nn_bin(d2, base);
                 const unsigned key = __float_as_uint(d2);
                 if (b < bstar || take_all) keep = true;
                 else if (key < kstar) keep = true;
@@ -611,6 +695,28 @@ cudaError_t wp_launch_nn_dist(int DP, bool hist, cudaStream_t s, const NNArgs& a
         case 32: return launch_dist<32>(hist, grid, s, a);
         case 48: return launch_dist<48>(hist, grid, s, a);
         case 64: return launch_dist<64>(hist, grid, s, a);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int DP>
+static cudaError_t launch_estimate(dim3 grid, cudaStream_t s, const NNArgs& a) {
+    const size_t smem = wp_nn_dist_smem_bytes(DP, true);
+    cudaFuncSetAttribute(wp_nn_estimate_kernel<DP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    wp_nn_estimate_kernel<DP><<<grid, NN_THREADS, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+// The per-query bin origins (a.qbase) from a.sample_n sampled entries.
+cudaError_t wp_launch_nn_estimate(int DP, cudaStream_t s, const NNArgs& a) {
+    const int qblocks = (a.R + NN_QPB - 1) / NN_QPB;
+    if (qblocks == 0) return cudaSuccess;
+    const dim3 grid(qblocks);
+    switch (DP) {
+        case 16: return launch_estimate<16>(grid, s, a);
+        case 32: return launch_estimate<32>(grid, s, a);
+        case 48: return launch_estimate<48>(grid, s, a);
+        case 64: return launch_estimate<64>(grid, s, a);
         default: return cudaErrorInvalidValue;
     }
 }
