@@ -227,13 +227,14 @@ struct wp_ctx {
     bool have_tracks = false;
     int nn_N = 0, nn_T = 0, nn_C = 0, nn_U = 0;
     long long nn_hits_total = 0;
+    int nn_sample_n = 0;  // entries sampled in proportion to their hits (d_nn_sample)
     long long nn_coords_version = -1;
     long long nn_pep_version = -1;
     long long pep_version = 0;
     std::vector<int16_t> nn_counts;
     std::vector<int32_t> nn_src_off, nn_src_id, nn_src_count, nn_src_hits, nn_uniq;
     DevBuf d_nn_coords, d_nn_hits, d_nn_src_off, d_nn_src_dense, d_nn_src_ratio, d_nn_src_hits, d_nn_dense_id,
-            d_nn_dense_pep, d_nn_dense_count, d_nn_queries, d_nn_qbin, d_nn_qbase, d_nn_qbelow, d_nn_qcap, d_nn_qoff,
+            d_nn_dense_pep, d_nn_dense_count, d_nn_queries, d_nn_qbin, d_nn_qbase, d_nn_sample, d_nn_qbelow, d_nn_qcap, d_nn_qoff,
             d_nn_cidx, d_nn_cd2, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
             d_nn_cand_score, d_nn_total, d_nn_subfrac, d_nn_cand_off, d_nn_cand_flat, d_nn_err, d_nn_shist,
             d_nn_sliceoff, d_nn_slicecap, d_nn_slicecnt;
@@ -777,8 +778,8 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
     a.qcap = ctx->d_nn_qcap.as<long long>();
     a.err = ctx->d_nn_err.as<int>();
     a.qbase = ctx->d_nn_qbase.as<int>();
-    a.sample_n = std::min(N, 4096);
-    a.sample_stride = N / a.sample_n;
+    a.sample = ctx->d_nn_sample.as<int>();
+    a.sample_n = ctx->nn_sample_n;
     a.hits_total = ctx->nn_hits_total;
     // Entry slices: enough CTAs (query blocks x slices) for two waves of
     // three CTAs per SM, each slice at least 1024 entries.
@@ -1687,6 +1688,26 @@ wp_status nn_install(wp_ctx* ctx, const int16_t* counts, int N, int T, int C, co
     }
     ctx->nn_hits_total = 0;
     for (int e = 0; e < N; e++) ctx->nn_hits_total += ehits[e];
+    // 4096 entries by systematic sampling of the cumulative hits (the
+    // midpoint of each of 4096 equal shares): each stands for the same
+    // number of hits, so the kNN search can estimate each read's k-hit
+    // radius from them
+    {
+        const int S = N > 0 ? 4096 : 0;
+        std::vector<int> sample(std::max(S, 1), 0);
+        long long cum = 0;
+        int e = 0;
+        for (int j = 0; j < S; j++) {
+            const long long target = ((2ll * j + 1) * ctx->nn_hits_total) / (2ll * S);
+            while (e < N - 1 && cum + ehits[e] <= target) cum += ehits[e++];
+            sample[j] = e;
+        }
+        WP_CUDA(ctx->d_nn_sample.ensure(sizeof(int) * sample.size()), "alloc");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_sample.p, sample.data(), sizeof(int) * sample.size(),
+                                cudaMemcpyHostToDevice, ctx->stream), "copy");
+        WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        ctx->nn_sample_n = S;
+    }
     ctx->nn_counts.assign(counts, counts + (size_t)N * T * C);
     ctx->nn_src_off.assign(src_off, src_off + (N > 0 ? N + 1 : 0));
     ctx->nn_src_id.assign(src_id, src_id + S);

@@ -135,11 +135,14 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
 }
 
 // Per query: where its k-hit radius lies, from a sample of the entries
-// (every sample_stride-th): a coarse histogram of the sample's hits, the
-// coarse bin where the running sample hits reach k x (sample hits / all
-// hits), and the fine-bin origin two octaves below that bin's start.  Only
-// the bins move with the estimate; the selection stays exact whatever it
-// says (a poor estimate only leaves more candidates).
+// drawn in proportion to their hits (systematic sampling of the cumulative
+// hits, so each sample point stands for the same number of hits): the
+// k-hit radius is the k / (all hits) quantile of the hits-weighted
+// distances, estimated by the sample's ceil(k x sample_n / all hits)-th
+// nearest point (binned coarsely); the query's fine bins start two octaves
+// below that coarse bin.  Only the bins move with the estimate; the
+// selection stays exact whatever it says (a poor estimate only leaves more
+// candidates).
 template <int DP>
 __global__ void __launch_bounds__(NN_THREADS) wp_nn_estimate_kernel(NNArgs a) {
     extern __shared__ __align__(16) unsigned char nn_smem[];
@@ -158,31 +161,27 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_estimate_kernel(NNArgs a) {
 #pragma unroll
         for (int i = 0; i < DP; i++) q[j][i] = valid[j] ? src[i] : 0.f;
     }
-    long long hs = 0;  // the sample's hits
     for (int s0 = 0; s0 < a.sample_n; s0 += NN_TE) {
         __syncthreads();
         const int n = min(NN_TE, a.sample_n - s0);
         for (int i = threadIdx.x; i < NN_TE * DP / 4; i += blockDim.x) {
             const int e = i / (DP / 4), part = i % (DP / 4);
             reinterpret_cast<float4*>(tile)[i] =
-                e < n ? reinterpret_cast<const float4*>(a.coords + (long)(s0 + e) * a.sample_stride * DP)[part]
+                e < n ? reinterpret_cast<const float4*>(a.coords + (long)a.sample[s0 + e] * DP)[part]
                       : make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        for (int i = threadIdx.x; i < NN_TE; i += blockDim.x)
-            thits[i] = i < n ? a.hits[(long)(s0 + i) * a.sample_stride] : 0;
         __syncthreads();
         for (int e = 0; e < n; e++) {
-            hs += thits[e];
 #pragma unroll
             for (int j = 0; j < NN_QPT; j++) {
                 const float d2 = nn_d2<DP>(q[j], tile + e * DP);
-                if (valid[j])
-                    atomicAdd(&hist[(threadIdx.x + j * NN_THREADS) * (NN_NB + 1) + nn_coarse_bin(d2)],
-                              (unsigned)thits[e]);
+                if (valid[j]) atomicAdd(&hist[(threadIdx.x + j * NN_THREADS) * (NN_NB + 1) + nn_coarse_bin(d2)], 1u);
             }
         }
     }
     __syncthreads();
+    // the sample point that stands for the k-th hit
+    const long long kth = (a.k * a.sample_n + a.hits_total - 1) / a.hits_total;
 #pragma unroll
     for (int j = 0; j < NN_QPT; j++) {
         if (!valid[j]) continue;
@@ -191,7 +190,7 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_estimate_kernel(NNArgs a) {
         int b = NN_NB - 1;
         for (int i = 0; i < NN_NB; i++) {
             run += h[i];
-            if (run * a.hits_total >= a.k * hs) {
+            if (run >= kth) {
                 b = i;
                 break;
             }
