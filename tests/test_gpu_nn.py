@@ -194,3 +194,17 @@ def test_nn_errors(gpu_ctx):
         assert np.all(nc == 0) and np.all(tot == 0.0)
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("which", ["k1", "k_all_but_one"])
+def test_nn_threshold_extremes(gpu_ctx, oracle, which):
+    """k = 1 (the k-hit radius is the nearest entry's) and k one below every
+    hit (the radius is the farthest entry's): the reads' distance bins sit
+    at the edges of their estimated windows, the selection stays exact."""
+    sm, ds, dts, rads, _ = _data(2, 8, 40, 30, 80, seed=444)
+    gpu_ctx.upload_model(sm, 8)
+    gpu_ctx.upload_tracks(dts)
+    k = 1 if which == "k1" else int(dts.src_hits.sum()) - 1
+    g = gpu_ctx.nn_classify(rads, k, 0.5, 10)
+    o = oracle.nn_classify(sm, 8, dts, rads, k, 0.5, 10)
+    _compare(g, o, f"kNN k={k}")
