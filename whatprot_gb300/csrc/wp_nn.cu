@@ -426,16 +426,33 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
             }
             const int s0 = keep ? a.src_off[e] : 0;
             const int ns = keep ? a.src_off[e + 1] - s0 : 0;
-            int nmax = ns;
-            for (int o = 16; o > 0; o >>= 1) nmax = max(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
-            for (int s = 0; s < nmax; s++) {
-                const bool act = s < ns;
+            // the kept entries' sources, flattened over the warp: source j of
+            // this batch belongs to the first lane whose inclusive prefix of
+            // source counts exceeds j (a popular track's many sources no
+            // longer hold the other lanes idle)
+            int pre = ns;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, pre, o);
+                if (lane >= o) pre += t;
+            }
+            const int nsrc = __shfl_sync(0xffffffffu, pre, 31);
+            const int excl = pre - ns;
+            for (int j0 = 0; j0 < nsrc; j0 += 32) {
+                const int j = j0 + lane;
+                const bool act = j < nsrc;
+                int L = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (__shfl_sync(0xffffffffu, pre, L + step - 1) <= j) L += step;
+                const int sL = __shfl_sync(0xffffffffu, s0, L) + j - __shfl_sync(0xffffffffu, excl, L);
+                const double wL = __shfl_sync(0xffffffffu, w, L);
                 int id = -1;
                 double val = 0.0;
                 if (act) {
-                    id = a.src_dense[s0 + s];
-                    val = w * a.src_ratio[s0 + s];
-                    total_part += w * (double)a.src_hits[s0 + s];
+                    id = a.src_dense[sL];
+                    val = wL * a.src_ratio[sL];
+                    total_part += wL * (double)a.src_hits[sL];
                 }
                 const unsigned actm = __ballot_sync(0xffffffffu, act);
                 if (actm == 0u) continue;
