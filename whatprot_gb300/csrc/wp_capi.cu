@@ -235,7 +235,7 @@ struct wp_ctx {
     std::vector<int32_t> nn_src_off, nn_src_id, nn_src_count, nn_src_hits, nn_uniq;
     DevBuf d_nn_coords, d_nn_hits, d_nn_src_off, d_nn_src_dense, d_nn_src_ratio, d_nn_src_hits, d_nn_dense_id,
             d_nn_dense_pep, d_nn_dense_count, d_nn_queries, d_nn_qbin, d_nn_qbase, d_nn_sample, d_nn_qbelow, d_nn_qcap, d_nn_qoff,
-            d_nn_cidx, d_nn_cd2, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
+            d_nn_cidx, d_nn_cd2, d_nn_chits, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
             d_nn_cand_score, d_nn_total, d_nn_subfrac, d_nn_cand_off, d_nn_cand_flat, d_nn_err, d_nn_shist,
             d_nn_sliceoff, d_nn_slicecap, d_nn_slicecnt;
 
@@ -853,6 +853,7 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
         const int nq = r1 - r0;
         WP_CUDA(ctx->d_nn_cidx.ensure(sizeof(int) * std::max<long long>(tot, 1)), "alloc kNN candidates");
         WP_CUDA(ctx->d_nn_cd2.ensure(sizeof(float) * std::max<long long>(tot, 1)), "alloc kNN candidates");
+        WP_CUDA(ctx->d_nn_chits.ensure(sizeof(int) * std::max<long long>(tot, 1)), "alloc kNN candidates");
         WP_CUDA(cudaMemcpyAsync(ctx->d_nn_qoff.p, off.data(), sizeof(long long) * nq, cudaMemcpyHostToDevice,
                                 ctx->stream), "copy offsets");
         a.queries = ctx->d_nn_queries.as<float>() + (size_t)r0 * DP;
@@ -861,6 +862,7 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
         a.qoff = ctx->d_nn_qoff.as<long long>();
         a.cand_idx = ctx->d_nn_cidx.as<int>();
         a.cand_d2 = ctx->d_nn_cd2.as<float>();
+        a.cand_hits = ctx->d_nn_chits.as<int>();
         {
             TimedLaunch tl(ctx, 4);
             WP_CUDA(wp_launch_nn_dist(DP, false, ctx->stream, a), "kNN collect");
@@ -881,6 +883,7 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
         b.qoff = a.qoff;
         b.cand_idx = a.cand_idx;
         b.cand_d2 = a.cand_d2;
+        b.cand_hits = a.cand_hits;
         b.hits = a.hits;
         b.src_off = ctx->d_nn_src_off.as<int>();
         b.src_dense = ctx->d_nn_src_dense.as<int>();

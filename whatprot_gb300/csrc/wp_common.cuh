@@ -279,6 +279,7 @@ struct NNArgs {
     const long long* qoff;  // candidate list offset (chunk-relative)
     int* cand_idx;
     float* cand_d2;
+    int* cand_hits;         // the entry's hits, next to its index
     int* err;
     int slices;             // entry slices (blockIdx.y)
     int slice_len;
@@ -307,6 +308,7 @@ struct NNSelectArgs {
     const long long* qoff;
     const int* cand_idx;
     const float* cand_d2;
+    const int* cand_hits;
     const int* hits;            // [N]
     const int* src_off;         // [N + 1]
     const int* src_dense;       // [S] dense id

@@ -282,6 +282,7 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
                     if (cnt[j] < cap[j]) {
                         a.cand_idx[off[j] + cnt[j]] = e0 + e;
                         a.cand_d2[off[j] + cnt[j]] = d2;
+                        a.cand_hits[off[j] + cnt[j]] = thits[e];
                     } else {
                         atomicExch(a.err, 1);
                     }
@@ -312,6 +313,35 @@ __device__ __forceinline__ long long warp_incl_scan(long long v) {
     return v;
 }
 
+// Radix-select step over a warp's 256-digit histogram, counting from digit
+// 255 down: the digit where the running count reaches `want`; *before gets
+// the count of the digits above it.  Lane l scans digits [248 - 8l, 256 - 8l).
+__device__ int nn_digit_from_top(const unsigned long long* hist, long long want, long long* before_out) {
+    const int lane = threadIdx.x & 31;
+    long long mine = 0;
+    for (int i = 0; i < 8; i++) mine += (long long)hist[255 - (lane * 8 + i)];
+    const long long incl = warp_incl_scan(mine);
+    const unsigned hit = __ballot_sync(0xffffffffu, incl >= want);
+    const int L = __ffs(hit) - 1;
+    long long before = __shfl_sync(0xffffffffu, incl - mine, L);
+    int digit = 0;
+    if (lane == L) {
+        long long c = before;
+        for (int i = 0; i < 8; i++) {
+            const int d = 255 - (L * 8 + i);
+            const long long hb = (long long)hist[d];
+            if (c + hb >= want) {
+                digit = d;
+                break;
+            }
+            c += hb;
+        }
+        before = c;
+    }
+    *before_out = __shfl_sync(0xffffffffu, before, L);
+    return __shfl_sync(0xffffffffu, digit, L);
+}
+
 __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelectArgs a) {
     extern __shared__ __align__(16) unsigned char nn_sel_smem[];
     unsigned long long(*s_hist)[256] = reinterpret_cast<unsigned long long(*)[256]>(nn_sel_smem);
@@ -335,10 +365,18 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
         // order (so in ascending entry index overall).
 
         // ---- hits-weighted radix select over the float bits of d2 in bin b*.
+        // keys of a fine bin share their top 13 bits: three passes over the
+        // low 19 (shifts 11, 3, 0; the last pass re-covers bits already
+        // fixed); the open-ended bins 0 and NB-1 take four
         unsigned prefix = 0u, pmask = 0u;
+        const bool fine = bstar >= 1 && bstar <= NN_NB - 2;
+        if (fine) {
+            prefix = (unsigned)(base + bstar - 1) << 19;
+            pmask = ~0u << 19;
+        }
         bool take_all = false;
-        for (int pass = 0; pass < 4 && !take_all; pass++) {
-            const int shift = 24 - 8 * pass;
+        for (int pass = 0; pass < (fine ? 3 : 4) && !take_all; pass++) {
+            const int shift = fine ? (pass == 0 ? 11 : pass == 1 ? 3 : 0) : 24 - 8 * pass;
             for (int i = lane; i < 256; i += 32) hist[i] = 0ull;
             __syncwarp();
             for (int sl = 0; sl < a.slices; sl++) {
@@ -348,7 +386,7 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
                     const float d2 = a.cand_d2[sb + i];
                     const unsigned key = __float_as_uint(d2);
                     if (nn_bin(d2, base) == bstar && (key & pmask) == prefix)
-                        atomicAdd(&hist[(key >> shift) & 255u], (unsigned long long)a.hits[a.cand_idx[sb + i]]);
+                        atomicAdd(&hist[(key >> shift) & 255u], (unsigned long long)a.cand_hits[sb + i]);
                 }
             }
             __syncwarp();
@@ -412,7 +450,7 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
             }
             // ties at kstar: keep in entry order while the tie hits before
             // this one are below `need`
-            const long long th = tie ? (long long)a.hits[e] : 0;
+            const long long th = tie ? (long long)a.cand_hits[sb + i] : 0;
             const long long incl = warp_incl_scan(th);
             if (tie && tie_cum + incl - th < need) keep = true;
             tie_cum += __shfl_sync(0xffffffffu, incl, 31);
@@ -503,30 +541,8 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
                     if ((kb & msk) == pre) atomicAdd(&hist[(kb >> shift) & 255ull], 1ull);
                 }
                 __syncwarp();
-                // scan from the largest digit down: lane l covers digits
-                // [248 - 8l, 256 - 8l)
-                long long mine = 0;
-                for (int i = 0; i < 8; i++) mine += (long long)hist[255 - (lane * 8 + i)];
-                const long long incl = warp_incl_scan(mine);
-                const unsigned hit = __ballot_sync(0xffffffffu, incl >= want);
-                const int L = __ffs(hit) - 1;
-                long long before = __shfl_sync(0xffffffffu, incl - mine, L);
-                int digit = 0;
-                if (lane == L) {
-                    long long c = before;
-                    for (int i = 0; i < 8; i++) {
-                        const int d = 255 - (L * 8 + i);
-                        const long long hb = (long long)hist[d];
-                        if (c + hb >= want) {
-                            digit = d;
-                            break;
-                        }
-                        c += hb;
-                    }
-                    before = c;
-                }
-                digit = __shfl_sync(0xffffffffu, digit, L);
-                before = __shfl_sync(0xffffffffu, before, L);
+                long long before = 0;
+                const int digit = nn_digit_from_top(hist, want, &before);
                 want -= before;
                 pre |= (unsigned long long)digit << shift;
                 msk |= 255ull << shift;
@@ -534,6 +550,30 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
             }
             sthr = pre;
             tie_keep = (int)want;  // ids with score == sthr to keep, largest ids first
+        }
+        // the tie_keep largest ids among those scoring exactly sthr: a radix
+        // select on the (distinct, non-negative) dense ids
+        int id_thr = 0x7fffffff;
+        if (!all && tie_keep > 0) {
+            unsigned pre2 = 0u, msk2 = 0u;
+            long long want2 = tie_keep;
+            for (int pass = 0; pass < 4; pass++) {
+                const int shift = 24 - 8 * pass;
+                for (int i = lane; i < 256; i += 32) hist[i] = 0ull;
+                __syncwarp();
+                for (int i = lane; i < ntouched; i += 32) {
+                    const unsigned id = (unsigned)touched[i];
+                    if (nn_dbits(acc[id]) == sthr && (id & msk2) == pre2) atomicAdd(&hist[(id >> shift) & 255u], 1ull);
+                }
+                __syncwarp();
+                long long before = 0;
+                const int digit = nn_digit_from_top(hist, want2, &before);
+                want2 -= before;
+                pre2 |= (unsigned)digit << shift;
+                msk2 |= 255u << shift;
+                __syncwarp();
+            }
+            id_thr = (int)pre2;
         }
         // gather the kept ids into shared memory (order fixed below by sort)
         for (int base = 0; base < ntouched; base += 32) {
@@ -548,16 +588,7 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
                 else {
                     const unsigned long long kb = nn_dbits(sc);
                     if (kb > sthr) sel = true;
-                    else if (kb == sthr) {
-                        // keep the tie_keep largest ids among the ties: count
-                        // ties with a larger id
-                        int larger = 0;
-                        for (int j = 0; j < ntouched; j++) {
-                            const int oid = touched[j];
-                            if (oid > id && nn_dbits(acc[oid]) == sthr) larger++;
-                        }
-                        sel = larger < tie_keep;
-                    }
+                    else if (kb == sthr) sel = id >= id_thr;
                 }
             }
             const unsigned sm = __ballot_sync(0xffffffffu, sel);
@@ -604,17 +635,23 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
             a.out_cand_score[(long)gq * h + i] = s_key[wib][i];
             if (a.out_cand_pep) a.out_cand_pep[(long)gq * h + i] = a.dense_pep[u];
         }
+        if (a.out_subfrac) {
+            // HybridClassifier: sum of adjusted score x peptide count, in
+            // candidate order (hybrid-classifier.cc:58-64); the terms formed
+            // in parallel, summed in order by one lane
+            __syncwarp();
+            for (int i = lane; i < nsel; i += 32)
+                s_key[wib][i] = (s_key[wib][i] / tot) * (double)a.dense_count[s_id[wib][i]];
+            __syncwarp();
+            if (lane == 0) {
+                double sf = 0.0;
+                for (int i = 0; i < nsel; i++) sf += s_key[wib][i];
+                a.out_subfrac[gq] = sf;
+            }
+        }
         if (lane == 0) {
             a.out_ncand[gq] = nsel;
             a.out_total[gq] = tot;
-            if (a.out_subfrac) {
-                // HybridClassifier: sum of adjusted score x peptide count, in
-                // candidate order (hybrid-classifier.cc:58-64)
-                double sf = 0.0;
-                for (int i = 0; i < nsel; i++)
-                    sf += (s_key[wib][i] / tot) * (double)a.dense_count[s_id[wib][i]];
-                a.out_subfrac[gq] = sf;
-            }
         }
         __syncwarp();
         // reset the per-warp accumulators
