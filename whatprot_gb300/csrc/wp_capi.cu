@@ -235,7 +235,7 @@ struct wp_ctx {
     std::vector<int32_t> nn_src_off, nn_src_id, nn_src_count, nn_src_hits, nn_uniq;
     DevBuf d_nn_coords, d_nn_hits, d_nn_src_off, d_nn_src_dense, d_nn_src_ratio, d_nn_src_hits, d_nn_dense_id,
             d_nn_dense_pep, d_nn_dense_count, d_nn_queries, d_nn_qbin, d_nn_qbase, d_nn_sample, d_nn_qbelow, d_nn_qcap, d_nn_qoff,
-            d_nn_cidx, d_nn_cd2, d_nn_chits, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
+            d_nn_cidx, d_nn_cd2, d_nn_chits, d_nn_cbin, d_nn_enorm, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
             d_nn_cand_score, d_nn_total, d_nn_subfrac, d_nn_cand_off, d_nn_cand_flat, d_nn_err, d_nn_shist,
             d_nn_sliceoff, d_nn_slicecap, d_nn_slicecnt;
 
@@ -683,16 +683,25 @@ wp_status nn_prepare(wp_ctx* ctx) {
     const int DP = nn_padded_dim(T * C);
     if (ctx->nn_coords_version != ctx->model_version) {
         std::vector<float> coords((size_t)std::max(N, 1) * DP, 0.0f);
+        std::vector<float> norms(std::max(N, 1), 0.0f);
         int cts[WP_MAX_CHANNELS];
-        for (long e = 0; e < N; e++)
+        for (long e = 0; e < N; e++) {
             for (int t = 0; t < T; t++) {
                 for (int c = 0; c < C; c++) cts[c] = ctx->nn_counts[(e * T + t) * C + c];
                 for (int c = 0; c < C; c++)
                     coords[e * DP + t * C + c] = (float)host_adjusted_mu(ctx->hm, c, cts);
             }
+            // squared norm in FP32, four partial sums as the kernels form |q|^2
+            float p[4] = {0.f, 0.f, 0.f, 0.f};
+            for (int i = 0; i < DP; i++) p[i % 4] = std::fma(coords[e * DP + i], coords[e * DP + i], p[i % 4]);
+            norms[e] = (p[0] + p[1]) + (p[2] + p[3]);
+        }
         WP_CUDA(ctx->d_nn_coords.ensure(sizeof(float) * coords.size()), "alloc coords");
         WP_CUDA(cudaMemcpyAsync(ctx->d_nn_coords.p, coords.data(), sizeof(float) * coords.size(),
                                 cudaMemcpyHostToDevice, ctx->stream), "copy coords");
+        WP_CUDA(ctx->d_nn_enorm.ensure(sizeof(float) * norms.size()), "alloc norms");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_enorm.p, norms.data(), sizeof(float) * norms.size(),
+                                cudaMemcpyHostToDevice, ctx->stream), "copy norms");
         WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
         ctx->nn_coords_version = ctx->model_version;
     }
@@ -770,6 +779,7 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
     NNArgs a;
     memset(&a, 0, sizeof(a));
     a.coords = ctx->d_nn_coords.as<float>();
+    a.enorm = ctx->d_nn_enorm.as<float>();
     a.hits = ctx->d_nn_hits.as<int>();
     a.N = N;
     a.k = k;
@@ -854,6 +864,7 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
         WP_CUDA(ctx->d_nn_cidx.ensure(sizeof(int) * std::max<long long>(tot, 1)), "alloc kNN candidates");
         WP_CUDA(ctx->d_nn_cd2.ensure(sizeof(float) * std::max<long long>(tot, 1)), "alloc kNN candidates");
         WP_CUDA(ctx->d_nn_chits.ensure(sizeof(int) * std::max<long long>(tot, 1)), "alloc kNN candidates");
+        WP_CUDA(ctx->d_nn_cbin.ensure(std::max<long long>(tot, 1)), "alloc kNN candidates");
         WP_CUDA(cudaMemcpyAsync(ctx->d_nn_qoff.p, off.data(), sizeof(long long) * nq, cudaMemcpyHostToDevice,
                                 ctx->stream), "copy offsets");
         a.queries = ctx->d_nn_queries.as<float>() + (size_t)r0 * DP;
@@ -863,6 +874,7 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
         a.cand_idx = ctx->d_nn_cidx.as<int>();
         a.cand_d2 = ctx->d_nn_cd2.as<float>();
         a.cand_hits = ctx->d_nn_chits.as<int>();
+        a.cand_bin = ctx->d_nn_cbin.as<unsigned char>();
         {
             TimedLaunch tl(ctx, 4);
             WP_CUDA(wp_launch_nn_dist(DP, false, ctx->stream, a), "kNN collect");
@@ -884,6 +896,7 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
         b.cand_idx = a.cand_idx;
         b.cand_d2 = a.cand_d2;
         b.cand_hits = a.cand_hits;
+        b.cand_bin = a.cand_bin;
         b.hits = a.hits;
         b.src_off = ctx->d_nn_src_off.as<int>();
         b.src_dense = ctx->d_nn_src_dense.as<int>();

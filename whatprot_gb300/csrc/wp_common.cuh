@@ -270,6 +270,7 @@ struct NNArgs {
     int R;                  // queries in this launch (chunk)
     int q0;                 // first query index of the chunk (into per-query arrays)
     const float* coords;    // [N][DP]
+    const float* enorm;     // [N] squared norm of each entry's coordinates
     const int* hits;        // [N] total hits per entry
     int N;
     long long k;
@@ -280,6 +281,7 @@ struct NNArgs {
     int* cand_idx;
     float* cand_d2;
     int* cand_hits;         // the entry's hits, next to its index
+    unsigned char* cand_bin;  // the distance bin the histogram counted it in
     int* err;
     int slices;             // entry slices (blockIdx.y)
     int slice_len;
@@ -309,6 +311,7 @@ struct NNSelectArgs {
     const int* cand_idx;
     const float* cand_d2;
     const int* cand_hits;
+    const unsigned char* cand_bin;
     const int* hits;            // [N]
     const int* src_off;         // [N + 1]
     const int* src_dense;       // [S] dense id

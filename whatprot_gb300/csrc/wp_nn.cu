@@ -77,15 +77,52 @@ __device__ __forceinline__ float nn_d2(const float* q, const float* e) {
 }
 
 
-// Load a tile of entries (coords and hits) into shared memory.
+// Squared distance for binning, as |q|^2 + |e|^2 - 2 q.e: one multiply-add
+// per coordinate instead of a subtract and a multiply-add.  Its rounding
+// error (about 1e-7 of |q|^2 + |e|^2) only moves entries lying that close to
+// a bin edge into the neighbouring bin; the candidates' exact distances
+// (nn_d2) decide their order.
 template <int DP>
-__device__ __forceinline__ void nn_load_tile(const NNArgs& a, int e0, int e_end, float* tile, int* thits) {
+__device__ __forceinline__ float nn_d2_dot(const float* q, float qn, const float* e, float en) {
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+    for (int i = 0; i < DP; i += 4) {
+        const float4 v = *reinterpret_cast<const float4*>(e + i);
+        a0 = fmaf(q[i], v.x, a0);
+        a1 = fmaf(q[i + 1], v.y, a1);
+        a2 = fmaf(q[i + 2], v.z, a2);
+        a3 = fmaf(q[i + 3], v.w, a3);
+    }
+    return fmaxf(fmaf(-2.f, (a0 + a1) + (a2 + a3), qn + en), 0.f);
+}
+
+// |q|^2 of a query held in registers (the same order in every kernel).
+template <int DP>
+__device__ __forceinline__ float nn_norm2(const float* q) {
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+    for (int i = 0; i < DP; i += 4) {
+        a0 = fmaf(q[i], q[i], a0);
+        a1 = fmaf(q[i + 1], q[i + 1], a1);
+        a2 = fmaf(q[i + 2], q[i + 2], a2);
+        a3 = fmaf(q[i + 3], q[i + 3], a3);
+    }
+    return (a0 + a1) + (a2 + a3);
+}
+
+// Load a tile of entries (coords, squared norms and hits) into shared memory.
+template <int DP>
+__device__ __forceinline__ void nn_load_tile(const NNArgs& a, int e0, int e_end, float* tile, int* thits,
+                                             float* ten) {
     const int n = min(NN_TE, e_end - e0);
     const float4* src = reinterpret_cast<const float4*>(a.coords + (long)e0 * DP);
     float4* dst = reinterpret_cast<float4*>(tile);
     for (int i = threadIdx.x; i < NN_TE * DP / 4; i += blockDim.x)
         dst[i] = (i < n * DP / 4) ? src[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int i = threadIdx.x; i < NN_TE; i += blockDim.x) thits[i] = i < n ? a.hits[e0 + i] : 0;
+    for (int i = threadIdx.x; i < NN_TE; i += blockDim.x) {
+        thits[i] = i < n ? a.hits[e0 + i] : 0;
+        ten[i] = i < n ? a.enorm[e0 + i] : 0.f;
+    }
 }
 
 template <int DP>
@@ -93,7 +130,8 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
     extern __shared__ __align__(16) unsigned char nn_smem[];
     float* tile = reinterpret_cast<float*>(nn_smem);
     int* thits = reinterpret_cast<int*>(tile + NN_TE * DP);
-    unsigned* hist = reinterpret_cast<unsigned*>(thits + NN_TE);  // [NN_QPB][NN_NB + 1]
+    float* ten = reinterpret_cast<float*>(thits + NN_TE);
+    unsigned* hist = reinterpret_cast<unsigned*>(ten + NN_TE);  // [NN_QPB][NN_NB + 1]
     const int qb = blockIdx.x * NN_QPB;
     const int s = blockIdx.y;
     const int e_lo = s * a.slice_len, e_hi = min(a.N, e_lo + a.slice_len);
@@ -110,15 +148,18 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
         for (int i = 0; i < DP; i++) q[j][i] = valid[j] ? src[i] : 0.f;
         base[j] = valid[j] ? a.qbase[a.q0 + qb + lq] : 0;
     }
+    float qn[NN_QPT];
+#pragma unroll
+    for (int j = 0; j < NN_QPT; j++) qn[j] = nn_norm2<DP>(q[j]);
     for (int e0 = e_lo; e0 < e_hi; e0 += NN_TE) {
         __syncthreads();
-        nn_load_tile<DP>(a, e0, e_hi, tile, thits);
+        nn_load_tile<DP>(a, e0, e_hi, tile, thits, ten);
         __syncthreads();
         const int n = min(NN_TE, e_hi - e0);
         for (int e = 0; e < n; e++) {
 #pragma unroll
             for (int j = 0; j < NN_QPT; j++) {
-                const float d2 = nn_d2<DP>(q[j], tile + e * DP);
+                const float d2 = nn_d2_dot<DP>(q[j], qn[j], tile + e * DP, ten[e]);
                 if (valid[j])
                     atomicAdd(&hist[(threadIdx.x + j * NN_THREADS) * (NN_NB + 1) + nn_bin(d2, base[j])],
                               (unsigned)thits[e]);
@@ -148,7 +189,8 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_estimate_kernel(NNArgs a) {
     extern __shared__ __align__(16) unsigned char nn_smem[];
     float* tile = reinterpret_cast<float*>(nn_smem);
     int* thits = reinterpret_cast<int*>(tile + NN_TE * DP);
-    unsigned* hist = reinterpret_cast<unsigned*>(thits + NN_TE);  // [NN_QPB][NN_NB + 1]
+    float* ten = reinterpret_cast<float*>(thits + NN_TE);
+    unsigned* hist = reinterpret_cast<unsigned*>(ten + NN_TE);  // [NN_QPB][NN_NB + 1]
     const int qb = blockIdx.x * NN_QPB;
     for (int i = threadIdx.x; i < NN_QPB * (NN_NB + 1); i += blockDim.x) hist[i] = 0u;
     float q[NN_QPT][DP];
@@ -161,6 +203,9 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_estimate_kernel(NNArgs a) {
 #pragma unroll
         for (int i = 0; i < DP; i++) q[j][i] = valid[j] ? src[i] : 0.f;
     }
+    float qn[NN_QPT];
+#pragma unroll
+    for (int j = 0; j < NN_QPT; j++) qn[j] = nn_norm2<DP>(q[j]);
     for (int s0 = 0; s0 < a.sample_n; s0 += NN_TE) {
         __syncthreads();
         const int n = min(NN_TE, a.sample_n - s0);
@@ -170,11 +215,12 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_estimate_kernel(NNArgs a) {
                 e < n ? reinterpret_cast<const float4*>(a.coords + (long)a.sample[s0 + e] * DP)[part]
                       : make_float4(0.f, 0.f, 0.f, 0.f);
         }
+        for (int i = threadIdx.x; i < NN_TE; i += blockDim.x) ten[i] = i < n ? a.enorm[a.sample[s0 + i]] : 0.f;
         __syncthreads();
         for (int e = 0; e < n; e++) {
 #pragma unroll
             for (int j = 0; j < NN_QPT; j++) {
-                const float d2 = nn_d2<DP>(q[j], tile + e * DP);
+                const float d2 = nn_d2_dot<DP>(q[j], qn[j], tile + e * DP, ten[e]);
                 if (valid[j]) atomicAdd(&hist[(threadIdx.x + j * NN_THREADS) * (NN_NB + 1) + nn_coarse_bin(d2)], 1u);
             }
         }
@@ -247,6 +293,7 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
     extern __shared__ __align__(16) unsigned char nn_smem[];
     float* tile = reinterpret_cast<float*>(nn_smem);
     int* thits = reinterpret_cast<int*>(tile + NN_TE * DP);
+    float* ten = reinterpret_cast<float*>(thits + NN_TE);
     const int qb = blockIdx.x * NN_QPB;
     const int s = blockIdx.y;
     const int e_lo = s * a.slice_len, e_hi = min(a.N, e_lo + a.slice_len);
@@ -269,20 +316,24 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
         cap[j] = valid[j] ? a.slicecap[(long)s * a.R_all + gq] : 0;
         cnt[j] = 0;
     }
+    float qn[NN_QPT];
+#pragma unroll
+    for (int j = 0; j < NN_QPT; j++) qn[j] = nn_norm2<DP>(q[j]);
     for (int e0 = e_lo; e0 < e_hi; e0 += NN_TE) {
         __syncthreads();
-        nn_load_tile<DP>(a, e0, e_hi, tile, thits);
+        nn_load_tile<DP>(a, e0, e_hi, tile, thits, ten);
         __syncthreads();
         const int n = min(NN_TE, e_hi - e0);
         for (int e = 0; e < n; e++) {
 #pragma unroll
             for (int j = 0; j < NN_QPT; j++) {
-                const float d2 = nn_d2<DP>(q[j], tile + e * DP);
-                if (nn_bin(d2, base[j]) <= bstar[j]) {
+                const int bin = nn_bin(nn_d2_dot<DP>(q[j], qn[j], tile + e * DP, ten[e]), base[j]);
+                if (bin <= bstar[j]) {
                     if (cnt[j] < cap[j]) {
                         a.cand_idx[off[j] + cnt[j]] = e0 + e;
-                        a.cand_d2[off[j] + cnt[j]] = d2;
+                        a.cand_d2[off[j] + cnt[j]] = nn_d2<DP>(q[j], tile + e * DP);
                         a.cand_hits[off[j] + cnt[j]] = thits[e];
+                        a.cand_bin[off[j] + cnt[j]] = (unsigned char)bin;
                     } else {
                         atomicExch(a.err, 1);
                     }
@@ -365,27 +416,37 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
         // order (so in ascending entry index overall).
 
         // ---- hits-weighted radix select over the float bits of d2 in bin b*.
-        // keys of a fine bin share their top 13 bits: three passes over the
-        // low 19 (shifts 11, 3, 0; the last pass re-covers bits already
-        // fixed); the open-ended bins 0 and NB-1 take four
-        unsigned prefix = 0u, pmask = 0u;
-        const bool fine = bstar >= 1 && bstar <= NN_NB - 2;
-        if (fine) {
-            prefix = (unsigned)(base + bstar - 1) << 19;
-            pmask = ~0u << 19;
+        // the keys of bin b*'s candidates share their top bits: the radix
+        // passes start below the common prefix of the smallest and largest
+        unsigned kmin = 0xffffffffu, kmax = 0u;
+        for (int sl = 0; sl < a.slices; sl++) {
+            const long long sb = a.qoff[lq] + a.sliceoff[(long)sl * a.R_all + gq];
+            const long long sn = min(a.slicecnt[(long)sl * a.R_all + gq], a.slicecap[(long)sl * a.R_all + gq]);
+            for (long long i = lane; i < sn; i += 32)
+                if (a.cand_bin[sb + i] == bstar) {
+                    const unsigned key = __float_as_uint(a.cand_d2[sb + i]);
+                    kmin = min(kmin, key);
+                    kmax = max(kmax, key);
+                }
         }
+        for (int o = 16; o > 0; o >>= 1) {
+            kmin = min(kmin, __shfl_xor_sync(0xffffffffu, kmin, o));
+            kmax = max(kmax, __shfl_xor_sync(0xffffffffu, kmax, o));
+        }
+        const int common = kmin <= kmax ? __clz((int)(kmin ^ kmax)) : 32;  // 32 when all keys are equal
+        const int rem = 32 - common;
+        unsigned pmask = common >= 32 ? 0xffffffffu : (common == 0 ? 0u : ~0u << rem);
+        unsigned prefix = kmin & pmask;
         bool take_all = false;
-        for (int pass = 0; pass < (fine ? 3 : 4) && !take_all; pass++) {
-            const int shift = fine ? (pass == 0 ? 11 : pass == 1 ? 3 : 0) : 24 - 8 * pass;
+        for (int shift = rem > 8 ? rem - 8 : 0;; shift = shift > 8 ? shift - 8 : 0) {
             for (int i = lane; i < 256; i += 32) hist[i] = 0ull;
             __syncwarp();
             for (int sl = 0; sl < a.slices; sl++) {
                 const long long sb = a.qoff[lq] + a.sliceoff[(long)sl * a.R_all + gq];
                 const long long sn = min(a.slicecnt[(long)sl * a.R_all + gq], a.slicecap[(long)sl * a.R_all + gq]);
                 for (long long i = lane; i < sn; i += 32) {
-                    const float d2 = a.cand_d2[sb + i];
-                    const unsigned key = __float_as_uint(d2);
-                    if (nn_bin(d2, base) == bstar && (key & pmask) == prefix)
+                    const unsigned key = __float_as_uint(a.cand_d2[sb + i]);
+                    if (a.cand_bin[sb + i] == bstar && (key & pmask) == prefix)
                         atomicAdd(&hist[(key >> shift) & 255u], (unsigned long long)a.cand_hits[sb + i]);
                 }
             }
@@ -424,6 +485,7 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
             prefix |= (unsigned)digit << shift;
             pmask |= 255u << shift;
             __syncwarp();
+            if (shift == 0) break;
         }
         const unsigned kstar = prefix;  // with take_all: unused
         // ---- contributions of the kept entries, in candidate (entry) order.
@@ -433,8 +495,8 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
         for (int sl = 0; sl < a.slices; sl++) {
           const long long sb = a.qoff[lq] + a.sliceoff[(long)sl * a.R_all + gq];
           const long long sn = min(a.slicecnt[(long)sl * a.R_all + gq], a.slicecap[(long)sl * a.R_all + gq]);
-          for (long long base = 0; base < sn; base += 32) {
-            const long long i = base + lane;
+          for (long long i0 = 0; i0 < sn; i0 += 32) {
+            const long long i = i0 + lane;
             bool keep = false;
             int e = -1;
             float d2 = 0.f;
@@ -442,7 +504,7 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
             if (i < sn) {
                 e = a.cand_idx[sb + i];
                 d2 = a.cand_d2[sb + i];
-                const int b = nn_bin(d2, base);
+                const int b = a.cand_bin[sb + i];
                 const unsigned key = __float_as_uint(d2);
                 if (b < bstar || take_all) keep = true;
                 else if (key < kstar) keep = true;
@@ -713,7 +775,7 @@ cudaError_t wp_launch_hybrid_finish(const int* ncand, const double* subfrac, int
 }
 
 size_t wp_nn_dist_smem_bytes(int DP, bool with_hist) {
-    size_t b = sizeof(float) * NN_TE * DP + sizeof(int) * NN_TE;
+    size_t b = sizeof(float) * NN_TE * DP + sizeof(int) * NN_TE + sizeof(float) * NN_TE;
     if (with_hist) b += sizeof(unsigned) * NN_QPB * (NN_NB + 1);
     return b;
 }
