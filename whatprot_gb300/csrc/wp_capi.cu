@@ -51,6 +51,10 @@ cudaError_t wp_launch_nn_dist(int DP, bool hist, cudaStream_t s, const NNArgs& a
 cudaError_t wp_launch_nn_select(int grid, cudaStream_t s, const NNSelectArgs& a);
 cudaError_t wp_launch_nn_threshold(cudaStream_t s, const NNArgs& a);
 cudaError_t wp_launch_nn_estimate(int DP, cudaStream_t s, const NNArgs& a);
+size_t wp_nn_sort_temp_bytes(int R);
+cudaError_t wp_launch_nn_sort_queries(const float* rows, int R, int DP, int TC, float* sorted, int* perm,
+                                      unsigned long long* keys, int* idx, void* temp, size_t temp_bytes,
+                                      cudaStream_t s);
 int wp_nn_bins();
 int wp_engine_max_threads();
 cudaError_t wp_launch_sim_reads(const SimParams& p, cudaStream_t s);
@@ -235,7 +239,8 @@ struct wp_ctx {
     std::vector<int32_t> nn_src_off, nn_src_id, nn_src_count, nn_src_hits, nn_uniq;
     DevBuf d_nn_coords, d_nn_hits, d_nn_src_off, d_nn_src_dense, d_nn_src_ratio, d_nn_src_hits, d_nn_dense_id,
             d_nn_dense_pep, d_nn_dense_count, d_nn_queries, d_nn_qbin, d_nn_qbase, d_nn_sample, d_nn_qbelow, d_nn_qcap, d_nn_qoff,
-            d_nn_cidx, d_nn_cd2, d_nn_chits, d_nn_cbin, d_nn_enorm, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
+            d_nn_cidx, d_nn_cd2, d_nn_chits, d_nn_cbin, d_nn_enorm, d_nn_tlo, d_nn_thi, d_nn_ttot,
+            d_nn_qsorted, d_nn_qperm, d_nn_qkeys, d_nn_qidx, d_nn_qtemp, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
             d_nn_cand_score, d_nn_total, d_nn_subfrac, d_nn_cand_off, d_nn_cand_flat, d_nn_err, d_nn_shist,
             d_nn_sliceoff, d_nn_slicecap, d_nn_slicecnt;
 
@@ -702,6 +707,36 @@ wp_status nn_prepare(wp_ctx* ctx) {
         WP_CUDA(ctx->d_nn_enorm.ensure(sizeof(float) * norms.size()), "alloc norms");
         WP_CUDA(cudaMemcpyAsync(ctx->d_nn_enorm.p, norms.data(), sizeof(float) * norms.size(),
                                 cudaMemcpyHostToDevice, ctx->stream), "copy norms");
+        // per tile of 32 consecutive entries: bounding box of the coordinates
+        // and the tile's hits (the kNN kernels skip tiles far from a read)
+        const int nt = std::max((N + 31) / 32, 1);
+        std::vector<float> tlo((size_t)nt * DP, 0.0f), thi((size_t)nt * DP, 0.0f);
+        std::vector<int> ttot(nt, 0);
+        for (int t = 0; t < (N + 31) / 32; t++) {
+            const int e1 = std::min(N, 32 * t + 32);
+            for (int i = 0; i < DP; i++) {
+                float lo = coords[(size_t)32 * t * DP + i], hi = lo;
+                for (int e = 32 * t + 1; e < e1; e++) {
+                    lo = std::min(lo, coords[(size_t)e * DP + i]);
+                    hi = std::max(hi, coords[(size_t)e * DP + i]);
+                }
+                tlo[(size_t)t * DP + i] = lo;
+                thi[(size_t)t * DP + i] = hi;
+            }
+            long long h = 0;
+            for (int e = 32 * t; e < e1; e++)
+                for (int k = ctx->nn_src_off[e]; k < ctx->nn_src_off[e + 1]; k++) h += ctx->nn_src_hits[k];
+            ttot[t] = (int)std::min<long long>(h, INT32_MAX);
+        }
+        WP_CUDA(ctx->d_nn_tlo.ensure(sizeof(float) * tlo.size()), "alloc tiles");
+        WP_CUDA(ctx->d_nn_thi.ensure(sizeof(float) * thi.size()), "alloc tiles");
+        WP_CUDA(ctx->d_nn_ttot.ensure(sizeof(int) * ttot.size()), "alloc tiles");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_tlo.p, tlo.data(), sizeof(float) * tlo.size(), cudaMemcpyHostToDevice,
+                                ctx->stream), "copy tiles");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_thi.p, thi.data(), sizeof(float) * thi.size(), cudaMemcpyHostToDevice,
+                                ctx->stream), "copy tiles");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_ttot.p, ttot.data(), sizeof(int) * ttot.size(), cudaMemcpyHostToDevice,
+                                ctx->stream), "copy tiles");
         WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
         ctx->nn_coords_version = ctx->model_version;
     }
@@ -776,10 +811,27 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
     }
     WP_CUDA(wp_launch_nn_queries(d_rads, R, T * C, DP, ctx->d_nn_queries.as<float>(), ctx->stream), "queries");
     ctx->launches++;
+    // reads in an order that groups alike ones (results go back by perm)
+    {
+        WP_CUDA(ctx->d_nn_qsorted.ensure(sizeof(float) * Rz * DP), "alloc");
+        WP_CUDA(ctx->d_nn_qperm.ensure(sizeof(int) * Rz), "alloc");
+        WP_CUDA(ctx->d_nn_qkeys.ensure(sizeof(unsigned long long) * 2 * Rz), "alloc");
+        WP_CUDA(ctx->d_nn_qidx.ensure(sizeof(int) * 2 * Rz), "alloc");
+        const size_t tb = wp_nn_sort_temp_bytes(R);
+        WP_CUDA(ctx->d_nn_qtemp.ensure(std::max<size_t>(tb, 1)), "alloc");
+        WP_CUDA(wp_launch_nn_sort_queries(ctx->d_nn_queries.as<float>(), R, DP, T * C, ctx->d_nn_qsorted.as<float>(),
+                                          ctx->d_nn_qperm.as<int>(), ctx->d_nn_qkeys.as<unsigned long long>(),
+                                          ctx->d_nn_qidx.as<int>(), ctx->d_nn_qtemp.p, tb, ctx->stream),
+                "sort queries");
+        ctx->launches += 3;
+    }
     NNArgs a;
     memset(&a, 0, sizeof(a));
     a.coords = ctx->d_nn_coords.as<float>();
     a.enorm = ctx->d_nn_enorm.as<float>();
+    a.tlo = ctx->d_nn_tlo.as<float>();
+    a.thi = ctx->d_nn_thi.as<float>();
+    a.ttot = ctx->d_nn_ttot.as<int>();
     a.hits = ctx->d_nn_hits.as<int>();
     a.N = N;
     a.k = k;
@@ -814,7 +866,7 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
     a.slicecnt = ctx->d_nn_slicecnt.as<long long>();
     // pass 1 over every read: the bins' origins from a sample, then the
     // histograms
-    a.queries = ctx->d_nn_queries.as<float>();
+    a.queries = ctx->d_nn_qsorted.as<float>();
     a.R = R;
     a.q0 = 0;
     {
@@ -867,7 +919,7 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
         WP_CUDA(ctx->d_nn_cbin.ensure(std::max<long long>(tot, 1)), "alloc kNN candidates");
         WP_CUDA(cudaMemcpyAsync(ctx->d_nn_qoff.p, off.data(), sizeof(long long) * nq, cudaMemcpyHostToDevice,
                                 ctx->stream), "copy offsets");
-        a.queries = ctx->d_nn_queries.as<float>() + (size_t)r0 * DP;
+        a.queries = ctx->d_nn_qsorted.as<float>() + (size_t)r0 * DP;
         a.R = nq;
         a.q0 = r0;
         a.qoff = ctx->d_nn_qoff.as<long long>();
@@ -885,6 +937,7 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
         b.R = nq;
         b.q0 = r0;
         b.qbin = a.qbin;
+        b.qperm = ctx->d_nn_qperm.as<int>();
         b.qbase = a.qbase;
         b.qbelow = a.qbelow;
         b.slices = a.slices;

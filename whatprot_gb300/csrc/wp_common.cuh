@@ -271,6 +271,9 @@ struct NNArgs {
     int q0;                 // first query index of the chunk (into per-query arrays)
     const float* coords;    // [N][DP]
     const float* enorm;     // [N] squared norm of each entry's coordinates
+    const float* tlo;       // [N / 32 rounded up][DP] per tile of 32 entries: smallest
+    const float* thi;       //   and largest coordinate, and the tile's hits
+    const int* ttot;
     const int* hits;        // [N] total hits per entry
     int N;
     long long k;
@@ -299,6 +302,7 @@ struct NNArgs {
 struct NNSelectArgs {
     int R;                      // queries in this chunk
     int q0;
+    const int* qperm;           // [R_all] read index of each (sorted) query slot
     const int* qbin;
     const int* qbase;           // per query bin origin (as NNArgs)
     const int* qbelow;

@@ -31,6 +31,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <cub/cub.cuh>
+
 #include "wp_common.cuh"
 
 #define NN_NB 64           // distance bins per query
@@ -110,6 +112,31 @@ __device__ __forceinline__ float nn_norm2(const float* q) {
     return (a0 + a1) + (a2 + a3);
 }
 
+// Lower bound of the squared distance from a query to any entry of a tile:
+// the distance to the tile's bounding box.
+template <int DP>
+__device__ __forceinline__ float nn_box_d2(const float* q, const float* lo, const float* hi) {
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+    for (int i = 0; i < DP; i += 2) {
+        const float g0 = fmaxf(fmaxf(lo[i] - q[i], q[i] - hi[i]), 0.f);
+        const float g1 = fmaxf(fmaxf(lo[i + 1] - q[i + 1], q[i + 1] - hi[i + 1]), 0.f);
+        a0 = fmaf(g0, g0, a0);
+        a1 = fmaf(g1, g1, a1);
+    }
+    return a0 + a1;
+}
+
+// A tile whose box bound clears a distance limit by this margin holds no
+// entry that nn_d2_dot puts below the limit (its rounding error is some
+// 1e-7 of |q|^2 + |e|^2).
+__device__ __forceinline__ bool nn_clears(float lb, float limit) {
+    return lb > limit + 1e-3f + 1e-4f * limit;
+}
+
+// Float value where a query's fine bin b starts.
+__device__ __forceinline__ float nn_bin_start(int base, int b) { return __uint_as_float((unsigned)(base + b - 1) << 19); }
+
 // Load a tile of entries (coords, squared norms and hits) into shared memory.
 template <int DP>
 __device__ __forceinline__ void nn_load_tile(const NNArgs& a, int e0, int e_end, float* tile, int* thits,
@@ -125,13 +152,21 @@ __device__ __forceinline__ void nn_load_tile(const NNArgs& a, int e0, int e_end,
     }
 }
 
+// A thread's queries are NN_QPT consecutive (sorted) slots, so a warp holds
+// 64 similar reads; its histogram rows sit at row j * NN_THREADS + tid
+// (bank-conflict free).  Per tile of 32 entries, each query first bounds
+// its distance to the tile's box: a tile beyond the start of the query's
+// last bin (open-ended, far beyond its k-hit radius) adds its hits to that
+// bin at once; the CTA loads the tile only if some query needs it, and a
+// warp whose queries all clear it skips the distances.
 template <int DP>
 __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
     extern __shared__ __align__(16) unsigned char nn_smem[];
     float* tile = reinterpret_cast<float*>(nn_smem);
     int* thits = reinterpret_cast<int*>(tile + NN_TE * DP);
     float* ten = reinterpret_cast<float*>(thits + NN_TE);
-    unsigned* hist = reinterpret_cast<unsigned*>(ten + NN_TE);  // [NN_QPB][NN_NB + 1]
+    float* box = ten + NN_TE;                                    // [2][DP]
+    unsigned* hist = reinterpret_cast<unsigned*>(box + 2 * DP);  // [NN_QPB][NN_NB + 1]
     const int qb = blockIdx.x * NN_QPB;
     const int s = blockIdx.y;
     const int e_lo = s * a.slice_len, e_hi = min(a.N, e_lo + a.slice_len);
@@ -139,29 +174,48 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
     float q[NN_QPT][DP];
     bool valid[NN_QPT];
     int base[NN_QPT];
+    float far[NN_QPT];
 #pragma unroll
     for (int j = 0; j < NN_QPT; j++) {
-        const int lq = threadIdx.x + j * NN_THREADS;
+        const int lq = threadIdx.x * NN_QPT + j;
         valid[j] = qb + lq < a.R;
         const float* src = a.queries + (long)(valid[j] ? qb + lq : 0) * DP;
 #pragma unroll
         for (int i = 0; i < DP; i++) q[j][i] = valid[j] ? src[i] : 0.f;
         base[j] = valid[j] ? a.qbase[a.q0 + qb + lq] : 0;
+        far[j] = valid[j] ? nn_bin_start(base[j], NN_NB - 1) : INFINITY;
     }
     float qn[NN_QPT];
 #pragma unroll
     for (int j = 0; j < NN_QPT; j++) qn[j] = nn_norm2<DP>(q[j]);
     for (int e0 = e_lo; e0 < e_hi; e0 += NN_TE) {
+        const int t = e0 / NN_TE;
         __syncthreads();
+        for (int i = threadIdx.x; i < DP; i += blockDim.x) {
+            box[i] = a.tlo[(long)t * DP + i];
+            box[DP + i] = a.thi[(long)t * DP + i];
+        }
+        __syncthreads();
+        bool need[NN_QPT];
+        bool any = false;
+#pragma unroll
+        for (int j = 0; j < NN_QPT; j++) {
+            need[j] = valid[j] && !nn_clears(nn_box_d2<DP>(q[j], box, box + DP), far[j]);
+            if (valid[j] && !need[j])
+                atomicAdd(&hist[(j * NN_THREADS + threadIdx.x) * (NN_NB + 1) + NN_NB - 1], (unsigned)a.ttot[t]);
+            any |= need[j];
+        }
+        if (!__syncthreads_or(any)) continue;
         nn_load_tile<DP>(a, e0, e_hi, tile, thits, ten);
         __syncthreads();
+        if (!__any_sync(0xffffffffu, any)) continue;
         const int n = min(NN_TE, e_hi - e0);
         for (int e = 0; e < n; e++) {
 #pragma unroll
             for (int j = 0; j < NN_QPT; j++) {
                 const float d2 = nn_d2_dot<DP>(q[j], qn[j], tile + e * DP, ten[e]);
-                if (valid[j])
-                    atomicAdd(&hist[(threadIdx.x + j * NN_THREADS) * (NN_NB + 1) + nn_bin(d2, base[j])],
+                if (need[j])
+                    atomicAdd(&hist[(j * NN_THREADS + threadIdx.x) * (NN_NB + 1) + nn_bin(d2, base[j])],
                               (unsigned)thits[e]);
             }
         }
@@ -170,8 +224,9 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
     // this slice's histograms, query-major within the slice
     for (int i = threadIdx.x; i < NN_QPB * NN_NB; i += blockDim.x) {
         const int lq = i / NN_NB, b = i % NN_NB;
+        const int row = (lq % NN_QPT) * NN_THREADS + lq / NN_QPT;
         if (qb + lq < a.R)
-            a.shist[((long)s * a.R_all + a.q0 + qb + lq) * NN_NB + b] = hist[lq * (NN_NB + 1) + b];
+            a.shist[((long)s * a.R_all + a.q0 + qb + lq) * NN_NB + b] = hist[row * (NN_NB + 1) + b];
     }
 }
 
@@ -180,8 +235,9 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
 // hits, so each sample point stands for the same number of hits): the
 // k-hit radius is the k / (all hits) quantile of the hits-weighted
 // distances, estimated by the sample's ceil(k x sample_n / all hits)-th
-// nearest point (binned coarsely); the query's fine bins start two octaves
-// below that coarse bin.  Only the bins move with the estimate; the
+// nearest point (binned coarsely); the query's fine bins start 3 1/8
+// octaves below that coarse bin and end, with the open last bin, 3/4 of an
+// octave above it.  Only the bins move with the estimate; the
 // selection stays exact whatever it says (a poor estimate only leaves more
 // candidates).
 template <int DP>
@@ -197,7 +253,7 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_estimate_kernel(NNArgs a) {
     bool valid[NN_QPT];
 #pragma unroll
     for (int j = 0; j < NN_QPT; j++) {
-        const int lq = threadIdx.x + j * NN_THREADS;
+        const int lq = threadIdx.x * NN_QPT + j;
         valid[j] = qb + lq < a.R;
         const float* src = a.queries + (long)(valid[j] ? qb + lq : 0) * DP;
 #pragma unroll
@@ -241,9 +297,11 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_estimate_kernel(NNArgs a) {
                 break;
             }
         }
-        // coarse bin b starts at float bits >> 21 == b - 1 + ((127 - 6) << 2)
+        // coarse bin b starts at float bits >> 21 == b - 1 + ((127 - 6) << 2);
+        // the fine bins start 50 sixteenths of an octave below it, so the
+        // last (open) fine bin starts three quarters of an octave above it
         const int ck = b - 1 + ((127 - 6) << 2);
-        a.qbase[a.q0 + qb + threadIdx.x + j * NN_THREADS] = 4 * ck - 32;
+        a.qbase[a.q0 + qb + threadIdx.x * NN_QPT + j] = 4 * ck - 50;
     }
 }
 
@@ -294,16 +352,18 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
     float* tile = reinterpret_cast<float*>(nn_smem);
     int* thits = reinterpret_cast<int*>(tile + NN_TE * DP);
     float* ten = reinterpret_cast<float*>(thits + NN_TE);
+    float* box = ten + NN_TE;  // [2][DP]
     const int qb = blockIdx.x * NN_QPB;
     const int s = blockIdx.y;
     const int e_lo = s * a.slice_len, e_hi = min(a.N, e_lo + a.slice_len);
     float q[NN_QPT][DP];
     bool valid[NN_QPT];
     int bstar[NN_QPT], base[NN_QPT];
+    float lim[NN_QPT];
     long long off[NN_QPT], cap[NN_QPT], cnt[NN_QPT];
 #pragma unroll
     for (int j = 0; j < NN_QPT; j++) {
-        const int lq = threadIdx.x + j * NN_THREADS;
+        const int lq = threadIdx.x * NN_QPT + j;
         valid[j] = qb + lq < a.R;
         const int l = valid[j] ? qb + lq : 0;
         const int gq = a.q0 + l;
@@ -315,14 +375,28 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
         off[j] = valid[j] ? a.qoff[l] + a.sliceoff[(long)s * a.R_all + gq] : 0;
         cap[j] = valid[j] ? a.slicecap[(long)s * a.R_all + gq] : 0;
         cnt[j] = 0;
+        // candidates lie below the start of bin b* + 1 (none beyond the open last bin)
+        lim[j] = !valid[j] ? -1.f : (bstar[j] >= NN_NB - 1 ? INFINITY : nn_bin_start(base[j], bstar[j] + 1));
     }
     float qn[NN_QPT];
 #pragma unroll
     for (int j = 0; j < NN_QPT; j++) qn[j] = nn_norm2<DP>(q[j]);
     for (int e0 = e_lo; e0 < e_hi; e0 += NN_TE) {
+        const int t = e0 / NN_TE;
         __syncthreads();
+        for (int i = threadIdx.x; i < DP; i += blockDim.x) {
+            box[i] = a.tlo[(long)t * DP + i];
+            box[DP + i] = a.thi[(long)t * DP + i];
+        }
+        __syncthreads();
+        bool any = false;
+#pragma unroll
+        for (int j = 0; j < NN_QPT; j++)
+            any |= valid[j] && !nn_clears(nn_box_d2<DP>(q[j], box, box + DP), lim[j]);
+        if (!__syncthreads_or(any)) continue;
         nn_load_tile<DP>(a, e0, e_hi, tile, thits, ten);
         __syncthreads();
+        if (!__any_sync(0xffffffffu, any)) continue;
         const int n = min(NN_TE, e_hi - e0);
         for (int e = 0; e < n; e++) {
 #pragma unroll
@@ -345,7 +419,7 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
 #pragma unroll
     for (int j = 0; j < NN_QPT; j++) {
         if (!valid[j]) continue;
-        a.slicecnt[(long)s * a.R_all + a.q0 + qb + threadIdx.x + j * NN_THREADS] = cnt[j];
+        a.slicecnt[(long)s * a.R_all + a.q0 + qb + threadIdx.x * NN_QPT + j] = cnt[j];
         if (cnt[j] > cap[j]) atomicExch(a.err, 1);
     }
 }
@@ -690,12 +764,13 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
                 __syncwarp();
             }
         }
-        // outputs
+        // outputs, at the read's own index
+        const int oq = a.qperm ? a.qperm[gq] : gq;
         for (int i = lane; i < nsel; i += 32) {
             const int u = s_id[wib][i];
-            a.out_cand_id[(long)gq * h + i] = a.dense_id[u];
-            a.out_cand_score[(long)gq * h + i] = s_key[wib][i];
-            if (a.out_cand_pep) a.out_cand_pep[(long)gq * h + i] = a.dense_pep[u];
+            a.out_cand_id[(long)oq * h + i] = a.dense_id[u];
+            a.out_cand_score[(long)oq * h + i] = s_key[wib][i];
+            if (a.out_cand_pep) a.out_cand_pep[(long)oq * h + i] = a.dense_pep[u];
         }
         if (a.out_subfrac) {
             // HybridClassifier: sum of adjusted score x peptide count, in
@@ -708,12 +783,12 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
             if (lane == 0) {
                 double sf = 0.0;
                 for (int i = 0; i < nsel; i++) sf += s_key[wib][i];
-                a.out_subfrac[gq] = sf;
+                a.out_subfrac[oq] = sf;
             }
         }
         if (lane == 0) {
-            a.out_ncand[gq] = nsel;
-            a.out_total[gq] = tot;
+            a.out_ncand[oq] = nsel;
+            a.out_total[oq] = tot;
         }
         __syncwarp();
         // reset the per-warp accumulators
@@ -775,7 +850,7 @@ cudaError_t wp_launch_hybrid_finish(const int* ncand, const double* subfrac, int
 }
 
 size_t wp_nn_dist_smem_bytes(int DP, bool with_hist) {
-    size_t b = sizeof(float) * NN_TE * DP + sizeof(int) * NN_TE + sizeof(float) * NN_TE;
+    size_t b = sizeof(float) * NN_TE * DP + sizeof(int) * NN_TE + sizeof(float) * NN_TE + sizeof(float) * 2 * DP;
     if (with_hist) b += sizeof(unsigned) * NN_QPB * (NN_NB + 1);
     return b;
 }
@@ -859,5 +934,59 @@ cudaError_t wp_launch_nn_queries(const double* rads, int R, int TC, int DP, floa
 cudaError_t wp_launch_nn_ragged(const int* cand, int h, const int* off, int R, int* out, cudaStream_t s) {
     if (R == 0) return cudaSuccess;
     wp_nn_ragged_kernel<<<R, 128, 0, s>>>(cand, h, off, R, out);
+    return cudaGetLastError();
+}
+
+// ---- query order ----------------------------------------------------------
+// Reads sorted by their first 16 intensities rounded to 0..15 (first one
+// most significant), so that the queries of a warp or CTA are alike and skip
+// the same far tiles.  Results go back to each read's own index.
+__global__ void wp_nn_qkey_kernel(const float* __restrict__ rows, int R, int DP, int TC,
+                                  unsigned long long* __restrict__ keys, int* __restrict__ idx) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    unsigned long long k = 0;
+    for (int i = 0; i < 16; i++) {
+        const float v = i < TC ? rows[(long)r * DP + i] : 0.f;
+        const int n = (int)fminf(fmaxf(rintf(v), 0.f), 15.f);
+        k = (k << 4) | (unsigned long long)n;
+    }
+    keys[r] = k;
+    idx[r] = r;
+}
+
+__global__ void wp_nn_qgather_kernel(const float* __restrict__ rows, const int* __restrict__ perm, int R, int DP,
+                                     float* __restrict__ out) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long)R * DP) return;
+    const long r = i / DP;
+    out[i] = rows[(long)perm[r] * DP + i % DP];
+}
+
+size_t wp_nn_sort_temp_bytes(int R) {
+    size_t b = 0;
+    cub::DoubleBuffer<unsigned long long> k(nullptr, nullptr);
+    cub::DoubleBuffer<int> v(nullptr, nullptr);
+    cub::DeviceRadixSort::SortPairs(nullptr, b, k, v, R);
+    return b;
+}
+
+// rows [R][DP] -> sorted [R][DP]; perm[slot] = read.  keys [2R], idx [2R].
+cudaError_t wp_launch_nn_sort_queries(const float* rows, int R, int DP, int TC, float* sorted, int* perm,
+                                      unsigned long long* keys, int* idx, void* temp, size_t temp_bytes,
+                                      cudaStream_t s) {
+    if (R == 0) return cudaSuccess;
+    wp_nn_qkey_kernel<<<(R + 255) / 256, 256, 0, s>>>(rows, R, DP, TC, keys, idx);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    cub::DoubleBuffer<unsigned long long> kb(keys, keys + R);
+    cub::DoubleBuffer<int> vb(idx, idx + R);
+    size_t tb = temp_bytes;
+    e = cub::DeviceRadixSort::SortPairs(temp, tb, kb, vb, R, 0, 64, s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(perm, vb.Current(), sizeof(int) * R, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    const long n = (long)R * DP;
+    wp_nn_qgather_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(rows, perm, R, DP, sorted);
     return cudaGetLastError();
 }
