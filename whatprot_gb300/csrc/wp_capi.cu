@@ -1757,12 +1757,12 @@ wp_status nn_install(wp_ctx* ctx, const int16_t* counts, int N, int T, int C, co
     }
     ctx->nn_hits_total = 0;
     for (int e = 0; e < N; e++) ctx->nn_hits_total += ehits[e];
-    // 4096 entries by systematic sampling of the cumulative hits (the
-    // midpoint of each of 4096 equal shares): each stands for the same
+    // 16384 entries by systematic sampling of the cumulative hits (the
+    // midpoint of each of 16384 equal shares): each stands for the same
     // number of hits, so the kNN search can estimate each read's k-hit
     // radius from them
     {
-        const int S = N > 0 ? 4096 : 0;
+        const int S = N > 0 ? 16384 : 0;
         std::vector<int> sample(std::max(S, 1), 0);
         long long cum = 0;
         int e = 0;

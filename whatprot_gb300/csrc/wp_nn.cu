@@ -235,9 +235,9 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
 // hits, so each sample point stands for the same number of hits): the
 // k-hit radius is the k / (all hits) quantile of the hits-weighted
 // distances, estimated by the sample's ceil(k x sample_n / all hits)-th
-// nearest point (binned coarsely); the query's fine bins start 3 1/8
-// octaves below that coarse bin and end, with the open last bin, 3/4 of an
-// octave above it.  Only the bins move with the estimate; the
+// nearest point (binned coarsely); the query's fine bins start 2 3/4
+// octaves below that coarse bin and end, with the open last bin, 1 1/8
+// octaves above it.  Only the bins move with the estimate; the
 // selection stays exact whatever it says (a poor estimate only leaves more
 // candidates).
 template <int DP>
@@ -298,10 +298,10 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_estimate_kernel(NNArgs a) {
             }
         }
         // coarse bin b starts at float bits >> 21 == b - 1 + ((127 - 6) << 2);
-        // the fine bins start 50 sixteenths of an octave below it, so the
-        // last (open) fine bin starts three quarters of an octave above it
+        // the fine bins start 44 sixteenths of an octave below it, so the
+        // last (open) fine bin starts 18 sixteenths above it
         const int ck = b - 1 + ((127 - 6) << 2);
-        a.qbase[a.q0 + qb + threadIdx.x * NN_QPT + j] = 4 * ck - 50;
+        a.qbase[a.q0 + qb + threadIdx.x * NN_QPT + j] = 4 * ck - 44;
     }
 }
 
