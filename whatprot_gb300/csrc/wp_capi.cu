@@ -52,6 +52,7 @@ cudaError_t wp_launch_nn_select(int grid, cudaStream_t s, const NNSelectArgs& a)
 cudaError_t wp_launch_nn_threshold(cudaStream_t s, const NNArgs& a);
 cudaError_t wp_launch_nn_estimate(int DP, cudaStream_t s, const NNArgs& a);
 size_t wp_nn_sort_temp_bytes(int R);
+cudaError_t wp_launch_nn_redo(const NNArgs& a, int* list, int* count, int shift, cudaStream_t s);
 cudaError_t wp_launch_nn_sort_queries(const float* rows, int R, int DP, int TC, float* sorted, int* perm,
                                       unsigned long long* keys, int* idx, void* temp, size_t temp_bytes,
                                       cudaStream_t s);
@@ -240,7 +241,7 @@ struct wp_ctx {
     DevBuf d_nn_coords, d_nn_hits, d_nn_src_off, d_nn_src_dense, d_nn_src_ratio, d_nn_src_hits, d_nn_dense_id,
             d_nn_dense_pep, d_nn_dense_count, d_nn_queries, d_nn_qbin, d_nn_qbase, d_nn_sample, d_nn_qbelow, d_nn_qcap, d_nn_qoff,
             d_nn_cidx, d_nn_cd2, d_nn_chits, d_nn_cbin, d_nn_enorm, d_nn_tlo, d_nn_thi, d_nn_ttot,
-            d_nn_qsorted, d_nn_qperm, d_nn_qkeys, d_nn_qidx, d_nn_qtemp, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
+            d_nn_qsorted, d_nn_qperm, d_nn_qkeys, d_nn_qidx, d_nn_qtemp, d_nn_redo, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
             d_nn_cand_score, d_nn_total, d_nn_subfrac, d_nn_cand_off, d_nn_cand_flat, d_nn_err, d_nn_shist,
             d_nn_sliceoff, d_nn_slicecap, d_nn_slicecnt;
 
@@ -881,6 +882,29 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
     }
     WP_CUDA(wp_launch_nn_threshold(ctx->stream, a), "kNN threshold");
     ctx->launches++;
+    // reads whose k-th hit lies beyond their bins: counted again with the
+    // bins moved up 2.5 octaves (at most three times; after that the open
+    // last bin is just a large candidate set)
+    WP_CUDA(ctx->d_nn_redo.ensure(sizeof(int) * (Rz + 1)), "alloc");
+    for (int round = 0; round < 3; round++) {
+        int* list = ctx->d_nn_redo.as<int>() + 1;
+        WP_CUDA(wp_launch_nn_redo(a, list, ctx->d_nn_redo.as<int>(), 40, ctx->stream), "kNN redo");
+        ctx->launches++;
+        int nredo = 0;
+        WP_CUDA(cudaMemcpyAsync(&nredo, ctx->d_nn_redo.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream), "copy");
+        WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        if (nredo == 0) break;
+        NNArgs r = a;
+        r.slots = list;
+        r.R = nredo;
+        {
+            TimedLaunch tl(ctx, 4);
+            WP_CUDA(wp_launch_nn_dist(DP, true, ctx->stream, r), "kNN histogram");
+            ctx->launches++;
+        }
+        WP_CUDA(wp_launch_nn_threshold(ctx->stream, r), "kNN threshold");
+        ctx->launches++;
+    }
     std::vector<long long> cap(R);
     WP_CUDA(cudaMemcpyAsync(cap.data(), a.qcap, sizeof(long long) * R, cudaMemcpyDeviceToHost, ctx->stream),
             "copy caps");

@@ -179,10 +179,11 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
     for (int j = 0; j < NN_QPT; j++) {
         const int lq = threadIdx.x * NN_QPT + j;
         valid[j] = qb + lq < a.R;
-        const float* src = a.queries + (long)(valid[j] ? qb + lq : 0) * DP;
+        const int slot = !valid[j] ? 0 : (a.slots ? a.slots[qb + lq] : qb + lq);
+        const float* src = a.queries + (long)slot * DP;
 #pragma unroll
         for (int i = 0; i < DP; i++) q[j][i] = valid[j] ? src[i] : 0.f;
-        base[j] = valid[j] ? a.qbase[a.q0 + qb + lq] : 0;
+        base[j] = valid[j] ? a.qbase[a.q0 + slot] : 0;
         far[j] = valid[j] ? nn_bin_start(base[j], NN_NB - 1) : INFINITY;
     }
     float qn[NN_QPT];
@@ -225,8 +226,10 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
     for (int i = threadIdx.x; i < NN_QPB * NN_NB; i += blockDim.x) {
         const int lq = i / NN_NB, b = i % NN_NB;
         const int row = (lq % NN_QPT) * NN_THREADS + lq / NN_QPT;
-        if (qb + lq < a.R)
-            a.shist[((long)s * a.R_all + a.q0 + qb + lq) * NN_NB + b] = hist[row * (NN_NB + 1) + b];
+        if (qb + lq < a.R) {
+            const int slot = a.slots ? a.slots[qb + lq] : qb + lq;
+            a.shist[((long)s * a.R_all + a.q0 + slot) * NN_NB + b] = hist[row * (NN_NB + 1) + b];
+        }
     }
 }
 
@@ -235,9 +238,9 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
 // hits, so each sample point stands for the same number of hits): the
 // k-hit radius is the k / (all hits) quantile of the hits-weighted
 // distances, estimated by the sample's ceil(k x sample_n / all hits)-th
-// nearest point (binned coarsely); the query's fine bins start 2 3/4
-// octaves below that coarse bin and end, with the open last bin, 1 1/8
-// octaves above it.  Only the bins move with the estimate; the
+// nearest point (binned coarsely); the query's fine bins start 3 3/8
+// octaves below that coarse bin and end, with the open last bin, half an
+// octave above it.  Only the bins move with the estimate; the
 // selection stays exact whatever it says (a poor estimate only leaves more
 // candidates).
 template <int DP>
@@ -298,10 +301,12 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_estimate_kernel(NNArgs a) {
             }
         }
         // coarse bin b starts at float bits >> 21 == b - 1 + ((127 - 6) << 2);
-        // the fine bins start 44 sixteenths of an octave below it, so the
-        // last (open) fine bin starts 18 sixteenths above it
+        // the fine bins start 54 sixteenths of an octave below it, so the
+        // last (open) fine bin starts half an octave above it (a read whose
+        // radius lies beyond is counted again with its bins moved up,
+        // wp_nn_redo_kernel)
         const int ck = b - 1 + ((127 - 6) << 2);
-        a.qbase[a.q0 + qb + threadIdx.x * NN_QPT + j] = 4 * ck - 44;
+        a.qbase[a.q0 + qb + threadIdx.x * NN_QPT + j] = 4 * ck - 54;
     }
 }
 
@@ -311,7 +316,7 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_estimate_kernel(NNArgs a) {
 __global__ void wp_nn_threshold_kernel(NNArgs a) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= a.R) return;
-    const int gq = a.q0 + q;
+    const int gq = a.q0 + (a.slots ? a.slots[q] : q);
     long long cum = 0, below = 0, cap = 0;
     int b = NN_NB - 1;
     bool found = false;
@@ -909,6 +914,27 @@ cudaError_t wp_launch_nn_estimate(int DP, cudaStream_t s, const NNArgs& a) {
         case 64: return launch_estimate<64>(grid, s, a);
         default: return cudaErrorInvalidValue;
     }
+}
+
+// Reads whose k-th hit fell in the open last bin (the estimate was low):
+// listed, their bins moved up by `shift` sixteenths of an octave, to be
+// counted again.
+__global__ void wp_nn_redo_kernel(NNArgs a, int* list, int* count, int shift) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= a.R) return;
+    const int gq = a.q0 + q;
+    if (a.qbin[gq] == NN_NB - 1 && a.qcap[gq] >= a.k) {
+        list[atomicAdd(count, 1)] = q;
+        a.qbase[gq] += shift;
+    }
+}
+
+cudaError_t wp_launch_nn_redo(const NNArgs& a, int* list, int* count, int shift, cudaStream_t s) {
+    if (a.R == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    wp_nn_redo_kernel<<<(a.R + 255) / 256, 256, 0, s>>>(a, list, count, shift);
+    return cudaGetLastError();
 }
 
 cudaError_t wp_launch_nn_threshold(cudaStream_t s, const NNArgs& a) {
