@@ -127,6 +127,30 @@ __device__ __forceinline__ float nn_box_d2(const float* q, const float* lo, cons
     return a0 + a1;
 }
 
+// The same with the box read from global memory (every lane of a warp reads
+// the same box, so the loads are broadcasts from L1).
+template <int DP>
+__device__ __forceinline__ float nn_box_d2_global(const float* q, const float* __restrict__ lo,
+                                                  const float* __restrict__ hi) {
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+    for (int i = 0; i < DP; i += 4) {
+        const float4 l = __ldg(reinterpret_cast<const float4*>(lo + i));
+        const float4 h = __ldg(reinterpret_cast<const float4*>(hi + i));
+        const float g0 = fmaxf(fmaxf(l.x - q[i], q[i] - h.x), 0.f);
+        const float g1 = fmaxf(fmaxf(l.y - q[i + 1], q[i + 1] - h.y), 0.f);
+        const float g2 = fmaxf(fmaxf(l.z - q[i + 2], q[i + 2] - h.z), 0.f);
+        const float g3 = fmaxf(fmaxf(l.w - q[i + 3], q[i + 3] - h.w), 0.f);
+        a0 = fmaf(g0, g0, a0);
+        a1 = fmaf(g1, g1, a1);
+        a0 = fmaf(g2, g2, a0);
+        a1 = fmaf(g3, g3, a1);
+    }
+    return a0 + a1;
+}
+
+#define NN_SUPER 32  // tiles whose boxes a CTA checks between two votes
+
 // A tile whose box bound clears a distance limit by this margin holds no
 // entry that nn_d2_dot puts below the limit (its rounding error is some
 // 1e-7 of |q|^2 + |e|^2).
@@ -189,35 +213,55 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
     float qn[NN_QPT];
 #pragma unroll
     for (int j = 0; j < NN_QPT; j++) qn[j] = nn_norm2<DP>(q[j]);
-    for (int e0 = e_lo; e0 < e_hi; e0 += NN_TE) {
-        const int t = e0 / NN_TE;
-        __syncthreads();
-        for (int i = threadIdx.x; i < DP; i += blockDim.x) {
-            box[i] = a.tlo[(long)t * DP + i];
-            box[DP + i] = a.thi[(long)t * DP + i];
-        }
-        __syncthreads();
-        bool need[NN_QPT];
-        bool any = false;
+    unsigned* vote = reinterpret_cast<unsigned*>(box);
+    for (int st0 = e_lo; st0 < e_hi; st0 += NN_TE * NN_SUPER) {
+        // which of the next NN_SUPER tiles each read needs; the others add
+        // their hits to the read's open last bin
+        const int t0 = st0 / NN_TE, nt = min(NN_SUPER, (e_hi - st0 + NN_TE - 1) / NN_TE);
+        unsigned nm[NN_QPT];
 #pragma unroll
-        for (int j = 0; j < NN_QPT; j++) {
-            need[j] = valid[j] && !nn_clears(nn_box_d2<DP>(q[j], box, box + DP), far[j]);
-            if (valid[j] && !need[j])
-                atomicAdd(&hist[(j * NN_THREADS + threadIdx.x) * (NN_NB + 1) + NN_NB - 1], (unsigned)a.ttot[t]);
-            any |= need[j];
-        }
-        if (!__syncthreads_or(any)) continue;
-        nn_load_tile<DP>(a, e0, e_hi, tile, thits, ten);
-        __syncthreads();
-        if (!__any_sync(0xffffffffu, any)) continue;
-        const int n = min(NN_TE, e_hi - e0);
-        for (int e = 0; e < n; e++) {
+        for (int j = 0; j < NN_QPT; j++) nm[j] = 0u;
+        for (int tt = 0; tt < nt; tt++) {
+            const long t = t0 + tt;
 #pragma unroll
             for (int j = 0; j < NN_QPT; j++) {
-                const float d2 = nn_d2_dot<DP>(q[j], qn[j], tile + e * DP, ten[e]);
-                if (need[j])
-                    atomicAdd(&hist[(j * NN_THREADS + threadIdx.x) * (NN_NB + 1) + nn_bin(d2, base[j])],
-                              (unsigned)thits[e]);
+                if (!valid[j]) continue;
+                if (!nn_clears(nn_box_d2_global<DP>(q[j], a.tlo + t * DP, a.thi + t * DP), far[j]))
+                    nm[j] |= 1u << tt;
+                else
+                    atomicAdd(&hist[(j * NN_THREADS + threadIdx.x) * (NN_NB + 1) + NN_NB - 1], (unsigned)a.ttot[t]);
+            }
+        }
+        unsigned wm = 0u;
+#pragma unroll
+        for (int j = 0; j < NN_QPT; j++) wm |= nm[j];
+        wm = __reduce_or_sync(0xffffffffu, wm);
+        __syncthreads();
+        if (threadIdx.x == 0) vote[0] = 0u;
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0 && wm) atomicOr(&vote[0], wm);
+        __syncthreads();
+        unsigned cm = vote[0];
+        while (cm) {
+            const int tt = __ffs(cm) - 1;
+            cm &= cm - 1;
+            const int e0 = st0 + tt * NN_TE;
+            __syncthreads();
+            nn_load_tile<DP>(a, e0, e_hi, tile, thits, ten);
+            __syncthreads();
+            if (!((wm >> tt) & 1u)) continue;
+            bool need[NN_QPT];
+#pragma unroll
+            for (int j = 0; j < NN_QPT; j++) need[j] = (nm[j] >> tt) & 1u;
+            const int n = min(NN_TE, e_hi - e0);
+            for (int e = 0; e < n; e++) {
+#pragma unroll
+                for (int j = 0; j < NN_QPT; j++) {
+                    const float d2 = nn_d2_dot<DP>(q[j], qn[j], tile + e * DP, ten[e]);
+                    if (need[j])
+                        atomicAdd(&hist[(j * NN_THREADS + threadIdx.x) * (NN_NB + 1) + nn_bin(d2, base[j])],
+                                  (unsigned)thits[e]);
+                }
             }
         }
     }
@@ -386,22 +430,33 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
     float qn[NN_QPT];
 #pragma unroll
     for (int j = 0; j < NN_QPT; j++) qn[j] = nn_norm2<DP>(q[j]);
-    for (int e0 = e_lo; e0 < e_hi; e0 += NN_TE) {
-        const int t = e0 / NN_TE;
-        __syncthreads();
-        for (int i = threadIdx.x; i < DP; i += blockDim.x) {
-            box[i] = a.tlo[(long)t * DP + i];
-            box[DP + i] = a.thi[(long)t * DP + i];
-        }
-        __syncthreads();
-        bool any = false;
+    unsigned* vote = reinterpret_cast<unsigned*>(box);
+    for (int st0 = e_lo; st0 < e_hi; st0 += NN_TE * NN_SUPER) {
+        const int t0 = st0 / NN_TE, nt = min(NN_SUPER, (e_hi - st0 + NN_TE - 1) / NN_TE);
+        unsigned wm = 0u;
+        for (int tt = 0; tt < nt; tt++) {
+            const long t = t0 + tt;
+            bool nd = false;
 #pragma unroll
-        for (int j = 0; j < NN_QPT; j++)
-            any |= valid[j] && !nn_clears(nn_box_d2<DP>(q[j], box, box + DP), lim[j]);
-        if (!__syncthreads_or(any)) continue;
+            for (int j = 0; j < NN_QPT; j++)
+                nd |= valid[j] && !nn_clears(nn_box_d2_global<DP>(q[j], a.tlo + t * DP, a.thi + t * DP), lim[j]);
+            if (nd) wm |= 1u << tt;
+        }
+        wm = __reduce_or_sync(0xffffffffu, wm);
+        __syncthreads();
+        if (threadIdx.x == 0) vote[0] = 0u;
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0 && wm) atomicOr(&vote[0], wm);
+        __syncthreads();
+        unsigned cm = vote[0];
+        while (cm) {
+        const int tt = __ffs(cm) - 1;
+        cm &= cm - 1;
+        const int e0 = st0 + tt * NN_TE;
+        __syncthreads();
         nn_load_tile<DP>(a, e0, e_hi, tile, thits, ten);
         __syncthreads();
-        if (!__any_sync(0xffffffffu, any)) continue;
+        if (!((wm >> tt) & 1u)) continue;
         const int n = min(NN_TE, e_hi - e0);
         for (int e = 0; e < n; e++) {
 #pragma unroll
@@ -419,6 +474,7 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
                     cnt[j]++;
                 }
             }
+        }
         }
     }
 #pragma unroll
@@ -489,7 +545,7 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
 
     for (long lq = gw; lq < a.R; lq += nw) {
         const int gq = a.q0 + (int)lq;
-        const int bstar = a.qbin[gq], base = a.qbase[gq];
+        const int bstar = a.qbin[gq];
         long long need = a.k - a.qbelow[gq];  // hits still needed from bin b*
         // The query's candidates: one segment per entry slice, in slice
         // order (so in ascending entry index overall).
