@@ -37,8 +37,9 @@
 
 #define NN_NB 64           // distance bins per query
 #define NN_TE 32           // entries per shared-memory tile
-#define NN_THREADS 128     // threads per CTA in the distance kernels
-#define NN_QPT 2           // queries per thread
+#define NN_THREADS 256     // threads per CTA in the distance kernels
+#define NN_QPT 1           // queries per thread (one: a warp's 32 sorted reads share
+                           // fewer far tiles than 64 would)
 #define NN_QPB (NN_THREADS * NN_QPT)
 #define NN_SEL_WARPS 4     // warps per CTA in the select kernel
 #define NN_HMAX 1024       // largest h
@@ -177,7 +178,7 @@ __device__ __forceinline__ void nn_load_tile(const NNArgs& a, int e0, int e_end,
 }
 
 // A thread's queries are NN_QPT consecutive (sorted) slots, so a warp holds
-// 64 similar reads; its histogram rows sit at row j * NN_THREADS + tid
+// 32 NN_QPT similar reads; its histogram rows sit at row j * NN_THREADS + tid
 // (bank-conflict free).  Per tile of 32 entries, each query first bounds
 // its distance to the tile's box: a tile beyond the start of the query's
 // last bin (open-ended, far beyond its k-hit radius) adds its hits to that
