@@ -179,6 +179,19 @@ wp_status wp_fit_begin(wp_ctx* ctx, const int16_t* dye_seq, int length,
 wp_status wp_fit_estep(wp_ctx* ctx, wp_fit_sums* out, double* sum_logp,
                        int* num_zero);
 
+/* Batched EM instances: one E-step for each of B models over its own list
+ * of num_reads staged reads (read_idx [B][num_reads], indices into the
+ * reads given to wp_fit_begin, repeats allowed), all in one launch -- the
+ * rounds of bootstrap_fit (fitters/bootstrap-fit.cc:37-93), which the
+ * reference fits one after another.  The models share the staged fit's
+ * channels, timesteps and emission parameters (mu, sig, bg_sig) and have no
+ * interactions; emission fitting must be off.  out [B]; sum_logp and
+ * num_zero [B] (nullable) as wp_fit_estep's.  The context's current model
+ * becomes models[0]. */
+wp_status wp_fit_estep_batch(wp_ctx* ctx, const wp_seq_model* models, int B,
+                             const int32_t* read_idx, int num_reads,
+                             wp_fit_sums* out, double* sum_logp, int* num_zero);
+
 /* E-step kernel choice: 0 (default) one CTA per read with its vectors in
  * shared memory when they fit, else one thread per read; 1 always one
  * thread per read (tests compare the two).  No reference counterpart. */
@@ -282,9 +295,26 @@ wp_status wp_fit_mstep(const wp_fit_sums* sums, int num_channels,
                        const wp_fit_settings* settings, wp_fit_params* next,
                        double* step_size);
 
+/* B fits at once (as wp_hmm_fit each, from the same start): instance b
+ * fits the reads read_idx[b * reads_each .. (b + 1) * reads_each) (indices
+ * into rads [num_reads][T][C], repeats allowed), all instances' E-steps in
+ * one launch per iteration (wp_fit_estep_batch) -- bootstrap_fit's rounds
+ * (fitters/bootstrap-fit.cc:37-93) as concurrent EM instances.  An instance
+ * stops as wp_hmm_fit does; out_params / out_log_ls / out_steps [B]
+ * (out_steps nullable).  Emission fitting is not supported here. */
+wp_status wp_hmm_fit_batch(wp_ctx* ctx, const wp_seq_model* start, int num_timesteps,
+                           const int16_t* dye_seq, int length, const double* rads,
+                           int num_reads, const wp_fit_settings* settings,
+                           double stopping_threshold, double max_runtime, int B,
+                           const int32_t* read_idx, int reads_each,
+                           wp_fit_params* out_params, double* out_log_ls,
+                           double* out_steps);
+
 /* bootstrap_fit (fitters/bootstrap-fit.cc:37-173): num_rounds fits
  * (wp_hmm_fit) on reads resampled with replacement (indices from a 64-bit
  * Mersenne twister seeded with `seed`; the reference seeds from the clock),
+ * run as concurrent EM instances (wp_fit_estep_batch) unless the emission
+ * parameters are fitted too (then one after another),
  * one fit on all reads (out_best, its step size and log-likelihood), and
  * per parameter the bounds of the central confidence_interval of the round
  * results (sorted; lower index floor((1-ci)/2 * rounds), upper floor((1 -

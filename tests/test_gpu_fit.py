@@ -292,3 +292,77 @@ def test_fit_emission_recovers_generating_model(gpu_ctx):
     held, _, _, _ = gpu_ctx.hmm_fit(start, T, seq, rads[:2000], 1e-4, 600.0)
     assert all(h.mu == s.mu and h.sig == s.sig and h.bg_sig == s.bg_sig
                for h, s in zip(held.channel_models, start.channel_models))
+
+
+# ---- batched EM instances (bootstrap rounds at once)
+def _fixture_start():
+    import os
+    z = np.load(os.path.join(GOLDEN, "fit_c2_t8.npz"))
+    C, T = int(z["C"]), int(z["T"])
+    st = z["start"]
+    sm = paper_model(C)
+    (sm.p_edman_failure, sm.p_detach, sm.p_initial_detach, sm.p_initial_detach_decay,
+     sm.p_initial_block, sm.p_cyclic_block) = st[:6]
+    for c in range(C):
+        sm.channel_models[c].p_bleach = st[6 + c]
+        sm.channel_models[c].p_dud = st[6 + C + c]
+    return z, sm, C, T
+
+
+SUM_FIELDS = ["p_edman_failure_num", "p_edman_failure_den", "p_initial_block_num", "p_initial_block_den",
+              "p_cyclic_block_num", "p_cyclic_block_den"]
+
+
+def _sum_vec(s, T, C):
+    v = [getattr(s, f) for f in SUM_FIELDS]
+    v += list(s.p_detach_x[:T - 1]) + list(s.p_detach_n[:T - 1])
+    v += list(s.p_bleach_num[:C]) + list(s.p_bleach_den[:C]) + list(s.p_dud_num[:C]) + list(s.p_dud_den[:C])
+    return np.array(v, np.float64)
+
+
+def test_estep_batch_matches_single_esteps(gpu_ctx):
+    """wp_fit_estep_batch: each instance's expected counts and log P equal a
+    single E-step with that model over that read list (FP64 sums formed in
+    another order: 1e-10 relative)."""
+    import copy
+    z, sm, C, T = _fixture_start()
+    rads, seq = z["rads"], z["seq"]
+    rng = np.random.default_rng(3)
+    models = []
+    for b in range(3):
+        m = copy.deepcopy(sm)
+        m.p_edman_failure *= 1.0 + 0.2 * b
+        m.p_detach *= 1.0 + 0.1 * b
+        for cm in m.channel_models:
+            cm.p_bleach *= 1.0 + 0.15 * b
+        models.append(m)
+    idx = rng.integers(0, len(rads), (3, 150)).astype(np.int32)
+    single = []
+    gpu_ctx.fit_set_emission(False)
+    for b in range(3):
+        gpu_ctx.upload_model(models[b], T)
+        gpu_ctx.fit_begin(seq, rads[idx[b]])
+        single.append(gpu_ctx.fit_estep())
+    gpu_ctx.upload_model(models[0], T)
+    gpu_ctx.fit_begin(seq, rads)
+    gpu_ctx.fit_set_emission(False)
+    out, sl, nz = gpu_ctx.fit_estep_batch(models, idx)
+    for b in range(3):
+        a, e = _sum_vec(out[b], T, C), _sum_vec(single[b][0], T, C)
+        assert np.allclose(a, e, rtol=1e-10, atol=1e-12), (b, np.max(np.abs(a - e) / np.maximum(np.abs(e), 1e-300)))
+        assert abs(sl[b] - single[b][1]) <= 1e-10 * abs(single[b][1]) and nz[b] == single[b][2]
+
+
+def test_fit_batch_matches_sequential_fits(gpu_ctx):
+    """wp_hmm_fit_batch: every instance converges to the fit wp_hmm_fit
+    reaches on the same reads (same iterations; FP64 sums in another order),
+    and the bootstrap's rounds go through it."""
+    z, sm, C, T = _fixture_start()
+    rads, seq = z["rads"], z["seq"]
+    idx = np.random.default_rng(4).integers(0, len(rads), (4, len(rads))).astype(np.int32)
+    fits, lls, steps = gpu_ctx.hmm_fit_batch(sm, T, seq, rads, idx, 1e-5)
+    for b in range(4):
+        f, step, ll, _ = gpu_ctx.hmm_fit(sm, T, seq, rads[idx[b]], 1e-5)
+        assert np.allclose(_params(fits[b]), _params(f), rtol=1e-7, atol=1e-10), b
+        assert abs(lls[b] - ll) <= 1e-9 * abs(ll)
+        assert abs(steps[b] - step) <= 1e-6 * max(step, 1e-12) + 1e-12

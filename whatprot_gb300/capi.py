@@ -38,7 +38,8 @@ EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload"
            "wp_autotune", "wp_mlp_create", "wp_mlp_destroy", "wp_mlp_train",
            "wp_mlp_train_step", "wp_mlp_shape", "wp_mlp_get", "wp_mlp_set", "wp_mlp_logits", "wp_mlp_propose",
            "wp_mlp_hybrid_classify", "wp_mlp_hybrid_classify_device", "wp_dedup_dye_tracks",
-           "wp_simulate_dye_tracks", "wp_dye_tracks_download", "wp_dye_tracks_to_nn"]
+           "wp_simulate_dye_tracks", "wp_dye_tracks_download", "wp_dye_tracks_to_nn", "wp_fit_estep_batch",
+           "wp_hmm_fit_batch"]
 
 
 class WpSeqModel(ctypes.Structure):
@@ -229,6 +230,10 @@ def load_library(path: Optional[str] = None):
     lib.wp_dye_tracks_download.restype = I
     lib.wp_dye_tracks_to_nn.argtypes = [V]
     lib.wp_dye_tracks_to_nn.restype = I
+    lib.wp_fit_estep_batch.argtypes = [V, V, I, V, I, V, V, V]
+    lib.wp_fit_estep_batch.restype = I
+    lib.wp_hmm_fit_batch.argtypes = [V, V, I, V, I, V, I, V, D, D, I, V, I, V, V, V]
+    lib.wp_hmm_fit_batch.restype = I
     LL, U64, F = ctypes.c_longlong, ctypes.c_ulonglong, ctypes.c_float
     lib.wp_mlp_create.argtypes = [V, I, U64, ctypes.POINTER(V)]
     lib.wp_mlp_create.restype = I
@@ -469,6 +474,51 @@ class Context:
         nz = ctypes.c_int(0)
         self._check(self.lib.wp_fit_estep(self.h, ctypes.byref(s), ctypes.byref(sl), ctypes.byref(nz)))
         return s, sl.value, nz.value
+
+    def fit_estep_batch(self, models, read_idx: np.ndarray):
+        """wp_fit_estep_batch: one E-step per model over its row of read_idx
+        (indices into the staged reads): (list of WpFitSums, sum log P [B],
+        reads with P == 0 [B])."""
+        B = len(models)
+        idx = np.ascontiguousarray(read_idx, dtype=np.int32).reshape(B, -1)
+        built = [seq_model_struct(m) for m in models]
+        arr = (WpSeqModel * B)(*[b[0] for b in built])
+        out = (WpFitSums * B)()
+        sl = np.zeros(B, np.float64)
+        nz = np.zeros(B, np.int32)
+        self._check(self.lib.wp_fit_estep_batch(self.h, ctypes.byref(arr), B, _ptr(idx), idx.shape[1],
+                                                ctypes.byref(out), _ptr(sl), _ptr(nz)))
+        return [out[b] for b in range(B)], sl, nz
+
+    def hmm_fit_batch(self, start: SequencingModel, num_timesteps: int, dye_seq, rads: np.ndarray,
+                      read_idx: np.ndarray, stopping_threshold: float, max_runtime: float = 1e300,
+                      holds: Optional[dict] = None):
+        """wp_hmm_fit_batch: B fits from `start` at once, fit b on the reads
+        rads[read_idx[b]]: (fitted SequencingModels, log-likelihoods [B],
+        step sizes [B])."""
+        m, keep = seq_model_struct(start)
+        seq = np.ascontiguousarray(dye_seq, dtype=np.int16)
+        rads = np.ascontiguousarray(rads, dtype=np.float64)
+        idx = np.ascontiguousarray(read_idx, dtype=np.int32)
+        B = idx.shape[0]
+        fs = WpFitSettings()
+        for k, v in (holds or {}).items():
+            if k in ("hold_p_bleach", "hold_p_dud"):
+                arr = getattr(fs, k)
+                for c, h in enumerate(v):
+                    arr[c] = 1 if h else 0
+            else:
+                setattr(fs, k, 1 if v else 0)
+        out = (WpFitParams * B)()
+        lls = np.zeros(B, np.float64)
+        steps = np.zeros(B, np.float64)
+        self._check(self.lib.wp_hmm_fit_batch(self.h, ctypes.byref(m), num_timesteps,
+                                              _ptr(seq) if len(seq) else None, len(seq), _ptr(rads), rads.shape[0],
+                                              ctypes.byref(fs), stopping_threshold, max_runtime, B, _ptr(idx),
+                                              idx.shape[1], ctypes.byref(out), _ptr(lls), _ptr(steps)))
+        self.num_timesteps = num_timesteps
+        self.num_channels = start.num_channels
+        return [self._params_to_model(start, out[b]) for b in range(B)], lls, steps
 
     def hmm_fit(self, start: SequencingModel, num_timesteps: int, dye_seq, rads: np.ndarray,
                 stopping_threshold: float, max_runtime: float = 1e300, holds: Optional[dict] = None,

@@ -226,6 +226,7 @@ struct wp_ctx {
     int fit_dmax = 0;
     std::vector<int16_t> fit_seq;
     DevBuf d_fit_rads, d_fit_lo, d_fit_hi, d_fit_tab, d_fit_scratch, d_fit_sums, d_fit_out, d_fit_logp;
+    DevBuf d_boot_models, d_boot_idx;  // batched EM instances
 
     // kNN training set (unique dye-tracks with sources).
     long long model_version = 0;
@@ -1246,16 +1247,14 @@ wp_status wp_probe_fp32_peak(wp_ctx* ctx, double* tflops) {
     return WP_OK;
 }
 
-wp_status wp_model_upload(wp_ctx* ctx, const wp_seq_model* m, int T) {
-    if (!ctx || !m) return WP_ERR_INVALID;
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    cudaSetDevice(ctx->device);
+// The device model of a sequencing model for T timesteps (no context state).
+wp_status build_dev_model(wp_ctx* ctx, const wp_seq_model* m, int T, DevModel* hp) {
     const int C = m->num_channels;
     if (C < 1 || C > WP_MAX_CHANNELS) return fail(ctx, WP_ERR_UNSUPPORTED, "num_channels out of range 1..4");
     if (T < 1 || T > WP_MAX_TIMESTEPS) return fail(ctx, WP_ERR_UNSUPPORTED, "num_timesteps out of range 1..64");
     if (!m->p_bleach || !m->p_dud || !m->bg_sig || !m->mu || !m->sig)
         return fail(ctx, WP_ERR_INVALID, "null per-channel array");
-    DevModel& h = ctx->hm;
+    DevModel& h = *hp;
     memset(&h, 0, sizeof(h));
     h.C = C;
     h.T = T;
@@ -1263,17 +1262,8 @@ wp_status wp_model_upload(wp_ctx* ctx, const wp_seq_model* m, int T) {
     h.p_ib = (float)m->p_initial_block;
     h.p_cb = (float)m->p_cyclic_block;
     h.has_block = (m->p_initial_block != 0.0 || m->p_cyclic_block != 0.0) ? 1 : 0;
-    for (int t = 0; t < T; t++) {  // DecayingRateModel (decaying-rate-model.cc:47-50)
-        ctx->raw_pdet[t] = m->p_detach + m->p_initial_detach * std::exp(-(double)t * m->p_initial_detach_decay);
-        h.p_det[t] = (float)ctx->raw_pdet[t];
-    }
-    ctx->raw_pf = m->p_edman_failure;
-    ctx->raw_pib = m->p_initial_block;
-    ctx->raw_pcb = m->p_cyclic_block;
-    for (int c = 0; c < C; c++) {
-        ctx->raw_pdud[c] = m->p_dud[c];
-        ctx->raw_pbleach[c] = m->p_bleach[c];
-    }
+    for (int t = 0; t < T; t++)  // DecayingRateModel (decaying-rate-model.cc:47-50)
+        h.p_det[t] = (float)(m->p_detach + m->p_initial_detach * std::exp(-(double)t * m->p_initial_detach_decay));
     h.interacting = 0;
     for (int c = 0; c < C; c++) {
         binomial_table(m->p_dud[c], WP_MAX_DYES_PER_CHANNEL, h.dud[c]);
@@ -1288,6 +1278,26 @@ wp_status wp_model_upload(wp_ctx* ctx, const wp_seq_model* m, int T) {
         }
     }
     wp_fill_emission_tables(h);
+    return WP_OK;
+}
+
+wp_status wp_model_upload(wp_ctx* ctx, const wp_seq_model* m, int T) {
+    if (!ctx || !m) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    DevModel& h = ctx->hm;
+    wp_status st = build_dev_model(ctx, m, T, &h);
+    if (st != WP_OK) return st;
+    const int C = m->num_channels;
+    for (int t = 0; t < T; t++)
+        ctx->raw_pdet[t] = m->p_detach + m->p_initial_detach * std::exp(-(double)t * m->p_initial_detach_decay);
+    ctx->raw_pf = m->p_edman_failure;
+    ctx->raw_pib = m->p_initial_block;
+    ctx->raw_pcb = m->p_cyclic_block;
+    for (int c = 0; c < C; c++) {
+        ctx->raw_pdud[c] = m->p_dud[c];
+        ctx->raw_pbleach[c] = m->p_bleach[c];
+    }
     WP_CUDA(cudaMemcpyAsync(ctx->d_model.p, &h, sizeof(DevModel), cudaMemcpyHostToDevice, ctx->stream),
             "copy model");
     WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync model");
@@ -1583,6 +1593,28 @@ wp_status wp_fit_emission_sums(wp_ctx* ctx, wp_emission_sums* out) {
     return WP_OK;
 }
 
+// Slot layout of wp_fit.cu -> wp_fit_sums.
+void fit_sums_from_slots(const double* sums, int T, int C, wp_fit_sums* out) {
+    memset(out, 0, sizeof(*out));
+    out->p_edman_failure_num = sums[0];
+    out->p_edman_failure_den = sums[1];
+    out->p_initial_block_num = sums[2];
+    out->p_initial_block_den = sums[3];
+    out->p_cyclic_block_num = sums[4];
+    out->p_cyclic_block_den = sums[5];
+    for (int t = 0; t + 1 < T; t++) {
+        out->p_detach_x[t] = sums[6 + 2 * t];
+        out->p_detach_n[t] = sums[7 + 2 * t];
+    }
+    for (int c = 0; c < C; c++) {
+        const int b = 6 + 2 * (T - 1) + 4 * c;
+        out->p_bleach_num[c] = sums[b];
+        out->p_bleach_den[c] = sums[b + 1];
+        out->p_dud_num[c] = sums[b + 2];
+        out->p_dud_den[c] = sums[b + 3];
+    }
+}
+
 wp_status wp_fit_begin(wp_ctx* ctx, const int16_t* dye_seq, int length, const double* rads, int R) {
     if (!ctx || length < 0 || R < 0 || (length > 0 && !dye_seq) || (R > 0 && !rads)) return WP_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
@@ -1718,24 +1750,7 @@ wp_status wp_fit_estep(wp_ctx* ctx, wp_fit_sums* out, double* sum_logp, int* num
     WP_CUDA(cudaMemcpyAsync(sums.data(), ctx->d_fit_out.p, sizeof(double) * nslots, cudaMemcpyDeviceToHost, ctx->stream), "copy sums");
     WP_CUDA(cudaMemcpyAsync(lp.data(), ctx->d_fit_logp.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy logp");
     WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
-    // Slot layout of wp_fit.cu.
-    out->p_edman_failure_num = sums[0];
-    out->p_edman_failure_den = sums[1];
-    out->p_initial_block_num = sums[2];
-    out->p_initial_block_den = sums[3];
-    out->p_cyclic_block_num = sums[4];
-    out->p_cyclic_block_den = sums[5];
-    for (int t = 0; t + 1 < T; t++) {
-        out->p_detach_x[t] = sums[6 + 2 * t];
-        out->p_detach_n[t] = sums[7 + 2 * t];
-    }
-    for (int c = 0; c < C; c++) {
-        const int b = 6 + 2 * (T - 1) + 4 * c;
-        out->p_bleach_num[c] = sums[b];
-        out->p_bleach_den[c] = sums[b + 1];
-        out->p_dud_num[c] = sums[b + 2];
-        out->p_dud_den[c] = sums[b + 3];
-    }
+    fit_sums_from_slots(sums.data(), T, C, out);
     memset(&ctx->fit_emis_last, 0, sizeof(ctx->fit_emis_last));
     if (emis) {
         // slots after the rates: [kind][c][n], kind w / x / xx (wp_fit.cu)
@@ -1755,6 +1770,139 @@ wp_status wp_fit_estep(wp_ctx* ctx, wp_fit_sums* out, double* sum_logp, int* num
     }
     if (sum_logp) *sum_logp = sl;
     if (num_zero) *num_zero = nz;
+    return WP_OK;
+}
+
+wp_status wp_fit_estep_batch(wp_ctx* ctx, const wp_seq_model* models, int B, const int32_t* read_idx, int Rb,
+                             wp_fit_sums* out, double* sum_logp, int* num_zero) {
+    if (!ctx || !models || B < 1 || Rb < 0 || !out || (Rb > 0 && !read_idx)) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if (!ctx->have_fit) return fail(ctx, WP_ERR_STATE, "fit not staged (wp_fit_begin)");
+    const int C = ctx->fit_C, T = ctx->fit_T, R = ctx->fit_R;
+    if (ctx->fit_emission) return fail(ctx, WP_ERR_UNSUPPORTED, "batched E-steps keep the emission parameters fixed");
+    // the instances' models: same shape and emission parameters as the staged
+    // fit (they share the reads' emission factors), no interactions
+    std::vector<DevModel> hm(B);
+    for (int b = 0; b < B; b++) {
+        if (models[b].num_channels != C) return fail(ctx, WP_ERR_INVALID, "model channels differ from the staged reads");
+        wp_status st = build_dev_model(ctx, &models[b], T, &hm[b]);
+        if (st != WP_OK) return st;
+        if (hm[b].interacting) return fail(ctx, WP_ERR_UNSUPPORTED, "the GPU fit does not support channel interactions");
+        for (int c = 0; c < C; c++)
+            if (hm[b].mu[c] != hm[0].mu[c] || hm[b].sig[c] != hm[0].sig[c] || hm[b].bg_sig[c] != hm[0].bg_sig[c])
+                return fail(ctx, WP_ERR_INVALID, "batched instances need the same emission parameters");
+        if (hm[b].has_block != hm[0].has_block)
+            return fail(ctx, WP_ERR_UNSUPPORTED, "batched instances must all block or all not block");
+    }
+    for (long i = 0; i < (long)B * Rb; i++)
+        if (read_idx[i] < 0 || read_idx[i] >= R) return fail(ctx, WP_ERR_INVALID, "read index out of range");
+    for (int b = 0; b < B; b++) {
+        memset(&out[b], 0, sizeof(out[b]));
+        if (sum_logp) sum_logp[b] = 0.0;
+        if (num_zero) num_zero[b] = 0;
+    }
+    if (Rb == 0 || R == 0) return WP_OK;
+    const bool hb = hm[0].has_block != 0;
+    // emission factors of the staged reads, from the shared emission model
+    ctx->hm = hm[0];
+    WP_CUDA(cudaMemcpyAsync(ctx->d_model.p, &hm[0], sizeof(DevModel), cudaMemcpyHostToDevice, ctx->stream), "copy model");
+    ctx->model_version++;
+    const int W = ctx->fit_dmax + 1;
+    const int entries = T * C * W;
+    WP_CUDA(ctx->d_fit_lo.ensure((size_t)R * T * C), "alloc");
+    WP_CUDA(ctx->d_fit_hi.ensure((size_t)R * T * C), "alloc");
+    WP_CUDA(ctx->d_fit_tab.ensure(sizeof(EmitEntry) * (size_t)R * entries), "alloc fit table");
+    {
+        long n = (long)R * T;
+        TimedLaunch tl(ctx, 1);
+        wp_prep_reads_kernel<<<(int)((n + 127) / 128), 128, 0, ctx->stream>>>(
+                ctx->d_model.as<DevModel>(), ctx->d_fit_rads.as<double>(), R, (unsigned)ctx->fit_dmax, DBL_MAX,
+                ctx->d_fit_lo.as<uint8_t>(), ctx->d_fit_hi.as<uint8_t>(), ctx->d_fit_tab.as<EmitEntry>(), entries);
+        ctx->launches++;
+        WP_CUDA(cudaGetLastError(), "fit prep launch");
+    }
+    int S = 1;
+    for (int c = 0; c < C; c++) S *= ctx->fit_D[c] + 1;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int nslots = wp_fit_nslots(T, C, false);
+    const size_t cta_smem = wp_fit_cta_smem_bytes(T, C, S, hb, false);
+    const int cta_per_sm = (long)cta_smem + (long)sizeof(SmemModel) <= (long)ctx->smem_optin
+                                   ? wp_fit_cta_ctas_per_sm(hb, cta_smem)
+                                   : 0;
+    if (cta_per_sm <= 0) return fail(ctx, WP_ERR_UNSUPPORTED, "batched E-steps need the CTA-per-read kernel");
+    // CTAs per instance: the device's resident CTAs shared out, at most one per read
+    const int G = (int)std::max<long>(1, std::min<long>((long)Rb, ((long)sms * cta_per_sm + B - 1) / B));
+    const long grid = (long)G * B;
+    if (grid > INT32_MAX) return fail(ctx, WP_ERR_UNSUPPORTED, "too many batched instances");
+    const long ck_stride = wp_fit_cta_ckpt_floats(T, S, hb);
+    WP_CUDA(ctx->d_fit_scratch.ensure(sizeof(float) * (size_t)grid * ck_stride), "alloc fit checkpoints");
+    WP_CUDA(ctx->d_fit_sums.ensure(sizeof(double) * (size_t)grid * nslots), "alloc fit sums");
+    WP_CUDA(ctx->d_fit_logp.ensure(sizeof(double) * (size_t)B * Rb), "alloc fit logp");
+    WP_CUDA(ctx->d_boot_models.ensure(sizeof(DevModel) * B), "alloc models");
+    WP_CUDA(ctx->d_boot_idx.ensure(sizeof(int) * (size_t)B * Rb), "alloc read lists");
+    WP_CUDA(cudaMemcpyAsync(ctx->d_boot_models.p, hm.data(), sizeof(DevModel) * B, cudaMemcpyHostToDevice,
+                            ctx->stream), "copy models");
+    WP_CUDA(cudaMemcpyAsync(ctx->d_boot_idx.p, read_idx, sizeof(int) * (size_t)B * Rb, cudaMemcpyHostToDevice,
+                            ctx->stream), "copy read lists");
+    FitArgs fa;
+    memset(&fa, 0, sizeof(fa));
+    fa.model = ctx->d_boot_models.as<DevModel>();
+    fa.rads = ctx->d_fit_rads.as<double>();
+    fa.R = Rb;
+    for (int c = 0; c < C; c++) fa.D[c] = ctx->fit_D[c];
+    {
+        int rem[WP_MAX_CHANNELS];
+        for (int c = 0; c < WP_MAX_CHANNELS; c++) rem[c] = ctx->fit_D[c];
+        const int len = (int)ctx->fit_seq.size();
+        for (int e = 0; e < WP_MAX_TIMESTEPS; e++) {
+            int d = e < len ? ctx->fit_seq[e] : -1;
+            fa.dye[e] = (int8_t)d;
+            fa.tot[e] = (uint8_t)(d >= 0 ? rem[d] : 0);  // DyeTrack(e, d)
+            if (d >= 0) rem[d]--;
+        }
+    }
+    fa.tab = ctx->d_fit_tab.as<EmitEntry>();
+    fa.W = W;
+    fa.scratch = ctx->d_fit_scratch.as<float>();
+    fa.sums = ctx->d_fit_sums.as<double>();
+    fa.logp = ctx->d_fit_logp.as<double>();
+    fa.nslots = nslots;
+    fa.emission = 0;
+    fa.inst_ctas = G;
+    fa.read_idx = ctx->d_boot_idx.as<int>();
+    {
+        TimedLaunch tl(ctx, 0);
+        WP_CUDA(wp_launch_fit_cta(hb, (int)grid, cta_smem, ctx->stream, fa, ctx->d_fit_scratch.as<float>(), ck_stride),
+                "fit E-step launch");
+        ctx->launches++;
+    }
+    // per-CTA sums [nslots][grid]; each instance's CTAs summed in CTA order
+    std::vector<double> part((size_t)nslots * grid), lp((size_t)B * Rb);
+    WP_CUDA(cudaMemcpyAsync(part.data(), ctx->d_fit_sums.p, sizeof(double) * part.size(), cudaMemcpyDeviceToHost,
+                            ctx->stream), "copy sums");
+    WP_CUDA(cudaMemcpyAsync(lp.data(), ctx->d_fit_logp.p, sizeof(double) * lp.size(), cudaMemcpyDeviceToHost,
+                            ctx->stream), "copy logp");
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    std::vector<double> sums(nslots);
+    for (int b = 0; b < B; b++) {
+        for (int k = 0; k < nslots; k++) {
+            double acc = 0.0;
+            for (int g = 0; g < G; g++) acc += part[(size_t)k * grid + (size_t)b * G + g];
+            sums[k] = acc;
+        }
+        fit_sums_from_slots(sums.data(), T, C, &out[b]);
+        double sl = 0.0;
+        int nz = 0;
+        for (int r = 0; r < Rb; r++) {
+            const double v = lp[(size_t)b * Rb + r];
+            if (std::isfinite(v)) sl += v;
+            else nz++;
+        }
+        if (sum_logp) sum_logp[b] = sl;
+        if (num_zero) num_zero[b] = nz;
+    }
     return WP_OK;
 }
 

@@ -262,6 +262,12 @@ struct FitArgs {
     double* logp;          // [R] log P per read (nullable)
     int nslots;
     int emission;           // also gather the emission statistics (slots fs_emis)
+    // Batched EM instances (bootstrap rounds): model[i] is instance i's
+    // model, CTAs [i * inst_ctas, (i + 1) * inst_ctas) serve it, and its R
+    // reads are read_idx[i * R .. (i + 1) * R) (indices into rads / tab);
+    // logp is then per (instance, read).  inst_ctas 0: one instance, reads 0..R-1.
+    int inst_ctas;
+    const int* read_idx;
 };
 
 // ---- kNN stage (wp_nn.cu) -------------------------------------------------

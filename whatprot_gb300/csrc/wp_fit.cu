@@ -749,7 +749,12 @@ template <bool HB>
 __global__ void __launch_bounds__(FIT_NT) wp_fit_cta_kernel(FitArgs a, float* ckpt, long ck_stride) {
     __shared__ SmemModel M;
     extern __shared__ __align__(16) unsigned char fit_smem[];
-    const DevModel& m = *a.model;
+    // batched instances: this CTA's instance and its place among the
+    // instance's CTAs
+    const int inst = a.inst_ctas > 0 ? (int)(blockIdx.x / a.inst_ctas) : 0;
+    const long lb = a.inst_ctas > 0 ? (long)(blockIdx.x % a.inst_ctas) : (long)blockIdx.x;
+    const long gs = a.inst_ctas > 0 ? (long)a.inst_ctas : (long)gridDim.x;
+    const DevModel& m = a.model[inst];
     const int T = m.T, C = m.C;
     int W[WP_MAX_CHANNELS], st[WP_MAX_CHANNELS];
     int S = 1;
@@ -795,7 +800,9 @@ __global__ void __launch_bounds__(FIT_NT) wp_fit_cta_kernel(FitArgs a, float* ck
     const float pf = m.pf, qf = 1.0f - m.pf;
     const int BV = 0, CUR = C + 5, F0 = C + 6, F1 = C + 7;
 
-    for (long r = blockIdx.x; r < a.R; r += gridDim.x) {
+    for (long kr = lb; kr < a.R; kr += gs) {
+        const long r = a.read_idx ? (long)a.read_idx[(long)inst * a.R + kr] : kr;  // the read
+        const long ro = a.read_idx ? (long)inst * a.R + kr : kr;                    // its output slot
         const EmitEntry* tab = a.tab + r * (long)T * C * a.W;
         // ---- emission weights per (t, j), normalised by 2^kmax[t]
         for (int t = threadIdx.x; t < T; t += blockDim.x) {
@@ -819,7 +826,7 @@ __global__ void __launch_bounds__(FIT_NT) wp_fit_cta_kernel(FitArgs a, float* ck
         for (int t = 0; t < T; t++)
             if (kmx[t] == WP_EXPO_ZERO) dead = true;
         if (dead) {  // some timestep emits nothing: P = 0
-            if (threadIdx.x == 0 && a.logp) a.logp[r] = -INFINITY;
+            if (threadIdx.x == 0 && a.logp) a.logp[ro] = -INFINITY;
             __syncthreads();
             continue;
         }
@@ -944,14 +951,14 @@ __global__ void __launch_bounds__(FIT_NT) wp_fit_cta_kernel(FitArgs a, float* ck
         }
         const float Ps = vec(BV).A[S - 1];
         if (!(Ps > 0.0f)) {
-            if (threadIdx.x == 0 && a.logp) a.logp[r] = -INFINITY;
+            if (threadIdx.x == 0 && a.logp) a.logp[ro] = -INFINITY;
             __syncthreads();
             continue;
         }
         int EP;
         const float Pm = frexpf(Ps, &EP);
         EP += Eb[0];
-        if (threadIdx.x == 0 && a.logp) a.logp[r] = log((double)Pm) + (double)EP * 0.69314718055994530942;
+        if (threadIdx.x == 0 && a.logp) a.logp[ro] = log((double)Pm) + (double)EP * 0.69314718055994530942;
         auto scale_of = [&](int Ea, int Ebc) { return ldexp(1.0 / (double)Pm, Ea + Ebc - EP); };
 
         // emission statistics of emission t from the buckets (thread 0, FP64)

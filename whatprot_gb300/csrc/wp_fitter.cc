@@ -535,6 +535,109 @@ wp_status wp_hmm_fit(wp_ctx* ctx, const wp_seq_model* start, int T, const int16_
 // confidence bounds from the sorted round results.  The reference seeds its
 // resampling from the clock; here the caller gives the seed (a 64-bit
 // Mersenne twister draws the indices).
+// B EM instances at once (the bootstrap rounds, which fitters/bootstrap-fit.
+// cc:37-93 fits one after another): every iteration one batched E-step of
+// the instances still running (wp_fit_estep_batch, each over its own read
+// list), then each instance's M-step on the host; an instance stops as
+// wp_hmm_fit does (step below the threshold or the time spent), the others
+// go on.  The final log-likelihoods come from one more batched E-step with
+// each instance's fitted model.
+wp_status wp_hmm_fit_batch(wp_ctx* ctx, const wp_seq_model* start, int T, const int16_t* dye_seq, int length,
+                           const double* rads, int R, const wp_fit_settings* settings, double stopping_threshold,
+                           double max_runtime, int B, const int32_t* idx, int R_each, wp_fit_params* out_rounds,
+                           double* out_log_ls, double* out_steps) {
+    if (!ctx || !start || !rads || R < 1 || B < 1 || R_each < 1 || !idx || !out_rounds || !out_log_ls)
+        return WP_ERR_INVALID;
+    if (settings && settings->fit_emission)
+        return wp_internal_fail(ctx, WP_ERR_UNSUPPORTED, "batched fits keep the emission parameters fixed");
+    const int C = start->num_channels;
+    if (C < 1 || C > WP_MAX_CHANNELS) return wp_internal_fail(ctx, WP_ERR_UNSUPPORTED, "num_channels out of range 1..4");
+    if (!start->p_bleach || !start->p_dud || !start->bg_sig || !start->mu || !start->sig)
+        return wp_internal_fail(ctx, WP_ERR_INVALID, "null per-channel array");
+    wp_fit_settings fs;
+    memset(&fs, 0, sizeof(fs));
+    if (settings) fs = *settings;
+    HostModel s0;
+    s0.C = C;
+    s0.p_edman_failure = start->p_edman_failure;
+    s0.p_detach = start->p_detach;
+    s0.p_initial_detach = start->p_initial_detach;
+    s0.p_initial_detach_decay = start->p_initial_detach_decay;
+    s0.p_initial_block = start->p_initial_block;
+    s0.p_cyclic_block = start->p_cyclic_block;
+    for (int c = 0; c < C; c++) {
+        s0.p_bleach[c] = start->p_bleach[c];
+        s0.p_dud[c] = start->p_dud[c];
+        s0.bg_sig[c] = start->bg_sig[c];
+        s0.mu[c] = start->mu[c];
+        s0.sig[c] = start->sig[c];
+    }
+    if (start->interactions) s0.inter.assign(start->interactions, start->interactions + C * C);
+    if (start->flat_interactions) s0.flat.assign(start->flat_interactions, start->flat_interactions + C * C);
+    wp_seq_model v0 = s0.view();
+    wp_status st = wp_model_upload(ctx, &v0, T);
+    if (st != WP_OK) return st;
+    st = wp_fit_begin(ctx, dye_seq, length, rads, R);
+    if (st != WP_OK) return st;
+    st = wp_fit_set_emission(ctx, 0);
+    if (st != WP_OK) return st;
+
+    std::vector<HostModel> cur(B, s0), fin(B, s0);
+    std::vector<double> step(B, 0.0);
+    std::vector<int> active(B);
+    for (int b = 0; b < B; b++) active[b] = b;
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<wp_seq_model> views;
+    std::vector<int32_t> lists;
+    std::vector<wp_fit_sums> sums;
+    while (!active.empty()) {
+        const int A = (int)active.size();
+        views.resize(A);
+        lists.resize((size_t)A * R_each);
+        sums.resize(A);
+        for (int a = 0; a < A; a++) {
+            views[a] = cur[active[a]].view();
+            memcpy(&lists[(size_t)a * R_each], idx + (size_t)active[a] * R_each, sizeof(int32_t) * R_each);
+        }
+        st = wp_fit_estep_batch(ctx, views.data(), A, lists.data(), R_each, sums.data(), nullptr, nullptr);
+        if (st != WP_OK) return st;
+        const double elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        std::vector<int> still;
+        for (int a = 0; a < A; a++) {
+            const int b = active[a];
+            wp_fit_params cp = to_params(cur[b]), nx;
+            st = wp_fit_mstep(&sums[a], C, T, dye_seq, length, (long long)R_each, &cp, &fs, &nx, &step[b]);
+            if (st != WP_OK) return st;
+            HostModel next = cur[b];
+            from_params(nx, &next);
+            if (step[b] < stopping_threshold || elapsed > max_runtime) fin[b] = next;
+            else {
+                cur[b] = next;
+                still.push_back(b);
+            }
+        }
+        active.swap(still);
+    }
+    // log_likelihood of each round's fit on its reads (fitters/hmm-fitter.h:119-142)
+    views.resize(B);
+    sums.resize(B);
+    for (int b = 0; b < B; b++) views[b] = fin[b].view();
+    std::vector<double> sl(B);
+    std::vector<int> nz(B);
+    st = wp_fit_estep_batch(ctx, views.data(), B, idx, R_each, sums.data(), sl.data(), nz.data());
+    if (st != WP_OK) return st;
+    for (int b = 0; b < B; b++) {
+        out_rounds[b] = to_params(fin[b]);
+        for (int c = C; c < WP_MAX_CHANNELS; c++) {
+            out_rounds[b].p_bleach[c] = out_rounds[b].p_dud[c] = 0.0;
+            out_rounds[b].mu[c] = out_rounds[b].sig[c] = out_rounds[b].bg_sig[c] = 0.0;
+        }
+        out_log_ls[b] = nz[b] > 0 ? -INFINITY : sl[b];
+        if (out_steps) out_steps[b] = step[b];
+    }
+    return WP_OK;
+}
+
 wp_status wp_hmm_bootstrap_fit(wp_ctx* ctx, const wp_seq_model* start, int T, const int16_t* dye_seq, int length,
                                const double* rads, int R, const wp_fit_settings* settings, double stopping_threshold,
                                double max_runtime, int num_rounds, double confidence_interval,
@@ -549,18 +652,30 @@ wp_status wp_hmm_bootstrap_fit(wp_ctx* ctx, const wp_seq_model* start, int T, co
     const size_t TC = (size_t)T * C;
     std::mt19937_64 gen(seed);
     std::uniform_int_distribution<int> pick(0, R - 1);  // inclusive bounds, as the reference's
-    std::vector<double> sub((size_t)R * TC);
+    // the rounds' resampled reads (bootstrap-fit.cc:61-70), as index lists
+    std::vector<int32_t> idx((size_t)num_rounds * R);
+    for (size_t i = 0; i < idx.size(); i++) idx[i] = pick(gen);
     double worst = 0.0;
-    for (int i = 0; i < num_rounds; i++) {
-        for (int j = 0; j < R; j++) {
-            const int src = pick(gen);
-            memcpy(&sub[(size_t)j * TC], rads + (size_t)src * TC, sizeof(double) * TC);
-        }
-        double step = 0.0;
-        wp_status st = wp_hmm_fit(ctx, start, T, dye_seq, length, sub.data(), R, settings, stopping_threshold,
-                                  max_runtime, &out_rounds[i], &step, &out_log_ls[i], nullptr);
+    if (!(settings && settings->fit_emission)) {
+        std::vector<double> steps(num_rounds);
+        wp_status st = wp_hmm_fit_batch(ctx, start, T, dye_seq, length, rads, R, settings, stopping_threshold,
+                                        max_runtime, num_rounds, idx.data(), R, out_rounds, out_log_ls,
+                                        steps.data());
         if (st != WP_OK) return st;
-        worst = std::max(worst, step);
+        for (double x : steps) worst = std::max(worst, x);
+    } else {
+        // emission parameters fitted per round: the rounds' emission factors
+        // differ, so they run one after another
+        std::vector<double> sub((size_t)R * TC);
+        for (int i = 0; i < num_rounds; i++) {
+            for (int j = 0; j < R; j++)
+                memcpy(&sub[(size_t)j * TC], rads + (size_t)idx[(size_t)i * R + j] * TC, sizeof(double) * TC);
+            double step = 0.0;
+            wp_status st = wp_hmm_fit(ctx, start, T, dye_seq, length, sub.data(), R, settings, stopping_threshold,
+                                      max_runtime, &out_rounds[i], &step, &out_log_ls[i], nullptr);
+            if (st != WP_OK) return st;
+            worst = std::max(worst, step);
+        }
     }
     double best_step = 0.0, best_ll = 0.0;
     wp_status st = wp_hmm_fit(ctx, start, T, dye_seq, length, rads, R, settings, stopping_threshold, max_runtime,
