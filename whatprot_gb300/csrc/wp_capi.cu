@@ -1832,8 +1832,9 @@ wp_status wp_fit_estep_batch(wp_ctx* ctx, const wp_seq_model* models, int B, con
                                    ? wp_fit_cta_ctas_per_sm(hb, cta_smem)
                                    : 0;
     if (cta_per_sm <= 0) return fail(ctx, WP_ERR_UNSUPPORTED, "batched E-steps need the CTA-per-read kernel");
-    // CTAs per instance: the device's resident CTAs shared out, at most one per read
-    const int G = (int)std::max<long>(1, std::min<long>((long)Rb, ((long)sms * cta_per_sm + B - 1) / B));
+    // CTAs per instance: the device's resident CTAs shared out (rounded down,
+    // so that all CTAs are resident in one wave), at most one per read
+    const int G = (int)std::max<long>(1, std::min<long>((long)Rb, ((long)sms * cta_per_sm) / B));
     const long grid = (long)G * B;
     if (grid > INT32_MAX) return fail(ctx, WP_ERR_UNSUPPORTED, "too many batched instances");
     const long ck_stride = wp_fit_cta_ckpt_floats(T, S, hb);
