@@ -53,6 +53,7 @@ cudaError_t wp_launch_nn_threshold(cudaStream_t s, const NNArgs& a);
 cudaError_t wp_launch_nn_estimate(int DP, cudaStream_t s, const NNArgs& a);
 size_t wp_nn_sort_temp_bytes(int R);
 cudaError_t wp_launch_nn_redo(const NNArgs& a, int* list, int* count, int shift, cudaStream_t s);
+cudaError_t wp_launch_nn_zero_hist(const NNArgs& a, cudaStream_t s);
 cudaError_t wp_launch_nn_sort_queries(const float* rows, int R, int DP, int TC, float* sorted, int* perm,
                                       unsigned long long* keys, int* idx, void* temp, size_t temp_bytes,
                                       cudaStream_t s);
@@ -898,11 +899,20 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
         NNArgs r = a;
         r.slots = list;
         r.R = nredo;
+        // few reads: each entry slice split over enough CTAs to fill the
+        // device, their counts added into the (zeroed) slice histograms
+        const int qb = (nredo + wp_nn_queries_per_block() - 1) / wp_nn_queries_per_block();
+        r.sub = std::max(1, std::min(64, (3 * sms) / std::max(1, qb * a.slices)));
+        if (r.sub > 1) {
+            WP_CUDA(wp_launch_nn_zero_hist(r, ctx->stream), "kNN zero");
+            ctx->launches++;
+        }
         {
             TimedLaunch tl(ctx, 4);
             WP_CUDA(wp_launch_nn_dist(DP, true, ctx->stream, r), "kNN histogram");
             ctx->launches++;
         }
+        r.sub = 0;
         WP_CUDA(wp_launch_nn_threshold(ctx->stream, r), "kNN threshold");
         ctx->launches++;
     }

@@ -301,6 +301,8 @@ struct NNArgs {
     long long* slicecnt;    // [slices][R_all] candidates slice s wrote
     int* qbase;             // [R_all] per query: float bits >> 19 where its bin 1 starts
     const int* slots;       // histogram / threshold over these R queries (null: 0..R-1)
+    int sub;                // histogram: CTAs per entry slice (> 1: each covers a
+                            // part and adds its counts to shist, zeroed first)
     const int* sample;      // [sample_n] entries drawn in proportion to their hits
     int sample_n;
     long long hits_total;   // hits over all entries

@@ -193,8 +193,17 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
     float* box = ten + NN_TE;                                    // [2][DP]
     unsigned* hist = reinterpret_cast<unsigned*>(box + 2 * DP);  // [NN_QPB][NN_NB + 1]
     const int qb = blockIdx.x * NN_QPB;
-    const int s = blockIdx.y;
-    const int e_lo = s * a.slice_len, e_hi = min(a.N, e_lo + a.slice_len);
+    // entry slice s, or with sub-slices part p of it (whole super-tiles)
+    const int sub = a.sub > 1 ? a.sub : 1;
+    const int s = blockIdx.y / sub, part = blockIdx.y % sub;
+    int e_lo = s * a.slice_len, e_hi = min(a.N, e_lo + a.slice_len);
+    if (sub > 1) {
+        const int st = (e_hi - e_lo + NN_TE * NN_SUPER - 1) / (NN_TE * NN_SUPER);  // super-tiles in the slice
+        const int a0 = (int)((long)st * part / sub), a1 = (int)((long)st * (part + 1) / sub);
+        const int lo = e_lo;
+        e_lo = min(e_hi, lo + a0 * NN_TE * NN_SUPER);
+        e_hi = min(e_hi, lo + a1 * NN_TE * NN_SUPER);
+    }
     for (int i = threadIdx.x; i < NN_QPB * (NN_NB + 1); i += blockDim.x) hist[i] = 0u;
     float q[NN_QPT][DP];
     bool valid[NN_QPT];
@@ -273,7 +282,13 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
         const int row = (lq % NN_QPT) * NN_THREADS + lq / NN_QPT;
         if (qb + lq < a.R) {
             const int slot = a.slots ? a.slots[qb + lq] : qb + lq;
-            a.shist[((long)s * a.R_all + a.q0 + slot) * NN_NB + b] = hist[row * (NN_NB + 1) + b];
+            unsigned* dst = &a.shist[((long)s * a.R_all + a.q0 + slot) * NN_NB + b];
+            const unsigned v = hist[row * (NN_NB + 1) + b];
+            if (sub > 1) {
+                if (v) atomicAdd(dst, v);
+            } else {
+                *dst = v;
+            }
         }
     }
 }
@@ -941,7 +956,7 @@ static cudaError_t launch_dist(bool hist, dim3 grid, cudaStream_t s, const NNArg
 cudaError_t wp_launch_nn_dist(int DP, bool hist, cudaStream_t s, const NNArgs& a) {
     const int qblocks = (a.R + NN_QPB - 1) / NN_QPB;
     if (qblocks == 0) return cudaSuccess;
-    const dim3 grid(qblocks, a.slices);
+    const dim3 grid(qblocks, a.slices * (hist && a.sub > 1 ? a.sub : 1));
     switch (DP) {
         case 16: return launch_dist<16>(hist, grid, s, a);
         case 32: return launch_dist<32>(hist, grid, s, a);
@@ -984,6 +999,24 @@ __global__ void wp_nn_redo_kernel(NNArgs a, int* list, int* count, int shift) {
         list[atomicAdd(count, 1)] = q;
         a.qbase[gq] += shift;
     }
+}
+
+// Zero the per-slice histograms of the listed reads (before a sub-sliced pass).
+__global__ void wp_nn_zero_hist_kernel(NNArgs a) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long n = (long)a.slices * a.R * NN_NB;
+    if (i >= n) return;
+    const int b = (int)(i % NN_NB);
+    const long sq = i / NN_NB;
+    const int q = (int)(sq % a.R), s = (int)(sq / a.R);
+    a.shist[((long)s * a.R_all + a.q0 + a.slots[q]) * NN_NB + b] = 0u;
+}
+
+cudaError_t wp_launch_nn_zero_hist(const NNArgs& a, cudaStream_t s) {
+    const long n = (long)a.slices * a.R * NN_NB;
+    if (n == 0) return cudaSuccess;
+    wp_nn_zero_hist_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    return cudaGetLastError();
 }
 
 cudaError_t wp_launch_nn_redo(const NNArgs& a, int* list, int* count, int shift, cudaStream_t s) {
