@@ -327,6 +327,7 @@ __global__ void __launch_bounds__(TK_WARPS * 32) wp_topk_warp_kernel(const float
     extern __shared__ unsigned long long tk_smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned long long* buf = tk_smem + (size_t)warp * TK_CAP;
+    unsigned* hist = reinterpret_cast<unsigned*>(tk_smem + (size_t)TK_WARPS * TK_CAP) + warp * 256;
     const unsigned lt = (1u << lane) - 1u;
     for (long row = (long)blockIdx.x * TK_WARPS + warp; row < R; row += (long)gridDim.x * TK_WARPS) {
         const float* l = logits + row * ld;
@@ -399,18 +400,68 @@ __global__ void __launch_bounds__(TK_WARPS * 32) wp_topk_warp_kernel(const float
         };
         int j0 = 0;
         if (vec4) {  // 16-byte rows: eight float4 per lane in flight
+            // eight independent online-softmax states (one per float4 slot,
+            // so the exponentials do not form one long dependent chain),
+            // merged below; the kept keys of a 1,024-logit chunk are placed
+            // with one warp scan of the lanes' counts (their order in the
+            // buffer does not matter: it is sorted)
             const float4* l4 = reinterpret_cast<const float4*>(l);
+            float mu[8], su[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                mu[u] = -INFINITY;
+                su[u] = 0.0f;
+            }
             for (; j0 + 1024 <= P; j0 += 1024) {
                 float4 v[8];
 #pragma unroll
                 for (int u = 0; u < 8; u++) v[u] = l4[(j0 >> 2) + 32 * u + lane];
+                unsigned km = 0u;
 #pragma unroll
                 for (int u = 0; u < 8; u++) {
-                    const int ja = j0 + 128 * u + 4 * lane;
-                    visit(ja, v[u].x, true);
-                    visit(ja + 1, v[u].y, true);
-                    visit(ja + 2, v[u].z, true);
-                    visit(ja + 3, v[u].w, true);
+                    const float mx = fmaxf(fmaxf(v[u].x, v[u].y), fmaxf(v[u].z, v[u].w));
+                    if (mx > mu[u]) {
+                        su[u] = su[u] * __expf(mu[u] - mx);
+                        mu[u] = mx;
+                    }
+                    su[u] += (__expf(v[u].x - mu[u]) + __expf(v[u].y - mu[u])) +
+                             (__expf(v[u].z - mu[u]) + __expf(v[u].w - mu[u]));
+                    km |= (v[u].x >= tf ? 1u : 0u) << (4 * u);
+                    km |= (v[u].y >= tf ? 1u : 0u) << (4 * u + 1);
+                    km |= (v[u].z >= tf ? 1u : 0u) << (4 * u + 2);
+                    km |= (v[u].w >= tf ? 1u : 0u) << (4 * u + 3);
+                }
+                const int mine = __popc(km);
+                int incl = mine;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                int pos = cnt + incl - mine;
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    unsigned m4 = (km >> (4 * u)) & 15u;
+                    while (m4) {
+                        const int c = __ffs(m4) - 1;
+                        m4 &= m4 - 1;
+                        const float x = c == 0 ? v[u].x : c == 1 ? v[u].y : c == 2 ? v[u].z : v[u].w;
+                        if (pos < TK_CAP)
+                            buf[pos] = ((unsigned long long)fkey(x) << 32) | (unsigned)(j0 + 128 * u + 4 * lane + c);
+                        pos++;
+                    }
+                }
+                cnt += __shfl_sync(0xffffffffu, incl, 31);
+            }
+            // the lane's softmax state from its eight
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                if (mu[u] == -INFINITY) continue;
+                if (mu[u] > m) {
+                    sum = (m == -INFINITY ? 0.0f : sum * __expf(m - mu[u])) + su[u];
+                    m = mu[u];
+                } else {
+                    sum += su[u] * __expf(mu[u] - m);
                 }
             }
         }
@@ -432,9 +483,75 @@ __global__ void __launch_bounds__(TK_WARPS * 32) wp_topk_warp_kernel(const float
             continue;
         }
         __syncwarp();
+        const int hh0 = min(h, P);
+        int nk = cnt;
+        if (cnt > 256 && hh0 <= 256) {
+            // only the h largest keys are needed: the h-th largest by a radix
+            // select over the kept (unique) keys, eight 8-bit digits from the
+            // top, then the keys at or above it moved to the front, so that
+            // the sort below covers 256 keys instead of 512 or 1,024
+            unsigned long long pre = 0ull, msk = 0ull;
+            int want = hh0;
+            for (int pass = 0; pass < 8; pass++) {
+                const int shift = 56 - 8 * pass;
+                for (int i = lane; i < 256; i += 32) hist[i] = 0u;
+                __syncwarp();
+                for (int i = lane; i < cnt; i += 32) {
+                    const unsigned long long k = buf[i];
+                    if ((k & msk) == pre) atomicAdd(&hist[(unsigned)(k >> shift) & 255u], 1u);
+                }
+                __syncwarp();
+                // digits from 255 down: lane l holds [248 - 8 l, 256 - 8 l)
+                int mine = 0;
+#pragma unroll
+                for (int i = 0; i < 8; i++) mine += (int)hist[255 - (lane * 8 + i)];
+                int incl = mine;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                const unsigned hit = __ballot_sync(0xffffffffu, incl >= want);
+                const int L = __ffs(hit) - 1;
+                int before = __shfl_sync(0xffffffffu, incl - mine, L);
+                int digit = 0;
+                if (lane == L) {
+                    int c = before;
+                    for (int i = 0; i < 8; i++) {
+                        const int d = 255 - (L * 8 + i);
+                        if (c + (int)hist[d] >= want) {
+                            digit = d;
+                            break;
+                        }
+                        c += (int)hist[d];
+                    }
+                    before = c;
+                }
+                digit = __shfl_sync(0xffffffffu, digit, L);
+                before = __shfl_sync(0xffffffffu, before, L);
+                want -= before;
+                pre |= (unsigned long long)digit << shift;
+                msk |= 255ull << shift;
+                __syncwarp();
+            }
+            // pre is the h-th largest key: keep the keys >= it (exactly h),
+            // compacted in place (a chunk is read before any lane writes)
+            int out = 0;
+            for (int i0 = 0; i0 < cnt; i0 += 32) {
+                const int i = i0 + lane;
+                const unsigned long long k = i < cnt ? buf[i] : 0ull;
+                const bool keep = i < cnt && k >= pre;
+                const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                __syncwarp();
+                if (keep) buf[out + __popc(bal & ((1u << lane) - 1u))] = k;
+                out += __popc(bal);
+                __syncwarp();
+            }
+            nk = out;
+        }
         int n2 = 1;
-        while (n2 < cnt) n2 <<= 1;
-        for (int i = cnt + lane; i < n2; i += 32) buf[i] = 0ull;
+        while (n2 < nk) n2 <<= 1;
+        for (int i = nk + lane; i < n2; i += 32) buf[i] = 0ull;
         __syncwarp();
         tk_warp_sort_desc(buf, n2);
         // the h largest, written ascending by (logit, index)
@@ -511,7 +628,7 @@ cudaError_t wp_mlp_launch_topk(const float* logits, int R, int P, int ld, int h,
     int* fail_count = fail + R;
     cudaError_t e = cudaMemsetAsync(fail_count, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
-    const size_t smem = sizeof(unsigned long long) * TK_WARPS * TK_CAP;
+    const size_t smem = sizeof(unsigned long long) * TK_WARPS * TK_CAP + sizeof(unsigned) * TK_WARPS * 256;
     int dev = 0;
     cudaGetDevice(&dev);
     // launch shape, once per device
