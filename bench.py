@@ -1196,9 +1196,17 @@ def main():
     fwd_avg_ms = fwd_ms / max(fwd_n, 1)
     flops_per_launch = algo_flops * split_steps / max(fwd_n, 1)
     achieved = flops_per_launch / (fwd_avg_ms * 1e-3) / 1e12 if fwd_n else None
+    # DRAM traffic of the engine passes from one ncu capture of a 5,000-read
+    # batch of this workload (26.9 + 32.1 + 8.4 + 1.6 MB over its four
+    # passes, profiles/wp_engine_kernel_c3t16_5k.md), scaled by the reads
+    # (the traffic is per pair) and spread over this step's forward launches
+    launches_per_step = fwd_n / split_steps if fwd_n else 0.0
+    traffic = (69.0e6 * R / 5000.0) / launches_per_step if launches_per_step else None
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": (achieved / peak) if (achieved and peak) else None, "traffic": None,
-                "kernel": "wp_forward_kernel",
+                "frac": (achieved / peak) if (achieved and peak) else None, "traffic": traffic,
+                "traffic_source": "ncu dram__bytes_read+write of the engine passes at 5,000 reads, scaled to "
+                                  "this batch by reads, per forward launch",
+                "kernel": "wp_engine_kernel (passes 1-4) + wp_dense_kernel",
                 "peak_source": "FP32 FMA loop measured live (wp_probe_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                 "algorithmic_flops_per_step": algo_flops,
                 "unpruned_flops_per_step": float(R) * unpruned_forward_flops(ds.seqs, T, C),
