@@ -243,7 +243,7 @@ struct wp_ctx {
     DevBuf d_nn_coords, d_nn_hits, d_nn_src_off, d_nn_src_dense, d_nn_src_ratio, d_nn_src_hits, d_nn_dense_id,
             d_nn_dense_pep, d_nn_dense_count, d_nn_queries, d_nn_qbin, d_nn_qbase, d_nn_sample, d_nn_qbelow, d_nn_qcap, d_nn_qoff,
             d_nn_cidx, d_nn_cd2, d_nn_chits, d_nn_cbin, d_nn_enorm, d_nn_tlo, d_nn_thi, d_nn_ttot,
-            d_nn_qsorted, d_nn_qperm, d_nn_qkeys, d_nn_qidx, d_nn_qtemp, d_nn_redo, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
+            d_nn_qsorted, d_nn_qperm, d_nn_qkeys, d_nn_qidx, d_nn_qtemp, d_nn_redo, d_nn_stmin, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
             d_nn_cand_score, d_nn_total, d_nn_subfrac, d_nn_cand_off, d_nn_cand_flat, d_nn_err, d_nn_shist,
             d_nn_sliceoff, d_nn_slicecap, d_nn_slicecnt;
 
@@ -864,6 +864,9 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
     WP_CUDA(ctx->d_nn_slicecap.ensure(sizeof(long long) * (size_t)a.slices * R), "alloc");
     WP_CUDA(ctx->d_nn_slicecnt.ensure(sizeof(long long) * (size_t)a.slices * R), "alloc");
     a.shist = ctx->d_nn_shist.as<unsigned>();
+    a.n_super = a.slices * ((a.slice_len + 1023) / 1024);
+    WP_CUDA(ctx->d_nn_stmin.ensure((size_t)R * a.n_super), "alloc kNN super-tile bins");
+    a.stmin = ctx->d_nn_stmin.as<unsigned char>();
     a.sliceoff = ctx->d_nn_sliceoff.as<long long>();
     a.slicecap = ctx->d_nn_slicecap.as<long long>();
     a.slicecnt = ctx->d_nn_slicecnt.as<long long>();

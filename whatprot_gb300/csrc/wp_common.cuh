@@ -303,6 +303,9 @@ struct NNArgs {
     const int* slots;       // histogram / threshold over these R queries (null: 0..R-1)
     int sub;                // histogram: CTAs per entry slice (> 1: each covers a
                             // part and adds its counts to shist, zeroed first)
+    unsigned char* stmin;   // [R_all][n_super] smallest bin of each read's entries per
+    int n_super;            // super-tile (1,024 entries from its slice's start;
+                            // n_super = slices x super-tiles per slice)
     const int* sample;      // [sample_n] entries drawn in proportion to their hits
     int sample_n;
     long long hits_total;   // hits over all entries

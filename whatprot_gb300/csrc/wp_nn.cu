@@ -196,7 +196,9 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
     // entry slice s, or with sub-slices part p of it (whole super-tiles)
     const int sub = a.sub > 1 ? a.sub : 1;
     const int s = blockIdx.y / sub, part = blockIdx.y % sub;
-    int e_lo = s * a.slice_len, e_hi = min(a.N, e_lo + a.slice_len);
+    const int slice0 = s * a.slice_len;
+    const int nsps = (a.slice_len + NN_TE * NN_SUPER - 1) / (NN_TE * NN_SUPER);  // super-tiles per slice
+    int e_lo = slice0, e_hi = min(a.N, e_lo + a.slice_len);
     if (sub > 1) {
         const int st = (e_hi - e_lo + NN_TE * NN_SUPER - 1) / (NN_TE * NN_SUPER);  // super-tiles in the slice
         const int a0 = (int)((long)st * part / sub), a1 = (int)((long)st * (part + 1) / sub);
@@ -229,8 +231,12 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
         // their hits to the read's open last bin
         const int t0 = st0 / NN_TE, nt = min(NN_SUPER, (e_hi - st0 + NN_TE - 1) / NN_TE);
         unsigned nm[NN_QPT];
+        int mb[NN_QPT];  // smallest bin of the read's entries in this super-tile
 #pragma unroll
-        for (int j = 0; j < NN_QPT; j++) nm[j] = 0u;
+        for (int j = 0; j < NN_QPT; j++) {
+            nm[j] = 0u;
+            mb[j] = NN_NB - 1;
+        }
         for (int tt = 0; tt < nt; tt++) {
             const long t = t0 + tt;
 #pragma unroll
@@ -268,10 +274,22 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_hist_kernel(NNArgs a) {
 #pragma unroll
                 for (int j = 0; j < NN_QPT; j++) {
                     const float d2 = nn_d2_dot<DP>(q[j], qn[j], tile + e * DP, ten[e]);
-                    if (need[j])
-                        atomicAdd(&hist[(j * NN_THREADS + threadIdx.x) * (NN_NB + 1) + nn_bin(d2, base[j])],
-                                  (unsigned)thits[e]);
+                    if (need[j]) {
+                        const int bin = nn_bin(d2, base[j]);
+                        mb[j] = min(mb[j], bin);
+                        atomicAdd(&hist[(j * NN_THREADS + threadIdx.x) * (NN_NB + 1) + bin], (unsigned)thits[e]);
+                    }
                 }
+            }
+        }
+        if (a.stmin) {
+            const int sti = s * nsps + (st0 - slice0) / (NN_TE * NN_SUPER);
+#pragma unroll
+            for (int j = 0; j < NN_QPT; j++) {
+                const int lq = threadIdx.x * NN_QPT + j;
+                if (!valid[j]) continue;
+                const int slot = a.slots ? a.slots[qb + lq] : qb + lq;
+                a.stmin[(long)(a.q0 + slot) * a.n_super + sti] = (unsigned char)mb[j];
             }
         }
     }
@@ -421,6 +439,7 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
     const int qb = blockIdx.x * NN_QPB;
     const int s = blockIdx.y;
     const int e_lo = s * a.slice_len, e_hi = min(a.N, e_lo + a.slice_len);
+    const int nsps = (a.slice_len + NN_TE * NN_SUPER - 1) / (NN_TE * NN_SUPER);
     float q[NN_QPT][DP];
     bool valid[NN_QPT];
     int bstar[NN_QPT], base[NN_QPT];
@@ -449,13 +468,22 @@ __global__ void __launch_bounds__(NN_THREADS) wp_nn_collect_kernel(NNArgs a) {
     unsigned* vote = reinterpret_cast<unsigned*>(box);
     for (int st0 = e_lo; st0 < e_hi; st0 += NN_TE * NN_SUPER) {
         const int t0 = st0 / NN_TE, nt = min(NN_SUPER, (e_hi - st0 + NN_TE - 1) / NN_TE);
+        // reads with no entry at or below b* in this super-tile (the
+        // histogram pass's smallest bin) need none of its tiles
+        bool sn[NN_QPT];
+        const int sti = s * nsps + (st0 - e_lo) / (NN_TE * NN_SUPER);
+#pragma unroll
+        for (int j = 0; j < NN_QPT; j++) {
+            const int lq = threadIdx.x * NN_QPT + j;
+            sn[j] = valid[j] && (!a.stmin || (int)a.stmin[(long)(a.q0 + qb + lq) * a.n_super + sti] <= bstar[j]);
+        }
         unsigned wm = 0u;
         for (int tt = 0; tt < nt; tt++) {
             const long t = t0 + tt;
             bool nd = false;
 #pragma unroll
             for (int j = 0; j < NN_QPT; j++)
-                nd |= valid[j] && !nn_clears(nn_box_d2_global<DP>(q[j], a.tlo + t * DP, a.thi + t * DP), lim[j]);
+                nd |= sn[j] && !nn_clears(nn_box_d2_global<DP>(q[j], a.tlo + t * DP, a.thi + t * DP), lim[j]);
             if (nd) wm |= 1u << tt;
         }
         wm = __reduce_or_sync(0xffffffffu, wm);
