@@ -103,3 +103,42 @@ def test_oracle_generator_matches_reference_statistics(oracle):
         assert np.all(np.abs(mean - z["mean"][i]) <= 5 * se), np.max(np.abs(mean - z["mean"][i]) / se)
         p = z["trivial"][i]
         assert abs((n - kept) / n - p) <= 5 * np.sqrt(max(p, 1e-5) * (1 - p) / n) + 1e-5
+
+
+def test_host_dedup_properties():
+    """The host dedup on a larger random set: distinct tracks strictly
+    increasing (lexicographic), sources ascending within a track, hits
+    adding up to the instances, counts those of each id's first instance."""
+    rng = np.random.default_rng(8)
+    n, T, C = 20000, 8, 3
+    tr = np.minimum(rng.geometric(0.5, (n, T, C)) - 1, 4).astype(np.int16)
+    ids = rng.integers(-50, 50, n).astype(np.int32)
+    cnt = rng.integers(1, 6, n).astype(np.int32)
+    d = dedup_dye_tracks(tr, ids, cnt)
+    flat = d.tracks.reshape(len(d), -1).astype(np.int64)
+    diff = flat[1:] - flat[:-1]
+    first = np.argmax(diff != 0, axis=1)
+    assert np.all(diff[np.arange(len(diff)), first] > 0)
+    for u in range(0, len(d), 97):
+        a, b = d.src_off[u], d.src_off[u + 1]
+        assert np.all(np.diff(d.src_id[a:b]) > 0)
+        rows = np.flatnonzero(np.all(tr.reshape(n, -1) == flat[u], axis=1))
+        for sid, sc, sh in zip(d.src_id[a:b], d.src_count[a:b], d.src_hits[a:b]):
+            inst = rows[ids[rows] == sid]
+            assert sh == len(inst) and sc == cnt[inst[0]]
+    assert int(d.src_hits.sum()) == n
+
+
+def test_dye_track_buffers_views():
+    """Reusable download buffers (host side): views of the asked sizes,
+    refusal of a set larger than the buffers or of another shape."""
+    from whatprot_gb300 import capi
+    b = capi.DyeTrackBuffers(10, 20, 4, 3, pinned=False)
+    counts, off, sid, scnt, shit = b.views(7, 12, 4, 3)
+    assert counts.shape == (7, 4, 3) and off.shape == (8,)
+    with pytest.raises(ValueError):
+        b.views(11, 5, 4, 3)
+    with pytest.raises(ValueError):
+        b.views(5, 21, 4, 3)
+    with pytest.raises(ValueError):
+        b.views(5, 5, 3, 3)
