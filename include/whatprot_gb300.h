@@ -357,14 +357,39 @@ wp_status wp_nn_tracks_upload(wp_ctx* ctx, const int16_t* counts, int num_tracks
                               const int32_t* src_off, const int32_t* src_id,
                               const int32_t* src_count, const int32_t* src_hits);
 
+/* Which k-hit set the kNN stage keeps (wp_nn_classify, wp_hybrid_classify).
+ *
+ * WP_NN_KDTREE (the default): the reference's.  NNClassifier searches a
+ * kd-tree built over the dye-tracks in their upload order
+ * (kd-tree/kd-tree.h:36-64, make-node.h:28-80) with a KBest that pops at
+ * most one entry per insertion (kd-tree/k-best.h:26-42), so it keeps the
+ * tracks within the final farthest kept one, which lies at or beyond the
+ * k-th hit.  The library builds the same tree on the host and replays that
+ * search on the GPU, so the kept tracks are the reference's.
+ *
+ * WP_NN_PREFIX: the shortest distance-ordered prefix of the tracks whose
+ * hits reach k (no tree search; faster).  It keeps what KBest keeps when
+ * tracks arrive nearest first. */
+#define WP_NN_KDTREE 0
+#define WP_NN_PREFIX 1
+wp_status wp_nn_set_selection(wp_ctx* ctx, int selection);
+
+/* The kd-tree NNClassifier builds (KDTree's constructor,
+ * kd-tree/kd-tree.h:36-43, make-node.h:28-80) over N entries with
+ * coordinates coords [N][D] (D <= 64) for k: writes the input index of the
+ * entry at each tree position (perm [N]) and the number of nodes.  Host
+ * only; exposed so the build can be checked against the reference's. */
+wp_status wp_nn_kd_tree_order(const double* coords, int N, int D, int k, int32_t* perm,
+                              int* out_num_nodes);
+
 /* NNClassifier::classify(radiometry, h) (classifiers/nn-classifier.cc:
  * 137-203) for R reads ([R][T][C] host doubles divided by mu): the k-hit
- * nearest dye-tracks, Gaussian weights exp(-d^2 / 2 sig^2), per-id scores
- * sum(weight * hits / count), and the top h ids.  Writes per read
- * out_ncand[r] <= h, out_cand_id / out_cand_score [R][h] (ascending score,
- * ties by ascending id) and out_total[r] = sum(weight * hits).  The k-hit
- * set is the shortest distance-ordered prefix whose hits reach k (the
- * reference's kd-tree search can keep a few more far tracks).  h <= 1024. */
+ * nearest dye-tracks (as wp_nn_set_selection picked), Gaussian weights
+ * exp(-d^2 / 2 sig^2), per-id scores sum(weight * hits / count), and the
+ * top h ids.  Writes per read out_ncand[r] <= h, out_cand_id /
+ * out_cand_score [R][h] (ascending score, ties by ascending id; the
+ * reference's heap leaves equal scores unordered) and out_total[r] =
+ * sum(weight * hits).  h <= 1024. */
 wp_status wp_nn_classify(wp_ctx* ctx, const double* rads, int num_reads, int k,
                          double sig, int h, int32_t* out_ncand,
                          int32_t* out_cand_id, double* out_cand_score,
@@ -533,7 +558,8 @@ void* wp_ctx_stream(const wp_ctx* ctx);
 /* Per-kernel timing with CUDA events recorded on the context's stream around
  * every launch while enabled.  kind: 0 forward (and fit E-step), 1 prep,
  * 2 combine, 3 flop count, 4 kNN distances, 5 kNN select, 6 simulator,
- * 7 dye-track dedup (all its kernels and sorts).  wp_timing_read
+ * 7 dye-track dedup (all its kernels and sorts), 8 kNN kd-tree search
+ * replay.  wp_timing_read
  * synchronises and returns the summed duration in ms
  * and the number of launches since the last enable.  No reference
  * counterpart (the reference only prints phase wall times,

@@ -17,6 +17,7 @@
 #include "classifiers/hmm-classifier.h"
 #include "classifiers/hybrid-classifier.h"
 #include "classifiers/nn-classifier.h"
+#include "kd-tree/kd-tree.h"
 #include "common/dye-track.h"
 #include "common/dye-seq.h"
 #include "common/radiometry.h"
@@ -111,9 +112,30 @@ std::vector<TrackData> make_tracks(int T, int C, const int16_t* counts, int N,
     return out;
 }
 
+// An entry for the reference's KDTree template that remembers its input
+// index (the template's requirements, kd-tree/kd-tree.h:22-31).
+struct OrderEntry {
+    std::vector<double> x;
+    int index = 0;
+    int hits = 1;
+    double operator[](int i) const { return x[i]; }
+};
+
 }  // namespace
 
 extern "C" {
+
+// KDTree's constructor (kd-tree/kd-tree.h:36-43) over coords [N][D] for k:
+// the input index of the entry at each position of its permuted vector.
+void ref_kd_tree_order(const double* coords, int N, int D, int k, int32_t* perm) {
+    std::vector<OrderEntry> v(N);
+    for (int i = 0; i < N; i++) {
+        v[i].x.assign(coords + (long)i * D, coords + (long)(i + 1) * D);
+        v[i].index = i;
+    }
+    KDTree<OrderEntry, OrderEntry> tree(k, D, std::move(v));
+    for (int i = 0; i < N; i++) perm[i] = tree.values[i].index;
+}
 
 // NNClassifier (nn-classifier.cc:100-215): for every read, classify(rad, h)
 // into [R][h] (ascending score, *ncand entries) and classify(rad) into

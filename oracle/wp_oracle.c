@@ -1339,10 +1339,20 @@ void wpo_improve_fit_batch(const wpo_model* m, int T, const int16_t* seq,
  * follow LeafNode::consider (kd-tree/leaf-node.h:31-62): FP64, summed in
  * groups of four then singly.
  *
- * Selection.  KBest::insert (kd-tree/k-best.h:26-42) keeps entries while the
- * hits of all but the farthest reach k, popping at most one entry per
- * insertion, so the set it ends with depends on the kd-tree's visiting
- * order.  This restatement keeps the order-independent set KBest holds when
+ * Selection (WPO_NN_KDTREE, the reference's).  KBest::insert
+ * (kd-tree/k-best.h:26-42) keeps entries while the hits of all but the
+ * farthest reach k, popping at most one entry per insertion, so the set it
+ * ends with depends on the kd-tree's visiting order.  The tree is built as
+ * make_node does (kd-tree/make-node.h:28-80: split on the first dimension
+ * of largest range, at the element nth_element of max-min-nth.h:20-116
+ * leaves at the middle, a leaf when either side would hold fewer than k
+ * entries) over the entries in their input order, and searched as
+ * InternalNode::search / LeafNode::search (internal-node.h:39-60,
+ * leaf-node.h:31-62) with a max-heap on (squared distance, tree position):
+ * KDTree keeps the entries in the permuted vector and the heap compares
+ * their addresses on equal distances.
+ *
+ * Selection (WPO_NN_PREFIX): the order-independent set KBest holds when
  * entries arrive nearest first: the shortest prefix of the entries sorted by
  * (squared distance, index) whose hits reach k (all entries if they never
  * do).
@@ -1394,9 +1404,311 @@ void wpo_nn_coords(const wpo_model* m, int T, const int16_t* counts, int N, doub
         }
 }
 
+/* ---- kd-tree (kd-tree/make-node.h, max-min-nth.h) over a permutation of
+ * the entries: pos[i] is the input index of the entry at tree position i. */
+typedef struct {
+    const double* coords;
+    int D;
+    int32_t* pos;
+} kd_arr;
+
+static double kd_val(const kd_arr* a, long i, int s) { return a->coords[(long)a->pos[i] * a->D + s]; }
+
+static void kd_swap(kd_arr* a, long i, long j) {
+    int32_t t = a->pos[i];
+    a->pos[i] = a->pos[j];
+    a->pos[j] = t;
+}
+
+/* partition (max-min-nth.h:20-52): returns the final left cursor and counts
+ * the values equal to the pivot's as the scans meet them. */
+static long kd_partition(kd_arr* a, long begin, long end, int s, long pivot, int* num_eq) {
+    *num_eq = 0;
+    long l = begin, r = end - 1;
+    double pv = kd_val(a, pivot, s);
+    kd_swap(a, pivot, r);
+    while (l < r) {
+        while (l < r) {
+            double lv = kd_val(a, l, s);
+            if (lv == pv) (*num_eq)++;
+            if (lv > pv) {
+                kd_swap(a, l, r);
+                r--;
+                break;
+            }
+            l++;
+        }
+        while (l < r) {
+            double rv = kd_val(a, r, s);
+            if (rv == pv) (*num_eq)++;
+            if (rv <= pv) {
+                kd_swap(a, r, l);
+                l++;
+                break;
+            }
+            r--;
+        }
+    }
+    return l;
+}
+
+/* partition_alternate (max-min-nth.h:54-78): pivot value at end - 1. */
+static void kd_partition_alternate(kd_arr* a, long begin, long end, int s) {
+    long l = begin, r = end - 1;
+    double pv = kd_val(a, r, s);
+    while (l < r) {
+        while (l < r) {
+            if (kd_val(a, l, s) >= pv) {
+                kd_swap(a, l, r);
+                r--;
+                break;
+            }
+            l++;
+        }
+        while (l < r) {
+            if (kd_val(a, r, s) < pv) {
+                kd_swap(a, r, l);
+                l++;
+                break;
+            }
+            r--;
+        }
+    }
+}
+
+/* nth_element (max-min-nth.h:86-107). */
+static long kd_nth_element(kd_arr* a, long begin, long end, int s, long nth) {
+    int num_eq;
+    long pivot = kd_partition(a, begin, end, s, nth, &num_eq);
+    long right = pivot, left = pivot - num_eq;
+    if (left <= nth && nth <= right) {
+        if (nth - left > right - nth) return right + 1;
+        kd_partition_alternate(a, begin, right + 1, s);
+        return left;
+    } else if (nth < left) {
+        kd_partition_alternate(a, begin, right + 1, s);
+        return kd_nth_element(a, begin, left, s, nth);
+    }
+    return kd_nth_element(a, right + 1, end, s, nth);
+}
+
+static int kd_new_node(wpo_kd_tree* t) {
+    if (t->num_nodes == t->cap) {
+        t->cap = t->cap ? 2 * t->cap : 64;
+        t->nodes = (wpo_kd_node*)realloc(t->nodes, sizeof(wpo_kd_node) * t->cap);
+    }
+    return t->num_nodes++;
+}
+
+/* make_node (make-node.h:28-80). */
+static int kd_make_node(wpo_kd_tree* t, kd_arr* a, int k, long begin, long end) {
+    const int D = a->D;
+    double mins[64], maxes[64];
+    for (int i = 0; i < D; i++) {
+        mins[i] = DBL_MAX;
+        maxes[i] = DBL_MIN;
+    }
+    for (long e = begin; e < end; e++)
+        for (int i = 0; i < D; i++) {
+            double v = kd_val(a, e, i);
+            if (v < mins[i]) mins[i] = v;   /* std::min(mins[i], v) */
+            if (maxes[i] < v) maxes[i] = v; /* std::max(maxes[i], v) */
+        }
+    double best = -1.0;
+    int s = -1;
+    for (int i = 0; i < D; i++) {
+        double range = maxes[i] - mins[i];
+        if (range > best) {
+            best = range;
+            s = i;
+        }
+    }
+    long nth = kd_nth_element(a, begin, end, s, begin + (end - begin) / 2);
+    int id = kd_new_node(t);
+    if (nth - begin < k || end - nth < k) {
+        wpo_kd_node* n = &t->nodes[id];
+        memset(n, 0, sizeof(*n));
+        n->leaf = 1;
+        n->begin = (int)begin;
+        n->end = (int)end;
+        return id;
+    }
+    double max_left = DBL_MIN, min_right = DBL_MAX;
+    for (long e = begin; e < nth; e++) {
+        double v = kd_val(a, e, s);
+        if (max_left < v) max_left = v;
+    }
+    for (long e = nth; e < end; e++) {
+        double v = kd_val(a, e, s);
+        if (v < min_right) min_right = v;
+    }
+    int left = kd_make_node(t, a, k, begin, nth);
+    int right = kd_make_node(t, a, k, nth, end);
+    wpo_kd_node* n = &t->nodes[id];
+    memset(n, 0, sizeof(*n));
+    n->s = s;
+    n->left = left;
+    n->right = right;
+    n->max_left = max_left;
+    n->min_right = min_right;
+    n->split = (max_left + min_right) / 2;
+    return id;
+}
+
+int wpo_kd_tree_build(const double* coords, int N, int D, int k, wpo_kd_tree* out) {
+    memset(out, 0, sizeof(*out));
+    if (D > 64) return -1;
+    out->N = N;
+    out->D = D;
+    out->pos = (int32_t*)malloc(sizeof(int32_t) * (N > 0 ? N : 1));
+    for (int i = 0; i < N; i++) out->pos[i] = i;
+    if (N == 0) return 0;
+    kd_arr a = {coords, D, out->pos};
+    out->root = kd_make_node(out, &a, k, 0, N);
+    return 0;
+}
+
+void wpo_kd_tree_free(wpo_kd_tree* t) {
+    free(t->nodes);
+    free(t->pos);
+    memset(t, 0, sizeof(*t));
+}
+
+/* KBest (k-best.h:22-62): a max-heap on (squared distance, tree position),
+ * the order of std::pair<double, E*>. */
+typedef struct {
+    double d;
+    int pos;
+} kb_item;
+
+typedef struct {
+    kb_item* heap;
+    int n, cap;
+    int k, hits;
+    double kth;
+    const int* pos_hits; /* hits of the entry at each tree position */
+} kbest;
+
+static int kb_less(kb_item a, kb_item b) { return a.d < b.d || (!(b.d < a.d) && a.pos < b.pos); }
+
+static void kb_push(kbest* kb, kb_item it) {
+    if (kb->n == kb->cap) {
+        kb->cap = kb->cap ? 2 * kb->cap : 1024;
+        kb->heap = (kb_item*)realloc(kb->heap, sizeof(kb_item) * kb->cap);
+    }
+    int i = kb->n++;
+    while (i > 0) {
+        int p = (i - 1) / 2;
+        if (!kb_less(kb->heap[p], it)) break;
+        kb->heap[i] = kb->heap[p];
+        i = p;
+    }
+    kb->heap[i] = it;
+}
+
+static void kb_pop(kbest* kb) {
+    kb_item last = kb->heap[--kb->n];
+    int i = 0;
+    for (;;) {
+        int c = 2 * i + 1;
+        if (c >= kb->n) break;
+        if (c + 1 < kb->n && kb_less(kb->heap[c], kb->heap[c + 1])) c++;
+        if (!kb_less(last, kb->heap[c])) break;
+        kb->heap[i] = kb->heap[c];
+        i = c;
+    }
+    if (kb->n > 0) kb->heap[i] = last;
+}
+
+/* KBest::insert (k-best.h:26-42). */
+static void kb_insert(kbest* kb, double d, int pos) {
+    kb->hits += kb->pos_hits[pos];
+    kb_item it = {d, pos};
+    kb_push(kb, it);
+    int top_hits = kb->pos_hits[kb->heap[0].pos];
+    if (kb->hits - top_hits >= kb->k) {
+        kb->hits -= top_hits;
+        kb_pop(kb);
+    }
+    if (kb->hits >= kb->k) kb->kth = kb->heap[0].d;
+}
+
+/* LeafNode::consider (leaf-node.h:31-62): FP64, groups of four with the
+ * early exit, then singly. */
+static void kd_consider(const wpo_kd_tree* t, const double* tree_coords, const double* q, int pos,
+                        kbest* kb) {
+    const int D = t->D;
+    const double* x = tree_coords + (long)pos * D;
+    double kth = kb->kth;
+    double d2 = 0.0;
+    int i = 0;
+    while (i < D - 3) {
+        double x1 = q[i] - x[i], x2 = q[i + 1] - x[i + 1];
+        double x3 = q[i + 2] - x[i + 2], x4 = q[i + 3] - x[i + 3];
+        d2 += x1 * x1 + x2 * x2 + x3 * x3 + x4 * x4;
+        if (d2 >= kth) return;
+        i += 4;
+    }
+    while (i < D) {
+        double xx = q[i] - x[i];
+        d2 += xx * xx;
+        i++;
+    }
+    if (d2 >= kth) return;
+    kb_insert(kb, d2, pos);
+}
+
+/* InternalNode::search / LeafNode::search (internal-node.h:39-60,
+ * leaf-node.h:25-29). */
+static void kd_search(const wpo_kd_tree* t, const double* tree_coords, int node, const double* q,
+                      kbest* kb) {
+    const wpo_kd_node* n = &t->nodes[node];
+    if (n->leaf) {
+        for (int p = n->begin; p < n->end; p++) kd_consider(t, tree_coords, q, p, kb);
+        return;
+    }
+    double qv = q[n->s];
+    if (qv < n->split) {
+        kd_search(t, tree_coords, n->left, q, kb);
+        double rd = n->min_right - qv;
+        if (kb->kth > rd * rd) kd_search(t, tree_coords, n->right, q, kb);
+    } else {
+        kd_search(t, tree_coords, n->right, q, kb);
+        double ld = qv - n->max_left;
+        if (kb->kth > ld * ld) kd_search(t, tree_coords, n->left, q, kb);
+    }
+}
+
+int wpo_kd_tree_search(const wpo_kd_tree* t, const double* tree_coords, const int* pos_hits,
+                       const double* q, int k, int32_t* out_pos, double* out_d2, int max_out) {
+    kbest kb;
+    memset(&kb, 0, sizeof(kb));
+    kb.k = k;
+    kb.kth = DBL_MAX;
+    kb.pos_hits = pos_hits;
+    if (t->N > 0) kd_search(t, tree_coords, t->root, q, &kb);
+    /* KBest::fill: farthest first */
+    int n = 0;
+    while (kb.n > 0) {
+        if (n < max_out) {
+            out_pos[n] = kb.heap[0].pos;
+            out_d2[n] = kb.heap[0].d;
+        }
+        n++;
+        kb_pop(&kb);
+    }
+    free(kb.heap);
+    return n;
+}
+
 typedef struct {
     const double* coords;
     int N, D;
+    int selection;
+    /* WPO_NN_KDTREE: the tree, coordinates and hits in tree order */
+    wpo_kd_tree tree;
+    double* tree_coords;
+    int* pos_hits;
     const int32_t *src_off, *src_id, *src_count, *src_hits;
     const int32_t* uniq; /* sorted distinct source ids */
     int U;
@@ -1470,6 +1782,21 @@ static void nn_one(const nn_job* j, int r, nn_cand* cand, double* acc, nn_score*
     const double* q = j->rads + (long)r * j->D;
     const int D = j->D;
     long total_hits = 0;
+    int m = 0;
+    if (j->selection == WPO_NN_KDTREE) {
+        /* KDTree::search then KBest::fill: farthest first; cand[] is kept
+         * nearest first like the prefix path (reversed below). */
+        int32_t* pos = (int32_t*)malloc(sizeof(int32_t) * (j->N > 0 ? j->N : 1));
+        double* d2s = (double*)malloc(sizeof(double) * (j->N > 0 ? j->N : 1));
+        m = wpo_kd_tree_search(&j->tree, j->tree_coords, j->pos_hits, q, j->k, pos, d2s, j->N);
+        for (int i = 0; i < m; i++) {
+            cand[m - 1 - i].d2 = d2s[i];
+            cand[m - 1 - i].idx = j->tree.pos[pos[i]];
+        }
+        free(pos);
+        free(d2s);
+        goto scores;
+    }
     for (int e = 0; e < j->N; e++) {
         const double* x = j->coords + (long)e * D;
         double d2 = 0.0;
@@ -1489,13 +1816,13 @@ static void nn_one(const nn_job* j, int r, nn_cand* cand, double* acc, nn_score*
         cand[e].idx = e;
     }
     qsort(cand, j->N, sizeof(nn_cand), nn_cand_cmp);
-    int m = 0;
     for (; m < j->N;) {
         int e = cand[m].idx;
         for (int s = j->src_off[e]; s < j->src_off[e + 1]; s++) total_hits += j->src_hits[s];
         m++;
         if (total_hits >= j->k) break;
     }
+scores:
     for (int u = 0; u < j->U; u++) acc[u] = 0.0;
     double total = 0.0;
     for (int i = m - 1; i >= 0; i--) { /* farthest first */
@@ -1582,6 +1909,18 @@ static void nn_run_job(nn_job* j, const wpo_model* m, int T, const int16_t* trac
     j->k = k;
     j->h = h;
     j->two_sig_sq = 2.0 * sig * sig;
+    if (j->selection == WPO_NN_KDTREE) {
+        wpo_kd_tree_build(coords, N, j->D, k, &j->tree);
+        j->tree_coords = (double*)malloc(sizeof(double) * ((long)N * j->D + 1));
+        j->pos_hits = (int*)malloc(sizeof(int) * (N > 0 ? N : 1));
+        for (long p = 0; p < N; p++) {
+            int e = j->tree.pos[p];
+            memcpy(j->tree_coords + p * j->D, coords + (long)e * j->D, sizeof(double) * j->D);
+            int hits = 0;
+            for (int s = src_off[e]; s < src_off[e + 1]; s++) hits += src_hits[s];
+            j->pos_hits[p] = hits;
+        }
+    }
     pthread_mutex_init(&j->lock, NULL);
     pthread_t* th = (pthread_t*)calloc(threads, sizeof(pthread_t));
     for (int i = 0; i < threads; i++) pthread_create(&th[i], NULL, nn_worker, j);
@@ -1590,16 +1929,22 @@ static void nn_run_job(nn_job* j, const wpo_model* m, int T, const int16_t* trac
     free(th);
     free(coords);
     free(uniq);
+    if (j->selection == WPO_NN_KDTREE) {
+        wpo_kd_tree_free(&j->tree);
+        free(j->tree_coords);
+        free(j->pos_hits);
+    }
 }
 
 void wpo_nn_classify_batch(const wpo_model* m, int T, const int16_t* track_counts, int N,
                            const int32_t* src_off, const int32_t* src_id,
                            const int32_t* src_count, const int32_t* src_hits,
                            const double* rads, int R, int k, double sig, int h,
-                           int threads, int32_t* out_ncand, int32_t* out_cand_id,
+                           int selection, int threads, int32_t* out_ncand, int32_t* out_cand_id,
                            double* out_cand_score, double* out_total) {
     nn_job j;
     memset(&j, 0, sizeof(j));
+    j.selection = selection;
     j.out_ncand = out_ncand;
     j.out_cand_id = out_cand_id;
     j.out_cand_score = out_cand_score;
@@ -1613,10 +1958,11 @@ void wpo_hybrid_classify_batch(const wpo_model* m, int T, const int16_t* track_c
                                const int32_t* src_count, const int32_t* src_hits,
                                const int16_t* seqs, const int32_t* offsets, const int32_t* ids,
                                const int32_t* counts, int P, const double* rads, int R, int k,
-                               double sig, int h, double dist_cutoff, int threads,
+                               double sig, int h, double dist_cutoff, int selection, int threads,
                                int32_t* out_id, double* out_score, double* out_total) {
     nn_job j;
     memset(&j, 0, sizeof(j));
+    j.selection = selection;
     j.out_ncand = (int32_t*)malloc(sizeof(int32_t) * (R > 0 ? R : 1));
     j.out_cand_id = (int32_t*)malloc(sizeof(int32_t) * ((long)R * h + 1));
     j.out_cand_score = (double*)malloc(sizeof(double) * ((long)R * h + 1));

@@ -154,16 +154,46 @@ void wpo_improve_fit_batch(const wpo_model* m, int T, const int16_t* seq,
 /* KDTEntry coordinates (nn-classifier.cc:59-74): out[(e*T + t)*C + c]. */
 void wpo_nn_coords(const wpo_model* m, int T, const int16_t* counts, int N, double* out);
 
+/* The kd-tree of KDTree (kd-tree/kd-tree.h:36-64, make-node.h:28-80) over
+ * N entries of D <= 64 coordinates coords [N][D]: pos[i] is the input index
+ * of the entry at tree position i (the vector make_node permutes); nodes
+ * as make_node creates them (a leaf holds tree positions [begin, end)). */
+typedef struct {
+    int leaf;
+    int s;            /* split dimension */
+    int begin, end;   /* leaf: tree positions */
+    int left, right;  /* internal: child nodes */
+    double max_left, min_right, split;
+} wpo_kd_node;
+
+typedef struct {
+    int N, D, root, num_nodes, cap;
+    wpo_kd_node* nodes;
+    int32_t* pos;
+} wpo_kd_tree;
+
+int wpo_kd_tree_build(const double* coords, int N, int D, int k, wpo_kd_tree* out);
+void wpo_kd_tree_free(wpo_kd_tree* t);
+/* KDTree::search: tree_coords [N][D] in tree order, pos_hits[i] the hits of
+ * the entry at tree position i; writes the kept tree positions and squared
+ * distances farthest first (KBest::fill) and returns their number. */
+int wpo_kd_tree_search(const wpo_kd_tree* t, const double* tree_coords, const int* pos_hits,
+                       const double* q, int k, int32_t* out_pos, double* out_d2, int max_out);
+
+/* k-hit set selections of the kNN stage */
+#define WPO_NN_KDTREE 0 /* the reference's kd-tree search with KBest */
+#define WPO_NN_PREFIX 1 /* the shortest distance-ordered prefix */
+
 /* NNClassifier::classify(radiometry, h) (nn-classifier.cc:120-203) for R
  * reads over N dye-tracks (counts [N][T][C], sources CSR src_off[N+1]);
  * writes per read the number of candidates (<= h), their ids and scores in
- * ascending score order ([R][h]) and the total score.  The k-hit set is the
- * order-independent one (see wp_oracle.c). */
+ * ascending score order ([R][h]) and the total score.  `selection` picks
+ * the k-hit set (see wp_oracle.c). */
 void wpo_nn_classify_batch(const wpo_model* m, int T, const int16_t* track_counts, int N,
                            const int32_t* src_off, const int32_t* src_id,
                            const int32_t* src_count, const int32_t* src_hits,
                            const double* rads, int R, int k, double sig, int h,
-                           int threads, int32_t* out_ncand, int32_t* out_cand_id,
+                           int selection, int threads, int32_t* out_ncand, int32_t* out_cand_id,
                            double* out_cand_score, double* out_total);
 
 /* HybridClassifier::classify (hybrid-classifier.cc:55-94) for R reads:
@@ -174,7 +204,7 @@ void wpo_hybrid_classify_batch(const wpo_model* m, int T, const int16_t* track_c
                                const int32_t* src_count, const int32_t* src_hits,
                                const int16_t* seqs, const int32_t* offsets, const int32_t* ids,
                                const int32_t* counts, int P, const double* rads, int R, int k,
-                               double sig, int h, double dist_cutoff, int threads,
+                               double sig, int h, double dist_cutoff, int selection, int threads,
                                int32_t* out_id, double* out_score, double* out_total);
 
 /* dedup_dye_tracks (simulation/dedup-dye-tracks.cc:35-141): n dye-tracks

@@ -53,3 +53,27 @@ def gpu_ctx():
     ctx = capi.Context(0)
     yield ctx
     ctx.close()
+
+
+def nn_lists_match(ids_a, sc_a, na, ids_b, sc_b, nb, rel):
+    """Two kNN top-h lists (ids and scores, ascending) name the same
+    candidates: the same number, scores equal to `rel` (of the largest),
+    and the same ids except among those scoring the list's smallest score,
+    where the reference's heap keeps an unspecified subset of equal scores
+    when more tie than fit in h.  Returns (match, boundary_tie)."""
+    if na != nb:
+        return False, False
+    if na == 0:
+        return True, False
+    a, b = np.asarray(sc_a[:na], np.float64), np.asarray(sc_b[:nb], np.float64)
+    sa, sb = np.sort(a), np.sort(b)
+    tol = rel * max(abs(sa[-1]), abs(sb[-1])) + 1e-300
+    if np.any(np.abs(sa - sb) > tol):
+        return False, False
+    lo = sa[0]
+    ia = {int(i) for i, v in zip(ids_a[:na], a) if v > lo + tol}
+    ib = {int(i) for i, v in zip(ids_b[:nb], b) if v > lo + tol}
+    if ia != ib:
+        return False, False
+    tie = {int(i) for i in ids_a[:na]} != {int(i) for i in ids_b[:nb]}
+    return True, tie

@@ -124,6 +124,30 @@ def nn_fixture(name, C, T, P, lmin, lmax, per_peptide, nreads, k, sig, h, cutoff
           float(np.mean(hid == true_ids)), "nn best vs truth", float(np.mean(bid == true_ids)))
 
 
+def nn_wide_fixture(name, C, T, P, lmin, lmax, per_peptide, nreads, k, sig, h, cutoff, seed):
+    """The same at the benchmark's k on a larger training set, too large to
+    store: the dye-tracks are regenerated from the stored dye-seqs by the
+    oracle's seeded, single-threaded simulate dt (wpo_simulate_dt), so the
+    fixture holds the dye-seqs, the seed, the reads and the reference's
+    outputs."""
+    from oracle_lib import Oracle
+    sm = paper_model(C)
+    ds = random_dye_seqs(P, C, lmin, lmax, max_per_channel=5, min_total=1, seed=seed)
+    dts, _ = Oracle().simulate_dt(sm, T, ds, per_peptide, seed + 1)
+    rads, true_ids = simulate_radiometries(sm, ds, T, nreads, seed=seed + 2)
+    ref = Reference()
+    nc, ids, sc, tot, bid, bsc, btot, secs = ref.nn_classify(sm, T, dts, rads, k, sig, h)
+    hid, hsc, htot, hsecs = ref.hybrid_classify(sm, T, dts, ds, rads, k, sig, h, cutoff)
+    flat, off = ragged(ds)
+    np.savez_compressed(os.path.join(HERE, name), C=C, T=T, k=k, sig=sig, h=h, cutoff=cutoff, seqs=flat,
+                        offsets=off, ids=ds.ids, counts=ds.counts, per_peptide=per_peptide, track_seed=seed + 1,
+                        num_tracks=len(dts), rads=rads, true_ids=true_ids, nn_ncand=nc, nn_ids=ids, nn_scores=sc,
+                        nn_total=tot, nn_best_id=bid, nn_best_score=bsc, nn_best_total=btot, hy_id=hid,
+                        hy_score=hsc, hy_total=htot)
+    print(name, len(dts), "tracks,", rads.shape[0], "reads; hybrid top-1 vs truth",
+          float(np.mean(hid == true_ids)), f"nn {secs:.1f}s hybrid {hsecs:.1f}s")
+
+
 def sim_fixture(name, seed):
     """Statistics of the reference's generate_dye_track: per dye-seq the mean
     live dye count per (t, c) and the fraction of undetectable tracks over
@@ -193,6 +217,8 @@ if __name__ == "__main__":
     if "nn" in which:
         nn_fixture("nn_c2_t8.npz", 2, 8, 60, 6, 12, 100, 200, 300, 0.5, 20, 5.0, seed=707)
         nn_fixture("nn_c3_t16.npz", 3, 16, 80, 8, 24, 60, 120, 200, 0.5, 30, 5.0, seed=808)
+    if "nn" in which or "nnwide" in which:
+        nn_wide_fixture("nn_c3_t16_2k.npz", 3, 16, 2000, 8, 30, 100, 100, 10000, 0.5, 200, 5.0, seed=1111)
     if "sim" in which:
         sim_fixture("sim_tracks_c3_t12.npz", seed=909)
     if "dedup" in which:

@@ -134,6 +134,9 @@ def _dedup_call(fn, counts, ids, cnts, canonical):
     return canonical_dye_tracks(oc[:u], off[:u + 1], sid[:ns], scnt[:ns], shits[:ns])
 
 
+SELECTIONS = {"kdtree": 0, "prefix": 1}
+
+
 class Oracle:
     def __init__(self):
         if not os.path.exists(ORACLE_SO):
@@ -163,12 +166,13 @@ class Oracle:
                                      ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
         L.wpo_nn_classify_batch.restype = None
         L.wpo_nn_classify_batch.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int] + [ctypes.c_void_p, ctypes.c_int] \
-            + [ctypes.c_void_p] * 5 + [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int] \
-            + [ctypes.c_void_p] * 4
+            + [ctypes.c_void_p] * 5 + [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int] + [ctypes.c_void_p] * 4
         L.wpo_hybrid_classify_batch.restype = None
         L.wpo_hybrid_classify_batch.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int, ctypes.c_void_p, ctypes.c_int] \
             + [ctypes.c_void_p] * 8 + [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
-                                       ctypes.c_int, ctypes.c_double, ctypes.c_int] + [ctypes.c_void_p] * 3
+                                       ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int] \
+            + [ctypes.c_void_p] * 3
         L.wpo_simulate_dt.restype = ctypes.c_int
         L.wpo_simulate_dt.argtypes = [ctypes.POINTER(WpoModel), ctypes.c_int] + [ctypes.c_void_p] * 4 \
             + [ctypes.c_int, ctypes.c_int, ctypes.c_uint64] + [ctypes.c_void_p] * 7
@@ -241,8 +245,10 @@ class Oracle:
                                 cutoff, threads, _p(out))
         return out
 
-    def nn_classify(self, sm, T, dts, rads, k, sig, h, threads=8):
-        """kNN top-h per read: (ncand [R], ids [R,h], scores [R,h], total [R])."""
+    def nn_classify(self, sm, T, dts, rads, k, sig, h, threads=8, selection="kdtree"):
+        """kNN top-h per read: (ncand [R], ids [R,h], scores [R,h], total [R]).
+        selection: "kdtree" (the reference's kd-tree search and KBest) or
+        "prefix" (the shortest distance-ordered prefix reaching k hits)."""
         m = to_wpo(sm)
         R = rads.shape[0]
         rads = np.ascontiguousarray(rads, dtype=np.float64)
@@ -252,12 +258,12 @@ class Oracle:
         sc = np.zeros((R, h), np.float64)
         tot = np.zeros(R, np.float64)
         self.lib.wpo_nn_classify_batch(ctypes.byref(m), T, _p(tr), len(dts), _p(dts.src_off), _p(dts.src_id),
-                                       _p(dts.src_count), _p(dts.src_hits), _p(rads), R, k, sig, h, threads,
-                                       _p(nc), _p(ids), _p(sc), _p(tot))
+                                       _p(dts.src_count), _p(dts.src_hits), _p(rads), R, k, sig, h,
+                                       SELECTIONS[selection], threads, _p(nc), _p(ids), _p(sc), _p(tot))
         return nc, ids, sc, tot
 
-    def hybrid_classify(self, sm, T, dts, dye_seqs, rads, k, sig, h, cutoff, threads=8):
-        """Hybrid per read: (ids, scores, totals)."""
+    def hybrid_classify(self, sm, T, dts, dye_seqs, rads, k, sig, h, cutoff, threads=8, selection="kdtree"):
+        """Hybrid per read: (ids, scores, totals); selection as nn_classify."""
         m = to_wpo(sm)
         R = rads.shape[0]
         rads = np.ascontiguousarray(rads, dtype=np.float64)
@@ -271,7 +277,7 @@ class Oracle:
         self.lib.wpo_hybrid_classify_batch(ctypes.byref(m), T, _p(tr), len(dts), _p(dts.src_off),
                                            _p(dts.src_id), _p(dts.src_count), _p(dts.src_hits), _p(flat),
                                            _p(off), _p(pid), _p(pc), len(dye_seqs), _p(rads), R, k, sig, h,
-                                           cutoff, threads, _p(oid), _p(osc), _p(otot))
+                                           cutoff, SELECTIONS[selection], threads, _p(oid), _p(osc), _p(otot))
         return oid, osc, otot
 
     def dedup_dye_tracks(self, counts, ids, cnts):

@@ -1,16 +1,22 @@
 """Parity of the GPU kNN stage (wp_nn_classify) and hybrid classifier
 (wp_hybrid_classify) with the oracle and with the reference.
 
-Tolerances.  Distances are FP32 on the GPU and FP64 in the oracle, so the
-entry at the k-hit boundary can differ when two distances agree to about
-1e-6: a read's candidate set must match the oracle's exactly for at least
-98 % of reads, and where it matches, scores and totals must agree to a
-relative 2e-5 (FP32 distances inside exp(-d^2 / 2 sig^2)).  Against the
-reference the k-hit set is allowed to differ (its kd-tree search can keep a
-few more far tracks), so the check there is on decisions: the hybrid's top-1
-id and the kNN best id agree for at least 95 % of reads, and the hybrid's
-scores agree to 1e-5 relative wherever the reference's kNN candidate set
-and total equal ours."""
+Two k-hit selections (wp_nn_set_selection): "kdtree", the reference's
+(its kd-tree built over the tracks in upload order, searched with KBest;
+the default), and "prefix", the shortest distance-ordered prefix reaching k
+hits.  Each is compared with the oracle's restatement of the same selection.
+
+Tolerances.  The kd-tree replay decides every push with FP64 distances
+summed as the reference sums them, so its kept set is the reference's; the
+brute-force collect keeps the same set (FP32 screening, FP64 at the
+boundary).  Near entries' weights are FP64 as in the reference, far ones
+FP32 (below 1e-8 of the largest weight).  So candidate lists must match the
+oracle's / reference's for every read except where the reference's heap
+picks among equal scores at the h-th place (named per read, at most a
+fifth of the reads), with scores within 1e-5 of the list's largest and the
+best score and total within 1e-5 relative.  The prefix selection's boundary
+entry is decided by FP32 distances: its lists must match the oracle's for
+>= 98 % of reads, scores within 2e-5."""
 import numpy as np
 import pytest
 
@@ -21,7 +27,9 @@ from whatprot_gb300.model import DyeSeqSet
 from whatprot_gb300.simulate import paper_model, random_dye_seqs, simulate_dye_track_set, simulate_radiometries
 
 pytestmark = pytest.mark.gpu
-REL = 2e-5
+REL = 2e-5     # prefix selection (FP32 boundary)
+REL_KD = 1e-5  # kd-tree selection
+SELECTIONS = ["kdtree", "prefix"]
 
 
 def _data(C, T, P, per, nreads, seed, inter=False, lmin=6, lmax=16):
@@ -35,20 +43,31 @@ def _data(C, T, P, per, nreads, seed, inter=False, lmin=6, lmax=16):
     return sm, ds, dts, rads, ids
 
 
-def _compare(gpu, ora, what, min_frac=0.98):
+def _compare(gpu, ora, what, selection):
+    """Candidate lists (ids, scores), totals and best scores of two kNN
+    results; returns the reads whose lists differ only by a tie at the h-th
+    place."""
+    from conftest import nn_lists_match
     gnc, gid, gsc, gtot = gpu
     onc, oid, osc, otot = ora
     R = len(gnc)
-    same = 0
+    rel = REL_KD if selection == "kdtree" else REL
+    same, ties = 0, []
     for r in range(R):
-        a = list(gid[r, :gnc[r]])
-        b = list(oid[r, :onc[r]])
-        if gnc[r] == onc[r] and a == b:
-            same += 1
-            assert abs(gtot[r] - otot[r]) <= REL * abs(otot[r]) + 1e-300, (what, r, gtot[r], otot[r])
-            np.testing.assert_allclose(gsc[r, :gnc[r]], osc[r, :onc[r]], rtol=REL, atol=1e-300,
-                                       err_msg=f"{what} read {r}")
-    assert same >= min_frac * R, f"{what}: candidate lists equal for {same}/{R} reads"
+        ok, tie = nn_lists_match(gid[r], gsc[r], gnc[r], oid[r], osc[r], onc[r], rel)
+        if not ok:
+            continue
+        same += 1
+        if tie:
+            ties.append(r)
+        assert abs(gtot[r] - otot[r]) <= rel * abs(otot[r]) + 1e-300, (what, r, gtot[r], otot[r])
+        if gnc[r] > 0:
+            gb, ob = np.max(gsc[r, :gnc[r]]), np.max(osc[r, :onc[r]])
+            assert abs(gb - ob) <= rel * abs(ob) + 1e-300, (what, r, gb, ob)
+    need = R if selection == "kdtree" else 0.98 * R
+    assert same >= need, f"{what}: candidate lists equal for {same}/{R} reads"
+    assert len(ties) <= 0.2 * R, f"{what}: {len(ties)} reads tied at the h-th place"
+    return ties
 
 
 NN_CASES = [
@@ -62,37 +81,50 @@ NN_CASES = [
 ]
 
 
+@pytest.mark.parametrize("selection", SELECTIONS)
 @pytest.mark.parametrize("case", NN_CASES, ids=[f"C{c[0]}T{c[1]}k{c[5]}h{c[7]}{'I' if c[8] else ''}"
                                                  for c in NN_CASES])
-def test_nn_vs_oracle(gpu_ctx, oracle, case):
+def test_nn_vs_oracle(gpu_ctx, oracle, case, selection):
     C, T, P, per, nreads, k, sig, h, inter = case
     sm, ds, dts, rads, _ = _data(C, T, P, per, nreads, seed=100 + C * 7 + T, inter=inter)
     gpu_ctx.upload_model(sm, T)
     gpu_ctx.upload_tracks(dts)
-    g = gpu_ctx.nn_classify(rads, k, sig, h)
-    o = oracle.nn_classify(sm, T, dts, rads, k, sig, h)
-    _compare(g, o, f"kNN {case}")
+    gpu_ctx.set_nn_selection(selection)
+    try:
+        g = gpu_ctx.nn_classify(rads, k, sig, h)
+    finally:
+        gpu_ctx.set_nn_selection("kdtree")
+    o = oracle.nn_classify(sm, T, dts, rads, k, sig, h, selection=selection)
+    _compare(g, o, f"kNN {case} {selection}", selection)
 
 
-def test_hybrid_vs_oracle(gpu_ctx, oracle):
-    """Same k-hit semantics on both sides: top-1 ids equal where the kNN
-    candidate lists are equal (>= 98 % of reads), scores to 2e-5."""
+@pytest.mark.parametrize("selection", SELECTIONS)
+def test_hybrid_vs_oracle(gpu_ctx, oracle, selection):
+    """The same selection on both sides: top-1 ids equal and adjusted scores
+    to 1e-5 (2e-5 prefix) wherever the kNN candidate lists are equal."""
+    from conftest import nn_lists_match
     sm, ds, dts, rads, _ = _data(3, 16, 60, 40, 100, seed=44)
     k, sig, h, cut = 150, 0.5, 30, 5.0
     gpu_ctx.upload_model(sm, 16)
     gpu_ctx.upload_peptides(ds)
     gpu_ctx.upload_tracks(dts)
-    gnc, gid, gsc, gtot = gpu_ctx.nn_classify(rads, k, sig, h)
-    onc, oid, osc, otot = oracle.nn_classify(sm, 16, dts, rads, k, sig, h)
-    hid, hsc, htot = gpu_ctx.hybrid_classify(rads, k, sig, h, cut)
-    oh_id, oh_sc, oh_tot = oracle.hybrid_classify(sm, 16, dts, ds, rads, k, sig, h, cut)
+    gpu_ctx.set_nn_selection(selection)
+    try:
+        gnc, gid, gsc, gtot = gpu_ctx.nn_classify(rads, k, sig, h)
+        hid, hsc, htot = gpu_ctx.hybrid_classify(rads, k, sig, h, cut)
+    finally:
+        gpu_ctx.set_nn_selection("kdtree")
+    onc, oid, osc, otot = oracle.nn_classify(sm, 16, dts, rads, k, sig, h, selection=selection)
+    oh_id, oh_sc, oh_tot = oracle.hybrid_classify(sm, 16, dts, ds, rads, k, sig, h, cut, selection=selection)
+    rel = REL_KD if selection == "kdtree" else REL
     same = 0
     for r in range(len(gnc)):
-        if gnc[r] == onc[r] and np.array_equal(gid[r, :gnc[r]], oid[r, :onc[r]]):
+        ok, tie = nn_lists_match(gid[r], gsc[r], gnc[r], oid[r], osc[r], onc[r], rel)
+        if ok and not tie:
             same += 1
             assert hid[r] == oh_id[r], r
-            assert abs(hsc[r] / htot[r] - oh_sc[r] / oh_tot[r]) <= REL * abs(oh_sc[r] / oh_tot[r]) + 1e-300
-    assert same >= 0.98 * len(gnc)
+            assert abs(hsc[r] / htot[r] - oh_sc[r] / oh_tot[r]) <= rel * abs(oh_sc[r] / oh_tot[r]) + 1e-300
+    assert same >= (0.8 if selection == "kdtree" else 0.98) * len(gnc)
 
 
 def test_nn_deterministic(gpu_ctx):
@@ -105,39 +137,64 @@ def test_nn_deterministic(gpu_ctx):
         assert np.array_equal(x, y)
 
 
-def _fixture(name):
-    z, ds = load_fixture(name)
-    dts = DyeTrackSet(z["tracks"], z["src_off"], z["src_id"], z["src_count"], z["src_hits"])
-    return z, ds, dts
-
-
-@pytest.mark.parametrize("name", ["nn_c2_t8.npz", "nn_c3_t16.npz"])
-def test_nn_and_hybrid_vs_reference(gpu_ctx, name):
-    z, ds, dts = _fixture(name)
-    C, T = int(z["C"]), int(z["T"])
+@pytest.mark.parametrize("name", ["nn_c2_t8.npz", "nn_c3_t16.npz", "nn_c3_t16_2k.npz"])
+def test_nn_and_hybrid_vs_reference(gpu_ctx, oracle, name):
+    """The default (kd-tree) selection against the reference's recorded
+    NNClassifier and HybridClassifier results: candidate lists equal on
+    every read up to ties at the h-th place, best scores and totals within
+    1e-5; hybrid top-1 ids equal and adjusted scores within 1e-5 on every
+    read without such a tie.  nn_c3_t16_2k is the benchmark's k = 10,000
+    on 118,488 tracks (regenerated by the oracle's seeded generator)."""
+    from test_oracle import nn_fixture_inputs
+    z, ds, dts, sm = nn_fixture_inputs(oracle, name)
+    T = int(z["T"])
     k, sig, h, cut = int(z["k"]), float(z["sig"]), int(z["h"]), float(z["cutoff"])
-    sm = paper_model(C)
     rads = z["rads"]
-    R = rads.shape[0]
     gpu_ctx.upload_model(sm, T)
     gpu_ctx.upload_peptides(ds)
     gpu_ctx.upload_tracks(dts)
-    gnc, gid, gsc, gtot = gpu_ctx.nn_classify(rads, k, sig, h)
-    best = np.array([gid[r, gnc[r] - 1] for r in range(R)])
-    assert np.mean(best == z["nn_best_id"]) >= 0.95
+    gpu_ctx.set_nn_selection("kdtree")
+    g = gpu_ctx.nn_classify(rads, k, sig, h)
+    ties = _compare(g, (z["nn_ncand"], z["nn_ids"], z["nn_scores"], z["nn_total"]), f"reference {name}", "kdtree")
     hid, hsc, htot = gpu_ctx.hybrid_classify(rads, k, sig, h, cut)
-    assert np.mean(hid == z["hy_id"]) >= 0.95, np.mean(hid == z["hy_id"])
-    same_set = 0
-    for r in range(R):
-        # the same k-hit set shows as the same candidates with the same total
-        if (gnc[r] == z["nn_ncand"][r] and set(gid[r, :gnc[r]]) == set(z["nn_ids"][r, :gnc[r]])
-                and abs(gtot[r] - z["nn_total"][r]) <= REL * z["nn_total"][r]):
-            same_set += 1
-            if hid[r] == z["hy_id"][r]:
-                adj_g = hsc[r] / htot[r]
-                adj_r = z["hy_score"][r] / z["hy_total"][r]
-                assert abs(adj_g - adj_r) <= 1e-5 * abs(adj_r) + 1e-300, (r, adj_g, adj_r)
-    assert same_set >= 0.3 * R
+    index = {int(i): n for n, i in enumerate(ds.ids)}
+    hmm_ties = []
+    for r in range(len(hid)):
+        if r in ties:
+            continue
+        if hid[r] != z["hy_id"][r]:
+            # the HMM over the same candidates: accepted where the two
+            # peptides' probabilities agree to 1e-5 (the FP32 engine's
+            # tolerance), checked with the oracle's FP64 log P
+            ll = oracle.loglik_all(sm, T, ds, rads[r:r + 1], cut)[0]
+            a, b = index[int(hid[r])], index[int(z["hy_id"][r])]
+            assert abs(ll[a] - ll[b]) <= 1e-5, (name, r, hid[r], z["hy_id"][r], ll[a], ll[b])
+            hmm_ties.append(r)
+        adj_g = hsc[r] / htot[r]
+        adj_r = z["hy_score"][r] / z["hy_total"][r]
+        assert abs(adj_g - adj_r) <= REL_KD * abs(adj_r) + 1e-300, (name, r, adj_g, adj_r)
+    assert len(hmm_ties) <= 0.05 * len(hid), (name, hmm_ties)
+
+
+def test_prefix_selection_vs_reference(gpu_ctx, oracle):
+    """The prefix selection keeps fewer far tracks than the reference: its
+    totals never exceed the reference's, and its hybrid top-1 still agrees
+    for >= 95 % of reads."""
+    from test_oracle import nn_fixture_inputs
+    z, ds, dts, sm = nn_fixture_inputs(oracle, "nn_c2_t8.npz")
+    T = int(z["T"])
+    k, sig, h, cut = int(z["k"]), float(z["sig"]), int(z["h"]), float(z["cutoff"])
+    gpu_ctx.upload_model(sm, T)
+    gpu_ctx.upload_peptides(ds)
+    gpu_ctx.upload_tracks(dts)
+    gpu_ctx.set_nn_selection("prefix")
+    try:
+        gnc, gid, gsc, gtot = gpu_ctx.nn_classify(z["rads"], k, sig, h)
+        hid, _, _ = gpu_ctx.hybrid_classify(z["rads"], k, sig, h, cut)
+    finally:
+        gpu_ctx.set_nn_selection("kdtree")
+    assert np.all(gtot <= z["nn_total"] * (1 + REL))
+    assert np.mean(hid == z["hy_id"]) >= 0.95
 
 
 def test_hybrid_is_knn_then_hmm(gpu_ctx):
@@ -196,8 +253,9 @@ def test_nn_errors(gpu_ctx):
         ctx.close()
 
 
+@pytest.mark.parametrize("selection", SELECTIONS)
 @pytest.mark.parametrize("which", ["k1", "k_all_but_one"])
-def test_nn_threshold_extremes(gpu_ctx, oracle, which):
+def test_nn_threshold_extremes(gpu_ctx, oracle, which, selection):
     """k = 1 (the k-hit radius is the nearest entry's) and k one below every
     hit (the radius is the farthest entry's): the reads' distance bins sit
     at the edges of their estimated windows, the selection stays exact."""
@@ -205,6 +263,10 @@ def test_nn_threshold_extremes(gpu_ctx, oracle, which):
     gpu_ctx.upload_model(sm, 8)
     gpu_ctx.upload_tracks(dts)
     k = 1 if which == "k1" else int(dts.src_hits.sum()) - 1
-    g = gpu_ctx.nn_classify(rads, k, 0.5, 10)
-    o = oracle.nn_classify(sm, 8, dts, rads, k, 0.5, 10)
-    _compare(g, o, f"kNN k={k}")
+    gpu_ctx.set_nn_selection(selection)
+    try:
+        g = gpu_ctx.nn_classify(rads, k, 0.5, 10)
+    finally:
+        gpu_ctx.set_nn_selection("kdtree")
+    o = oracle.nn_classify(sm, 8, dts, rads, k, 0.5, 10, selection=selection)
+    _compare(g, o, f"kNN k={k}", selection)

@@ -44,7 +44,7 @@ def _stale(target, sources):
 def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cc")))
-    headers = sorted(glob.glob(os.path.join(CSRC, "*.cuh"))) + [
+    headers = sorted(glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))) + [
         os.path.join(REPO, "include", "whatprot_gb300.h")]
     cc = nvcc()
     objs = []

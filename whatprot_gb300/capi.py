@@ -39,7 +39,10 @@ EXPORTS = ["wp_ctx_create", "wp_ctx_destroy", "wp_last_error", "wp_model_upload"
            "wp_mlp_train_step", "wp_mlp_shape", "wp_mlp_get", "wp_mlp_set", "wp_mlp_logits", "wp_mlp_propose",
            "wp_mlp_hybrid_classify", "wp_mlp_hybrid_classify_device", "wp_dedup_dye_tracks",
            "wp_simulate_dye_tracks", "wp_dye_tracks_download", "wp_dye_tracks_to_nn", "wp_fit_estep_batch",
-           "wp_hmm_fit_batch"]
+           "wp_hmm_fit_batch", "wp_nn_set_selection", "wp_nn_kd_tree_order"]
+
+# k-hit set of the kNN stage (wp_nn_set_selection)
+NN_SELECTIONS = {"kdtree": 0, "prefix": 1}
 
 
 class WpSeqModel(ctypes.Structure):
@@ -209,6 +212,10 @@ def load_library(path: Optional[str] = None):
     lib.wp_nn_tracks_upload.restype = I
     lib.wp_nn_classify.argtypes = [V, V, I, I, D, I, V, V, V, V]
     lib.wp_nn_classify.restype = I
+    lib.wp_nn_set_selection.argtypes = [V, I]
+    lib.wp_nn_set_selection.restype = I
+    lib.wp_nn_kd_tree_order.argtypes = [V, I, I, I, V, ctypes.POINTER(I)]
+    lib.wp_nn_kd_tree_order.restype = I
     lib.wp_hybrid_classify.argtypes = [V, V, I, I, D, I, D, V, V, V]
     lib.wp_hybrid_classify.restype = I
     lib.wp_hybrid_classify_device.argtypes = [V, V, I, I, D, I, D, V, V, V]
@@ -613,6 +620,14 @@ class Context:
                                                     _ptr(shit)))
         return DyeTrackSet(counts[:U], off[:U + 1], sid[:S], scnt[:S], shit[:S])
 
+    def set_nn_selection(self, selection: str) -> None:
+        """wp_nn_set_selection: "kdtree" (the reference's kd-tree search
+        with KBest, the default) or "prefix" (the shortest distance-ordered
+        prefix reaching k hits)."""
+        if selection not in NN_SELECTIONS:
+            raise ValueError(f"unknown kNN selection {selection!r}")
+        self._check(self.lib.wp_nn_set_selection(self.h, NN_SELECTIONS[selection]))
+
     def nn_classify(self, rads: np.ndarray, k: int, sig: float, h: int):
         """wp_nn_classify: (ncand [R], ids [R,h], scores [R,h], total [R])."""
         rads = np.ascontiguousarray(rads, dtype=np.float64)
@@ -730,7 +745,7 @@ class Context:
         self._check(self.lib.wp_timing_enable(self.h, 1 if on else 0))
 
     KIND_FORWARD, KIND_PREP, KIND_COMBINE, KIND_FLOPS, KIND_KNN_DIST, KIND_KNN_SELECT = 0, 1, 2, 3, 4, 5
-    KIND_SIM, KIND_DEDUP = 6, 7
+    KIND_SIM, KIND_DEDUP, KIND_KNN_TREE = 6, 7, 8
 
     def timing_read(self, kind: int) -> Tuple[float, int]:
         ms = ctypes.c_double()
@@ -845,16 +860,32 @@ class HMMFitter:
         return float("-inf") if nz else sl
 
 
+def kd_tree_order(coords: np.ndarray, k: int):
+    """wp_nn_kd_tree_order (host only): the kd-tree NNClassifier builds
+    over coords [N, D] for k; returns (perm [N], number of nodes), perm[i]
+    the input index of the entry at tree position i."""
+    lib = load_library()
+    x = np.ascontiguousarray(coords, dtype=np.float64)
+    N, D = x.shape
+    perm = np.zeros(max(N, 1), np.int32)
+    nn = ctypes.c_int(0)
+    st = lib.wp_nn_kd_tree_order(_ptr(x), N, D, int(k), _ptr(perm), ctypes.byref(nn))
+    if st != 0:
+        raise WpError(st, STATUS.get(st, str(st)))
+    return perm[:N], nn.value
+
+
 class NNClassifier:
     """Host mirror of NNClassifier (classifiers/nn-classifier.h:60-82) on the
     GPU kNN stage.  The reference's constructor moves the dye-tracks out of
     the caller's vector; this one copies them to the device."""
 
     def __init__(self, num_timesteps: int, num_channels: int, seq_model: SequencingModel, k: int,
-                 sig: float, dye_tracks, device: int = 0):
+                 sig: float, dye_tracks, device: int = 0, selection: str = "kdtree"):
         self.ctx = Context(device)
         self.ctx.upload_model(seq_model, num_timesteps)
         self.ctx.upload_tracks(dye_tracks)
+        self.ctx.set_nn_selection(selection)
         self.k, self.sig = k, sig
 
     def classify(self, radiometries: np.ndarray, h: Optional[int] = None):
@@ -888,11 +919,12 @@ class HybridClassifier:
 
     def __init__(self, num_timesteps: int, num_channels: int, seq_model: SequencingModel,
                  dist_cutoff: float, k: int, sig: float, dye_tracks, h: int, dye_seqs: DyeSeqSet,
-                 device: int = 0):
+                 device: int = 0, selection: str = "kdtree"):
         self.ctx = Context(device)
         self.ctx.upload_model(seq_model, num_timesteps)
         self.ctx.upload_peptides(dye_seqs)
         self.ctx.upload_tracks(dye_tracks)
+        self.ctx.set_nn_selection(selection)
         self.k, self.sig, self.h, self.dist_cutoff = k, sig, h, dist_cutoff
 
     def classify(self, radiometries: np.ndarray):

@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "wp_common.cuh"
+#include "wp_kdtree.h"
 
 // Kernels.
 __global__ void wp_prep_reads_kernel(const DevModel*, const double*, int, unsigned, double,
@@ -58,6 +59,10 @@ cudaError_t wp_launch_nn_sort_queries(const float* rows, int R, int DP, int TC, 
                                       unsigned long long* keys, int* idx, void* temp, size_t temp_bytes,
                                       cudaStream_t s);
 int wp_nn_bins();
+cudaError_t wp_launch_kbest(int grid, cudaStream_t s, const KBArgs& a);
+size_t wp_kbest_smem_bytes(int TC, int NC, int stack_cap, bool inter);
+int wp_kbest_warps_per_cta();
+int wp_kbest_chunk();
 int wp_engine_max_threads();
 cudaError_t wp_launch_sim_reads(const SimParams& p, cudaStream_t s);
 size_t wp_dedup_temp_bytes(int n);
@@ -202,8 +207,8 @@ struct wp_ctx {
         cudaEvent_t a, b;
     };
     std::vector<Timed> timed;
-    double t_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    long long t_n[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double t_ms[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    long long t_n[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     size_t nn_acc_cleared = 0;  // bytes of the kNN accumulators known to be zero
 
     // engine launch shapes (autotuned per shape key) and classify graphs
@@ -246,6 +251,18 @@ struct wp_ctx {
             d_nn_qsorted, d_nn_qperm, d_nn_qkeys, d_nn_qidx, d_nn_qtemp, d_nn_redo, d_nn_stmin, d_nn_acc, d_nn_mark, d_nn_touched, d_nn_ncand, d_nn_cand_id, d_nn_cand_pep,
             d_nn_cand_score, d_nn_total, d_nn_subfrac, d_nn_cand_off, d_nn_cand_flat, d_nn_err, d_nn_shist,
             d_nn_sliceoff, d_nn_slicecap, d_nn_slicecnt;
+    // The device arrays above hold the entries in the order of the kd-tree
+    // NNClassifier builds for k = nn_tree_k (wp_kdtree.cc): tree position p
+    // is input entry nn_perm[p].
+    int nn_selection = WP_NN_KDTREE;
+    long long nn_tree_k = -1;
+    std::vector<int> nn_perm;
+    std::vector<KDNode> nn_nodes;
+    int nn_depth = 0, nn_NC = 0;
+    bool nn_inter = false;
+    DevBuf d_nn_cnt8, d_nn_nodes, d_nn_ctab, d_nn_ecoord, d_nn_llo, d_nn_lhi;
+    // the replay's scratch and results (wp_kbest.cu)
+    DevBuf d_kb_reg, d_kb_prev, d_kb_stage, d_kb_next, d_kb_work, d_kb_tfd, d_kb_tfpos, d_kb_tfflag;
 
     // Per-batch scratch.
     DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_Lpk, d_Upk, d_allow, d_flags, d_table, d_res_mant, d_res_expo,
@@ -684,65 +701,164 @@ int nn_padded_dim(int TC) {
     return -1;
 }
 
-// Entry coordinates for the current model (KDTEntry::operator[],
-// nn-classifier.cc:59-74), as FP32 rows padded with zeros.
-wp_status nn_prepare(wp_ctx* ctx) {
-    const int T = ctx->nn_T, C = ctx->nn_C, N = ctx->nn_N;
-    const int DP = nn_padded_dim(T * C);
-    if (ctx->nn_coords_version != ctx->model_version) {
-        std::vector<float> coords((size_t)std::max(N, 1) * DP, 0.0f);
-        std::vector<float> norms(std::max(N, 1), 0.0f);
-        int cts[WP_MAX_CHANNELS];
-        for (long e = 0; e < N; e++) {
-            for (int t = 0; t < T; t++) {
-                for (int c = 0; c < C; c++) cts[c] = ctx->nn_counts[(e * T + t) * C + c];
-                for (int c = 0; c < C; c++)
-                    coords[e * DP + t * C + c] = (float)host_adjusted_mu(ctx->hm, c, cts);
+// The kNN training set on the device for the current model and k: the
+// entries in the order of the kd-tree NNClassifier builds over them
+// (KDTree's constructor, kd-tree/kd-tree.h:36-43, with KDTEntry's
+// coordinates, nn-classifier.cc:59-74), and with them their FP32
+// coordinates, norms, hits and sources, the boxes of every 32 tree
+// positions and of every leaf, the counts as bytes and the tree itself.
+// Rebuilt when the model (coordinates) or k (leaf size) changes.
+wp_status nn_prepare(wp_ctx* ctx, long long k) {
+    const int T = ctx->nn_T, C = ctx->nn_C, N = ctx->nn_N, TC = T * C;
+    const int DP = nn_padded_dim(TC);
+    if (ctx->nn_coords_version == ctx->model_version && ctx->nn_tree_k == k) return WP_OK;
+    // FP64 coordinates in input order
+    std::vector<double> x64((size_t)std::max(N, 1) * TC, 0.0);
+    int cts[WP_MAX_CHANNELS];
+    int most = 0;
+    bool bytes_ok = true;
+    for (long e = 0; e < N; e++)
+        for (int t = 0; t < T; t++) {
+            for (int c = 0; c < C; c++) {
+                cts[c] = ctx->nn_counts[(e * T + t) * C + c];
+                if (cts[c] < 0 || cts[c] > 255) bytes_ok = false;
+                most = std::max(most, cts[c]);
             }
-            // squared norm in FP32, four partial sums as the kernels form |q|^2
-            float p[4] = {0.f, 0.f, 0.f, 0.f};
-            for (int i = 0; i < DP; i++) p[i % 4] = std::fma(coords[e * DP + i], coords[e * DP + i], p[i % 4]);
-            norms[e] = (p[0] + p[1]) + (p[2] + p[3]);
+            for (int c = 0; c < C; c++) x64[e * TC + t * C + c] = host_adjusted_mu(ctx->hm, c, cts);
         }
-        WP_CUDA(ctx->d_nn_coords.ensure(sizeof(float) * coords.size()), "alloc coords");
-        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_coords.p, coords.data(), sizeof(float) * coords.size(),
-                                cudaMemcpyHostToDevice, ctx->stream), "copy coords");
-        WP_CUDA(ctx->d_nn_enorm.ensure(sizeof(float) * norms.size()), "alloc norms");
-        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_enorm.p, norms.data(), sizeof(float) * norms.size(),
-                                cudaMemcpyHostToDevice, ctx->stream), "copy norms");
-        // per tile of 32 consecutive entries: bounding box of the coordinates
-        // and the tile's hits (the kNN kernels skip tiles far from a read)
-        const int nt = std::max((N + 31) / 32, 1);
-        std::vector<float> tlo((size_t)nt * DP, 0.0f), thi((size_t)nt * DP, 0.0f);
-        std::vector<int> ttot(nt, 0);
-        for (int t = 0; t < (N + 31) / 32; t++) {
-            const int e1 = std::min(N, 32 * t + 32);
-            for (int i = 0; i < DP; i++) {
-                float lo = coords[(size_t)32 * t * DP + i], hi = lo;
-                for (int e = 32 * t + 1; e < e1; e++) {
-                    lo = std::min(lo, coords[(size_t)e * DP + i]);
-                    hi = std::max(hi, coords[(size_t)e * DP + i]);
-                }
-                tlo[(size_t)t * DP + i] = lo;
-                thi[(size_t)t * DP + i] = hi;
-            }
-            long long h = 0;
-            for (int e = 32 * t; e < e1; e++)
-                for (int k = ctx->nn_src_off[e]; k < ctx->nn_src_off[e + 1]; k++) h += ctx->nn_src_hits[k];
-            ttot[t] = (int)std::min<long long>(h, INT32_MAX);
-        }
-        WP_CUDA(ctx->d_nn_tlo.ensure(sizeof(float) * tlo.size()), "alloc tiles");
-        WP_CUDA(ctx->d_nn_thi.ensure(sizeof(float) * thi.size()), "alloc tiles");
-        WP_CUDA(ctx->d_nn_ttot.ensure(sizeof(int) * ttot.size()), "alloc tiles");
-        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_tlo.p, tlo.data(), sizeof(float) * tlo.size(), cudaMemcpyHostToDevice,
-                                ctx->stream), "copy tiles");
-        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_thi.p, thi.data(), sizeof(float) * thi.size(), cudaMemcpyHostToDevice,
-                                ctx->stream), "copy tiles");
-        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_ttot.p, ttot.data(), sizeof(int) * ttot.size(), cudaMemcpyHostToDevice,
-                                ctx->stream), "copy tiles");
-        WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
-        ctx->nn_coords_version = ctx->model_version;
+    const int kk = (int)std::min<long long>(k, INT32_MAX);
+    if (wp_kdtree_build(x64.data(), N, TC, kk, &ctx->nn_perm, &ctx->nn_nodes, &ctx->nn_depth) != 0)
+        return fail(ctx, WP_ERR_UNSUPPORTED, "kNN tree: shape not supported");
+    const std::vector<int>& perm = ctx->nn_perm;
+    // FP32 coordinates and squared norms in tree order
+    std::vector<float> coords((size_t)std::max(N, 1) * DP, 0.0f);
+    std::vector<float> norms(std::max(N, 1), 0.0f);
+    for (long p = 0; p < N; p++) {
+        const long e = perm[p];
+        for (int i = 0; i < TC; i++) coords[p * DP + i] = (float)x64[e * TC + i];
+        // squared norm in FP32, four partial sums as the kernels form |q|^2
+        float q[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int i = 0; i < DP; i++) q[i % 4] = std::fma(coords[p * DP + i], coords[p * DP + i], q[i % 4]);
+        norms[p] = (q[0] + q[1]) + (q[2] + q[3]);
     }
+    // hits and sources in tree order
+    std::vector<int> ehits(std::max(N, 1), 0), off(N + 1, 0);
+    const int S = N > 0 ? ctx->nn_src_off[N] : 0;
+    std::vector<int> dense(std::max(S, 1), 0), shits(std::max(S, 1), 0);
+    std::vector<double> ratio(std::max(S, 1), 0.0);
+    for (int p = 0; p < N; p++) {
+        const int e = perm[p];
+        int o = off[p];
+        long long h = 0;
+        for (int j = ctx->nn_src_off[e]; j < ctx->nn_src_off[e + 1]; j++, o++) {
+            dense[o] = (int)(std::lower_bound(ctx->nn_uniq.begin(), ctx->nn_uniq.end(), ctx->nn_src_id[j]) -
+                             ctx->nn_uniq.begin());
+            ratio[o] = (double)ctx->nn_src_hits[j] / (double)ctx->nn_src_count[j];  // hits / count (nn-classifier.cc:154-158)
+            shits[o] = ctx->nn_src_hits[j];
+            h += ctx->nn_src_hits[j];
+        }
+        off[p + 1] = o;
+        ehits[p] = (int)h;
+    }
+    // 16384 entries by systematic sampling of the cumulative hits (the
+    // midpoint of each of 16384 equal shares): each stands for the same
+    // number of hits, so the kNN search can estimate each read's k-hit
+    // radius from them
+    const int SN = N > 0 ? 16384 : 0;
+    std::vector<int> sample(std::max(SN, 1), 0);
+    {
+        long long cum = 0;
+        int p = 0;
+        for (int j = 0; j < SN; j++) {
+            const long long target = ((2ll * j + 1) * ctx->nn_hits_total) / (2ll * SN);
+            while (p < N - 1 && cum + ehits[p] <= target) cum += ehits[p++];
+            sample[j] = p;
+        }
+    }
+    // per tile of 32 tree positions: bounding box of the coordinates and the
+    // tile's hits (the kNN kernels skip tiles far from a read)
+    const int nt = std::max((N + 31) / 32, 1);
+    std::vector<float> tlo((size_t)nt * DP, 0.0f), thi((size_t)nt * DP, 0.0f);
+    std::vector<int> ttot(nt, 0);
+    for (int t = 0; t < (N + 31) / 32; t++) {
+        const int e1 = std::min(N, 32 * t + 32);
+        for (int i = 0; i < DP; i++) {
+            float lo = coords[(size_t)32 * t * DP + i], hi = lo;
+            for (int e = 32 * t + 1; e < e1; e++) {
+                lo = std::min(lo, coords[(size_t)e * DP + i]);
+                hi = std::max(hi, coords[(size_t)e * DP + i]);
+            }
+            tlo[(size_t)t * DP + i] = lo;
+            thi[(size_t)t * DP + i] = hi;
+        }
+        long long h = 0;
+        for (int e = 32 * t; e < e1; e++) h += ehits[e];
+        ttot[t] = (int)std::min<long long>(h, INT32_MAX);
+    }
+    // per leaf: bounding box
+    const int nn = std::max((int)ctx->nn_nodes.size(), 1);
+    std::vector<float> llo((size_t)nn * DP, 0.0f), lhi((size_t)nn * DP, 0.0f);
+    for (size_t id = 0; id < ctx->nn_nodes.size(); id++) {
+        const KDNode& nd = ctx->nn_nodes[id];
+        if (!nd.leaf) continue;
+        for (int i = 0; i < DP; i++) {
+            float lo = FLT_MAX, hi = -FLT_MAX;
+            for (int p = nd.begin; p < nd.end; p++) {
+                lo = std::min(lo, coords[(size_t)p * DP + i]);
+                hi = std::max(hi, coords[(size_t)p * DP + i]);
+            }
+            llo[id * DP + i] = lo;
+            lhi[id * DP + i] = hi;
+        }
+    }
+    // counts as bytes and the coordinate of each count per channel
+    // (non-interacting models), else FP64 coordinates, in tree order
+    ctx->nn_inter = ctx->hm.interacting != 0;
+    ctx->nn_NC = bytes_ok ? most + 1 : 0;
+    std::vector<uint8_t> cnt8((size_t)std::max(N, 1) * DP, 0);
+    if (bytes_ok)
+        for (long p = 0; p < N; p++)
+            for (int i = 0; i < TC; i++) cnt8[p * DP + i] = (uint8_t)ctx->nn_counts[(long)perm[p] * TC + i];
+    std::vector<double> ctab((size_t)C * std::max(ctx->nn_NC, 1), 0.0);
+    for (int c = 0; c < C; c++)
+        for (int n = 0; n < ctx->nn_NC; n++) {
+            int one[WP_MAX_CHANNELS] = {0, 0, 0, 0};
+            one[c] = n;
+            ctab[(size_t)c * ctx->nn_NC + n] = host_adjusted_mu(ctx->hm, c, one);
+        }
+    std::vector<double> ecoord;
+    if (ctx->nn_inter) {
+        ecoord.assign((size_t)std::max(N, 1) * TC, 0.0);
+        for (long p = 0; p < N; p++)
+            std::memcpy(&ecoord[p * TC], &x64[(size_t)perm[p] * TC], sizeof(double) * TC);
+    }
+    auto up = [&](DevBuf& b, const void* src, size_t bytes) -> cudaError_t {
+        cudaError_t e = b.ensure(std::max<size_t>(bytes, 16));
+        if (e != cudaSuccess) return e;
+        return cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    };
+    WP_CUDA(up(ctx->d_nn_coords, coords.data(), sizeof(float) * coords.size()), "upload kNN coordinates");
+    WP_CUDA(up(ctx->d_nn_enorm, norms.data(), sizeof(float) * norms.size()), "upload kNN norms");
+    WP_CUDA(up(ctx->d_nn_hits, ehits.data(), sizeof(int) * ehits.size()), "upload kNN hits");
+    WP_CUDA(up(ctx->d_nn_src_off, off.data(), sizeof(int) * off.size()), "upload kNN sources");
+    WP_CUDA(up(ctx->d_nn_src_dense, dense.data(), sizeof(int) * dense.size()), "upload kNN sources");
+    WP_CUDA(up(ctx->d_nn_src_ratio, ratio.data(), sizeof(double) * ratio.size()), "upload kNN sources");
+    WP_CUDA(up(ctx->d_nn_src_hits, shits.data(), sizeof(int) * shits.size()), "upload kNN sources");
+    WP_CUDA(up(ctx->d_nn_sample, sample.data(), sizeof(int) * sample.size()), "upload kNN sample");
+    WP_CUDA(up(ctx->d_nn_tlo, tlo.data(), sizeof(float) * tlo.size()), "upload kNN tiles");
+    WP_CUDA(up(ctx->d_nn_thi, thi.data(), sizeof(float) * thi.size()), "upload kNN tiles");
+    WP_CUDA(up(ctx->d_nn_ttot, ttot.data(), sizeof(int) * ttot.size()), "upload kNN tiles");
+    WP_CUDA(up(ctx->d_nn_llo, llo.data(), sizeof(float) * llo.size()), "upload kNN leaves");
+    WP_CUDA(up(ctx->d_nn_lhi, lhi.data(), sizeof(float) * lhi.size()), "upload kNN leaves");
+    WP_CUDA(up(ctx->d_nn_cnt8, cnt8.data(), cnt8.size()), "upload kNN counts");
+    WP_CUDA(up(ctx->d_nn_ctab, ctab.data(), sizeof(double) * ctab.size()), "upload kNN count table");
+    if (ctx->nn_inter) WP_CUDA(up(ctx->d_nn_ecoord, ecoord.data(), sizeof(double) * ecoord.size()), "upload kNN coordinates");
+    if (!ctx->nn_nodes.empty())
+        WP_CUDA(up(ctx->d_nn_nodes, ctx->nn_nodes.data(), sizeof(KDNode) * ctx->nn_nodes.size()), "upload kNN tree");
+    WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    ctx->nn_sample_n = SN;
+    ctx->nn_coords_version = ctx->model_version;
+    ctx->nn_tree_k = k;
     return WP_OK;
 }
 
@@ -778,14 +894,104 @@ wp_status nn_prepare_peptides(wp_ctx* ctx) {
     return WP_OK;
 }
 
+// The reference's k-hit set for R query slots (wp_kbest.cu): per slot the
+// final top of KBest.  Slots whose scratch ran out are replayed again by
+// fewer warps with four times the scratch, then sixteen times.
+wp_status nn_replay(wp_ctx* ctx, const double* d_rads, int R, long long k) {
+    const int T = ctx->nn_T, C = ctx->nn_C, TC = T * C;
+    if (ctx->nn_NC == 0) return fail(ctx, WP_ERR_UNSUPPORTED, "kd-tree kNN needs dye counts in 0..255");
+    const size_t Rz = (size_t)std::max(R, 1);
+    WP_CUDA(ctx->d_kb_tfd.ensure(sizeof(double) * Rz), "alloc");
+    WP_CUDA(ctx->d_kb_tfpos.ensure(sizeof(int) * Rz), "alloc");
+    WP_CUDA(ctx->d_kb_tfflag.ensure(sizeof(int) * Rz), "alloc");
+    WP_CUDA(ctx->d_kb_next.ensure(sizeof(int)), "alloc");
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    KBArgs a;
+    memset(&a, 0, sizeof(a));
+    a.next = ctx->d_kb_next.as<int>();
+    a.qperm = ctx->d_nn_qperm.as<int>();
+    a.rads = d_rads;
+    a.TC = TC;
+    a.C = C;
+    a.DP = nn_padded_dim(TC);
+    a.N = ctx->nn_N;
+    a.k = k;
+    a.cnt = ctx->d_nn_cnt8.as<uint8_t>();
+    a.ctab = ctx->d_nn_ctab.as<double>();
+    a.NC = ctx->nn_NC;
+    a.interact = ctx->nn_inter ? 1 : 0;
+    a.ecoord = ctx->nn_inter ? ctx->d_nn_ecoord.as<double>() : nullptr;
+    a.coords32 = ctx->d_nn_coords.as<float>();
+    a.tlo = ctx->d_nn_tlo.as<float>();
+    a.thi = ctx->d_nn_thi.as<float>();
+    a.llo = ctx->d_nn_llo.as<float>();
+    a.lhi = ctx->d_nn_lhi.as<float>();
+    a.hits = ctx->d_nn_hits.as<int>();
+    a.nodes = ctx->d_nn_nodes.as<KDNode>();
+    a.stack_cap = ctx->nn_depth + 2;
+    a.tf_d = ctx->d_kb_tfd.as<double>();
+    a.tf_pos = ctx->d_kb_tfpos.as<int>();
+    a.tf_flag = ctx->d_kb_tfflag.as<int>();
+    const size_t smem = wp_kbest_smem_bytes(TC, a.NC, a.stack_cap, a.interact != 0);
+    int dev_smem = 0;
+    cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    if (smem > (size_t)dev_smem) return fail(ctx, WP_ERR_UNSUPPORTED, "kd-tree kNN: per-read tables exceed shared memory");
+    const int per_sm = std::max(1, std::min(4, (int)((size_t)dev_smem / smem)));
+    const int ch = wp_kbest_chunk();
+    std::vector<int> redo;
+    for (int round = 0; round < 3; round++) {
+        // live entries stay below about k plus the extras KBest keeps
+        const long long grow = 1ll << (2 * round);
+        const long long stage = std::min<long long>((std::max<long long>(32768, 2 * k + 8192)) * grow, 1ll << 26);
+        a.stagecap = (int)stage;
+        a.regcap = (int)(((2 * stage + 2048ll * ch) + ch - 1) / ch * ch);
+        if (a.regcap / ch > 65535) a.regcap = 65535 * ch;
+        int grid = sms * per_sm;
+        if (round > 0) grid = std::max(1, std::min(grid, ((int)redo.size() + 3) / 4));
+        const long warps = (long)grid * wp_kbest_warps_per_cta();
+        WP_CUDA(ctx->d_kb_reg.ensure(sizeof(KBItem) * 2 * (size_t)a.regcap * warps), "alloc kNN replay scratch");
+        WP_CUDA(ctx->d_kb_prev.ensure(sizeof(int) * 2 * (size_t)(a.regcap / ch) * warps), "alloc kNN replay scratch");
+        WP_CUDA(ctx->d_kb_stage.ensure(sizeof(KBItem) * (size_t)a.stagecap * warps), "alloc kNN replay scratch");
+        a.reg = ctx->d_kb_reg.as<KBItem>();
+        a.prev = ctx->d_kb_prev.as<int>();
+        a.stage = ctx->d_kb_stage.as<KBItem>();
+        if (round == 0) {
+            a.nwork = R;
+            a.work = nullptr;
+        } else {
+            WP_CUDA(ctx->d_kb_work.ensure(sizeof(int) * redo.size()), "alloc");
+            WP_CUDA(cudaMemcpyAsync(ctx->d_kb_work.p, redo.data(), sizeof(int) * redo.size(), cudaMemcpyHostToDevice,
+                                    ctx->stream), "copy");
+            a.nwork = (int)redo.size();
+            a.work = ctx->d_kb_work.as<int>();
+        }
+        WP_CUDA(cudaMemsetAsync(a.next, 0, sizeof(int), ctx->stream), "clear");
+        {
+            TimedLaunch tl(ctx, 8);
+            WP_CUDA(wp_launch_kbest(grid, ctx->stream, a), "kNN kd-tree replay");
+            ctx->launches++;
+        }
+        std::vector<int> flags(R);
+        WP_CUDA(cudaMemcpyAsync(flags.data(), a.tf_flag, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream), "copy");
+        WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+        redo.clear();
+        for (int r = 0; r < R; r++)
+            if (flags[r] & 4) redo.push_back(r);
+        if (redo.empty()) return WP_OK;
+    }
+    return fail(ctx, WP_ERR_UNSUPPORTED, "kd-tree kNN: replay scratch exhausted");
+}
+
 // The kNN stage for R reads already on the device (FP64 [R][T][C]):
 // per read the top-h candidates in ascending (score, id) order, the total
 // and, when hybrid, candidate peptide indices and the subfraction.
 wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, int h, bool hybrid) {
     const int T = ctx->nn_T, C = ctx->nn_C, N = ctx->nn_N;
     const int DP = nn_padded_dim(T * C);
-    wp_status st = nn_prepare(ctx);
+    wp_status st = nn_prepare(ctx, k);
     if (st != WP_OK) return st;
+    const bool exact = ctx->nn_selection == WP_NN_KDTREE;
     if (hybrid) {
         st = nn_prepare_peptides(ctx);
         if (st != WP_OK) return st;
@@ -828,6 +1034,10 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
                 "sort queries");
         ctx->launches += 3;
     }
+    if (exact) {
+        st = nn_replay(ctx, d_rads, R, k);
+        if (st != WP_OK) return st;
+    }
     NNArgs a;
     memset(&a, 0, sizeof(a));
     a.coords = ctx->d_nn_coords.as<float>();
@@ -846,6 +1056,8 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
     a.sample = ctx->d_nn_sample.as<int>();
     a.sample_n = ctx->nn_sample_n;
     a.hits_total = ctx->nn_hits_total;
+    a.tf_d = exact ? ctx->d_kb_tfd.as<double>() : nullptr;
+    a.tf_flag = exact ? ctx->d_kb_tfflag.as<int>() : nullptr;
     // Entry slices: enough CTAs (query blocks x slices) for two waves of
     // three CTAs per SM, each slice at least 1024 entries.
     int sms = 0;
@@ -1009,6 +1221,30 @@ wp_status nn_run(wp_ctx* ctx, const double* d_rads, int R, int k, double sig, in
         b.out_cand_score = ctx->d_nn_cand_score.as<double>();
         b.out_total = ctx->d_nn_total.as<double>();
         b.out_subfrac = hybrid ? ctx->d_nn_subfrac.as<double>() : nullptr;
+        b.two_sig_sq = 2.0 * sig * sig;
+        if (ctx->nn_NC > 0) {
+            b.rads = d_rads;
+            b.TC = T * C;
+            b.C = C;
+            b.DP = DP;
+            b.NC = ctx->nn_NC;
+            b.cnt = ctx->d_nn_cnt8.as<uint8_t>();
+            b.ctab = ctx->d_nn_ctab.as<double>();
+            b.ecoord = ctx->nn_inter ? ctx->d_nn_ecoord.as<double>() : nullptr;
+        }
+        if (exact) {
+            b.tf_d = ctx->d_kb_tfd.as<double>();
+            b.tf_pos = ctx->d_kb_tfpos.as<int>();
+            b.tf_flag = ctx->d_kb_tfflag.as<int>();
+            b.rads = d_rads;
+            b.TC = T * C;
+            b.C = C;
+            b.DP = DP;
+            b.NC = ctx->nn_NC;
+            b.cnt = ctx->d_nn_cnt8.as<uint8_t>();
+            b.ctab = ctx->d_nn_ctab.as<double>();
+            b.ecoord = ctx->nn_inter ? ctx->d_nn_ecoord.as<double>() : nullptr;
+        }
         {
             TimedLaunch tl(ctx, 5);
             WP_CUDA(wp_launch_nn_select(sel_grid, ctx->stream, b), "kNN select");
@@ -1213,7 +1449,7 @@ wp_status wp_timing_enable(wp_ctx* ctx, int enable) {
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
     collect_timing(ctx);
-    for (int k = 0; k < 8; k++) {
+    for (int k = 0; k < 9; k++) {
         ctx->t_ms[k] = 0.0;
         ctx->t_n[k] = 0;
     }
@@ -1222,7 +1458,7 @@ wp_status wp_timing_enable(wp_ctx* ctx, int enable) {
 }
 
 wp_status wp_timing_read(wp_ctx* ctx, int kind, double* total_ms, long long* launches) {
-    if (!ctx || kind < 0 || kind > 7) return WP_ERR_INVALID;
+    if (!ctx || kind < 0 || kind > 8) return WP_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
     collect_timing(ctx);
@@ -1943,26 +2179,6 @@ wp_status nn_install(wp_ctx* ctx, const int16_t* counts, int N, int T, int C, co
     }
     ctx->nn_hits_total = 0;
     for (int e = 0; e < N; e++) ctx->nn_hits_total += ehits[e];
-    // 16384 entries by systematic sampling of the cumulative hits (the
-    // midpoint of each of 16384 equal shares): each stands for the same
-    // number of hits, so the kNN search can estimate each read's k-hit
-    // radius from them
-    {
-        const int S = N > 0 ? 16384 : 0;
-        std::vector<int> sample(std::max(S, 1), 0);
-        long long cum = 0;
-        int e = 0;
-        for (int j = 0; j < S; j++) {
-            const long long target = ((2ll * j + 1) * ctx->nn_hits_total) / (2ll * S);
-            while (e < N - 1 && cum + ehits[e] <= target) cum += ehits[e++];
-            sample[j] = e;
-        }
-        WP_CUDA(ctx->d_nn_sample.ensure(sizeof(int) * sample.size()), "alloc");
-        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_sample.p, sample.data(), sizeof(int) * sample.size(),
-                                cudaMemcpyHostToDevice, ctx->stream), "copy");
-        WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
-        ctx->nn_sample_n = S;
-    }
     ctx->nn_counts.assign(counts, counts + (size_t)N * T * C);
     ctx->nn_src_off.assign(src_off, src_off + (N > 0 ? N + 1 : 0));
     ctx->nn_src_id.assign(src_id, src_id + S);
@@ -1975,32 +2191,32 @@ wp_status nn_install(wp_ctx* ctx, const int16_t* counts, int N, int T, int C, co
     ctx->nn_T = T;
     ctx->nn_C = C;
     ctx->nn_U = (int)ctx->nn_uniq.size();
-    std::vector<int> dense(std::max(S, 1), 0);
-    std::vector<double> ratio(std::max(S, 1), 0.0);
-    for (int i = 0; i < S; i++) {
-        dense[i] = (int)(std::lower_bound(ctx->nn_uniq.begin(), ctx->nn_uniq.end(), src_id[i]) - ctx->nn_uniq.begin());
-        ratio[i] = (double)src_hits[i] / (double)src_count[i];  // hits / count (nn-classifier.cc:154-158)
-    }
-    std::vector<int> off(ctx->nn_src_off);
-    if (off.empty()) off.push_back(0);
-    WP_CUDA(ctx->d_nn_hits.ensure(sizeof(int) * ehits.size()), "alloc");
-    WP_CUDA(ctx->d_nn_src_off.ensure(sizeof(int) * off.size()), "alloc");
-    WP_CUDA(ctx->d_nn_src_dense.ensure(sizeof(int) * dense.size()), "alloc");
-    WP_CUDA(ctx->d_nn_src_ratio.ensure(sizeof(double) * ratio.size()), "alloc");
-    WP_CUDA(ctx->d_nn_src_hits.ensure(sizeof(int) * std::max(S, 1)), "alloc");
     WP_CUDA(ctx->d_nn_dense_id.ensure(sizeof(int) * std::max(ctx->nn_U, 1)), "alloc");
-    WP_CUDA(cudaMemcpyAsync(ctx->d_nn_hits.p, ehits.data(), sizeof(int) * ehits.size(), cudaMemcpyHostToDevice, ctx->stream), "copy");
-    WP_CUDA(cudaMemcpyAsync(ctx->d_nn_src_off.p, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, ctx->stream), "copy");
-    WP_CUDA(cudaMemcpyAsync(ctx->d_nn_src_dense.p, dense.data(), sizeof(int) * dense.size(), cudaMemcpyHostToDevice, ctx->stream), "copy");
-    WP_CUDA(cudaMemcpyAsync(ctx->d_nn_src_ratio.p, ratio.data(), sizeof(double) * ratio.size(), cudaMemcpyHostToDevice, ctx->stream), "copy");
-    if (S > 0)
-        WP_CUDA(cudaMemcpyAsync(ctx->d_nn_src_hits.p, src_hits, sizeof(int) * S, cudaMemcpyHostToDevice, ctx->stream), "copy");
     if (ctx->nn_U > 0)
         WP_CUDA(cudaMemcpyAsync(ctx->d_nn_dense_id.p, ctx->nn_uniq.data(), sizeof(int) * ctx->nn_U, cudaMemcpyHostToDevice, ctx->stream), "copy");
     WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
     ctx->have_tracks = true;
     ctx->nn_coords_version = -1;
+    ctx->nn_tree_k = -1;
     ctx->nn_pep_version = -1;
+    return WP_OK;
+}
+
+wp_status wp_nn_set_selection(wp_ctx* ctx, int selection) {
+    if (!ctx || (selection != WP_NN_KDTREE && selection != WP_NN_PREFIX)) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->nn_selection = selection;
+    return WP_OK;
+}
+
+wp_status wp_nn_kd_tree_order(const double* coords, int N, int D, int k, int32_t* perm, int* out_num_nodes) {
+    if (N < 0 || D < 1 || D > 64 || (N > 0 && (!coords || !perm))) return WP_ERR_INVALID;
+    std::vector<int> p;
+    std::vector<KDNode> nodes;
+    int depth = 0;
+    if (wp_kdtree_build(coords, N, D, k, &p, &nodes, &depth) != 0) return WP_ERR_UNSUPPORTED;
+    for (int i = 0; i < N; i++) perm[i] = p[i];
+    if (out_num_nodes) *out_num_nodes = (int)nodes.size();
     return WP_OK;
 }
 

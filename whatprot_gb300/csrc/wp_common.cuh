@@ -16,6 +16,7 @@
 #include <stdint.h>
 
 #include "../../include/whatprot_gb300.h"
+#include "wp_kdtree.h"
 
 #define WP_W (WP_MAX_DYES_PER_CHANNEL + 1)      // extent cap per channel
 #define WP_TRI (WP_W * (WP_W + 1) / 2)          // triangular table size
@@ -309,6 +310,11 @@ struct NNArgs {
     const int* sample;      // [sample_n] entries drawn in proportion to their hits
     int sample_n;
     long long hits_total;   // hits over all entries
+    // The reference's k-hit set: per query (q0 + local) the final top's
+    // squared distance and flags (NNSelectArgs); the threshold then places
+    // b* at the bin holding that distance instead of the k-th hit.
+    const double* tf_d;
+    const int* tf_flag;
 };
 
 struct NNSelectArgs {
@@ -349,7 +355,91 @@ struct NNSelectArgs {
     double* out_cand_score;     // [R][h]
     double* out_total;
     double* out_subfrac;        // may be null
+    // The reference's k-hit set (KNN_KDTREE): per query slot the final top
+    // of the kd-tree search's KBest (wp_kbest.cu); an entry is kept iff its
+    // (FP64 squared distance, tree position) is at most (tf_d, tf_pos).
+    // Null: the shortest distance-ordered prefix reaching k hits.
+    const double* tf_d;         // [R_all]
+    const int* tf_pos;
+    const int* tf_flag;         // bit 0: every entry kept
+    const double* rads;         // [reads][TC] FP64 queries (read order); with
+                                // them the near entries' weights use FP64
+                                // distances
+    double two_sig_sq;          // 2 sig^2
+    int TC, C, DP, NC;
+    const uint8_t* cnt;         // [N][DP] counts per coordinate (tree order)
+    const double* ctab;         // [C][NC] coordinate of count n on channel c
+    const double* ecoord;       // [N][TC] FP64 coordinates (interacting models), or null
 };
+
+// ---- the reference's k-hit set (wp_kbest.cu) ------------------------------
+// One kept entry of the replayed KBest: squared distance, tree position and
+// hits.
+struct KBItem {
+    double d;
+    int pos;
+    int hits;
+};
+
+struct KBArgs {
+    int nwork;                  // query slots to process
+    const int* work;            // their indices (null: 0 .. nwork-1)
+    int* next;                  // work counter, zero on entry
+    const int* qperm;           // read index of each slot (null: identity)
+    const double* rads;         // [reads][TC] FP64 queries
+    int TC, C, DP, N;
+    long long k;
+    const uint8_t* cnt;         // [N][DP] counts (tree order)
+    const double* ctab;         // [C][NC] coordinate of count n
+    int NC;
+    int interact;               // coordinates depend on other channels' counts:
+    const double* ecoord;       //   [N][TC] FP64 coordinates
+    const float* coords32;      //   [N][DP] FP32 coordinates
+    const float* tlo;           // [tiles][DP] per 32 tree positions: box
+    const float* thi;
+    const float* llo;           // [nodes][DP] per leaf: box
+    const float* lhi;
+    const int* hits;            // [N] hits per entry (tree order)
+    const KDNode* nodes;        // nodes[0] the root
+    int stack_cap;              // deepest level + 1
+    KBItem* reg;                // per warp: two regions of regcap entries
+    int* prev;                  // per warp: two regions of regcap / 16 links
+    KBItem* stage;              // per warp: stagecap entries
+    int regcap, stagecap;
+    double* tf_d;               // per slot: the final top
+    int* tf_pos;
+    int* tf_flag;               // 1 every entry kept, 2 a refused entry tied
+                                // the final top's distance, 4 scratch too small
+};
+
+// FP64 squared distance from a query to entry p as LeafNode::consider sums
+// it (kd-tree/leaf-node.h:31-62): per coordinate x = q - e, x * x, summed in
+// groups of four while i < D - 3, then singly.  Coordinates from the count
+// table (ctab[c][n], non-interacting models) or from ecoord.
+__device__ __forceinline__ double wp_nn_exact_d2(const double* q64, long p, int TC, int C, int DP,
+                                                 const uint8_t* cnt, const double* ctab, int NC,
+                                                 const double* ecoord) {
+    double acc = 0.0;
+    int i = 0;
+    const uint8_t* row = cnt + p * DP;
+    const double* e = ecoord ? ecoord + p * TC : nullptr;
+    for (; i + 3 < TC; i += 4) {
+        double t[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const double ev = e ? e[i + u] : ctab[((i + u) % C) * NC + row[i + u]];
+            const double x = __dsub_rn(q64[i + u], ev);
+            t[u] = __dmul_rn(x, x);
+        }
+        acc = __dadd_rn(acc, __dadd_rn(__dadd_rn(__dadd_rn(t[0], t[1]), t[2]), t[3]));
+    }
+    for (; i < TC; i++) {
+        const double ev = e ? e[i] : ctab[(i % C) * NC + row[i]];
+        const double x = __dsub_rn(q64[i], ev);
+        acc = __dadd_rn(acc, __dmul_rn(x, x));
+    }
+    return acc;
+}
 
 // ---- read simulator (wp_sim.cu) -------------------------------------------
 // Event probabilities are 33-bit thresholds: an event with probability p

@@ -398,10 +398,19 @@ __global__ void wp_nn_threshold_kernel(NNArgs a) {
     long long cum = 0, below = 0, cap = 0;
     int b = NN_NB - 1;
     bool found = false;
+    // The reference's k-hit set: b* is the bin holding the final top's
+    // distance plus the binning distance's rounding (the margin of
+    // nn_clears), or the open last bin when every entry is kept.
+    int bound_bin = -1;
+    if (a.tf_d) {
+        const double td = a.tf_d[gq];
+        bound_bin = (a.tf_flag[gq] & 1) ? NN_NB - 1
+                                         : nn_bin((float)(td * (1.0 + 1e-4) + 1e-3) * (1.f + 1e-6f), a.qbase[gq]);
+    }
     for (int i = 0; i < NN_NB; i++) {
         long long hi = 0;
         for (int s = 0; s < a.slices; s++) hi += a.shist[((long)s * a.R_all + gq) * NN_NB + i];
-        if (!found && cum + hi >= a.k) {
+        if (!found && (bound_bin >= 0 ? i == bound_bin : cum + hi >= a.k)) {
             found = true;
             b = i;
             below = cum;
@@ -591,6 +600,18 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
         const int gq = a.q0 + (int)lq;
         const int bstar = a.qbin[gq];
         long long need = a.k - a.qbelow[gq];  // hits still needed from bin b*
+        // the reference's k-hit set: entries at or below the replayed final
+        // top (FP64 distance, tree position); FP32 distances decide unless
+        // they lie within their rounding margin of the top's
+        const bool exact = a.tf_d != nullptr;
+        const double tf_d = exact ? a.tf_d[gq] : 0.0;
+        const int tf_pos = exact ? a.tf_pos[gq] : 0;
+        const bool tf_all = exact && (a.tf_flag[gq] & 1);
+        const double tf_m = 2e-5 * tf_d + 1e-3;
+        const double* q64 = exact ? a.rads + (long)(a.qperm ? a.qperm[gq] : gq) * a.TC : nullptr;
+        unsigned kstar_out = 0u;
+        bool take_all_out = false;
+        if (!exact) {
         // The query's candidates: one segment per entry slice, in slice
         // order (so in ascending entry index overall).
 
@@ -666,7 +687,26 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
             __syncwarp();
             if (shift == 0) break;
         }
-        const unsigned kstar = prefix;  // with take_all: unused
+        kstar_out = prefix;
+        take_all_out = take_all;
+        }
+        const bool take_all = exact ? tf_all : take_all_out;
+        const unsigned kstar = kstar_out;  // with take_all: unused
+        // Weights of the entries near the read (within 18.5 x 2 sig^2 of the
+        // nearest, i.e. above 1e-8 of the largest weight) from FP64
+        // distances, as the reference forms them; the far ones from FP32
+        // (their error is below 1e-8 of the largest weight).
+        float dmin = INFINITY;
+        if (a.rads) {
+            for (int sl = 0; sl < a.slices; sl++) {
+                const long long sb = a.qoff[lq] + a.sliceoff[(long)sl * a.R_all + gq];
+                const long long sn = min(a.slicecnt[(long)sl * a.R_all + gq], a.slicecap[(long)sl * a.R_all + gq]);
+                for (long long i = lane; i < sn; i += 32) dmin = fminf(dmin, a.cand_d2[sb + i]);
+            }
+            for (int o = 16; o > 0; o >>= 1) dmin = fminf(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
+        }
+        const double wlim = (double)dmin + 18.5 * a.two_sig_sq + 1e-3;
+        const double* qw = a.rads ? a.rads + (long)(a.qperm ? a.qperm[gq] : gq) * a.TC : nullptr;
         // ---- contributions of the kept entries, in candidate (entry) order.
         double total_part = 0.0;
         int ntouched = 0;
@@ -685,7 +725,14 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
                 d2 = a.cand_d2[sb + i];
                 const int b = a.cand_bin[sb + i];
                 const unsigned key = __float_as_uint(d2);
-                if (b < bstar || take_all) keep = true;
+                if (take_all) keep = true;
+                else if (exact) {
+                    if ((double)d2 < tf_d - tf_m) keep = true;
+                    else if ((double)d2 <= tf_d + tf_m) {
+                        const double d64 = wp_nn_exact_d2(q64, e, a.TC, a.C, a.DP, a.cnt, a.ctab, a.NC, a.ecoord);
+                        keep = d64 < tf_d || (d64 == tf_d && e <= tf_pos);
+                    }
+                } else if (b < bstar) keep = true;
                 else if (key < kstar) keep = true;
                 else if (key == kstar) tie = true;
             }
@@ -699,9 +746,14 @@ __global__ void __launch_bounds__(NN_SEL_WARPS * 32) wp_nn_select_kernel(NNSelec
             // part applied in FP64 so far entries keep a non-zero weight
             double w = 0.0;
             if (keep) {
-                const float x = -d2 * a.inv_two_sig_sq * 1.4426950408889634f;
-                const float fl = floorf(x);
-                w = ldexp((double)exp2f(x - fl), (int)fl);
+                if (qw && (double)d2 < wlim) {
+                    const double d64 = wp_nn_exact_d2(qw, e, a.TC, a.C, a.DP, a.cnt, a.ctab, a.NC, a.ecoord);
+                    w = exp(-d64 / a.two_sig_sq);
+                } else {
+                    const float x = -d2 * a.inv_two_sig_sq * 1.4426950408889634f;
+                    const float fl = floorf(x);
+                    w = ldexp((double)exp2f(x - fl), (int)fl);
+                }
             }
             const int s0 = keep ? a.src_off[e] : 0;
             const int ns = keep ? a.src_off[e + 1] - s0 : 0;
@@ -1023,7 +1075,8 @@ __global__ void wp_nn_redo_kernel(NNArgs a, int* list, int* count, int shift) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= a.R) return;
     const int gq = a.q0 + q;
-    if (a.qbin[gq] == NN_NB - 1 && a.qcap[gq] >= a.k) {
+    const bool beyond = a.tf_d ? !(a.tf_flag[gq] & 1) : a.qcap[gq] >= a.k;
+    if (a.qbin[gq] == NN_NB - 1 && beyond) {
         list[atomicAdd(count, 1)] = q;
         a.qbase[gq] += shift;
     }
