@@ -62,6 +62,7 @@ struct KBSmem {
     int ch[KB_CUR];
     double q64[64];        // the query
     float q32[64];
+    int qpos[64];          // screened entries waiting for their FP64 distances
 };
 
 struct KBState {
@@ -83,10 +84,13 @@ struct KBState {
 struct KBCtx {
     const KBArgs* a;
     KBSmem* sm;
-    KBItem* reg[2];
-    int* prev[2];
+    KBItem* reg0;   // region r at reg0 + r * rc (a runtime-indexed array
+    int* prev0;     // would live in local memory)
+    long rc, pc;
     KBItem* stage;
     int lane;
+    __device__ __forceinline__ KBItem* reg(int r) const { return reg0 + r * rc; }
+    __device__ __forceinline__ int* prev(int r) const { return prev0 + r * pc; }
 };
 
 __device__ __forceinline__ bool kb_gt(double da, int pa, double db, int pb) {
@@ -102,7 +106,7 @@ __device__ __forceinline__ bool kb_nonempty(const KBSmem* sm, int b) { return (s
 
 // Append an entry to bucket b's chain in the active region; false when the
 // region is full.
-__device__ bool kb_append(KBCtx& c, KBState& st, int b, double d, int pos, int hits) {
+__device__ __forceinline__ bool kb_append(KBCtx& c, KBState& st, int b, double d, int pos, int hits) {
     KBSmem* sm = c.sm;
     const bool ne = kb_nonempty(sm, b);
     int f = ne ? sm->fill[b] : KB_CH;
@@ -118,12 +122,12 @@ __device__ bool kb_append(KBCtx& c, KBState& st, int b, double d, int pos, int h
     }
     __syncwarp();
     if (c.lane == 0) {
-        if (fresh) c.prev[st.act][chunk] = ne ? oldtail : -1;
+        if (fresh) c.prev(st.act)[chunk] = ne ? oldtail : -1;
         KBItem it;
         it.d = d;
         it.pos = pos;
         it.hits = hits;
-        c.reg[st.act][(long)chunk * KB_CH + f] = it;
+        c.reg(st.act)[(long)chunk * KB_CH + f] = it;
         sm->tail[b] = (uint16_t)chunk;
         sm->fill[b] = (uint8_t)(f + 1);
         sm->ne[b >> 5] |= 1u << (b & 31);
@@ -134,10 +138,10 @@ __device__ bool kb_append(KBCtx& c, KBState& st, int b, double d, int pos, int h
 
 // Every live entry (bucket chains and the rest of the current bucket) into
 // the staging buffer; returns their number, or -1 if they do not fit.
-__device__ int kb_gather(KBCtx& c, KBState& st) {
+__device__ __forceinline__ int kb_gather(KBCtx& c, KBState& st) {
     KBSmem* sm = c.sm;
-    const KBItem* reg = c.reg[st.act];
-    const int* prev = c.prev[st.act];
+    const KBItem* reg = c.reg(st.act);
+    const int* prev = c.prev(st.act);
     const int cap = c.a->stagecap;
     int n = 0;
     for (int w = 0; w < KB_B / 32; w++) {
@@ -171,7 +175,7 @@ __device__ int kb_gather(KBCtx& c, KBState& st) {
 
 // Redistribute the live entries into the other region with bucket shift
 // `sh`, the largest one in the highest bucket.  Leaves no current bucket.
-__device__ void kb_rebase(KBCtx& c, KBState& st, int sh) {
+__device__ __forceinline__ void kb_rebase(KBCtx& c, KBState& st, int sh) {
     const int n = kb_gather(c, st);
     if (n < 0) {
         st.fatal = 1;
@@ -209,10 +213,10 @@ __device__ void kb_rebase(KBCtx& c, KBState& st, int sh) {
 
 // Load bucket b as the current bucket, sorted; false (nothing changed) if
 // it holds more than KB_CUR entries.
-__device__ bool kb_enter(KBCtx& c, KBState& st, int b) {
+__device__ __forceinline__ bool kb_enter(KBCtx& c, KBState& st, int b) {
     KBSmem* sm = c.sm;
-    const KBItem* reg = c.reg[st.act];
-    const int* prev = c.prev[st.act];
+    const KBItem* reg = c.reg(st.act);
+    const int* prev = c.prev(st.act);
     int chunk = sm->tail[b], f = sm->fill[b], n = 0;
     while (chunk >= 0) {
         if (n + f > KB_CUR) return false;
@@ -271,7 +275,7 @@ __device__ __forceinline__ void kb_load_top(KBCtx& c, KBState& st) {
 }
 
 // Make the highest non-empty bucket below the current one current.
-__device__ void kb_descend(KBCtx& c, KBState& st) {
+__device__ __forceinline__ void kb_descend(KBCtx& c, KBState& st) {
     for (int guard = 0; guard < 64; guard++) {
         const int lim = st.cb;  // buckets < lim
         const int top_w = (lim - 1) >> 5;
@@ -312,7 +316,7 @@ __device__ void kb_descend(KBCtx& c, KBState& st) {
     st.fatal = 5;
 }
 
-__device__ void kb_pop(KBCtx& c, KBState& st) {
+__device__ __forceinline__ void kb_pop(KBCtx& c, KBState& st) {
     st.ptr++;
     if (st.ptr == st.len) {
         kb_descend(c, st);
@@ -322,7 +326,7 @@ __device__ void kb_pop(KBCtx& c, KBState& st) {
 }
 
 // Insert below the top into the current bucket, keeping it sorted.
-__device__ void kb_cur_insert(KBCtx& c, KBState& st, double d, int pos, int hits) {
+__device__ __forceinline__ void kb_cur_insert(KBCtx& c, KBState& st, double d, int pos, int hits) {
     KBSmem* sm = c.sm;
     int at = st.len;
     for (int i0 = st.ptr + 1; i0 < st.len; i0 += 32) {
@@ -362,7 +366,7 @@ __device__ void kb_cur_insert(KBCtx& c, KBState& st, double d, int pos, int hits
 }
 
 // KBest::insert.
-__device__ void kb_insert(KBCtx& c, KBState& st, double d, int pos, int hits) {
+__device__ __forceinline__ void kb_insert(KBCtx& c, KBState& st, double d, int pos, int hits) {
     const long long k = c.a->k;
     st.S += hits;
     if (st.fill_mode) {
@@ -444,7 +448,7 @@ __device__ __forceinline__ int kb_byte(const uint32_t (&w)[DP / 4], int i) {
 // i < D - 3, then single terms; every term from the per-read table
 // sq64[i][n] = (q_i - coordinate(i, n))^2.
 template <int DP>
-__device__ double kb_d64_tab(const uint32_t (&w)[DP / 4], const double* sq64, int NC, int TC) {
+__device__ __forceinline__ double kb_d64_tab(const uint32_t (&w)[DP / 4], const double* sq64, int NC, int TC) {
     double acc = 0.0;
 #pragma unroll
     for (int i = 0; i < DP; i += 4) {
@@ -464,7 +468,7 @@ __device__ double kb_d64_tab(const uint32_t (&w)[DP / 4], const double* sq64, in
 }
 
 template <int DP>
-__device__ float kb_d32_tab(const uint32_t (&w)[DP / 4], const float* sq32, int NC, int TC) {
+__device__ __forceinline__ float kb_d32_tab(const uint32_t (&w)[DP / 4], const float* sq32, int NC, int TC) {
     float a0 = 0.f, a1 = 0.f;
 #pragma unroll
     for (int i = 0; i < DP; i += 2) {
@@ -475,7 +479,7 @@ __device__ float kb_d32_tab(const uint32_t (&w)[DP / 4], const float* sq32, int 
 }
 
 // The same from FP64 coordinates (models with dye interactions).
-__device__ double kb_d64_coords(const double* __restrict__ e, const double* q, int TC) {
+__device__ __forceinline__ double kb_d64_coords(const double* __restrict__ e, const double* q, int TC) {
     double acc = 0.0;
     int i = 0;
     for (; i + 3 < TC; i += 4) {
@@ -511,11 +515,10 @@ __global__ void __launch_bounds__(KB_WARPS * 32) wp_kbest_kernel(KBArgs a) {
     c.a = &a;
     c.sm = sm;
     c.lane = lane;
-    const long rc = a.regcap, pc = a.regcap / KB_CH;
-    c.reg[0] = a.reg + gw * 2 * rc;
-    c.reg[1] = c.reg[0] + rc;
-    c.prev[0] = a.prev + gw * 2 * pc;
-    c.prev[1] = c.prev[0] + pc;
+    c.rc = a.regcap;
+    c.pc = a.regcap / KB_CH;
+    c.reg0 = a.reg + gw * 2 * c.rc;
+    c.prev0 = a.prev + gw * 2 * c.pc;
     c.stage = a.stage + gw * (long)a.stagecap;
 
     for (;;) {
@@ -613,25 +616,28 @@ __global__ void __launch_bounds__(KB_WARPS * 32) wp_kbest_kernel(KBArgs a) {
                 for (int o = 16; o > 0; o >>= 1) g2 += __shfl_xor_sync(0xffffffffu, g2, o);
                 if ((double)g2 > st.kth * (1.0 + 1e-4) + 1e-3) continue;
             }
-            for (long t = n.begin >> 5; t <= (long)(n.end - 1) >> 5 && !st.fatal; t++) {
-                if (!st.fill_mode) {
-                    float g2 = 0.f;
-                    for (int i = lane; i < a.TC; i += 32) {
-                        const float lo = a.tlo[t * a.DP + i], hi = a.thi[t * a.DP + i];
-                        const float qq = sm->q32[i];
-                        const float g = fmaxf(fmaxf(lo - qq, qq - hi), 0.f);
-                        g2 = fmaf(g, g, g2);
-                    }
-                    for (int o = 16; o > 0; o >>= 1) g2 += __shfl_xor_sync(0xffffffffu, g2, o);
-                    if ((double)g2 > st.kth * (1.0 + 1e-4) + 1e-3) continue;
-                }
+            // Tiles of 32 tree positions: each lane screens one entry in FP32
+            // (the next tile's counts already loading); entries that may lie
+            // below kth join a queue in tree order; 32 queued entries at a
+            // time get their FP64 distances (one per lane) and are offered
+            // to KBest in order, each against the kth of that moment.
+            const long t_lo = n.begin >> 5, t_hi = (long)(n.end - 1) >> 5;
+            int qn = 0;
+            uint32_t w[DP / 4], wn[DP / 4];
+#pragma unroll
+            for (int i = 0; i < DP / 4; i++) w[i] = wn[i] = 0u;
+            if (!INTER) {
+                const long p0 = t_lo * 32 + lane;
+                if (p0 >= n.begin && p0 < n.end) kb_row<DP>(a.cnt, p0, w);
+            }
+            for (long t = t_lo; t <= t_hi && !st.fatal; t++) {
                 const long p = t * 32 + lane;
                 const bool in = p >= n.begin && p < n.end;
+                const long pn = p + 32;
+                if (!INTER && t < t_hi && pn >= n.begin && pn < n.end) kb_row<DP>(a.cnt, pn, wn);
                 bool cand = false;
-                double d64 = 0.0;
-                int h = 0;
-                if (INTER) {
-                    if (in) {
+                if (in) {
+                    if (INTER) {
                         const float* e = a.coords32 + p * a.DP;
                         float acc = 0.f;
                         for (int i = 0; i < a.TC; i++) {
@@ -639,35 +645,51 @@ __global__ void __launch_bounds__(KB_WARPS * 32) wp_kbest_kernel(KBArgs a) {
                             acc = fmaf(x, x, acc);
                         }
                         cand = st.fill_mode || (double)acc < st.kth * (1.0 + 2e-5) + 1e-3;
-                        if (cand) {
-                            d64 = kb_d64_coords(a.ecoord + p * a.TC, sm->q64, a.TC);
-                            h = a.hits[p];
-                        }
-                    }
-                } else {
-                    if (in) {
-                        uint32_t w[DP / 4];
-                        kb_row<DP>(a.cnt, p, w);
+                    } else {
                         const float d32 = kb_d32_tab<DP>(w, sq32, a.NC, a.TC);
                         cand = st.fill_mode || (double)d32 < st.kth * (1.0 + 1e-5);
-                        if (cand) {
-                            d64 = kb_d64_tab<DP>(w, sq64, a.NC, a.TC);
-                            h = a.hits[p];
-                        }
                     }
                 }
-                unsigned m = __ballot_sync(0xffffffffu, cand);
-                while (m) {
-                    const int j = __ffs(m) - 1;
-                    m &= m - 1;
-                    const double dj = __shfl_sync(0xffffffffu, d64, j);
-                    const int hj = __shfl_sync(0xffffffffu, h, j);
-                    if (dj < st.kth) {
-                        kb_insert(c, st, dj, (int)(t * 32 + j), hj);
-                        if (st.fatal) break;
-                    } else if (dj == st.kth) {
-                        st.tie_d = fmin(st.tie_d, dj);
+#pragma unroll
+                for (int i = 0; i < DP / 4; i++) w[i] = wn[i];
+                const unsigned m = __ballot_sync(0xffffffffu, cand);
+                if (cand) sm->qpos[qn + __popc(m & ((1u << lane) - 1u))] = (int)p;
+                qn += __popc(m);
+                __syncwarp();
+                while (qn >= 32 || (t == t_hi && qn > 0)) {
+                    const int cnt = min(32, qn);
+                    double d64 = 0.0;
+                    int h = 0, pos = 0;
+                    if (lane < cnt) {
+                        pos = sm->qpos[lane];
+                        if (INTER) {
+                            d64 = kb_d64_coords(a.ecoord + (long)pos * a.TC, sm->q64, a.TC);
+                        } else {
+                            uint32_t r[DP / 4];
+                            kb_row<DP>(a.cnt, pos, r);
+                            d64 = kb_d64_tab<DP>(r, sq64, a.NC, a.TC);
+                        }
+                        h = a.hits[pos];
                     }
+                    // the rest of the queue moves to its front
+                    int rest = 0;
+                    if (lane + cnt < qn) rest = sm->qpos[lane + cnt];
+                    __syncwarp();
+                    if (lane + cnt < qn) sm->qpos[lane] = rest;
+                    __syncwarp();
+                    qn -= cnt;
+                    for (int j = 0; j < cnt; j++) {
+                        const double dj = __shfl_sync(0xffffffffu, d64, j);
+                        const int hj = __shfl_sync(0xffffffffu, h, j);
+                        const int pj = __shfl_sync(0xffffffffu, pos, j);
+                        if (dj < st.kth) {
+                            kb_insert(c, st, dj, pj, hj);
+                            if (st.fatal) break;
+                        } else if (dj == st.kth) {
+                            st.tie_d = fmin(st.tie_d, dj);
+                        }
+                    }
+                    if (st.fatal) break;
                 }
             }
         }
