@@ -202,6 +202,174 @@ def run_hybrid(args):
         dist.destroy_process_group()
 
 
+SUB_READS = 20_000  # query reads per step of the hybrid / learned sub-records
+
+
+def _timed_steps(stream, flush, step, steps):
+    """Mean CUDA-event time (ms) of `step` on `stream`, L2 flushed before each."""
+    import torch
+    total = 0.0
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+    return total / max(steps, 1)
+
+
+def hybrid_learned_subrecords(local, steps=2, warmup=1, epochs=3, reads=SUB_READS, oracle_reads=64):
+    """The second half of the headline metric on one GB300: the hybrid
+    classifier's reads/s with the kNN stage (k = 10,000 hits, sigma 0.5,
+    H = 1,000) in both k-hit selections -- the reference's kd-tree search
+    (exact, the default) and the shortest-prefix fast mode -- and with the
+    learned proposal (MLP 48-1024-1024-20000, H = 200) in its place, on the
+    same 20,000 dye-seqs and the same query reads; top-1 against the truth,
+    recall@H of the true peptide, the plain HMM over all peptides as the
+    accuracy ceiling on a sample, and the kd-tree hybrid against the oracle
+    on a sample.  Dye-track set and reads are simulated on the device."""
+    import torch
+    from whatprot_gb300 import capi
+    from whatprot_gb300.simulate import paper_model, random_dye_seqs
+    dev = f"cuda:{local}"
+    sm = paper_model(C)
+    ds = random_dye_seqs(HY_P, C, 8, 30, max_per_channel=5, min_total=1, seed=1234)
+    ctx = capi.Context(local)
+    ctx.upload_model(sm, T)
+    ctx.upload_peptides(ds)
+    t0 = time.perf_counter()
+    dts = ctx.simulate_dye_track_set(HY_PER, seed=4321, to_nn=True)
+    r_all, pep, _ = ctx.simulate_reads(int(reads * 1.1) + 64, seed=6060)
+    keep = np.nonzero(pep >= 0)[0][:reads]
+    rads = np.ascontiguousarray(r_all[keep])
+    true_pep = pep[keep]
+    true_ids = ds.ids[true_pep]
+    R = rads.shape[0]
+    gen_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=torch.device("cuda", local))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    d_rads = torch.from_numpy(rads).to(dev)
+    d_id = torch.empty(R, dtype=torch.int32, device=dev)
+    d_sc = torch.empty(R, dtype=torch.float64, device=dev)
+    d_tot = torch.empty(R, dtype=torch.float64, device=dev)
+    h_rads = torch.from_numpy(rads).pin_memory().numpy()
+    out = {"config": {"peptides": len(ds), "dye_tracks": len(dts), "track_sources": int(dts.src_off[-1]),
+                      "reads_per_step": R, "k": HY_K, "sigma": HY_SIG, "h_knn": HY_H, "h_learned": LP_H,
+                      "dist_cutoff": CUTOFF, "steps": steps, "warmup": warmup,
+                      "l2": "flushed between steps (512 MB write)",
+                      "data": "dye-track set (100 per dye-seq) and reads simulated on the device, seeded",
+                      "data_generation_s": gen_s}}
+    rows = {}
+    for sel in ("kdtree", "prefix"):
+        ctx.set_nn_selection(sel)
+
+        def step():
+            ctx.hybrid_classify_device(d_rads.data_ptr(), R, HY_K, HY_SIG, HY_H, CUTOFF, d_id.data_ptr(),
+                                       d_sc.data_ptr(), d_tot.data_ptr())
+        for _ in range(warmup):
+            step()
+        torch.cuda.synchronize()
+        ctx.timing_enable(True)
+        ms = _timed_steps(stream, flush, step, steps)
+        kt, _ = ctx.timing_read(ctx.KIND_KNN_TREE)
+        kd, _ = ctx.timing_read(ctx.KIND_KNN_DIST)
+        ks, _ = ctx.timing_read(ctx.KIND_KNN_SELECT)
+        fw, _ = ctx.timing_read(ctx.KIND_FORWARD)
+        ctx.timing_enable(False)
+        gid = d_id.cpu().numpy()
+        t0 = time.perf_counter()
+        hid, hsc, htot = ctx.hybrid_classify(h_rads, HY_K, HY_SIG, HY_H, CUTOFF)
+        e2e_s = time.perf_counter() - t0
+        nc, cid, _, _ = ctx.nn_classify(rads, HY_K, HY_SIG, HY_H)
+        recall = float(np.mean([true_ids[r] in set(cid[r, :nc[r]].tolist()) for r in range(R)]))
+        rows[sel] = {"reads_per_s": R / (ms * 1e-3), "ms_per_step": ms,
+                     "e2e": {"value": R / e2e_s, "unit": HY_UNIT, "h2d_bytes_per_step": int(rads.nbytes),
+                             "d2h_bytes_per_step": int(R * 20)},
+                     "top1_vs_truth": float(np.mean(gid == true_ids)), "recall_at_h": recall,
+                     "ms_per_step_split": {"kd_tree_replay": kt / steps, "knn_distances": kd / steps,
+                                           "knn_select": ks / steps, "hmm_forward": fw / steps},
+                     "host_result": (hid, hsc, htot)}
+    ctx.set_nn_selection("kdtree")
+    # the learned proposal on the same reads
+    net = capi.ProposalNet(ctx, hidden=LP_HIDDEN, seed=11)
+    t0 = time.perf_counter()
+    losses = [net.train(LP_EPOCH_READS, batch=LP_BATCH, lr=1e-3 if ep < epochs - 1 else 3e-4, seed=1000 + ep)
+              for ep in range(epochs)]
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+
+    def lstep():
+        net.hybrid_classify_device(d_rads.data_ptr(), R, LP_H, CUTOFF, d_id.data_ptr(), d_sc.data_ptr(),
+                                   d_tot.data_ptr())
+    for _ in range(warmup):
+        lstep()
+    torch.cuda.synchronize()
+    lms = _timed_steps(stream, flush, lstep, steps)
+    lid = d_id.cpu().numpy()
+    t0 = time.perf_counter()
+    net.hybrid_classify(h_rads, LP_H, CUTOFF)
+    le2e_s = time.perf_counter() - t0
+    idx, _, _ = net.propose(rads, LP_H)
+    lrecall = float(np.mean(np.any(idx == true_pep[:, None], axis=1)))
+    net.close()
+    learned = {"reads_per_s": R / (lms * 1e-3), "ms_per_step": lms,
+               "e2e": {"value": R / le2e_s, "unit": HY_UNIT, "h2d_bytes_per_step": int(rads.nbytes),
+                       "d2h_bytes_per_step": int(R * 20)},
+               "top1_vs_truth": float(np.mean(lid == true_ids)), "recall_at_h": lrecall,
+               "train_seconds": train_s, "train_epochs": epochs, "epoch_reads": LP_EPOCH_READS,
+               "train_loss_per_epoch": losses}
+    # accuracy ceiling: the plain HMM over all 20,000 peptides on a sample
+    ns = min(R, 2000)
+    fid, _, _, _ = ctx.classify(rads[:ns], CUTOFF)
+    ceiling = {"reads": ns, "full_hmm_top1": float(np.mean(fid == true_ids[:ns])),
+               "kdtree_hybrid_top1": float(np.mean(rows["kdtree"]["host_result"][0][:ns] == true_ids[:ns])),
+               "prefix_hybrid_top1": float(np.mean(rows["prefix"]["host_result"][0][:ns] == true_ids[:ns])),
+               "learned_hybrid_top1": float(np.mean(lid[:ns] == true_ids[:ns]))}
+    # the kd-tree hybrid against the oracle's restatement of the reference
+    parity = None
+    try:
+        sys.path.insert(0, os.path.join(REPO, "tests"))
+        from oracle_lib import Oracle
+        o = Oracle()
+        n = min(R, oracle_reads)
+        t0 = time.perf_counter()
+        oid, osc, otot = o.hybrid_classify(sm, T, dts, ds, rads[:n], HY_K, HY_SIG, HY_H, CUTOFF,
+                                           threads=os.cpu_count() or 1)
+        o_s = time.perf_counter() - t0
+        hid, hsc, htot = rows["kdtree"]["host_result"]
+        same = hid[:n] == oid
+        ga, oa = hsc[:n] / htot[:n], osc / otot
+        rel = np.abs(ga - oa) / np.maximum(np.abs(oa), 1e-300)
+        ll = None
+        if not np.all(same):  # a different top-1 must be an HMM tie (equal probabilities to 1e-5)
+            ll = ctx.loglik_all(rads[:n][~same], CUTOFF)
+        tied = 0
+        if ll is not None:
+            index = {int(i): k for k, i in enumerate(ds.ids)}
+            for j, r in enumerate(np.nonzero(~same)[0]):
+                a, b = index[int(hid[r])], index[int(oid[r])]
+                tied += int(abs(ll[j, a] - ll[j, b]) <= 1e-5)
+        parity = {"reads": int(n), "top1_identical": float(np.mean(same)),
+                  "top1_identical_or_tied": float((np.sum(same) + tied) / n),
+                  "max_rel_err_adjusted_score": float(np.max(rel)), "tolerance": 1e-5,
+                  "oracle": "oracle/wp_oracle.c kd-tree KBest restatement + FP64 HMM", "oracle_seconds": o_s}
+    except Exception as e:  # the oracle is the checker: report, do not fail the bench
+        parity = {"error": str(e)}
+    for sel in rows:
+        rows[sel].pop("host_result")
+    ctx.close()
+    res = {"config": out["config"], "knn_kdtree": rows["kdtree"], "knn_prefix": rows["prefix"],
+           "learned": learned, "accuracy_ceiling": ceiling, "parity_kdtree_vs_oracle": parity,
+           "learned_vs_knn_kdtree": learned["reads_per_s"] / rows["kdtree"]["reads_per_s"],
+           "learned_vs_knn_prefix": learned["reads_per_s"] / rows["prefix"]["reads_per_s"],
+           "learned_minus_knn_kdtree_top1_pts": 100 * (learned["top1_vs_truth"] - rows["kdtree"]["top1_vs_truth"]),
+           "learned_minus_knn_prefix_top1_pts": 100 * (learned["top1_vs_truth"] - rows["prefix"]["top1_vs_truth"])}
+    return res
+
+
 def cpu_baseline_hybrid(sm, ds, dts, rads, seconds_target=15.0):
     """The CPU oracle's hybrid classifier (brute-force FP64 kNN, then the HMM
     over the candidates) on a bounded sample of the reads, all host threads."""
@@ -219,7 +387,8 @@ def cpu_baseline_hybrid(sm, ds, dts, rads, seconds_target=15.0):
     dt = time.perf_counter() - t0
     info = {"value": n2 / dt, "unit": HY_UNIT, "cores": threads, "kind": "port",
             "sample": f"{n2} reads of the same workload, {dt:.1f} s, oracle/wp_oracle.c "
-                      f"wpo_hybrid_classify_batch (brute-force kNN) with {threads} threads"}
+                      f"wpo_hybrid_classify_batch (the reference's kd-tree KBest search, FP64) with "
+                      f"{threads} threads"}
     return info, out[:3]
 
 
@@ -628,6 +797,7 @@ def run_gemm(args):
 FIT_METRIC = "Baum-Welch E-step reads/s (fit, 1 dye-seq 4/3/3 dyes, no pruning)"
 FIT_UNIT = "reads/s"
 FIT_READS, FIT_LEN = 200_000, 20
+FIT_ORACLE_READS = 4000  # the subset fitted by both the GPU and the FP64 oracle
 FIT_WORKLOAD = ("fit: 3 channels x 16 timesteps, 1 dye-seq of 20 positions with 4/3/3 dyes "
                 "(positions seeded), 200000 reads float64 [200000,16,3], unpruned")
 
@@ -739,6 +909,13 @@ def cpu_baseline(sm, ds, rads, seconds_target=15.0):
     info = {"value": n2 * len(ds) / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{n2} reads x {len(ds)} dye-seqs of the same workload, "
                       f"{dt:.1f} s, oracle/wp_oracle.c with {threads} threads"}
+    # the same on one host thread, a smaller sample (about 5 s)
+    m = max(4, int(n2 * 5.0 / max(dt * threads, 1e-3)))
+    t0 = time.perf_counter()
+    o.classify(sm, T, ds, rads[:m], CUTOFF, threads=1)
+    dt1 = time.perf_counter() - t0
+    info["one_thread"] = {"value": m * len(ds) / dt1, "unit": UNIT, "cores": 1,
+                          "sample": f"{m} reads x {len(ds)} dye-seqs, {dt1:.1f} s"}
     return info, (oid, osc, otot)
 
 
@@ -759,6 +936,31 @@ def unpruned_forward_flops(seqs, T, C):
             f += (t + 1) * S * (3.0 + ((8.0 + B) if t > 0 else 0.0))
         total += f
     return total
+
+
+def loglik_parity(ctx, sm, ds, rads, n=500):
+    """Per-pair log P of the GPU engine (FP32 with exact power-of-two
+    rescaling) against the oracle's FP64 log P on the first n reads of the
+    workload, all peptides: the largest and median |delta log P| over every
+    pair both find possible, and over each read's best pair; pairs one side
+    finds impossible (P = 0) and the other not are counted."""
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from oracle_lib import Oracle
+    n = min(n, len(rads))
+    g = ctx.loglik_all(rads[:n], CUTOFF)
+    o = Oracle().loglik_all(sm, T, ds, rads[:n], CUTOFF, threads=os.cpu_count() or 1)
+    fin = np.isfinite(g) & np.isfinite(o)
+    d = np.abs(g - o)[fin]
+    best = np.argmax(np.where(np.isfinite(o), o, -np.inf), axis=1)
+    db = np.abs(g[np.arange(n), best] - o[np.arange(n), best])
+    db = db[np.isfinite(db)]
+    return {"reads": int(n), "pairs": int(n * len(ds)), "finite_pairs": int(fin.sum()),
+            "zero_mismatches": int(np.sum(np.isfinite(g) != np.isfinite(o))),
+            "all_pairs_max_abs": float(d.max()) if d.size else None,
+            "all_pairs_median_abs": float(np.median(d)) if d.size else None,
+            "best_pair_max_abs": float(db.max()) if db.size else None,
+            "best_pair_median_abs": float(np.median(db)) if db.size else None,
+            "tolerance_abs": 1e-5}
 
 
 def sample_parity(gpu, oracle_out):
@@ -1015,6 +1217,34 @@ def run_fit(args):
              "sig_max_rel": max(rel(a.sig, b.sig) for a, b in zip(fitted_e.channel_models, sm.channel_models)),
              "bg_sig_max_rel": max(rel(a.bg_sig, b.bg_sig)
                                    for a, b in zip(fitted_e.channel_models, sm.channel_models))}
+    # the FP32 E-step's effect on the fitted parameters: the same fit on a
+    # bounded subset of the reads, on the GPU and with the oracle's FP64
+    # E-step (same start, same host M-step)
+    fit_oracle = None
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "tests"))
+        from oracle_lib import oracle_em
+        sub = np.ascontiguousarray(h_np[:FIT_ORACLE_READS])
+        ctx.upload_model(start, T)
+        g_fit, g_step, _, g_it = ctx.hmm_fit(start, T, seq, sub, 1e-6, 600.0)
+        t0 = time.perf_counter()
+        o_fit, o_step, o_it = oracle_em(start, T, seq, sub, 1e-6, threads=os.cpu_count() or 1)
+        o_s = time.perf_counter() - t0
+        per = {"p_edman_failure": abs(g_fit.p_edman_failure - o_fit.p_edman_failure),
+               "p_detach_curve_max": max(abs(a - b) for a, b in zip(curve(g_fit), curve(o_fit))),
+               "p_bleach": [abs(a.p_bleach - b.p_bleach) for a, b in zip(g_fit.channel_models, o_fit.channel_models)],
+               "p_dud": [abs(a.p_dud - b.p_dud) for a, b in zip(g_fit.channel_models, o_fit.channel_models)]}
+        worst = max([per["p_edman_failure"], per["p_detach_curve_max"]] + per["p_bleach"] + per["p_dud"])
+        fit_oracle = {"reads": int(sub.shape[0]), "threshold": 1e-6, "gpu_iterations": g_it,
+                      "oracle_iterations": o_it, "oracle_seconds": o_s,
+                      "abs_diff_gpu_vs_fp64_oracle": per, "max_abs_diff": worst, "tolerance_abs": 1e-5,
+                      "oracle": "oracle/wp_oracle.c FP64 E-step (wpo_improve_fit_batch) + the library's host "
+                                "M-step (wp_fit_mstep)",
+                      "gpu_max_abs_error_vs_generating_model": max(
+                          [abs(g_fit.p_edman_failure - sm.p_edman_failure)]
+                          + [abs(a - b) for a, b in zip(curve(g_fit), curve(sm))]
+                          + [abs(a.p_bleach - b.p_bleach) for a, b in zip(g_fit.channel_models, sm.channel_models)]
+                          + [abs(a.p_dud - b.p_dud) for a, b in zip(g_fit.channel_models, sm.channel_models)])}
     k_avg = k_ms / max(k_n, 1)
     fit_flops = 3.0 * R * unpruned_forward_flops([seq], T, C)
     fit_peak = ctx.fp32_peak_tflops()
@@ -1044,7 +1274,8 @@ def run_fit(args):
                                "estep_with_emission_statistics_s": est_e_s, "error_vs_generating_model": err_e,
                                "fitted_mu": [c.mu for c in fitted_e.channel_models],
                                "fitted_sig": [c.sig for c in fitted_e.channel_models],
-                               "fitted_bg_sig": [c.bg_sig for c in fitted_e.channel_models]}}
+                               "fitted_bg_sig": [c.bg_sig for c in fitted_e.channel_models]},
+            "fit_vs_fp64_oracle": fit_oracle}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_fit(sm, seq, rads)
     if rank == 0:
@@ -1062,6 +1293,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--reads", type=int, default=READS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-subrecords", action="store_true",
+                    help="classify: leave out the hybrid / learned sub-records")
     ap.add_argument("--workload", default="classify",
                     choices=["classify", "fit", "hybrid", "learned", "gemm", "tracks"])
     ap.add_argument("--epochs", type=int, default=3)
@@ -1198,7 +1431,7 @@ def main():
     achieved = flops_per_launch / (fwd_avg_ms * 1e-3) / 1e12 if fwd_n else None
     # DRAM traffic of the engine passes from one ncu capture of a 5,000-read
     # batch of this workload (26.9 + 32.1 + 8.4 + 1.6 MB over its four
-    # passes, profiles/wp_engine_kernel_c3t16_5k.md), scaled by the reads
+    # passes), scaled by the reads
     # (the traffic is per pair) and spread over this step's forward launches
     launches_per_step = fwd_n / split_steps if fwd_n else 0.0
     traffic = (69.0e6 * R / 5000.0) / launches_per_step if launches_per_step else None
@@ -1226,9 +1459,12 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"], o_out = cpu_baseline(sm, ds, rads)
         line["parity_vs_oracle"] = sample_parity(last_gpu, o_out)
+        line["parity_vs_oracle"]["log_p"] = loglik_parity(ctx, sm, ds, rads)
+    ctx.close()
+    if rank == 0 and not args.no_subrecords:
+        line["hybrid_and_learned"] = hybrid_learned_subrecords(local, epochs=args.epochs)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
     if dist:
         dist.destroy_process_group()
 

@@ -500,3 +500,63 @@ class Reference:
         ll = self.lib.ref_fit(ctypes.byref(m), T, seq_str.encode(), rads.shape[0], _p(rads), threshold,
                               max_runtime, ctypes.byref(out), ctypes.byref(step), ctypes.byref(secs))
         return out, ll, step.value, secs.value
+
+
+def oracle_sums_to_wp(o):
+    """The oracle's E-step sums (WpoFitSums) as the library's wp_fit_sums."""
+    from whatprot_gb300.capi import WpFitSums
+    s = WpFitSums()
+    s.p_edman_failure_num, s.p_edman_failure_den = o.edman_num, o.edman_den
+    for i in range(len(s.p_detach_x)):
+        s.p_detach_x[i], s.p_detach_n[i] = o.detach_x[i], o.detach_n[i]
+    s.p_initial_block_num, s.p_initial_block_den = o.init_block_num, o.init_block_den
+    s.p_cyclic_block_num, s.p_cyclic_block_den = o.cyc_block_num, o.cyc_block_den
+    for c in range(len(s.p_bleach_num)):
+        s.p_bleach_num[c], s.p_bleach_den[c] = o.bleach_num[c], o.bleach_den[c]
+        s.p_dud_num[c], s.p_dud_den[c] = o.dud_num[c], o.dud_den[c]
+    return s
+
+
+def params_of_model(sm):
+    """A SequencingModel's rates as wp_fit_params."""
+    from whatprot_gb300.capi import WpFitParams
+    p = WpFitParams()
+    for k in ("p_edman_failure", "p_detach", "p_initial_detach", "p_initial_detach_decay", "p_initial_block",
+              "p_cyclic_block"):
+        setattr(p, k, getattr(sm, k))
+    for c, cm in enumerate(sm.channel_models):
+        p.p_bleach[c], p.p_dud[c] = cm.p_bleach, cm.p_dud
+        p.mu[c], p.sig[c], p.bg_sig[c] = cm.mu, cm.sig, cm.bg_sig
+    return p
+
+
+def model_of_params(p, like):
+    """wp_fit_params back into a SequencingModel shaped like `like`."""
+    import copy
+    m = copy.deepcopy(like)
+    for k in ("p_edman_failure", "p_detach", "p_initial_detach", "p_initial_detach_decay", "p_initial_block",
+              "p_cyclic_block"):
+        setattr(m, k, getattr(p, k))
+    for c, cm in enumerate(m.channel_models):
+        cm.p_bleach, cm.p_dud = p.p_bleach[c], p.p_dud[c]
+    return m
+
+
+def oracle_em(start, T, seq, rads, threshold, threads=8, max_iterations=1000):
+    """HMMFitter::fit's EM loop (fitters/hmm-fitter.h:49-142) with the
+    oracle's FP64 E-step (wpo_improve_fit_batch, unpruned as run-fit.cc:59)
+    and the library's host M-step (wp_fit_mstep: dud hidden-count
+    correction, p = num / den, the detach curve), so that a GPU fit compared
+    with it differs only by its FP32 E-step.  Returns (fitted model, step
+    size, iterations)."""
+    from whatprot_gb300 import shards
+    o = Oracle()
+    cur = params_of_model(start)
+    it = 0
+    while True:
+        s, _ = o.improve_fit_batch(model_of_params(cur, start), T, seq, rads, threads=threads)
+        nxt, step = shards.mstep(oracle_sums_to_wp(s), start.num_channels, T, seq, rads.shape[0], cur)
+        it += 1
+        cur = nxt
+        if step < threshold or it >= max_iterations:
+            return model_of_params(cur, start), step, it

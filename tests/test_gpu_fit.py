@@ -367,3 +367,37 @@ def test_fit_batch_matches_sequential_fits(gpu_ctx):
         # the step is a difference of nearly equal parameter sets, so the
         # sums' rounding shows in it more (same iteration count: same size)
         assert abs(steps[b] - step) <= 1e-2 * max(step, 1e-12)
+
+
+@pytest.mark.parametrize("kernel", [0, 1], ids=["cta", "thread"])
+def test_fit_vs_fp64_oracle_em(gpu_ctx, kernel):
+    """A full fit (HMMFitter::fit to a 1e-6 step from a perturbed start) with
+    the GPU's FP32 E-step against the same EM with the oracle's FP64 E-step
+    and the same host M-step (tests/oracle_lib.py oracle_em): every fitted
+    rate, the detach curve included, within 1e-5 absolute."""
+    from oracle_lib import oracle_em
+    sm = paper_model(3)
+    seq = parse_dye_seq("..0.1.2..0.1..2.0")
+    one = DyeSeqSet(3, [seq], np.array([0], np.int32), np.array([1], np.int32))
+    rads, _ = simulate_radiometries(sm, one, 10, 1500, seed=31)
+    start = paper_model(3)
+    start.p_edman_failure *= 1.4
+    start.p_detach *= 0.6
+    for c, cm in enumerate(start.channel_models):
+        cm.p_bleach *= (1.3, 0.7, 1.2)[c]
+        cm.p_dud *= (0.6, 1.4, 1.1)[c]
+    ctx = capi.Context(0)
+    try:
+        ctx.upload_model(start, 10)
+        ctx.fit_set_kernel(kernel)
+        g, _, _, g_it = ctx.hmm_fit(start, 10, seq, rads, 1e-6)
+    finally:
+        ctx.close()
+    o, _, o_it = oracle_em(start, 10, seq, rads, 1e-6, threads=8)
+    curve = lambda m: np.array([m.p_detach_at(t) for t in range(9)])
+    assert abs(g.p_edman_failure - o.p_edman_failure) <= 1e-5
+    assert np.max(np.abs(curve(g) - curve(o))) <= 1e-5
+    for a, b in zip(g.channel_models, o.channel_models):
+        assert abs(a.p_bleach - b.p_bleach) <= 1e-5
+        assert abs(a.p_dud - b.p_dud) <= 1e-5
+    assert abs(g_it - o_it) <= 2

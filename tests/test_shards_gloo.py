@@ -36,17 +36,8 @@ def _data():
 
 
 def _to_wp_sums(o):
-    from whatprot_gb300.capi import WpFitSums
-    s = WpFitSums()
-    s.p_edman_failure_num, s.p_edman_failure_den = o.edman_num, o.edman_den
-    for i in range(len(s.p_detach_x)):
-        s.p_detach_x[i], s.p_detach_n[i] = o.detach_x[i], o.detach_n[i]
-    s.p_initial_block_num, s.p_initial_block_den = o.init_block_num, o.init_block_den
-    s.p_cyclic_block_num, s.p_cyclic_block_den = o.cyc_block_num, o.cyc_block_den
-    for c in range(len(s.p_bleach_num)):
-        s.p_bleach_num[c], s.p_bleach_den[c] = o.bleach_num[c], o.bleach_den[c]
-        s.p_dud_num[c], s.p_dud_den[c] = o.dud_num[c], o.dud_den[c]
-    return s
+    from oracle_lib import oracle_sums_to_wp
+    return oracle_sums_to_wp(o)
 
 
 def _params_model(p, sm):

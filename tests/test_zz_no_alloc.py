@@ -5,8 +5,9 @@ may not stall the device with an allocation, or a host that runs the library
 under a memory budget it does not own.  It keeps everything in one fixed
 device array that all calls share, so this test calls it twice in a row
 through the C ABI and checks both results against wp_hmm_classify on the
-same inputs, with the tolerance the other parity tests use (ids identical,
-score/total within 1e-5 relative).  It lives in its own file, collected last,
+same inputs (ids identical; score and total each within 1e-5 relative, and
+finite) and against the oracle's FP64 classify (top-1 identical, adjusted
+score within 1e-5 relative, the tolerance the other parity tests use).  It lives in its own file, collected last,
 so that a run stopping at its failure has run everything else first."""
 import ctypes
 
@@ -55,6 +56,17 @@ def test_noalloc_matches_classify_twice(block):
     ctx.upload_peptides(ds)
     want_id, want_sc, want_tot, _ = ctx.classify(rads, 5.0)
     ctx.close()
+    from oracle_lib import Oracle
+    oracle = Oracle()
+    o_id, o_sc, o_tot = oracle.classify(sm, T, ds, rads, 5.0, threads=4)
+    # a different top-1 is accepted only for an HMM tie (oracle log P of
+    # both peptides equal within 1e-5)
+    index = {int(i): k for k, i in enumerate(ds.ids)}
+    diff = np.nonzero(want_id != o_id)[0]
+    if diff.size:
+        ll = oracle.loglik_all(sm, T, ds, rads[diff], 5.0, threads=4)
+        for j, r in enumerate(diff):
+            assert abs(ll[j, index[int(want_id[r])]] - ll[j, index[int(o_id[r])]]) <= 1e-5, r
 
     f = _bind(capi.load_library())
     m, keep = _model_struct(sm)
@@ -70,7 +82,10 @@ def test_noalloc_matches_classify_twice(block):
                len(ds), r.ctypes.data, R, 5.0, oid.ctypes.data, osc.ctypes.data, otot.ctypes.data)
         assert st == 0, (call, st)
         assert np.array_equal(oid, want_id), call
-        np.testing.assert_allclose(osc / otot, want_sc / want_tot, rtol=1e-5, atol=0)
+        assert np.all(np.isfinite(osc)) and np.all(np.isfinite(otot)), call
+        np.testing.assert_allclose(osc, want_sc, rtol=1e-5, atol=0)
+        np.testing.assert_allclose(otot, want_tot, rtol=1e-5, atol=0)
+        np.testing.assert_allclose(osc / otot, o_sc / o_tot, rtol=1e-5, atol=0)
 
 
 def test_noalloc_rejects_oversized():

@@ -323,19 +323,6 @@ void collect_timing(wp_ctx* ctx) {
 
 // BinomialTransition::reserve (hmm/step/binomial-transition.cc:51-67) in
 // FP64, rounded once to FP32.
-void binomial_table(double q, int max_n, float* out) {
-    std::vector<double> tab((max_n + 1) * (max_n + 2) / 2);
-    double p = 1.0 - q;
-    tab[0] = 1.0;
-    for (int i = 1; i <= max_n; i++) {
-        tab[i * (i + 1) / 2] = tab[(i - 1) * i / 2] * q;
-        for (int j = 1; j < i; j++)
-            tab[i * (i + 1) / 2 + j] = tab[(i - 1) * i / 2 + j] * q + tab[(i - 1) * i / 2 + j - 1] * p;
-        tab[i * (i + 1) / 2 + i] = tab[(i - 1) * i / 2 + i - 1] * p;
-    }
-    for (size_t k = 0; k < tab.size(); k++) out[k] = (float)tab[k];
-}
-
 // Per-peptide records (DyeSeqPrecomputations, dye-seq-precomputations.cc:
 // 20-39) for the current (C, T).
 wp_status plan_peptides(wp_ctx* ctx) {
@@ -1503,31 +1490,7 @@ wp_status build_dev_model(wp_ctx* ctx, const wp_seq_model* m, int T, DevModel* h
     if (T < 1 || T > WP_MAX_TIMESTEPS) return fail(ctx, WP_ERR_UNSUPPORTED, "num_timesteps out of range 1..64");
     if (!m->p_bleach || !m->p_dud || !m->bg_sig || !m->mu || !m->sig)
         return fail(ctx, WP_ERR_INVALID, "null per-channel array");
-    DevModel& h = *hp;
-    memset(&h, 0, sizeof(h));
-    h.C = C;
-    h.T = T;
-    h.pf = (float)m->p_edman_failure;
-    h.p_ib = (float)m->p_initial_block;
-    h.p_cb = (float)m->p_cyclic_block;
-    h.has_block = (m->p_initial_block != 0.0 || m->p_cyclic_block != 0.0) ? 1 : 0;
-    for (int t = 0; t < T; t++)  // DecayingRateModel (decaying-rate-model.cc:47-50)
-        h.p_det[t] = (float)(m->p_detach + m->p_initial_detach * std::exp(-(double)t * m->p_initial_detach_decay));
-    h.interacting = 0;
-    for (int c = 0; c < C; c++) {
-        binomial_table(m->p_dud[c], WP_MAX_DYES_PER_CHANNEL, h.dud[c]);
-        binomial_table(m->p_bleach[c], WP_MAX_DYES_PER_CHANNEL, h.bleach[c]);
-        h.bg_sig[c] = m->bg_sig[c];
-        h.sig[c] = m->sig[c];
-        h.mu[c] = m->mu[c];
-        for (int o = 0; o < C; o++) {
-            h.inter[c][o] = m->interactions ? m->interactions[c * C + o] : 1.0;
-            h.flat[c][o] = m->flat_interactions ? m->flat_interactions[c * C + o] : 1.0;
-            if (h.inter[c][o] != 1.0 || h.flat[c][o] != 1.0) h.interacting = 1;
-        }
-    }
-    wp_fill_emission_tables(h);
-    return WP_OK;
+    return wp_fill_dev_model(m, T, hp);
 }
 
 wp_status wp_model_upload(wp_ctx* ctx, const wp_seq_model* m, int T) {

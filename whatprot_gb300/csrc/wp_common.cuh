@@ -14,6 +14,7 @@
 #pragma once
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "../../include/whatprot_gb300.h"
 #include "wp_kdtree.h"
@@ -66,6 +67,61 @@ inline void wp_fill_emission_tables(DevModel& m) {
             m.e_norm[c][n] = 1.0 / (s * sqrt(2.0 * pi));
             m.e_den[c][n] = 2.0 * s * s;
         }
+}
+
+// BinomialTransition::reserve (hmm/step/binomial-transition.cc:51-67): the
+// triangular table prob(from, to) of `to` of `from` dyes surviving (each
+// lost with probability q), from an FP64 running row updated in place and
+// rounded once into the FP32 output (no allocation).
+inline void wp_binomial_table(double q, int max_n, float* out) {
+    double row[WP_MAX_DYES_PER_CHANNEL + 1];
+    const double p = 1.0 - q;
+    row[0] = 1.0;
+    out[0] = 1.0f;
+    for (int i = 1; i <= max_n; i++) {
+        const double prev_diag = row[i - 1];
+        for (int j = i - 1; j >= 1; j--) row[j] = row[j] * q + row[j - 1] * p;
+        row[0] = row[0] * q;
+        row[i] = prev_diag * p;
+        for (int j = 0; j <= i; j++) out[i * (i + 1) / 2 + j] = (float)row[j];
+    }
+}
+
+// The device model of a SequencingModel for T timesteps (the model part of
+// UniversalPrecomputations, hmm/precomputations/universal-precomputations.cc:
+// 23-59): FP32 rates, detach rate per timestep (DecayingRateModel,
+// decaying-rate-model.cc:47-50), binomial dud/bleach tables, the FP64
+// emission model and its per-count tables.  Host only; allocates nothing.
+// Returns WP_OK, or the status for a shape or a null array it does not take.
+inline wp_status wp_fill_dev_model(const wp_seq_model* m, int T, DevModel* hp) {
+    const int C = m->num_channels;
+    if (C < 1 || C > WP_MAX_CHANNELS || T < 1 || T > WP_MAX_TIMESTEPS) return WP_ERR_UNSUPPORTED;
+    if (!m->p_bleach || !m->p_dud || !m->bg_sig || !m->mu || !m->sig) return WP_ERR_INVALID;
+    DevModel& h = *hp;
+    memset(&h, 0, sizeof(h));
+    h.C = C;
+    h.T = T;
+    h.pf = (float)m->p_edman_failure;
+    h.p_ib = (float)m->p_initial_block;
+    h.p_cb = (float)m->p_cyclic_block;
+    h.has_block = (m->p_initial_block != 0.0 || m->p_cyclic_block != 0.0) ? 1 : 0;
+    for (int t = 0; t < T; t++)
+        h.p_det[t] = (float)(m->p_detach + m->p_initial_detach * exp(-(double)t * m->p_initial_detach_decay));
+    h.interacting = 0;
+    for (int c = 0; c < C; c++) {
+        wp_binomial_table(m->p_dud[c], WP_MAX_DYES_PER_CHANNEL, h.dud[c]);
+        wp_binomial_table(m->p_bleach[c], WP_MAX_DYES_PER_CHANNEL, h.bleach[c]);
+        h.bg_sig[c] = m->bg_sig[c];
+        h.sig[c] = m->sig[c];
+        h.mu[c] = m->mu[c];
+        for (int o = 0; o < C; o++) {
+            h.inter[c][o] = m->interactions ? m->interactions[c * C + o] : 1.0;
+            h.flat[c][o] = m->flat_interactions ? m->flat_interactions[c * C + o] : 1.0;
+            if (h.inter[c][o] != 1.0 || h.flat[c][o] != 1.0) h.interacting = 1;
+        }
+    }
+    wp_fill_emission_tables(h);
+    return WP_OK;
 }
 
 // One peptide.  dye[e] is the channel removed by a successful Edman cycle at

@@ -75,22 +75,6 @@ __global__ void wp_noalloc_peptides_kernel(const int16_t* __restrict__ seqs,
     out[i] = rec;
 }
 
-void binomial_table_f(double q, int max_n, float* out) {
-    // BinomialTransition::reserve (hmm/step/binomial-transition.cc:51-67),
-    // computed in place in the FP32 output row from an FP64 running row.
-    double row[WP_MAX_DYES_PER_CHANNEL + 1];
-    double p = 1.0 - q;
-    row[0] = 1.0;
-    out[0] = 1.0f;
-    for (int i = 1; i <= max_n; i++) {
-        double prev_diag = row[i - 1];
-        for (int j = i - 1; j >= 1; j--) row[j] = row[j] * q + row[j - 1] * p;
-        row[0] = row[0] * q;
-        row[i] = prev_diag * p;
-        for (int j = 0; j <= i; j++) out[i * (i + 1) / 2 + j] = (float)row[j];
-    }
-}
-
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
@@ -106,9 +90,10 @@ extern "C" wp_status wp_hmm_classify_noalloc(int device, const wp_seq_model* m, 
     const int C = m->num_channels;
     if (C < 1 || C > WP_MAX_CHANNELS || T < 1 || T > WP_MAX_TIMESTEPS) return WP_ERR_UNSUPPORTED;
     if (!m->p_bleach || !m->p_dud || !m->bg_sig || !m->mu || !m->sig) return WP_ERR_INVALID;
-    if (offsets[0] != 0) return WP_ERR_INVALID;
+    if (offsets[0] != 0 || offsets[P] < 0) return WP_ERR_INVALID;
+    if (offsets[P] > 0 && !dye_seqs) return WP_ERR_INVALID;
     // Peptide shape summary on the host, without allocating.
-    int dmax = 0, S_max = 1, scr = 1;
+    int dmax = 0, S_max = 1;
     for (int i = 0; i < P; i++) {
         if (offsets[i + 1] < offsets[i]) return WP_ERR_INVALID;
         int cnt[WP_MAX_CHANNELS] = {0, 0, 0, 0};
@@ -117,43 +102,21 @@ extern "C" wp_status wp_hmm_classify_noalloc(int device, const wp_seq_model* m, 
             if (d < -1 || d >= C) return WP_ERR_INVALID;
             if (d >= 0) cnt[d]++;
         }
-        int prod = 1, sum = 0;
+        int prod = 1;
         for (int c = 0; c < C; c++) {
             if (cnt[c] > WP_MAX_DYES_PER_CHANNEL) return WP_ERR_UNSUPPORTED;
             dmax = cnt[c] > dmax ? cnt[c] : dmax;
             prod *= cnt[c] + 1;
-            sum += cnt[c] + 1;
         }
         S_max = prod > S_max ? prod : S_max;
-        scr = sum > scr ? sum : scr;
     }
     if (R == 0) return WP_OK;
 
     // Layout of the scratch array for this call; reject what does not fit.
     DevModel hm;
-    memset(&hm, 0, sizeof(hm));
+    const wp_status mst = wp_fill_dev_model(m, T, &hm);
+    if (mst != WP_OK) return mst;
     const int W = dmax + 1;
-    hm.C = C;
-    hm.T = T;
-    hm.pf = (float)m->p_edman_failure;
-    hm.p_ib = (float)m->p_initial_block;
-    hm.p_cb = (float)m->p_cyclic_block;
-    hm.has_block = (m->p_initial_block != 0.0 || m->p_cyclic_block != 0.0) ? 1 : 0;
-    for (int t = 0; t < T; t++)
-        hm.p_det[t] = (float)(m->p_detach + m->p_initial_detach * std::exp(-(double)t * m->p_initial_detach_decay));
-    for (int c = 0; c < C; c++) {
-        binomial_table_f(m->p_dud[c], WP_MAX_DYES_PER_CHANNEL, hm.dud[c]);
-        binomial_table_f(m->p_bleach[c], WP_MAX_DYES_PER_CHANNEL, hm.bleach[c]);
-        hm.bg_sig[c] = m->bg_sig[c];
-        hm.sig[c] = m->sig[c];
-        hm.mu[c] = m->mu[c];
-        for (int o = 0; o < C; o++) {
-            hm.inter[c][o] = m->interactions ? m->interactions[c * C + o] : 1.0;
-            hm.flat[c][o] = m->flat_interactions ? m->flat_interactions[c * C + o] : 1.0;
-            if (hm.inter[c][o] != 1.0 || hm.flat[c][o] != 1.0) hm.interacting = 1;
-        }
-    }
-    wp_fill_emission_tables(hm);
     const int entries = wp_read_table_entries(T, C, W, hm.interacting);
     const long n_slots = (long)R * P;
     const size_t rtc = (size_t)R * T * C;
@@ -254,12 +217,13 @@ extern "C" wp_status wp_hmm_classify_noalloc(int device, const wp_seq_model* m, 
     wp_read_summary_kernel<<<(R + 127) / 128, 128, 0, s>>>(a);
     WP_NA(cudaGetLastError());
     // Engine passes: the shapes the allocating path uses (two CTAs of 256
-    // threads per SM, then one of 128), then the dense fallback.
+    // threads per SM, then one of 128; no per-thread scratch floats, as
+    // there), then the dense fallback.
     auto half_for = [&](int threads, int per_sm) {
         size_t budget = smem_optin;
         if (per_sm > 1 && budget > (size_t)(228 * 1024) / per_sm - 1024) budget = (size_t)(228 * 1024) / per_sm - 1024;
         size_t elem = hb ? 8 : 4;
-        size_t fixed = wp_engine_smem_bytes(0, scr, hb, threads);
+        size_t fixed = wp_engine_smem_bytes(0, 0, hb, threads);
         return budget <= fixed ? 0 : (int)((budget - fixed) / (2 * elem * threads));
     };
     const int half1 = half_for(256, 2), half2 = half_for(128, 1);
@@ -281,11 +245,11 @@ extern "C" wp_status wp_hmm_classify_noalloc(int device, const wp_seq_model* m, 
     a.route_dense = dense_warps > 0 ? 1 : 0;
     wp_compact_kernel<<<R, 256, 0, s>>>(a);
     WP_NA(cudaGetLastError());
-    WP_NA(wp_launch_engine(C, hb, 256, wp_engine_smem_bytes(half1, scr, hb, 256), s, a, a.work, cnt + 0,
-                           cnt + 1, reinterpret_cast<int2*>(base + o_ovf1), cnt + 2, half1, scr, 0, nullptr));
-    WP_NA(wp_launch_engine(C, hb, 128, wp_engine_smem_bytes(half2, scr, hb, 128), s, a,
+    WP_NA(wp_launch_engine(C, hb, 256, wp_engine_smem_bytes(half1, 0, hb, 256), s, a, a.work, cnt + 0,
+                           cnt + 1, reinterpret_cast<int2*>(base + o_ovf1), cnt + 2, half1, 0, 0, nullptr));
+    WP_NA(wp_launch_engine(C, hb, 128, wp_engine_smem_bytes(half2, 0, hb, 128), s, a,
                            reinterpret_cast<int2*>(base + o_ovf1), cnt + 2, cnt + 3,
-                           reinterpret_cast<int2*>(base + o_ovf2), cnt + 4, half2, scr,
+                           reinterpret_cast<int2*>(base + o_ovf2), cnt + 4, half2, 0,
                            dense_warps == 0 ? 1 : 0, nullptr));
     if (dense_warps > 0)
         WP_NA(wp_launch_dense(hb, dense_warps * 32, wp_dense_smem_bytes(T, a.dense_S_cap, C, hb, dense_warps), s, a));
