@@ -950,7 +950,7 @@ def loglik_parity(ctx, sm, ds, rads, n=500):
     g = ctx.loglik_all(rads[:n], CUTOFF)
     o = Oracle().loglik_all(sm, T, ds, rads[:n], CUTOFF, threads=os.cpu_count() or 1)
     fin = np.isfinite(g) & np.isfinite(o)
-    d = np.abs(g - o)[fin]
+    d = np.abs(g[fin] - o[fin])
     best = np.argmax(np.where(np.isfinite(o), o, -np.inf), axis=1)
     db = np.abs(g[np.arange(n), best] - o[np.arange(n), best])
     db = db[np.isfinite(db)]
