@@ -434,6 +434,138 @@ __device__ __noinline__ float emission_narrow(V* cur, int stride, int t, PBox nx
     return part;
 }
 
+// Edman (edman-transition.cc:62-162) and emission (peptide-emission.cc:
+// 212-243) of one timestep in one pass, for emission boxes at most 4 wide
+// per channel without interactions: edman_gather followed by
+// emission_narrow, with the emission box's state j outer and the Edman
+// slice e inner, so that a state's index work (its place in the bleached
+// box bx, its dye counts, the channels with a state one dye up) is done once
+// per state instead of once per (state, slice), and the Edman output is
+// multiplied by its emission factor before it is stored.  cur holds the
+// bleached box (t slices), nxt receives the emission box (t + 1 slices).
+// The bleached box's per-slice volume must be at most 255.  Returns the sum
+// of the new states; *kmax_out the normalising exponent (WP_EXPO_ZERO: every
+// factor of some channel is zero), *em0_out the all-zero state's factor.
+template <int C, bool HB>
+__device__ __noinline__ float edman_emit(const typename StateOf<HB>::V* __restrict__ cur,
+                                         typename StateOf<HB>::V* __restrict__ nxt, int stride, int t, PBox bx,
+                                         PBox nx, uint64_t dye_pk, uint64_t tot_pk, const float2* __restrict__ edman,
+                                         float pf, const EmitEntry* __restrict__ tab, int W, bool allow_t, float sf,
+                                         int* kmax_out, float* em0_out) {
+    using V = typename StateOf<HB>::V;
+    // per channel: the box's emission entries normalised by their largest
+    // exponent (as emission_narrow)
+    float g[C][4];
+    int kmax = 0;
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+        const EmitEntry* row = tab + (t * C + c) * W + bget(nx.lo, c);
+        const int wc = bget(nx.w, c);
+        EmitEntry en[4];
+        int km = WP_EXPO_ZERO;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            en[k].mant = 0.0f;
+            en[k].expo = WP_EXPO_ZERO;
+            if (k < wc) en[k] = row[k];
+            if (en[k].mant != 0.0f) km = max(km, en[k].expo);
+        }
+        if (km == WP_EXPO_ZERO) {
+            *kmax_out = WP_EXPO_ZERO;
+            return 0.0f;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            g[c][k] = en[k].mant != 0.0f ? en[k].mant * exp2i(max(en[k].expo - km, -200)) : 0.0f;
+        kmax += km;
+    }
+    *kmax_out = kmax;
+    if (allow_t) {
+        float em0 = 1.0f;
+#pragma unroll
+        for (int c = 0; c < C; c++) em0 *= g[c][0];
+        *em0_out = em0;
+    }
+    // the bleached box's strides, one byte per channel
+    uint32_t stpk = 0;
+    int vb = 1;
+#pragma unroll
+    for (int c = C - 1; c >= 0; c--) {
+        stpk = bset(stpk, c, vb);
+        vb *= bget(bx.w, c);
+    }
+    const int vn = bvol<C>(nx.w);
+    const int sb = vb * stride, sn = vn * stride;
+    float part = 0.0f;
+    int jc[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) jc[c] = 0;
+    for (int j = 0; j < vn; j++) {
+        int ib = 0;
+        uint32_t cnt = nx.lo, up = 0;
+        float w = sf;
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+            const int k = jc[c];
+            ib += k * bget(stpk, c);
+            cnt += (uint32_t)k << (8 * c);
+            if (k + 1 < bget(bx.w, c)) up |= 1u << c;
+            w *= k == 0 ? g[c][0] : k == 1 ? g[c][1] : k == 2 ? g[c][2] : g[c][3];
+        }
+        const V* col = cur + ib * stride;
+        V* out = nxt + j * stride;
+        uint64_t dp = dye_pk, tp = tot_pk;
+        V prev = vzero(V());
+        for (int e = 0; e <= t; e++) {
+            const V f = e < t ? col[e * sb] : vzero(V());
+            V v;
+            if constexpr (HB) {
+                v = make_float2(pf * f.x, f.y);  // broken-N copied unchanged
+            } else {
+                v = pf * f;
+            }
+            if (e >= 1) {
+                const int d4 = (int)(dp & 15);  // dye channel + 1 (0: no dye)
+                const int tot_i = (int)(tp & 15);
+                dp >>= 4;
+                tp >>= 4;
+                const int sh = 8 * max(d4 - 1, 0);
+                const float2 cf = edman[(d4 ? tot_i : 0) * 16 + (int)((cnt >> sh) & 0xffu)];
+                float xin;
+                if constexpr (HB) {
+                    xin = prev.x;
+                } else {
+                    xin = prev;
+                }
+                float add = cf.x * xin;
+                if (d4 && ((up >> (d4 - 1)) & 1u)) {
+                    const V xr = col[(e - 1) * sb + (int)((stpk >> sh) & 0xffu) * stride];
+                    if constexpr (HB) {
+                        add = fmaf(cf.y, xr.x, add);
+                    } else {
+                        add = fmaf(cf.y, xr, add);
+                    }
+                }
+                if constexpr (HB) {
+                    v.x += add;
+                } else {
+                    v += add;
+                }
+            }
+            prev = f;
+            const V sv = vmul(w, v);
+            out[e * sn] = sv;
+            part += vtotal(sv);
+        }
+#pragma unroll
+        for (int c = C - 1; c >= 0; c--) {
+            if (++jc[c] < bget(nx.w, c)) break;
+            jc[c] = 0;
+        }
+    }
+    return part;
+}
+
 // Runs one pair.  Returns 1 when its boxes exceed the slab (nothing
 // written), else 0 with P = *mant * 2^*expo (mant == 0: P == 0).
 template <int C, bool HB>
@@ -563,6 +695,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         int kmax = 0;
         float part = 0.0f;
         float em0 = 0.0f;
+        bool fused = false;  // Edman and emission done together (edman_emit)
         if (t > 0) {
             bscale = 1.0f;
             // Cyclic block (block-transition.cc:33-62) over e < t and the
@@ -600,7 +733,20 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             // (success) and e (failure) of the bleached box into the
             // emission box; both boxes share the lower corner L_t.
             if (!single) {
-                edman_gather<C, HB>(cur, nxt, stride, t, bx, nx, pk, dye_pk, tot_pk, pep, M.edman, m.pf);
+                fused = pk && !m.interacting && bvol<C>(bx.w) <= 255;
+#pragma unroll
+                for (int c = 0; c < C; c++) fused = fused && bget(nx.w, c) <= 4;
+                if (fused) {
+                    part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, dye_pk, tot_pk, M.edman, m.pf, tab, a.W,
+                                             allow_t, fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
+                    if (kmax == WP_EXPO_ZERO) {
+                        *out_mant = 0.0f;
+                        *out_expo = 0;
+                        return 0;
+                    }
+                } else {
+                    edman_gather<C, HB>(cur, nxt, stride, t, bx, nx, pk, dye_pk, tot_pk, pep, M.edman, m.pf);
+                }
                 V* tmp = cur;
                 cur = nxt;
                 nxt = tmp;
@@ -613,7 +759,9 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         bool narrow = !m.interacting;
 #pragma unroll
         for (int c = 0; c < C; c++) narrow = narrow && bget(nx.w, c) <= 4;
-        if (single) {
+        if (fused) {
+            // edman_emit applied the emission
+        } else if (single) {
             // The box's one state has factor prod_c mant_c * 2^(sum_c expo_c);
             // the multiplier also carries the pending rescale and bscale.
             float wv = fac_prev * bscale * exp2i(min(-k_prev, 127));
