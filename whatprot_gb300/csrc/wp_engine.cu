@@ -103,6 +103,34 @@ __device__ __noinline__ void binomial_step(const V* __restrict__ src, V* __restr
     }
     const int win = bget(in.w, ch), from0 = bget(in.lo, ch);
     const int sk = inner * stride;
+    if (win <= 3 && wout <= 3) {
+        // The coefficients prob(from0 + k -> to0 + k2) in registers; each
+        // input column (its up to 3 states along ch) is loaded once and
+        // gives all the column's outputs.
+        float cf[3][3];
+#pragma unroll
+        for (int k2 = 0; k2 < 3; k2++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const int from = from0 + k, to = to0 + k2;
+                cf[k2][k] = (k < win && k2 < wout && from >= to) ? tab[from * (from + 1) / 2 + to] : 0.0f;
+            }
+        for (int o = 0; o < outer; o++) {
+            const V* s = src + o * win * sk;
+            V* d = dst + o * wout * sk;
+            for (int i = 0; i < inner; i++) {
+                const V* si = s + i * stride;
+                const V x0 = si[0];
+                const V x1 = win > 1 ? si[sk] : vzero(V());
+                const V x2 = win > 2 ? si[2 * sk] : vzero(V());
+                V* di = d + i * stride;
+#pragma unroll
+                for (int k2 = 0; k2 < 3; k2++)
+                    if (k2 < wout) di[k2 * sk] = vfma(cf[k2][2], x2, vfma(cf[k2][1], x1, vmul(cf[k2][0], x0)));
+            }
+        }
+        return;
+    }
     if (win <= 4) {
         // Coefficients depend on (to, from) only: load them once per output
         // row, then one predicated dot product per column.
@@ -447,7 +475,7 @@ __device__ __noinline__ float emission_narrow(V* cur, int stride, int t, PBox nx
 // of the new states; *kmax_out the normalising exponent (WP_EXPO_ZERO: every
 // factor of some channel is zero), *em0_out the all-zero state's factor.
 template <int C, bool HB>
-__device__ __noinline__ float edman_emit(const typename StateOf<HB>::V* __restrict__ cur,
+__device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __restrict__ cur,
                                          typename StateOf<HB>::V* __restrict__ nxt, int stride, int t, PBox bx,
                                          PBox nx, uint64_t dye_pk, uint64_t tot_pk, const float2* __restrict__ edman,
                                          float pf, const EmitEntry* __restrict__ tab, int W, bool allow_t, float sf,
