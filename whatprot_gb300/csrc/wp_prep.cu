@@ -35,6 +35,7 @@
 
 #define WP_COMPACT_SORT 1024  // candidate slots per read the compaction orders by shape
 #define WP_COMPACT_UNIQ 1024  // distinct dye-count vectors the compaction tabulates per read
+#define WP_COMPACT_CHUNK 2048  // slots the compaction routes per round of list appends
 
 
 // ChannelModel::adjusted_mu (parameterization/model/channel-model.h:35-54).
@@ -266,8 +267,9 @@ __global__ void wp_read_summary_kernel(BatchArgs a) {
     a.flags[r] = (uint8_t)empty;
 }
 
-// One CTA per read.  Warp-aggregated appends keep each warp's pairs
-// contiguous in the work list (they share the read's data in L1).
+// One CTA per read (at most 1,024 threads, a multiple of 32).  CTA-aggregated
+// appends keep the read's pairs of each list contiguous (they share the
+// read's data in L1) and cost one global atomic per list per 2,048 slots.
 __global__ void wp_compact_kernel(BatchArgs a) {
     const int r = blockIdx.x;
     const DevModel& m = *a.model;
@@ -280,6 +282,8 @@ __global__ void wp_compact_kernel(BatchArgs a) {
     const int lane = threadIdx.x & 31;
     // the read's box words, shared by all its pairs
     __shared__ uint32_t sL[WP_MAX_TIMESTEPS], sU[WP_MAX_TIMESTEPS];
+    __shared__ int s_live;  // the read's non-empty pairs
+    if (threadIdx.x == 0) s_live = 0;
     for (int t = threadIdx.x; t < m.T; t += blockDim.x) {
         sL[t] = a.Lpk[(long)r * m.T + t];
         sU[t] = a.Upk[(long)r * m.T + t];
@@ -330,57 +334,103 @@ __global__ void wp_compact_kernel(BatchArgs a) {
             }
     }
     __syncthreads();
-    for (int base = g0; base < g1; base += blockDim.x) {
-        // Walk the peptides in shape order (all-peptides mode: the global
-        // order; candidate mode: the read's sorted slots), so that the
-        // engine's warps get pairs of similar size; results still go to
-        // their own slots, so the candidate order (ties) is unchanged.
-        int g = base + threadIdx.x;
-        if (g < g1 && a.perm) g = g0 + a.perm[g - g0];
-        if (g < g1 && sorted) g = g0 + (int)(order[g - g0] & 0xffffffffu);
-        int dest = -1;  // tier index, WP_MAX_TIERS: the dense kernel's list
-        if (base + threadIdx.x < g1) {
-            int p = slot_pep(a, r, g);
-            const PeptideRec& pep = a.peps[p];
-            bool live = !read_empty;
-            for (int c = 0; c < C; c++)
-                if (pep.D[c] < minD[c]) live = false;
-            if (live) {
-                // the pair's largest box waits in its result slot for the
-                // engine, which checks it against its slab before any write
-                const int vm = vtab ? s_vmax[a.pep_u[p]] : pair_vmax(C, m.T, sL, sU, pep.D);
-                a.res_expo[g] = vm;
-                dest = 0;
-                if (a.n_tiers > 0) {
-                    dest = WP_MAX_TIERS;
-                    for (int k = a.n_tiers - 1; k >= 0; k--)
-                        if (vm <= a.tier_half[k]) dest = k;
-                    if (dest == WP_MAX_TIERS && !a.route_dense) {
-                        atomicExch(a.err, 2);  // no shape holds this pair
-                        dest = -1;
+    // Lists are appended per CTA: the read's pairs of a list take one
+    // contiguous range (one global atomic per list per chunk of slots, not
+    // one per warp), in the walk's order.
+    constexpr int NL = WP_MAX_TIERS + 1;
+    __shared__ uint8_t s_dest[WP_COMPACT_CHUNK];
+    __shared__ int s_off[WP_COMPACT_CHUNK / 32][NL];  // per (iteration, warp): count, then start
+    const int wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int per_chunk = (WP_COMPACT_CHUNK / blockDim.x) * blockDim.x;
+    for (int c0 = g0; c0 < g1; c0 += per_chunk) {
+        const int c1 = min(g1, c0 + per_chunk);
+        const int nit = (c1 - c0 + blockDim.x - 1) / blockDim.x;
+        // phase A: each slot's list (or none), counted per warp and list
+        for (int it = 0; it < nit; it++) {
+            const int base = c0 + it * blockDim.x;
+            // Walk the peptides in shape order (all-peptides mode: the
+            // global order; candidate mode: the read's sorted slots), so
+            // that the engine's warps get pairs of similar size; results
+            // still go to their own slots, so the candidate order (ties) is
+            // unchanged.
+            int g = base + threadIdx.x;
+            if (g < g1 && a.perm) g = g0 + a.perm[g - g0];
+            if (g < g1 && sorted) g = g0 + (int)(order[g - g0] & 0xffffffffu);
+            int dest = -1;  // tier index, WP_MAX_TIERS: the dense kernel's list
+            if (base + threadIdx.x < g1) {
+                int p = slot_pep(a, r, g);
+                const PeptideRec& pep = a.peps[p];
+                bool live = !read_empty;
+                for (int c = 0; c < C; c++)
+                    if (pep.D[c] < minD[c]) live = false;
+                if (live) {
+                    // the pair's largest box waits in its result slot for
+                    // the engine, which checks it against its slab before
+                    // any write
+                    const int vm = vtab ? s_vmax[a.pep_u[p]] : pair_vmax(C, m.T, sL, sU, pep.D);
+                    a.res_expo[g] = vm;
+                    dest = 0;
+                    if (a.n_tiers > 0) {
+                        dest = WP_MAX_TIERS;
+                        for (int k = a.n_tiers - 1; k >= 0; k--)
+                            if (vm <= a.tier_half[k]) dest = k;
+                        if (dest == WP_MAX_TIERS && !a.route_dense) {
+                            atomicExch(a.err, 2);  // no shape holds this pair
+                            dest = -1;
+                        }
                     }
                 }
+                if (dest < 0) {
+                    a.res_mant[g] = 0.0f;
+                    a.res_expo[g] = 0;
+                }
             }
-            if (dest < 0) {
-                a.res_mant[g] = 0.0f;
-                a.res_expo[g] = 0;
-            }
-        }
-        if (a.live_count) {
+            s_dest[it * blockDim.x + threadIdx.x] = dest < 0 ? 0xffu : (uint8_t)dest;
             const unsigned lm = __ballot_sync(0xffffffffu, dest >= 0);
-            if (lane == 0 && lm) atomicAdd(a.live_count, __popc(lm));
+            if (lane == 0 && lm) atomicAdd(&s_live, __popc(lm));
+            for (int k = 0; k < NL; k++) {
+                const unsigned mask = __ballot_sync(0xffffffffu, dest == k);
+                if (lane == 0) s_off[it * nwarp + wid][k] = __popc(mask);
+            }
         }
-        // warp-aggregated appends, one per list
-        for (int k = 0; k <= WP_MAX_TIERS; k++) {
-            const unsigned mask = __ballot_sync(0xffffffffu, dest == k);
-            if (!mask) continue;
-            const bool dense = k == WP_MAX_TIERS;
-            int* count = dense ? a.ovf_count : a.n_tiers > 0 ? a.tier_count[k] : a.work_count;
-            int2* list = dense ? a.ovf : a.n_tiers > 0 ? a.tier_list[k] : a.work;
-            int pos = 0;
-            if (lane == 0) pos = atomicAdd(count, __popc(mask));
-            pos = __shfl_sync(0xffffffffu, pos, 0);
-            if (dest == k) list[pos + __popc(mask & ((1u << lane) - 1))] = make_int2(r, g);
+        __syncthreads();
+        // one range per list: its start, then each (iteration, warp)'s start
+        if (threadIdx.x < NL) {
+            const int k = threadIdx.x;
+            const int n = nit * nwarp;
+            int total = 0;
+            for (int i = 0; i < n; i++) total += s_off[i][k];
+            int start = 0;
+            if (total > 0) {
+                const bool dense = k == WP_MAX_TIERS;
+                int* count = dense ? a.ovf_count : a.n_tiers > 0 ? a.tier_count[k] : a.work_count;
+                start = atomicAdd(count, total);
+            }
+            for (int i = 0; i < n; i++) {
+                const int c = s_off[i][k];
+                s_off[i][k] = start;
+                start += c;
+            }
         }
+        __syncthreads();
+        // phase B: the appends
+        for (int it = 0; it < nit; it++) {
+            const int base = c0 + it * blockDim.x;
+            int g = base + threadIdx.x;
+            if (g < g1 && a.perm) g = g0 + a.perm[g - g0];
+            if (g < g1 && sorted) g = g0 + (int)(order[g - g0] & 0xffffffffu);
+            const uint8_t d8 = s_dest[it * blockDim.x + threadIdx.x];
+            const int dest = d8 == 0xffu ? -1 : (int)d8;
+            for (int k = 0; k < NL; k++) {
+                const unsigned mask = __ballot_sync(0xffffffffu, dest == k);
+                if (dest == k) {
+                    const bool dense = k == WP_MAX_TIERS;
+                    int2* list = dense ? a.ovf : a.n_tiers > 0 ? a.tier_list[k] : a.work;
+                    list[s_off[it * nwarp + wid][k] + __popc(mask & ((1u << lane) - 1))] = make_int2(r, g);
+                }
+            }
+        }
+        __syncthreads();
     }
+    if (threadIdx.x == 0 && a.live_count && s_live) atomicAdd(a.live_count, s_live);
 }
