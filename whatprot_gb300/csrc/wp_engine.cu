@@ -31,12 +31,16 @@
 // most timesteps of most pairs have a one-state emission box: a dud or
 // bleach step along a channel that is one wide on both sides is a single
 // coefficient, carried to the next emission multiply instead of a pass over
-// the state; and a one-state emission box runs Edman and emission as one
-// loop over the Edman slices.  Edman coefficients come from a per-CTA table
-// indexed by (remaining dyes of the cut channel, dye count of the state).
+// the state (checked for all channels at once with word operations); and
+// Edman and emission run as one loop, state outer and Edman slice inner,
+// for every emission box at most 4 wide per channel, one-state boxes
+// included.  Edman coefficients come from a per-CTA table indexed by
+// (remaining dyes of the cut channel, dye count of the state).
 // All lanes of a warp process the same timestep together (lanes are pairs
 // of one read), so a warp pays for every path any of its lanes takes in a
-// timestep; the number of distinct paths is kept small for that reason.
+// timestep; the number of distinct paths is kept small for that reason.  A
+// separate one-state path (cheaper per lane) cost more than it saved, as
+// warps whose lanes mixed one-state and wider boxes ran both paths.
 //
 // With blocking (p_initial_block or p_cyclic_block nonzero) each state holds
 // the normal and the broken-N value as a float2.
@@ -78,6 +82,12 @@ __device__ __forceinline__ int bget(uint32_t v, int c) { return (int)((v >> (8 *
 __device__ __forceinline__ uint32_t bset(uint32_t v, int c, int x) {
     return (v & ~(0xffu << (8 * c))) | ((uint32_t)x << (8 * c));
 }
+// The bytes of a packed word that hold channels.
+template <int C>
+__device__ __forceinline__ uint32_t chan_mask() {
+    return C >= 4 ? 0xffffffffu : (1u << (8 * C)) - 1u;
+}
+
 template <int C>
 __device__ __forceinline__ int bvol(uint32_t w) {
     int v = 1;
@@ -717,9 +727,6 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         }
         const PBox nx = box_of(lw, uw);
         const bool allow_t = (lw >> 31) != 0;
-        // One-state emission box: Edman and emission run as one loop over
-        // the Edman slices (most timesteps of most pairs).
-        const bool single = t > 0 && pk && !m.interacting && bvol<C>(nx.w) == 1;
         int kmax = 0;
         float part = 0.0f;
         float em0 = 0.0f;
@@ -740,7 +747,19 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             // Detach (detach-transition.cc:36-68) was folded into the last
             // rescale: pd already holds it, fac_prev carries (1 - p).
             // Bleach per channel: channel c moves from the previous box to
-            // [L_t, min(U_t + 1, U_{t-1})).
+            // [L_t, min(U_t + 1, U_{t-1})).  L_t <= L_{t-1} (a suffix
+            // maximum), so a channel one wide in the previous box stays one
+            // wide exactly when L_t = L_{t-1}; when that holds for every
+            // channel (most timesteps) the step is one coefficient per
+            // channel, prob(L -> L), and the box does not change.
+            if ((bx.w & chan_mask<C>()) == (0x01010101u & chan_mask<C>()) &&
+                ((bx.lo ^ nx.lo) & chan_mask<C>()) == 0) {
+#pragma unroll
+                for (int c = 0; c < C; c++) {
+                    const int l = bget(nx.lo, c);
+                    bscale *= M.bleach[c][l * (l + 3) / 2];
+                }
+            } else
 #pragma unroll 1
             for (int c = 0; c < C; c++) {
                 const int ln = bget(nx.lo, c);
@@ -760,26 +779,24 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             // Edman (edman-transition.cc:62-162) as a gather from slices e-1
             // (success) and e (failure) of the bleached box into the
             // emission box; both boxes share the lower corner L_t.
-            if (!single) {
-                fused = pk && !m.interacting && bvol<C>(bx.w) <= 255;
+            fused = pk && !m.interacting && bvol<C>(bx.w) <= 255;
 #pragma unroll
-                for (int c = 0; c < C; c++) fused = fused && bget(nx.w, c) <= 4;
-                if (fused) {
-                    part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, dye_pk, tot_pk, M.edman, m.pf, tab, a.W,
-                                             allow_t, fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
-                    if (kmax == WP_EXPO_ZERO) {
-                        *out_mant = 0.0f;
-                        *out_expo = 0;
-                        return 0;
-                    }
-                } else {
-                    edman_gather<C, HB>(cur, nxt, stride, t, bx, nx, pk, dye_pk, tot_pk, pep, M.edman, m.pf);
+            for (int c = 0; c < C; c++) fused = fused && bget(nx.w, c) <= 4;
+            if (fused) {
+                part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, dye_pk, tot_pk, M.edman, m.pf, tab, a.W,
+                                         allow_t, fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
+                if (kmax == WP_EXPO_ZERO) {
+                    *out_mant = 0.0f;
+                    *out_expo = 0;
+                    return 0;
                 }
-                V* tmp = cur;
-                cur = nxt;
-                nxt = tmp;
-                bx = nx;
+            } else {
+                edman_gather<C, HB>(cur, nxt, stride, t, bx, nx, pk, dye_pk, tot_pk, pep, M.edman, m.pf);
             }
+            V* tmp = cur;
+            cur = nxt;
+            nxt = tmp;
+            bx = nx;
         }
         // ---- Emission t (peptide-emission.cc:212-243).  Factors normalised
         // by the largest exponent over the pair's box (a power of two, carried
@@ -789,86 +806,6 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         for (int c = 0; c < C; c++) narrow = narrow && bget(nx.w, c) <= 4;
         if (fused) {
             // edman_emit applied the emission
-        } else if (single) {
-            // The box's one state has factor prod_c mant_c * 2^(sum_c expo_c);
-            // the multiplier also carries the pending rescale and bscale.
-            float wv = fac_prev * bscale * exp2i(min(-k_prev, 127));
-            float g1 = 1.0f;
-            bool dead = false;
-#pragma unroll
-            for (int c = 0; c < C; c++) {
-                const EmitEntry en = tab[(t * C + c) * a.W + bget(nx.lo, c)];
-                dead = dead || en.mant == 0.0f;
-                wv *= en.mant;
-                g1 *= en.mant;
-                kmax += en.expo;
-            }
-            if (dead) {
-                *out_mant = 0.0f;
-                *out_expo = 0;
-                return 0;
-            }
-            if (allow_t) em0 = g1;
-            // Edman gather into the one state (the bleached box has width 1
-            // or 2 per channel, lower corner L_t), times the emission factor.
-            const float pf = m.pf;
-            uint32_t stpk = 0;  // the bleached box's strides, one byte per channel (<= 8)
-            int vb = 1;
-#pragma unroll
-            for (int c = C - 1; c >= 0; c--) {
-                stpk = bset(stpk, c, vb);
-                vb *= bget(bx.w, c);
-            }
-            uint64_t dp = dye_pk, tp = tot_pk;
-            V xprev = vzero(V());
-            for (int e = 0; e <= t; e++) {
-                const V f = e < t ? cur[e * vb * stride] : vzero(V());
-                V v;
-                if constexpr (HB) {
-                    v = make_float2(pf * f.x, f.y);  // broken-N copied unchanged
-                } else {
-                    v = pf * f;
-                }
-                if (e >= 1) {
-                    const int d4 = (int)(dp & 15);  // dye channel + 1 (0: no dye)
-                    const int tot_i = (int)(tp & 15);
-                    dp >>= 4;
-                    tp >>= 4;
-                    float xin;
-                    if constexpr (HB) {
-                        xin = xprev.x;
-                    } else {
-                        xin = xprev;
-                    }
-                    const int sh = 8 * max(d4 - 1, 0);
-                    const int nc = (int)((bx.lo >> sh) & 0xffu);
-                    const float2 cf = M.edman[(d4 ? tot_i : 0) * 16 + nc];
-                    float add = cf.x * xin;
-                    if (d4 && ((bx.w >> sh) & 0xffu) > 1) {
-                        const int ir = (e - 1) * vb + (int)((stpk >> sh) & 0xffu);
-                        float xr;
-                        if constexpr (HB) {
-                            xr = cur[ir * stride].x;
-                        } else {
-                            xr = cur[ir * stride];
-                        }
-                        add = fmaf(cf.y, xr, add);
-                    }
-                    if constexpr (HB) {
-                        v.x += add;
-                    } else {
-                        v += add;
-                    }
-                }
-                xprev = f;
-                const V s = vmul(wv, v);
-                nxt[e * stride] = s;
-                part += vtotal(s);
-            }
-            V* tmp = cur;
-            cur = nxt;
-            nxt = tmp;
-            bx = nx;
         } else if (narrow) {
             part = emission_narrow<C, V>(cur, stride, t, nx, tab, a.W, allow_t,
                                          fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
