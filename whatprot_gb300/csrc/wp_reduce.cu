@@ -41,7 +41,27 @@ __device__ __forceinline__ bool cand_better(const Cand& a, const Cand& b) {
 }
 
 
-// One warp per read (blockDim.x == 128: four reads per CTA).
+// Exact FP32 sum of two floats as (s, err): s + err == a + b (Knuth's
+// TwoSum, six additions, no branch).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& err) {
+    s = a + b;
+    const float bp = s - a;
+    const float ap = s - bp;
+    err = (a - ap) + (b - bp);
+}
+
+// One warp per read (blockDim.x == 128: four reads per CTA), one pass over
+// the read's slots.  Each lane keeps its best candidate and the sum of its
+// slots' P * count relative to 2^El, El the largest exponent it has met (the
+// sum is rescaled by an exact power of two when El grows).  The sum is a
+// float pair (hi, lo) fed by exact products (mant * count and its FMA
+// remainder) through TwoSum, about 48 significant bits, so the per-slot work
+// stays on the FP32 pipes: this GPU's FP64 rate is a small fraction of its
+// FP32 rate and an FP64 multiply-add per slot made this kernel FP64-bound.
+// Terms below 2^-100 of the lane's reference are dropped (below the FP64
+// resolution of a total that holds at least one term of 2^El / 2).  Counts
+// of 2^24 or more (not exact in FP32) go to an FP64 side sum.  The lanes'
+// sums meet in FP64 relative to E, the best's exponent.
 __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
                                  double* __restrict__ out_score, double* __restrict__ out_total,
                                  double* __restrict__ out_log, const int* __restrict__ pep_ids) {
@@ -51,9 +71,60 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
     const int g0 = slot_begin(a, r);
     const int g1 = a.slot_off ? a.slot_off[r + 1] : g0 + a.P;
     Cand best = {0.0f, 0, INT_MAX, -1};
-    for (int g = g0 + lane; g < g1; g += 32) {
-        Cand c = {a.res_mant[g], a.res_expo[g], g - g0, g};
-        if (cand_better(c, best)) best = c;
+    int El = INT_MIN;  // the lane's reference exponent (none yet)
+    float hi = 0.0f, lo = 0.0f;
+    double big = 0.0;  // terms with counts >= 2^24, relative to 2^El
+    // four slots per lane in flight: the loads first, then the slots in the
+    // lane's order (g, g + 32, g + 64, ...)
+    for (int gb = g0 + lane; gb < g1; gb += 128) {
+        float mv[4];
+        int ev[4], cv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int g = gb + 32 * u;
+            mv[u] = 0.0f;
+            ev[u] = 0;
+            cv[u] = 0;
+            if (g < g1) {
+                mv[u] = a.res_mant[g];
+                ev[u] = a.res_expo[g];
+                cv[u] = a.counts[slot_pep(a, r, g)];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int g = gb + 32 * u;
+            if (g >= g1) break;
+            const float mm = mv[u];
+            const int ex = ev[u];
+            Cand c = {mm, ex, g - g0, g};
+            if (cand_better(c, best)) best = c;
+            if (mm > 0.0f) {
+                if (ex > El) {
+                    const float f = El == INT_MIN || El - ex < -100 ? 0.0f : exp2i(El - ex);
+                    hi *= f;
+                    lo *= f;
+                    big *= (double)f;
+                    El = ex;
+                }
+                const int d = ex - El;
+                if (d >= -100) {
+                    const int cnt = cv[u];
+                    const float s2 = exp2i(d);
+                    if (cnt < (1 << 24)) {
+                        const float cf = (float)cnt;
+                        const float p = mm * cf;
+                        const float pe = fmaf(mm, cf, -p);  // exact: p + pe == mm * cnt
+                        float sum, err;
+                        two_sum(hi, p * s2, sum, err);
+                        hi = sum;
+                        lo += err + pe * s2;
+                    } else {
+                        big += (double)cnt * (double)(mm * s2);
+                    }
+                }
+            }
+        }
     }
     for (int o = 16; o > 0; o >>= 1) {
         Cand c;
@@ -63,11 +134,12 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
         c.idx = __shfl_xor_sync(0xffffffffu, best.idx, o);
         if (cand_better(c, best)) best = c;
     }
+    // E: the best's exponent, the largest exponent of any nonzero slot
     const int E = best.mant > 0.0f ? best.expo : 0;
     double tot = 0.0;
-    for (int g = g0 + lane; g < g1; g += 32) {
-        float mm = a.res_mant[g];
-        if (mm > 0.0f) tot += (double)a.counts[slot_pep(a, r, g)] * ldexp((double)mm, a.res_expo[g] - E);
+    if (El != INT_MIN && El - E >= -1000) {
+        const double sc = __longlong_as_double((long long)(1023 + El - E) << 52);  // 2^(El - E)
+        tot = (((double)hi + (double)lo) + big) * sc;
     }
     for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
     if (lane != 0) return;
