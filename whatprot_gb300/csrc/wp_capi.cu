@@ -34,6 +34,7 @@
 __global__ void wp_prep_reads_kernel(const DevModel*, const double*, int, unsigned, double,
                                      uint8_t*, uint8_t*, EmitEntry*, int);
 __global__ void wp_read_summary_kernel(BatchArgs);
+__global__ void wp_window_factors_kernel(BatchArgs);
 __global__ void wp_compact_kernel(BatchArgs);
 __global__ void wp_reduce_kernel(BatchArgs, int32_t*, double*, double*, double*, const int*);
 __global__ void wp_logp_kernel(const float*, const int*, long, double*);
@@ -265,7 +266,8 @@ struct wp_ctx {
     DevBuf d_kb_reg, d_kb_prev, d_kb_stage, d_kb_next, d_kb_work, d_kb_tfd, d_kb_tfpos, d_kb_tfflag;
 
     // Per-batch scratch.
-    DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_Lpk, d_Upk, d_allow, d_flags, d_table, d_res_mant, d_res_expo,
+    DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_Lpk, d_Upk, d_allow, d_flags, d_table, d_gtab, d_gdelta, d_gK,
+            d_res_mant, d_res_expo,
             d_work, d_ovf1, d_ovf2, d_ovf3, d_ovf4, d_counters, d_cand, d_slot_off, d_out_id, d_out_score,
             d_out_total, d_out_log, d_logp, d_flops, d_err;
 };
@@ -480,6 +482,13 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
     WP_CUDA(ctx->d_Upk.ensure(sizeof(uint32_t) * (size_t)R * T), "alloc");
     WP_CUDA(ctx->d_flags.ensure((size_t)R), "alloc");
     WP_CUDA(ctx->d_table.ensure(sizeof(EmitEntry) * (size_t)R * entries), "alloc emission table");
+    // window-normalised factors for the engine (non-interacting models)
+    const bool window_factors = !ctx->hm.interacting;
+    if (window_factors) {
+        WP_CUDA(ctx->d_gtab.ensure(sizeof(float) * (size_t)R * entries), "alloc window factors");
+        WP_CUDA(ctx->d_gdelta.ensure((size_t)R * entries), "alloc window factors");
+        WP_CUDA(ctx->d_gK.ensure(sizeof(int) * (size_t)R * T), "alloc window factors");
+    }
     WP_CUDA(ctx->d_err.ensure(sizeof(int)), "alloc");
     WP_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(int), ctx->stream), "clear err");
 
@@ -501,6 +510,11 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
     a.Upk = ctx->d_Upk.as<uint32_t>();
     a.flags = ctx->d_flags.as<uint8_t>();
     a.tab = ctx->d_table.as<EmitEntry>();
+    if (window_factors) {
+        a.gtab = ctx->d_gtab.as<float>();
+        a.gdelta = ctx->d_gdelta.as<uint8_t>();
+        a.gK = ctx->d_gK.as<int>();
+    }
     a.err = ctx->d_err.as<int>();
 
     {
@@ -514,6 +528,11 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         wp_read_summary_kernel<<<(R + 127) / 128, 128, 0, ctx->stream>>>(a);
         ctx->launches++;
         WP_CUDA(cudaGetLastError(), "summary launch");
+        if (window_factors) {
+            wp_window_factors_kernel<<<(int)((n + 127) / 128), 128, 0, ctx->stream>>>(a);
+            ctx->launches++;
+            WP_CUDA(cudaGetLastError(), "window factors launch");
+        }
     }
     if (mode == MODE_FLOPS) {
         long np = (long)R * ctx->P;

@@ -156,6 +156,7 @@ struct EmitEntry {
 };
 
 #define WP_EXPO_ZERO (-100000)
+#define WP_GK_NONE (-2147483647 - 1)  // gK: no window factors for this (read, t)
 
 __host__ __device__ inline int wp_ipow(int b, int e) {
     int r = 1;
@@ -203,6 +204,18 @@ struct BatchArgs {
     uint32_t* Upk;             // per (r, t): U byte per channel
     uint8_t* flags;            // per r: bit 0 = the read prunes every pair
     const EmitEntry* tab;      // per read: emission factors
+    // Non-interacting models (all null otherwise, or where unused): per
+    // (r, t, c, n) the emission factor normalised over the read's pruning
+    // window [cmin, cmax) of (t, c), in FP32 (gtab); per (r, t) the sum over
+    // channels of the windows' normalising exponents (gK), or WP_GK_NONE
+    // when some factor lies more than 2^100 below its window's largest; per
+    // (r, t, c) and box [L_t, u), u in (L_t, U_t], the window's exponent
+    // minus the box's at byte u - 1 (gdelta).  Written by
+    // wp_window_factors_kernel; the engine scales them instead of
+    // normalising each pair's box itself.
+    float* gtab;
+    uint8_t* gdelta;
+    int* gK;
     const int* cand;           // per slot: peptide index (null: all peptides)
     const int* perm;           // all-peptides mode: peptides in shape order (or null)
     const int* shape_rank;     // candidate mode: each peptide's position in that order (or null)

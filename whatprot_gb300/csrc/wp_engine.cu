@@ -396,28 +396,48 @@ __device__ __noinline__ void edman_gather(const typename StateOf<HB>::V* __restr
     }
 }
 
-// Emission multiply for boxes at most 4 wide per channel without
-// interactions (peptide-emission.cc:212-243): per channel the box's entries
-// normalised by their largest exponent, in registers; the factor of state n
-// is prod_c g[c][n_c - L_t] * 2^kmax, times sf (the pending rescale and
-// folded coefficients).  Returns the sum of the multiplied states;
-// *kmax_out receives the normalising exponent (WP_EXPO_ZERO: every factor
-// of some channel is zero), *em0_out the all-zero state's factor when
-// allow_t.  Out of line, as edman_gather.
-template <int C, class V>
-__device__ __noinline__ float emission_narrow(V* cur, int stride, int t, PBox nx, const EmitEntry* __restrict__ tab,
-                                              int W, bool allow_t, float sf, int* kmax_out, float* em0_out) {
+// A read's emission factors as the engine reads them: the (mant, expo)
+// table, and where present the window-normalised FP32 factors with their
+// per-box exponent corrections (wp_window_factors_kernel).
+struct ReadEmit {
+    const EmitEntry* tab;  // [(t C + c) W + n]
+    const float* gt;       // same layout, null when absent
+    const uint8_t* gd;     // [(t C + c) W + u - 1]
+    int W;
+};
+
+// Emission factors of the box nx at timestep t (at most 4 wide per channel,
+// no interactions), per channel normalised by the box's largest exponent:
+// g[c][k] for count L_c + k (0 beyond the box), and *kmax_out the sum of
+// the normalising exponents.  gk is the (read, t)'s sum of window
+// exponents: the window factors times 2^gdelta are these numbers exactly;
+// with WP_GK_NONE they are normalised here from the table.  Returns false
+// when every factor of some channel is zero (only detected on the table
+// path; on the other the zero factors give the pair P = 0 at this step's
+// rescale).
+template <int C>
+__device__ __forceinline__ bool narrow_factors(const ReadEmit& re, int gk, int t, PBox nx, float (&g)[C][4],
+                                               int* kmax_out) {
+    if (gk != WP_GK_NONE) {
+        int kmax = gk;
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+            const int wc = bget(nx.w, c);
+            const int base = (t * C + c) * re.W + bget(nx.lo, c);
+            const int dl = re.gd[base + max(wc, 1) - 1];
+            const float sc = exp2i(dl);
+            const float* row = re.gt + base;
+#pragma unroll
+            for (int k = 0; k < 4; k++) g[c][k] = k < wc ? row[k] * sc : 0.0f;
+            kmax -= dl;
+        }
+        *kmax_out = kmax;
+        return true;
+    }
     int kmax = 0;
-    float part = 0.0f;
-    float em0 = 0.0f;
-    // Per channel: the box's entries normalised by their largest
-    // exponent, in registers; the factor of state n is
-    // prod_c g[c][n_c - L_t] * 2^kmax.
-    float g[C][4];
-    bool dead = false;
 #pragma unroll
     for (int c = 0; c < C; c++) {
-        const EmitEntry* row = tab + (t * C + c) * W + bget(nx.lo, c);
+        const EmitEntry* row = re.tab + (t * C + c) * re.W + bget(nx.lo, c);
         const int wc = bget(nx.w, c);
         EmitEntry en[4];
         int km = WP_EXPO_ZERO;
@@ -428,13 +448,35 @@ __device__ __noinline__ float emission_narrow(V* cur, int stride, int t, PBox nx
             if (k < wc) en[k] = row[k];
             if (en[k].mant != 0.0f) km = max(km, en[k].expo);
         }
+        if (km == WP_EXPO_ZERO) return false;
 #pragma unroll
         for (int k = 0; k < 4; k++)
             g[c][k] = en[k].mant != 0.0f ? en[k].mant * exp2i(max(en[k].expo - km, -200)) : 0.0f;
-        if (km == WP_EXPO_ZERO) dead = true;
         kmax += km;
     }
-    if (dead) {
+    *kmax_out = kmax;
+    return true;
+}
+
+// Emission multiply for boxes at most 4 wide per channel without
+// interactions (peptide-emission.cc:212-243): per channel the box's entries
+// normalised by their largest exponent, in registers; the factor of state n
+// is prod_c g[c][n_c - L_t] * 2^kmax, times sf (the pending rescale and
+// folded coefficients).  Returns the sum of the multiplied states;
+// *kmax_out receives the normalising exponent (WP_EXPO_ZERO: every factor
+// of some channel is zero), *em0_out the all-zero state's factor when
+// allow_t.  Out of line, as edman_gather.
+template <int C, class V>
+__device__ __noinline__ float emission_narrow(V* cur, int stride, int t, PBox nx, ReadEmit re, int gk,
+                                              bool allow_t, float sf, int* kmax_out, float* em0_out) {
+    int kmax = 0;
+    float part = 0.0f;
+    float em0 = 0.0f;
+    // Per channel: the box's entries normalised by their largest
+    // exponent, in registers; the factor of state n is
+    // prod_c g[c][n_c - L_t] * 2^kmax.
+    float g[C][4];
+    if (!narrow_factors<C>(re, gk, t, nx, g, &kmax)) {
         *kmax_out = WP_EXPO_ZERO;
         return 0.0f;
     }
@@ -488,34 +530,16 @@ template <int C, bool HB>
 __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __restrict__ cur,
                                          typename StateOf<HB>::V* __restrict__ nxt, int stride, int t, PBox bx,
                                          PBox nx, uint64_t dye_pk, uint64_t tot_pk, const float2* __restrict__ edman,
-                                         float pf, const EmitEntry* __restrict__ tab, int W, bool allow_t, float sf,
+                                         float pf, const ReadEmit& re, int gk, bool allow_t, float sf,
                                          int* kmax_out, float* em0_out) {
     using V = typename StateOf<HB>::V;
     // per channel: the box's emission entries normalised by their largest
     // exponent (as emission_narrow)
     float g[C][4];
     int kmax = 0;
-#pragma unroll
-    for (int c = 0; c < C; c++) {
-        const EmitEntry* row = tab + (t * C + c) * W + bget(nx.lo, c);
-        const int wc = bget(nx.w, c);
-        EmitEntry en[4];
-        int km = WP_EXPO_ZERO;
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            en[k].mant = 0.0f;
-            en[k].expo = WP_EXPO_ZERO;
-            if (k < wc) en[k] = row[k];
-            if (en[k].mant != 0.0f) km = max(km, en[k].expo);
-        }
-        if (km == WP_EXPO_ZERO) {
-            *kmax_out = WP_EXPO_ZERO;
-            return 0.0f;
-        }
-#pragma unroll
-        for (int k = 0; k < 4; k++)
-            g[c][k] = en[k].mant != 0.0f ? en[k].mant * exp2i(max(en[k].expo - km, -200)) : 0.0f;
-        kmax += km;
+    if (!narrow_factors<C>(re, gk, t, nx, g, &kmax)) {
+        *kmax_out = WP_EXPO_ZERO;
+        return 0.0f;
     }
     *kmax_out = kmax;
     if (allow_t) {
@@ -614,6 +638,12 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
     const DevModel& m = *a.model;
     const int T = m.T;
     const EmitEntry* tab = a.tab + (long)r * a.entries;
+    ReadEmit re;
+    re.tab = tab;
+    re.W = a.W;
+    re.gt = a.gtab ? a.gtab + (long)r * a.entries : nullptr;
+    re.gd = a.gdelta ? a.gdelta + (long)r * a.entries : nullptr;
+    const int* gKr = a.gtab ? a.gK + (long)r * T : nullptr;
     const uint32_t* Lpk = a.Lpk + (long)r * T;
     const uint32_t* Upk = a.Upk + (long)r * T;
     uint32_t D1 = 0;  // D_c + 1 per channel, packed
@@ -716,14 +746,17 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         return false;
     };
     uint32_t lw_next = Lpk[0], uw_next = Upk[0];
+    int gk_next = gKr ? gKr[0] : WP_GK_NONE;
     int t = 0;
     for (;;) {
         // this timestep's box words; the next timestep's are fetched now so
         // their latency hides behind this timestep's work
         const uint32_t lw = lw_next, uw = uw_next;
+        const int gk = gk_next;
         if (t + 1 < T) {
             lw_next = Lpk[t + 1];
             uw_next = Upk[t + 1];
+            if (gKr) gk_next = gKr[t + 1];
         }
         const PBox nx = box_of(lw, uw);
         const bool allow_t = (lw >> 31) != 0;
@@ -783,7 +816,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
 #pragma unroll
             for (int c = 0; c < C; c++) fused = fused && bget(nx.w, c) <= 4;
             if (fused) {
-                part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, dye_pk, tot_pk, M.edman, m.pf, tab, a.W,
+                part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, dye_pk, tot_pk, M.edman, m.pf, re, gk,
                                          allow_t, fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
                 if (kmax == WP_EXPO_ZERO) {
                     *out_mant = 0.0f;
@@ -807,7 +840,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         if (fused) {
             // edman_emit applied the emission
         } else if (narrow) {
-            part = emission_narrow<C, V>(cur, stride, t, nx, tab, a.W, allow_t,
+            part = emission_narrow<C, V>(cur, stride, t, nx, re, gk, allow_t,
                                          fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
             if (kmax == WP_EXPO_ZERO) {
                 *out_mant = 0.0f;

@@ -11,6 +11,9 @@
 //                           cmin_{t'} and min_{t'<=t} cmax_{t'}, the
 //                           allow-detached flag of each emission and whether
 //                           the read prunes every pair.
+//   wp_window_factors_kernel  one thread per (read, timestep): the emission
+//                           factors normalised over the pruning window, for
+//                           the engine (non-interacting models).
 //   wp_compact_kernel       one CTA per read: pairs whose pruned range is
 //                           empty get probability 0 (PeptideHMM::probability,
 //                           hmm/hmm/peptide-hmm.cc:94-100); the others are
@@ -265,6 +268,67 @@ __global__ void wp_read_summary_kernel(BatchArgs a) {
         a.Upk[(long)r * T + t] = upk;
     }
     a.flags[r] = (uint8_t)empty;
+}
+
+// One thread per (read, t), non-interacting models, after the summary: the
+// window-normalised emission factors the engine reads (BatchArgs::gtab, gK,
+// gdelta).  For a pair's box [L_t, u) of channel c the engine multiplies the
+// window factors by 2^gdelta, which gives exactly mant * 2^(expo - k_box), k_box
+// the box's largest exponent (both factors are powers of two and nothing
+// leaves the normal range while every factor is within 2^100 of its
+// window's largest), and adds sum_c (k_window - gdelta) as the box's
+// normalising exponent: the same numbers the engine's own normalisation of
+// the box gives.  Where a factor lies further below, gK = WP_GK_NONE and the
+// engine normalises that (read, t) itself.
+__global__ void wp_window_factors_kernel(BatchArgs a) {
+    const DevModel& m = *a.model;
+    const int T = m.T, C = m.C, W = a.W;
+    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= (long)a.R * T) return;
+    const int r = (int)(gid / T), t = (int)(gid % T);
+    const long rt = (long)r * T + t;
+    const EmitEntry* tab = a.tab + (long)r * a.entries + (long)t * C * W;  // [(t C + c) W + n]
+    float* gt = a.gtab + rt * C * W;
+    uint8_t* gd = a.gdelta + rt * C * W;
+    const uint8_t* lo = a.lo + rt * C;
+    const uint8_t* hi = a.hi + rt * C;
+    const uint8_t* Ls = a.Lsuf + rt * C;
+    const uint8_t* Up = a.Upre + rt * C;
+    int K = 0;
+    bool ok = true;
+    for (int c = 0; c < C; c++) {
+        const EmitEntry* row = tab + c * W;
+        int km = WP_EXPO_ZERO;  // the window's largest exponent
+        for (int n = lo[c]; n < hi[c] && n < W; n++)
+            if (row[n].mant != 0.0f) km = max(km, row[n].expo);
+        for (int n = 0; n < W; n++) {
+            const EmitEntry en = row[n];  // zero outside the window
+            float v = 0.0f;
+            if (en.mant != 0.0f) {
+                const int d = en.expo - km;
+                if (d < -100)
+                    ok = false;
+                else
+                    v = en.mant * exp2i(d);
+            }
+            gt[c * W + n] = v;
+        }
+        if (km != WP_EXPO_ZERO) K += km;
+        // boxes [L_t, u): the window's exponent minus the box's largest (0
+        // while the box has no nonzero factor; its pairs get P = 0)
+        const int L = Ls[c], U = Up[c];
+        int run = WP_EXPO_ZERO;
+        for (int u = 1; u <= W; u++) {
+            int dl = 0;
+            if (u > L && u <= U) {
+                const EmitEntry en = row[u - 1];
+                if (en.mant != 0.0f) run = max(run, en.expo);
+                if (run != WP_EXPO_ZERO) dl = km - run;
+            }
+            gd[c * W + u - 1] = (uint8_t)(dl <= 100 ? dl : 0);
+        }
+    }
+    a.gK[rt] = ok ? K : WP_GK_NONE;
 }
 
 // One CTA per read (at most 1,024 threads, a multiple of 32).  CTA-aggregated
