@@ -267,6 +267,7 @@ struct wp_ctx {
 
     // Per-batch scratch.
     DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_Lpk, d_Upk, d_allow, d_flags, d_table, d_gtab, d_gdelta, d_gK,
+            d_gone,
             d_res_mant, d_res_expo,
             d_work, d_ovf1, d_ovf2, d_ovf3, d_ovf4, d_counters, d_cand, d_slot_off, d_out_id, d_out_score,
             d_out_total, d_out_log, d_logp, d_flops, d_err;
@@ -488,6 +489,7 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         WP_CUDA(ctx->d_gtab.ensure(sizeof(float) * (size_t)R * entries), "alloc window factors");
         WP_CUDA(ctx->d_gdelta.ensure((size_t)R * entries), "alloc window factors");
         WP_CUDA(ctx->d_gK.ensure(sizeof(int) * (size_t)R * T), "alloc window factors");
+        WP_CUDA(ctx->d_gone.ensure(sizeof(float4) * (size_t)R * T), "alloc window factors");
     }
     WP_CUDA(ctx->d_err.ensure(sizeof(int)), "alloc");
     WP_CUDA(cudaMemsetAsync(ctx->d_err.p, 0, sizeof(int), ctx->stream), "clear err");
@@ -514,6 +516,7 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         a.gtab = ctx->d_gtab.as<float>();
         a.gdelta = ctx->d_gdelta.as<uint8_t>();
         a.gK = ctx->d_gK.as<int>();
+        a.gone = ctx->d_gone.as<float4>();
     }
     a.err = ctx->d_err.as<int>();
 

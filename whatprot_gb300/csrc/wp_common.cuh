@@ -216,6 +216,11 @@ struct BatchArgs {
     float* gtab;
     uint8_t* gdelta;
     int* gK;
+    // per (r, t), with gtab, C <= 3: where the read's box [L_t, U_t) is one
+    // state in every channel (so is every non-empty pair's), that state's
+    // factor mantissa per channel (x, y, z) and the sum of its exponents in
+    // w (int bits); w = WP_GK_NONE otherwise
+    float4* gone;
     const int* cand;           // per slot: peptide index (null: all peptides)
     const int* perm;           // all-peptides mode: peptides in shape order (or null)
     const int* shape_rank;     // candidate mode: each peptide's position in that order (or null)

@@ -411,13 +411,28 @@ struct ReadEmit {
 // g[c][k] for count L_c + k (0 beyond the box), and *kmax_out the sum of
 // the normalising exponents.  gk is the (read, t)'s sum of window
 // exponents: the window factors times 2^gdelta are these numbers exactly;
-// with WP_GK_NONE they are normalised here from the table.  Returns false
+// with WP_GK_NONE they are normalised here from the table.  one: the
+// (read, t)'s one-state factors (BatchArgs::gone).  Returns false
 // when every factor of some channel is zero (only detected on the table
 // path; on the other the zero factors give the pair P = 0 at this step's
 // rescale).
 template <int C>
-__device__ __forceinline__ bool narrow_factors(const ReadEmit& re, int gk, int t, PBox nx, float (&g)[C][4],
-                                               int* kmax_out) {
+__device__ __forceinline__ bool narrow_factors(const ReadEmit& re, int gk, float4 one, int t, PBox nx,
+                                               float (&g)[C][4], int* kmax_out) {
+    if constexpr (C <= 3) {
+        // the read's box is one state in every channel: that state's factor
+        // mantissas and exponent sum, as the two paths below would give
+        if (__float_as_int(one.w) != WP_GK_NONE) {
+            const float mv[3] = {one.x, one.y, one.z};
+#pragma unroll
+            for (int c = 0; c < C; c++) {
+                g[c][0] = mv[c];
+                g[c][1] = g[c][2] = g[c][3] = 0.0f;
+            }
+            *kmax_out = __float_as_int(one.w);
+            return true;
+        }
+    }
     if (gk != WP_GK_NONE) {
         int kmax = gk;
 #pragma unroll
@@ -467,7 +482,7 @@ __device__ __forceinline__ bool narrow_factors(const ReadEmit& re, int gk, int t
 // of some channel is zero), *em0_out the all-zero state's factor when
 // allow_t.  Out of line, as edman_gather.
 template <int C, class V>
-__device__ __noinline__ float emission_narrow(V* cur, int stride, int t, PBox nx, ReadEmit re, int gk,
+__device__ __noinline__ float emission_narrow(V* cur, int stride, int t, PBox nx, ReadEmit re, int gk, float4 one,
                                               bool allow_t, float sf, int* kmax_out, float* em0_out) {
     int kmax = 0;
     float part = 0.0f;
@@ -476,7 +491,7 @@ __device__ __noinline__ float emission_narrow(V* cur, int stride, int t, PBox nx
     // exponent, in registers; the factor of state n is
     // prod_c g[c][n_c - L_t] * 2^kmax.
     float g[C][4];
-    if (!narrow_factors<C>(re, gk, t, nx, g, &kmax)) {
+    if (!narrow_factors<C>(re, gk, one, t, nx, g, &kmax)) {
         *kmax_out = WP_EXPO_ZERO;
         return 0.0f;
     }
@@ -530,14 +545,14 @@ template <int C, bool HB>
 __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __restrict__ cur,
                                          typename StateOf<HB>::V* __restrict__ nxt, int stride, int t, PBox bx,
                                          PBox nx, uint64_t dye_pk, uint64_t tot_pk, const float2* __restrict__ edman,
-                                         float pf, const ReadEmit& re, int gk, bool allow_t, float sf,
+                                         float pf, const ReadEmit& re, int gk, float4 one, bool allow_t, float sf,
                                          int* kmax_out, float* em0_out) {
     using V = typename StateOf<HB>::V;
     // per channel: the box's emission entries normalised by their largest
     // exponent (as emission_narrow)
     float g[C][4];
     int kmax = 0;
-    if (!narrow_factors<C>(re, gk, t, nx, g, &kmax)) {
+    if (!narrow_factors<C>(re, gk, one, t, nx, g, &kmax)) {
         *kmax_out = WP_EXPO_ZERO;
         return 0.0f;
     }
@@ -644,6 +659,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
     re.gt = a.gtab ? a.gtab + (long)r * a.entries : nullptr;
     re.gd = a.gdelta ? a.gdelta + (long)r * a.entries : nullptr;
     const int* gKr = a.gtab ? a.gK + (long)r * T : nullptr;
+    const float4* gOr = a.gone ? a.gone + (long)r * T : nullptr;
     const uint32_t* Lpk = a.Lpk + (long)r * T;
     const uint32_t* Upk = a.Upk + (long)r * T;
     uint32_t D1 = 0;  // D_c + 1 per channel, packed
@@ -747,16 +763,20 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
     };
     uint32_t lw_next = Lpk[0], uw_next = Upk[0];
     int gk_next = gKr ? gKr[0] : WP_GK_NONE;
+    const float4 one_none = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(WP_GK_NONE));
+    float4 one_next = gOr ? gOr[0] : one_none;
     int t = 0;
     for (;;) {
         // this timestep's box words; the next timestep's are fetched now so
         // their latency hides behind this timestep's work
         const uint32_t lw = lw_next, uw = uw_next;
         const int gk = gk_next;
+        const float4 one = one_next;
         if (t + 1 < T) {
             lw_next = Lpk[t + 1];
             uw_next = Upk[t + 1];
             if (gKr) gk_next = gKr[t + 1];
+            if (gOr) one_next = gOr[t + 1];
         }
         const PBox nx = box_of(lw, uw);
         const bool allow_t = (lw >> 31) != 0;
@@ -816,7 +836,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
 #pragma unroll
             for (int c = 0; c < C; c++) fused = fused && bget(nx.w, c) <= 4;
             if (fused) {
-                part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, dye_pk, tot_pk, M.edman, m.pf, re, gk,
+                part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, dye_pk, tot_pk, M.edman, m.pf, re, gk, one,
                                          allow_t, fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
                 if (kmax == WP_EXPO_ZERO) {
                     *out_mant = 0.0f;
@@ -840,7 +860,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         if (fused) {
             // edman_emit applied the emission
         } else if (narrow) {
-            part = emission_narrow<C, V>(cur, stride, t, nx, re, gk, allow_t,
+            part = emission_narrow<C, V>(cur, stride, t, nx, re, gk, one, allow_t,
                                          fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
             if (kmax == WP_EXPO_ZERO) {
                 *out_mant = 0.0f;

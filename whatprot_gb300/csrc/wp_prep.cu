@@ -329,6 +329,23 @@ __global__ void wp_window_factors_kernel(BatchArgs a) {
         }
     }
     a.gK[rt] = ok ? K : WP_GK_NONE;
+    if (a.gone) {
+        // one-state read box in every channel: the state's own factors
+        float mv[3] = {0.0f, 0.0f, 0.0f};
+        int K1 = 0;
+        bool one = C <= 3;
+        for (int c = 0; c < C && one; c++) {
+            const int L = Ls[c];
+            if (Up[c] != L + 1 || L >= W) {
+                one = false;
+                break;
+            }
+            const EmitEntry en = tab[c * W + L];
+            mv[c] = en.mant;
+            if (en.mant != 0.0f) K1 += en.expo;
+        }
+        a.gone[rt] = make_float4(mv[0], mv[1], mv[2], __int_as_float(one ? K1 : WP_GK_NONE));
+    }
 }
 
 // One CTA per read (at most 1,024 threads, a multiple of 32).  CTA-aggregated
