@@ -134,17 +134,28 @@ struct PeptideRec {
     // T <= 17): dye_pk nibble e = dye[e] + 1, tot_pk nibble e = tot[e].
     uint64_t dye_pk;
     uint64_t tot_pk;
+    // The same positions as one Edman code byte each (ecode[0]: positions
+    // 0..7, ecode[1]: 8..15): (tot << 3) | channel for a dye, 4 for none.
+    // The engine's Edman step reads the coefficient row tot and, through a
+    // byte permute with selector 0x4440 | (code & 7), the dye count of the
+    // cut channel (selector 0x4444: the constant zero byte).
+    uint64_t ecode[2];
 };
 
-// Fills dye_pk / tot_pk from dye[] and tot[] (tot <= 15 per channel).
+// Fills dye_pk / tot_pk / ecode from dye[] and tot[] (tot <= 15 per channel).
 __host__ __device__ inline void wp_pack_peptide(PeptideRec& r) {
     uint64_t d = 0, t = 0;
+    uint64_t ec[2] = {0, 0};
     for (int e = 0; e < 16 && e < WP_MAX_TIMESTEPS; e++) {
         d |= (uint64_t)((r.dye[e] + 1) & 15) << (4 * e);
         t |= (uint64_t)(r.tot[e] & 15) << (4 * e);
+        const uint64_t code = r.dye[e] >= 0 ? (uint64_t)(((r.tot[e] & 15) << 3) | (r.dye[e] & 3)) : 4u;
+        ec[e >> 3] |= code << (8 * (e & 7));
     }
     r.dye_pk = d;
     r.tot_pk = t;
+    r.ecode[0] = ec[0];
+    r.ecode[1] = ec[1];
 }
 
 // Emission factor of one table entry: value = mant * 2^expo exactly as the
@@ -253,7 +264,8 @@ struct BatchArgs {
 };
 
 // Largest state box, in elements with the Edman slices counted, that any
-// step of a pair uses: the start box [L_0, D + 1), and per timestep t >= 1
+// step of a pair uses: the emission box of t = 0 (the engine writes the
+// start state after its duds directly there), and per timestep t >= 1
 // the previous emission box, the bleach output / Edman input box
 // [L_t, min(U_t + 1, U_{t-1})), the boxes in between (channels bleached so
 // far at their new width, the others at the old) and the emission box,
@@ -266,7 +278,7 @@ __device__ inline int pair_vmax(int C, int T, const uint32_t* Lw, const uint32_t
         const int l = (int)((Lw[0] >> (8 * c)) & 0x7fu);
         lo_p[c] = l;
         w_p[c] = min((int)((Uw[0] >> (8 * c)) & 0xffu), d1) - l;
-        vmax *= d1 - l;
+        vmax *= w_p[c];
     }
     for (int t = 1; t < T; t++) {
         const uint32_t lw = Lw[t], uw = Uw[t];

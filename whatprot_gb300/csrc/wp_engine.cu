@@ -50,6 +50,7 @@
 #include "wp_common.cuh"
 
 #define WP_ENGINE_THREADS 256
+#define WP_ENGINE_CODES 16  // Edman code bytes per thread (positions 0..15)
 
 template <bool HB>
 struct StateOf;
@@ -118,13 +119,16 @@ __device__ __noinline__ void binomial_step(const V* __restrict__ src, V* __restr
         // input column (its up to 3 states along ch) is loaded once and
         // gives all the column's outputs.
         float cf[3][3];
+        // prob(from0 + k -> to0) sits at rb[k]; prob(from0 + k -> to0 + k2)
+        // at rb[k] + k2 (triangular rows), nonzero only for from >= to.
+        const int rb0 = from0 * (from0 + 1) / 2 + to0;
+        const int rb[3] = {rb0, rb0 + from0 + 1, rb0 + 2 * from0 + 3};
+        const int d = from0 - to0;
 #pragma unroll
         for (int k2 = 0; k2 < 3; k2++)
 #pragma unroll
-            for (int k = 0; k < 3; k++) {
-                const int from = from0 + k, to = to0 + k2;
-                cf[k2][k] = (k < win && k2 < wout && from >= to) ? tab[from * (from + 1) / 2 + to] : 0.0f;
-            }
+            for (int k = 0; k < 3; k++)
+                cf[k2][k] = (k < win && k2 < wout && d + k - k2 >= 0) ? tab[rb[k] + k2] : 0.0f;
         for (int o = 0; o < outer; o++) {
             const V* s = src + o * win * sk;
             V* d = dst + o * wout * sk;
@@ -537,14 +541,19 @@ __device__ __noinline__ float emission_narrow(V* cur, int stride, int t, PBox nx
 // box bx, its dye counts, the channels with a state one dye up) is done once
 // per state instead of once per (state, slice), and the Edman output is
 // multiplied by its emission factor before it is stored.  cur holds the
-// bleached box (t slices), nxt receives the emission box (t + 1 slices).
-// The bleached box's per-slice volume must be at most 255.  Returns the sum
-// of the new states; *kmax_out the normalising exponent (WP_EXPO_ZERO: every
-// factor of some channel is zero), *em0_out the all-zero state's factor.
+// bleached box (t >= 1 slices), nxt receives the emission box (t + 1
+// slices).  codes: the pair's Edman code per position (PeptideRec::ecode),
+// one byte per position at codes[k * stride]; a byte permute of the state's
+// packed dye counts by the code's selector gives the cut channel's count
+// (and whether the state one dye up exists), so a slice costs no shifts of
+// the packed dye sequence.  The bleached box's per-slice volume must be at
+// most 255.  Returns the sum of the new states; *kmax_out the normalising
+// exponent (WP_EXPO_ZERO: every factor of some channel is zero), *em0_out
+// the all-zero state's factor.
 template <int C, bool HB>
 __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __restrict__ cur,
                                          typename StateOf<HB>::V* __restrict__ nxt, int stride, int t, PBox bx,
-                                         PBox nx, uint64_t dye_pk, uint64_t tot_pk, const float2* __restrict__ edman,
+                                         PBox nx, const uint8_t* __restrict__ codes, const float2* __restrict__ edman,
                                          float pf, const ReadEmit& re, int gk, float4 one, bool allow_t, float sf,
                                          int* kmax_out, float* em0_out) {
     using V = typename StateOf<HB>::V;
@@ -573,65 +582,92 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
     }
     const int vn = bvol<C>(nx.w);
     const int sb = vb * stride, sn = vn * stride;
+    const char* edb = reinterpret_cast<const char*>(edman);
     float part = 0.0f;
     int jc[C];
 #pragma unroll
     for (int c = 0; c < C; c++) jc[c] = 0;
     for (int j = 0; j < vn; j++) {
         int ib = 0;
-        uint32_t cnt = nx.lo, up = 0;
+        // byte c: the state's dye count in channel c, bit 7 set when the
+        // state one dye up in c lies in the bleached box
+        uint32_t X = nx.lo;
         float w = sf;
 #pragma unroll
         for (int c = 0; c < C; c++) {
             const int k = jc[c];
             ib += k * bget(stpk, c);
-            cnt += (uint32_t)k << (8 * c);
-            if (k + 1 < bget(bx.w, c)) up |= 1u << c;
+            X += (uint32_t)k << (8 * c);
+            if (k + 1 < bget(bx.w, c)) X |= 0x80u << (8 * c);
             w *= k == 0 ? g[c][0] : k == 1 ? g[c][1] : k == 2 ? g[c][2] : g[c][3];
         }
-        const V* col = cur + ib * stride;
+        const V* cs = cur + ib * stride;  // slice e - 1 of the state's column
         V* out = nxt + j * stride;
-        uint64_t dp = dye_pk, tp = tot_pk;
-        V prev = vzero(V());
-        for (int e = 0; e <= t; e++) {
-            const V f = e < t ? col[e * sb] : vzero(V());
+        // Edman success into slice e from slice e - 1 (value prev): the
+        // state's own count (x) and the state one dye up losing the cut dye (y)
+        auto success = [&](const uint8_t* cp, const V prev) -> float {
+            const uint32_t code = *cp;
+            const uint32_t sel = 0x4440u | (code & 7u);
+            const uint32_t b = __byte_perm(X, 0u, sel);
+            const float2 cf = *reinterpret_cast<const float2*>(edb + ((code & 0x78u) << 4) + ((b & 0x7fu) << 3));
+            float xin;
+            if constexpr (HB) {
+                xin = prev.x;
+            } else {
+                xin = prev;
+            }
+            float add = cf.x * xin;
+            if (b & 0x80u) {
+                const V xr = cs[(int)__byte_perm(stpk, 0u, sel) * stride];
+                if constexpr (HB) {
+                    add = fmaf(cf.y, xr.x, add);
+                } else {
+                    add = fmaf(cf.y, xr, add);
+                }
+            }
+            return add;
+        };
+        // slice 0: failure only
+        V prev = cs[0];
+        {
             V v;
             if constexpr (HB) {
-                v = make_float2(pf * f.x, f.y);  // broken-N copied unchanged
+                v = make_float2(pf * prev.x, prev.y);  // broken-N copied unchanged
             } else {
-                v = pf * f;
+                v = pf * prev;
             }
-            if (e >= 1) {
-                const int d4 = (int)(dp & 15);  // dye channel + 1 (0: no dye)
-                const int tot_i = (int)(tp & 15);
-                dp >>= 4;
-                tp >>= 4;
-                const int sh = 8 * max(d4 - 1, 0);
-                const float2 cf = edman[(d4 ? tot_i : 0) * 16 + (int)((cnt >> sh) & 0xffu)];
-                float xin;
-                if constexpr (HB) {
-                    xin = prev.x;
-                } else {
-                    xin = prev;
-                }
-                float add = cf.x * xin;
-                if (d4 && ((up >> (d4 - 1)) & 1u)) {
-                    const V xr = col[(e - 1) * sb + (int)((stpk >> sh) & 0xffu) * stride];
-                    if constexpr (HB) {
-                        add = fmaf(cf.y, xr.x, add);
-                    } else {
-                        add = fmaf(cf.y, xr, add);
-                    }
-                }
-                if constexpr (HB) {
-                    v.x += add;
-                } else {
-                    v += add;
-                }
+            const V sv = vmul(w, v);
+            out[0] = sv;
+            part += vtotal(sv);
+        }
+        const uint8_t* cp = codes;
+        for (int e = 1; e < t; e++) {
+            const float add = success(cp, prev);
+            cs += sb;
+            cp += stride;
+            const V f = *cs;
+            V v;
+            if constexpr (HB) {
+                v = make_float2(fmaf(pf, f.x, add), f.y);
+            } else {
+                v = fmaf(pf, f, add);
             }
             prev = f;
             const V sv = vmul(w, v);
             out[e * sn] = sv;
+            part += vtotal(sv);
+        }
+        {
+            // slice t: success only (the bleached box has t slices)
+            const float add = success(cp, prev);
+            V v;
+            if constexpr (HB) {
+                v = make_float2(add, 0.0f);
+            } else {
+                v = add;
+            }
+            const V sv = vmul(w, v);
+            out[t * sn] = sv;
             part += vtotal(sv);
         }
 #pragma unroll
@@ -647,7 +683,7 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
 // written), else 0 with P = *mant * 2^*expo (mant == 0: P == 0).
 template <int C, bool HB>
 __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
-                           const PeptideRec& pep, typename StateOf<HB>::V* slab, int stride,
+                           const PeptideRec& pep, typename StateOf<HB>::V* slab, uint8_t* codes, int stride,
                            int half, int vmax, float* out_mant, int* out_expo) {
     using V = typename StateOf<HB>::V;
     const DevModel& m = *a.model;
@@ -684,49 +720,55 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
     // packed 4 bits each (positions < 16) so the Edman loop reads registers.
     const bool pk = T <= 17;
     const uint64_t dye_pk = pep.dye_pk, tot_pk = pep.tot_pk;
+    if (pk) {
+        // the Edman code of each position, one byte per position in the
+        // thread's slice of shared memory (read by edman_emit)
+        const uint64_t ec0 = pep.ecode[0], ec1 = pep.ecode[1];
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            if (k < T - 1) codes[k * stride] = (uint8_t)((k < 8 ? ec0 : ec1) >> (8 * (k & 7)));
+    }
 
     V* cur = slab;
     V* nxt = slab + half * stride;
 
-    // ---- t = 0: start state (0, D) (peptide-state-vector.cc:38-40) in the
-    // box [L_0, D + 1), initial block, duds.
-    PBox bx;
-    bx.lo = Lpk[0] & 0x7f7f7f7fu;
-    bx.w = 0;
-#pragma unroll
-    for (int c = 0; c < C; c++) bx.w = bset(bx.w, c, bget(D1, c) - bget(bx.lo, c));
+    // ---- t = 0: the start state (0, D) (peptide-state-vector.cc:38-40),
+    // the initial block (block-transition.cc:33-62) and the dud steps
+    // (dud-transition.cc:25-37).  From a single state the duds give state n
+    // of the emission box [L_0, min(U_0, D + 1)) the start value times
+    // prob(D_c -> n_c) of each channel in turn: the reference's
+    // channel-by-channel passes multiply the same factors in the same order,
+    // and states outside the box are pruned, so the box is written directly.
+    PBox bx = emission_box(0);
     {
         const int v = bvol<C>(bx.w);
-        for (int i = 0; i < v - 1; i++) cur[i * stride] = vzero(V());
-        V start;
-        if constexpr (HB) {
-            start = make_float2(1.0f - m.p_ib, m.p_ib);  // block-transition.cc:33-62
-        } else {
-            start = 1.0f;
+        int jc[C];
+#pragma unroll
+        for (int c = 0; c < C; c++) jc[c] = 0;
+        for (int j = 0; j < v; j++) {
+            V s;
+            if constexpr (HB) {
+                s = make_float2(1.0f - m.p_ib, m.p_ib);
+            } else {
+                s = 1.0f;
+            }
+#pragma unroll
+            for (int c = 0; c < C; c++) {
+                const int d = pep.D[c], n = bget(bx.lo, c) + jc[c];
+                s = vmul(M.dud[c][d * (d + 1) / 2 + n], s);
+            }
+            cur[j * stride] = s;
+#pragma unroll
+            for (int c = C - 1; c >= 0; c--) {
+                if (++jc[c] < bget(bx.w, c)) break;
+                jc[c] = 0;
+            }
         }
-        cur[(v - 1) * stride] = start;
     }
     // A binomial step along a channel whose input and output boxes are both
     // one wide is one coefficient for the whole state: it is carried in
     // bscale and applied with the next emission multiply instead of a pass.
     float bscale = 1.0f;
-    {
-        const PBox n0 = emission_box(0);
-#pragma unroll 1
-        for (int c = 0; c < C; c++) {
-            const int wout = bget(n0.w, c);
-            if (bget(bx.w, c) == 1 && wout == 1) {
-                const int from = bget(bx.lo, c), to = bget(bx.lo, c);
-                bscale *= M.dud[c][from * (from + 1) / 2 + to];
-            } else {
-                binomial_step<C, V>(cur, nxt, stride, 1, bx, c, bget(bx.lo, c), wout, M.dud[c]);
-                V* tmp = cur;
-                cur = nxt;
-                nxt = tmp;
-            }
-            bx.w = bset(bx.w, c, wout);
-        }
-    }
 
     int expo = 0;           // the true state is the stored state times 2^expo
     float pd = 0.0f;        // detached state, in the rescaled frame
@@ -746,8 +788,16 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             *out_expo = 0;
             return true;
         }
+        // tot = fm * 2^k, fm in [0.5, 1) (frexpf; normal numbers from the bits)
         int k;
-        const float fm = frexpf(tot, &k);
+        float fm;
+        const int bits = __float_as_int(tot);
+        if (bits >= 0x00800000) {
+            k = (bits >> 23) - 126;
+            fm = __int_as_float((bits & 0x007fffff) | 0x3f000000);
+        } else {
+            fm = frexpf(tot, &k);
+        }
         if (t == T - 1) {
             *out_mant = fm;
             *out_expo = expo + k;
@@ -836,7 +886,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
 #pragma unroll
             for (int c = 0; c < C; c++) fused = fused && bget(nx.w, c) <= 4;
             if (fused) {
-                part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, dye_pk, tot_pk, M.edman, m.pf, re, gk, one,
+                part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, codes, M.edman, m.pf, re, gk, one,
                                          allow_t, fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
                 if (kmax == WP_EXPO_ZERO) {
                     *out_mant = 0.0f;
@@ -905,6 +955,8 @@ __global__ void __launch_bounds__(WP_ENGINE_THREADS) wp_engine_kernel(BatchArgs 
     const int nt = blockDim.x;
     V* slab_region = reinterpret_cast<V*>(smem_raw + ((sizeof(SmemModel) + 15) & ~(size_t)15));
     V* slab = slab_region + threadIdx.x;
+    // per-thread Edman code bytes after the slabs (wp_engine_smem_bytes)
+    uint8_t* codes = reinterpret_cast<uint8_t*>(slab_region + 2 * (size_t)L.slab_half * nt) + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const int count = *L.in_count;
     for (;;) {
@@ -918,8 +970,8 @@ __global__ void __launch_bounds__(WP_ENGINE_THREADS) wp_engine_kernel(BatchArgs 
             const int p = slot_pep(a, rg.x, rg.y);
             float mant;
             int ex;
-            int ov = engine_pair<C, HB>(a, M, rg.x, a.peps[p], slab, nt, L.slab_half, a.res_expo[rg.y], &mant,
-                                        &ex);
+            int ov = engine_pair<C, HB>(a, M, rg.x, a.peps[p], slab, codes, nt, L.slab_half, a.res_expo[rg.y],
+                                        &mant, &ex);
             if (ov) {
                 if (L.spill_error) {
                     atomicExch(a.err, 2);
@@ -937,12 +989,12 @@ __global__ void __launch_bounds__(WP_ENGINE_THREADS) wp_engine_kernel(BatchArgs 
     }
 }
 
-// Shared memory of one engine CTA: the model, two slab halves per thread
-// and scr_floats more words per thread.
+// Shared memory of one engine CTA: the model, two slab halves per thread,
+// 16 Edman code bytes per thread and scr_floats more words per thread.
 size_t wp_engine_smem_bytes(int slab_half, int scr_floats, bool has_block, int threads) {
     size_t elem = has_block ? sizeof(float2) : sizeof(float);
     return ((sizeof(SmemModel) + 15) & ~(size_t)15) + (size_t)2 * slab_half * threads * elem +
-           (size_t)scr_floats * threads * sizeof(float);
+           (size_t)WP_ENGINE_CODES * threads + (size_t)scr_floats * threads * sizeof(float);
 }
 
 template <int C, bool HB>
