@@ -566,6 +566,9 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
         return 0.0f;
     }
     *kmax_out = kmax;
+    float w0 = sf;
+#pragma unroll
+    for (int c = 0; c < C; c++) w0 *= g[c][0];
     if (allow_t) {
         float em0 = 1.0f;
 #pragma unroll
@@ -580,6 +583,10 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
         stpk = bset(stpk, c, vb);
         vb *= bget(bx.w, c);
     }
+    // the box's first state: bit 7 of byte c set where the bleached box is
+    // wider than one in channel c (bytes of bx.w are at most 16, and 0 past
+    // the channels, so no byte carries into the next)
+    const uint32_t up0 = (bx.w + 0x7e7e7e7eu) & 0x80808080u;
     const int vn = bvol<C>(nx.w);
     const int sb = vb * stride, sn = vn * stride;
     const char* edb = reinterpret_cast<const char*>(edman);
@@ -591,15 +598,19 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
         int ib = 0;
         // byte c: the state's dye count in channel c, bit 7 set when the
         // state one dye up in c lies in the bleached box
-        uint32_t X = nx.lo;
-        float w = sf;
+        uint32_t X = nx.lo | up0;
+        float w = w0;
+        if (j > 0) {
+            X = nx.lo;
+            w = sf;
 #pragma unroll
-        for (int c = 0; c < C; c++) {
-            const int k = jc[c];
-            ib += k * bget(stpk, c);
-            X += (uint32_t)k << (8 * c);
-            if (k + 1 < bget(bx.w, c)) X |= 0x80u << (8 * c);
-            w *= k == 0 ? g[c][0] : k == 1 ? g[c][1] : k == 2 ? g[c][2] : g[c][3];
+            for (int c = 0; c < C; c++) {
+                const int k = jc[c];
+                ib += k * bget(stpk, c);
+                X += (uint32_t)k << (8 * c);
+                if (k + 1 < bget(bx.w, c)) X |= 0x80u << (8 * c);
+                w *= k == 0 ? g[c][0] : k == 1 ? g[c][1] : k == 2 ? g[c][2] : g[c][3];
+            }
         }
         const V* cs = cur + ib * stride;  // slice e - 1 of the state's column
         V* out = nxt + j * stride;
@@ -670,10 +681,12 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
             out[t * sn] = sv;
             part += vtotal(sv);
         }
+        if (j + 1 < vn) {
 #pragma unroll
-        for (int c = C - 1; c >= 0; c--) {
-            if (++jc[c] < bget(nx.w, c)) break;
-            jc[c] = 0;
+            for (int c = C - 1; c >= 0; c--) {
+                if (++jc[c] < bget(nx.w, c)) break;
+                jc[c] = 0;
+            }
         }
     }
     return part;
@@ -687,7 +700,10 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
                            int half, int vmax, float* out_mant, int* out_expo) {
     using V = typename StateOf<HB>::V;
     const DevModel& m = *a.model;
+    // model scalars in registers (stores to the slab cannot move them)
     const int T = m.T;
+    const float pf = m.pf;
+    const bool interacting = m.interacting != 0;
     const EmitEntry* tab = a.tab + (long)r * a.entries;
     ReadEmit re;
     re.tab = tab;
@@ -702,12 +718,15 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
 #pragma unroll
     for (int c = 0; c < C; c++) D1 = bset(D1, c, pep.D[c] + 1);
     // Emission box of timestep t: [L_t, min(U_t, D + 1)), packed.
+    // All bytes are below 128 (counts and bounds are at most 16, 0 past the
+    // channels), so byte-wise min and difference work on the whole word: bit
+    // 7 of (uw | 0x80...) - D1 is set in byte c exactly where U >= D + 1, no
+    // borrow crosses a byte, and min(U, D + 1) > L for a live pair.
     auto box_of = [&](uint32_t lw, uint32_t uw) {
         PBox b;
         b.lo = lw & 0x7f7f7f7fu;  // bit 31 of the word is the allow flag
-        b.w = 0;
-#pragma unroll
-        for (int c = 0; c < C; c++) b.w = bset(b.w, c, min(bget(uw, c), bget(D1, c)) - bget(b.lo, c));
+        const uint32_t msk = ((((uw | 0x80808080u) - D1) >> 7) & 0x01010101u) * 0xffu;
+        b.w = ((D1 & msk) | (uw & ~msk)) - b.lo;
         return b;
     };
     auto emission_box = [&](int t) { return box_of(Lpk[t], Upk[t]); };
@@ -830,6 +849,9 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         }
         const PBox nx = box_of(lw, uw);
         const bool allow_t = (lw >> 31) != 0;
+        // every channel of the emission box at most 4 wide (bytes below 128:
+        // byte + 123 reaches bit 7 exactly from 5 up, no carry)
+        const bool narrow = !interacting && ((nx.w + 0x7b7b7b7bu) & 0x80808080u) == 0;
         int kmax = 0;
         float part = 0.0f;
         float em0 = 0.0f;
@@ -882,11 +904,11 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             // Edman (edman-transition.cc:62-162) as a gather from slices e-1
             // (success) and e (failure) of the bleached box into the
             // emission box; both boxes share the lower corner L_t.
-            fused = pk && !m.interacting && bvol<C>(bx.w) <= 255;
-#pragma unroll
-            for (int c = 0; c < C; c++) fused = fused && bget(nx.w, c) <= 4;
+            // (with C <= 3 the bleached box of a narrow emission box is at
+            // most 5^3 states per slice)
+            fused = pk && narrow && (C <= 3 || bvol<C>(bx.w) <= 255);
             if (fused) {
-                part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, codes, M.edman, m.pf, re, gk, one,
+                part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, codes, M.edman, pf, re, gk, one,
                                          allow_t, fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
                 if (kmax == WP_EXPO_ZERO) {
                     *out_mant = 0.0f;
@@ -894,7 +916,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
                     return 0;
                 }
             } else {
-                edman_gather<C, HB>(cur, nxt, stride, t, bx, nx, pk, dye_pk, tot_pk, pep, M.edman, m.pf);
+                edman_gather<C, HB>(cur, nxt, stride, t, bx, nx, pk, dye_pk, tot_pk, pep, M.edman, pf);
             }
             V* tmp = cur;
             cur = nxt;
@@ -904,9 +926,6 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         // ---- Emission t (peptide-emission.cc:212-243).  Factors normalised
         // by the largest exponent over the pair's box (a power of two, carried
         // in expo); the pending rescale is folded into the multiplier.
-        bool narrow = !m.interacting;
-#pragma unroll
-        for (int c = 0; c < C; c++) narrow = narrow && bget(nx.w, c) <= 4;
         if (fused) {
             // edman_emit applied the emission
         } else if (narrow) {
@@ -918,7 +937,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
                 return 0;
             }
         } else {
-            part = emission_table<C, V>(cur, stride, t, nx, a.W, tab, m.interacting != 0, fac_prev * bscale, k_prev,
+            part = emission_table<C, V>(cur, stride, t, nx, a.W, tab, interacting, fac_prev * bscale, k_prev,
                                         &kmax, &em0);
             if (kmax == WP_EXPO_ZERO) {
                 *out_mant = 0.0f;
