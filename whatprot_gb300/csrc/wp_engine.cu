@@ -788,6 +788,8 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
     // one wide is one coefficient for the whole state: it is carried in
     // bscale and applied with the next emission multiply instead of a pass.
     float bscale = 1.0f;
+    uint32_t fold_lo = 0xffffffffu;  // corner of the cached folded bleach product
+    float fold_k = 1.0f;
 
     int expo = 0;           // the true state is the stored state times 2^expo
     float pd = 0.0f;        // detached state, in the rescaled frame
@@ -879,11 +881,18 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             // channel, prob(L -> L), and the box does not change.
             if ((bx.w & chan_mask<C>()) == (0x01010101u & chan_mask<C>()) &&
                 ((bx.lo ^ nx.lo) & chan_mask<C>()) == 0) {
+                // the product over channels depends on L_t alone: kept from
+                // the last timestep that folded the same corner
+                if (nx.lo != fold_lo) {
+                    fold_lo = nx.lo;
+                    fold_k = 1.0f;
 #pragma unroll
-                for (int c = 0; c < C; c++) {
-                    const int l = bget(nx.lo, c);
-                    bscale *= M.bleach[c][l * (l + 3) / 2];
+                    for (int c = 0; c < C; c++) {
+                        const int l = bget(nx.lo, c);
+                        fold_k *= M.bleach[c][l * (l + 3) / 2];
+                    }
                 }
+                bscale = fold_k;
             } else
 #pragma unroll 1
             for (int c = 0; c < C; c++) {
