@@ -186,12 +186,15 @@ struct SmemModel {
     float bleach[WP_MAX_CHANNELS][WP_TRI];
     float p_det[WP_MAX_TIMESTEPS];
     // Edman success coefficients (edman-transition.cc:62-162) at
-    // [tot * 16 + n]: for a state with n dyes left of the channel cut at a
-    // position with tot dyes of that channel remaining, x = (1 - p_fail) *
-    // (tot - n) / tot (the cut dye was another one) and y = (1 - p_fail) *
-    // (n + 1) / tot (the state one dye up lost the cut dye).  Row tot = 0
-    // (no dye at the position): x = 1 - p_fail, y = 0.
-    float2 edman[16 * 16];
+    // [n * 17 + tot]: for a state with n dyes left of the channel cut at a
+    // position with tot dyes of that channel remaining, edx = (1 - p_fail) *
+    // (tot - n) / tot (the cut dye was another one) and edy = (1 - p_fail) *
+    // (n + 1) / tot (the state one dye up lost the cut dye).  tot = 0 (no dye
+    // at the position): edx = 1 - p_fail, edy = 0.  Rows of 17 words: the
+    // lanes of a warp (pairs of one read, different peptides) mostly read
+    // one count n at different tot, which then fall in different banks.
+    float edx[16 * 17];
+    float edy[16 * 17];
 };
 
 // Everything one batch of reads needs on the device.  Per-read arrays are
@@ -320,16 +323,19 @@ __device__ __forceinline__ void load_smem_model(SmemModel& S, const DevModel& m)
         S.bleach[c][k] = m.bleach[c][k];
     }
     for (int t = threadIdx.x; t < m.T; t += blockDim.x) S.p_det[t] = m.p_det[t];
-    for (int i = threadIdx.x; i < 16 * 16; i += blockDim.x) {
-        const int tot = i >> 4, n = i & 15;
+    for (int i = threadIdx.x; i < 16 * 17; i += blockDim.x) {
+        const int n = i / 17, tot = i % 17;
         const float qf = 1.0f - m.pf;
         float2 v = make_float2(qf, 0.0f);
-        if (tot > 0) {
+        if (tot > 15) {
+            v = make_float2(0.0f, 0.0f);  // padding, never read
+        } else if (tot > 0) {
             const float c1 = qf * __frcp_rn((float)tot);
             v.x = n < tot ? fmaf(-(float)n, c1, qf) : 0.0f;
             v.y = (float)(n + 1) * c1;
         }
-        S.edman[i] = v;
+        S.edx[i] = v.x;
+        S.edy[i] = v.y;
     }
 }
 

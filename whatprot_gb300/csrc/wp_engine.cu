@@ -303,7 +303,8 @@ template <int C, bool HB>
 __device__ __noinline__ void edman_gather(const typename StateOf<HB>::V* __restrict__ cur,
                                           typename StateOf<HB>::V* __restrict__ nxt, int stride, int t, PBox bx,
                                           PBox nx, bool pk, uint64_t dye_pk, uint64_t tot_pk,
-                                          const PeptideRec& pep, const float2* __restrict__ edman, float pf) {
+                                          const PeptideRec& pep, const float* __restrict__ edx,
+                                          const float* __restrict__ edy, float pf) {
     using V = typename StateOf<HB>::V;
     const float qf = 1.0f - pf;
     int stb[C];
@@ -325,8 +326,7 @@ __device__ __noinline__ void edman_gather(const typename StateOf<HB>::V* __restr
                 tot_i = pep.tot[e - 1];
             }
         }
-        // Edman coefficients of this slice: row DyeTrack(e - 1, dc)
-        const float2* ed = edman + tot_i * 16;
+        // Edman coefficients of this slice: column DyeTrack(e - 1, dc)
         int d_lo = 0, d_wb = 0, d_st = 0;
 #pragma unroll
         for (int c = 0; c < C; c++)
@@ -368,7 +368,7 @@ __device__ __noinline__ void edman_gather(const typename StateOf<HB>::V* __restr
                     for (int c = 0; c < C; c++)
                         if (c == dc) jd = jc[c];
                     const int nc = d_lo + jd;
-                    const float2 cf = ed[nc];
+                    const float2 cf = make_float2(edx[nc * 17 + tot_i], edy[nc * 17 + tot_i]);
                     add = cf.x * xin;
                     if (jd + 1 < d_wb) {
                         float xr;
@@ -553,8 +553,8 @@ __device__ __noinline__ float emission_narrow(V* cur, int stride, int t, PBox nx
 template <int C, bool HB>
 __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __restrict__ cur,
                                          typename StateOf<HB>::V* __restrict__ nxt, int stride, int t, PBox bx,
-                                         PBox nx, const uint8_t* __restrict__ codes, const float2* __restrict__ edman,
-                                         float pf, const ReadEmit& re, int gk, float4 one, bool allow_t, float sf,
+                                         PBox nx, const uint8_t* __restrict__ codes, const float* __restrict__ edx,
+                                         const float* __restrict__ edy, float pf, const ReadEmit& re, int gk, float4 one, bool allow_t, float sf,
                                          int* kmax_out, float* em0_out) {
     using V = typename StateOf<HB>::V;
     // per channel: the box's emission entries normalised by their largest
@@ -589,7 +589,6 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
     const uint32_t up0 = (bx.w + 0x7e7e7e7eu) & 0x80808080u;
     const int vn = bvol<C>(nx.w);
     const int sb = vb * stride, sn = vn * stride;
-    const char* edb = reinterpret_cast<const char*>(edman);
     float part = 0.0f;
     int jc[C];
 #pragma unroll
@@ -620,20 +619,20 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
             const uint32_t code = *cp;
             const uint32_t sel = 0x4440u | (code & 7u);
             const uint32_t b = __byte_perm(X, 0u, sel);
-            const float2 cf = *reinterpret_cast<const float2*>(edb + ((code & 0x78u) << 4) + ((b & 0x7fu) << 3));
+            const int ci = (int)(b & 0x7fu) * 17 + (int)(code >> 3);  // (count, tot)
             float xin;
             if constexpr (HB) {
                 xin = prev.x;
             } else {
                 xin = prev;
             }
-            float add = cf.x * xin;
+            float add = edx[ci] * xin;
             if (b & 0x80u) {
                 const V xr = cs[(int)__byte_perm(stpk, 0u, sel) * stride];
                 if constexpr (HB) {
-                    add = fmaf(cf.y, xr.x, add);
+                    add = fmaf(edy[ci], xr.x, add);
                 } else {
-                    add = fmaf(cf.y, xr, add);
+                    add = fmaf(edy[ci], xr, add);
                 }
             }
             return add;
@@ -917,7 +916,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             // most 5^3 states per slice)
             fused = pk && narrow && (C <= 3 || bvol<C>(bx.w) <= 255);
             if (fused) {
-                part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, codes, M.edman, pf, re, gk, one,
+                part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, codes, M.edx, M.edy, pf, re, gk, one,
                                          allow_t, fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
                 if (kmax == WP_EXPO_ZERO) {
                     *out_mant = 0.0f;
@@ -925,7 +924,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
                     return 0;
                 }
             } else {
-                edman_gather<C, HB>(cur, nxt, stride, t, bx, nx, pk, dye_pk, tot_pk, pep, M.edman, pf);
+                edman_gather<C, HB>(cur, nxt, stride, t, bx, nx, pk, dye_pk, tot_pk, pep, M.edx, M.edy, pf);
             }
             V* tmp = cur;
             cur = nxt;
