@@ -36,6 +36,8 @@ __global__ void wp_prep_reads_kernel(const DevModel*, const double*, int, unsign
 __global__ void wp_read_summary_kernel(BatchArgs);
 __global__ void wp_window_factors_kernel(BatchArgs);
 __global__ void wp_compact_kernel(BatchArgs);
+__global__ void wp_compact_groups_kernel(BatchArgs);
+size_t wp_compact_groups_smem_bytes(int n_grp, int P);
 __global__ void wp_reduce_kernel(BatchArgs, int32_t*, double*, double*, double*, const int*);
 __global__ void wp_logp_kernel(const float*, const int*, long, double*);
 __global__ void wp_count_flops_kernel(BatchArgs, double*);
@@ -200,6 +202,8 @@ struct wp_ctx {
     std::vector<PeptideRec> recs;
     DevBuf d_peps, d_ids, d_counts, d_perm, d_shape_rank, d_uniq_D, d_pep_u;
     int n_uniq_D = 0;
+    DevBuf d_grp_start, d_grp_D, d_pep_Dw;  // runs of perm with one dye-count vector
+    int n_grp = 0;
 
     // Kernel timing.
     bool timing = false;
@@ -415,6 +419,36 @@ wp_status plan_peptides(wp_ctx* ctx) {
     WP_CUDA(ctx->d_perm.ensure(sizeof(int) * std::max(P, 1)), "alloc perm");
     WP_CUDA(cudaMemcpyAsync(ctx->d_perm.p, perm.data(), sizeof(int) * P, cudaMemcpyHostToDevice, ctx->stream),
             "copy perm");
+    // Groups: the runs of the shape order with one dye-count vector (the key
+    // orders by the vector, so each vector is one run).
+    {
+        std::vector<int> gs;
+        std::vector<uint32_t> gd, pdw(P);
+        for (int i = 0; i < P; i++) {
+            uint32_t k = 0;
+            for (int c = 0; c < WP_MAX_CHANNELS; c++) k |= (uint32_t)ctx->recs[i].D[c] << (8 * c);
+            pdw[i] = k;
+        }
+        for (int i = 0; i < P; i++)
+            if (i == 0 || pdw[perm[i]] != pdw[perm[i - 1]]) {
+                gs.push_back(i);
+                gd.push_back(pdw[perm[i]]);
+            }
+        gs.push_back(P);
+        ctx->n_grp = (int)gd.size();
+        WP_CUDA(ctx->d_grp_start.ensure(sizeof(int) * gs.size()), "alloc groups");
+        WP_CUDA(ctx->d_grp_D.ensure(sizeof(uint32_t) * std::max<size_t>(gd.size(), 1)), "alloc groups");
+        WP_CUDA(ctx->d_pep_Dw.ensure(sizeof(uint32_t) * std::max(P, 1)), "alloc groups");
+        WP_CUDA(cudaMemcpyAsync(ctx->d_grp_start.p, gs.data(), sizeof(int) * gs.size(), cudaMemcpyHostToDevice,
+                                ctx->stream), "copy groups");
+        if (!gd.empty())
+            WP_CUDA(cudaMemcpyAsync(ctx->d_grp_D.p, gd.data(), sizeof(uint32_t) * gd.size(), cudaMemcpyHostToDevice,
+                                    ctx->stream), "copy groups");
+        if (P > 0)
+            WP_CUDA(cudaMemcpyAsync(ctx->d_pep_Dw.p, pdw.data(), sizeof(uint32_t) * P, cudaMemcpyHostToDevice,
+                                    ctx->stream), "copy groups");
+        WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+    }
     WP_CUDA(ctx->d_peps.ensure(sizeof(PeptideRec) * std::max(P, 1)), "alloc peptides");
     WP_CUDA(cudaMemcpyAsync(ctx->d_peps.p, ctx->recs.data(), sizeof(PeptideRec) * P,
                             cudaMemcpyHostToDevice, ctx->stream), "copy peptides");
@@ -565,6 +599,16 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
     a.uniq_D = ctx->d_uniq_D.as<uint32_t>();
     a.pep_u = ctx->d_pep_u.as<int>();
     a.n_uniq = ctx->n_uniq_D;
+    // Classify over all peptides: the compaction works per group of
+    // peptides with one dye-count vector and writes nothing for empty pairs
+    // (the reduce tells them by their vector); loglik keeps every slot written.
+    if (mode == MODE_CLASSIFY && !a.cand && ctx->n_grp <= WP_GROUP_MAX) {
+        a.grp_start = ctx->d_grp_start.as<int>();
+        a.grp_D = ctx->d_grp_D.as<uint32_t>();
+        a.n_grp = ctx->n_grp;
+        a.pep_Dw = ctx->d_pep_Dw.as<uint32_t>();
+        a.dead_by_shape = 1;
+    }
     ctx->last_slots = n_slots;
     const size_t ns = (size_t)std::max<long>(n_slots, 1);
     WP_CUDA(ctx->d_res_mant.ensure(sizeof(float) * ns), "alloc results");
@@ -631,7 +675,22 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         a.live_count = cnt + 10;
         {
             TimedLaunch tl(ctx, 1);
-            wp_compact_kernel<<<R, 256, 0, ctx->stream>>>(a);
+            if (a.dead_by_shape) {
+                // persistent: as many CTAs as are resident, at most one warp per read
+                const size_t gsm = wp_compact_groups_smem_bytes(a.n_grp, a.P);
+                WP_CUDA(cudaFuncSetAttribute(wp_compact_groups_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)gsm), "compact attribute");
+                int per_sm = 0;
+                WP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wp_compact_groups_kernel,
+                                                                      WP_GROUP_WARPS * 32, gsm), "compact occupancy");
+                int sms = 1;
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+                const int grid = std::max(1, std::min(sms * std::max(per_sm, 1),
+                                                      (R + WP_GROUP_WARPS - 1) / WP_GROUP_WARPS));
+                wp_compact_groups_kernel<<<grid, WP_GROUP_WARPS * 32, gsm, ctx->stream>>>(a);
+            } else {
+                wp_compact_kernel<<<R, 256, 0, ctx->stream>>>(a);
+            }
             ctx->launches++;
             WP_CUDA(cudaGetLastError(), "compact launch");
         }

@@ -22,6 +22,9 @@
 #define WP_W (WP_MAX_DYES_PER_CHANNEL + 1)      // extent cap per channel
 #define WP_TRI (WP_W * (WP_W + 1) / 2)          // triangular table size
 #define WP_MAX_TIERS 4                          // engine passes the compaction routes to
+#define WP_GROUP_WARPS 8      // warps per CTA of wp_compact_groups_kernel (one read at a time each)
+#define WP_GROUP_MAX 512      // dye-count vectors (groups) that kernel takes
+#define WP_GROUP_PERM_SMEM 8192  // peptides up to which it stages the shape order in shared memory
 
 struct DevModel {
     int C;
@@ -241,6 +244,16 @@ struct BatchArgs {
     const uint32_t* uniq_D;    // distinct dye-count vectors, byte c = channel c (or null)
     const int* pep_u;          // per peptide: its vector's index in uniq_D
     int n_uniq;
+    // All-peptides mode: the runs of perm with one dye-count vector
+    // ("groups"): group u is perm[grp_start[u] .. grp_start[u + 1]) with
+    // vector grp_D[u] (byte c = channel c); pep_Dw[p] is peptide p's vector.
+    const int* grp_start;
+    const uint32_t* grp_D;
+    int n_grp;
+    const uint32_t* pep_Dw;
+    // nonzero: the compaction wrote no result for empty pairs (all-peptides
+    // mode, wp_compact_groups_kernel); the reduce tells them by their shape
+    int dead_by_shape;
     const int* slot_off;       // [R + 1] or null
     float* res_mant;           // per slot: P = res_mant * 2^res_expo
     int* res_expo;
@@ -300,6 +313,49 @@ __device__ inline int pair_vmax(int C, int T, const uint32_t* Lw, const uint32_t
         vmax = max(vmax, max(max(vp, vb), max(vn, vm)));
     }
     return vmax;
+}
+
+// pair_vmax with the channel count fixed and the dye counts packed one per
+// byte (register arithmetic only; pair_vmax_w picks C at run time).
+template <int C>
+__device__ __forceinline__ int pair_vmax_c(int T, const uint32_t* Lw, const uint32_t* Uw, uint32_t Dw) {
+    int lo_p[C], w_p[C], d1[C];
+    int vmax = 1;
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+        d1[c] = (int)((Dw >> (8 * c)) & 0xffu) + 1;
+        const int l = (int)((Lw[0] >> (8 * c)) & 0x7fu);
+        lo_p[c] = l;
+        w_p[c] = min((int)((Uw[0] >> (8 * c)) & 0xffu), d1[c]) - l;
+        vmax *= w_p[c];
+    }
+    for (int t = 1; t < T; t++) {
+        const uint32_t lw = Lw[t], uw = Uw[t];
+        int vp = t, vb = t, vn = t + 1, vm = t;
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+            const int ln = (int)((lw >> (8 * c)) & 0x7fu);
+            const int wn = min((int)((uw >> (8 * c)) & 0xffu), d1[c]) - ln;
+            const int wb = min(ln + wn + 1, lo_p[c] + w_p[c]) - ln;
+            vp *= w_p[c];
+            vb *= wb;
+            vn *= wn;
+            vm *= max(wb, w_p[c]);
+            lo_p[c] = ln;
+            w_p[c] = wn;
+        }
+        vmax = max(vmax, max(max(vp, vb), max(vn, vm)));
+    }
+    return vmax;
+}
+
+__device__ __forceinline__ int pair_vmax_w(int C, int T, const uint32_t* Lw, const uint32_t* Uw, uint32_t Dw) {
+    switch (C) {
+        case 1: return pair_vmax_c<1>(T, Lw, Uw, Dw);
+        case 2: return pair_vmax_c<2>(T, Lw, Uw, Dw);
+        case 3: return pair_vmax_c<3>(T, Lw, Uw, Dw);
+        default: return pair_vmax_c<4>(T, Lw, Uw, Dw);
+    }
 }
 
 __host__ __device__ inline int slot_begin(const BatchArgs& a, int r) {

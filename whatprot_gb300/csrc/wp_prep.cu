@@ -376,13 +376,11 @@ __global__ void wp_compact_kernel(BatchArgs a) {
     const bool vtab = a.uniq_D && a.n_uniq > 0 && a.n_uniq <= WP_COMPACT_UNIQ && !read_empty;
     if (vtab) {
         for (int u = threadIdx.x; u < a.n_uniq; u += blockDim.x) {
-            uint8_t D[WP_MAX_CHANNELS];
+            const uint32_t Dw = a.uniq_D[u];
             bool ok = true;
-            for (int c = 0; c < WP_MAX_CHANNELS; c++) {
-                D[c] = (uint8_t)((a.uniq_D[u] >> (8 * c)) & 0xffu);
-                if (c < C && D[c] < minD[c]) ok = false;
-            }
-            s_vmax[u] = ok ? pair_vmax(C, m.T, sL, sU, D) : 0;
+            for (int c = 0; c < C; c++)
+                if ((int)((Dw >> (8 * c)) & 0xffu) < minD[c]) ok = false;
+            s_vmax[u] = ok ? pair_vmax_w(C, m.T, sL, sU, Dw) : 0;
         }
     }
     // Candidate mode: the read's slots in the peptides' shape order (up to
@@ -448,7 +446,10 @@ __global__ void wp_compact_kernel(BatchArgs a) {
                     // the pair's largest box waits in its result slot for
                     // the engine, which checks it against its slab before
                     // any write
-                    const int vm = vtab ? s_vmax[a.pep_u[p]] : pair_vmax(C, m.T, sL, sU, pep.D);
+                    const int vm = vtab ? s_vmax[a.pep_u[p]]
+                                        : pair_vmax_w(C, m.T, sL, sU,
+                                                      (uint32_t)pep.D[0] | ((uint32_t)pep.D[1] << 8) |
+                                                              ((uint32_t)pep.D[2] << 16) | ((uint32_t)pep.D[3] << 24));
                     a.res_expo[g] = vm;
                     dest = 0;
                     if (a.n_tiers > 0) {
@@ -514,4 +515,139 @@ __global__ void wp_compact_kernel(BatchArgs a) {
         __syncthreads();
     }
     if (threadIdx.x == 0 && a.live_count && s_live) atomicAdd(a.live_count, s_live);
+}
+
+// All-peptides mode, one warp per read: the compaction of wp_compact_kernel
+// done once per group of peptides sharing a dye-count vector (a run of the
+// shape order).  Whether a pair is empty (L_0 > D on some channel) and its
+// largest box depend on the peptide through that vector alone, so each group
+// is routed as a whole: its pairs go, in the shape order, to the list of the
+// first engine pass whose slab holds the box, with the box size left in
+// their result slots for the engine.  Empty pairs get no write: the reduce
+// (BatchArgs::dead_by_shape) gives them P = 0 from their vector.  The read's
+// pairs of a list take one contiguous range (one global atomic per list).
+// Persistent CTAs (wp_compact_groups_smem_bytes): the groups and the shape
+// order are staged in shared memory once per CTA, so a warp's per-read work
+// waits on global memory only for the read's box words and the list atomics.
+size_t wp_compact_groups_smem_bytes(int n_grp, int P) {
+    size_t b = (size_t)(n_grp + 1) * sizeof(int) + (size_t)n_grp * sizeof(uint32_t);
+    if (P <= WP_GROUP_PERM_SMEM) b += (size_t)P * sizeof(int);
+    return (b + 15) & ~(size_t)15;
+}
+
+__global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(BatchArgs a) {
+    constexpr int NL = WP_MAX_TIERS + 1;
+    extern __shared__ __align__(16) unsigned char g_smem[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ uint32_t sL[WP_GROUP_WARPS][WP_MAX_TIMESTEPS], sU[WP_GROUP_WARPS][WP_MAX_TIMESTEPS];
+    __shared__ uint16_t s_live[WP_GROUP_WARPS][WP_GROUP_MAX];  // routed groups, in order
+    __shared__ uint16_t s_vm[WP_GROUP_WARPS][WP_GROUP_MAX];    // per group: largest box (engine passes)
+    __shared__ uint8_t s_dest[WP_GROUP_WARPS][WP_GROUP_MAX];   // per group: list (WP_MAX_TIERS: dense)
+    const int n_grp = a.n_grp;
+    int* gstart = reinterpret_cast<int*>(g_smem);
+    uint32_t* gD = reinterpret_cast<uint32_t*>(gstart + n_grp + 1);
+    const bool perm_smem = a.P <= WP_GROUP_PERM_SMEM;
+    int* sperm = reinterpret_cast<int*>(gD + n_grp);
+    for (int i = threadIdx.x; i <= n_grp; i += blockDim.x) gstart[i] = a.grp_start[i];
+    for (int i = threadIdx.x; i < n_grp; i += blockDim.x) gD[i] = a.grp_D[i];
+    if (perm_smem)
+        for (int i = threadIdx.x; i < a.P; i += blockDim.x) sperm[i] = a.perm[i];
+    __syncthreads();
+    const int* perm = perm_smem ? sperm : a.perm;
+    const DevModel& m = *a.model;
+    const int T = m.T, C = m.C;
+    const int nwarps = gridDim.x * WP_GROUP_WARPS;
+    for (int r = blockIdx.x * WP_GROUP_WARPS + wid; r < a.R; r += nwarps) {
+        for (int t = lane; t < T; t += 32) {
+            sL[wid][t] = a.Lpk[(long)r * T + t];
+            sU[wid][t] = a.Upk[(long)r * T + t];
+        }
+        const bool read_empty = a.flags[r] != 0;
+        __syncwarp();
+        const uint32_t L0 = sL[wid][0] & 0x7f7f7f7fu;
+        int tot[NL];
+#pragma unroll
+        for (int k = 0; k < NL; k++) tot[k] = 0;
+        int n_live = 0;  // routed groups so far (warp-uniform)
+        for (int u0 = 0; u0 < n_grp && !read_empty; u0 += 32) {
+            const int u = u0 + lane;
+            int dest = -1;  // -1: empty pairs; -2: no shape holds them (P = 0, err = 2)
+            int vm = 0, cnt = 0;
+            if (u < n_grp) {
+                const uint32_t D = gD[u];
+                // every byte D_c >= L_0,c (bytes below 128: bit 7 of (D | 0x80..) -
+                // L0 stays set exactly where D_c >= L_0,c; bytes past the channels are 0)
+                if (((((D | 0x80808080u) - L0) & 0x80808080u) == 0x80808080u)) {
+                    vm = pair_vmax_w(C, T, sL[wid], sU[wid], D);
+                    cnt = gstart[u + 1] - gstart[u];
+                    dest = 0;
+                    if (a.n_tiers > 0) {
+                        dest = WP_MAX_TIERS;
+                        for (int k = a.n_tiers - 1; k >= 0; k--)
+                            if (vm <= a.tier_half[k]) dest = k;
+                        if (dest == WP_MAX_TIERS && !a.route_dense) dest = -2;
+                    }
+                }
+            }
+            if (dest == -2) atomicExch(a.err, 2);  // no shape holds this pair
+            const unsigned lm = __ballot_sync(0xffffffffu, dest != -1);
+            if (dest != -1) {
+                const int at = n_live + __popc(lm & ((1u << lane) - 1));
+                s_live[wid][at] = (uint16_t)u;
+                s_vm[wid][at] = (uint16_t)min(vm, 65535);
+                s_dest[wid][at] = (uint8_t)(dest < 0 ? 0xffu : dest);
+            }
+            n_live += __popc(lm);
+#pragma unroll
+            for (int k = 0; k < NL; k++)
+                if (dest == k) tot[k] += cnt;
+        }
+        // each list's range for this read: lane k takes list k's atomic
+        int base[NL];
+        int mine = 0, live_pairs = 0;
+#pragma unroll
+        for (int k = 0; k < NL; k++) {
+            int v = tot[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            live_pairs += v;
+            if (lane == k) mine = v;
+        }
+        int b = 0;
+        if (lane < NL && mine > 0) {
+            int* count = lane == WP_MAX_TIERS ? a.ovf_count : a.n_tiers > 0 ? a.tier_count[lane] : a.work_count;
+            b = atomicAdd(count, mine);
+        }
+#pragma unroll
+        for (int k = 0; k < NL; k++) base[k] = __shfl_sync(0xffffffffu, b, k);
+        if (lane == 0 && a.live_count && live_pairs) atomicAdd(a.live_count, live_pairs);
+        __syncwarp();
+        // the appends, group by group in the shape order
+        const long gr = (long)r * a.P;
+        for (int i = 0; i < n_live; i++) {
+            const int u = s_live[wid][i];
+            const int d8 = s_dest[wid][i];
+            const int vm = s_vm[wid][i];
+            const int p0 = gstart[u], cnt = gstart[u + 1] - p0;
+            int2* list = nullptr;
+            int at = 0;
+#pragma unroll
+            for (int k = 0; k < NL; k++)
+                if (d8 == k) {
+                    list = k == WP_MAX_TIERS ? a.ovf : a.n_tiers > 0 ? a.tier_list[k] : a.work;
+                    at = base[k];
+                    base[k] += cnt;
+                }
+            for (int j = lane; j < cnt; j += 32) {
+                const int g = (int)(gr + perm[p0 + j]);
+                if (list) {
+                    a.res_expo[g] = vm;
+                    list[at + j] = make_int2(r, g);
+                } else {
+                    a.res_mant[g] = 0.0f;
+                    a.res_expo[g] = 0;
+                }
+            }
+        }
+        __syncwarp();
+    }
 }

@@ -71,6 +71,16 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
     const int g0 = slot_begin(a, r);
     const int g1 = a.slot_off ? a.slot_off[r + 1] : g0 + a.P;
     Cand best = {0.0f, 0, INT_MAX, -1};
+    // dead_by_shape: slots of empty pairs hold nothing; a pair is empty when
+    // the read is or when L_0 > D on some channel (every byte of the
+    // peptide's vector D >= L_0, bytes below 128, else empty)
+    const bool by_shape = a.dead_by_shape != 0;
+    uint32_t L0 = 0;
+    bool read_empty = false;
+    if (by_shape) {
+        L0 = a.Lpk[(long)r * a.model->T] & 0x7f7f7f7fu;
+        read_empty = a.flags[r] != 0;
+    }
     int El = INT_MIN;  // the lane's reference exponent (none yet)
     float hi = 0.0f, lo = 0.0f;
     double big = 0.0;  // terms with counts >= 2^24, relative to 2^El
@@ -86,9 +96,17 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
             ev[u] = 0;
             cv[u] = 0;
             if (g < g1) {
-                mv[u] = a.res_mant[g];
-                ev[u] = a.res_expo[g];
-                cv[u] = a.counts[slot_pep(a, r, g)];
+                const int p = slot_pep(a, r, g);
+                bool live = true;
+                if (by_shape) {
+                    const uint32_t D = a.pep_Dw[p];
+                    live = !read_empty && (((D | 0x80808080u) - L0) & 0x80808080u) == 0x80808080u;
+                }
+                if (live) {
+                    mv[u] = a.res_mant[g];
+                    ev[u] = a.res_expo[g];
+                    cv[u] = a.counts[p];
+                }
             }
         }
 #pragma unroll
