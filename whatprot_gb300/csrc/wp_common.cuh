@@ -52,6 +52,7 @@ struct DevModel {
     double e_sig[WP_MAX_CHANNELS][WP_W + 1];
     double e_norm[WP_MAX_CHANNELS][WP_W + 1];
     double e_den[WP_MAX_CHANNELS][WP_W + 1];
+    double e_l2den[WP_MAX_CHANNELS][WP_W + 1];  // log2(e) / e_den: the pdf's exponent in base 2
 };
 
 // Host side: fills the e_* tables of a non-interacting model from mu, sig
@@ -69,6 +70,7 @@ inline void wp_fill_emission_tables(DevModel& m) {
             m.e_sig[c][n] = s;
             m.e_norm[c][n] = 1.0 / (s * sqrt(2.0 * pi));
             m.e_den[c][n] = 2.0 * s * s;
+            m.e_l2den[c][n] = 1.4426950408889634074 / m.e_den[c][n];
         }
 }
 

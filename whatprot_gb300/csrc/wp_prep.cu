@@ -139,7 +139,9 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
                     double mu = dev_adjusted_mu(m, c, counts_hi);
                     s = dist_cutoff * dev_sigma(m, c, mu);
                 }
-                unsigned new_cts = (unsigned)lround((rad[t * C + c] + s) / mu1);
+                // x / 1.0 == x exactly: the division (slow in FP64) only where mu != 1
+                const double q = mu1 == 1.0 ? rad[t * C + c] + s : (rad[t * C + c] + s) / mu1;
+                unsigned new_cts = (unsigned)lround(q);
                 if (new_cts > max_num_dyes + 1) new_cts = max_num_dyes + 1;
                 if (new_cts != counts_hi[c]) {
                     did_change = true;
@@ -199,13 +201,36 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
         // pdf of channel c depends on n_c only: store per (t, c, n).
         for (int c = 0; c < C; c++) {
             for (int n = 0; n < W; n++) {
-                double v = 0.0;
+                EmitEntry en;
+                en.mant = 0.0f;
+                en.expo = WP_EXPO_ZERO;
                 if ((unsigned)n >= lo[c] && (unsigned)n < hi[c]) {
-                    // pdf_helper (channel-model.h:61-70) from the tables
+                    // pdf_helper (channel-model.h:61-70) from the tables:
+                    // norm * exp(-offset^2 / den) = norm * 2^y, y in FP64; the
+                    // power of two of its integer part is exact and 2^frac
+                    // (in [1, 2)) is taken in FP32, which the FP32 mantissa
+                    // stored keeps to a few units in the last place.  Far
+                    // tails (y <= -1000, where FP64 itself nears underflow)
+                    // take the FP64 exp so that zeros fall where the
+                    // reference's do.
                     const double offset = rad[t * C + c] - m.e_amu[c][n];
-                    v = m.e_norm[c][n] * exp(-offset * offset / m.e_den[c][n]);
+                    const double y = -(offset * offset) * m.e_l2den[c][n];
+                    if (y > -1000.0) {
+                        const double fl = floor(y);
+                        const float fr = exp2f((float)(y - fl));
+                        int ex;
+                        const double mt = frexp(m.e_norm[c][n] * (double)fr, &ex);
+                        en.mant = (float)mt;
+                        en.expo = ex + (int)fl;
+                        if (en.mant >= 1.0f) {  // rounding up to 1.0
+                            en.mant = 0.5f;
+                            en.expo += 1;
+                        }
+                    } else {
+                        en = make_entry(m.e_norm[c][n] * exp(-offset * offset / m.e_den[c][n]));
+                    }
                 }
-                out[(t * C + c) * W + n] = make_entry(v);
+                out[(t * C + c) * W + n] = en;
             }
         }
     } else {
