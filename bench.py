@@ -1430,11 +1430,11 @@ def main():
     flops_per_launch = algo_flops * split_steps / max(fwd_n, 1)
     achieved = flops_per_launch / (fwd_avg_ms * 1e-3) / 1e12 if fwd_n else None
     # DRAM traffic of the engine passes from one ncu capture of a 5,000-read
-    # batch of this workload (26.9 + 32.1 + 8.4 + 1.6 MB over its four
-    # passes), scaled by the reads
-    # (the traffic is per pair) and spread over this step's forward launches
+    # batch of this workload (38.3 + 3.85 + 2.69 + 0.62 MB over its four
+    # passes), scaled by the reads (the traffic is per pair) and spread over
+    # this step's forward launches
     launches_per_step = fwd_n / split_steps if fwd_n else 0.0
-    traffic = (69.0e6 * R / 5000.0) / launches_per_step if launches_per_step else None
+    traffic = (45.5e6 * R / 5000.0) / launches_per_step if launches_per_step else None
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if (achieved and peak) else None, "traffic": traffic,
                 "traffic_source": "ncu dram__bytes_read+write of the engine passes at 5,000 reads, scaled to "
