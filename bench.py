@@ -837,6 +837,108 @@ def make_data(seed: int, reads: int):
     return sm, ds, rads[:reads].copy(), ids[:reads].copy()
 
 
+class GpmDram:
+    """DRAM traffic over an interval from NVML's GPU performance monitoring
+    (GPM) counters, read through the driver's libnvidia-ml with ctypes: the
+    DRAM bandwidth utilisation between two samples (percent of the
+    theoretical bandwidth, bus width x memory clock x 2) times that
+    bandwidth and the interval.  `measure(fn)` returns (bytes, seconds,
+    percent) or raises; the GPU is only read, nothing is set."""
+
+    METRIC_DRAM_BW_UTIL = 10
+    METRIC_MAX = 210
+
+    def __init__(self, device: int):
+        import ctypes
+        import torch
+        self.ct = ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        self.lib = lib
+        if lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        props = torch.cuda.get_device_properties(device)
+        self.handle = ctypes.c_void_p()
+        uuid = ("GPU-" + str(props.uuid)).encode()
+        if lib.nvmlDeviceGetHandleByUUID(ctypes.c_char_p(uuid), ctypes.byref(self.handle)) != 0:
+            raise RuntimeError("no NVML handle for the device")
+
+        class Support(ctypes.Structure):
+            _fields_ = [("version", ctypes.c_uint), ("isSupportedDevice", ctypes.c_uint)]
+
+        sup = Support(1, 0)
+        if lib.nvmlGpmQueryDeviceSupport(self.handle, ctypes.byref(sup)) != 0 or not sup.isSupportedDevice:
+            raise RuntimeError("GPM not supported on this device")
+
+        class Info(ctypes.Structure):
+            _fields_ = [("shortName", ctypes.c_char_p), ("longName", ctypes.c_char_p), ("unit", ctypes.c_char_p)]
+
+        class Metric(ctypes.Structure):
+            _fields_ = [("metricId", ctypes.c_uint), ("nvmlReturn", ctypes.c_int), ("value", ctypes.c_double),
+                        ("metricInfo", Info)]
+
+        class MetricsGet(ctypes.Structure):
+            _fields_ = [("version", ctypes.c_uint), ("numMetrics", ctypes.c_uint), ("sample1", ctypes.c_void_p),
+                        ("sample2", ctypes.c_void_p), ("metrics", Metric * GpmDram.METRIC_MAX)]
+
+        self.MetricsGet = MetricsGet
+        # the theoretical bandwidth the percentage refers to: bus width x
+        # maximum memory clock x 2 (double data rate)
+        mhz, bits = ctypes.c_uint(0), ctypes.c_uint(0)
+        if (lib.nvmlDeviceGetMaxClockInfo(self.handle, 2, ctypes.byref(mhz)) != 0 or
+                lib.nvmlDeviceGetMemoryBusWidth(self.handle, ctypes.byref(bits)) != 0 or not mhz.value or
+                not bits.value):
+            raise RuntimeError("memory clock or bus width unavailable")
+        self.peak_bytes_s = 2.0 * mhz.value * 1e6 * bits.value / 8.0
+
+    def measure(self, fn):
+        ct, lib = self.ct, self.lib
+        s1, s2 = ct.c_void_p(), ct.c_void_p()
+        if lib.nvmlGpmSampleAlloc(ct.byref(s1)) != 0 or lib.nvmlGpmSampleAlloc(ct.byref(s2)) != 0:
+            raise RuntimeError("GPM sample allocation failed")
+        try:
+            if lib.nvmlGpmSampleGet(self.handle, s1) != 0:
+                raise RuntimeError("GPM sample failed")
+            t0 = time.perf_counter()
+            fn()
+            t1 = time.perf_counter()
+            if lib.nvmlGpmSampleGet(self.handle, s2) != 0:
+                raise RuntimeError("GPM sample failed")
+            mg = self.MetricsGet()
+            mg.version = 1
+            mg.numMetrics = 1
+            mg.sample1 = s1
+            mg.sample2 = s2
+            mg.metrics[0].metricId = self.METRIC_DRAM_BW_UTIL
+            if lib.nvmlGpmMetricsGet(ct.byref(mg)) != 0 or mg.metrics[0].nvmlReturn != 0:
+                raise RuntimeError("GPM metrics unavailable")
+            pct = mg.metrics[0].value
+            return pct / 100.0 * self.peak_bytes_s * (t1 - t0), t1 - t0, pct
+        finally:
+            lib.nvmlGpmSampleFree(s1)
+            lib.nvmlGpmSampleFree(s2)
+
+
+def engine_traffic_live(ctx, device: int, steps_equiv_ms: float):
+    """DRAM bytes of one replay of the engine passes (all passes and the
+    dense kernel of the last classify batch), measured on this run: NVML GPM
+    over enough replays to span a few hundred ms (GPM samples refresh every
+    100 ms).  Returns (bytes per replay, source note) or (None, reason)."""
+    import torch
+    try:
+        g = GpmDram(device)
+    except Exception as e:  # noqa: BLE001 - any NVML absence is reported, not fatal
+        return None, f"NVML GPM unavailable: {e}"
+    reps = max(8, int(400.0 / max(steps_equiv_ms, 0.1)))
+    ctx.engine_replay(2)  # warm
+    try:
+        nbytes, secs, pct = g.measure(lambda: (ctx.engine_replay(reps), torch.cuda.synchronize()))
+    except Exception as e:  # noqa: BLE001
+        return None, f"NVML GPM failed: {e}"
+    return nbytes / reps, (f"NVML GPM DRAM bandwidth utilisation {pct:.2f} % of the theoretical "
+                           f"{g.peak_bytes_s / 1e9:.0f} GB/s over {reps} replays of the engine passes "
+                           f"({secs * 1e3:.0f} ms), per replay")
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -1425,6 +1527,9 @@ def main():
     e2e = {"value": pairs * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(rads.nbytes),
            "d2h_bytes_per_step": int(R * (4 + 8 + 8 + 8))}
 
+    # DRAM traffic of the engine passes, measured now (replays of the last
+    # batch's passes under NVML GPM); the ncu figure below is the fallback
+    live_bytes, live_src = engine_traffic_live(ctx, local, fwd_ms / split_steps if split_steps else 20.0)
     peak = ctx.fp32_peak_tflops()
     fwd_avg_ms = fwd_ms / max(fwd_n, 1)
     flops_per_launch = algo_flops * split_steps / max(fwd_n, 1)
@@ -1434,11 +1539,16 @@ def main():
     # passes), scaled by the reads (the traffic is per pair) and spread over
     # this step's forward launches
     launches_per_step = fwd_n / split_steps if fwd_n else 0.0
-    traffic = (45.5e6 * R / 5000.0) / launches_per_step if launches_per_step else None
+    traffic_ncu = (45.5e6 * R / 5000.0) / launches_per_step if launches_per_step else None
+    ncu_src = ("ncu dram__bytes_read+write of the engine passes at 5,000 reads, scaled to this batch by reads, "
+               "per forward launch")
+    if live_bytes is not None and launches_per_step:
+        traffic, traffic_src = live_bytes / launches_per_step, live_src + ", per forward launch"
+    else:
+        traffic, traffic_src = traffic_ncu, ncu_src + (f" ({live_src})" if live_src else "")
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if (achieved and peak) else None, "traffic": traffic,
-                "traffic_source": "ncu dram__bytes_read+write of the engine passes at 5,000 reads, scaled to "
-                                  "this batch by reads, per forward launch",
+                "traffic_source": traffic_src, "traffic_ncu": traffic_ncu, "traffic_ncu_source": ncu_src,
                 "kernel": "wp_engine_kernel (passes 1-4) + wp_dense_kernel",
                 "peak_source": "FP32 FMA loop measured live (wp_probe_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                 "algorithmic_flops_per_step": algo_flops,

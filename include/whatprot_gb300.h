@@ -567,6 +567,15 @@ void* wp_ctx_stream(const wp_ctx* ctx);
 wp_status wp_timing_enable(wp_ctx* ctx, int enable);
 wp_status wp_timing_read(wp_ctx* ctx, int kind, double* total_ms, long long* launches);
 
+/* Runs the engine passes and the dense kernel of the last wp_hmm_classify /
+ * wp_hmm_classify_device batch on this context again, `reps` times, on the
+ * context's stream (same work lists, the same results written again), and
+ * returns their elapsed time in ms.  For measurements of the forward
+ * kernels alone (e.g. their DRAM traffic over an interval).  WP_ERR_STATE if
+ * no classify batch is held (another kind of call, or a buffer reallocated,
+ * since).  No reference counterpart. */
+wp_status wp_engine_replay(wp_ctx* ctx, int reps, double* ms);
+
 /* Measured FP32 fused-multiply-add throughput of the context's device in
  * TFLOP/s (2 flops per FMA), from a timed loop of independent FMA chains on
  * every SM.  The denominator of the forward kernel's roofline. */

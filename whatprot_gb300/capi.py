@@ -180,6 +180,8 @@ def load_library(path: Optional[str] = None):
     lib.wp_timing_read.restype = I
     lib.wp_probe_fp32_peak.argtypes = [V, ctypes.POINTER(D)]
     lib.wp_probe_fp32_peak.restype = I
+    lib.wp_engine_replay.argtypes = [V, I, ctypes.POINTER(D)]
+    lib.wp_engine_replay.restype = I
     lib.wp_last_batch_stats.argtypes = [V, V]
     lib.wp_last_batch_stats.restype = I
     lib.wp_fit_set_kernel.argtypes = [V, I]
@@ -761,6 +763,13 @@ class Context:
     def fp32_peak_tflops(self) -> float:
         out = ctypes.c_double()
         self._check(self.lib.wp_probe_fp32_peak(self.h, ctypes.byref(out)))
+        return out.value
+
+    def engine_replay(self, reps: int) -> float:
+        """wp_engine_replay: the last classify batch's engine passes run
+        `reps` more times; their elapsed ms."""
+        out = ctypes.c_double()
+        self._check(self.lib.wp_engine_replay(self.h, int(reps), ctypes.byref(out)))
         return out.value
 
 

@@ -164,9 +164,22 @@ struct GraphKey {
     }
 };
 
+// The engine launches of the last classify batch (wp_engine_replay).
+struct EngineReplay {
+    bool valid = false;
+    long long epoch = -1;  // g_alloc_epoch when recorded
+    BatchArgs a;
+    int C = 0, T = 0, nt = 0, dense_warps = 0;
+    bool hb = false;
+    int threads[WP_MAX_TIERS], half[WP_MAX_TIERS];
+    int2* list[WP_MAX_TIERS];
+    int* cnt = nullptr;
+};
+
 struct wp_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    EngineReplay replay;
     std::mutex mu;
     std::string err;
     long long launches = 0;
@@ -497,6 +510,7 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
                     int32_t* d_out_id, double* d_out_score, double* d_out_total, double* d_out_log,
                     double* d_flops, const int32_t* d_cand_in = nullptr, const int32_t* d_cand_off_in = nullptr) {
     const int C = ctx->hm.C, T = ctx->hm.T;
+    ctx->replay.valid = false;
     wp_status st = plan_peptides(ctx);
     if (st != WP_OK) return st;
     const bool hb = ctx->hm.has_block != 0;
@@ -711,6 +725,23 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
             size_t smem = wp_dense_smem_bytes(T, a.dense_S_cap, C, hb, dense_warps);
             WP_CUDA(wp_launch_dense(hb, dense_warps * 32, smem, ctx->stream, a), "dense launch");
             ctx->launches++;
+        }
+        if (mode == MODE_CLASSIFY) {
+            EngineReplay& rp = ctx->replay;
+            rp.a = a;
+            rp.C = C;
+            rp.T = T;
+            rp.hb = hb;
+            rp.nt = nt;
+            rp.dense_warps = dense_warps;
+            for (int k = 0; k < nt; k++) {
+                rp.threads[k] = tiers[k].threads;
+                rp.half[k] = tiers[k].half;
+                rp.list[k] = lists[k]->as<int2>();
+            }
+            rp.cnt = cnt;
+            rp.epoch = g_alloc_epoch;
+            rp.valid = true;
         }
     }
     if (mode == MODE_CLASSIFY) {
@@ -1532,6 +1563,53 @@ wp_status wp_timing_read(wp_ctx* ctx, int kind, double* total_ms, long long* lau
     collect_timing(ctx);
     if (total_ms) *total_ms = ctx->t_ms[kind];
     if (launches) *launches = ctx->t_n[kind];
+    return WP_OK;
+}
+
+wp_status wp_engine_replay(wp_ctx* ctx, int reps, double* ms) {
+    if (!ctx || reps < 0) return WP_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    WP_CUDA(cudaSetDevice(ctx->device), "set device");
+    EngineReplay& rp = ctx->replay;
+    if (!rp.valid || rp.epoch != g_alloc_epoch) return fail(ctx, WP_ERR_STATE, "no classify batch to replay");
+    BatchArgs a = rp.a;
+    a.replay_trust = 1;  // the result slots hold results now, not box sizes
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    WP_CUDA(cudaEventCreate(&e0), "event");
+    WP_CUDA(cudaEventCreate(&e1), "event");
+    WP_CUDA(cudaEventRecord(e0, ctx->stream), "event");
+    for (int r = 0; r < reps; r++) {
+        // the lists and their counts are as the compaction left them (no
+        // pass hands pairs on: each holds only pairs its slab holds); the
+        // heads go back to the start
+        for (int k = 0; k < rp.nt; k++)
+            WP_CUDA(cudaMemsetAsync(rp.cnt + 2 * k + 1, 0, sizeof(int), ctx->stream), "reset head");
+        WP_CUDA(cudaMemsetAsync(rp.cnt + 9, 0, sizeof(int), ctx->stream), "reset head");
+        for (int k = 0; k < rp.nt; k++) {
+            const bool last = k + 1 == rp.nt;
+            size_t smem = wp_engine_smem_bytes(rp.half[k], 0, rp.hb, rp.threads[k]);
+            WP_CUDA(wp_launch_engine(rp.C, rp.hb, rp.threads[k], smem, ctx->stream, a, rp.list[k], rp.cnt + 2 * k,
+                                     rp.cnt + 2 * k + 1, last ? rp.a.ovf : rp.list[k + 1],
+                                     last ? rp.cnt + 8 : rp.cnt + 2 * (k + 1), rp.half[k], 0, 1, nullptr),
+                    "engine pass");
+            ctx->launches++;
+        }
+        if (rp.dense_warps > 0) {
+            size_t smem = wp_dense_smem_bytes(rp.T, rp.a.dense_S_cap, rp.C, rp.hb, rp.dense_warps);
+            WP_CUDA(wp_launch_dense(rp.hb, rp.dense_warps * 32, smem, ctx->stream, a), "dense launch");
+            ctx->launches++;
+        }
+    }
+    WP_CUDA(cudaEventRecord(e1, ctx->stream), "event");
+    WP_CUDA(cudaEventSynchronize(e1), "sync");
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ms) *ms = t;
+    int err = 0;
+    WP_CUDA(cudaMemcpy(&err, ctx->d_err.p, sizeof(int), cudaMemcpyDeviceToHost), "read err");
+    if (err) return fail(ctx, WP_ERR_CUDA, "internal: a replayed pass met a pair its slab does not hold");
     return WP_OK;
 }
 

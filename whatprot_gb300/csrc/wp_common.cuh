@@ -256,6 +256,10 @@ struct BatchArgs {
     // nonzero: the compaction wrote no result for empty pairs (all-peptides
     // mode, wp_compact_groups_kernel); the reduce tells them by their shape
     int dead_by_shape;
+    // nonzero (wp_engine_replay): the engine passes run lists whose pairs
+    // they have run before, so the result slot holds a result, not the
+    // routed box size; the slot is still read, its value ignored
+    int replay_trust;
     const int* slot_off;       // [R + 1] or null
     float* res_mant;           // per slot: P = res_mant * 2^res_expo
     int* res_expo;

@@ -997,8 +997,8 @@ __global__ void __launch_bounds__(WP_ENGINE_THREADS) wp_engine_kernel(BatchArgs 
             const int p = slot_pep(a, rg.x, rg.y);
             float mant;
             int ex;
-            int ov = engine_pair<C, HB>(a, M, rg.x, a.peps[p], slab, codes, nt, L.slab_half, a.res_expo[rg.y],
-                                        &mant, &ex);
+            const int vmax = a.res_expo[rg.y] & (a.replay_trust ? 0 : -1);
+            int ov = engine_pair<C, HB>(a, M, rg.x, a.peps[p], slab, codes, nt, L.slab_half, vmax, &mant, &ex);
             if (ov) {
                 if (L.spill_error) {
                     atomicExch(a.err, 2);
