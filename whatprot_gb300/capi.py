@@ -418,13 +418,23 @@ class Context:
         self._pep_counts = counts.copy()
 
     def classify(self, rads: np.ndarray, dist_cutoff: float = DBL_MAX,
-                 cand: Optional[np.ndarray] = None, cand_off: Optional[np.ndarray] = None):
+                 cand: Optional[np.ndarray] = None, cand_off: Optional[np.ndarray] = None, out=None):
+        """wp_hmm_classify: (best id, score, total, log score) per read.  out:
+        four caller-owned arrays (int32, float64 x 3, at least R each) to
+        write into and return instead of fresh ones (e.g. pinned buffers
+        reused across batches)."""
         rads = np.ascontiguousarray(rads, dtype=np.float64)
         R = rads.shape[0]
-        oid = np.zeros(R, np.int32)
-        osc = np.zeros(R, np.float64)
-        otot = np.zeros(R, np.float64)
-        olog = np.zeros(R, np.float64)
+        if out is not None:
+            oid, osc, otot, olog = out
+            for arr, dt in zip(out, (np.int32, np.float64, np.float64, np.float64)):
+                if arr.dtype != dt or arr.shape[0] < R or not arr.flags.c_contiguous:
+                    raise ValueError("out arrays: int32, float64, float64, float64, contiguous, at least R long")
+        else:
+            oid = np.zeros(R, np.int32)
+            osc = np.zeros(R, np.float64)
+            otot = np.zeros(R, np.float64)
+            olog = np.zeros(R, np.float64)
         if cand is not None:
             cand = np.ascontiguousarray(cand, np.int32)
             cand_off = np.ascontiguousarray(cand_off, np.int32)
