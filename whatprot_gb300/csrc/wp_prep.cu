@@ -556,6 +556,8 @@ __global__ void wp_compact_kernel(BatchArgs a) {
 // waits on global memory only for the read's box words and the list atomics.
 size_t wp_compact_groups_smem_bytes(int n_grp, int P) {
     size_t b = (size_t)(n_grp + 1) * sizeof(int) + (size_t)n_grp * sizeof(uint32_t);
+    b += (size_t)WP_GROUP_WARPS * n_grp * (sizeof(uint32_t) + sizeof(uint16_t));  // sort keys, order
+    b = (b + 15) & ~(size_t)15;
     if (P <= WP_GROUP_PERM_SMEM) b += (size_t)P * sizeof(int);
     return (b + 15) & ~(size_t)15;
 }
@@ -572,7 +574,11 @@ __global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(
     int* gstart = reinterpret_cast<int*>(g_smem);
     uint32_t* gD = reinterpret_cast<uint32_t*>(gstart + n_grp + 1);
     const bool perm_smem = a.P <= WP_GROUP_PERM_SMEM;
-    int* sperm = reinterpret_cast<int*>(gD + n_grp);
+    uint32_t* s_key = gD + n_grp + (size_t)wid * n_grp;  // this warp's sort keys
+    uint16_t* s_ord = reinterpret_cast<uint16_t*>(gD + n_grp + (size_t)WP_GROUP_WARPS * n_grp) + (size_t)wid * n_grp;
+    int* sperm = reinterpret_cast<int*>(
+            (reinterpret_cast<uintptr_t>(gD + n_grp + (size_t)WP_GROUP_WARPS * n_grp) +
+             (size_t)WP_GROUP_WARPS * n_grp * sizeof(uint16_t) + 15) & ~(uintptr_t)15);
     for (int i = threadIdx.x; i <= n_grp; i += blockDim.x) gstart[i] = a.grp_start[i];
     for (int i = threadIdx.x; i < n_grp; i += blockDim.x) gD[i] = a.grp_D[i];
     if (perm_smem)
@@ -590,6 +596,14 @@ __global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(
         const bool read_empty = a.flags[r] != 0;
         __syncwarp();
         const uint32_t L0 = sL[wid][0] & 0x7f7f7f7fu;
+        // U_max - 1 per channel (byte): a group's dyes clamped to it give
+        // the same boxes at every timestep (min(U_t, D + 1) = min(U_t,
+        // D' + 1) for D' = min(D, U_max - 1)), so pairs whose clamped counts
+        // agree run the same steps; the appends order groups by them
+        uint32_t um = 0;
+        for (int t = lane; t < T; t += 32) um = __vmaxu4(um, sU[wid][t]);
+        for (int o = 16; o > 0; o >>= 1) um = __vmaxu4(um, __shfl_xor_sync(0xffffffffu, um, o));
+        const uint32_t um1 = __vsubus4(um, 0x01010101u);  // U >= 1 on every channel of a read with pairs
         int tot[NL];
 #pragma unroll
         for (int k = 0; k < NL; k++) tot[k] = 0;
@@ -621,6 +635,10 @@ __global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(
                 s_live[wid][at] = (uint16_t)u;
                 s_vm[wid][at] = (uint16_t)min(vm, 65535);
                 s_dest[wid][at] = (uint8_t)(dest < 0 ? 0xffu : dest);
+                // sort key: list, clamped counts (4 bits a channel), position
+                const uint32_t dc = __vminu4(gD[u], um1);
+                const uint32_t d16 = (dc & 0xfu) | ((dc >> 4) & 0xf0u) | ((dc >> 8) & 0xf00u) | ((dc >> 12) & 0xf000u);
+                s_key[at] = ((uint32_t)(dest < 0 ? 7 : dest) << 25) | (d16 << 9) | (uint32_t)at;
             }
             n_live += __popc(lm);
 #pragma unroll
@@ -646,9 +664,18 @@ __global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(
         for (int k = 0; k < NL; k++) base[k] = __shfl_sync(0xffffffffu, b, k);
         if (lane == 0 && a.live_count && live_pairs) atomicAdd(a.live_count, live_pairs);
         __syncwarp();
-        // the appends, group by group in the shape order
+        // rank of each routed group by its key (keys are distinct)
+        for (int i = lane; i < n_live; i += 32) {
+            const uint32_t ki = s_key[i];
+            int rank = 0;
+            for (int j = 0; j < n_live; j++) rank += s_key[j] < ki ? 1 : 0;
+            s_ord[rank] = (uint16_t)i;
+        }
+        __syncwarp();
+        // the appends, group by group in key order
         const long gr = (long)r * a.P;
-        for (int i = 0; i < n_live; i++) {
+        for (int o = 0; o < n_live; o++) {
+            const int i = s_ord[o];
             const int u = s_live[wid][i];
             const int d8 = s_dest[wid][i];
             const int vm = s_vm[wid][i];
