@@ -613,9 +613,10 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
         }
         const V* cs = cur + ib * stride;  // slice e - 1 of the state's column
         V* out = nxt + j * stride;
-        // Edman success into slice e from slice e - 1 (value prev): the
-        // state's own count (x) and the state one dye up losing the cut dye (y)
-        auto success = [&](const uint8_t* cp, const V prev) -> float {
+        // Edman success into slice e from slice e - 1 (value prev, column
+        // sp): the state's own count (x) and the state one dye up losing the
+        // cut dye (y)
+        auto success = [&](const uint8_t* cp, const V prev, const V* sp) -> float {
             const uint32_t code = *cp;
             const uint32_t sel = 0x4440u | (code & 7u);
             const uint32_t b = __byte_perm(X, 0u, sel);
@@ -628,7 +629,7 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
             }
             float add = edx[ci] * xin;
             if (b & 0x80u) {
-                const V xr = cs[(int)__byte_perm(stpk, 0u, sel) * stride];
+                const V xr = sp[(int)__byte_perm(stpk, 0u, sel) * stride];
                 if constexpr (HB) {
                     add = fmaf(edy[ci], xr.x, add);
                 } else {
@@ -651,8 +652,32 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
             part += vtotal(sv);
         }
         const uint8_t* cp = codes;
-        for (int e = 1; e < t; e++) {
-            const float add = success(cp, prev);
+        // slices in pairs: two independent chains per step (and two sums)
+        float part2 = 0.0f;
+        int e = 1;
+        for (; e + 1 < t; e += 2) {
+            const V f0 = cs[sb], f1 = cs[2 * sb];
+            const float a0 = success(cp, prev, cs);
+            const float a1 = success(cp + stride, f0, cs + sb);
+            V v0, v1;
+            if constexpr (HB) {
+                v0 = make_float2(fmaf(pf, f0.x, a0), f0.y);
+                v1 = make_float2(fmaf(pf, f1.x, a1), f1.y);
+            } else {
+                v0 = fmaf(pf, f0, a0);
+                v1 = fmaf(pf, f1, a1);
+            }
+            const V s0 = vmul(w, v0), s1 = vmul(w, v1);
+            out[e * sn] = s0;
+            out[(e + 1) * sn] = s1;
+            part += vtotal(s0);
+            part2 += vtotal(s1);
+            prev = f1;
+            cs += 2 * sb;
+            cp += 2 * stride;
+        }
+        if (e < t) {
+            const float add = success(cp, prev, cs);
             cs += sb;
             cp += stride;
             const V f = *cs;
@@ -667,9 +692,10 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
             out[e * sn] = sv;
             part += vtotal(sv);
         }
+        part += part2;
         {
             // slice t: success only (the bleached box has t slices)
-            const float add = success(cp, prev);
+            const float add = success(cp, prev, cs);
             V v;
             if constexpr (HB) {
                 v = make_float2(add, 0.0f);
