@@ -129,19 +129,47 @@ __device__ __noinline__ void binomial_step(const V* __restrict__ src, V* __restr
 #pragma unroll
             for (int k = 0; k < 3; k++)
                 cf[k2][k] = (k < win && k2 < wout && d + k - k2 >= 0) ? tab[rb[k] + k2] : 0.0f;
-        for (int o = 0; o < outer; o++) {
-            const V* s = src + o * win * sk;
-            V* d = dst + o * wout * sk;
-            for (int i = 0; i < inner; i++) {
-                const V* si = s + i * stride;
-                const V x0 = si[0];
-                const V x1 = win > 1 ? si[sk] : vzero(V());
-                const V x2 = win > 2 ? si[2 * sk] : vzero(V());
-                V* di = d + i * stride;
-#pragma unroll
-                for (int k2 = 0; k2 < 3; k2++)
-                    if (k2 < wout) di[k2 * sk] = vfma(cf[k2][2], x2, vfma(cf[k2][1], x1, vmul(cf[k2][0], x0)));
+        // the outer x inner columns as one sequence, two at a time
+        // (independent loads and chains)
+        const int n = outer * inner;
+        const int ostep_in = win * sk - inner * stride, ostep_out = wout * sk - inner * stride;
+        const V* si = src;
+        V* di = dst;
+        int i = 0;
+        auto next = [&]() {
+            si += stride;
+            di += stride;
+            if (++i == inner) {
+                i = 0;
+                si += ostep_in;
+                di += ostep_out;
             }
+        };
+        int q = 0;
+        for (; q + 1 < n; q += 2) {
+            const V* sa = si;
+            V* da = di;
+            next();
+            const V* sb = si;
+            V* db = di;
+            next();
+            const V a0 = sa[0], b0 = sb[0];
+            const V a1 = win > 1 ? sa[sk] : vzero(V()), b1 = win > 1 ? sb[sk] : vzero(V());
+            const V a2 = win > 2 ? sa[2 * sk] : vzero(V()), b2 = win > 2 ? sb[2 * sk] : vzero(V());
+#pragma unroll
+            for (int k2 = 0; k2 < 3; k2++)
+                if (k2 < wout) {
+                    da[k2 * sk] = vfma(cf[k2][2], a2, vfma(cf[k2][1], a1, vmul(cf[k2][0], a0)));
+                    db[k2 * sk] = vfma(cf[k2][2], b2, vfma(cf[k2][1], b1, vmul(cf[k2][0], b0)));
+                }
+        }
+        if (q < n) {
+            const V x0 = si[0];
+            const V x1 = win > 1 ? si[sk] : vzero(V());
+            const V x2 = win > 2 ? si[2 * sk] : vzero(V());
+#pragma unroll
+            for (int k2 = 0; k2 < 3; k2++)
+                if (k2 < wout) di[k2 * sk] = vfma(cf[k2][2], x2, vfma(cf[k2][1], x1, vmul(cf[k2][0], x0)));
         }
         return;
     }
