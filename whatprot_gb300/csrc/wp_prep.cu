@@ -604,46 +604,89 @@ __global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(
         for (int t = lane; t < T; t += 32) um = __vmaxu4(um, sU[wid][t]);
         for (int o = 16; o > 0; o >>= 1) um = __vmaxu4(um, __shfl_xor_sync(0xffffffffu, um, o));
         const uint32_t um1 = __vsubus4(um, 0x01010101u);  // U >= 1 on every channel of a read with pairs
+        // the non-empty groups (every byte D_c >= L_0,c: bytes below 128,
+        // bit 7 of (D | 0x80..) - L0 stays set exactly where D_c >= L_0,c;
+        // bytes past the channels are 0), keyed by their clamped counts
+        int n_live = 0;  // warp-uniform
+        for (int u0 = 0; u0 < n_grp && !read_empty; u0 += 32) {
+            const int u = u0 + lane;
+            bool live = false;
+            uint32_t D = 0;
+            if (u < n_grp) {
+                D = gD[u];
+                live = ((((D | 0x80808080u) - L0) & 0x80808080u) == 0x80808080u);
+            }
+            const unsigned lm = __ballot_sync(0xffffffffu, live);
+            if (live) {
+                const int at = n_live + __popc(lm & ((1u << lane) - 1));
+                s_live[wid][at] = (uint16_t)u;
+                // sort key: clamped counts (4 bits a channel), position
+                const uint32_t dc = __vminu4(D, um1);
+                const uint32_t d16 = (dc & 0xfu) | ((dc >> 4) & 0xf0u) | ((dc >> 8) & 0xf00u) | ((dc >> 12) & 0xf000u);
+                s_key[at] = (d16 << 9) | (uint32_t)at;
+            }
+            n_live += __popc(lm);
+        }
+        __syncwarp();
+        // rank of each group by its key (keys are distinct)
+        for (int i = lane; i < n_live; i += 32) {
+            const uint32_t ki = s_key[i];
+            int rank = 0;
+            for (int j = 0; j < n_live; j++) rank += s_key[j] < ki ? 1 : 0;
+            s_ord[rank] = (uint16_t)i;
+        }
+        __syncwarp();
+        // The largest box depends on the counts through the clamped ones
+        // alone (pair_vmax takes min(U_t, D + 1) = min(U_t, D' + 1)), so it
+        // is computed once per run of equal clamped counts in key order, by
+        // the run's first group, and the pass list follows from it.
         int tot[NL];
 #pragma unroll
         for (int k = 0; k < NL; k++) tot[k] = 0;
-        int n_live = 0;  // routed groups so far (warp-uniform)
-        for (int u0 = 0; u0 < n_grp && !read_empty; u0 += 32) {
-            const int u = u0 + lane;
-            int dest = -1;  // -1: empty pairs; -2: no shape holds them (P = 0, err = 2)
-            int vm = 0, cnt = 0;
-            if (u < n_grp) {
-                const uint32_t D = gD[u];
-                // every byte D_c >= L_0,c (bytes below 128: bit 7 of (D | 0x80..) -
-                // L0 stays set exactly where D_c >= L_0,c; bytes past the channels are 0)
-                if (((((D | 0x80808080u) - L0) & 0x80808080u) == 0x80808080u)) {
-                    vm = pair_vmax_w(C, T, sL[wid], sU[wid], D);
-                    cnt = gstart[u + 1] - gstart[u];
-                    dest = 0;
-                    if (a.n_tiers > 0) {
-                        dest = WP_MAX_TIERS;
-                        for (int k = a.n_tiers - 1; k >= 0; k--)
-                            if (vm <= a.tier_half[k]) dest = k;
-                        if (dest == WP_MAX_TIERS && !a.route_dense) dest = -2;
-                    }
+        int carry = 0;  // the last run's box size (warp-uniform)
+        for (int o0 = 0; o0 < n_live; o0 += 32) {
+            const int o = o0 + lane;
+            int i = 0;
+            bool start = false;
+            uint32_t dk = 0;
+            if (o < n_live) {
+                i = s_ord[o];
+                dk = s_key[i] >> 9;
+                start = o == 0 || (s_key[s_ord[o - 1]] >> 9) != dk;
+            }
+            int vm = 0;
+            if (start) {
+                const uint32_t Dw = (dk & 0xfu) | ((dk & 0xf0u) << 4) | ((dk & 0xf00u) << 8) | ((dk & 0xf000u) << 12);
+                vm = pair_vmax_w(C, T, sL[wid], sU[wid], Dw);
+            }
+            // each lane takes the box size of the nearest run start at or
+            // before it (an earlier chunk's: carry)
+            const unsigned sm = __ballot_sync(0xffffffffu, start);
+            const unsigned before = sm & (0xffffffffu >> (31 - lane));
+            const int src = before ? 31 - __clz(before) : 0;
+            const int vs = __shfl_sync(0xffffffffu, vm, src);
+            if (o < n_live) {
+                const int v = before ? vs : carry;
+                const int u = s_live[wid][i];
+                int dest = 0;  // -2: no shape holds these pairs (P = 0, err = 2)
+                if (a.n_tiers > 0) {
+                    dest = WP_MAX_TIERS;
+                    for (int k = a.n_tiers - 1; k >= 0; k--)
+                        if (v <= a.tier_half[k]) dest = k;
+                    if (dest == WP_MAX_TIERS && !a.route_dense) dest = -2;
                 }
-            }
-            if (dest == -2) atomicExch(a.err, 2);  // no shape holds this pair
-            const unsigned lm = __ballot_sync(0xffffffffu, dest != -1);
-            if (dest != -1) {
-                const int at = n_live + __popc(lm & ((1u << lane) - 1));
-                s_live[wid][at] = (uint16_t)u;
-                s_vm[wid][at] = (uint16_t)min(vm, 65535);
-                s_dest[wid][at] = (uint8_t)(dest < 0 ? 0xffu : dest);
-                // sort key: list, clamped counts (4 bits a channel), position
-                const uint32_t dc = __vminu4(gD[u], um1);
-                const uint32_t d16 = (dc & 0xfu) | ((dc >> 4) & 0xf0u) | ((dc >> 8) & 0xf00u) | ((dc >> 12) & 0xf000u);
-                s_key[at] = ((uint32_t)(dest < 0 ? 7 : dest) << 25) | (d16 << 9) | (uint32_t)at;
-            }
-            n_live += __popc(lm);
+                if (dest == -2) atomicExch(a.err, 2);
+                s_vm[wid][i] = (uint16_t)min(v, 65535);
+                s_dest[wid][i] = (uint8_t)(dest < 0 ? 0xffu : dest);
+                const int cnt = gstart[u + 1] - gstart[u];
 #pragma unroll
-            for (int k = 0; k < NL; k++)
-                if (dest == k) tot[k] += cnt;
+                for (int k = 0; k < NL; k++)
+                    if (dest == k) tot[k] += cnt;
+            }
+            const int last = min(31, n_live - 1 - o0);  // the chunk's last position's lane
+            const unsigned lb = sm & (0xffffffffu >> (31 - last));
+            const int vl = __shfl_sync(0xffffffffu, vm, lb ? 31 - __clz(lb) : 0);
+            if (lb) carry = vl;
         }
         // each list's range for this read: lane k takes list k's atomic
         int base[NL];
@@ -663,14 +706,6 @@ __global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(
 #pragma unroll
         for (int k = 0; k < NL; k++) base[k] = __shfl_sync(0xffffffffu, b, k);
         if (lane == 0 && a.live_count && live_pairs) atomicAdd(a.live_count, live_pairs);
-        __syncwarp();
-        // rank of each routed group by its key (keys are distinct)
-        for (int i = lane; i < n_live; i += 32) {
-            const uint32_t ki = s_key[i];
-            int rank = 0;
-            for (int j = 0; j < n_live; j++) rank += s_key[j] < ki ? 1 : 0;
-            s_ord[rank] = (uint16_t)i;
-        }
         __syncwarp();
         // the appends, group by group in key order
         const long gr = (long)r * a.P;
