@@ -184,18 +184,41 @@ __device__ __noinline__ void binomial_step(const V* __restrict__ src, V* __restr
                 const int from = from0 + k;
                 cf[k] = (k < win && from >= to) ? tab[from * (from + 1) / 2 + to] : 0.0f;
             }
-            for (int o = 0; o < outer; o++) {
-                const V* s = src + o * win * sk;
-                V* d = dst + (o * wout + k2) * sk;
-                for (int i = 0; i < inner; i++) {
-                    const V* si = s + i * stride;
-                    V acc = vmul(cf[0], si[0]);
-                    if (win > 1) acc = vfma(cf[1], si[sk], acc);
-                    if (win > 2) acc = vfma(cf[2], si[2 * sk], acc);
-                    if (win > 3) acc = vfma(cf[3], si[3 * sk], acc);
-                    d[i * stride] = acc;
+            // the columns as one sequence, two at a time (as above)
+            const int n = outer * inner;
+            const int ostep_in = win * sk - inner * stride, ostep_out = wout * sk - inner * stride;
+            const V* si = src;
+            V* di = dst + k2 * sk;
+            int i = 0;
+            auto next = [&]() {
+                si += stride;
+                di += stride;
+                if (++i == inner) {
+                    i = 0;
+                    si += ostep_in;
+                    di += ostep_out;
                 }
+            };
+            auto dot = [&](const V* x) {
+                V acc = vmul(cf[0], x[0]);
+                if (win > 1) acc = vfma(cf[1], x[sk], acc);
+                if (win > 2) acc = vfma(cf[2], x[2 * sk], acc);
+                if (win > 3) acc = vfma(cf[3], x[3 * sk], acc);
+                return acc;
+            };
+            int q = 0;
+            for (; q + 1 < n; q += 2) {
+                const V* sa = si;
+                V* da = di;
+                next();
+                const V* sb = si;
+                V* db = di;
+                next();
+                const V ra = dot(sa), rb = dot(sb);
+                *da = ra;
+                *db = rb;
             }
+            if (q < n) *di = dot(si);
         }
         return;
     }
