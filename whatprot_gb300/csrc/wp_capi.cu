@@ -1870,7 +1870,7 @@ wp_status wp_autotune(wp_ctx* ctx, const double* rads, int R, double dist_cutoff
                 ctx->force_cfg = true;
                 double ms_best_c = 1e300;
                 bool ok = true;
-                for (int rep = 0; rep < 3 && ok; rep++) {  // first run warms up
+                for (int rep = 0; rep < 5 && ok; rep++) {  // first run warms up; best of four
                     cudaEventRecord(e0, ctx->stream);
                     if (run_batch(ctx, ctx->d_rads.as<double>(), R, dist_cutoff, nullptr, nullptr, MODE_CLASSIFY,
                                   nullptr, ctx->d_out_id.as<int>(), ctx->d_out_score.as<double>(),
