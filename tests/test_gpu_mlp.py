@@ -4,8 +4,10 @@ GPU's rounding points), and what training gains.
 
 Tolerance: the oracle rounds to BF16 where the GPU does, so only the
 tensor cores' FP32 summation order differs (and the BF16 roundings it can
-tip): logits within 1e-3 of the largest logit magnitude, each gradient
-within 2 % relative Frobenius error and a cosine similarity above 0.9995."""
+tip): loss within 1e-4 relative, logits within 3e-4 of the largest logit
+magnitude, each gradient within 1e-3 relative Frobenius error and a cosine
+similarity above 0.99999 (measured on three seeds: loss 2e-6, logits up to
+9e-5, gradients up to 1e-4, cosines 1 - 1e-8)."""
 import os
 import sys
 
@@ -42,14 +44,14 @@ def test_gradients_match_oracle():
         d_y = torch.from_numpy(pep.astype(np.int32)).cuda()
         loss = net.train_step(d_x.data_ptr(), d_y.data_ptr(), B, 0.0)
         ora_loss, g, L = mlp_oracle.gradients(params, x.astype(np.float64), pep, len(ds))
-        assert abs(loss - ora_loss) <= 1e-3 * max(1.0, abs(ora_loss))
+        assert abs(loss - ora_loss) <= 1e-4 * max(1.0, abs(ora_loss))
         logits = net.logits(rads)
-        assert np.max(np.abs(logits - L[:, :len(ds)])) <= 1e-3 * np.max(np.abs(L))
+        assert np.max(np.abs(logits - L[:, :len(ds)])) <= 3e-4 * np.max(np.abs(L))
         for i, n in enumerate(capi.ProposalNet.PARAMS):
             gg = net.get(i, grad=True).astype(np.float64).reshape(g[n].shape)
             rel = np.linalg.norm(gg - g[n]) / max(np.linalg.norm(g[n]), 1e-30)
             cos = float(np.sum(gg * g[n]) / max(np.linalg.norm(gg) * np.linalg.norm(g[n]), 1e-30))
-            assert rel <= 0.02 and cos >= 0.9995, (n, rel, cos)
+            assert rel <= 1e-3 and cos >= 0.99999, (n, rel, cos)
         net.close()
     finally:
         ctx.close()
