@@ -617,9 +617,6 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
         return 0.0f;
     }
     *kmax_out = kmax;
-    float w0 = sf;
-#pragma unroll
-    for (int c = 0; c < C; c++) w0 *= g[c][0];
     if (allow_t) {
         float em0 = 1.0f;
 #pragma unroll
@@ -641,27 +638,22 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
     const int vn = bvol<C>(nx.w);
     const int sb = vb * stride, sn = vn * stride;
     float part = 0.0f;
+    // The box's states in row-major order, as an odometer over the
+    // channels: the state's index in the bleached box (ib), its packed
+    // counts with the one-dye-up bits (X), and the prefix products of its
+    // emission factors (pre[c] = sf g[0][k_0] ... g[c][k_c], the order of
+    // w0's product) are updated as the odometer turns.
     int jc[C];
+    float pre[C];
 #pragma unroll
-    for (int c = 0; c < C; c++) jc[c] = 0;
+    for (int c = 0; c < C; c++) {
+        jc[c] = 0;
+        pre[c] = (c == 0 ? sf : pre[c > 0 ? c - 1 : 0]) * g[c][0];
+    }
+    int ib = 0;
+    uint32_t X = nx.lo | up0;
     for (int j = 0; j < vn; j++) {
-        int ib = 0;
-        // byte c: the state's dye count in channel c, bit 7 set when the
-        // state one dye up in c lies in the bleached box
-        uint32_t X = nx.lo | up0;
-        float w = w0;
-        if (j > 0) {
-            X = nx.lo;
-            w = sf;
-#pragma unroll
-            for (int c = 0; c < C; c++) {
-                const int k = jc[c];
-                ib += k * bget(stpk, c);
-                X += (uint32_t)k << (8 * c);
-                if (k + 1 < bget(bx.w, c)) X |= 0x80u << (8 * c);
-                w *= k == 0 ? g[c][0] : k == 1 ? g[c][1] : k == 2 ? g[c][2] : g[c][3];
-            }
-        }
+        const float w = pre[C - 1];
         const V* cs = cur + ib * stride;  // slice e - 1 of the state's column
         V* out = nxt + j * stride;
         // Edman success into slice e from slice e - 1 (value prev, column
@@ -758,10 +750,32 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
             part += vtotal(sv);
         }
         if (j + 1 < vn) {
+            bool carry = true;
 #pragma unroll
             for (int c = C - 1; c >= 0; c--) {
-                if (++jc[c] < bget(nx.w, c)) break;
-                jc[c] = 0;
+                if (carry) {
+                    const int st_c = bget(stpk, c);
+                    const int k = jc[c] + 1;
+                    if (k < bget(nx.w, c)) {
+                        jc[c] = k;
+                        ib += st_c;
+                        X += 1u << (8 * c);
+                        if (k + 1 >= bget(bx.w, c)) X &= ~(0x80u << (8 * c));
+                        carry = false;
+                    } else {
+                        // channel c back to its first count (its one-up bit
+                        // as for the box's first state)
+                        ib -= jc[c] * st_c;
+                        X = (X - ((uint32_t)jc[c] << (8 * c))) | (up0 & (0x80u << (8 * c)));
+                        jc[c] = 0;
+                    }
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < C; c++) {
+                const int k = jc[c];
+                pre[c] = (c == 0 ? sf : pre[c > 0 ? c - 1 : 0]) *
+                         (k == 0 ? g[c][0] : k == 1 ? g[c][1] : k == 2 ? g[c][2] : g[c][3]);
             }
         }
     }
@@ -870,6 +884,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
     int expo = 0;           // the true state is the stored state times 2^expo
     float pd = 0.0f;        // detached state, in the rescaled frame
     int k_prev = 0;         // exponent removed at the last rescale
+    float scale_prev = 1.0f;  // 2^-k_prev (exp2i clamps at 2^127 as the multiplier did)
     float fac_prev = 1.0f;  // (1 - p_detach) pending from the last timestep
     // Closes timestep t after its emission multiply: the detached state
     // (kept only while the box includes zero, peptide-emission.cc:218-223),
@@ -905,6 +920,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
         // p_detached += p * sum of the states
         pd = (pd + M.p_det[t] * part) * f;
         k_prev = k;
+        scale_prev = f;
         fac_prev = 1.0f - M.p_det[t];
         return false;
     };
@@ -994,7 +1010,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             fused = pk && narrow && (C <= 3 || bvol<C>(bx.w) <= 255);
             if (fused) {
                 part = edman_emit<C, HB>(cur, nxt, stride, t, bx, nx, codes, M.edx, M.edy, pf, re, gk, one,
-                                         allow_t, fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
+                                         allow_t, fac_prev * bscale * scale_prev, &kmax, &em0);
                 if (kmax == WP_EXPO_ZERO) {
                     *out_mant = 0.0f;
                     *out_expo = 0;
@@ -1015,7 +1031,7 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
             // edman_emit applied the emission
         } else if (narrow) {
             part = emission_narrow<C, V>(cur, stride, t, nx, re, gk, one, allow_t,
-                                         fac_prev * bscale * exp2i(min(-k_prev, 127)), &kmax, &em0);
+                                         fac_prev * bscale * scale_prev, &kmax, &em0);
             if (kmax == WP_EXPO_ZERO) {
                 *out_mant = 0.0f;
                 *out_expo = 0;
