@@ -3,9 +3,10 @@
 //   wp_prep_reads_kernel    one thread per (read, timestep): the emission
 //                           pruning box [cmin, cmax) of the reference's
 //                           PeptideEmission (hmm/step/peptide-emission.cc:
-//                           50-163) and the emission factors, computed in FP64
-//                           as the reference does and stored as (FP32
-//                           mantissa, int exponent).
+//                           50-163), in FP64 as the reference computes it,
+//                           and the emission factors, stored as (FP32
+//                           mantissa, int exponent) of norm * 2^y with y in
+//                           FP64 (the FP64 exp only in the far tails).
 //   wp_read_summary_kernel  one thread per read: the closed-form pruning boxes
 //                           every pair of the read shares, L_t = max_{t'>=t}
 //                           cmin_{t'} and min_{t'<=t} cmax_{t'}, the
@@ -14,12 +15,19 @@
 //   wp_window_factors_kernel  one thread per (read, timestep): the emission
 //                           factors normalised over the pruning window, for
 //                           the engine (non-interacting models).
-//   wp_compact_kernel       one CTA per read: pairs whose pruned range is
-//                           empty get probability 0 (PeptideHMM::probability,
+//   wp_compact_kernel       one CTA per read (candidate lists, loglik):
+//                           pairs whose pruned range is empty get
+//                           probability 0 (PeptideHMM::probability,
 //                           hmm/hmm/peptide-hmm.cc:94-100); the others are
 //                           appended to the work list of the first engine
 //                           pass whose per-thread slab holds their largest
 //                           box (pair_vmax), or to the dense kernel's list.
+//   wp_compact_groups_kernel  the same for classify over all peptides, one
+//                           warp per read and one decision per group of
+//                           peptides with one dye-count vector, the groups
+//                           appended in the order of their counts clamped to
+//                           the read's bounds (pairs that take the same
+//                           steps side by side); empty pairs get no write.
 //
 // Pruning.  After the reference's forward and backward prune passes
 // (hmm/hmm/peptide-hmm.cc:63-83) the box of emission t of a pair is
