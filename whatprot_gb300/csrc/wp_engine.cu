@@ -28,14 +28,18 @@
 // for the instruction cache.
 //
 // Two shortcuts follow from the box statistics of real workloads, where
-// most timesteps of most pairs have a one-state emission box: a dud or
-// bleach step along a channel that is one wide on both sides is a single
-// coefficient, carried to the next emission multiply instead of a pass over
-// the state (checked for all channels at once with word operations); and
-// Edman and emission run as one loop, state outer and Edman slice inner,
-// for every emission box at most 4 wide per channel, one-state boxes
-// included.  Edman coefficients come from a per-CTA table indexed by
-// (remaining dyes of the cut channel, dye count of the state).
+// most timesteps of most pairs have a one-state emission box: a bleach step
+// along a channel that is one wide on both sides is a single coefficient,
+// carried to the next emission multiply instead of a pass over the state
+// (checked for all channels at once with word operations); and Edman and
+// emission run as one loop, state outer and Edman slice inner (two slices
+// at a time), for every emission box at most 4 wide per channel, one-state
+// boxes included.  The start state goes through the duds as one product per
+// state, written straight into the first emission box.  Edman coefficients
+// come from per-CTA tables indexed by (dye count of the state, remaining
+// dyes of the cut channel); each position's (cut channel, remaining dyes)
+// is a code byte in the thread's slice of shared memory, and one byte
+// permute of the state's packed counts picks the count it needs.
 // All lanes of a warp process the same timestep together (lanes are pairs
 // of one read), so a warp pays for every path any of its lanes takes in a
 // timestep; the number of distinct paths is kept small for that reason.  A
