@@ -1036,7 +1036,9 @@ wp_status nn_replay(wp_ctx* ctx, const double* d_rads, int R, long long k) {
     int dev_smem = 0;
     cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
     if (smem > (size_t)dev_smem) return fail(ctx, WP_ERR_UNSUPPORTED, "kd-tree kNN: per-read tables exceed shared memory");
-    const int per_sm = std::max(1, std::min(4, (int)((size_t)dev_smem / smem)));
+    // as many CTAs per SM as its shared memory holds (each warp walks one read
+    // at a time, latency-bound: residency is what speeds it up)
+    const int per_sm = std::max(1, std::min(8, (int)((size_t)(228 * 1024) / (smem + 1024))));
     const int ch = wp_kbest_chunk();
     std::vector<int> redo;
     for (int round = 0; round < 3; round++) {
@@ -1047,7 +1049,10 @@ wp_status nn_replay(wp_ctx* ctx, const double* d_rads, int R, long long k) {
         a.regcap = (int)(((2 * stage + 2048ll * ch) + ch - 1) / ch * ch);
         if (a.regcap / ch > 65535) a.regcap = 65535 * ch;
         int grid = sms * per_sm;
-        if (round > 0) grid = std::max(1, std::min(grid, ((int)redo.size() + 3) / 4));
+        if (round > 0) {
+            const int wpc = wp_kbest_warps_per_cta();
+            grid = std::max(1, std::min(grid, ((int)redo.size() + wpc - 1) / wpc));
+        }
         const long warps = (long)grid * wp_kbest_warps_per_cta();
         WP_CUDA(ctx->d_kb_reg.ensure(sizeof(KBItem) * 2 * (size_t)a.regcap * warps), "alloc kNN replay scratch");
         WP_CUDA(ctx->d_kb_prev.ensure(sizeof(int) * 2 * (size_t)(a.regcap / ch) * warps), "alloc kNN replay scratch");

@@ -47,10 +47,10 @@
 
 #define KB_B 2048      // buckets
 #define KB_CH 16       // entries per chunk
-#define KB_CUR 512     // capacity of the current bucket
+#define KB_CUR 256     // capacity of the current bucket
 #define KB_SHDEF 44    // bucket = FP64 bits >> 44: exponent and 8 mantissa bits
 #define KB_SHMIN 20    // narrowest buckets a refinement may reach
-#define KB_WARPS 4     // warps per CTA
+#define KB_WARPS 2     // warps per CTA
 
 // Per-warp shared memory (fixed part).
 struct KBSmem {
