@@ -80,6 +80,14 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
     if (by_shape) {
         L0 = a.Lpk[(long)r * a.model->T] & 0x7f7f7f7fu;
         read_empty = a.flags[r] != 0;
+        // every empty pair has P = 0 and the first slot wins among zeros,
+        // so empty slots need no look: the first slot stands for them
+        if (g1 > g0) {
+            best.mant = 0.0f;
+            best.expo = 0;
+            best.key = 0;
+            best.idx = g0;
+        }
     }
     int El = INT_MIN;  // the lane's reference exponent (none yet)
     float hi = 0.0f, lo = 0.0f;
@@ -106,6 +114,8 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
                     mv[u] = a.res_mant[g];
                     ev[u] = a.res_expo[g];
                     cv[u] = a.counts[p];
+                } else {
+                    cv[u] = -1;  // empty pair: nothing to take
                 }
             }
         }
@@ -113,6 +123,7 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
         for (int u = 0; u < 4; u++) {
             const int g = gb + 32 * u;
             if (g >= g1) break;
+            if (cv[u] < 0) continue;
             const float mm = mv[u];
             const int ex = ev[u];
             Cand c = {mm, ex, g - g0, g};
