@@ -286,7 +286,7 @@ struct wp_ctx {
     DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_Lpk, d_Upk, d_allow, d_flags, d_table, d_gtab, d_gdelta, d_gK,
             d_gone,
             d_res_mant, d_res_expo,
-            d_work, d_ovf1, d_ovf2, d_ovf3, d_ovf4, d_counters, d_cand, d_slot_off, d_out_id, d_out_score,
+            d_work, d_ovf1, d_ovf2, d_ovf3, d_ovf4, d_ovf5, d_counters, d_cand, d_slot_off, d_out_id, d_out_score,
             d_out_total, d_out_log, d_logp, d_flops, d_err;
 };
 
@@ -632,10 +632,11 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
     WP_CUDA(ctx->d_ovf2.ensure(sizeof(int2) * ns), "alloc work list");
     WP_CUDA(ctx->d_ovf3.ensure(sizeof(int2) * ns), "alloc work list");
     WP_CUDA(ctx->d_ovf4.ensure(sizeof(int2) * ns), "alloc work list");
-    // counters: [2k, 2k + 1] list count / head of engine pass k (k < 4),
-    // [8, 9] the dense kernel's, [10] non-empty pairs
-    WP_CUDA(ctx->d_counters.ensure(sizeof(int) * 12), "alloc counters");
-    WP_CUDA(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(int) * 12, ctx->stream), "clear counters");
+    WP_CUDA(ctx->d_ovf5.ensure(sizeof(int2) * ns), "alloc work list");
+    // counters (WP_CNT_*): list count / head per engine pass, the dense
+    // kernel's, the non-empty pairs
+    WP_CUDA(ctx->d_counters.ensure(sizeof(int) * WP_CNT_N), "alloc counters");
+    WP_CUDA(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(int) * WP_CNT_N, ctx->stream), "clear counters");
     int* cnt = ctx->d_counters.as<int>();
     a.res_mant = ctx->d_res_mant.as<float>();
     a.res_expo = ctx->d_res_expo.as<int>();
@@ -643,8 +644,8 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
     a.work_count = cnt + 0;
     a.work_head = cnt + 1;
     a.ovf = ctx->d_ovf2.as<int2>();
-    a.ovf_count = cnt + 8;
-    a.ovf_head = cnt + 9;
+    a.ovf_count = cnt + WP_CNT_DENSE;
+    a.ovf_head = cnt + WP_CNT_DENSE + 1;
     a.dense_S_cap = ((ctx->S_max + 31) / 32) * 32;
     if (n_slots > 0) {
         // Dense fallback shape: as many warps as fit (0: unavailable).
@@ -664,8 +665,10 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
             return fail(ctx, WP_ERR_UNSUPPORTED, "shared memory too small for the pair engine");
         // Engine passes ("tiers") in order of growing slab: pass 1, a middle
         // pass of 3 CTAs of 128 threads per SM for the pairs just too large
-        // for pass 1, the last configured pass, and a pass of one CTA of 128
-        // threads per SM for what is left short of the dense kernel.
+        // for pass 1, the last configured pass, and passes of one CTA of 128
+        // and of 64 threads per SM for what is left short of the dense
+        // kernel (one thread per pair stays faster than the dense kernel's
+        // warp over every state while the box fits).
         struct Tier {
             int threads, per_sm, half;
         };
@@ -677,7 +680,9 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         if (half2 > tiers[nt - 1].half) tiers[nt++] = {cfg.t2, cfg.s2, half2};
         const int hbig = slab_half_for(ctx, 128, 1, hb);
         if (hbig > tiers[nt - 1].half) tiers[nt++] = {128, 1, hbig};
-        DevBuf* lists[WP_MAX_TIERS] = {&ctx->d_work, &ctx->d_ovf1, &ctx->d_ovf3, &ctx->d_ovf4};
+        const int hhuge = slab_half_for(ctx, 64, 1, hb);
+        if (hhuge > tiers[nt - 1].half) tiers[nt++] = {64, 1, hhuge};
+        DevBuf* lists[WP_MAX_TIERS] = {&ctx->d_work, &ctx->d_ovf1, &ctx->d_ovf3, &ctx->d_ovf4, &ctx->d_ovf5};
         // the compaction sends each pair to the first pass whose slab holds it
         a.n_tiers = nt;
         for (int k = 0; k < nt; k++) {
@@ -686,7 +691,7 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
             a.tier_count[k] = cnt + 2 * k;
         }
         a.route_dense = dense_warps > 0 ? 1 : 0;
-        a.live_count = cnt + 10;
+        a.live_count = cnt + WP_CNT_LIVE;
         {
             TimedLaunch tl(ctx, 1);
             if (a.dead_by_shape) {
@@ -715,7 +720,7 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
             WP_CUDA(wp_launch_engine(C, hb, tiers[k].threads, smem, ctx->stream, a, lists[k]->as<int2>(),
                                      cnt + 2 * k, cnt + 2 * k + 1,
                                      last ? ctx->d_ovf2.as<int2>() : lists[k + 1]->as<int2>(),
-                                     last ? cnt + 8 : cnt + 2 * (k + 1), tiers[k].half, 0,
+                                     last ? cnt + WP_CNT_DENSE : cnt + 2 * (k + 1), tiers[k].half, 0,
                                      last && dense_warps == 0 ? 1 : 0, k == 0 ? &ctx->last_engine_grid : nullptr),
                     "engine pass");
             ctx->launches++;
@@ -1536,15 +1541,16 @@ wp_status wp_last_batch_stats(wp_ctx* ctx, long long* stats) {
     if (!ctx || !stats) return WP_ERR_INVALID;
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
-    int c[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int c[WP_CNT_N] = {0};
     if (ctx->d_counters.p) {
         WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
         WP_CUDA(cudaMemcpy(c, ctx->d_counters.p, sizeof(c), cudaMemcpyDeviceToHost), "read counters");
     }
     stats[0] = ctx->last_slots;
-    stats[1] = c[10];
-    stats[2] = c[2] + c[4] + c[6];
-    stats[3] = c[8];
+    stats[1] = c[WP_CNT_LIVE];
+    stats[2] = 0;
+    for (int k = 1; k < WP_MAX_TIERS; k++) stats[2] += c[2 * k];
+    stats[3] = c[WP_CNT_DENSE];
     return WP_OK;
 }
 
@@ -1589,13 +1595,13 @@ wp_status wp_engine_replay(wp_ctx* ctx, int reps, double* ms) {
         // heads go back to the start
         for (int k = 0; k < rp.nt; k++)
             WP_CUDA(cudaMemsetAsync(rp.cnt + 2 * k + 1, 0, sizeof(int), ctx->stream), "reset head");
-        WP_CUDA(cudaMemsetAsync(rp.cnt + 9, 0, sizeof(int), ctx->stream), "reset head");
+        WP_CUDA(cudaMemsetAsync(rp.cnt + WP_CNT_DENSE + 1, 0, sizeof(int), ctx->stream), "reset head");
         for (int k = 0; k < rp.nt; k++) {
             const bool last = k + 1 == rp.nt;
             size_t smem = wp_engine_smem_bytes(rp.half[k], 0, rp.hb, rp.threads[k]);
             WP_CUDA(wp_launch_engine(rp.C, rp.hb, rp.threads[k], smem, ctx->stream, a, rp.list[k], rp.cnt + 2 * k,
                                      rp.cnt + 2 * k + 1, last ? rp.a.ovf : rp.list[k + 1],
-                                     last ? rp.cnt + 8 : rp.cnt + 2 * (k + 1), rp.half[k], 0, 1, nullptr),
+                                     last ? rp.cnt + WP_CNT_DENSE : rp.cnt + 2 * (k + 1), rp.half[k], 0, 1, nullptr),
                     "engine pass");
             ctx->launches++;
         }

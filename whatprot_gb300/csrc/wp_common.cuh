@@ -21,7 +21,12 @@
 
 #define WP_W (WP_MAX_DYES_PER_CHANNEL + 1)      // extent cap per channel
 #define WP_TRI (WP_W * (WP_W + 1) / 2)          // triangular table size
-#define WP_MAX_TIERS 4                          // engine passes the compaction routes to
+#define WP_MAX_TIERS 5                          // engine passes the compaction routes to
+// Batch counters: [2k, 2k + 1] list count / head of engine pass k, then the
+// dense kernel's count / head, then the non-empty pairs.
+#define WP_CNT_DENSE (2 * WP_MAX_TIERS)
+#define WP_CNT_LIVE (2 * WP_MAX_TIERS + 2)
+#define WP_CNT_N (2 * WP_MAX_TIERS + 3)
 #define WP_GROUP_WARPS 8      // warps per CTA of wp_compact_groups_kernel (one read at a time each)
 #define WP_GROUP_MAX 512      // dye-count vectors (groups) that kernel takes
 #define WP_GROUP_PERM_SMEM 8192  // peptides up to which it stages the shape order in shared memory
