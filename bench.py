@@ -1464,7 +1464,7 @@ def main():
     elif args.no_autotune:  # default shapes (used for short profiling runs)
         tuned_cfg, tuned_ms = (256, 2, 256, 1), None
     else:
-        tuned_cfg, tuned_ms = ctx.autotune(rads[:min(R, 20000)], CUTOFF)
+        tuned_cfg, tuned_ms = ctx.autotune(rads[:min(R, 50000)], CUTOFF)
     for _ in range(args.warmup):  # the second call captures the CUDA graph
         step_device()
     torch.cuda.synchronize()
