@@ -1553,7 +1553,7 @@ def main():
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if (achieved and peak) else None, "traffic": traffic,
                 "traffic_source": traffic_src, "traffic_ncu": traffic_ncu, "traffic_ncu_source": ncu_src,
-                "kernel": "wp_engine_kernel (passes 1-4) + wp_dense_kernel",
+                "kernel": "wp_engine_kernel (passes 1-5) + wp_dense_kernel",
                 "peak_source": "FP32 FMA loop measured live (wp_probe_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                 "algorithmic_flops_per_step": algo_flops,
                 "unpruned_flops_per_step": float(R) * unpruned_forward_flops(ds.seqs, T, C),
