@@ -1539,11 +1539,11 @@ def main():
     flops_per_launch = algo_flops * split_steps / max(fwd_n, 1)
     achieved = flops_per_launch / (fwd_avg_ms * 1e-3) / 1e12 if fwd_n else None
     # DRAM traffic of the engine passes from one ncu capture of a 5,000-read
-    # batch of this workload (38.3 + 3.85 + 2.69 + 0.62 MB over its four
-    # passes), scaled by the reads (the traffic is per pair) and spread over
-    # this step's forward launches
+    # batch of this workload (38.1 + 3.85 + 2.69 + 0.62 + 0.10 MB over its
+    # five passes), scaled by the reads (the traffic is per pair) and spread
+    # over this step's forward launches
     launches_per_step = fwd_n / split_steps if fwd_n else 0.0
-    traffic_ncu = (45.5e6 * R / 5000.0) / launches_per_step if launches_per_step else None
+    traffic_ncu = (45.4e6 * R / 5000.0) / launches_per_step if launches_per_step else None
     ncu_src = ("ncu dram__bytes_read+write of the engine passes at 5,000 reads, scaled to this batch by reads, "
                "per forward launch")
     if live_bytes is not None and launches_per_step:
