@@ -215,7 +215,7 @@ struct wp_ctx {
     std::vector<PeptideRec> recs;
     DevBuf d_peps, d_ids, d_counts, d_perm, d_shape_rank, d_uniq_D, d_pep_u;
     int n_uniq_D = 0;
-    DevBuf d_grp_start, d_grp_D, d_pep_Dw;  // runs of perm with one dye-count vector
+    DevBuf d_grp_start, d_grp_D;  // runs of perm with one dye-count vector
     int n_grp = 0;
 
     // Kernel timing.
@@ -285,7 +285,7 @@ struct wp_ctx {
     // Per-batch scratch.
     DevBuf d_rads, d_lo, d_hi, d_Ls, d_Up, d_Lpk, d_Upk, d_allow, d_flags, d_table, d_gtab, d_gdelta, d_gK,
             d_gone,
-            d_res_mant, d_res_expo,
+            d_res_mant, d_res_expo, d_pair_info, d_rd,
             d_work, d_ovf1, d_ovf2, d_ovf3, d_ovf4, d_ovf5, d_counters, d_cand, d_slot_off, d_out_id, d_out_score,
             d_out_total, d_out_log, d_logp, d_flops, d_err;
 };
@@ -451,14 +451,10 @@ wp_status plan_peptides(wp_ctx* ctx) {
         ctx->n_grp = (int)gd.size();
         WP_CUDA(ctx->d_grp_start.ensure(sizeof(int) * gs.size()), "alloc groups");
         WP_CUDA(ctx->d_grp_D.ensure(sizeof(uint32_t) * std::max<size_t>(gd.size(), 1)), "alloc groups");
-        WP_CUDA(ctx->d_pep_Dw.ensure(sizeof(uint32_t) * std::max(P, 1)), "alloc groups");
         WP_CUDA(cudaMemcpyAsync(ctx->d_grp_start.p, gs.data(), sizeof(int) * gs.size(), cudaMemcpyHostToDevice,
                                 ctx->stream), "copy groups");
         if (!gd.empty())
             WP_CUDA(cudaMemcpyAsync(ctx->d_grp_D.p, gd.data(), sizeof(uint32_t) * gd.size(), cudaMemcpyHostToDevice,
-                                    ctx->stream), "copy groups");
-        if (P > 0)
-            WP_CUDA(cudaMemcpyAsync(ctx->d_pep_Dw.p, pdw.data(), sizeof(uint32_t) * P, cudaMemcpyHostToDevice,
                                     ctx->stream), "copy groups");
         WP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
     }
@@ -613,20 +609,26 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
     a.uniq_D = ctx->d_uniq_D.as<uint32_t>();
     a.pep_u = ctx->d_pep_u.as<int>();
     a.n_uniq = ctx->n_uniq_D;
-    // Classify over all peptides: the compaction works per group of
-    // peptides with one dye-count vector and writes nothing for empty pairs
-    // (the reduce tells them by their vector); loglik keeps every slot written.
-    if (mode == MODE_CLASSIFY && !a.cand && ctx->n_grp <= WP_GROUP_MAX) {
-        a.grp_start = ctx->d_grp_start.as<int>();
-        a.grp_D = ctx->d_grp_D.as<uint32_t>();
-        a.n_grp = ctx->n_grp;
-        a.pep_Dw = ctx->d_pep_Dw.as<uint32_t>();
-        a.dead_by_shape = 1;
-    }
     ctx->last_slots = n_slots;
     const size_t ns = (size_t)std::max<long>(n_slots, 1);
     WP_CUDA(ctx->d_res_mant.ensure(sizeof(float) * ns), "alloc results");
     WP_CUDA(ctx->d_res_expo.ensure(sizeof(int) * ns), "alloc results");
+    // Classify over all peptides: the compaction works per group of
+    // peptides with one dye-count vector and gives only non-empty pairs a
+    // result index (BatchArgs::pair_info); loglik keeps one per slot.
+    const bool groups = mode == MODE_CLASSIFY && !a.cand && ctx->n_grp <= WP_GROUP_MAX;
+    if (groups) {
+        a.grp_start = ctx->d_grp_start.as<int>();
+        a.grp_D = ctx->d_grp_D.as<uint32_t>();
+        a.n_grp = ctx->n_grp;
+        WP_CUDA(ctx->d_pair_info.ensure(sizeof(int2) * ns), "alloc results");
+        WP_CUDA(ctx->d_rd.ensure(sizeof(int) * 2 * (size_t)std::max(R, 1)), "alloc results");
+        a.pair_info = ctx->d_pair_info.as<int2>();
+        a.rd_base = ctx->d_rd.as<int>();
+        a.rd_n = a.rd_base + R;
+        // every read's range is written by the compaction; with no slots
+        // the reduce reads none
+    }
     WP_CUDA(ctx->d_work.ensure(sizeof(int2) * ns), "alloc work list");
     WP_CUDA(ctx->d_ovf1.ensure(sizeof(int2) * ns), "alloc work list");
     WP_CUDA(ctx->d_ovf2.ensure(sizeof(int2) * ns), "alloc work list");
@@ -694,7 +696,7 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         a.live_count = cnt + WP_CNT_LIVE;
         {
             TimedLaunch tl(ctx, 1);
-            if (a.dead_by_shape) {
+            if (groups) {
                 // persistent: as many CTAs as are resident, at most one warp per read
                 const size_t gsm = wp_compact_groups_smem_bytes(a.n_grp, a.P);
                 WP_CUDA(cudaFuncSetAttribute(wp_compact_groups_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

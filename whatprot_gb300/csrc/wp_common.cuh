@@ -253,22 +253,30 @@ struct BatchArgs {
     int n_uniq;
     // All-peptides mode: the runs of perm with one dye-count vector
     // ("groups"): group u is perm[grp_start[u] .. grp_start[u + 1]) with
-    // vector grp_D[u] (byte c = channel c); pep_Dw[p] is peptide p's vector.
+    // vector grp_D[u] (byte c = channel c).
     const int* grp_start;
     const uint32_t* grp_D;
     int n_grp;
-    const uint32_t* pep_Dw;
-    // nonzero: the compaction wrote no result for empty pairs (all-peptides
-    // mode, wp_compact_groups_kernel); the reduce tells them by their shape
-    int dead_by_shape;
-    // nonzero (wp_engine_replay): the engine passes run lists whose pairs
-    // they have run before, so the result slot holds a result, not the
-    // routed box size; the slot is still read, its value ignored
+    // Result indices.  pair_info null: a pair's result index is its slot
+    // g, work items are (r, g), every slot gets a result, and the pair's
+    // largest box waits in res_expo[g] for the engine.  pair_info set
+    // (wp_compact_groups_kernel): only non-empty pairs get a result index;
+    // read r's are rd_base[r] .. rd_base[r] + rd_n[r] - 1, in the
+    // compaction's order; work items are (r, d) and pair_info[d] = (the
+    // pair's slot offset within its read, its largest box); a pair without
+    // one has P = 0.
+    int2* pair_info;
+    int* rd_base;
+    int* rd_n;
+    // nonzero (wp_engine_replay, pair_info null): the engine passes run
+    // lists whose pairs they have run before, so the result slot holds a
+    // result, not the routed box size; the slot is still read, its value
+    // ignored
     int replay_trust;
     const int* slot_off;       // [R + 1] or null
-    float* res_mant;           // per slot: P = res_mant * 2^res_expo
+    float* res_mant;           // per result index: P = res_mant * 2^res_expo
     int* res_expo;
-    int2* work;                // non-empty (r, g) pairs
+    int2* work;                // non-empty pairs (r, result index)
     int* work_count;
     int* work_head;
     int2* ovf;                 // pairs whose state exceeds the thread slab
@@ -374,6 +382,17 @@ __host__ __device__ inline int slot_begin(const BatchArgs& a, int r) {
 }
 __host__ __device__ inline int slot_pep(const BatchArgs& a, int r, int g) {
     return a.cand ? a.cand[g] : g - r * a.P;
+}
+// The slot of work item rg = (r, result index) and the pair's largest box
+// (BatchArgs::pair_info).
+__device__ __forceinline__ int item_slot(const BatchArgs& a, int2 rg, int* vmax) {
+    if (a.pair_info) {
+        const int2 inf = a.pair_info[rg.y];
+        *vmax = inf.y;
+        return slot_begin(a, rg.x) + inf.x;
+    }
+    *vmax = a.res_expo[rg.y] & (a.replay_trust ? 0 : -1);
+    return rg.y;
 }
 
 // 2^x as a float for x <= 127 (0 below the subnormal range).

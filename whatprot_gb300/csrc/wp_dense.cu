@@ -407,7 +407,8 @@ __global__ void __launch_bounds__(WP_DENSE_WARPS_MAX * 32) wp_dense_kernel(Batch
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= count) break;
         const int2 rg = a.ovf[idx];
-        const PeptideRec& pep = a.peps[slot_pep(a, rg.x, rg.y)];
+        int vmax;
+        const PeptideRec& pep = a.peps[slot_pep(a, rg.x, item_slot(a, rg, &vmax))];
         float mant;
         int ex;
         pair_forward<HAS_BLOCK>(a, M, rg.x, m, pep, wb, a.dense_S_cap, lane, &mant, &ex, a.err);

@@ -16,9 +16,9 @@
 // k of thread i at k * blockDim.x + i) so every access of a warp hits 32
 // distinct banks whatever the index.  The compaction (wp_prep.cu) routes
 // each pair to the first pass whose slab holds its largest box and leaves
-// that box's size in the pair's result slot; a pass checks it against its
-// slab before any write and hands a pair that does not fit to the next
-// pass's list.
+// that box's size with the pair (BatchArgs::pair_info, or its result slot);
+// a pass checks it against its slab before any write and hands a pair that
+// does not fit to the next pass's list.
 //
 // Boxes are kept packed, one byte per channel in a 32-bit word (lower
 // corner) and another (width), so that the per-channel loops need no
@@ -825,8 +825,8 @@ __device__ int engine_pair(const BatchArgs& a, const SmemModel& M, int r,
     };
     auto emission_box = [&](int t) { return box_of(Lpk[t], Upk[t]); };
 
-    // The largest box any step of this pair uses (pair_vmax, left in the
-    // pair's result slot by the compaction) must fit the slab half; a pair
+    // The largest box any step of this pair uses (pair_vmax, left with the
+    // pair by the compaction: item_slot) must fit the slab half; a pair
     // that does not is handed to the next pass before anything is written.
     if (vmax > half) return 1;
     // Dye channel and remaining dyes of that channel per Edman position,
@@ -1091,10 +1091,10 @@ __global__ void __launch_bounds__(WP_ENGINE_THREADS) wp_engine_kernel(BatchArgs 
         const int w = base + lane;
         if (w < count) {
             const int2 rg = L.in[w];
-            const int p = slot_pep(a, rg.x, rg.y);
+            int vmax;
+            const int p = slot_pep(a, rg.x, item_slot(a, rg, &vmax));
             float mant;
             int ex;
-            const int vmax = a.res_expo[rg.y] & (a.replay_trust ? 0 : -1);
             int ov = engine_pair<C, HB>(a, M, rg.x, a.peps[p], slab, codes, nt, L.slab_half, vmax, &mant, &ex);
             if (ov) {
                 if (L.spill_error) {

@@ -555,10 +555,13 @@ __global__ void wp_compact_kernel(BatchArgs a) {
 // shape order).  Whether a pair is empty (L_0 > D on some channel) and its
 // largest box depend on the peptide through that vector alone, so each group
 // is routed as a whole: its pairs go, in the shape order, to the list of the
-// first engine pass whose slab holds the box, with the box size left in
-// their result slots for the engine.  Empty pairs get no write: the reduce
-// (BatchArgs::dead_by_shape) gives them P = 0 from their vector.  The read's
-// pairs of a list take one contiguous range (one global atomic per list).
+// first engine pass whose slab holds the box.  Result indices are dense
+// (BatchArgs::pair_info): the read's non-empty pairs take one contiguous
+// range in the order of the appends, each with its peptide and box size
+// beside it, so the engine's result writes and the reduce's reads are
+// coalesced and empty pairs cost nothing (P = 0 without a result).  The
+// read's pairs of a list take one contiguous range (one global atomic per
+// list).
 // Persistent CTAs (wp_compact_groups_smem_bytes): the groups and the shape
 // order are staged in shared memory once per CTA, so a warp's per-read work
 // waits on global memory only for the read's box words and the list atomics.
@@ -706,17 +709,25 @@ __global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(
             live_pairs += v;
             if (lane == k) mine = v;
         }
+        // and lane NL the read's range of result indices (the count of
+        // non-empty pairs is the allocator)
         int b = 0;
         if (lane < NL && mine > 0) {
             int* count = lane == WP_MAX_TIERS ? a.ovf_count : a.n_tiers > 0 ? a.tier_count[lane] : a.work_count;
             b = atomicAdd(count, mine);
+        } else if (lane == NL && live_pairs > 0) {
+            b = atomicAdd(a.live_count, live_pairs);
         }
 #pragma unroll
         for (int k = 0; k < NL; k++) base[k] = __shfl_sync(0xffffffffu, b, k);
-        if (lane == 0 && a.live_count && live_pairs) atomicAdd(a.live_count, live_pairs);
+        int dpos = __shfl_sync(0xffffffffu, b, NL);
+        if (lane == 0) {
+            a.rd_base[r] = dpos;
+            a.rd_n[r] = live_pairs;
+        }
         __syncwarp();
-        // the appends, group by group in key order
-        const long gr = (long)r * a.P;
+        // the appends, group by group in key order: result indices follow
+        // the same order
         for (int o = 0; o < n_live; o++) {
             const int i = s_ord[o];
             const int u = s_live[wid][i];
@@ -732,16 +743,13 @@ __global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(
                     at = base[k];
                     base[k] += cnt;
                 }
+            if (!list) continue;  // no pass holds these pairs (err = 2): P = 0
             for (int j = lane; j < cnt; j += 32) {
-                const int g = (int)(gr + perm[p0 + j]);
-                if (list) {
-                    a.res_expo[g] = vm;
-                    list[at + j] = make_int2(r, g);
-                } else {
-                    a.res_mant[g] = 0.0f;
-                    a.res_expo[g] = 0;
-                }
+                const int d = dpos + j;
+                a.pair_info[d] = make_int2(perm[p0 + j], vm);  // slot offset = peptide
+                list[at + j] = make_int2(r, d);
             }
+            dpos += cnt;
         }
         __syncwarp();
     }

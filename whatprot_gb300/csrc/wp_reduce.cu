@@ -71,18 +71,17 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
     const int g0 = slot_begin(a, r);
     const int g1 = a.slot_off ? a.slot_off[r + 1] : g0 + a.P;
     Cand best = {0.0f, 0, INT_MAX, -1};
-    // dead_by_shape: slots of empty pairs hold nothing; a pair is empty when
-    // the read is or when L_0 > D on some channel (every byte of the
-    // peptide's vector D >= L_0, bytes below 128, else empty)
-    const bool by_shape = a.dead_by_shape != 0;
-    uint32_t L0 = 0;
-    bool read_empty = false;
-    if (by_shape) {
-        L0 = a.Lpk[(long)r * a.model->T] & 0x7f7f7f7fu;
-        read_empty = a.flags[r] != 0;
-        // every empty pair has P = 0 and the first slot wins among zeros,
-        // so empty slots need no look: the first slot stands for them
+    // Result indices i0 .. i1 - 1: the read's slots, or (pair_info) its
+    // non-empty pairs, each with its slot offset beside it.  A pair without
+    // a result index has P = 0, and as the first slot wins among zeros, the
+    // first slot stands for all of them.
+    const bool dense = a.pair_info != nullptr;
+    int i0 = g0, i1 = g1;
+    if (dense) {
+        i0 = i1 = 0;
         if (g1 > g0) {
+            i0 = a.rd_base[r];
+            i1 = i0 + a.rd_n[r];
             best.mant = 0.0f;
             best.expo = 0;
             best.key = 0;
@@ -92,41 +91,32 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
     int El = INT_MIN;  // the lane's reference exponent (none yet)
     float hi = 0.0f, lo = 0.0f;
     double big = 0.0;  // terms with counts >= 2^24, relative to 2^El
-    // four slots per lane in flight: the loads first, then the slots in the
-    // lane's order (g, g + 32, g + 64, ...)
-    for (int gb = g0 + lane; gb < g1; gb += 128) {
+    // four results per lane in flight: the loads first, then the results
+    // in the lane's order (i, i + 32, i + 64, ...)
+    for (int ib = i0 + lane; ib < i1; ib += 128) {
         float mv[4];
-        int ev[4], cv[4];
+        int ev[4], cv[4], kv[4];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            const int g = gb + 32 * u;
+            const int i = ib + 32 * u;
             mv[u] = 0.0f;
             ev[u] = 0;
             cv[u] = 0;
-            if (g < g1) {
-                const int p = slot_pep(a, r, g);
-                bool live = true;
-                if (by_shape) {
-                    const uint32_t D = a.pep_Dw[p];
-                    live = !read_empty && (((D | 0x80808080u) - L0) & 0x80808080u) == 0x80808080u;
-                }
-                if (live) {
-                    mv[u] = a.res_mant[g];
-                    ev[u] = a.res_expo[g];
-                    cv[u] = a.counts[p];
-                } else {
-                    cv[u] = -1;  // empty pair: nothing to take
-                }
+            kv[u] = 0;
+            if (i < i1) {
+                const int key = dense ? a.pair_info[i].x : i - g0;  // slot offset
+                mv[u] = a.res_mant[i];
+                ev[u] = a.res_expo[i];
+                cv[u] = a.counts[slot_pep(a, r, g0 + key)];
+                kv[u] = key;
             }
         }
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            const int g = gb + 32 * u;
-            if (g >= g1) break;
-            if (cv[u] < 0) continue;
+            if (ib + 32 * u >= i1) break;
             const float mm = mv[u];
             const int ex = ev[u];
-            Cand c = {mm, ex, g - g0, g};
+            Cand c = {mm, ex, kv[u], g0 + kv[u]};
             if (cand_better(c, best)) best = c;
             if (mm > 0.0f) {
                 if (ex > El) {
