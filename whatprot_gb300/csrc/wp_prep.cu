@@ -47,6 +47,7 @@
 #define WP_COMPACT_SORT 1024  // candidate slots per read the compaction orders by shape
 #define WP_COMPACT_UNIQ 1024  // distinct dye-count vectors the compaction tabulates per read
 #define WP_COMPACT_CHUNK 2048  // slots the compaction routes per round of list appends
+#define WP_GROUP_BUCKETS 512  // clamped dye-count vectors the group compaction counting-sorts per read
 
 
 // ChannelModel::adjusted_mu (parameterization/model/channel-model.h:35-54).
@@ -581,6 +582,7 @@ __global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(
     __shared__ uint16_t s_live[WP_GROUP_WARPS][WP_GROUP_MAX];  // routed groups, in order
     __shared__ uint16_t s_vm[WP_GROUP_WARPS][WP_GROUP_MAX];    // per group: largest box (engine passes)
     __shared__ uint8_t s_dest[WP_GROUP_WARPS][WP_GROUP_MAX];   // per group: list (WP_MAX_TIERS: dense)
+    __shared__ uint16_t s_bkt[WP_GROUP_WARPS][WP_GROUP_BUCKETS];  // the counting sort's buckets
     const int n_grp = a.n_grp;
     int* gstart = reinterpret_cast<int*>(g_smem);
     uint32_t* gD = reinterpret_cast<uint32_t*>(gstart + n_grp + 1);
@@ -639,12 +641,65 @@ __global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(
             n_live += __popc(lm);
         }
         __syncwarp();
-        // rank of each group by its key (keys are distinct)
-        for (int i = lane; i < n_live; i += 32) {
-            const uint32_t ki = s_key[i];
-            int rank = 0;
-            for (int j = 0; j < n_live; j++) rank += s_key[j] < ki ? 1 : 0;
-            s_ord[rank] = (uint16_t)i;
+        // The groups in key order (s_ord).  When the clamped counts take at
+        // most WP_GROUP_BUCKETS values: a stable counting sort over them as
+        // a mixed-radix number, channel C - 1 most significant (the order
+        // of the key's bits), 32 positions a round with one writer per
+        // bucket and round; else the rank of each key among all (keys are
+        // distinct).  Both give the same order.
+        int range = 1;
+        for (int c = 0; c < C; c++) range *= min((int)((um1 >> (8 * c)) & 0xffu), 15) + 1;
+        if (range <= WP_GROUP_BUCKETS) {
+            uint16_t* bk = s_bkt[wid];
+            auto bucket = [&](int i) {
+                const uint32_t d16 = s_key[i] >> 9;
+                int b = 0;
+                for (int c = C - 1; c >= 0; c--)
+                    b = b * (min((int)((um1 >> (8 * c)) & 0xffu), 15) + 1) + (int)((d16 >> (4 * c)) & 0xfu);
+                return b;
+            };
+            for (int b = lane; b < range; b += 32) bk[b] = 0;
+            __syncwarp();
+            for (int i0 = 0; i0 < n_live; i0 += 32) {
+                const int i = i0 + lane;
+                const int b = i < n_live ? bucket(i) : -1 - lane;  // idle lanes: a bucket of their own
+                const unsigned peers = __match_any_sync(0xffffffffu, b);
+                if (i < n_live && lane == __ffs(peers) - 1) bk[b] = (uint16_t)(bk[b] + __popc(peers));
+                __syncwarp();
+            }
+            // bucket sizes to first positions: each lane scans a block of buckets
+            const int per = (range + 31) >> 5;
+            const int b0 = min(lane * per, range), b1 = min(b0 + per, range);
+            int sz = 0;
+            for (int b = b0; b < b1; b++) sz += bk[b];
+            int incl = sz;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            int run = incl - sz;
+            for (int b = b0; b < b1; b++) {
+                const int n = bk[b];
+                bk[b] = (uint16_t)run;
+                run += n;
+            }
+            __syncwarp();
+            for (int i0 = 0; i0 < n_live; i0 += 32) {
+                const int i = i0 + lane;
+                const int b = i < n_live ? bucket(i) : -1 - lane;
+                const unsigned peers = __match_any_sync(0xffffffffu, b);
+                if (i < n_live) s_ord[bk[b] + __popc(peers & ((1u << lane) - 1))] = (uint16_t)i;
+                __syncwarp();
+                if (i < n_live && lane == __ffs(peers) - 1) bk[b] = (uint16_t)(bk[b] + __popc(peers));
+                __syncwarp();
+            }
+        } else {
+            for (int i = lane; i < n_live; i += 32) {
+                const uint32_t ki = s_key[i];
+                int rank = 0;
+                for (int j = 0; j < n_live; j++) rank += s_key[j] < ki ? 1 : 0;
+                s_ord[rank] = (uint16_t)i;
+            }
         }
         __syncwarp();
         // The largest box depends on the counts through the clamped ones
@@ -726,30 +781,68 @@ __global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(
             a.rd_n[r] = live_pairs;
         }
         __syncwarp();
-        // the appends, group by group in key order: result indices follow
-        // the same order
-        for (int o = 0; o < n_live; o++) {
-            const int i = s_ord[o];
-            const int u = s_live[wid][i];
-            const int d8 = s_dest[wid][i];
-            const int vm = s_vm[wid][i];
-            const int p0 = gstart[u], cnt = gstart[u + 1] - p0;
-            int2* list = nullptr;
-            int at = 0;
-#pragma unroll
-            for (int k = 0; k < NL; k++)
-                if (d8 == k) {
-                    list = k == WP_MAX_TIERS ? a.ovf : a.n_tiers > 0 ? a.tier_list[k] : a.work;
-                    at = base[k];
-                    base[k] += cnt;
+        // The appends, in key order, 32 groups a round: a group's pairs
+        // take the next places of its list and the next result indices
+        // (scans of the group sizes, per list and over all), and the lanes
+        // share the round's pairs.  Groups no pass holds (err = 2) take
+        // neither: P = 0.
+        for (int o0 = 0; o0 < n_live; o0 += 32) {
+            const int o = o0 + lane;
+            int cnt = 0, p0 = 0, vm = 0, d8 = 0xff;
+            if (o < n_live) {
+                const int i = s_ord[o];
+                d8 = s_dest[wid][i];
+                if (d8 != 0xff) {
+                    const int u = s_live[wid][i];
+                    p0 = gstart[u];
+                    cnt = gstart[u + 1] - p0;
+                    vm = s_vm[wid][i];
                 }
-            if (!list) continue;  // no pass holds these pairs (err = 2): P = 0
-            for (int j = lane; j < cnt; j += 32) {
-                const int d = dpos + j;
-                a.pair_info[d] = make_int2(perm[p0 + j], vm);  // slot offset = peptide
-                list[at + j] = make_int2(r, d);
             }
-            dpos += cnt;
+            int lpos = 0;  // the group's first place in its list
+#pragma unroll
+            for (int k = 0; k < NL; k++) {
+                const int v = d8 == k ? cnt : 0;
+                int inc = v;
+                for (int sft = 1; sft < 32; sft <<= 1) {
+                    const int w = __shfl_up_sync(0xffffffffu, inc, sft);
+                    if (lane >= sft) inc += w;
+                }
+                if (d8 == k) lpos = base[k] + inc - v;
+                base[k] += __shfl_sync(0xffffffffu, inc, 31);
+            }
+            int incl = cnt;
+            for (int sft = 1; sft < 32; sft <<= 1) {
+                const int w = __shfl_up_sync(0xffffffffu, incl, sft);
+                if (lane >= sft) incl += w;
+            }
+            const int excl = incl - cnt;  // the group's first pair in the round
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            for (int q0 = 0; q0 < total; q0 += 32) {
+                const int q = q0 + lane;
+                // the group holding pair q: the last lane whose first pair is <= q
+                int src = 0;
+                for (int sft = 16; sft > 0; sft >>= 1) {
+                    const int e = __shfl_sync(0xffffffffu, excl, src + sft);
+                    if (e <= q) src += sft;
+                }
+                const int g_excl = __shfl_sync(0xffffffffu, excl, src);
+                const int g_p0 = __shfl_sync(0xffffffffu, p0, src);
+                const int g_vm = __shfl_sync(0xffffffffu, vm, src);
+                const int g_lpos = __shfl_sync(0xffffffffu, lpos, src);
+                const int g_d8 = __shfl_sync(0xffffffffu, d8, src);
+                if (q < total) {
+                    const int j = q - g_excl;
+                    const int d = dpos + q;
+                    int2* list = a.work;
+#pragma unroll
+                    for (int k = 0; k < NL; k++)
+                        if (g_d8 == k) list = k == WP_MAX_TIERS ? a.ovf : a.n_tiers > 0 ? a.tier_list[k] : a.work;
+                    a.pair_info[d] = make_int2(perm[g_p0 + j], g_vm);  // slot offset = peptide
+                    list[g_lpos + j] = make_int2(r, d);
+                }
+            }
+            dpos += total;
         }
         __syncwarp();
     }
