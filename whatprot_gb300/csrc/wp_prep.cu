@@ -3,10 +3,12 @@
 //   wp_prep_reads_kernel    one thread per (read, timestep): the emission
 //                           pruning box [cmin, cmax) of the reference's
 //                           PeptideEmission (hmm/step/peptide-emission.cc:
-//                           50-163), in FP64 as the reference computes it,
-//                           and the emission factors, stored as (FP32
-//                           mantissa, int exponent) of norm * 2^y with y in
-//                           FP64 (the FP64 exp only in the far tails).
+//                           50-163), in FP64 as the reference computes it
+//                           (without interactions from per-CTA tables of
+//                           its thresholds), and the emission factors,
+//                           stored as (FP32 mantissa, int exponent) of
+//                           norm * 2^y with y in FP64 (the FP64 exp only in
+//                           the far tails).
 //   wp_read_summary_kernel  one thread per read: the closed-form pruning boxes
 //                           every pair of the read shares, L_t = max_{t'>=t}
 //                           cmin_{t'} and min_{t'<=t} cmax_{t'}, the
@@ -112,6 +114,32 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
                                      EmitEntry* __restrict__ table, int entries_per_read) {
     const DevModel& m = *model;
     const int T = m.T, C = m.C;
+    const bool tabled = !m.interacting;  // per-count quantities from the model's tables
+    // Non-interacting models: the pruning thresholds mu_d + s_d and mu_d -
+    // s_d (s_d = dist_cutoff * sigma_d) per (channel, count), once per CTA,
+    // each rounded as the reference's separate multiply and add round it.
+    // And the pdf's normalisation 1 / (sigma sqrt(2 pi)) as an FP32
+    // mantissa in [0.5, 1) and an exponent.
+    __shared__ double s_thi[WP_MAX_CHANNELS][WP_W + 1], s_tlo[WP_MAX_CHANNELS][WP_W + 1];
+    __shared__ float s_nm[WP_MAX_CHANNELS][WP_W + 1];
+    __shared__ int s_ne[WP_MAX_CHANNELS][WP_W + 1];
+    if (tabled) {
+        for (int k = threadIdx.x; k < C * (WP_W + 1); k += blockDim.x) {
+            const int c = k / (WP_W + 1), d = k % (WP_W + 1);
+            const double sd = __dmul_rn(dist_cutoff, m.e_sig[c][d]);
+            s_thi[c][d] = __dadd_rn(m.e_amu[c][d], sd);
+            s_tlo[c][d] = __dsub_rn(m.e_amu[c][d], sd);
+            int ne;
+            float nm = (float)frexp(m.e_norm[c][d], &ne);
+            if (nm >= 1.0f) {  // rounding up to 1.0
+                nm = 0.5f;
+                ne += 1;
+            }
+            s_nm[c][d] = nm;
+            s_ne[c][d] = ne;
+        }
+        __syncthreads();
+    }
     long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= (long)R * T) return;
     int r = (int)(gid / T), t = (int)(gid % T);
@@ -123,6 +151,29 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
             lo[c] = 0;
             hi[c] = max_num_dyes + 1;
         }
+    } else if (tabled) {
+        // Without interactions channel c's mu and sigma depend on its own
+        // count alone, so the reference's fixed point over the other
+        // channels' counts changes nothing here and is skipped; the scans
+        // for the first count with mu + s > x and, from there, the first
+        // with mu - s > x compare x with the thresholds.
+        for (int c = 0; c < C; c++) {
+            const double x = rad[t * C + c];
+            unsigned cmin = max_num_dyes + 1;
+            for (unsigned d = 0; d < max_num_dyes + 1; d++)
+                if (s_thi[c][d] > x) {
+                    cmin = d;
+                    break;
+                }
+            unsigned cmax = max_num_dyes + 1;
+            for (unsigned d = cmin; d < max_num_dyes + 1; d++)
+                if (s_tlo[c][d] > x) {
+                    cmax = d;
+                    break;
+                }
+            lo[c] = cmin;
+            hi[c] = cmax;
+        }
     } else {
         unsigned counts_lo[WP_MAX_CHANNELS] = {0, 0, 0, 0};
         unsigned counts_hi[WP_MAX_CHANNELS] = {0, 0, 0, 0};
@@ -131,7 +182,6 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
         // The reference loops to a fixed point without a bound and cycles
         // forever for intensities below about -0.5 mu; stop after 1000
         // rounds (the oracle uses the same bound).
-        const bool tabled = !m.interacting;  // per-count quantities from the model's tables
         while (did_change && guard < 1000) {
             did_change = false;
             guard++;
@@ -217,20 +267,21 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
                     // pdf_helper (channel-model.h:61-70) from the tables:
                     // norm * exp(-offset^2 / den) = norm * 2^y, y in FP64; the
                     // power of two of its integer part is exact and 2^frac
-                    // (in [1, 2)) is taken in FP32, which the FP32 mantissa
-                    // stored keeps to a few units in the last place.  Far
-                    // tails (y <= -1000, where FP64 itself nears underflow)
-                    // take the FP64 exp so that zeros fall where the
-                    // reference's do.
+                    // (in [1, 2)) times norm's mantissa is taken in FP32,
+                    // which the FP32 mantissa stored keeps to about one
+                    // unit in the last place (FP64 runs at a small fraction
+                    // of the FP32 rate on this GPU).  Far tails (y <= -1000,
+                    // where FP64 itself nears underflow) take the FP64 exp
+                    // so that zeros fall where the reference's do.
                     const double offset = rad[t * C + c] - m.e_amu[c][n];
                     const double y = -(offset * offset) * m.e_l2den[c][n];
                     if (y > -1000.0) {
                         const double fl = floor(y);
                         const float fr = exp2f((float)(y - fl));
-                        int ex;
-                        const double mt = frexp(m.e_norm[c][n] * (double)fr, &ex);
-                        en.mant = (float)mt;
-                        en.expo = ex + (int)fl;
+                        const float pm = s_nm[c][n] * fr;  // in [0.5, 2]
+                        const bool up = pm >= 1.0f;
+                        en.mant = up ? 0.5f * pm : pm;
+                        en.expo = s_ne[c][n] + (up ? 1 : 0) + (int)fl;
                         if (en.mant >= 1.0f) {  // rounding up to 1.0
                             en.mant = 0.5f;
                             en.expo += 1;

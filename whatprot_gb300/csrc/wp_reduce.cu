@@ -60,8 +60,8 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& err) 
 // FP32 rate and an FP64 multiply-add per slot made this kernel FP64-bound.
 // Terms below 2^-100 of the lane's reference are dropped (below the FP64
 // resolution of a total that holds at least one term of 2^El / 2).  Counts
-// of 2^24 or more (not exact in FP32) go to an FP64 side sum.  The lanes'
-// sums meet in FP64 relative to E, the best's exponent.
+// of 2^24 or more (not exact in FP32) are added as two terms.  The lanes'
+// sums meet in FP32 pairs relative to E, the best's exponent.
 __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
                                  double* __restrict__ out_score, double* __restrict__ out_total,
                                  double* __restrict__ out_log, const int* __restrict__ pep_ids) {
@@ -90,7 +90,16 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
     }
     int El = INT_MIN;  // the lane's reference exponent (none yet)
     float hi = 0.0f, lo = 0.0f;
-    double big = 0.0;  // terms with counts >= 2^24, relative to 2^El
+    // adds mm * cf * s2 (cf an integer exact in FP32, s2 a power of two):
+    // the product exactly as its FP32 rounding and the FMA remainder
+    auto add_term = [&](float mm, float cf, float s2) {
+        const float p = mm * cf;
+        const float pe = fmaf(mm, cf, -p);  // exact: p + pe == mm * cf
+        float sum, err;
+        two_sum(hi, p * s2, sum, err);
+        hi = sum;
+        lo += err + pe * s2;
+    };
     // four results per lane in flight: the loads first, then the results
     // in the lane's order (i, i + 32, i + 64, ...)
     for (int ib = i0 + lane; ib < i1; ib += 128) {
@@ -123,7 +132,6 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
                     const float f = El == INT_MIN || El - ex < -100 ? 0.0f : exp2i(El - ex);
                     hi *= f;
                     lo *= f;
-                    big *= (double)f;
                     El = ex;
                 }
                 const int d = ex - El;
@@ -131,15 +139,10 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
                     const int cnt = cv[u];
                     const float s2 = exp2i(d);
                     if (cnt < (1 << 24)) {
-                        const float cf = (float)cnt;
-                        const float p = mm * cf;
-                        const float pe = fmaf(mm, cf, -p);  // exact: p + pe == mm * cnt
-                        float sum, err;
-                        two_sum(hi, p * s2, sum, err);
-                        hi = sum;
-                        lo += err + pe * s2;
-                    } else {
-                        big += (double)cnt * (double)(mm * s2);
+                        add_term(mm, (float)cnt, s2);
+                    } else {  // not exact in FP32: its high and low bits apart
+                        add_term(mm, (float)(cnt & ~0xfff), s2);
+                        add_term(mm, (float)(cnt & 0xfff), s2);
                     }
                 }
             }
@@ -154,14 +157,28 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
         if (cand_better(c, best)) best = c;
     }
     // E: the best's exponent, the largest exponent of any nonzero slot
+    // (El <= E on every lane).  The lanes' pairs meet relative to 2^E in
+    // FP32: scaled by 2^(El - E) (exact, or so far below the best's own
+    // term, 2^(E - 1) or more, that FP64 would not hold them either), then
+    // summed over the warp with TwoSum, the errors kept in the low words;
+    // FP64 (a slow pipe on this GPU) only for lane 0's final sum.
     const int E = best.mant > 0.0f ? best.expo : 0;
-    double tot = 0.0;
-    if (El != INT_MIN && El - E >= -1000) {
-        const double sc = __longlong_as_double((long long)(1023 + El - E) << 52);  // 2^(El - E)
-        tot = (((double)hi + (double)lo) + big) * sc;
+    float th = 0.0f, tl = 0.0f;
+    if (El != INT_MIN) {
+        const float sf = exp2i(max(El - E, -200));
+        th = hi * sf;
+        tl = lo * sf;
     }
-    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, th, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, tl, o);
+        float sum, err;
+        two_sum(th, oh, sum, err);
+        th = sum;
+        tl = (tl + ol) + err;
+    }
     if (lane != 0) return;
+    const double tot = (double)th + (double)tl;
     if (best.idx < 0) {  // no candidates
         out_id[r] = -1;
         out_score[r] = 0.0;
@@ -171,19 +188,30 @@ __global__ void wp_reduce_kernel(BatchArgs a, int32_t* __restrict__ out_id,
     }
     out_id[r] = pep_ids[slot_pep(a, r, best.idx)];
     const double sc = (double)best.mant;
-    if (!(tot > 0.0) || isnan(sc / tot)) {
+    // the reference's NaN patch (score / total NaN): with sc in [0, 1) that
+    // is the case exactly when tot is not positive (or NaN)
+    if (!(tot > 0.0)) {
         out_score[r] = 0.0;
         out_total[r] = 1.0;
         if (out_log) out_log[r] = -INFINITY;
         return;
     }
-    const double s_abs = ldexp(sc, E), t_abs = ldexp(tot, E);
-    if (s_abs >= DBL_MIN && isfinite(s_abs) && isfinite(t_abs)) {
-        out_score[r] = s_abs;
-        out_total[r] = t_abs;
-    } else {  // outside the double range: same power of two on both
-        out_score[r] = sc;
-        out_total[r] = tot;
+    // sc * 2^E and tot * 2^E; where both stay normal that is an add to
+    // their exponent fields (sc, tot > 0), else ldexp
+    const long long sb = __double_as_longlong(sc), tb = __double_as_longlong(tot);
+    const int es = (int)(sb >> 52) + E, et = (int)(tb >> 52) + E;
+    if (sb > 0 && es >= 1 && es <= 2046 && et >= 1 && et <= 2046) {
+        out_score[r] = __longlong_as_double(sb + ((long long)E << 52));
+        out_total[r] = __longlong_as_double(tb + ((long long)E << 52));
+    } else {
+        const double s_abs = ldexp(sc, E), t_abs = ldexp(tot, E);
+        if (s_abs >= DBL_MIN && isfinite(s_abs) && isfinite(t_abs)) {
+            out_score[r] = s_abs;
+            out_total[r] = t_abs;
+        } else {  // outside the double range: same power of two on both
+            out_score[r] = sc;
+            out_total[r] = tot;
+        }
     }
     if (out_log) out_log[r] = log(sc) + (double)E * 0.69314718055994530942;
 }
