@@ -50,6 +50,7 @@
 #define WP_COMPACT_UNIQ 1024  // distinct dye-count vectors the compaction tabulates per read
 #define WP_COMPACT_CHUNK 2048  // slots the compaction routes per round of list appends
 #define WP_GROUP_BUCKETS 512  // clamped dye-count vectors the group compaction counting-sorts per read
+static_assert(WP_GROUP_BUCKETS >= WP_GROUP_MAX, "the group compaction lists its runs in the buckets");
 
 
 // ChannelModel::adjusted_mu (parameterization/model/channel-model.h:35-54).
@@ -755,35 +756,52 @@ __global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(
         __syncwarp();
         // The largest box depends on the counts through the clamped ones
         // alone (pair_vmax takes min(U_t, D + 1) = min(U_t, D' + 1)), so it
-        // is computed once per run of equal clamped counts in key order, by
-        // the run's first group, and the pass list follows from it.
+        // is computed once per run of equal clamped counts in key order:
+        // the runs' clamped counts are listed first (in the sort's buckets,
+        // free now), then the lanes take one run each, and the pass list of
+        // every group follows from its run's box.
+        uint16_t* runs = s_bkt[wid];
+        int n_runs = 0;  // warp-uniform
+        for (int o0 = 0; o0 < n_live; o0 += 32) {
+            const int o = o0 + lane;
+            bool start = false;
+            uint32_t dk = 0;
+            if (o < n_live) {
+                dk = s_key[s_ord[o]] >> 9;
+                start = o == 0 || (s_key[s_ord[o - 1]] >> 9) != dk;
+            }
+            const unsigned sm = __ballot_sync(0xffffffffu, start);
+            if (start) runs[n_runs + __popc(sm & ((1u << lane) - 1))] = (uint16_t)dk;
+            n_runs += __popc(sm);
+        }
+        __syncwarp();
+        for (int k0 = 0; k0 < n_runs; k0 += 32) {
+            const int k = k0 + lane;
+            int vm = 0;
+            if (k < n_runs) {
+                const uint32_t dk = runs[k];
+                const uint32_t Dw = (dk & 0xfu) | ((dk & 0xf0u) << 4) | ((dk & 0xf00u) << 8) | ((dk & 0xf000u) << 12);
+                vm = pair_vmax_w(C, T, sL[wid], sU[wid], Dw);
+            }
+            __syncwarp();
+            if (k < n_runs) runs[k] = (uint16_t)min(vm, 65535);  // above every slab half
+        }
+        __syncwarp();
         int tot[NL];
 #pragma unroll
         for (int k = 0; k < NL; k++) tot[k] = 0;
-        int carry = 0;  // the last run's box size (warp-uniform)
+        int run0 = 0;  // runs started before this chunk (warp-uniform)
         for (int o0 = 0; o0 < n_live; o0 += 32) {
             const int o = o0 + lane;
             int i = 0;
             bool start = false;
-            uint32_t dk = 0;
             if (o < n_live) {
                 i = s_ord[o];
-                dk = s_key[i] >> 9;
-                start = o == 0 || (s_key[s_ord[o - 1]] >> 9) != dk;
+                start = o == 0 || (s_key[s_ord[o - 1]] >> 9) != (s_key[i] >> 9);
             }
-            int vm = 0;
-            if (start) {
-                const uint32_t Dw = (dk & 0xfu) | ((dk & 0xf0u) << 4) | ((dk & 0xf00u) << 8) | ((dk & 0xf000u) << 12);
-                vm = pair_vmax_w(C, T, sL[wid], sU[wid], Dw);
-            }
-            // each lane takes the box size of the nearest run start at or
-            // before it (an earlier chunk's: carry)
             const unsigned sm = __ballot_sync(0xffffffffu, start);
-            const unsigned before = sm & (0xffffffffu >> (31 - lane));
-            const int src = before ? 31 - __clz(before) : 0;
-            const int vs = __shfl_sync(0xffffffffu, vm, src);
             if (o < n_live) {
-                const int v = before ? vs : carry;
+                const int v = runs[run0 + __popc(sm & (0xffffffffu >> (31 - lane))) - 1];
                 const int u = s_live[wid][i];
                 int dest = 0;  // -2: no shape holds these pairs (P = 0, err = 2)
                 if (a.n_tiers > 0) {
@@ -793,17 +811,14 @@ __global__ void __launch_bounds__(WP_GROUP_WARPS * 32) wp_compact_groups_kernel(
                     if (dest == WP_MAX_TIERS && !a.route_dense) dest = -2;
                 }
                 if (dest == -2) atomicExch(a.err, 2);
-                s_vm[wid][i] = (uint16_t)min(v, 65535);
+                s_vm[wid][i] = (uint16_t)v;
                 s_dest[wid][i] = (uint8_t)(dest < 0 ? 0xffu : dest);
                 const int cnt = gstart[u + 1] - gstart[u];
 #pragma unroll
                 for (int k = 0; k < NL; k++)
                     if (dest == k) tot[k] += cnt;
             }
-            const int last = min(31, n_live - 1 - o0);  // the chunk's last position's lane
-            const unsigned lb = sm & (0xffffffffu >> (31 - last));
-            const int vl = __shfl_sync(0xffffffffu, vm, lb ? 31 - __clz(lb) : 0);
-            if (lb) carry = vl;
+            run0 += __popc(sm);
         }
         // each list's range for this read: lane k takes list k's atomic
         int base[NL];
