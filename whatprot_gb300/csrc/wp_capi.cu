@@ -35,6 +35,7 @@ __global__ void wp_prep_reads_kernel(const DevModel*, const double*, int, unsign
                                      uint8_t*, uint8_t*, EmitEntry*, int);
 __global__ void wp_read_summary_kernel(BatchArgs);
 __global__ void wp_window_factors_kernel(BatchArgs);
+size_t wp_window_smem_bytes(int C, int W, int threads);
 __global__ void wp_compact_kernel(BatchArgs);
 __global__ void wp_compact_groups_kernel(BatchArgs);
 size_t wp_compact_groups_smem_bytes(int n_grp, int P);
@@ -576,7 +577,10 @@ wp_status run_batch(wp_ctx* ctx, const double* d_rads, int R, double dist_cutoff
         ctx->launches++;
         WP_CUDA(cudaGetLastError(), "summary launch");
         if (window_factors) {
-            wp_window_factors_kernel<<<(int)((n + 127) / 128), 128, 0, ctx->stream>>>(a);
+            const size_t wsm = wp_window_smem_bytes(C, W, 128);
+            WP_CUDA(cudaFuncSetAttribute(wp_window_factors_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)wsm), "window factors attribute");
+            wp_window_factors_kernel<<<(int)((n + 127) / 128), 128, wsm, ctx->stream>>>(a);
             ctx->launches++;
             WP_CUDA(cudaGetLastError(), "window factors launch");
         }

@@ -16,7 +16,8 @@
 //                           the read prunes every pair.
 //   wp_window_factors_kernel  one thread per (read, timestep): the emission
 //                           factors normalised over the pruning window, for
-//                           the engine (non-interacting models).
+//                           the engine (non-interacting models); the CTA's
+//                           rows staged through shared memory.
 //   wp_compact_kernel       one CTA per read (candidate lists, loglik):
 //                           pairs whose pruned range is empty get
 //                           probability 0 (PeptideHMM::probability,
@@ -121,7 +122,12 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
     // each rounded as the reference's separate multiply and add round it.
     // And the pdf's normalisation 1 / (sigma sqrt(2 pi)) as an FP32
     // mantissa in [0.5, 1) and an exponent.
+    // The thresholds also rounded to FP32 (rounding is monotone, so FP32
+    // order decides every comparison but ties, which go to FP64), and
+    // log2(e) / (2 sigma^2) times 2^40 (exact) for the exponent's fixed point.
     __shared__ double s_thi[WP_MAX_CHANNELS][WP_W + 1], s_tlo[WP_MAX_CHANNELS][WP_W + 1];
+    __shared__ double s_l2d40[WP_MAX_CHANNELS][WP_W + 1];
+    __shared__ float s_thi_f[WP_MAX_CHANNELS][WP_W + 1], s_tlo_f[WP_MAX_CHANNELS][WP_W + 1];
     __shared__ float s_nm[WP_MAX_CHANNELS][WP_W + 1];
     __shared__ int s_ne[WP_MAX_CHANNELS][WP_W + 1];
     if (tabled) {
@@ -130,6 +136,9 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
             const double sd = __dmul_rn(dist_cutoff, m.e_sig[c][d]);
             s_thi[c][d] = __dadd_rn(m.e_amu[c][d], sd);
             s_tlo[c][d] = __dsub_rn(m.e_amu[c][d], sd);
+            s_thi_f[c][d] = (float)s_thi[c][d];
+            s_tlo_f[c][d] = (float)s_tlo[c][d];
+            s_l2d40[c][d] = m.e_l2den[c][d] * 0x1p40;
             int ne;
             float nm = (float)frexp(m.e_norm[c][d], &ne);
             if (nm >= 1.0f) {  // rounding up to 1.0
@@ -160,18 +169,23 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
         // with mu - s > x compare x with the thresholds.
         for (int c = 0; c < C; c++) {
             const double x = rad[t * C + c];
+            const float xf = (float)x;
             unsigned cmin = max_num_dyes + 1;
-            for (unsigned d = 0; d < max_num_dyes + 1; d++)
-                if (s_thi[c][d] > x) {
+            for (unsigned d = 0; d < max_num_dyes + 1; d++) {
+                const float tf = s_thi_f[c][d];
+                if (tf > xf || (tf == xf && s_thi[c][d] > x)) {
                     cmin = d;
                     break;
                 }
+            }
             unsigned cmax = max_num_dyes + 1;
-            for (unsigned d = cmin; d < max_num_dyes + 1; d++)
-                if (s_tlo[c][d] > x) {
+            for (unsigned d = cmin; d < max_num_dyes + 1; d++) {
+                const float tf = s_tlo_f[c][d];
+                if (tf > xf || (tf == xf && s_tlo[c][d] > x)) {
                     cmax = d;
                     break;
                 }
+            }
             lo[c] = cmin;
             hi[c] = cmax;
         }
@@ -266,23 +280,28 @@ __global__ void wp_prep_reads_kernel(const DevModel* __restrict__ model,
                 en.expo = WP_EXPO_ZERO;
                 if ((unsigned)n >= lo[c] && (unsigned)n < hi[c]) {
                     // pdf_helper (channel-model.h:61-70) from the tables:
-                    // norm * exp(-offset^2 / den) = norm * 2^y, y in FP64; the
-                    // power of two of its integer part is exact and 2^frac
-                    // (in [1, 2)) times norm's mantissa is taken in FP32,
-                    // which the FP32 mantissa stored keeps to about one
-                    // unit in the last place (FP64 runs at a small fraction
-                    // of the FP32 rate on this GPU).  Far tails (y <= -1000,
-                    // where FP64 itself nears underflow) take the FP64 exp
-                    // so that zeros fall where the reference's do.
+                    // norm * exp(-offset^2 / den) = norm * 2^y, y in FP64
+                    // (as y * 2^40, exact); y rounded to 24 fractional bits
+                    // by one conversion to a 64-bit integer gives the
+                    // power of two of its integer part exactly and the
+                    // fraction exactly as an FP32 number; 2^frac (in
+                    // [1, 2)) times norm's mantissa is taken in FP32, which
+                    // the FP32 mantissa stored keeps to about one unit in
+                    // the last place (FP64 runs at a small fraction of the
+                    // FP32 rate on this GPU).  Far tails (y <= -1000, where
+                    // FP64 itself nears underflow) take the FP64 exp so
+                    // that zeros fall where the reference's do.
                     const double offset = rad[t * C + c] - m.e_amu[c][n];
-                    const double y = -(offset * offset) * m.e_l2den[c][n];
-                    if (y > -1000.0) {
-                        const double fl = floor(y);
-                        const float fr = exp2f((float)(y - fl));
+                    const double y40 = -(offset * offset) * s_l2d40[c][n];
+                    if (y40 > -1000.0 * 0x1p40) {
+                        // round(y * 2^24): floor(y * 2^40), then to nearest
+                        const long long q24 = (__double2ll_rd(y40) + (1ll << 15)) >> 16;
+                        const int fl = (int)(q24 >> 24);
+                        const float fr = exp2f((float)(int)(q24 & 0xffffff) * 0x1p-24f);
                         const float pm = s_nm[c][n] * fr;  // in [0.5, 2]
                         const bool up = pm >= 1.0f;
                         en.mant = up ? 0.5f * pm : pm;
-                        en.expo = s_ne[c][n] + (up ? 1 : 0) + (int)fl;
+                        en.expo = s_ne[c][n] + (up ? 1 : 0) + fl;
                         if (en.mant >= 1.0f) {  // rounding up to 1.0
                             en.mant = 0.5f;
                             en.expo += 1;
@@ -366,71 +385,103 @@ __global__ void wp_read_summary_kernel(BatchArgs a) {
 // normalising exponent: the same numbers the engine's own normalisation of
 // the box gives.  Where a factor lies further below, gK = WP_GK_NONE and the
 // engine normalises that (read, t) itself.
+// Shared memory of wp_window_factors_kernel: per item its table row and its
+// outputs (C W entries, floats and bytes).
+size_t wp_window_smem_bytes(int C, int W, int threads) {
+    return (size_t)threads * C * W * (sizeof(EmitEntry) + sizeof(float) + 1);
+}
+
 __global__ void wp_window_factors_kernel(BatchArgs a) {
     const DevModel& m = *a.model;
     const int T = m.T, C = m.C, W = a.W;
-    const long gid = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= (long)a.R * T) return;
-    const int r = (int)(gid / T), t = (int)(gid % T);
-    const long rt = (long)r * T + t;
-    const EmitEntry* tab = a.tab + (long)r * a.entries + (long)t * C * W;  // [(t C + c) W + n]
-    float* gt = a.gtab + rt * C * W;
-    uint8_t* gd = a.gdelta + rt * C * W;
-    const uint8_t* lo = a.lo + rt * C;
-    const uint8_t* hi = a.hi + rt * C;
-    const uint8_t* Ls = a.Lsuf + rt * C;
-    const uint8_t* Up = a.Upre + rt * C;
-    int K = 0;
-    bool ok = true;
-    for (int c = 0; c < C; c++) {
-        const EmitEntry* row = tab + c * W;
-        int km = WP_EXPO_ZERO;  // the window's largest exponent
-        for (int n = lo[c]; n < hi[c] && n < W; n++)
-            if (row[n].mant != 0.0f) km = max(km, row[n].expo);
-        for (int n = 0; n < W; n++) {
-            const EmitEntry en = row[n];  // zero outside the window
-            float v = 0.0f;
-            if (en.mant != 0.0f) {
-                const int d = en.expo - km;
-                if (d < -100)
-                    ok = false;
-                else
-                    v = en.mant * exp2i(d);
+    const int CW = C * W;
+    // The CTA's (read, t) items are consecutive and so are their table rows
+    // and output rows (C W entries per item), so the rows go through shared
+    // memory: the loads and stores of the CTA are coalesced, not one
+    // thread's row after another's.
+    extern __shared__ __align__(16) unsigned char w_smem[];
+    EmitEntry* s_tab = reinterpret_cast<EmitEntry*>(w_smem);
+    float* s_gt = reinterpret_cast<float*>(s_tab + (size_t)blockDim.x * CW);
+    uint8_t* s_gd = reinterpret_cast<uint8_t*>(s_gt + (size_t)blockDim.x * CW);
+    const long item0 = (long)blockIdx.x * blockDim.x;
+    const long n_items_all = (long)a.R * T;
+    const int n_items = (int)min((long)blockDim.x, n_items_all - item0);
+    const int n_ent = n_items * CW;
+    {
+        const EmitEntry* src = a.tab + item0 * CW;  // [r][t][c][n]: item (r, t) at (r T + t) C W
+        for (int k = threadIdx.x; k < n_ent; k += blockDim.x) s_tab[k] = src[k];
+    }
+    __syncthreads();
+    const long gid = item0 + threadIdx.x;
+    if (threadIdx.x < n_items) {
+        const int r = (int)(gid / T), t = (int)(gid % T);
+        const long rt = (long)r * T + t;
+        const EmitEntry* tab = s_tab + threadIdx.x * CW;  // [c W + n]
+        float* gt = s_gt + threadIdx.x * CW;
+        uint8_t* gd = s_gd + threadIdx.x * CW;
+        const uint8_t* lo = a.lo + rt * C;
+        const uint8_t* hi = a.hi + rt * C;
+        const uint8_t* Ls = a.Lsuf + rt * C;
+        const uint8_t* Up = a.Upre + rt * C;
+        int K = 0;
+        bool ok = true;
+        for (int c = 0; c < C; c++) {
+            const EmitEntry* row = tab + c * W;
+            int km = WP_EXPO_ZERO;  // the window's largest exponent
+            for (int n = lo[c]; n < hi[c] && n < W; n++)
+                if (row[n].mant != 0.0f) km = max(km, row[n].expo);
+            for (int n = 0; n < W; n++) {
+                const EmitEntry en = row[n];  // zero outside the window
+                float v = 0.0f;
+                if (en.mant != 0.0f) {
+                    const int d = en.expo - km;
+                    if (d < -100)
+                        ok = false;
+                    else
+                        v = en.mant * exp2i(d);
+                }
+                gt[c * W + n] = v;
             }
-            gt[c * W + n] = v;
+            if (km != WP_EXPO_ZERO) K += km;
+            // boxes [L_t, u): the window's exponent minus the box's largest (0
+            // while the box has no nonzero factor; its pairs get P = 0)
+            const int L = Ls[c], U = Up[c];
+            int run = WP_EXPO_ZERO;
+            for (int u = 1; u <= W; u++) {
+                int dl = 0;
+                if (u > L && u <= U) {
+                    const EmitEntry en = row[u - 1];
+                    if (en.mant != 0.0f) run = max(run, en.expo);
+                    if (run != WP_EXPO_ZERO) dl = km - run;
+                }
+                gd[c * W + u - 1] = (uint8_t)(dl <= 100 ? dl : 0);
+            }
         }
-        if (km != WP_EXPO_ZERO) K += km;
-        // boxes [L_t, u): the window's exponent minus the box's largest (0
-        // while the box has no nonzero factor; its pairs get P = 0)
-        const int L = Ls[c], U = Up[c];
-        int run = WP_EXPO_ZERO;
-        for (int u = 1; u <= W; u++) {
-            int dl = 0;
-            if (u > L && u <= U) {
-                const EmitEntry en = row[u - 1];
-                if (en.mant != 0.0f) run = max(run, en.expo);
-                if (run != WP_EXPO_ZERO) dl = km - run;
+        a.gK[rt] = ok ? K : WP_GK_NONE;
+        if (a.gone) {
+            // one-state read box in every channel: the state's own factors
+            float mv[3] = {0.0f, 0.0f, 0.0f};
+            int K1 = 0;
+            bool one = C <= 3;
+            for (int c = 0; c < C && one; c++) {
+                const int L = Ls[c];
+                if (Up[c] != L + 1 || L >= W) {
+                    one = false;
+                    break;
+                }
+                const EmitEntry en = tab[c * W + L];
+                mv[c] = en.mant;
+                if (en.mant != 0.0f) K1 += en.expo;
             }
-            gd[c * W + u - 1] = (uint8_t)(dl <= 100 ? dl : 0);
+            a.gone[rt] = make_float4(mv[0], mv[1], mv[2], __int_as_float(one ? K1 : WP_GK_NONE));
         }
     }
-    a.gK[rt] = ok ? K : WP_GK_NONE;
-    if (a.gone) {
-        // one-state read box in every channel: the state's own factors
-        float mv[3] = {0.0f, 0.0f, 0.0f};
-        int K1 = 0;
-        bool one = C <= 3;
-        for (int c = 0; c < C && one; c++) {
-            const int L = Ls[c];
-            if (Up[c] != L + 1 || L >= W) {
-                one = false;
-                break;
-            }
-            const EmitEntry en = tab[c * W + L];
-            mv[c] = en.mant;
-            if (en.mant != 0.0f) K1 += en.expo;
-        }
-        a.gone[rt] = make_float4(mv[0], mv[1], mv[2], __int_as_float(one ? K1 : WP_GK_NONE));
+    __syncthreads();
+    float* dst_gt = a.gtab + item0 * CW;
+    uint8_t* dst_gd = a.gdelta + item0 * CW;
+    for (int k = threadIdx.x; k < n_ent; k += blockDim.x) {
+        dst_gt[k] = s_gt[k];
+        dst_gd[k] = s_gd[k];
     }
 }
 
