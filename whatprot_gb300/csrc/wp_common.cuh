@@ -145,10 +145,12 @@ struct PeptideRec {
     uint64_t dye_pk;
     uint64_t tot_pk;
     // The same positions as one Edman code byte each (ecode[0]: positions
-    // 0..7, ecode[1]: 8..15): (tot << 3) | channel for a dye, 4 for none.
+    // 0..7, ecode[1]: 8..15): (tot << 4) | channel for a dye, 4 for none.
     // The engine's Edman step reads the coefficient row tot and, through a
-    // byte permute with selector 0x4440 | (code & 7), the dye count of the
-    // cut channel (selector 0x4444: the constant zero byte).
+    // byte permute with the code byte itself as the selector, the dye count
+    // of the cut channel in the result's byte 0 (selector nibble 0 is the
+    // channel, its sign-extension bit clear; for none it is 4, the constant
+    // zero byte; the result's other bytes are not used).
     uint64_t ecode[2];
 };
 
@@ -159,7 +161,7 @@ __host__ __device__ inline void wp_pack_peptide(PeptideRec& r) {
     for (int e = 0; e < 16 && e < WP_MAX_TIMESTEPS; e++) {
         d |= (uint64_t)((r.dye[e] + 1) & 15) << (4 * e);
         t |= (uint64_t)(r.tot[e] & 15) << (4 * e);
-        const uint64_t code = r.dye[e] >= 0 ? (uint64_t)(((r.tot[e] & 15) << 3) | (r.dye[e] & 3)) : 4u;
+        const uint64_t code = r.dye[e] >= 0 ? (uint64_t)(((r.tot[e] & 15) << 4) | (r.dye[e] & 3)) : 4u;
         ec[e >> 3] |= code << (8 * (e & 7));
     }
     r.dye_pk = d;

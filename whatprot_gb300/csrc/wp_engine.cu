@@ -84,6 +84,14 @@ struct PBox {
     uint32_t w;
 };
 __device__ __forceinline__ int bget(uint32_t v, int c) { return (int)((v >> (8 * c)) & 0xffu); }
+// prmt.b32 in its default mode: byte n of the result is the byte of {y, x}
+// (x: bytes 0-3, y: 4-7) that nibble n of s selects, its sign replicated
+// where the nibble's bit 3 is set.
+__device__ __forceinline__ uint32_t prmt(uint32_t x, uint32_t y, uint32_t s) {
+    uint32_t d;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(x), "r"(y), "r"(s));
+    return d;
+}
 __device__ __forceinline__ uint32_t bset(uint32_t v, int c, int x) {
     return (v & ~(0xffu << (8 * c))) | ((uint32_t)x << (8 * c));
 }
@@ -599,9 +607,9 @@ __device__ __noinline__ float emission_narrow(V* cur, int stride, int t, PBox nx
 // bleached box (t >= 1 slices), nxt receives the emission box (t + 1
 // slices).  codes: the pair's Edman code per position (PeptideRec::ecode),
 // one byte per position at codes[k * stride]; a byte permute of the state's
-// packed dye counts by the code's selector gives the cut channel's count
-// (and whether the state one dye up exists), so a slice costs no shifts of
-// the packed dye sequence.  The bleached box's per-slice volume must be at
+// packed dye counts with the code byte as the selector gives the cut
+// channel's count (and whether the state one dye up exists), so a slice
+// costs no shifts of the packed dye sequence.  The bleached box's per-slice volume must be at
 // most 255.  Returns the sum of the new states; *kmax_out the normalising
 // exponent (WP_EXPO_ZERO: every factor of some channel is zero), *em0_out
 // the all-zero state's factor.
@@ -665,9 +673,10 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
         // cut dye (y)
         auto success = [&](const uint8_t* cp, const V prev, const V* sp) -> float {
             const uint32_t code = *cp;
-            const uint32_t sel = 0x4440u | (code & 7u);
-            const uint32_t b = __byte_perm(X, 0u, sel);
-            const int ci = (int)(b & 0x7fu) * 17 + (int)(code >> 3);  // (count, tot)
+            // byte 0: the cut channel's count and its one-up bit (the code
+            // byte is the selector; the other bytes are not used)
+            const uint32_t b = prmt(X, 0u, code);
+            const int ci = (int)(b & 0x7fu) * 17 + (int)(code >> 4);  // (count, tot)
             float xin;
             if constexpr (HB) {
                 xin = prev.x;
@@ -676,7 +685,7 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
             }
             float add = edx[ci] * xin;
             if (b & 0x80u) {
-                const V xr = sp[(int)__byte_perm(stpk, 0u, sel) * stride];
+                const V xr = sp[(int)(prmt(stpk, 0u, code) & 0xffu) * stride];
                 if constexpr (HB) {
                     add = fmaf(edy[ci], xr.x, add);
                 } else {
