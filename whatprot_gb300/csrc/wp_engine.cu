@@ -652,20 +652,23 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
     float part = 0.0f;
     // The box's states in row-major order, as an odometer over the
     // channels: the state's index in the bleached box (ib), its packed
-    // counts with the one-dye-up bits (X), and the prefix products of its
-    // emission factors (pre[c] = sf g[0][k_0] ... g[c][k_c], the order of
-    // w0's product) are updated as the odometer turns.
+    // counts with the one-dye-up bits (X), and each channel's emission
+    // factor (gc[c] = g[c][k_c]) are updated as the odometer turns; the
+    // state's weight is sf g[0][k_0] ... g[C-1][k_{C-1}], multiplied in
+    // that order.
     int jc[C];
-    float pre[C];
+    float gc[C];
 #pragma unroll
     for (int c = 0; c < C; c++) {
         jc[c] = 0;
-        pre[c] = (c == 0 ? sf : pre[c > 0 ? c - 1 : 0]) * g[c][0];
+        gc[c] = g[c][0];
     }
     int ib = 0;
     uint32_t X = nx.lo | up0;
     for (int j = 0; j < vn; j++) {
-        const float w = pre[C - 1];
+        float w = sf;
+#pragma unroll
+        for (int c = 0; c < C; c++) w *= gc[c];
         const V* cs = cur + ib * stride;  // slice e - 1 of the state's column
         V* out = nxt + j * stride;
         // Edman success into slice e from slice e - 1 (value prev, column
@@ -774,6 +777,7 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
                         ib += st_c;
                         X += 1u << (8 * c);
                         if (k + 1 >= bget(bx.w, c)) X &= ~(0x80u << (8 * c));
+                        gc[c] = k == 1 ? g[c][1] : k == 2 ? g[c][2] : g[c][3];
                         carry = false;
                     } else {
                         // channel c back to its first count (its one-up bit
@@ -781,14 +785,9 @@ __device__ __forceinline__ float edman_emit(const typename StateOf<HB>::V* __res
                         ib -= jc[c] * st_c;
                         X = (X - ((uint32_t)jc[c] << (8 * c))) | (up0 & (0x80u << (8 * c)));
                         jc[c] = 0;
+                        gc[c] = g[c][0];
                     }
                 }
-            }
-#pragma unroll
-            for (int c = 0; c < C; c++) {
-                const int k = jc[c];
-                pre[c] = (c == 0 ? sf : pre[c > 0 ? c - 1 : 0]) *
-                         (k == 0 ? g[c][0] : k == 1 ? g[c][1] : k == 2 ? g[c][2] : g[c][3]);
             }
         }
     }
